@@ -1,0 +1,980 @@
+/* CPU restatement of OpenZL's universal decoder for the numeric codec graph
+ * (formats 21-23). Test infrastructure only: the checker the GPU decoder is
+ * compared against. Each function cites the reference code it restates. */
+#include <stdio.h>
+
+#include "ozo_internal.h"
+
+typedef struct {
+    int type;          /* OZO_TYPE_* */
+    size_t w;          /* element width in bytes */
+    size_t n;          /* number of elements */
+    const uint8_t* p;  /* content */
+    uint8_t* own;      /* owned allocation, if any */
+    int filled;
+} OStream;
+
+static void ost_free(OStream* s)
+{
+    free(s->own);
+    memset(s, 0, sizeof(*s));
+}
+static uint8_t* ost_alloc(OStream* s, int type, size_t w, size_t n)
+{
+    s->type = type;
+    s->w = w;
+    s->n = n;
+    s->own = (uint8_t*)malloc(n * w + 16);
+    s->p = s->own;
+    s->filled = 1;
+    return s->own;
+}
+static void ost_ref(OStream* s, int type, size_t w, size_t n, const uint8_t* p)
+{
+    s->type = type;
+    s->w = w;
+    s->n = n;
+    s->p = p;
+    s->own = NULL;
+    s->filled = 1;
+}
+
+/* ---------------------------------------------------------------------
+ * LSB-first bitpack decode (src/openzl/codecs/bitpack/spec.md,
+ * common_bitpack_kernel.c). Element i occupies bits [i*nbBits, (i+1)*nbBits)
+ * of the little-endian byte stream. Returns bytes consumed.
+ * ------------------------------------------------------------------- */
+static size_t bitunpack(uint64_t* dst, size_t n, const uint8_t* src, size_t srcSize, int nbBits)
+{
+    size_t const need = (n * (size_t)nbBits + 7) / 8;
+    if (need > srcSize) return (size_t)-1;
+    for (size_t i = 0; i < n; i++) {
+        size_t bit = i * (size_t)nbBits;
+        uint64_t v = 0;
+        for (int b = 0; b < nbBits; b++) {
+            size_t q = bit + (size_t)b;
+            v |= (uint64_t)((src[q >> 3] >> (q & 7)) & 1) << b;
+        }
+        dst[i] = v;
+    }
+    return need;
+}
+
+/* ---------------------------------------------------------------------
+ * Backward bit reader shared by FSE and Huffman (src/openzl/fse/bitstream.h):
+ * the stream is read from its last byte towards its first; the highest set
+ * bit of the last byte is an end marker; fields are read most significant
+ * bit first. Bits below position 0 read as zero.
+ * ------------------------------------------------------------------- */
+typedef struct {
+    const uint8_t* src;
+    int64_t pos; /* number of unread bits */
+} BRd;
+
+static int brd_init(BRd* r, const uint8_t* src, size_t size)
+{
+    if (size == 0) return -1;
+    uint8_t last = src[size - 1];
+    if (last == 0) return -1;
+    r->src = src;
+    r->pos = (int64_t)(size - 1) * 8 + ozo_highbit32(last);
+    return 0;
+}
+static uint32_t brd_peek(const BRd* r, int nb)
+{
+    uint32_t v = 0;
+    for (int i = 0; i < nb; i++) {
+        int64_t q = r->pos - 1 - i;
+        uint32_t bit = q >= 0 ? ((r->src[q >> 3] >> (q & 7)) & 1) : 0;
+        v = (v << 1) | bit;
+    }
+    return v;
+}
+static uint32_t brd_read(BRd* r, int nb)
+{
+    uint32_t v = brd_peek(r, nb);
+    r->pos -= nb;
+    return v;
+}
+
+/* ---------------------------------------------------------------------
+ * FSE normalized-count header (src/openzl/fse/common/entropy_common.c:42-185,
+ * FSE_readNCount): 4 bits tableLog-5, then per symbol a variable-width count
+ * with a 2-bit repeat code for runs of zero counts. Returns bytes read.
+ * ------------------------------------------------------------------- */
+static int64_t fse_read_ncount(int16_t* norm, unsigned* maxSV, unsigned* tableLog,
+                               const uint8_t* src, size_t size)
+{
+    size_t bitpos = 0;
+    size_t const total = size * 8;
+#define GETBITS(nb) ({ uint32_t _v = 0; for (int _i = 0; _i < (nb); _i++) { size_t _q = bitpos + _i; \
+        _v |= (uint32_t)(_q < total ? ((src[_q >> 3] >> (_q & 7)) & 1) : 0) << _i; } _v; })
+    unsigned const maxSV1 = *maxSV + 1;
+    memset(norm, 0, maxSV1 * sizeof(int16_t));
+    if (size < 1) return -OZO_ERR_CORRUPTION;
+    int nbBits = (int)GETBITS(4) + 5;
+    bitpos += 4;
+    if (nbBits > 15) return -OZO_ERR_CORRUPTION;
+    *tableLog = (unsigned)nbBits;
+    int remaining = (1 << nbBits) + 1;
+    int threshold = 1 << nbBits;
+    nbBits++;
+    unsigned charnum = 0;
+    int previous0 = 0;
+    while (remaining > 1 && charnum < maxSV1) {
+        if (previous0) {
+            unsigned n0 = charnum;
+            while (GETBITS(2) == 3) { n0 += 3; bitpos += 2; }
+            n0 += GETBITS(2);
+            bitpos += 2;
+            if (n0 > maxSV1) return -OZO_ERR_CORRUPTION;
+            charnum = n0;
+            if (charnum >= maxSV1) break;
+        }
+        int const max = (2 * threshold - 1) - remaining;
+        int count;
+        uint32_t const low = GETBITS(nbBits - 1);
+        if ((int)low < max) {
+            count = (int)low;
+            bitpos += (size_t)(nbBits - 1);
+        } else {
+            count = (int)GETBITS(nbBits);
+            if (count >= threshold) count -= max;
+            bitpos += (size_t)nbBits;
+        }
+        count--;
+        remaining -= count < 0 ? -count : count;
+        norm[charnum++] = (int16_t)count;
+        previous0 = !count;
+        while (remaining < threshold) {
+            nbBits--;
+            threshold >>= 1;
+        }
+    }
+#undef GETBITS
+    if (remaining != 1) return -OZO_ERR_CORRUPTION;
+    if (charnum > maxSV1) return -OZO_ERR_CORRUPTION;
+    if (bitpos > total) return -OZO_ERR_CORRUPTION;
+    *maxSV = charnum - 1;
+    return (int64_t)((bitpos + 7) >> 3);
+}
+
+/* FSE decoding table (src/openzl/fse/decompress/fse_decompress.c:73-171). */
+typedef struct {
+    uint16_t newState;
+    uint8_t symbol;
+    uint8_t nbBits;
+} FseD;
+
+static int fse_build_dtable(FseD* dt, const int16_t* norm, unsigned maxSV, unsigned tableLog)
+{
+    uint32_t const tableSize = 1u << tableLog;
+    uint32_t const mask = tableSize - 1;
+    uint32_t const step = (tableSize >> 1) + (tableSize >> 3) + 3;
+    uint32_t high = tableSize - 1;
+    uint16_t next[256];
+    for (unsigned s = 0; s <= maxSV; s++) {
+        if (norm[s] == -1) {
+            dt[high--].symbol = (uint8_t)s;
+            next[s] = 1;
+        } else {
+            next[s] = (uint16_t)norm[s];
+        }
+    }
+    uint32_t pos = 0;
+    for (unsigned s = 0; s <= maxSV; s++) {
+        for (int i = 0; i < norm[s]; i++) {
+            dt[pos].symbol = (uint8_t)s;
+            do { pos = (pos + step) & mask; } while (pos > high);
+        }
+    }
+    if (pos != 0) return -1;
+    for (uint32_t u = 0; u < tableSize; u++) {
+        uint8_t const s = dt[u].symbol;
+        uint32_t const x = next[s]++;
+        dt[u].nbBits = (uint8_t)(tableLog - (unsigned)ozo_highbit32(x));
+        dt[u].newState = (uint16_t)((x << dt[u].nbBits) - tableSize);
+    }
+    return 0;
+}
+
+/* Interleaved-state FSE decode (src/openzl/fse/decompress/fse_decompress.c:
+ * 255-337): nbStates states read their initial values in order, symbol i is
+ * produced by state i % nbStates, and every symbol except the last one of
+ * each state is followed by that state's transition. */
+static int fse_decode(uint8_t* dst, size_t dstSize, const uint8_t* src, size_t srcSize,
+                      const FseD* dt, unsigned tableLog, unsigned nbStates)
+{
+    BRd r;
+    if (brd_init(&r, src, srcSize)) return -OZO_ERR_CORRUPTION;
+    uint32_t st[4];
+    for (unsigned k = 0; k < nbStates; k++) st[k] = brd_read(&r, (int)tableLog);
+    if (dstSize < nbStates) return -OZO_ERR_CORRUPTION;
+    size_t const lastTransition = dstSize - nbStates;
+    for (size_t i = 0; i < dstSize; i++) {
+        unsigned const k = (unsigned)(i % nbStates);
+        FseD const e = dt[st[k]];
+        dst[i] = e.symbol;
+        if (i < lastTransition) st[k] = e.newState + brd_read(&r, e.nbBits);
+    }
+    if (r.pos != 0) return -OZO_ERR_CORRUPTION;
+    return 0;
+}
+
+/* ---------------------------------------------------------------------
+ * Huffman: weights -> canonical decoding table
+ * (src/openzl/codecs/entropy/decode_entropy_binding.c:205-284,
+ * src/openzl/fse/decompress/huf_decompress.c:342-454). Symbols are ranked by
+ * weight then by value; a symbol of weight w spans 2^(w-1) cells and codes
+ * on tableLog+1-w bits.
+ * ------------------------------------------------------------------- */
+typedef struct {
+    uint8_t symbol;
+    uint8_t nbBits;
+} HufD;
+
+static int huf_build_dtable(HufD* dt, unsigned* tableLogOut, const uint8_t* weights, size_t nbWeights)
+{
+    if (nbWeights < 2 || nbWeights > 256) return -1;
+    uint32_t sum = 0;
+    unsigned counts[16] = { 0 };
+    for (size_t i = 0; i < nbWeights; i++) {
+        if (weights[i] > 12) return -1;
+        sum += (1u << weights[i]) >> 1;
+        counts[weights[i]]++;
+    }
+    if (sum == 0 || (sum & (sum - 1))) return -1;
+    unsigned const tableLog = (unsigned)ozo_highbit32(sum);
+    if (tableLog > 12) return -1;
+    if (nbWeights - counts[0] < 2) return -1;
+    uint32_t pos = 0;
+    for (unsigned w = 1; w <= tableLog; w++) {
+        for (size_t s = 0; s < nbWeights; s++) {
+            if (weights[s] != w) continue;
+            uint32_t const len = (1u << w) >> 1;
+            for (uint32_t u = 0; u < len; u++) {
+                dt[pos + u].symbol = (uint8_t)s;
+                dt[pos + u].nbBits = (uint8_t)(tableLog + 1 - w);
+            }
+            pos += len;
+        }
+    }
+    *tableLogOut = tableLog;
+    return 0;
+}
+
+static int huf_decode_stream(uint8_t* dst, size_t n, const uint8_t* src, size_t size,
+                             const HufD* dt, unsigned tableLog)
+{
+    BRd r;
+    if (brd_init(&r, src, size)) return -OZO_ERR_CORRUPTION;
+    for (size_t i = 0; i < n; i++) {
+        HufD const e = dt[brd_peek(&r, (int)tableLog)];
+        dst[i] = e.symbol;
+        r.pos -= e.nbBits;
+    }
+    if (r.pos != 0) return -OZO_ERR_CORRUPTION;
+    return 0;
+}
+
+/* 4-stream layout: 6-byte jump table of three LE16 stream sizes, output split
+ * into segments of (dstSize+3)/4 (src/openzl/fse/decompress/huf_decompress.c:
+ * 562-660). */
+static int huf_decode_4x(uint8_t* dst, size_t n, const uint8_t* src, size_t size,
+                         const HufD* dt, unsigned tableLog)
+{
+    if (size < 10) return -OZO_ERR_CORRUPTION;
+    size_t const l1 = ozo_rd16(src), l2 = ozo_rd16(src + 2), l3 = ozo_rd16(src + 4);
+    if (l1 + l2 + l3 + 6 > size) return -OZO_ERR_CORRUPTION;
+    size_t const l4 = size - 6 - l1 - l2 - l3;
+    size_t const seg = (n + 3) / 4;
+    if (3 * seg > n) return -OZO_ERR_CORRUPTION;
+    const uint8_t* s = src + 6;
+    int rc;
+    if ((rc = huf_decode_stream(dst, seg, s, l1, dt, tableLog))) return rc;
+    if ((rc = huf_decode_stream(dst + seg, seg, s + l1, l2, dt, tableLog))) return rc;
+    if ((rc = huf_decode_stream(dst + 2 * seg, seg, s + l1 + l2, l3, dt, tableLog))) return rc;
+    return huf_decode_stream(dst + 3 * seg, n - 3 * seg, s + l1 + l2 + l3, l4, dt, tableLog);
+}
+
+/* ---------------------------------------------------------------------
+ * Decoder signatures (src/openzl/codecs/decoder_registry.c:88-161 and the
+ * graph macros it names): number of singleton inputs with their types,
+ * whether variable inputs are accepted, and the regenerated type.
+ * ------------------------------------------------------------------- */
+typedef struct {
+    int known;
+    int nbSO;
+    int soTypes[2];
+    int voType;   /* 0 when the decoder takes no variable inputs */
+    int outType;  /* type of the regenerated stream */
+} DecSig;
+
+static DecSig sig_of(unsigned id)
+{
+    DecSig d = { 0 };
+    d.known = 1;
+    switch (id) {
+        case TR_DELTA_INT:
+        case TR_ZIGZAG:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_NUMERIC; d.outType = OZO_TYPE_NUMERIC; break;
+        case TR_TRANSPOSE_SPLIT:
+            d.nbSO = 0; d.voType = OZO_TYPE_SERIAL; d.outType = OZO_TYPE_STRUCT; break;
+        case TR_CONV_SERIAL_TO_STRUCT:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_STRUCT; d.outType = OZO_TYPE_SERIAL; break;
+        case TR_CONV_STRUCT_TO_SERIAL:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_SERIAL; d.outType = OZO_TYPE_STRUCT; break;
+        case TR_CONV_STRUCT_TO_NUM_LE:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_NUMERIC; d.outType = OZO_TYPE_STRUCT; break;
+        case TR_CONV_NUM_TO_STRUCT_LE:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_STRUCT; d.outType = OZO_TYPE_NUMERIC; break;
+        case TR_CONV_SERIAL_TO_NUM_LE:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_NUMERIC; d.outType = OZO_TYPE_SERIAL; break;
+        case TR_CONV_NUM_TO_SERIAL_LE:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_SERIAL; d.outType = OZO_TYPE_NUMERIC; break;
+        case TR_BITPACK_SERIAL:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_SERIAL; d.outType = OZO_TYPE_SERIAL; break;
+        case TR_BITPACK_INT:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_SERIAL; d.outType = OZO_TYPE_NUMERIC; break;
+        case TR_FLATPACK:
+            d.nbSO = 2; d.soTypes[0] = OZO_TYPE_SERIAL; d.soTypes[1] = OZO_TYPE_SERIAL;
+            d.outType = OZO_TYPE_SERIAL; break;
+        case TR_FLOAT_DECONSTRUCT:
+            d.nbSO = 2; d.soTypes[0] = OZO_TYPE_STRUCT; d.soTypes[1] = OZO_TYPE_SERIAL;
+            d.outType = OZO_TYPE_NUMERIC; break;
+        case TR_TOKENIZE_FIXED:
+            d.nbSO = 2; d.soTypes[0] = OZO_TYPE_STRUCT; d.soTypes[1] = OZO_TYPE_NUMERIC;
+            d.outType = OZO_TYPE_STRUCT; break;
+        case TR_TOKENIZE_NUMERIC:
+            d.nbSO = 2; d.soTypes[0] = OZO_TYPE_NUMERIC; d.soTypes[1] = OZO_TYPE_NUMERIC;
+            d.outType = OZO_TYPE_NUMERIC; break;
+        case TR_SPLITN:
+            d.nbSO = 0; d.voType = OZO_TYPE_SERIAL; d.outType = OZO_TYPE_SERIAL; break;
+        case TR_SPLITN_STRUCT:
+            d.nbSO = 0; d.voType = OZO_TYPE_STRUCT; d.outType = OZO_TYPE_STRUCT; break;
+        case TR_SPLITN_NUM:
+            d.nbSO = 0; d.voType = OZO_TYPE_NUMERIC; d.outType = OZO_TYPE_NUMERIC; break;
+        case TR_CONSTANT_SERIAL:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_SERIAL; d.outType = OZO_TYPE_SERIAL; break;
+        case TR_CONSTANT_FIXED:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_STRUCT; d.outType = OZO_TYPE_STRUCT; break;
+        case TR_FSE_V2:
+        case TR_HUFFMAN_V2:
+            d.nbSO = 2; d.soTypes[0] = OZO_TYPE_NUMERIC; d.soTypes[1] = OZO_TYPE_SERIAL;
+            d.outType = OZO_TYPE_SERIAL; break;
+        case TR_FSE_NCOUNT:
+            d.nbSO = 1; d.soTypes[0] = OZO_TYPE_SERIAL; d.outType = OZO_TYPE_NUMERIC; break;
+        default:
+            d.known = 0;
+    }
+    return d;
+}
+
+/* ---------------------------------------------------------------------
+ * Decoders. `in` holds the decoder's inputs in the decoder's own order
+ * (src/openzl/decompress/decompress2.c:1132-1138 reverses stream slots).
+ * ------------------------------------------------------------------- */
+static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, size_t hsz,
+                   OStream* out)
+{
+    DecSig const sg = sig_of(id);
+    switch (id) {
+        case TR_DELTA_INT: { /* decode_delta_binding.c:11-58 */
+            size_t const w = in[0]->w, nd = in[0]->n;
+            size_t n = 0;
+            if (hsz) {
+                if (hsz != w) return -OZO_ERR_CORRUPTION;
+                n = nd + 1;
+            } else if (nd) {
+                return -OZO_ERR_CORRUPTION;
+            }
+            uint8_t* o = ost_alloc(out, OZO_TYPE_NUMERIC, w, n);
+            if (n) {
+                uint64_t const m = w == 8 ? ~0ull : ((1ull << (8 * w)) - 1);
+                uint64_t v = ozo_rdN(hdr, w);
+                for (size_t i = 0; i < n; i++) {
+                    if (i) v = (v + ozo_rdN(in[0]->p + (i - 1) * w, w)) & m;
+                    for (size_t b = 0; b < w; b++) o[i * w + b] = (uint8_t)(v >> (8 * b));
+                }
+            }
+            return 0;
+        }
+        case TR_ZIGZAG: { /* decode_zigzag_kernel.c */
+            size_t const w = in[0]->w, n = in[0]->n;
+            uint8_t* o = ost_alloc(out, OZO_TYPE_NUMERIC, w, n);
+            uint64_t const m = w == 8 ? ~0ull : ((1ull << (8 * w)) - 1);
+            for (size_t i = 0; i < n; i++) {
+                uint64_t z = ozo_rdN(in[0]->p + i * w, w);
+                uint64_t v = ((z >> 1) ^ (0 - (z & 1))) & m;
+                for (size_t b = 0; b < w; b++) o[i * w + b] = (uint8_t)(v >> (8 * b));
+            }
+            return 0;
+        }
+        case TR_TRANSPOSE_SPLIT: { /* decode_transpose_binding.c:37-75 */
+            if (nbIn == 0) return -OZO_ERR_CORRUPTION;
+            size_t const n = in[0]->n, W = nbIn;
+            for (size_t i = 0; i < nbIn; i++)
+                if (in[i]->type != OZO_TYPE_SERIAL || in[i]->n != n) return -OZO_ERR_CORRUPTION;
+            uint8_t* o = ost_alloc(out, OZO_TYPE_STRUCT, W, n);
+            for (size_t e = 0; e < n; e++)
+                for (size_t b = 0; b < W; b++) o[e * W + b] = in[b]->p[e];
+            return 0;
+        }
+        case TR_CONV_NUM_TO_STRUCT_LE: { /* decode_conversion_binding.c:190-225 */
+            size_t const w = in[0]->w;
+            if (!(w == 1 || w == 2 || w == 4 || w == 8)) return -OZO_ERR_CORRUPTION;
+            ost_ref(out, OZO_TYPE_NUMERIC, w, in[0]->n, in[0]->p);
+            return 0;
+        }
+        case TR_CONV_STRUCT_TO_NUM_LE: /* decode_conversion_binding.c:178-188 */
+            ost_ref(out, OZO_TYPE_STRUCT, in[0]->w, in[0]->n, in[0]->p);
+            return 0;
+        case TR_CONV_SERIAL_TO_NUM_LE: /* decode_conversion_binding.c:60-64 */
+            ost_ref(out, OZO_TYPE_SERIAL, 1, in[0]->n * in[0]->w, in[0]->p);
+            return 0;
+        case TR_CONV_SERIAL_TO_STRUCT: /* decode_conversion_binding.c:112-122 */
+            ost_ref(out, OZO_TYPE_SERIAL, 1, in[0]->n * in[0]->w, in[0]->p);
+            return 0;
+        case TR_CONV_NUM_TO_SERIAL_LE: { /* decode_conversion_binding.c:72-110 */
+            if (hsz != 1) return -OZO_ERR_CORRUPTION;
+            size_t const w = (size_t)1 << hdr[0];
+            if (!(w == 1 || w == 2 || w == 4 || w == 8)) return -OZO_ERR_CORRUPTION;
+            size_t const bytes = in[0]->n * in[0]->w;
+            if (bytes % w) return -OZO_ERR_CORRUPTION;
+            uint8_t* o = ost_alloc(out, OZO_TYPE_NUMERIC, w, bytes / w);
+            memcpy(o, in[0]->p, bytes);
+            return 0;
+        }
+        case TR_CONV_STRUCT_TO_SERIAL: { /* decode_conversion_binding.c:125-160 */
+            const uint8_t* p = hdr;
+            uint64_t ew;
+            if (ozo_varint_dec(&p, hdr + hsz, &ew) || p != hdr + hsz || ew == 0) return -OZO_ERR_CORRUPTION;
+            size_t const bytes = in[0]->n * in[0]->w;
+            if (bytes % ew) return -OZO_ERR_CORRUPTION;
+            ost_ref(out, OZO_TYPE_STRUCT, (size_t)ew, bytes / ew, in[0]->p);
+            return 0;
+        }
+        case TR_BITPACK_SERIAL:
+        case TR_BITPACK_INT: { /* decode_bitpack_binding.c:9-60 */
+            if (hsz < 1 || hsz > 2) return -OZO_ERR_CORRUPTION;
+            size_t const w = (size_t)1 << ((hdr[0] >> 6) & 3);
+            int const nbBits = 1 + (hdr[0] & 0x3f);
+            if ((size_t)nbBits > 8 * w) return -OZO_ERR_CORRUPTION;
+            if (id == TR_BITPACK_SERIAL && w != 1) return -OZO_ERR_CORRUPTION;
+            size_t const srcSize = in[0]->n;
+            size_t const maxN = srcSize * 8 / (size_t)nbBits;
+            size_t n = maxN;
+            if (hsz > 1) {
+                if (hdr[1] > maxN) return -OZO_ERR_CORRUPTION;
+                n = maxN - hdr[1];
+            }
+            if ((n * (size_t)nbBits + 7) / 8 != srcSize) return -OZO_ERR_CORRUPTION;
+            uint8_t* o = ost_alloc(out, sg.outType, w, n);
+            uint64_t* tmp = (uint64_t*)malloc((n + 1) * 8);
+            bitunpack(tmp, n, in[0]->p, srcSize, nbBits);
+            for (size_t i = 0; i < n; i++)
+                for (size_t b = 0; b < w; b++) o[i * w + b] = (uint8_t)(tmp[i] >> (8 * b));
+            free(tmp);
+            return 0;
+        }
+        case TR_FLATPACK: { /* decode_flatpack_binding.c, decode_flatpack_kernel.c:19-60 */
+            const OStream* alpha = in[0];
+            const OStream* packed = in[1];
+            size_t const asz = alpha->n;
+            if (asz > 256) return -OZO_ERR_CORRUPTION;
+            size_t const psz = packed->n;
+            size_t n = 0;
+            unsigned nbBits = asz <= 1 ? (unsigned)asz : 1u + (unsigned)ozo_highbit32((uint32_t)asz - 1);
+            if (psz && asz) {
+                uint32_t last = packed->p[psz - 1] | 1;
+                size_t pad = (size_t)__builtin_clz(last << 24) + 1;
+                n = (8 * psz - pad) / nbBits;
+            }
+            uint8_t* o = ost_alloc(out, OZO_TYPE_SERIAL, 1, n);
+            size_t bit = 0;
+            for (size_t i = 0; i < n; i++) {
+                unsigned idx = 0;
+                for (unsigned b = 0; b < nbBits; b++, bit++)
+                    idx |= (unsigned)((packed->p[bit >> 3] >> (bit & 7)) & 1) << b;
+                if (idx >= asz) return -OZO_ERR_CORRUPTION;
+                o[i] = alpha->p[idx];
+            }
+            if (psz && asz) {
+                /* terminator bit then zero padding */
+                if (!((packed->p[bit >> 3] >> (bit & 7)) & 1)) return -OZO_ERR_CORRUPTION;
+                if ((bit >> 3) != psz - 1) return -OZO_ERR_CORRUPTION;
+            }
+            return 0;
+        }
+        case TR_FLOAT_DECONSTRUCT: { /* decode_float_deconstruct_binding.c:13-70 */
+            const OStream* sf = in[0];
+            const OStream* ex = in[1];
+            if (hsz != 1 || hdr[0] > 2) return -OZO_ERR_CORRUPTION;
+            size_t const n = ex->n;
+            if (sf->n != n) return -OZO_ERR_CORRUPTION;
+            unsigned const t = hdr[0];
+            size_t const sfw = t == 0 ? 3 : (t == 1 ? 1 : 2);
+            if (sf->w != sfw || ex->w != 1) return -OZO_ERR_CORRUPTION;
+            size_t const ow = t == 0 ? 4 : 2;
+            uint8_t* o = ost_alloc(out, OZO_TYPE_NUMERIC, ow, n);
+            for (size_t i = 0; i < n; i++) {
+                if (t == 1) {
+                    uint8_t s = sf->p[i];
+                    uint16_t v = (uint16_t)((s >> 1) | ((uint16_t)s << 15) | ((uint16_t)ex->p[i] << 7));
+                    ozo_wr16(o + 2 * i, v);
+                } else if (t == 2) {
+                    uint16_t s = ozo_rd16(sf->p + 2 * i);
+                    uint16_t v = (uint16_t)((s >> 1) | (uint16_t)(s << 15) | ((uint16_t)ex->p[i] << 10));
+                    ozo_wr16(o + 2 * i, v);
+                } else {
+                    uint32_t s = (uint32_t)ozo_rdN(sf->p + 3 * i, 3);
+                    uint32_t v = ((uint32_t)ex->p[i] << 23) | (s << 31) | (s >> 1);
+                    ozo_wr32(o + 4 * i, v);
+                }
+            }
+            return 0;
+        }
+        case TR_TOKENIZE_FIXED:
+        case TR_TOKENIZE_NUMERIC: { /* decode_tokenize_binding.c:9-38 */
+            const OStream* alpha = in[0];
+            const OStream* idx = in[1];
+            size_t const w = alpha->w, n = idx->n, iw = idx->w;
+            uint8_t* o = ost_alloc(out, sg.outType, w, n);
+            for (size_t i = 0; i < n; i++) {
+                uint64_t k = ozo_rdN(idx->p + i * iw, iw);
+                if (k >= alpha->n) return -OZO_ERR_CORRUPTION;
+                memcpy(o + i * w, alpha->p + k * w, w);
+            }
+            return 0;
+        }
+        case TR_SPLITN:
+        case TR_SPLITN_STRUCT:
+        case TR_SPLITN_NUM: { /* decode_splitN_binding.c:16-80 */
+            size_t w = 1;
+            int type = sg.outType;
+            if (nbIn == 0) {
+                if (hsz) {
+                    const uint8_t* p = hdr;
+                    uint64_t v;
+                    if (ozo_varint_dec(&p, hdr + hsz, &v)) return -OZO_ERR_CORRUPTION;
+                    w = (size_t)v;
+                }
+            } else {
+                w = in[0]->w;
+                type = in[0]->type;
+            }
+            size_t total = 0;
+            for (size_t i = 0; i < nbIn; i++) {
+                if (in[i]->type != type || in[i]->w != w) return -OZO_ERR_CORRUPTION;
+                total += in[i]->n;
+            }
+            uint8_t* o = ost_alloc(out, sg.outType, w, total);
+            size_t pos = 0;
+            for (size_t i = 0; i < nbIn; i++) {
+                memcpy(o + pos, in[i]->p, in[i]->n * w);
+                pos += in[i]->n * w;
+            }
+            return 0;
+        }
+        case TR_CONSTANT_SERIAL:
+        case TR_CONSTANT_FIXED: { /* decode_constant_binding.c:10-45 */
+            if (in[0]->n != 1) return -OZO_ERR_CORRUPTION;
+            const uint8_t* p = hdr;
+            uint64_t n;
+            if (ozo_varint_dec(&p, hdr + hsz, &n) || p != hdr + hsz || n < 1) return -OZO_ERR_CORRUPTION;
+            size_t const w = in[0]->w;
+            uint8_t* o = ost_alloc(out, sg.outType, w, (size_t)n);
+            for (size_t i = 0; i < n; i++) memcpy(o + i * w, in[0]->p, w);
+            return 0;
+        }
+        case TR_FSE_NCOUNT: { /* decode_entropy_binding.c:118-143 */
+            int16_t norm[256];
+            unsigned maxSV = 255, tl = 0;
+            int64_t r = fse_read_ncount(norm, &maxSV, &tl, in[0]->p, in[0]->n);
+            if (r < 0 || (size_t)r != in[0]->n) return -OZO_ERR_CORRUPTION;
+            uint8_t* o = ost_alloc(out, OZO_TYPE_NUMERIC, 2, maxSV + 1);
+            for (unsigned s = 0; s <= maxSV; s++) ozo_wr16(o + 2 * s, (uint16_t)norm[s]);
+            return 0;
+        }
+        case TR_FSE_V2: { /* decode_entropy_binding.c:24-116 */
+            const OStream* normS = in[0];
+            const OStream* bits = in[1];
+            if (normS->w != 2) return -OZO_ERR_CORRUPTION;
+            size_t const nbSym = normS->n;
+            if (nbSym < 2 || nbSym > 256) return -OZO_ERR_CORRUPTION;
+            int16_t norm[256];
+            unsigned sum = 0;
+            for (size_t i = 0; i < nbSym; i++) {
+                norm[i] = (int16_t)ozo_rd16(normS->p + 2 * i);
+                if (norm[i] < -1) return -OZO_ERR_CORRUPTION;
+                sum += norm[i] == -1 ? 1u : (unsigned)norm[i];
+            }
+            if (sum == 0 || (sum & (sum - 1))) return -OZO_ERR_CORRUPTION;
+            unsigned const tl = (unsigned)ozo_highbit32(sum);
+            if (tl < 5 || tl > 12) return -OZO_ERR_CORRUPTION;
+            if (hsz < 2 || hsz > 9) return -OZO_ERR_CORRUPTION;
+            unsigned const nbStates = hdr[0];
+            if (nbStates != 2 && nbStates != 4) return -OZO_ERR_CORRUPTION;
+            size_t const dstSize = (size_t)ozo_rdN(hdr + 1, hsz - 1);
+            if (dstSize < 2) return -OZO_ERR_CORRUPTION;
+            FseD* dt = (FseD*)malloc(sizeof(FseD) << tl);
+            if (fse_build_dtable(dt, norm, (unsigned)nbSym - 1, tl)) { free(dt); return -OZO_ERR_CORRUPTION; }
+            uint8_t* o = ost_alloc(out, OZO_TYPE_SERIAL, 1, dstSize);
+            int rc = fse_decode(o, dstSize, bits->p, bits->n, dt, tl, nbStates);
+            free(dt);
+            return rc;
+        }
+        case TR_HUFFMAN_V2: { /* decode_entropy_binding.c:286-347 */
+            const OStream* wS = in[0];
+            const OStream* bits = in[1];
+            if (wS->w != 1) return -OZO_ERR_CORRUPTION;
+            if (hsz < 2 || hsz > 9) return -OZO_ERR_CORRUPTION;
+            int const x4 = hdr[0] & 1;
+            size_t const dstSize = (size_t)ozo_rdN(hdr + 1, hsz - 1);
+            if (dstSize < 2) return -OZO_ERR_CORRUPTION;
+            HufD dt[4096];
+            unsigned tl;
+            if (huf_build_dtable(dt, &tl, wS->p, wS->n)) return -OZO_ERR_CORRUPTION;
+            uint8_t* o = ost_alloc(out, OZO_TYPE_SERIAL, 1, dstSize);
+            return x4 ? huf_decode_4x(o, dstSize, bits->p, bits->n, dt, tl)
+                      : huf_decode_stream(o, dstSize, bits->p, bits->n, dt, tl);
+        }
+        default:
+            return -OZO_ERR_UNSUPPORTED;
+    }
+}
+
+/* ---------------------------------------------------------------------
+ * Frame and block parsing, and the stream-slot executor
+ * (src/openzl/decompress/decode_frameheader.c:237-340, 938-1171;
+ * src/openzl/decompress/decompress2.c:632-834, 1046-1290, 1442-1570).
+ * ------------------------------------------------------------------- */
+typedef struct {
+    unsigned version;
+    int hasContentCk, hasCompressedCk;
+    size_t nbOutputs;
+    int types[16];
+    uint64_t sizes[16];
+    size_t headerSize;
+} FrameHdr;
+
+static int decode_type(unsigned t)
+{
+    static const int m[4] = { OZO_TYPE_SERIAL, OZO_TYPE_STRUCT, OZO_TYPE_NUMERIC, OZO_TYPE_STRING };
+    return m[t & 3];
+}
+
+static int64_t parse_frame_header(FrameHdr* fh, const uint8_t* src, size_t size)
+{
+    memset(fh, 0, sizeof(*fh));
+    if (size < 9) return -OZO_ERR_SRC_SIZE;
+    uint32_t const magic = ozo_rd32(src);
+    if (magic < OZO_MAGIC_BASE + 21 || magic > OZO_MAGIC_BASE + 23) return -OZO_ERR_VERSION;
+    fh->version = magic - OZO_MAGIC_BASE;
+    size_t pos = 4;
+    uint8_t const flags = src[pos++];
+    fh->hasContentCk = flags & 1;
+    fh->hasCompressedCk = (flags >> 1) & 1;
+    int const hasComment = (flags >> 2) & 1;
+    uint8_t const t1 = src[pos++];
+    size_t nbOut = t1 & 15;
+    if (nbOut == 15) return -OZO_ERR_UNSUPPORTED;
+    if (nbOut == 0 || nbOut > 14) return -OZO_ERR_UNSUPPORTED;
+    fh->nbOutputs = nbOut;
+    for (size_t n = 0; n < nbOut && n < 2; n++) fh->types[n] = decode_type(t1 >> (4 + 2 * n));
+    if (nbOut > 2) {
+        uint8_t tok = 0;
+        for (size_t n = 2; n < nbOut; n++) {
+            size_t const sh = ((n - 2) % 4) * 2;
+            if (sh == 0) {
+                if (pos >= size) return -OZO_ERR_SRC_SIZE;
+                tok = src[pos++];
+            }
+            fh->types[n] = decode_type(tok >> sh);
+        }
+    }
+    const uint8_t* p = src + pos;
+    if (*p == 0) return -OZO_ERR_UNSUPPORTED; /* unknown sizes */
+    for (size_t n = 0; n < nbOut; n++) {
+        uint64_t v;
+        if (ozo_varint_dec(&p, src + size, &v) || v == 0) return -OZO_ERR_CORRUPTION;
+        fh->sizes[n] = v - 1;
+    }
+    for (size_t n = 0; n < nbOut; n++)
+        if (fh->types[n] == OZO_TYPE_STRING) return -OZO_ERR_UNSUPPORTED;
+    pos = (size_t)(p - src);
+    if (fh->version >= 22 && hasComment) {
+        uint64_t csz;
+        if (ozo_varint_dec(&p, src + size, &csz) || csz == 0) return -OZO_ERR_CORRUPTION;
+        pos = (size_t)(p - src) + (size_t)csz;
+        if (pos > size) return -OZO_ERR_SRC_SIZE;
+    }
+    if (fh->hasCompressedCk) {
+        if (pos + 1 > size) return -OZO_ERR_SRC_SIZE;
+        if ((ozo_xxh3_64(src, pos) & 255) != src[pos]) return -OZO_ERR_CHECKSUM;
+        pos++;
+    }
+    fh->headerSize = pos;
+    return (int64_t)pos;
+}
+
+typedef struct {
+    unsigned id;
+    size_t hdrStart, hdrSize;
+    size_t nbVOs, nbRegens;
+    uint32_t* dist;
+} DNode;
+
+/* Decodes one block; appends each output to outs[]. Returns block size. */
+static int64_t decode_block(const FrameHdr* fh, const uint8_t* src, size_t size, size_t start,
+                            uint8_t** outBuf, size_t* outLen, int* outType, size_t* outW)
+{
+    const uint8_t* p = src + start;
+    const uint8_t* const end = src + size;
+    uint64_t nbDec, nbStored;
+    if (ozo_varint_dec(&p, end, &nbDec) || nbDec == 0) return -OZO_ERR_CORRUPTION;
+    nbDec--;
+    if (ozo_varint_dec(&p, end, &nbStored)) return -OZO_ERR_CORRUPTION;
+    if (nbDec >= 20000 || nbStored >= 110000) return -OZO_ERR_CORRUPTION;
+    size_t const nd = (size_t)nbDec, ns = (size_t)nbStored;
+    DNode* nodes = (DNode*)calloc(nd + 1, sizeof(DNode));
+    uint64_t* tmp = (uint64_t*)calloc(nd + ns + 8, 8);
+    uint8_t* trt = (uint8_t*)calloc(nd + 1, 1);
+    size_t* storedSizes = (size_t*)calloc(ns + 1, sizeof(size_t));
+    uint32_t* dists = NULL;
+    OStream* streams = NULL;
+    int64_t ret = 0;
+#define FAIL(code) do { ret = -(code); goto done; } while (0)
+    size_t r;
+    /* codec types: 1 bit each */
+    r = bitunpack(tmp, nd, p, (size_t)(end - p), 1);
+    if (r == (size_t)-1) FAIL(OZO_ERR_SRC_SIZE);
+    p += r;
+    size_t nbStd = 0;
+    for (size_t u = 0; u < nd; u++) { trt[u] = (uint8_t)tmp[u]; nbStd += !tmp[u]; }
+    if (nbStd != nd) FAIL(OZO_ERR_UNSUPPORTED); /* custom codecs */
+    /* standard IDs: nextPow2(63) = 6 bits each */
+    r = bitunpack(tmp, nd, p, (size_t)(end - p), ozo_nextpow2(TR_END));
+    if (r == (size_t)-1) FAIL(OZO_ERR_SRC_SIZE);
+    p += r;
+    for (size_t u = 0; u < nd; u++) nodes[u].id = (unsigned)tmp[u];
+    /* codec header sizes: 1-bit non-zero flags, then varint(size-1) */
+    r = bitunpack(tmp, nd, p, (size_t)(end - p), 1);
+    if (r == (size_t)-1) FAIL(OZO_ERR_SRC_SIZE);
+    p += r;
+    size_t totalTH = 0;
+    for (size_t u = 0; u < nd; u++) {
+        size_t hs = 0;
+        if (tmp[u]) {
+            uint64_t v;
+            if (ozo_varint_dec(&p, end, &v)) FAIL(OZO_ERR_CORRUPTION);
+            hs = (size_t)v + 1;
+        }
+        nodes[u].hdrStart = totalTH;
+        nodes[u].hdrSize = hs;
+        totalTH += hs;
+    }
+    /* number of variable inputs: 1-bit flags, then varint(n-1) */
+    r = bitunpack(tmp, nd, p, (size_t)(end - p), 1);
+    if (r == (size_t)-1) FAIL(OZO_ERR_SRC_SIZE);
+    p += r;
+    for (size_t u = 0; u < nd; u++) {
+        nodes[u].nbVOs = 0;
+        if (tmp[u]) {
+            uint64_t v;
+            if (ozo_varint_dec(&p, end, &v)) FAIL(OZO_ERR_CORRUPTION);
+            nodes[u].nbVOs = (size_t)v + 1;
+        }
+    }
+    /* number of regenerated streams: 1-bit flags, then varint(n-2) */
+    r = bitunpack(tmp, nd, p, (size_t)(end - p), 1);
+    if (r == (size_t)-1) FAIL(OZO_ERR_SRC_SIZE);
+    p += r;
+    size_t totalRegens = 0;
+    for (size_t u = 0; u < nd; u++) {
+        nodes[u].nbRegens = 1;
+        if (tmp[u]) {
+            uint64_t v;
+            if (ozo_varint_dec(&p, end, &v)) FAIL(OZO_ERR_CORRUPTION);
+            nodes[u].nbRegens = (size_t)v + 2;
+        }
+        totalRegens += nodes[u].nbRegens;
+    }
+    /* regenerated-stream distances */
+    dists = (uint32_t*)calloc(totalRegens + 1, 4);
+    {
+        uint64_t* dt = (uint64_t*)calloc(totalRegens + 1, 8);
+        r = bitunpack(dt, totalRegens, p, (size_t)(end - p), ozo_nextpow2(totalRegens + ns));
+        if (r == (size_t)-1) { free(dt); FAIL(OZO_ERR_SRC_SIZE); }
+        p += r;
+        for (size_t i = 0; i < totalRegens; i++) dists[i] = (uint32_t)dt[i];
+        free(dt);
+    }
+    for (size_t u = 0, d = 0; u < nd; u++) { nodes[u].dist = dists + d; d += nodes[u].nbRegens; }
+    /* stored stream sizes */
+    for (size_t u = 0; u < ns; u++) {
+        uint64_t v;
+        if (ozo_varint_dec(&p, end, &v) || v >= 0xFFFFFFFFu) FAIL(OZO_ERR_CORRUPTION);
+        storedSizes[u] = (size_t)v;
+    }
+    /* stream slots: regenerated ones marked, the rest filled from storage */
+    {
+        size_t const total = ns + totalRegens;
+        size_t const firstOutput = total - fh->nbOutputs;
+        streams = (OStream*)calloc(total + 1, sizeof(OStream));
+        uint8_t* isRegen = (uint8_t*)calloc(total + 1, 1);
+        size_t sidx = 0;
+        for (size_t u = 0; u < nd; u++) {
+            DecSig const sg = sig_of(nodes[u].id);
+            if (!sg.known) { free(isRegen); FAIL(OZO_ERR_UNSUPPORTED); }
+            if (!sg.voType && nodes[u].nbVOs) { free(isRegen); FAIL(OZO_ERR_CORRUPTION); }
+            size_t const inEnd = sidx + (size_t)sg.nbSO + nodes[u].nbVOs;
+            if (inEnd > firstOutput) { free(isRegen); FAIL(OZO_ERR_CORRUPTION); }
+            for (size_t k = 0; k < nodes[u].nbRegens; k++) {
+                size_t const o = inEnd + nodes[u].dist[k];
+                if (o >= total || isRegen[o]) { free(isRegen); FAIL(OZO_ERR_CORRUPTION); }
+                isRegen[o] = 1;
+            }
+            sidx = inEnd;
+        }
+        size_t pos = (size_t)(p - src);
+        size_t const thStart = pos;
+        pos += totalTH;
+        if (pos > size) { free(isRegen); FAIL(OZO_ERR_SRC_SIZE); }
+        size_t st = 0;
+        for (size_t i = 0; i < total; i++) {
+            if (isRegen[i]) continue;
+            if (st == ns) { free(isRegen); FAIL(OZO_ERR_CORRUPTION); }
+            if (pos + storedSizes[st] > size) { free(isRegen); FAIL(OZO_ERR_SRC_SIZE); }
+            ost_ref(&streams[i], OZO_TYPE_SERIAL, 1, storedSizes[st], src + pos);
+            pos += storedSizes[st];
+            st++;
+        }
+        free(isRegen);
+        if (st != ns) FAIL(OZO_ERR_CORRUPTION);
+        uint32_t contentCk = 0;
+        if (fh->hasContentCk) {
+            if (pos + 4 > size) FAIL(OZO_ERR_SRC_SIZE);
+            contentCk = ozo_rd32(src + pos);
+            pos += 4;
+        }
+        if (fh->hasCompressedCk) {
+            if (pos + 4 > size) FAIL(OZO_ERR_SRC_SIZE);
+            uint32_t const want = ozo_rd32(src + pos);
+            if ((uint32_t)ozo_xxh3_64(src + start, pos - start) != want) FAIL(OZO_ERR_CHECKSUM);
+            pos += 4;
+        }
+        /* run decoders in order */
+        sidx = 0;
+        for (size_t u = 0; u < nd; u++) {
+            DecSig const sg = sig_of(nodes[u].id);
+            size_t const nbIn = (size_t)sg.nbSO + nodes[u].nbVOs;
+            OStream* ins[300];
+            if (nbIn > 300) FAIL(OZO_ERR_UNSUPPORTED);
+            for (size_t k = 0; k < nbIn; k++) {
+                OStream* s = &streams[sidx + k];
+                size_t const inb = nbIn - 1 - k;
+                if (!s->filled) FAIL(OZO_ERR_CORRUPTION);
+                if ((int)inb < sg.nbSO) {
+                    if (s->type != sg.soTypes[inb]) FAIL(OZO_ERR_CORRUPTION);
+                } else if (!(s->type & sg.voType)) {
+                    FAIL(OZO_ERR_CORRUPTION);
+                }
+                ins[inb] = s;
+            }
+            if (nodes[u].nbRegens != 1) FAIL(OZO_ERR_CORRUPTION);
+            OStream* out = &streams[sidx + nbIn + nodes[u].dist[0]];
+            if (out->filled) FAIL(OZO_ERR_CORRUPTION);
+            int rc = dec_run(nodes[u].id, ins, nbIn, src + thStart + nodes[u].hdrStart,
+                             nodes[u].hdrSize, out);
+            if (rc) FAIL(-rc);
+            /* a stream that references its input takes over the input's buffer */
+            for (size_t k = 0; k < nbIn; k++) {
+                OStream* s = &streams[sidx + k];
+                if (s->own && out->p == s->p && !out->own) { out->own = s->own; s->own = NULL; }
+                ost_free(s);
+            }
+            sidx += nbIn;
+        }
+        /* outputs: last nbOutputs slots, in reverse order */
+        {
+            size_t catLen = 0;
+            for (size_t o = 0; o < fh->nbOutputs; o++) {
+                OStream* s = &streams[total - 1 - o];
+                if (!s->filled) FAIL(OZO_ERR_CORRUPTION);
+                catLen += s->n * s->w;
+            }
+            uint8_t* cat = (uint8_t*)malloc(catLen + 1);
+            size_t cp = 0;
+            for (size_t o = 0; o < fh->nbOutputs; o++) {
+                OStream* s = &streams[total - 1 - o];
+                size_t const b = s->n * s->w;
+                memcpy(cat + cp, s->p, b);
+                cp += b;
+                outBuf[o] = (uint8_t*)realloc(outBuf[o], outLen[o] + b + 1);
+                memcpy(outBuf[o] + outLen[o], s->p, b);
+                outLen[o] += b;
+                if (outType[o] == 0) { outType[o] = s->type; outW[o] = s->w; }
+                else if (outType[o] != s->type || outW[o] != s->w) { free(cat); FAIL(OZO_ERR_CORRUPTION); }
+            }
+            if (fh->hasContentCk && (uint32_t)ozo_xxh3_64(cat, catLen) != contentCk) {
+                free(cat);
+                FAIL(OZO_ERR_CHECKSUM);
+            }
+            free(cat);
+        }
+        ret = (int64_t)(pos - start);
+    }
+done:
+#undef FAIL
+    if (streams) {
+        size_t total = ns;
+        for (size_t u = 0; u < nd; u++) total += nodes[u].nbRegens;
+        for (size_t i = 0; i < total; i++) ost_free(&streams[i]);
+    }
+    free(streams);
+    free(nodes);
+    free(tmp);
+    free(trt);
+    free(storedSizes);
+    free(dists);
+    return ret;
+}
+
+int64_t ozo_decompressed_size(const void* src, size_t srcSize)
+{
+    FrameHdr fh;
+    int64_t r = parse_frame_header(&fh, (const uint8_t*)src, srcSize);
+    if (r < 0) return r;
+    if (fh.nbOutputs != 1) return -OZO_ERR_UNSUPPORTED;
+    return (int64_t)fh.sizes[0];
+}
+
+int64_t ozo_decompress(const void* srcv, size_t size, void* dst, size_t dstCap, int* outType,
+                       int* outEltWidth)
+{
+    const uint8_t* src = (const uint8_t*)srcv;
+    FrameHdr fh;
+    int64_t r = parse_frame_header(&fh, src, size);
+    if (r < 0) return r;
+    if (fh.nbOutputs != 1) return -OZO_ERR_UNSUPPORTED;
+    size_t pos = (size_t)r;
+    uint8_t* bufs[1] = { NULL };
+    size_t lens[1] = { 0 };
+    int types[1] = { 0 };
+    size_t ws[1] = { 0 };
+    for (;;) {
+        if (pos >= size) { free(bufs[0]); return -OZO_ERR_SRC_SIZE; }
+        if (src[pos] == 0) { pos++; break; }
+        int64_t b = decode_block(&fh, src, size, pos, bufs, lens, types, ws);
+        if (b < 0) { free(bufs[0]); return b; }
+        pos += (size_t)b;
+    }
+    if (lens[0] != fh.sizes[0]) { free(bufs[0]); return -OZO_ERR_CORRUPTION; }
+    if (lens[0] > dstCap) { free(bufs[0]); return -OZO_ERR_DST_SIZE; }
+    if (lens[0]) memcpy(dst, bufs[0], lens[0]);
+    free(bufs[0]);
+    if (outType) *outType = types[0] ? types[0] : fh.types[0];
+    if (outEltWidth) *outEltWidth = (int)(ws[0] ? ws[0] : 1);
+    return (int64_t)lens[0];
+}
