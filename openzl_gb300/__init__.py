@@ -1,0 +1,17 @@
+"""openzl_gb300: GB300-native OpenZL numeric codec-graph path.
+
+Python host bindings over the C-ABI library (include/openzl_gb300.h). The
+GPU path is the only path: importing works anywhere, but every decode call
+needs the compiled library (openzl_gb300.build.build()) and a CUDA device,
+and raises if either is missing.
+"""
+from ._lib import (  # noqa: F401
+    ZLError,
+    DCtx,
+    GpuBatch,
+    decompress,
+    get_decompressed_size,
+    get_compressed_size,
+    library,
+    library_path,
+)

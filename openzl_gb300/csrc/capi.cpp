@@ -1,0 +1,387 @@
+// C entry points of openzl_gb300 (declared in include/openzl_gb300.h).
+//
+// The ZL_* functions keep the reference's names and semantics
+// (include/openzl/zl_decompress.h, zl_errors.h); the ozl_gpu_* functions are
+// the device-resident additions. No exception crosses this boundary.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/openzl_gb300.h"
+#include "dec_exec.h"
+#include "dec_plan.h"
+
+namespace {
+
+ZL_Report ok(size_t v) { return ZL_Report{ ZL_ErrorCode_no_error, v }; }
+ZL_Report fail(int code) { return ZL_Report{ ZL_ErrorCode(code), 0 }; }
+
+// Grow-only device allocation with slack so that kernels may read whole
+// aligned words around the ends of the streams they hold.
+struct DevBuf {
+    uint8_t* p = nullptr;
+    size_t cap = 0;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    bool reserve(size_t bytes)
+    {
+        size_t const want = bytes + 256;
+        if (want <= cap) return true;
+        release();
+        if (cudaMalloc(&p, want) != cudaSuccess) {
+            p = nullptr;
+            return false;
+        }
+        cap = want;
+        return true;
+    }
+    uint8_t* data() const { return p ? p + 64 : nullptr; } // 64 bytes of slack in front
+};
+
+std::once_flag gPrepOnce;
+cudaError_t gPrepErr = cudaSuccess;
+cudaError_t prepare()
+{
+    std::call_once(gPrepOnce, [] { gPrepErr = ozl::prepareKernels(); });
+    return gPrepErr;
+}
+
+} // namespace
+
+// A planned decode of one or more frames, with its device resources.
+struct OZL_GpuBatch_s {
+    bool checkContent = true;
+    bool checkCompressed = true;
+    ozl::DecodePlan plan;
+    ozl::DeviceLayout layout;
+    DevBuf pool, scratch, arena, params, status;
+    std::vector<const uint8_t*> dFrames;
+    std::vector<uint8_t*> dOuts;
+    std::vector<size_t> sizes;
+    long launches = 0;
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t graphStream = nullptr;
+    std::string err;
+
+    ~OZL_GpuBatch_s() { dropGraph(); }
+    void dropGraph()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+
+    ZL_Report makePlan(size_t n, const void* const* hF, const size_t* fs, const void* const* dF,
+                       void* const* dO, const size_t* caps)
+    {
+        dropGraph();
+        if (prepare() != cudaSuccess) { err = "kernel attributes could not be set"; return fail(ZL_ErrorCode_GENERIC); }
+        int rc = plan.build(n, reinterpret_cast<const uint8_t* const*>(hF), fs, caps, checkContent,
+                            checkCompressed, err);
+        if (rc) return fail(rc);
+        dFrames.assign(reinterpret_cast<const uint8_t* const*>(dF), reinterpret_cast<const uint8_t* const*>(dF) + n);
+        dOuts.assign(reinterpret_cast<uint8_t* const*>(dO), reinterpret_cast<uint8_t* const*>(dO) + n);
+        sizes.resize(n);
+        for (size_t i = 0; i < n; i++) sizes[i] = size_t(plan.frames[i].decodedSize);
+        // size pass, allocate, then the real layout
+        rc = ozl::layoutPlan(plan, dFrames.data(), dOuts.data(), nullptr, nullptr, nullptr, nullptr, layout, err);
+        if (rc) return fail(rc);
+        if (!pool.reserve(layout.pool.size()) || !scratch.reserve(layout.scratchBytes)
+            || !arena.reserve(plan.arenaBytes) || !params.reserve(plan.params.size()) || !status.reserve(64)) {
+            err = "device allocation failed";
+            return fail(ZL_ErrorCode_allocation);
+        }
+        rc = ozl::layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), scratch.data(),
+                             pool.data(), layout, err);
+        if (rc) return fail(rc);
+        if (!layout.pool.empty()
+            && cudaMemcpy(pool.data(), layout.pool.data(), layout.pool.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            err = "descriptor upload failed";
+            return fail(ZL_ErrorCode_GENERIC);
+        }
+        if (!plan.params.empty()
+            && cudaMemcpy(params.data(), plan.params.data(), plan.params.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            err = "parameter upload failed";
+            return fail(ZL_ErrorCode_GENERIC);
+        }
+        launches = 0;
+        return ok(size_t(plan.totalOut));
+    }
+
+    ZL_Report enqueue(cudaStream_t s)
+    {
+        if (cudaMemsetAsync(status.data(), 0, 4, s) != cudaSuccess) return fail(ZL_ErrorCode_GENERIC);
+        long n = ozl::runLaunches(layout, pool.data(), scratch.data(), reinterpret_cast<uint32_t*>(status.data()), s);
+        if (n < 0) {
+            err = std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError());
+            return fail(ZL_ErrorCode_GENERIC);
+        }
+        launches = n;
+        return ok(0);
+    }
+
+    ZL_Report run(cudaStream_t s, bool useGraph)
+    {
+        if (!useGraph) return enqueue(s);
+        if (s == nullptr) {
+            err = "CUDA graph capture needs a non-default stream";
+            return fail(ZL_ErrorCode_parameter_invalid);
+        }
+        if (!graph || graphStream != s) {
+            dropGraph();
+            cudaGraph_t g = nullptr;
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                err = "stream capture failed";
+                return fail(ZL_ErrorCode_GENERIC);
+            }
+            ZL_Report r = enqueue(s);
+            cudaError_t e = cudaStreamEndCapture(s, &g);
+            if (ZL_isError(r)) { if (g) cudaGraphDestroy(g); return r; }
+            if (e != cudaSuccess) { err = "stream capture failed"; return fail(ZL_ErrorCode_GENERIC); }
+            e = cudaGraphInstantiate(&graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { graph = nullptr; err = "graph instantiation failed"; return fail(ZL_ErrorCode_GENERIC); }
+            graphStream = s;
+        }
+        if (cudaGraphLaunch(graph, s) != cudaSuccess) { err = "graph launch failed"; return fail(ZL_ErrorCode_GENERIC); }
+        return ok(0);
+    }
+
+    ZL_Report check(cudaStream_t s)
+    {
+        uint32_t st = 0;
+        if (cudaMemcpyAsync(&st, status.data(), 4, cudaMemcpyDeviceToHost, s) != cudaSuccess
+            || cudaStreamSynchronize(s) != cudaSuccess) {
+            err = std::string("device error: ") + cudaGetErrorString(cudaGetLastError());
+            return fail(ZL_ErrorCode_GENERIC);
+        }
+        if (st) {
+            err = st == 13 ? "compressed checksum mismatch"
+                           : st == 14 ? "content checksum mismatch" : st == 80 ? "device wait timed out" : "corruption";
+            return fail(int(st));
+        }
+        return ok(size_t(plan.totalOut));
+    }
+};
+
+struct ZL_DCtx_s {
+    OZL_GpuBatch_s batch;
+    bool sticky = false;
+    DevBuf frame, out;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    ~ZL_DCtx_s()
+    {
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+extern "C" {
+
+int ZL_isError(ZL_Report r) { return r._code != ZL_ErrorCode_no_error; }
+size_t ZL_validResult(ZL_Report r) { return r._value; }
+ZL_ErrorCode ZL_errorCode(ZL_Report r) { return r._code; }
+
+const char* ZL_ErrorCode_toString(ZL_ErrorCode code)
+{
+    switch (code) {
+        case ZL_ErrorCode_no_error: return "No error detected";
+        case ZL_ErrorCode_GENERIC: return "Error (generic)";
+        case ZL_ErrorCode_srcSize_tooSmall: return "Source size too small";
+        case ZL_ErrorCode_srcSize_tooLarge: return "Source size too large";
+        case ZL_ErrorCode_dstCapacity_tooSmall: return "Destination capacity too small";
+        case ZL_ErrorCode_header_unknown: return "Unknown header";
+        case ZL_ErrorCode_frameParameter_unsupported: return "Frame parameter unsupported";
+        case ZL_ErrorCode_corruption: return "Corrupted input";
+        case ZL_ErrorCode_compressedChecksumWrong: return "Compressed checksum mismatch";
+        case ZL_ErrorCode_contentChecksumWrong: return "Content checksum mismatch";
+        case ZL_ErrorCode_parameter_invalid: return "Invalid parameter";
+        case ZL_ErrorCode_invalidTransform: return "Codec not on the GPU path";
+        case ZL_ErrorCode_formatVersion_unsupported: return "Format version unsupported";
+        case ZL_ErrorCode_formatVersion_notSet: return "Format version not set";
+        case ZL_ErrorCode_allocation: return "Allocation failure";
+        case ZL_ErrorCode_temporaryLibraryLimitation: return "Temporary library limitation";
+        default: return "Error";
+    }
+}
+
+const char* ozl_gpu_version(void) { return "openzl_gb300 0.1 (sm_103a)"; }
+
+ZL_Report ZL_getDecompressedSize(const void* src, size_t size)
+{
+    if (!src || size < 7) return fail(ZL_ErrorCode_srcSize_tooSmall);
+    const uint8_t* p = static_cast<const uint8_t*>(src);
+    uint32_t const magic = uint32_t(p[0]) | (uint32_t(p[1]) << 8) | (uint32_t(p[2]) << 16) | (uint32_t(p[3]) << 24);
+    if (magic < 0xD7B1A5C0u + 21 || magic > 0xD7B1A5C0u + 23) return fail(ZL_ErrorCode_formatVersion_unsupported);
+    if ((p[5] & 15) != 1) return fail(ZL_ErrorCode_invalidRequest_singleOutputFrameOnly);
+    uint64_t v = 0;
+    size_t i = 6;
+    for (int sh = 0; sh < 70; sh += 7) {
+        if (i >= size) return fail(ZL_ErrorCode_srcSize_tooSmall);
+        uint8_t b = p[i++];
+        v |= uint64_t(b & 0x7f) << sh;
+        if (!(b & 0x80)) break;
+    }
+    if (v == 0) return fail(ZL_ErrorCode_temporaryLibraryLimitation);
+    return ok(size_t(v - 1));
+}
+
+ZL_Report ZL_getCompressedSize(const void* src, size_t size)
+{
+    ozl::DecodePlan plan;
+    std::string err;
+    const uint8_t* f = static_cast<const uint8_t*>(src);
+    int rc = plan.build(1, &f, &size, nullptr, false, false, err);
+    if (rc) return fail(rc);
+    return ok(size_t(plan.frames[0].frameBytes));
+}
+
+ZL_DCtx* ZL_DCtx_create(void)
+{
+    try {
+        return new ZL_DCtx_s();
+    } catch (...) {
+        return nullptr;
+    }
+}
+
+void ZL_DCtx_free(ZL_DCtx* dctx) { delete dctx; }
+
+ZL_Report ZL_DCtx_setParameter(ZL_DCtx* dctx, ZL_DParam param, int value)
+{
+    if (!dctx) return fail(ZL_ErrorCode_parameter_invalid);
+    switch (param) {
+        case ZL_DParam_stickyParameters: dctx->sticky = value != 0; break;
+        case ZL_DParam_checkCompressedChecksum: dctx->batch.checkCompressed = value != ZL_TernaryParam_disable; break;
+        case ZL_DParam_checkContentChecksum: dctx->batch.checkContent = value != ZL_TernaryParam_disable; break;
+        default: return fail(ZL_ErrorCode_parameter_invalid);
+    }
+    return ok(0);
+}
+
+const char* ZL_DCtx_getErrorContextString(const ZL_DCtx* dctx, ZL_Report report)
+{
+    if (!dctx) return ZL_ErrorCode_toString(report._code);
+    return dctx->err.empty() ? ZL_ErrorCode_toString(report._code) : dctx->err.c_str();
+}
+
+static void resetParams(ZL_DCtx* d)
+{
+    if (!d->sticky) {
+        d->batch.checkCompressed = true;
+        d->batch.checkContent = true;
+    }
+}
+
+ZL_Report ozl_gpu_decompress(ZL_DCtx* dctx, void* d_dst, size_t dstCap, const void* h_frame, const void* d_frame,
+                             size_t cSize, void* stream)
+{
+    if (!dctx || !h_frame || !d_frame) return fail(ZL_ErrorCode_parameter_invalid);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ZL_Report r = dctx->batch.makePlan(1, &h_frame, &cSize, &d_frame, &d_dst, &dstCap);
+    if (!ZL_isError(r)) r = dctx->batch.run(s, false);
+    if (!ZL_isError(r)) r = dctx->batch.check(s);
+    if (ZL_isError(r)) dctx->err = dctx->batch.err;
+    resetParams(dctx);
+    return r;
+}
+
+ZL_Report ZL_DCtx_decompress(ZL_DCtx* dctx, void* dst, size_t dstCap, const void* src, size_t cSize)
+{
+    if (!dctx || !src) return fail(ZL_ErrorCode_parameter_invalid);
+    ZL_Report ds = ZL_getDecompressedSize(src, cSize);
+    if (ZL_isError(ds)) { resetParams(dctx); return ds; }
+    size_t const outSize = ZL_validResult(ds);
+    if (outSize > dstCap) { resetParams(dctx); return fail(ZL_ErrorCode_dstCapacity_tooSmall); }
+    if (!dctx->stream && cudaStreamCreateWithFlags(&dctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        dctx->err = "no CUDA device";
+        return fail(ZL_ErrorCode_GENERIC);
+    }
+    if (!dctx->frame.reserve(cSize + 64) || !dctx->out.reserve(outSize + 64)) {
+        dctx->err = "device allocation failed";
+        return fail(ZL_ErrorCode_allocation);
+    }
+    cudaStream_t s = dctx->stream;
+    if (cudaMemcpyAsync(dctx->frame.data(), src, cSize, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+        dctx->err = "copy to device failed";
+        return fail(ZL_ErrorCode_GENERIC);
+    }
+    const void* dF = dctx->frame.data();
+    void* dO = dctx->out.data();
+    ZL_Report r = dctx->batch.makePlan(1, &src, &cSize, &dF, &dO, &dstCap);
+    if (!ZL_isError(r)) r = dctx->batch.run(s, false);
+    if (!ZL_isError(r) && outSize
+        && cudaMemcpyAsync(dst, dctx->out.data(), outSize, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        r = fail(ZL_ErrorCode_GENERIC);
+    if (!ZL_isError(r)) r = dctx->batch.check(s);
+    if (ZL_isError(r)) dctx->err = dctx->batch.err;
+    resetParams(dctx);
+    return ZL_isError(r) ? r : ok(outSize);
+}
+
+ZL_Report ZL_decompress(void* dst, size_t dstCap, const void* src, size_t cSize)
+{
+    ZL_DCtx* d = ZL_DCtx_create();
+    if (!d) return fail(ZL_ErrorCode_allocation);
+    ZL_Report r = ZL_DCtx_decompress(d, dst, dstCap, src, cSize);
+    ZL_DCtx_free(d);
+    return r;
+}
+
+OZL_GpuBatch* ozl_gpu_batch_create(void)
+{
+    try {
+        return new OZL_GpuBatch_s();
+    } catch (...) {
+        return nullptr;
+    }
+}
+
+void ozl_gpu_batch_free(OZL_GpuBatch* b) { delete b; }
+
+ZL_Report ozl_gpu_batch_setParameter(OZL_GpuBatch* b, ZL_DParam param, int value)
+{
+    if (!b) return fail(ZL_ErrorCode_parameter_invalid);
+    switch (param) {
+        case ZL_DParam_checkCompressedChecksum: b->checkCompressed = value != ZL_TernaryParam_disable; break;
+        case ZL_DParam_checkContentChecksum: b->checkContent = value != ZL_TernaryParam_disable; break;
+        case ZL_DParam_stickyParameters: break;
+        default: return fail(ZL_ErrorCode_parameter_invalid);
+    }
+    return ok(0);
+}
+
+ZL_Report ozl_gpu_batch_plan(OZL_GpuBatch* b, size_t n, const void* const* hF, const size_t* fs,
+                             const void* const* dF, void* const* dO, const size_t* caps)
+{
+    if (!b || !hF || !fs || !dF || !dO) return fail(ZL_ErrorCode_parameter_invalid);
+    return b->makePlan(n, hF, fs, dF, dO, caps);
+}
+
+ZL_Report ozl_gpu_batch_run(OZL_GpuBatch* b, void* stream, int useGraph)
+{
+    if (!b) return fail(ZL_ErrorCode_parameter_invalid);
+    return b->run(static_cast<cudaStream_t>(stream), useGraph != 0);
+}
+
+ZL_Report ozl_gpu_batch_check(OZL_GpuBatch* b, void* stream)
+{
+    if (!b) return fail(ZL_ErrorCode_parameter_invalid);
+    return b->check(static_cast<cudaStream_t>(stream));
+}
+
+size_t ozl_gpu_batch_launches(const OZL_GpuBatch* b) { return b ? size_t(b->launches) : 0; }
+
+const size_t* ozl_gpu_batch_sizes(const OZL_GpuBatch* b) { return b ? b->sizes.data() : nullptr; }
+
+const char* ozl_gpu_batch_error(const OZL_GpuBatch* b) { return b ? b->err.c_str() : ""; }
+
+} // extern "C"

@@ -1,0 +1,20 @@
+// Kernel dispatch for a laid-out decode plan.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "dec_plan.h"
+
+namespace ozl {
+
+// Enqueues every launch of `layout` on `stream`. `dPool` holds the uploaded
+// descriptor pool, `dScratch` the look-back status and hash block sums,
+// `dStatus` the batch error word. Returns the number of kernels launched, or
+// a negative value if a launch could not be issued.
+long runLaunches(const DeviceLayout& layout, uint8_t* dPool, uint8_t* dScratch, uint32_t* dStatus,
+                 cudaStream_t stream);
+
+// Applies the shared-memory carve-out attributes the entropy kernels need.
+// Call once per device before the first launch (and before graph capture).
+cudaError_t prepareKernels();
+
+} // namespace ozl

@@ -1,0 +1,1076 @@
+// Host-side decode planner.
+//
+// OpenZL's universal decoder (src/openzl/decompress/decompress2.c:1266-1290,
+// runDecoders/processStream) walks a frame's decoder list serially, creating
+// each regenerated stream when its decoder runs. On the GPU the same walk is
+// done once on the host, before any payload is touched: every stream's type,
+// width and element count follows from the frame headers and codec headers
+// alone (the one exception, the FSE normalized-count header, is parsed here
+// from the stored stream). The planner then
+//   1. fuses numeric chains (delta <- zigzag <- view <- transpose|bitpack) into
+//      one pipeline task,
+//   2. places streams: outputs of views and concatenations (splitN) are laid
+//      directly where their consumer wants them, so those decoders cost no
+//      copy, and the last decoder writes straight into the caller's buffer,
+//   3. assigns dependency levels and groups tasks per (level, codec kind),
+//      one kernel launch per group across all frames of a batch.
+#include "dec_plan.h"
+
+#include <algorithm>
+#include <cstring>
+#include <functional>
+#include <type_traits>
+
+namespace ozl {
+
+namespace {
+
+// Standard transform IDs (src/openzl/common/wire_format.h:211-306).
+enum : uint32_t {
+    T_DELTA = 1,
+    T_ZIGZAG = 3,
+    T_TSPLIT = 4,
+    T_CONV_SERIAL_TO_STRUCT = 5,
+    T_CONV_STRUCT_TO_SERIAL = 6,
+    T_CONV_STRUCT_TO_NUM = 7,
+    T_CONV_NUM_TO_STRUCT = 8,
+    T_CONV_SERIAL_TO_NUM = 9,
+    T_CONV_NUM_TO_SERIAL = 10,
+    T_BITPACK_SERIAL = 27,
+    T_BITPACK_INT = 28,
+    T_FLATPACK = 29,
+    T_FLOATDEC = 33,
+    T_TOKENIZE_FIXED = 36,
+    T_TOKENIZE_NUMERIC = 37,
+    T_SPLITN = 40,
+    T_CONST_SERIAL = 44,
+    T_CONST_FIXED = 45,
+    T_SPLITN_STRUCT = 47,
+    T_SPLITN_NUM = 48,
+    T_FSE = 49,
+    T_HUF = 50,
+    T_NCOUNT = 52,
+    T_ID_END = 63,
+};
+
+enum : int { TY_SERIAL = 1, TY_STRUCT = 2, TY_NUMERIC = 4, TY_STRING = 8 };
+
+// Decoder signature: singleton inputs (types in decoder order), variable
+// input type, regenerated type. Mirrors the graph descriptions registered in
+// src/openzl/codecs/decoder_registry.c:88-161.
+struct Sig {
+    bool known;
+    int nbSO;
+    int so[2];
+    int vo;
+    int out;
+    bool view;    // regenerated bytes equal the input bytes
+    bool concat;  // regenerated stream is the concatenation of the inputs
+};
+
+Sig signature(uint32_t id)
+{
+    switch (id) {
+        case T_DELTA:
+        case T_ZIGZAG: return { true, 1, { TY_NUMERIC, 0 }, 0, TY_NUMERIC, false, false };
+        case T_TSPLIT: return { true, 0, { 0, 0 }, TY_SERIAL, TY_STRUCT, false, false };
+        case T_CONV_SERIAL_TO_STRUCT: return { true, 1, { TY_STRUCT, 0 }, 0, TY_SERIAL, true, false };
+        case T_CONV_STRUCT_TO_SERIAL: return { true, 1, { TY_SERIAL, 0 }, 0, TY_STRUCT, true, false };
+        case T_CONV_STRUCT_TO_NUM: return { true, 1, { TY_NUMERIC, 0 }, 0, TY_STRUCT, true, false };
+        case T_CONV_NUM_TO_STRUCT: return { true, 1, { TY_STRUCT, 0 }, 0, TY_NUMERIC, true, false };
+        case T_CONV_SERIAL_TO_NUM: return { true, 1, { TY_NUMERIC, 0 }, 0, TY_SERIAL, true, false };
+        case T_CONV_NUM_TO_SERIAL: return { true, 1, { TY_SERIAL, 0 }, 0, TY_NUMERIC, true, false };
+        case T_BITPACK_SERIAL: return { true, 1, { TY_SERIAL, 0 }, 0, TY_SERIAL, false, false };
+        case T_BITPACK_INT: return { true, 1, { TY_SERIAL, 0 }, 0, TY_NUMERIC, false, false };
+        case T_FLATPACK: return { true, 2, { TY_SERIAL, TY_SERIAL }, 0, TY_SERIAL, false, false };
+        case T_FLOATDEC: return { true, 2, { TY_STRUCT, TY_SERIAL }, 0, TY_NUMERIC, false, false };
+        case T_TOKENIZE_FIXED: return { true, 2, { TY_STRUCT, TY_NUMERIC }, 0, TY_STRUCT, false, false };
+        case T_TOKENIZE_NUMERIC: return { true, 2, { TY_NUMERIC, TY_NUMERIC }, 0, TY_NUMERIC, false, false };
+        case T_SPLITN: return { true, 0, { 0, 0 }, TY_SERIAL, TY_SERIAL, false, true };
+        case T_SPLITN_STRUCT: return { true, 0, { 0, 0 }, TY_STRUCT, TY_STRUCT, false, true };
+        case T_SPLITN_NUM: return { true, 0, { 0, 0 }, TY_NUMERIC, TY_NUMERIC, false, true };
+        case T_CONST_SERIAL: return { true, 1, { TY_SERIAL, 0 }, 0, TY_SERIAL, false, false };
+        case T_CONST_FIXED: return { true, 1, { TY_STRUCT, 0 }, 0, TY_STRUCT, false, false };
+        case T_FSE:
+        case T_HUF: return { true, 2, { TY_NUMERIC, TY_SERIAL }, 0, TY_SERIAL, false, false };
+        case T_NCOUNT: return { true, 1, { TY_SERIAL, 0 }, 0, TY_NUMERIC, false, false };
+        default: return { false, 0, { 0, 0 }, 0, 0, false, false };
+    }
+}
+
+// ZL error codes used by the planner (include/openzl/zl_errors_types.h).
+enum : int {
+    E_GENERIC = 1,
+    E_SRC_SMALL = 3,
+    E_DST_SMALL = 5,
+    E_HEADER = 10,
+    E_CORRUPT = 12,
+    E_CK_COMPRESSED = 13,
+    E_VERSION = 60,
+    E_LIMIT = 81,
+    E_TRANSFORM = 32,
+};
+
+struct Reader {
+    const uint8_t* p;
+    const uint8_t* end;
+    bool varint(uint64_t& v)
+    {
+        v = 0;
+        for (int sh = 0; sh < 70; sh += 7) {
+            if (p >= end) return false;
+            uint8_t b = *p++;
+            v |= uint64_t(b & 0x7f) << sh;
+            if (!(b & 0x80)) return true;
+        }
+        return false;
+    }
+    // n fields of nbBits, LSB-first (frame-header bit-packed arrays).
+    bool unpack(std::vector<uint64_t>& dst, size_t n, int nbBits)
+    {
+        size_t need = (n * size_t(nbBits) + 7) / 8;
+        if (size_t(end - p) < need) return false;
+        dst.assign(n, 0);
+        for (size_t i = 0; i < n; i++) {
+            size_t bit = i * size_t(nbBits);
+            uint64_t v = 0;
+            for (int b = 0; b < nbBits; b++) {
+                size_t q = bit + size_t(b);
+                v |= uint64_t((p[q >> 3] >> (q & 7)) & 1) << b;
+            }
+            dst[i] = v;
+        }
+        p += need;
+        return true;
+    }
+};
+
+int nextPow2Bits(uint64_t v)
+{
+    int n = 0;
+    while (n < 64 && (uint64_t(1) << n) < v) n++;
+    return n;
+}
+
+uint64_t readLEn(const uint8_t* p, size_t n)
+{
+    uint64_t v = 0;
+    for (size_t i = 0; i < n; i++) v |= uint64_t(p[i]) << (8 * i);
+    return v;
+}
+
+uint32_t readLE32(const uint8_t* p) { return uint32_t(readLEn(p, 4)); }
+
+int highbit32(uint32_t v) { return 31 - __builtin_clz(v); }
+
+// FSE normalized-count header parser (the format of
+// src/openzl/fse/common/entropy_common.c:42-185). Returns bytes consumed or -1.
+long parseNCount(int16_t* norm, unsigned& nbSym, const uint8_t* src, size_t size)
+{
+    size_t pos = 0;
+    size_t const total = size * 8;
+    auto bits = [&](int nb) -> uint32_t {
+        uint32_t v = 0;
+        for (int i = 0; i < nb; i++) {
+            size_t q = pos + size_t(i);
+            if (q < total) v |= uint32_t((src[q >> 3] >> (q & 7)) & 1) << i;
+        }
+        return v;
+    };
+    if (size == 0) return -1;
+    int nb = int(bits(4)) + 5;
+    pos += 4;
+    if (nb > 15) return -1;
+    int remaining = (1 << nb) + 1, threshold = 1 << nb;
+    nb++;
+    unsigned sym = 0;
+    bool prev0 = false;
+    std::memset(norm, 0, 256 * sizeof(int16_t));
+    while (remaining > 1 && sym < 256) {
+        if (prev0) {
+            unsigned z = sym;
+            while (bits(2) == 3) { z += 3; pos += 2; }
+            z += bits(2);
+            pos += 2;
+            if (z > 256) return -1;
+            sym = z;
+            if (sym >= 256) break;
+        }
+        int const max = (2 * threshold - 1) - remaining;
+        uint32_t const low = bits(nb - 1);
+        int count;
+        if (int(low) < max) {
+            count = int(low);
+            pos += size_t(nb - 1);
+        } else {
+            count = int(bits(nb));
+            if (count >= threshold) count -= max;
+            pos += size_t(nb);
+        }
+        count--;
+        remaining -= count < 0 ? -count : count;
+        norm[sym++] = int16_t(count);
+        prev0 = (count == 0);
+        while (remaining < threshold) {
+            nb--;
+            threshold >>= 1;
+        }
+    }
+    if (remaining != 1 || sym > 256 || pos > total) return -1;
+    nbSym = sym;
+    return long((pos + 7) / 8);
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+int DecodePlan::build(size_t nbFrames, const uint8_t* const* hFrames, const size_t* frameSizes,
+                      const size_t* dstCapacities, bool ckContent, bool ckCompressed,
+                      std::string& err)
+{
+    frames.assign(nbFrames, FramePlan());
+    streams.clear();
+    nodes.clear();
+    hashes.clear();
+    params.clear();
+    arenaBytes = 0;
+    totalOut = 0;
+    for (size_t f = 0; f < nbFrames; f++) {
+        int rc = planFrame(int(f), hFrames[f], frameSizes[f],
+                           dstCapacities ? dstCapacities[f] : SIZE_MAX, ckContent, ckCompressed, err);
+        if (rc) {
+            err = "frame " + std::to_string(f) + ": " + err;
+            return rc;
+        }
+        totalOut += frames[f].decodedSize;
+    }
+    return 0;
+}
+
+// Frame header (src/openzl/decompress/decode_frameheader.c:237-340).
+int DecodePlan::planFrame(int f, const uint8_t* src, size_t size, size_t dstCap, bool ckContent,
+                          bool ckCompressed, std::string& err)
+{
+    if (size < 9) { err = "frame too small"; return E_SRC_SMALL; }
+    uint32_t const magic = readLE32(src);
+    if (magic < 0xD7B1A5C0u + 21 || magic > 0xD7B1A5C0u + 23) {
+        err = "unsupported format version or bad magic";
+        return E_VERSION;
+    }
+    unsigned const version = magic - 0xD7B1A5C0u;
+    size_t pos = 4;
+    uint8_t const flags = src[pos++];
+    bool const hasContentCk = flags & 1, hasCompressedCk = (flags >> 1) & 1, hasComment = (flags >> 2) & 1;
+    uint8_t const t1 = src[pos++];
+    size_t const nbOut = t1 & 15;
+    if (nbOut != 1) { err = "only single-output frames are supported"; return E_LIMIT; }
+    static const int typeMap[4] = { TY_SERIAL, TY_STRUCT, TY_NUMERIC, TY_STRING };
+    int const outType = typeMap[(t1 >> 4) & 3];
+    if (outType == TY_STRING) { err = "string outputs are not supported"; return E_LIMIT; }
+    Reader rd{ src + pos, src + size };
+    uint64_t sz1;
+    if (!rd.varint(sz1) || sz1 == 0) { err = "unknown decompressed size"; return E_LIMIT; }
+    uint64_t const outSize = sz1 - 1;
+    if (outSize > dstCap) { err = "destination too small"; return E_DST_SMALL; }
+    if (version >= 22 && hasComment) {
+        uint64_t c;
+        if (!rd.varint(c) || c == 0 || c > size_t(rd.end - rd.p)) { err = "bad comment"; return E_CORRUPT; }
+        rd.p += c;
+    }
+    pos = size_t(rd.p - src);
+    if (hasCompressedCk) {
+        if (pos + 1 > size) { err = "truncated header"; return E_SRC_SMALL; }
+        // header checksum byte: low 8 bits of XXH3 over the header; verified on
+        // the device together with the block checksums.
+        if (ckCompressed)
+            hashes.push_back(PlanHash{ f, false, 0, pos, src[pos], E_CK_COMPRESSED, true });
+        pos++;
+    }
+    frames[f].outType = outType;
+    uint64_t produced = 0;
+    for (;;) {
+        if (pos >= size) { err = "missing end-of-frame marker"; return E_SRC_SMALL; }
+        if (src[pos] == 0) break;
+        size_t consumed = 0;
+        uint64_t blockBytes = 0;
+        int rc = planBlock(f, src, size, pos, &consumed, hasContentCk, hasCompressedCk, ckContent,
+                           ckCompressed, nbOut, produced, &blockBytes, err);
+        if (rc) return rc;
+        pos += consumed;
+        produced += blockBytes;
+    }
+    if (produced != outSize) { err = "decoded size does not match the frame header"; return E_CORRUPT; }
+    frames[f].decodedSize = outSize;
+    frames[f].frameBytes = pos + 1;
+    return 0;
+}
+
+// One block: chunk header (src/openzl/decompress/decode_frameheader.c:938-1171),
+// stored streams (src/openzl/decompress/decompress2.c:632-834), checksums
+// (decompress2.c:1478-1570).
+int DecodePlan::planBlock(int f, const uint8_t* src, size_t size, size_t start, size_t* consumed,
+                          bool hasContentCk, bool hasCompressedCk, bool ckContent, bool ckCompressed,
+                          size_t nbOutputs, uint64_t outOffset, uint64_t* outBytes, std::string& err)
+{
+    Reader rd{ src + start, src + size };
+    uint64_t nd, ns;
+    if (!rd.varint(nd) || nd == 0) { err = "bad decoder count"; return E_CORRUPT; }
+    nd--;
+    if (!rd.varint(ns)) { err = "bad stored-stream count"; return E_CORRUPT; }
+    if (nd >= 20000 || ns >= 110000) { err = "graph too large"; return E_LIMIT; }
+    std::vector<uint64_t> trt, ids, hflags, vflags, rflags;
+    if (!rd.unpack(trt, nd, 1)) { err = "truncated codec types"; return E_SRC_SMALL; }
+    for (uint64_t t : trt)
+        if (t) { err = "custom codecs are not on the GPU path"; return E_TRANSFORM; }
+    if (!rd.unpack(ids, nd, nextPow2Bits(T_ID_END))) { err = "truncated codec ids"; return E_SRC_SMALL; }
+    if (!rd.unpack(hflags, nd, 1)) { err = "truncated header sizes"; return E_SRC_SMALL; }
+    std::vector<uint64_t> hsz(nd, 0), hstart(nd, 0);
+    uint64_t totalTH = 0;
+    for (size_t u = 0; u < nd; u++) {
+        if (hflags[u]) {
+            uint64_t v;
+            if (!rd.varint(v)) { err = "bad header size"; return E_CORRUPT; }
+            hsz[u] = v + 1;
+        }
+        hstart[u] = totalTH;
+        totalTH += hsz[u];
+    }
+    if (!rd.unpack(vflags, nd, 1)) { err = "truncated VO counts"; return E_SRC_SMALL; }
+    std::vector<uint64_t> nbVO(nd, 0), nbRegen(nd, 1);
+    for (size_t u = 0; u < nd; u++)
+        if (vflags[u]) {
+            uint64_t v;
+            if (!rd.varint(v)) { err = "bad VO count"; return E_CORRUPT; }
+            nbVO[u] = v + 1;
+        }
+    if (!rd.unpack(rflags, nd, 1)) { err = "truncated regen counts"; return E_SRC_SMALL; }
+    uint64_t totalRegen = 0;
+    for (size_t u = 0; u < nd; u++) {
+        if (rflags[u]) {
+            uint64_t v;
+            if (!rd.varint(v)) { err = "bad regen count"; return E_CORRUPT; }
+            nbRegen[u] = v + 2;
+        }
+        totalRegen += nbRegen[u];
+    }
+    std::vector<uint64_t> dist;
+    if (!rd.unpack(dist, totalRegen, nextPow2Bits(totalRegen + ns))) { err = "truncated distances"; return E_SRC_SMALL; }
+    std::vector<uint64_t> storedSize(ns);
+    for (size_t i = 0; i < ns; i++)
+        if (!rd.varint(storedSize[i]) || storedSize[i] >= 0xFFFFFFFFull) { err = "bad stored size"; return E_CORRUPT; }
+
+    // ---- stream slots -----------------------------------------------------
+    size_t const total = ns + totalRegen;
+    size_t const firstOutput = total - nbOutputs;
+    int const sBase = int(streams.size());
+    int const nBase = int(nodes.size());
+    streams.resize(streams.size() + total);
+    std::vector<char> isRegen(total, 0);
+    std::vector<Sig> sigs(nd);
+    {
+        size_t sidx = 0, d = 0;
+        for (size_t u = 0; u < nd; u++) {
+            sigs[u] = signature(uint32_t(ids[u]));
+            if (!sigs[u].known) {
+                err = "codec id " + std::to_string(ids[u]) + " is not on the GPU path";
+                return E_TRANSFORM;
+            }
+            if (!sigs[u].vo && nbVO[u]) { err = "unexpected variable inputs"; return E_CORRUPT; }
+            if (nbRegen[u] != 1) { err = "multi-output decoders are not on the GPU path"; return E_TRANSFORM; }
+            size_t const inEnd = sidx + size_t(sigs[u].nbSO) + nbVO[u];
+            if (inEnd > firstOutput) { err = "graph inconsistency"; return E_CORRUPT; }
+            size_t const o = inEnd + dist[d];
+            d += nbRegen[u];
+            if (o >= total || isRegen[o]) { err = "graph inconsistency"; return E_CORRUPT; }
+            isRegen[o] = 1;
+            sidx = inEnd;
+        }
+    }
+    size_t pos = size_t(rd.p - src);
+    size_t const thStart = pos;
+    pos += totalTH;
+    if (pos > size) { err = "truncated codec headers"; return E_SRC_SMALL; }
+    {
+        size_t st = 0;
+        for (size_t i = 0; i < total; i++) {
+            if (isRegen[i]) continue;
+            if (st == ns) { err = "stream count mismatch"; return E_CORRUPT; }
+            if (pos + storedSize[st] > size) { err = "truncated stored stream"; return E_SRC_SMALL; }
+            PlanStream& s = streams[sBase + int(i)];
+            s.type = TY_SERIAL;
+            s.w = 1;
+            s.n = storedSize[st];
+            s.loc = L_FRAME;
+            s.frame = f;
+            s.off = pos;
+            pos += storedSize[st];
+            st++;
+        }
+        if (st != ns) { err = "stream count mismatch"; return E_CORRUPT; }
+    }
+    uint32_t contentCk = 0;
+    if (hasContentCk) {
+        if (pos + 4 > size) { err = "truncated checksum"; return E_SRC_SMALL; }
+        contentCk = readLE32(src + pos);
+        pos += 4;
+    }
+    if (hasCompressedCk) {
+        if (pos + 4 > size) { err = "truncated checksum"; return E_SRC_SMALL; }
+        if (ckCompressed)
+            hashes.push_back(PlanHash{ f, false, start, pos - start, readLE32(src + pos), E_CK_COMPRESSED, false });
+        pos += 4;
+    }
+
+    // ---- nodes and sizes (forward, decoder order) ------------------------
+    auto S = [&](size_t local) -> PlanStream& { return streams[sBase + int(local)]; };
+    {
+        size_t sidx = 0, d = 0;
+        for (size_t u = 0; u < nd; u++) {
+            PlanNode nodeU;
+            nodeU.id = uint32_t(ids[u]);
+            nodeU.frame = f;
+            nodeU.hdr = src + thStart + hstart[u];
+            nodeU.hsz = size_t(hsz[u]);
+            Sig const& sg = sigs[u];
+            size_t const nbIn = size_t(sg.nbSO) + nbVO[u];
+            nodeU.ins.resize(nbIn);
+            for (size_t k = 0; k < nbIn; k++) {
+                size_t const inb = nbIn - 1 - k; // decoder input order is reversed
+                PlanStream& s = S(sidx + k);
+                if (s.type == 0) { err = "input stream not filled"; return E_CORRUPT; }
+                if (int(inb) < sg.nbSO ? s.type != sg.so[inb] : !(s.type & sg.vo)) {
+                    err = "input type mismatch";
+                    return E_CORRUPT;
+                }
+                nodeU.ins[inb] = sBase + int(sidx + k);
+            }
+            size_t const oLocal = sidx + nbIn + dist[d];
+            d += nbRegen[u];
+            nodeU.out = sBase + int(oLocal);
+            PlanStream& O = S(oLocal);
+            O.producer = nBase + int(u);
+            O.type = sg.out;
+            const uint8_t* h = nodeU.hdr;
+            size_t const hs = nodeU.hsz;
+            auto in = [&](int k) -> PlanStream& { return streams[nodeU.ins[k]]; };
+            switch (nodeU.id) {
+                case T_DELTA: {
+                    O.w = in(0).w;
+                    if (hs) {
+                        if (hs != in(0).w) { err = "delta header size"; return E_CORRUPT; }
+                        O.n = in(0).n + 1;
+                    } else {
+                        if (in(0).n) { err = "delta without first value"; return E_CORRUPT; }
+                        O.n = 0;
+                    }
+                    break;
+                }
+                case T_ZIGZAG: O.w = in(0).w; O.n = in(0).n; break;
+                case T_TSPLIT: {
+                    if (nbIn == 0) { err = "empty transpose"; return E_CORRUPT; }
+                    for (size_t k = 0; k < nbIn; k++)
+                        if (in(int(k)).n != in(0).n || in(int(k)).w != 1) { err = "transpose plane sizes"; return E_CORRUPT; }
+                    O.w = uint32_t(nbIn);
+                    O.n = in(0).n;
+                    break;
+                }
+                case T_CONV_NUM_TO_STRUCT: {
+                    uint32_t w = in(0).w;
+                    if (!(w == 1 || w == 2 || w == 4 || w == 8)) { err = "numeric width"; return E_CORRUPT; }
+                    O.w = w; O.n = in(0).n;
+                    break;
+                }
+                case T_CONV_STRUCT_TO_NUM: O.w = in(0).w; O.n = in(0).n; break;
+                case T_CONV_SERIAL_TO_NUM:
+                case T_CONV_SERIAL_TO_STRUCT: O.w = 1; O.n = in(0).n * in(0).w; break;
+                case T_CONV_NUM_TO_SERIAL: {
+                    if (hs != 1 || h[0] > 3) { err = "conversion header"; return E_HEADER; }
+                    uint32_t w = 1u << h[0];
+                    uint64_t b = in(0).bytes();
+                    if (b % w) { err = "conversion size"; return E_CORRUPT; }
+                    O.w = w; O.n = b / w;
+                    break;
+                }
+                case T_CONV_STRUCT_TO_SERIAL: {
+                    Reader hr{ h, h + hs };
+                    uint64_t w;
+                    if (!hr.varint(w) || w == 0 || hr.p != h + hs) { err = "conversion header"; return E_HEADER; }
+                    uint64_t b = in(0).bytes();
+                    if (b % w) { err = "conversion size"; return E_CORRUPT; }
+                    O.w = uint32_t(w); O.n = b / w;
+                    break;
+                }
+                case T_BITPACK_SERIAL:
+                case T_BITPACK_INT: {
+                    if (hs < 1 || hs > 2) { err = "bitpack header"; return E_HEADER; }
+                    uint32_t w = 1u << ((h[0] >> 6) & 3);
+                    int nbBits = 1 + (h[0] & 0x3f);
+                    if (uint32_t(nbBits) > 8 * w) { err = "bitpack width"; return E_CORRUPT; }
+                    if (nodeU.id == T_BITPACK_SERIAL && w != 1) { err = "bitpack width"; return E_HEADER; }
+                    uint64_t srcSize = in(0).n;
+                    uint64_t maxN = srcSize * 8 / uint64_t(nbBits);
+                    uint64_t n = maxN;
+                    if (hs > 1) {
+                        if (h[1] > maxN) { err = "bitpack header"; return E_CORRUPT; }
+                        n -= h[1];
+                    }
+                    if ((n * uint64_t(nbBits) + 7) / 8 != srcSize) { err = "bitpack size"; return E_CORRUPT; }
+                    O.w = w; O.n = n;
+                    nodeU.nbBits = uint8_t(nbBits);
+                    break;
+                }
+                case T_FLATPACK: {
+                    PlanStream& A = in(0);
+                    PlanStream& P = in(1);
+                    if (A.n > 256) { err = "flatpack alphabet"; return E_CORRUPT; }
+                    uint64_t n = 0;
+                    unsigned nb = A.n <= 1 ? unsigned(A.n) : 1u + unsigned(highbit32(uint32_t(A.n - 1)));
+                    if (P.n && A.n) {
+                        if (P.loc != L_FRAME) { err = "flatpack over a regenerated stream"; return E_LIMIT; }
+                        uint32_t last = src[P.off + P.n - 1] | 1u;
+                        uint64_t pad = uint64_t(__builtin_clz(last << 24)) + 1;
+                        n = (8 * P.n - pad) / nb;
+                    }
+                    O.w = 1; O.n = n;
+                    nodeU.nbBits = uint8_t(nb);
+                    break;
+                }
+                case T_FLOATDEC: {
+                    if (hs != 1 || h[0] > 2) { err = "float header"; return E_CORRUPT; }
+                    uint32_t const sfw = h[0] == 0 ? 3 : (h[0] == 1 ? 1 : 2);
+                    if (in(0).n != in(1).n || in(0).w != sfw || in(1).w != 1) { err = "float inputs"; return E_CORRUPT; }
+                    O.w = h[0] == 0 ? 4 : 2;
+                    O.n = in(1).n;
+                    break;
+                }
+                case T_TOKENIZE_FIXED:
+                case T_TOKENIZE_NUMERIC: {
+                    uint32_t iw = in(1).w;
+                    if (!(iw == 1 || iw == 2 || iw == 4 || iw == 8)) { err = "index width"; return E_CORRUPT; }
+                    O.w = in(0).w; O.n = in(1).n;
+                    break;
+                }
+                case T_SPLITN:
+                case T_SPLITN_STRUCT:
+                case T_SPLITN_NUM: {
+                    uint32_t w = 1;
+                    if (nbIn == 0) {
+                        if (hs) {
+                            Reader hr{ h, h + hs };
+                            uint64_t v;
+                            if (!hr.varint(v)) { err = "splitN header"; return E_CORRUPT; }
+                            w = uint32_t(v);
+                        }
+                    } else {
+                        w = in(0).w;
+                    }
+                    uint64_t n = 0;
+                    for (size_t k = 0; k < nbIn; k++) {
+                        if (in(int(k)).w != w || in(int(k)).type != in(0).type) { err = "splitN inputs"; return E_CORRUPT; }
+                        n += in(int(k)).n;
+                    }
+                    O.w = w; O.n = n;
+                    break;
+                }
+                case T_CONST_SERIAL:
+                case T_CONST_FIXED: {
+                    if (in(0).n != 1) { err = "constant input"; return E_CORRUPT; }
+                    Reader hr{ h, h + hs };
+                    uint64_t n;
+                    if (!hr.varint(n) || hr.p != h + hs || n < 1) { err = "constant header"; return E_CORRUPT; }
+                    O.w = in(0).w; O.n = n;
+                    break;
+                }
+                case T_NCOUNT: {
+                    PlanStream& I = in(0);
+                    if (I.loc != L_FRAME) { err = "ncount over a regenerated stream"; return E_LIMIT; }
+                    int16_t norm[256];
+                    unsigned nbSym = 0;
+                    long r = parseNCount(norm, nbSym, src + I.off, size_t(I.n));
+                    if (r < 0 || uint64_t(r) != I.n) { err = "bad normalized counts"; return E_CORRUPT; }
+                    size_t const off = (params.size() + 15) & ~size_t(15);
+                    params.resize(off + 2 * nbSym);
+                    std::memcpy(params.data() + off, norm, 2 * nbSym);
+                    O.w = 2; O.n = nbSym;
+                    O.loc = L_PARAM;
+                    O.off = off;
+                    nodeU.dead = true; // executed here, on the host
+                    break;
+                }
+                case T_FSE: {
+                    PlanStream& N = in(0);
+                    if (N.w != 2) { err = "FSE counts width"; return E_CORRUPT; }
+                    if (N.loc != L_PARAM) { err = "FSE counts not from an ncount stream"; return E_LIMIT; }
+                    if (N.n < 2 || N.n > 256) { err = "FSE symbol count"; return E_CORRUPT; }
+                    const int16_t* norm = reinterpret_cast<const int16_t*>(params.data() + N.off);
+                    unsigned sum = 0;
+                    for (uint64_t i = 0; i < N.n; i++) {
+                        if (norm[i] < -1) { err = "FSE counts"; return E_CORRUPT; }
+                        sum += norm[i] == -1 ? 1u : unsigned(norm[i]);
+                    }
+                    if (sum == 0 || (sum & (sum - 1))) { err = "FSE counts sum"; return E_CORRUPT; }
+                    int tl = highbit32(sum);
+                    if (tl < 5 || tl > 12) { err = "FSE table log"; return E_CORRUPT; }
+                    if (hs < 2 || hs > 9 || (h[0] != 2 && h[0] != 4)) { err = "FSE header"; return E_CORRUPT; }
+                    uint64_t dstSize = readLEn(h + 1, hs - 1);
+                    if (dstSize < 2 || dstSize >= (1ull << 32)) { err = "FSE size"; return E_CORRUPT; }
+                    if (in(1).n >= (1ull << 32)) { err = "FSE stream size"; return E_LIMIT; }
+                    O.w = 1; O.n = dstSize;
+                    nodeU.nbBits = uint8_t(tl);
+                    break;
+                }
+                case T_HUF: {
+                    if (in(0).w != 1) { err = "Huffman weights width"; return E_CORRUPT; }
+                    if (in(0).n < 2 || in(0).n > 256) { err = "Huffman weights count"; return E_CORRUPT; }
+                    if (hs < 2 || hs > 9) { err = "Huffman header"; return E_CORRUPT; }
+                    uint64_t dstSize = readLEn(h + 1, hs - 1);
+                    if (dstSize < 2 || dstSize >= (1ull << 32)) { err = "Huffman size"; return E_CORRUPT; }
+                    if (in(1).n >= (1ull << 32)) { err = "Huffman stream size"; return E_LIMIT; }
+                    O.w = 1; O.n = dstSize;
+                    break;
+                }
+                default:
+                    err = "unsupported codec";
+                    return E_TRANSFORM;
+            }
+            nodes.push_back(std::move(nodeU));
+            sidx += nbIn;
+        }
+    }
+
+    // ---- outputs --------------------------------------------------------
+    PlanStream& OUT = S(total - 1);
+    if (OUT.type == 0) { err = "output not regenerated"; return E_CORRUPT; }
+    frames[f].outWidth = OUT.w;
+    frames[f].outType = OUT.type;
+    *outBytes = OUT.bytes();
+
+    // ---- fusion of numeric chains (delta <- zigzag <- view <- tsplit|bitpack)
+    auto isNumView = [&](const PlanNode& nd_) {
+        return !nd_.dead && signature(nd_.id).view;
+    };
+    for (int u = nBase; u < int(nodes.size()); u++) {
+        PlanNode& C = nodes[u];
+        if (C.dead) continue;
+        if (C.id != T_DELTA && C.id != T_ZIGZAG && C.id != T_TSPLIT && C.id != T_BITPACK_INT
+            && C.id != T_BITPACK_SERIAL)
+            continue;
+        uint32_t const w = streams[C.out].w;
+        if (C.id == T_TSPLIT) {
+            if (w == 1 || w == 2 || w == 4 || w == 8) C.srcMode = SRC_PLANES;
+            continue; // general widths use the transpose kernel
+        }
+        if (C.id == T_BITPACK_INT || C.id == T_BITPACK_SERIAL) {
+            C.srcMode = SRC_BITPACK;
+            continue;
+        }
+        int cur = C.ins[0];
+        if (C.id == T_DELTA) {
+            C.delta = 1;
+            int p = streams[cur].producer;
+            if (p >= 0 && !nodes[p].dead && nodes[p].id == T_ZIGZAG) {
+                C.zigzag = 1;
+                nodes[p].dead = true;
+                cur = nodes[p].ins[0];
+            }
+        } else {
+            C.zigzag = 1;
+        }
+        int p = streams[cur].producer;
+        std::vector<int> views;
+        while (p >= 0 && isNumView(nodes[p])) {
+            views.push_back(p);
+            cur = nodes[p].ins[0];
+            p = streams[cur].producer;
+        }
+        if (p >= 0 && !nodes[p].dead && nodes[p].id == T_TSPLIT && nodes[p].ins.size() == w) {
+            C.srcMode = SRC_PLANES;
+            C.ins = nodes[p].ins;
+            nodes[p].dead = true;
+            for (int v : views) nodes[v].dead = true;
+        } else if (p >= 0 && !nodes[p].dead && (nodes[p].id == T_BITPACK_INT || nodes[p].id == T_BITPACK_SERIAL)
+                   && streams[nodes[p].out].w == w) {
+            C.srcMode = SRC_BITPACK;
+            C.nbBits = nodes[p].nbBits;
+            C.ins = nodes[p].ins;
+            nodes[p].dead = true;
+            for (int v : views) nodes[v].dead = true;
+        } else {
+            C.srcMode = SRC_PLAIN;
+            if (!views.empty()) {
+                // read through the views directly
+                C.ins = { cur };
+                for (int v : views) nodes[v].dead = true;
+            }
+        }
+    }
+
+    // ---- placement (reverse decoder order) ------------------------------
+    OUT.loc = L_OUT;
+    OUT.frame = f;
+    OUT.off = outOffset;
+    auto alloc = [&](PlanStream& s) {
+        s.loc = L_ARENA;
+        s.off = arenaBytes;
+        arenaBytes += (s.bytes() + 63) & ~uint64_t(63);
+    };
+    for (int u = int(nodes.size()) - 1; u >= nBase; u--) {
+        PlanNode& nd_ = nodes[u];
+        if (nd_.dead) continue;
+        Sig const sg = signature(nd_.id);
+        PlanStream& O = streams[nd_.out];
+        if (sg.view) {
+            PlanStream& I = streams[nd_.ins[0]];
+            if (O.loc == L_NONE) {
+                O.loc = L_ALIAS;
+                O.parent = nd_.ins[0];
+            } else if (I.loc == L_NONE && I.producer >= 0) {
+                I.loc = L_SUB;
+                I.parent = nd_.out;
+                I.off = 0;
+            }
+            // else: stored input into a placed output -> copy task (emitted later)
+            continue;
+        }
+        if (O.loc == L_NONE) alloc(O);
+        if (sg.concat) {
+            uint64_t off = 0;
+            for (int s : nd_.ins) {
+                PlanStream& I = streams[s];
+                if (I.loc == L_NONE && I.producer >= 0) {
+                    I.loc = L_SUB;
+                    I.parent = nd_.out;
+                    I.off = off;
+                }
+                off += I.bytes();
+            }
+        }
+    }
+    *consumed = pos - start;
+    if (hasContentCk && ckContent)
+        hashes.push_back(PlanHash{ f, true, outOffset, *outBytes, contentCk, 14, false });
+    return 0;
+}
+
+} // namespace ozl
+
+// ---------------------------------------------------------------------------
+// Layout: dependency levels, copy tasks, per-(level, kind) task arrays with
+// absolute device addresses. Called once with null bases to size the pools,
+// then again with the real allocations.
+namespace ozl {
+
+namespace {
+
+struct Pool {
+    std::vector<uint8_t> bytes;
+    template <class T>
+    size_t put(const std::vector<T>& v)
+    {
+        size_t off = (bytes.size() + 63) & ~size_t(63);
+        bytes.resize(off + v.size() * sizeof(T));
+        if (!v.empty()) std::memcpy(bytes.data() + off, v.data(), v.size() * sizeof(T));
+        return off;
+    }
+};
+
+struct Buckets {
+    std::vector<NumPipeTask> num;
+    std::vector<TransposeTask> tr;
+    std::vector<CopyTask> copy;
+    std::vector<ConstTask> cst;
+    std::vector<FseTask> fse;
+    std::vector<HufTask> huf;
+    std::vector<TokenizeTask> tok;
+    std::vector<FloatDecTask> flt;
+    std::vector<FlatpackTask> flat;
+};
+
+uint32_t ceilDiv(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }
+
+} // namespace
+
+int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* const* dOuts,
+               uint8_t* dArena, uint8_t* dParams, uint8_t* dScratch, uint8_t* dPool,
+               DeviceLayout& out, std::string& err)
+{
+    const auto& streams = plan.streams;
+    const auto& nodes = plan.nodes;
+    std::vector<uint8_t*> addrMemo(streams.size(), nullptr);
+    std::vector<char> addrDone(streams.size(), 0);
+    // Resolves a stream's device address (recursion depth is bounded by the
+    // placement chain length, which is at most the graph depth).
+    std::function<uint8_t*(int)> addr = [&](int s) -> uint8_t* {
+        if (addrDone[s]) return addrMemo[s];
+        const PlanStream& S = streams[s];
+        uint8_t* a = nullptr;
+        switch (S.loc) {
+            case L_FRAME: a = const_cast<uint8_t*>(dFrames[S.frame]) + S.off; break;
+            case L_OUT: a = dOuts[S.frame] + S.off; break;
+            case L_ARENA: a = dArena + S.off; break;
+            case L_PARAM: a = dParams + S.off; break;
+            case L_SUB: a = addr(S.parent) + S.off; break;
+            case L_ALIAS: a = addr(S.parent); break;
+            default: a = nullptr;
+        }
+        addrMemo[s] = a;
+        addrDone[s] = 1;
+        return a;
+    };
+
+    // ---- levels ------------------------------------------------------------
+    std::vector<int> level(nodes.size(), 0);
+    auto streamLevel = [&](int s) {
+        int p = streams[s].producer;
+        return (p >= 0 && !nodes[p].dead) ? level[p] : 0;
+    };
+    struct CopyReq { int src, dst; uint64_t dstOff; int level; };
+    std::vector<CopyReq> copies;
+    int maxLevel = 0;
+    for (size_t u = 0; u < nodes.size(); u++) {
+        const PlanNode& nd = nodes[u];
+        if (nd.dead) continue;
+        int lv = 0;
+        const PlanStream& O = streams[nd.out];
+        bool const isView = nd.id == 5 || nd.id == 6 || nd.id == 7 || nd.id == 8 || nd.id == 9 || nd.id == 10;
+        bool const isConcat = nd.id == 40 || nd.id == 47 || nd.id == 48;
+        if (isView) {
+            int const I = nd.ins[0];
+            const PlanStream& IS = streams[I];
+            if (O.loc == L_ALIAS || (IS.loc == L_SUB && IS.parent == nd.out)) {
+                lv = streamLevel(I);
+            } else {
+                lv = streamLevel(I) + 1;
+                copies.push_back(CopyReq{ I, nd.out, 0, lv });
+            }
+        } else if (isConcat) {
+            uint64_t off = 0;
+            for (int I : nd.ins) {
+                const PlanStream& IS = streams[I];
+                if (IS.loc == L_SUB && IS.parent == nd.out) {
+                    lv = std::max(lv, streamLevel(I));
+                } else {
+                    int const cl = streamLevel(I) + 1;
+                    copies.push_back(CopyReq{ I, nd.out, off, cl });
+                    lv = std::max(lv, cl);
+                }
+                off += IS.bytes();
+            }
+        } else {
+            for (int I : nd.ins) lv = std::max(lv, streamLevel(I));
+            lv += 1;
+        }
+        level[u] = lv;
+        maxLevel = std::max(maxLevel, lv);
+    }
+    int const hashLevel = maxLevel + 1;
+
+    // ---- tasks per level ---------------------------------------------------
+    std::vector<Buckets> B(size_t(hashLevel) + 1);
+    for (const CopyReq& c : copies) {
+        uint64_t bytes = streams[c.src].bytes();
+        if (!bytes) continue;
+        CopyTask t{ addr(c.dst) + c.dstOff, addr(c.src), bytes, 0 };
+        B[c.level].copy.push_back(t);
+    }
+    // pointer arrays (planes) live in the pool; collect them first
+    std::vector<const uint8_t*> ptrs;
+    std::vector<std::pair<size_t, size_t>> ptrFix; // (bucket task index marker) unused
+    struct PendingPlanes { int lvl; bool isNum; size_t taskIdx; size_t ptrOff; };
+    std::vector<PendingPlanes> pend;
+    for (size_t u = 0; u < nodes.size(); u++) {
+        const PlanNode& nd = nodes[u];
+        if (nd.dead) continue;
+        int const lv = level[u];
+        const PlanStream& O = streams[nd.out];
+        uint8_t* o = addr(nd.out);
+        auto in = [&](int k) { return addr(nd.ins[k]); };
+        switch (nd.id) {
+            case 1: case 3: case 4: case 27: case 28: {
+                if (nd.id == 4 && nd.srcMode != SRC_PLANES) {
+                    TransposeTask t{ o, nullptr, O.n, O.w, 0 };
+                    pend.push_back(PendingPlanes{ lv, false, B[lv].tr.size(), ptrs.size() });
+                    for (int s : nd.ins) ptrs.push_back(addr(s));
+                    B[lv].tr.push_back(t);
+                    break;
+                }
+                NumPipeTask t{};
+                t.out = o;
+                t.n = O.n;
+                t.w = O.w;
+                t.srcMode = nd.srcMode;
+                t.nbBits = nd.nbBits;
+                t.zigzag = nd.zigzag;
+                t.delta = nd.delta;
+                if (nd.delta && O.n) {
+                    uint64_t first = 0;
+                    for (size_t b = 0; b < nd.hsz; b++) first |= uint64_t(nd.hdr[b]) << (8 * b);
+                    t.first = first;
+                }
+                if (nd.srcMode == SRC_PLANES) {
+                    pend.push_back(PendingPlanes{ lv, true, B[lv].num.size(), ptrs.size() });
+                    for (int s : nd.ins) ptrs.push_back(addr(s));
+                } else {
+                    t.src = in(0);
+                }
+                if (O.n) B[lv].num.push_back(t);
+                break;
+            }
+            case 5: case 6: case 7: case 8: case 9: case 10: case 40: case 47: case 48:
+                break; // views and concatenations: placement or copy tasks
+            case 29: {
+                FlatpackTask t{ o, in(0), in(1), O.n, uint32_t(streams[nd.ins[0]].n), nd.nbBits, 0 };
+                if (O.n) B[lv].flat.push_back(t);
+                break;
+            }
+            case 33: {
+                FloatDecTask t{ o, in(0), in(1), O.n, nd.hdr[0], 0 };
+                if (O.n) B[lv].flt.push_back(t);
+                break;
+            }
+            case 36: case 37: {
+                TokenizeTask t{ o, in(0), in(1), O.n, uint32_t(streams[nd.ins[0]].n), streams[nd.ins[0]].w,
+                                streams[nd.ins[1]].w, 0 };
+                if (O.n) B[lv].tok.push_back(t);
+                break;
+            }
+            case 44: case 45: {
+                ConstTask t{ o, in(0), O.n, O.w, 0 };
+                B[lv].cst.push_back(t);
+                break;
+            }
+            case 49: {
+                FseTask t{};
+                t.out = o;
+                t.bits = in(1);
+                t.norm = reinterpret_cast<const int16_t*>(in(0));
+                t.bitsSize = uint32_t(streams[nd.ins[1]].n);
+                t.dstSize = uint32_t(O.n);
+                t.nbSym = uint16_t(streams[nd.ins[0]].n);
+                t.nbStates = nd.hdr[0];
+                t.tableLog = nd.nbBits;
+                B[lv].fse.push_back(t);
+                break;
+            }
+            case 50: {
+                HufTask t{};
+                t.out = o;
+                t.bits = in(1);
+                t.weights = in(0);
+                t.bitsSize = uint32_t(streams[nd.ins[1]].n);
+                t.dstSize = uint32_t(O.n);
+                t.nbWeights = uint16_t(streams[nd.ins[0]].n);
+                t.x4 = nd.hdr[0] & 1;
+                B[lv].huf.push_back(t);
+                break;
+            }
+            default:
+                err = "layout: unexpected codec " + std::to_string(nd.id);
+                return 32;
+        }
+    }
+
+    // ---- pool assembly -----------------------------------------------------
+    Pool pool;
+    size_t const ptrOff = pool.put(ptrs);
+    for (const PendingPlanes& p : pend) {
+        auto* arr = reinterpret_cast<const uint8_t* const*>(dPool + ptrOff) + p.ptrOff;
+        if (p.isNum) B[p.lvl].num[p.taskIdx].planes = arr;
+        else B[p.lvl].tr[p.taskIdx].planes = arr;
+    }
+    out.launches.clear();
+    uint64_t scratch = 0;
+    auto addTiled = [&](int kind, int lv, auto& tasks, auto tilesOf) {
+        if (tasks.empty()) return;
+        std::vector<TileRef> tiles;
+        for (size_t i = 0; i < tasks.size(); i++) {
+            uint32_t nt = tilesOf(tasks[i]);
+            tasks[i].tileBase = uint32_t(tiles.size());
+            for (uint32_t k = 0; k < nt; k++) tiles.push_back(TileRef{ uint32_t(i), k });
+        }
+        Launch L{};
+        L.kind = kind;
+        L.level = lv;
+        L.taskOff = pool.put(tasks);
+        L.nbTasks = uint32_t(tasks.size());
+        L.tileOff = pool.put(tiles);
+        L.nbTiles = uint32_t(tiles.size());
+        if (kind == KIND_NUMPIPE) {
+            bool anyDelta = false;
+            for (auto& t : tasks) anyDelta |= reinterpret_cast<const NumPipeTask&>(t).delta != 0;
+            if (anyDelta) {
+                L.needsScan = true;
+                L.statusOff = scratch;
+                L.statusBytes = 64 + 16 * uint64_t(tiles.size());
+                scratch += (L.statusBytes + 255) & ~uint64_t(255);
+            }
+        }
+        out.launches.push_back(L);
+    };
+    auto addPlain = [&](int kind, int lv, auto& tasks) {
+        if (tasks.empty()) return;
+        Launch L{};
+        if constexpr (std::is_same_v<std::decay_t<decltype(tasks[0])>, FseTask>) {
+            // similar chunks side by side: largest tables first, then by length
+            std::sort(tasks.begin(), tasks.end(), [](const FseTask& a, const FseTask& b) {
+                return a.tableLog != b.tableLog ? a.tableLog > b.tableLog : a.dstSize > b.dstSize;
+            });
+            uint32_t tlMax = 5;
+            for (auto& t : tasks) tlMax = std::max<uint32_t>(tlMax, t.tableLog);
+            L.param0 = tlMax;
+        }
+        L.kind = kind;
+        L.level = lv;
+        L.taskOff = pool.put(tasks);
+        L.nbTasks = uint32_t(tasks.size());
+        out.launches.push_back(L);
+    };
+    for (int lv = 0; lv <= maxLevel; lv++) {
+        Buckets& b = B[lv];
+        addTiled(KIND_COPY, lv, b.copy, [](const CopyTask& t) { return ceilDiv(t.bytes, kTileBytes); });
+        addTiled(KIND_CONST, lv, b.cst, [](const ConstTask& t) { return ceilDiv(t.n * t.w, kTileBytes); });
+        addPlain(KIND_FSE, lv, b.fse);
+        addPlain(KIND_HUF, lv, b.huf);
+        addTiled(KIND_FLATPACK, lv, b.flat, [](const FlatpackTask& t) { return ceilDiv(t.n, kTileBytes); });
+        addTiled(KIND_TOKENIZE, lv, b.tok, [](const TokenizeTask& t) { return ceilDiv(t.n, kTileElems); });
+        addTiled(KIND_FLOATDEC, lv, b.flt, [](const FloatDecTask& t) { return ceilDiv(t.n, kTileElems); });
+        addTiled(KIND_TRANSPOSE, lv, b.tr, [](const TransposeTask& t) { return ceilDiv(t.n, kTileElems); });
+        addTiled(KIND_NUMPIPE, lv, b.num, [](const NumPipeTask& t) { return ceilDiv(t.n, kTileElems); });
+    }
+    // checksums: one launch after everything else
+    if (!plan.hashes.empty()) {
+        std::vector<HashTask> ht;
+        std::vector<TileRef> blocks;
+        for (const PlanHash& h : plan.hashes) {
+            HashTask t{};
+            t.data = h.inOutput ? dOuts[h.frame] + h.off : dFrames[h.frame] + h.off;
+            t.len = h.len;
+            t.expected = h.expected;
+            t.errCode = h.err;
+            t.low8 = h.low8 ? 1 : 0;
+            t.aligned8 = (reinterpret_cast<uintptr_t>(t.data) & 7) == 0;
+            t.nbBlocks = h.len > 240 ? uint32_t((h.len - 1) / kHashBlock) : 0;
+            t.blockBase = uint32_t(blocks.size());
+            for (uint32_t k = 0; k < t.nbBlocks; k++) blocks.push_back(TileRef{ uint32_t(ht.size()), k });
+            ht.push_back(t);
+        }
+        uint64_t const sumsOff = scratch;
+        scratch += ((uint64_t)blocks.size() * 64 + 255) & ~uint64_t(255);
+        for (HashTask& t : ht) t.blockSums = reinterpret_cast<uint64_t*>(dScratch + sumsOff) + 8ull * t.blockBase;
+        Launch L{};
+        L.kind = KIND_HASH;
+        L.level = hashLevel;
+        L.taskOff = pool.put(ht);
+        L.nbTasks = uint32_t(ht.size());
+        L.tileOff = pool.put(blocks);
+        L.nbTiles = uint32_t(blocks.size());
+        out.launches.push_back(L);
+    }
+    out.pool = std::move(pool.bytes);
+    out.arenaBytes = plan.arenaBytes;
+    out.scratchBytes = scratch;
+    out.paramBytes = plan.params.size();
+    return 0;
+}
+
+} // namespace ozl

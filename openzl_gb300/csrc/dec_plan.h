@@ -1,0 +1,121 @@
+// Host-side decode planner: turns OpenZL frames into device task lists.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "dec_tasks.h"
+
+namespace ozl {
+
+// Kernel families, in the order they launch within one dependency level.
+enum Kind : int {
+    KIND_COPY = 0,
+    KIND_CONST,
+    KIND_FSE,
+    KIND_HUF,
+    KIND_FLATPACK,
+    KIND_TOKENIZE,
+    KIND_FLOATDEC,
+    KIND_TRANSPOSE,
+    KIND_NUMPIPE,
+    KIND_HASH,
+    KIND_COUNT
+};
+
+struct Launch {
+    int kind;
+    int level;
+    size_t taskOff;   // byte offset of the task array in the descriptor pool
+    uint32_t nbTasks;
+    size_t tileOff;   // byte offset of the TileRef array (tiled kinds)
+    uint32_t nbTiles;
+    size_t statusOff; // scratch offset of look-back status (NUMPIPE with delta)
+    size_t statusBytes;
+    bool needsScan;
+    uint32_t param0;  // kind-specific launch shape (FSE: max table log)
+};
+
+// Where a stream's bytes live.
+enum LocKind : int { L_NONE = 0, L_FRAME, L_ARENA, L_OUT, L_PARAM, L_SUB, L_ALIAS };
+
+struct PlanStream {
+    int type = 0;
+    uint32_t w = 1;
+    uint64_t n = 0;
+    int producer = -1; // node index, -1 = stored
+    int loc = L_NONE;
+    int frame = -1;    // for L_FRAME / L_OUT
+    int parent = -1;   // for L_SUB / L_ALIAS
+    uint64_t off = 0;  // offset within the location
+    uint64_t bytes() const { return n * w; }
+};
+
+struct PlanNode {
+    uint32_t id = 0;          // standard transform ID
+    int frame = -1;
+    const uint8_t* hdr = nullptr;
+    size_t hsz = 0;
+    std::vector<int> ins;     // streams, in the decoder's own input order
+    int out = -1;
+    bool dead = false;        // absorbed by a fused consumer, or a no-op view
+    int level = 0;
+    // fused numeric pipeline parameters
+    uint8_t srcMode = SRC_PLAIN, nbBits = 0, zigzag = 0, delta = 0;
+};
+
+struct PlanHash {
+    int frame;
+    bool inOutput;      // content checksum (output region) vs compressed (frame region)
+    uint64_t off, len;
+    uint32_t expected;
+    uint32_t err;
+    bool low8;          // frame-header checksum: compare the low 8 bits only
+};
+
+struct FramePlan {
+    uint64_t decodedSize = 0;
+    uint64_t frameBytes = 0;  // compressed size including the end-of-frame byte
+    int outType = 0;
+    uint32_t outWidth = 1;
+};
+
+class DecodePlan {
+  public:
+    // Parses and plans. Returns 0 or a ZL error code; `err` gets a message.
+    int build(size_t nbFrames, const uint8_t* const* hFrames, const size_t* frameSizes,
+              const size_t* dstCapacities, bool checkContent, bool checkCompressed,
+              std::string& err);
+
+    std::vector<FramePlan> frames;
+    std::vector<PlanStream> streams;
+    std::vector<PlanNode> nodes;
+    std::vector<PlanHash> hashes;
+    std::vector<uint8_t> params;  // host-decoded small streams (FSE normalized counts)
+    uint64_t arenaBytes = 0;
+    uint64_t totalOut = 0;
+
+  private:
+    int planFrame(int f, const uint8_t* src, size_t size, size_t dstCap, bool ckContent,
+                  bool ckCompressed, std::string& err);
+    int planBlock(int f, const uint8_t* src, size_t size, size_t start, size_t* consumed,
+                  bool hasContentCk, bool hasCompressedCk, bool ckContent, bool ckCompressed,
+                  size_t nbOutputs, uint64_t outOffset, uint64_t* outBytes, std::string& err);
+};
+
+// Resolved, device-ready plan: task pools and launch list.
+struct DeviceLayout {
+    std::vector<uint8_t> pool;     // task descriptors, tile lists, pointer arrays
+    std::vector<Launch> launches;
+    uint64_t arenaBytes = 0;       // intermediate streams
+    uint64_t scratchBytes = 0;     // look-back status + hash block sums
+    uint64_t paramBytes = 0;
+};
+
+// Produces task descriptors with absolute device addresses.
+int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* const* dOuts,
+               uint8_t* dArena, uint8_t* dParams, uint8_t* dScratch, uint8_t* dPool,
+               DeviceLayout& out, std::string& err);
+
+} // namespace ozl

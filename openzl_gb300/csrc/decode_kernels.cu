@@ -1,0 +1,904 @@
+// sm_103a decode kernels for OpenZL's numeric codec graph.
+//
+// All work here is integer and HBM/latency bound: no tensor cores. Each
+// kernel takes a task array plus, for data-parallel kinds, a tile list; the
+// host planner (dec_plan.cpp) builds both. Kernels never trap: malformed
+// input sets the batch status word (first error wins) and the kernel moves
+// on. Every spin-wait is bounded.
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "dec_tasks.h"
+#include "dec_exec.h"
+
+namespace ozl {
+
+// ---------------------------------------------------------------------------
+// helpers
+
+__device__ __forceinline__ void reportError(uint32_t* status, uint32_t code)
+{
+    atomicCAS(status, 0u, code);
+}
+
+// 8 bytes from any address inside a buffer that this library allocated with
+// at least 16 bytes of slack on both sides of every stream it reads this way.
+__device__ __forceinline__ uint64_t ld64Any(const uint8_t* p)
+{
+    uintptr_t const a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(7);
+    unsigned const s = unsigned(reinterpret_cast<uintptr_t>(p) - a) * 8u;
+    uint64_t const lo = *reinterpret_cast<const uint64_t*>(a);
+    if (s == 0) return lo;
+    uint64_t const hi = *reinterpret_cast<const uint64_t*>(a + 8);
+    return (lo >> s) | (hi << (64u - s));
+}
+
+__device__ __forceinline__ uint64_t ldElem(const uint8_t* p, uint32_t w)
+{
+    switch (w) {
+        case 1: return *p;
+        case 2: return (reinterpret_cast<uintptr_t>(p) & 1) ? (uint64_t(p[0]) | (uint64_t(p[1]) << 8))
+                                                           : *reinterpret_cast<const uint16_t*>(p);
+        case 4:
+            if (!(reinterpret_cast<uintptr_t>(p) & 3)) return *reinterpret_cast<const uint32_t*>(p);
+            return uint64_t(p[0]) | (uint64_t(p[1]) << 8) | (uint64_t(p[2]) << 16) | (uint64_t(p[3]) << 24);
+        default:
+            if (!(reinterpret_cast<uintptr_t>(p) & 7)) return *reinterpret_cast<const uint64_t*>(p);
+            {
+                uint64_t v = 0;
+                for (int b = 0; b < 8; b++) v |= uint64_t(p[b]) << (8 * b);
+                return v;
+            }
+    }
+}
+
+__device__ __forceinline__ void stElem(uint8_t* p, uint64_t v, uint32_t w)
+{
+    switch (w) {
+        case 1: *p = uint8_t(v); break;
+        case 2:
+            if (!(reinterpret_cast<uintptr_t>(p) & 1)) *reinterpret_cast<uint16_t*>(p) = uint16_t(v);
+            else { p[0] = uint8_t(v); p[1] = uint8_t(v >> 8); }
+            break;
+        case 4:
+            if (!(reinterpret_cast<uintptr_t>(p) & 3)) *reinterpret_cast<uint32_t*>(p) = uint32_t(v);
+            else for (int b = 0; b < 4; b++) p[b] = uint8_t(v >> (8 * b));
+            break;
+        default:
+            if (!(reinterpret_cast<uintptr_t>(p) & 7)) *reinterpret_cast<uint64_t*>(p) = v;
+            else for (int b = 0; b < 8; b++) p[b] = uint8_t(v >> (8 * b));
+    }
+}
+
+__device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
+
+__device__ __forceinline__ uint64_t widthMask(uint32_t w)
+{
+    return w >= 8 ? ~0ull : ((1ull << (8 * w)) - 1);
+}
+
+// ---------------------------------------------------------------------------
+// copy / constant: tiles of kTileBytes output bytes
+
+__global__ void kCopy(const CopyTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    CopyTask const t = tasks[tr.task];
+    uint64_t const b0 = uint64_t(tr.tile) * kTileBytes;
+    uint64_t const b1 = min(t.bytes, b0 + kTileBytes);
+    bool const vec = !((reinterpret_cast<uintptr_t>(t.dst + b0) | reinterpret_cast<uintptr_t>(t.src + b0)) & 15);
+    if (vec) {
+        uint64_t const nv = (b1 - b0) / 16;
+        const uint4* s = reinterpret_cast<const uint4*>(t.src + b0);
+        uint4* d = reinterpret_cast<uint4*>(t.dst + b0);
+        for (uint64_t i = threadIdx.x; i < nv; i += blockDim.x) d[i] = s[i];
+        for (uint64_t i = b0 + nv * 16 + threadIdx.x; i < b1; i += blockDim.x) t.dst[i] = t.src[i];
+    } else {
+        for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) t.dst[i] = t.src[i];
+    }
+}
+
+__global__ void kConst(const ConstTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    ConstTask const t = tasks[tr.task];
+    uint64_t const total = t.n * t.w;
+    uint64_t const b0 = uint64_t(tr.tile) * kTileBytes;
+    uint64_t const b1 = min(total, b0 + kTileBytes);
+    if (t.w == 1) {
+        uint8_t const v = t.value[0];
+        uint32_t const v4 = v * 0x01010101u;
+        // head bytes up to 16-byte alignment, then 16-byte stores
+        uint64_t a = b0;
+        uintptr_t const base = reinterpret_cast<uintptr_t>(t.out);
+        uint64_t const alignStart = min(b1, (((base + b0 + 15) & ~uintptr_t(15)) - base));
+        for (uint64_t i = a + threadIdx.x; i < alignStart; i += blockDim.x) t.out[i] = v;
+        a = alignStart;
+        uint64_t const nv = (b1 - a) / 16;
+        uint4 const q = make_uint4(v4, v4, v4, v4);
+        uint4* d = reinterpret_cast<uint4*>(t.out + a);
+        for (uint64_t i = threadIdx.x; i < nv; i += blockDim.x) d[i] = q;
+        for (uint64_t i = a + nv * 16 + threadIdx.x; i < b1; i += blockDim.x) t.out[i] = v;
+    } else {
+        for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) t.out[i] = t.value[i % t.w];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused numeric pipeline with decoupled look-back prefix sum.
+//
+// Tile = kTileElems output elements, 256 threads, 32 elements per thread.
+// y[0] = first value, y[i] = source[i-1] for delta tasks; out = inclusive
+// prefix sum of y modulo 2^(8w). Non-delta tasks write y directly.
+
+constexpr int kNPThreads = 256;
+constexpr int kNPPer = kTileElems / kNPThreads; // 32
+
+__device__ __forceinline__ uint64_t fetchSource(const NumPipeTask& t, uint64_t j)
+{
+    switch (t.srcMode) {
+        case SRC_PLAIN: return ldElem(t.src + j * t.w, t.w);
+        case SRC_PLANES: {
+            uint64_t v = 0;
+            for (uint32_t b = 0; b < t.w; b++) v |= uint64_t(t.planes[b][j]) << (8 * b);
+            return v;
+        }
+        default: {
+            uint64_t const bit = j * t.nbBits;
+            const uint8_t* p = t.src + (bit >> 3);
+            unsigned const sh = unsigned(bit & 7);
+            uintptr_t const a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(7);
+            unsigned const s = unsigned(reinterpret_cast<uintptr_t>(p) - a) * 8u + sh; // < 64
+            uint64_t const lo = *reinterpret_cast<const uint64_t*>(a);
+            uint64_t const hi = *reinterpret_cast<const uint64_t*>(a + 8);
+            uint64_t v = s ? ((lo >> s) | (hi << (64u - s))) : lo;
+            if (t.nbBits < 64) v &= (1ull << t.nbBits) - 1;
+            return v;
+        }
+    }
+}
+
+// Look-back status per tile: word 0 = flag (0 none, 1 aggregate, 2 prefix), word 1 = value.
+__device__ __forceinline__ void publish(unsigned long long* st, uint32_t tile, uint64_t value, uint64_t flag)
+{
+    volatile unsigned long long* s = st + 2 * tile;
+    s[1] = value;
+    __threadfence();
+    s[0] = flag;
+}
+
+__global__ void __launch_bounds__(kNPThreads) kNumPipe(const NumPipeTask* __restrict__ tasks,
+                                                       const TileRef* __restrict__ tiles,
+                                                       unsigned long long* __restrict__ scan,
+                                                       uint32_t* __restrict__ status)
+{
+    __shared__ uint64_t sv[kTileElems + kTileElems / 32];
+    __shared__ uint64_t warpTot[kNPThreads / 32];
+    __shared__ uint32_t sTile;
+    __shared__ uint64_t sPrefix;
+    uint32_t tileIdx;
+    if (scan) {
+        // dynamic tile order: a tile only waits on tiles acquired before it
+        if (threadIdx.x == 0) sTile = atomicAdd(reinterpret_cast<unsigned int*>(scan), 1u);
+        __syncthreads();
+        tileIdx = sTile;
+    } else {
+        tileIdx = blockIdx.x;
+    }
+    TileRef const tr = tiles[tileIdx];
+    NumPipeTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kTileElems;
+    uint32_t const cnt = uint32_t(umin64(kTileElems, t.n - e0));
+    uint64_t const mask = widthMask(t.w);
+    auto sidx = [](uint32_t i) { return i + (i >> 5); };
+
+    // 1. striped, coalesced source reads -> shared memory
+    for (uint32_t k = threadIdx.x; k < cnt; k += kNPThreads) {
+        uint64_t const i = e0 + k;
+        uint64_t y;
+        if (t.delta && i == 0) {
+            y = t.first;
+        } else {
+            uint64_t const j = t.delta ? i - 1 : i;
+            y = fetchSource(t, j);
+            if (t.zigzag) y = (y >> 1) ^ (0 - (y & 1));
+        }
+        sv[sidx(k)] = y & mask;
+    }
+    __syncthreads();
+
+    if (t.delta) {
+        // 2. per-thread serial scan over a blocked segment of 32 elements
+        uint32_t const b = threadIdx.x * kNPPer;
+        uint64_t acc = 0;
+        for (int q = 0; q < kNPPer; q++) {
+            uint32_t const k = b + q;
+            if (k < cnt) {
+                acc += sv[sidx(k)];
+                sv[sidx(k)] = acc;
+            }
+        }
+        // 3. block exclusive scan of thread totals
+        uint64_t incl = acc;
+        unsigned const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t const v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= unsigned(o)) incl += v;
+        }
+        if (lane == 31) warpTot[wid] = incl;
+        __syncthreads();
+        uint64_t warpPre = 0, tileAgg = 0;
+        for (unsigned w2 = 0; w2 < kNPThreads / 32; w2++) {
+            if (w2 < wid) warpPre += warpTot[w2];
+            tileAgg += warpTot[w2];
+        }
+        uint64_t const threadPre = warpPre + incl - acc;
+        // 4. decoupled look-back across the task's tiles
+        if (threadIdx.x == 0) {
+            unsigned long long* st = scan + 8; // header: counter (+ padding)
+            uint64_t prefix = 0;
+            uint32_t const g = tileIdx;
+            if (tr.tile == 0) {
+                publish(st, g, tileAgg, 2);
+            } else {
+                publish(st, g, tileAgg, 1);
+                int64_t p = int64_t(g) - 1;
+                uint32_t spins = 0;
+                bool ok = true;
+                while (true) {
+                    volatile unsigned long long* s = st + 2 * p;
+                    unsigned long long f = s[0];
+                    if (f == 0) {
+                        if (++spins > (1u << 26)) { ok = false; break; }
+                        continue;
+                    }
+                    __threadfence();
+                    prefix += s[1];
+                    if (f == 2) break;
+                    p--;
+                }
+                if (!ok) reportError(status, DERR_TIMEOUT);
+                publish(st, g, prefix + tileAgg, 2);
+            }
+            sPrefix = prefix;
+        }
+        __syncthreads();
+        uint64_t const add = sPrefix + threadPre;
+        for (int q = 0; q < kNPPer; q++) {
+            uint32_t const k = b + q;
+            if (k < cnt) sv[sidx(k)] += add;
+        }
+        __syncthreads();
+    }
+
+    // 5. striped stores
+    uint8_t* const out = t.out + e0 * t.w;
+    if (t.w == 1) {
+        for (uint32_t k = threadIdx.x; k < cnt; k += kNPThreads) out[k] = uint8_t(sv[sidx(k)]);
+    } else {
+        for (uint32_t k = threadIdx.x; k < cnt; k += kNPThreads) stElem(out + uint64_t(k) * t.w, sv[sidx(k)], t.w);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// generic transpose (any width)
+__global__ void kTranspose(const TransposeTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    TransposeTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kTileElems;
+    uint64_t const e1 = umin64(t.n, e0 + kTileElems);
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x)
+        for (uint32_t b = 0; b < t.W; b++) t.out[i * t.W + b] = t.planes[b][i];
+}
+
+// ---------------------------------------------------------------------------
+// tokenize: dictionary gather out[i] = alphabet[idx[i]]
+__global__ void kTokenize(const TokenizeTask* __restrict__ tasks, const TileRef* __restrict__ tiles,
+                          uint32_t* __restrict__ status)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    TokenizeTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kTileElems;
+    uint64_t const e1 = umin64(t.n, e0 + kTileElems);
+    bool bad = false;
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+        uint64_t const k = ldElem(t.idx + i * t.iw, t.iw);
+        if (k >= t.alphabetSize) { bad = true; continue; }
+        if (t.w == 4 || t.w == 2 || t.w == 1 || t.w == 8) stElem(t.out + i * t.w, ldElem(t.alphabet + k * t.w, t.w), t.w);
+        else for (uint32_t b = 0; b < t.w; b++) t.out[i * t.w + b] = t.alphabet[k * t.w + b];
+    }
+    if (bad) reportError(status, DERR_CORRUPTION);
+}
+
+// ---------------------------------------------------------------------------
+// float deconstruct (decode_float_deconstruct_kernel.c semantics)
+__global__ void kFloatDec(const FloatDecTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    FloatDecTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kTileElems;
+    uint64_t const e1 = umin64(t.n, e0 + kTileElems);
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+        uint32_t const ex = t.exponent[i];
+        if (t.eltType == 1) {
+            uint32_t const s = t.signFrac[i];
+            stElem(t.out + 2 * i, uint16_t((s >> 1) | (s << 15) | (ex << 7)), 2);
+        } else if (t.eltType == 2) {
+            uint32_t const s = uint32_t(t.signFrac[2 * i]) | (uint32_t(t.signFrac[2 * i + 1]) << 8);
+            stElem(t.out + 2 * i, uint16_t((s >> 1) | (s << 15) | (ex << 10)), 2);
+        } else {
+            uint32_t const s = uint32_t(t.signFrac[3 * i]) | (uint32_t(t.signFrac[3 * i + 1]) << 8)
+                    | (uint32_t(t.signFrac[3 * i + 2]) << 16);
+            stElem(t.out + 4 * i, (ex << 23) | (s << 31) | (s >> 1), 4);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// flatpack: alphabet + LSB-first indices terminated by a 1 bit
+__global__ void kFlatpack(const FlatpackTask* __restrict__ tasks, const TileRef* __restrict__ tiles,
+                          uint32_t* __restrict__ status)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    FlatpackTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kTileBytes;
+    uint64_t const e1 = umin64(t.n, e0 + kTileBytes);
+    bool bad = false;
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+        uint64_t const bit = i * t.nbBits;
+        uint32_t v = uint32_t(ld64Any(t.packed + (bit >> 3)) >> (bit & 7)) & ((1u << t.nbBits) - 1);
+        if (v >= t.alphabetSize) { bad = true; v = 0; }
+        t.out[i] = t.alphabet[v];
+    }
+    if (tr.tile == 0 && threadIdx.x == 0) {
+        // terminator: the bit after the last index is set and is the last set bit
+        uint64_t const endBit = t.n * t.nbBits;
+        uint8_t const last = t.packed[endBit >> 3];
+        if (!((last >> (endBit & 7)) & 1) || (last >> (endBit & 7)) != 1) bad = true;
+    }
+    if (bad) reportError(status, DERR_CORRUPTION);
+}
+
+// ---------------------------------------------------------------------------
+// Backward bit reader (FSE / Huffman bitstreams): reads fields most
+// significant bit first from the end of the stream towards its start.
+struct BitRev {
+    const uint8_t* base;
+    int64_t pos;     // unread bits
+    int64_t cbase;   // bit index of cont's least significant bit
+    uint64_t cont;
+
+    __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size)
+    {
+        base = p;
+        if (size == 0) return false;
+        uint8_t const last = p[size - 1];
+        if (last == 0) return false;
+        pos = int64_t(size - 1) * 8 + (31 - __clz(uint32_t(last)));
+        refill();
+        return true;
+    }
+    __device__ __forceinline__ void refill()
+    {
+        int64_t b = ((pos + 7) >> 3) - 8;
+        if (b < 0) b = 0;
+        cbase = b * 8;
+        cont = ld64Any(base + b);
+    }
+    __device__ __forceinline__ uint32_t peek(unsigned nb) const
+    {
+        int64_t const sh = pos - int64_t(nb) - cbase;
+        uint64_t const v = sh >= 0 ? (cont >> sh) : (cont << (-sh));
+        return uint32_t(v) & ((1u << nb) - 1);
+    }
+    __device__ __forceinline__ void skip(unsigned nb)
+    {
+        pos -= nb;
+        if (pos - cbase < 32 && cbase > 0) refill();
+    }
+    __device__ __forceinline__ uint32_t read(unsigned nb)
+    {
+        uint32_t const v = peek(nb);
+        skip(nb);
+        return v;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// FSE: one lane per chunk, lane-private decoding table in shared memory.
+// Table entry: newState (16) | nbBits (8) | symbol (8).
+//
+// Table construction restates src/openzl/fse/decompress/fse_decompress.c:
+// 73-171; decode order restates fse_decompress.c:255-337 (state i % nbStates
+// emits symbol i; the last symbol of each state has no transition).
+__global__ void kFse(const FseTask* __restrict__ tasks, uint32_t nbTasks, uint32_t lanesPerCta,
+                     uint32_t tableLogMax, uint32_t* __restrict__ status)
+{
+    extern __shared__ uint32_t smemFse[];
+    uint32_t const lane = threadIdx.x;
+    uint32_t const ti = blockIdx.x * lanesPerCta + lane;
+    if (lane >= lanesPerCta || ti >= nbTasks) return;
+    FseTask const t = tasks[ti];
+    uint32_t* const dt = smemFse + (size_t(lane) << tableLogMax);
+    uint32_t const tl = t.tableLog;
+    uint32_t const size = 1u << tl, mask = size - 1;
+    uint32_t const step = (size >> 1) + (size >> 3) + 3;
+    uint32_t high = size - 1;
+    uint16_t next[256];
+    for (uint32_t s = 0; s < t.nbSym; s++) {
+        int16_t const c = t.norm[s];
+        if (c == -1) {
+            dt[high--] = s;
+            next[s] = 1;
+        } else {
+            next[s] = uint16_t(c);
+        }
+    }
+    uint32_t pos = 0;
+    for (uint32_t s = 0; s < t.nbSym; s++) {
+        int const c = t.norm[s];
+        for (int i = 0; i < c; i++) {
+            dt[pos] = s;
+            do { pos = (pos + step) & mask; } while (pos > high);
+        }
+    }
+    for (uint32_t u = 0; u < size; u++) {
+        uint32_t const s = dt[u] & 0xff;
+        uint32_t const x = next[s]++;
+        uint32_t const nb = tl - (31 - __clz(x));
+        uint32_t const ns = (x << nb) - size;
+        dt[u] = s | (nb << 8) | (ns << 16);
+    }
+
+    BitRev br;
+    if (!br.init(t.bits, t.bitsSize)) { reportError(status, DERR_CORRUPTION); return; }
+    uint32_t const nst = t.nbStates;
+    uint32_t st0 = br.read(tl), st1 = br.read(tl), st2 = 0, st3 = 0;
+    if (nst == 4) { st2 = br.read(tl); st3 = br.read(tl); }
+    uint32_t const n = t.dstSize;
+    uint32_t const lastTr = n - nst;
+    uint8_t* const out = t.out;
+    // Bytes are packed four at a time into aligned 32-bit stores; the
+    // unaligned head and the last partial word go out as single bytes.
+    uint32_t const head = uint32_t((4 - (reinterpret_cast<uintptr_t>(out) & 3)) & 3);
+    uint32_t const bodyEnd = n < head ? n : head + ((n - head) & ~3u);
+    uint32_t word = 0;
+    uint32_t i = 0;
+    auto emit = [&](uint32_t idx, uint32_t sym) {
+        if (idx < head || idx >= bodyEnd) {
+            out[idx] = uint8_t(sym);
+            return;
+        }
+        uint32_t const q = (idx - head) & 3;
+        word |= sym << (8 * q);
+        if (q == 3) {
+            *reinterpret_cast<uint32_t*>(out + idx - 3) = word;
+            word = 0;
+        }
+    };
+    if (nst == 4) {
+        for (; i + 4 <= lastTr; i += 4) {
+            uint32_t e;
+            e = dt[st0]; emit(i, e & 0xff); st0 = (e >> 16) + br.read((e >> 8) & 0xff);
+            e = dt[st1]; emit(i + 1, e & 0xff); st1 = (e >> 16) + br.read((e >> 8) & 0xff);
+            e = dt[st2]; emit(i + 2, e & 0xff); st2 = (e >> 16) + br.read((e >> 8) & 0xff);
+            e = dt[st3]; emit(i + 3, e & 0xff); st3 = (e >> 16) + br.read((e >> 8) & 0xff);
+        }
+    } else {
+        for (; i + 2 <= lastTr; i += 2) {
+            uint32_t e;
+            e = dt[st0]; emit(i, e & 0xff); st0 = (e >> 16) + br.read((e >> 8) & 0xff);
+            e = dt[st1]; emit(i + 1, e & 0xff); st1 = (e >> 16) + br.read((e >> 8) & 0xff);
+        }
+    }
+    for (; i < n; i++) {
+        uint32_t const k = i % nst;
+        uint32_t& s = k == 0 ? st0 : (k == 1 ? st1 : (k == 2 ? st2 : st3));
+        uint32_t const e = dt[s];
+        emit(i, e & 0xff);
+        if (i < lastTr) s = (e >> 16) + br.read((e >> 8) & 0xff);
+    }
+    if (br.pos != 0) reportError(status, DERR_CORRUPTION);
+}
+
+// ---------------------------------------------------------------------------
+// Huffman: weights -> canonical table (symbols ranked by weight then value;
+// weight w spans 2^(w-1) cells, nbBits = tableLog + 1 - w), after
+// src/openzl/fse/decompress/huf_decompress.c:342-454. One lane per stream;
+// the 4 streams of a 4X chunk share the chunk's table. Entry: symbol | nbBits<<8.
+constexpr uint32_t kHufTableLog = 12;
+
+__device__ bool hufBuild(uint16_t* dt, const uint8_t* weights, uint32_t nbW, uint32_t& tlOut)
+{
+    uint32_t counts[16];
+    for (int k = 0; k < 16; k++) counts[k] = 0;
+    uint32_t sum = 0;
+    for (uint32_t s = 0; s < nbW; s++) {
+        uint32_t const w = weights[s];
+        if (w > 12) return false;
+        counts[w]++;
+        sum += (1u << w) >> 1;
+    }
+    if (sum == 0 || (sum & (sum - 1))) return false;
+    uint32_t const tl = 31 - __clz(sum);
+    if (tl > 12 || nbW - counts[0] < 2) return false;
+    uint32_t start[16];
+    uint32_t p = 0;
+    for (uint32_t w = 1; w <= tl; w++) {
+        start[w] = p;
+        p += counts[w] << (w - 1);
+    }
+    for (uint32_t s = 0; s < nbW; s++) {
+        uint32_t const w = weights[s];
+        if (!w) continue;
+        uint32_t const len = 1u << (w - 1);
+        uint16_t const e = uint16_t(s | ((tl + 1 - w) << 8));
+        for (uint32_t u = 0; u < len; u++) dt[start[w] + u] = e;
+        start[w] += len;
+    }
+    tlOut = tl;
+    return true;
+}
+
+__global__ void kHuf(const HufTask* __restrict__ tasks, uint32_t nbTasks, uint32_t chunksPerCta,
+                     uint32_t* __restrict__ status)
+{
+    extern __shared__ uint16_t smemHuf[];
+    __shared__ uint32_t sTl[32];
+    __shared__ uint8_t sOk[32];
+    uint32_t const c = threadIdx.x >> 2;       // chunk slot in this CTA
+    uint32_t const sIdx = threadIdx.x & 3;     // stream within the chunk
+    uint32_t const ti = blockIdx.x * chunksPerCta + c;
+    bool const active = c < chunksPerCta && ti < nbTasks;
+    uint16_t* const dt = smemHuf + (size_t(c) << kHufTableLog);
+    HufTask t{};
+    if (active) {
+        t = tasks[ti];
+        if (sIdx == 0) {
+            uint32_t tl = 0;
+            sOk[c] = hufBuild(dt, t.weights, t.nbWeights, tl) ? 1 : 0;
+            sTl[c] = tl;
+        }
+    }
+    __syncthreads();
+    if (!active) return;
+    if (!sOk[c]) {
+        if (sIdx == 0) reportError(status, DERR_CORRUPTION);
+        return;
+    }
+    uint32_t const tl = sTl[c];
+    const uint8_t* sp;
+    uint32_t ssize, n, o0;
+    if (t.x4) {
+        if (t.bitsSize < 10) { if (sIdx == 0) reportError(status, DERR_CORRUPTION); return; }
+        uint32_t const l1 = t.bits[0] | (t.bits[1] << 8);
+        uint32_t const l2 = t.bits[2] | (t.bits[3] << 8);
+        uint32_t const l3 = t.bits[4] | (t.bits[5] << 8);
+        if (6ull + l1 + l2 + l3 > t.bitsSize) { if (sIdx == 0) reportError(status, DERR_CORRUPTION); return; }
+        uint32_t const l4 = t.bitsSize - 6 - l1 - l2 - l3;
+        uint32_t const seg = (t.dstSize + 3) / 4;
+        if (3ull * seg > t.dstSize) { if (sIdx == 0) reportError(status, DERR_CORRUPTION); return; }
+        uint32_t const lens[4] = { l1, l2, l3, l4 };
+        uint32_t off = 6;
+        for (uint32_t k = 0; k < sIdx; k++) off += lens[k];
+        sp = t.bits + off;
+        ssize = lens[sIdx];
+        o0 = seg * sIdx;
+        n = sIdx == 3 ? t.dstSize - 3 * seg : seg;
+    } else {
+        if (sIdx != 0) return;
+        sp = t.bits;
+        ssize = t.bitsSize;
+        o0 = 0;
+        n = t.dstSize;
+    }
+    BitRev br;
+    if (!br.init(sp, ssize)) { reportError(status, DERR_CORRUPTION); return; }
+    uint8_t* const out = t.out + o0;
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t const e = dt[br.peek(tl)];
+        out[i] = uint8_t(e & 0xff);
+        br.skip(e >> 8);
+    }
+    if (br.pos != 0) reportError(status, DERR_CORRUPTION);
+}
+
+// ---------------------------------------------------------------------------
+// XXH3-64 checksums. Phase 1: per 1 KiB block, the 16-stripe sum of every
+// accumulator lane's increments (they commute within a block). Phase 2: per
+// task, the block chain acc = scramble(acc + blockSum) on 8 lanes, then the
+// tail stripes and the final merge on one lane. Constants are XXH3's
+// published secret and primes.
+__constant__ uint8_t kXxhSecret[192] = {
+    0xb8, 0xfe, 0x6c, 0x39, 0x23, 0xa4, 0x4b, 0xbe, 0x7c, 0x01, 0x81, 0x2c, 0xf7, 0x21, 0xad, 0x1c,
+    0xde, 0xd4, 0x6d, 0xe9, 0x83, 0x90, 0x97, 0xdb, 0x72, 0x40, 0xa4, 0xa4, 0xb7, 0xb3, 0x67, 0x1f,
+    0xcb, 0x79, 0xe6, 0x4e, 0xcc, 0xc0, 0xe5, 0x78, 0x82, 0x5a, 0xd0, 0x7d, 0xcc, 0xff, 0x72, 0x21,
+    0xb8, 0x08, 0x46, 0x74, 0xf7, 0x43, 0x24, 0x8e, 0xe0, 0x35, 0x90, 0xe6, 0x81, 0x3a, 0x26, 0x4c,
+    0x3c, 0x28, 0x52, 0xbb, 0x91, 0xc3, 0x00, 0xcb, 0x88, 0xd0, 0x65, 0x8b, 0x1b, 0x53, 0x2e, 0xa3,
+    0x71, 0x64, 0x48, 0x97, 0xa2, 0x0d, 0xf9, 0x4e, 0x38, 0x19, 0xef, 0x46, 0xa9, 0xde, 0xac, 0xd8,
+    0xa8, 0xfa, 0x76, 0x3f, 0xe3, 0x9c, 0x34, 0x3f, 0xf9, 0xdc, 0xbb, 0xc7, 0xc7, 0x0b, 0x4f, 0x1d,
+    0x8a, 0x51, 0xe0, 0x4b, 0xcd, 0xb4, 0x59, 0x31, 0xc8, 0x9f, 0x7e, 0xc9, 0xd9, 0x78, 0x73, 0x64,
+    0xea, 0xc5, 0xac, 0x83, 0x34, 0xd3, 0xeb, 0xc3, 0xc5, 0x81, 0xa0, 0xff, 0xfa, 0x13, 0x63, 0xeb,
+    0x17, 0x0d, 0xdd, 0x51, 0xb7, 0xf0, 0xda, 0x49, 0xd3, 0x16, 0x55, 0x26, 0x29, 0xd4, 0x68, 0x9e,
+    0x2b, 0x16, 0xbe, 0x58, 0x7d, 0x47, 0xa1, 0xfc, 0x8f, 0xf8, 0xb8, 0xd1, 0x7a, 0xd0, 0x31, 0xce,
+    0x45, 0xcb, 0x3a, 0x8f, 0x95, 0x16, 0x04, 0x28, 0xaf, 0xd7, 0xfb, 0xca, 0xbb, 0x4b, 0x40, 0x7e,
+};
+
+#define XP32_1 0x9E3779B1u
+#define XP32_2 0x85EBCA77u
+#define XP32_3 0xC2B2AE3Du
+#define XP64_1 0x9E3779B185EBCA87ull
+#define XP64_2 0xC2B2AE3D27D4EB4Full
+#define XP64_3 0x165667B19E3779F9ull
+#define XP64_4 0x85EBCA77C2B2AE63ull
+#define XP64_5 0x27D4EB2F165667C5ull
+#define XPMX1 0x165667919E3779F9ull
+#define XPMX2 0x9FB21C651E98DF25ull
+
+__device__ __forceinline__ uint64_t secret64(int off)
+{
+    uint64_t v = 0;
+    for (int b = 0; b < 8; b++) v |= uint64_t(kXxhSecret[off + b]) << (8 * b);
+    return v;
+}
+__device__ __forceinline__ uint32_t secret32(int off)
+{
+    return uint32_t(kXxhSecret[off]) | (uint32_t(kXxhSecret[off + 1]) << 8) | (uint32_t(kXxhSecret[off + 2]) << 16)
+            | (uint32_t(kXxhSecret[off + 3]) << 24);
+}
+__device__ __forceinline__ uint64_t fold128(uint64_t a, uint64_t b)
+{
+    return (a * b) ^ __umul64hi(a, b);
+}
+__device__ __forceinline__ uint64_t xAvalanche(uint64_t h)
+{
+    h ^= h >> 37;
+    h *= XPMX1;
+    return h ^ (h >> 32);
+}
+__device__ __forceinline__ uint64_t x64Avalanche(uint64_t h)
+{
+    h ^= h >> 33;
+    h *= XP64_2;
+    h ^= h >> 29;
+    h *= XP64_3;
+    return h ^ (h >> 32);
+}
+__device__ __forceinline__ uint64_t ldData(const uint8_t* p, bool aligned)
+{
+    if (aligned && !(reinterpret_cast<uintptr_t>(p) & 7)) return *reinterpret_cast<const uint64_t*>(p);
+    uint64_t v = 0;
+    for (int b = 0; b < 8; b++) v |= uint64_t(p[b]) << (8 * b);
+    return v;
+}
+__device__ __forceinline__ uint64_t mix16(const uint8_t* in, int soff, bool al)
+{
+    return fold128(ldData(in, al) ^ secret64(soff), ldData(in + 8, al) ^ secret64(soff + 8));
+}
+
+__device__ uint64_t xxh3Short(const uint8_t* in, uint64_t len, bool al)
+{
+    if (len <= 16) {
+        if (len > 8) {
+            uint64_t lo = ldData(in, al) ^ (secret64(24) ^ secret64(32));
+            uint64_t hi = ldData(in + len - 8, al) ^ (secret64(40) ^ secret64(48));
+            uint64_t const swapped = (uint64_t(__byte_perm(uint32_t(lo), 0, 0x0123)) << 32)
+                    | __byte_perm(uint32_t(lo >> 32), 0, 0x0123);
+            uint64_t acc = len + swapped + hi + fold128(lo, hi);
+            return xAvalanche(acc);
+        }
+        if (len >= 4) {
+            uint64_t i1 = 0, i2 = 0;
+            for (int b = 0; b < 4; b++) {
+                i1 |= uint64_t(in[b]) << (8 * b);
+                i2 |= uint64_t(in[len - 4 + b]) << (8 * b);
+            }
+            uint64_t k = (i2 + (i1 << 32)) ^ (secret64(8) ^ secret64(16));
+            k ^= ((k << 49) | (k >> 15)) ^ ((k << 24) | (k >> 40));
+            k *= XPMX2;
+            k ^= (k >> 35) + len;
+            k *= XPMX2;
+            return k ^ (k >> 28);
+        }
+        if (len > 0) {
+            uint32_t c = (uint32_t(in[0]) << 16) | (uint32_t(in[len >> 1]) << 24) | in[len - 1] | (uint32_t(len) << 8);
+            return x64Avalanche(uint64_t(c) ^ uint64_t(secret32(0) ^ secret32(4)));
+        }
+        return x64Avalanche(secret64(56) ^ secret64(64));
+    }
+    if (len <= 128) {
+        uint64_t acc = len * XP64_1;
+        if (len > 32) {
+            if (len > 64) {
+                if (len > 96) {
+                    acc += mix16(in + 48, 96, al);
+                    acc += mix16(in + len - 64, 112, al);
+                }
+                acc += mix16(in + 32, 64, al);
+                acc += mix16(in + len - 48, 80, al);
+            }
+            acc += mix16(in + 16, 32, al);
+            acc += mix16(in + len - 32, 48, al);
+        }
+        acc += mix16(in, 0, al);
+        acc += mix16(in + len - 16, 16, al);
+        return xAvalanche(acc);
+    }
+    uint64_t acc = len * XP64_1;
+    uint64_t const rounds = len / 16;
+    for (uint64_t i = 0; i < 8; i++) acc += mix16(in + 16 * i, int(16 * i), al);
+    acc = xAvalanche(acc);
+    for (uint64_t i = 8; i < rounds; i++) acc += mix16(in + 16 * i, int(16 * (i - 8) + 3), al);
+    acc += mix16(in + len - 16, 136 - 17, al);
+    return xAvalanche(acc);
+}
+
+// Phase 1: one warp per 1 KiB block; lane = (stripe group g, accumulator i).
+__global__ void kHashBlocks(const HashTask* __restrict__ tasks, const TileRef* __restrict__ blocks, uint32_t nbBlocks)
+{
+    uint32_t const warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t const lane = threadIdx.x & 31;
+    if (warp >= nbBlocks) return;
+    TileRef const br = blocks[warp];
+    HashTask const t = tasks[br.task];
+    const uint8_t* const blk = t.data + uint64_t(br.tile) * kHashBlock;
+    uint32_t const i = lane & 7, g = lane >> 3;
+    bool const al = t.aligned8 != 0;
+    uint64_t s = 0;
+    for (uint32_t st = g; st < 16; st += 4) {
+        const uint8_t* const stripe = blk + 64 * st;
+        uint64_t const v = ldData(stripe + 8 * i, al);
+        uint64_t const vx = ldData(stripe + 8 * (i ^ 1), al);
+        uint64_t const k = v ^ secret64(int(8 * st + 8 * i));
+        s += vx + uint64_t(uint32_t(k)) * (k >> 32);
+    }
+    s += __shfl_xor_sync(0xffffffffu, s, 8);
+    s += __shfl_xor_sync(0xffffffffu, s, 16);
+    if (lane < 8) t.blockSums[8ull * br.tile + lane] = s;
+}
+
+// Phase 2: one warp per task.
+__global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks, uint32_t* __restrict__ status)
+{
+    uint32_t const ti = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t const lane = threadIdx.x & 31;
+    if (ti >= nbTasks) return;
+    HashTask const t = tasks[ti];
+    bool const al = t.aligned8 != 0;
+    uint64_t h;
+    if (t.len <= 240) {
+        if (lane != 0) return;
+        h = xxh3Short(t.data, t.len, al);
+    } else {
+        uint64_t const init[8] = { XP32_3, XP64_1, XP64_2, XP64_3, XP64_4, XP32_2, XP64_5, XP32_1 };
+        uint32_t const i = lane & 7;
+        uint64_t acc = init[i];
+        uint64_t const key = secret64(int(192 - 64 + 8 * i));
+        for (uint32_t b = 0; b < t.nbBlocks; b++) {
+            acc += t.blockSums[8ull * b + i];
+            acc ^= acc >> 47;
+            acc ^= key;
+            acc *= XP32_1;
+        }
+        uint64_t a[8];
+        for (int k = 0; k < 8; k++) a[k] = __shfl_sync(0xffffffffu, acc, k);
+        if (lane != 0) return;
+        uint64_t const len = t.len;
+        uint64_t const nbStripes = ((len - 1) - uint64_t(kHashBlock) * t.nbBlocks) / 64;
+        const uint8_t* const last = t.data + uint64_t(kHashBlock) * t.nbBlocks;
+        for (uint64_t st = 0; st < nbStripes; st++)
+            for (int k = 0; k < 8; k++) {
+                uint64_t const v = ldData(last + 64 * st + 8 * k, al);
+                uint64_t const x = v ^ secret64(int(8 * st + 8 * k));
+                a[k ^ 1] += v;
+                a[k] += uint64_t(uint32_t(x)) * (x >> 32);
+            }
+        for (int k = 0; k < 8; k++) {
+            uint64_t const v = ldData(t.data + len - 64 + 8 * k, al);
+            uint64_t const x = v ^ secret64(192 - 64 - 7 + 8 * k);
+            a[k ^ 1] += v;
+            a[k] += uint64_t(uint32_t(x)) * (x >> 32);
+        }
+        uint64_t r = len * XP64_1;
+        for (int k = 0; k < 4; k++)
+            r += fold128(a[2 * k] ^ secret64(11 + 16 * k), a[2 * k + 1] ^ secret64(11 + 16 * k + 8));
+        h = xAvalanche(r);
+    }
+    bool const ok = t.low8 ? ((h & 255) == t.expected) : (uint32_t(h) == t.expected);
+    if (!ok) reportError(status, t.errCode);
+}
+
+} // namespace ozl
+
+// ---------------------------------------------------------------------------
+// dispatch
+namespace ozl {
+
+namespace {
+constexpr uint32_t kFseSmemBudget = 96 * 1024;  // per CTA: two CTAs per SM
+constexpr uint32_t kHufChunksPerCta = 8;
+uint32_t fseLanes(uint32_t tlMax)
+{
+    uint32_t const per = 4u << tlMax;
+    uint32_t lanes = kFseSmemBudget / per;
+    return lanes > 32 ? 32 : (lanes < 1 ? 1 : lanes);
+}
+} // namespace
+
+cudaError_t prepareKernels()
+{
+    cudaError_t e = cudaFuncSetAttribute(kFse, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFseSmemBudget));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(kHuf, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(kHufChunksPerCta * (2u << kHufTableLog)));
+}
+
+long runLaunches(const DeviceLayout& L, uint8_t* dPool, uint8_t* dScratch, uint32_t* dStatus, cudaStream_t s)
+{
+    long count = 0;
+    for (const Launch& l : L.launches) {
+        const void* tasks = dPool + l.taskOff;
+        const TileRef* tiles = reinterpret_cast<const TileRef*>(dPool + l.tileOff);
+        switch (l.kind) {
+            case KIND_COPY:
+                kCopy<<<l.nbTiles, 256, 0, s>>>(static_cast<const CopyTask*>(tasks), tiles);
+                break;
+            case KIND_CONST:
+                kConst<<<l.nbTiles, 256, 0, s>>>(static_cast<const ConstTask*>(tasks), tiles);
+                break;
+            case KIND_FSE: {
+                uint32_t const lanes = fseLanes(l.param0);
+                uint32_t const grid = (l.nbTasks + lanes - 1) / lanes;
+                kFse<<<grid, 32, lanes * (4u << l.param0), s>>>(static_cast<const FseTask*>(tasks), l.nbTasks, lanes,
+                                                                 l.param0, dStatus);
+                break;
+            }
+            case KIND_HUF: {
+                uint32_t const grid = (l.nbTasks + kHufChunksPerCta - 1) / kHufChunksPerCta;
+                kHuf<<<grid, 4 * kHufChunksPerCta, kHufChunksPerCta * (2u << kHufTableLog), s>>>(
+                        static_cast<const HufTask*>(tasks), l.nbTasks, kHufChunksPerCta, dStatus);
+                break;
+            }
+            case KIND_FLATPACK:
+                kFlatpack<<<l.nbTiles, 256, 0, s>>>(static_cast<const FlatpackTask*>(tasks), tiles, dStatus);
+                break;
+            case KIND_TOKENIZE:
+                kTokenize<<<l.nbTiles, 256, 0, s>>>(static_cast<const TokenizeTask*>(tasks), tiles, dStatus);
+                break;
+            case KIND_FLOATDEC:
+                kFloatDec<<<l.nbTiles, 256, 0, s>>>(static_cast<const FloatDecTask*>(tasks), tiles);
+                break;
+            case KIND_TRANSPOSE:
+                kTranspose<<<l.nbTiles, 256, 0, s>>>(static_cast<const TransposeTask*>(tasks), tiles);
+                break;
+            case KIND_NUMPIPE: {
+                unsigned long long* scan = nullptr;
+                if (l.needsScan) {
+                    scan = reinterpret_cast<unsigned long long*>(dScratch + l.statusOff);
+                    if (cudaMemsetAsync(scan, 0, l.statusBytes, s) != cudaSuccess) return -1;
+                }
+                kNumPipe<<<l.nbTiles, kNPThreads, 0, s>>>(static_cast<const NumPipeTask*>(tasks), tiles, scan, dStatus);
+                break;
+            }
+            case KIND_HASH: {
+                if (l.nbTiles) {
+                    uint32_t const grid = (l.nbTiles * 32 + 255) / 256;
+                    kHashBlocks<<<grid, 256, 0, s>>>(static_cast<const HashTask*>(tasks), tiles, l.nbTiles);
+                    count++;
+                }
+                uint32_t const grid = (l.nbTasks * 32 + 255) / 256;
+                kHashFinish<<<grid, 256, 0, s>>>(static_cast<const HashTask*>(tasks), l.nbTasks, dStatus);
+                break;
+            }
+            default:
+                return -1;
+        }
+        count++;
+        if (cudaPeekAtLastError() != cudaSuccess) return -1;
+    }
+    return count;
+}
+
+} // namespace ozl

@@ -204,3 +204,7 @@ int64_t ref_describe(const void* src, size_t srcSize, char* out, size_t outCap)
     ZL_ReflectionCtx_free(rc);
     return (int64_t)n;
 }
+
+/* XXH3-64 as the reference library computes it (its vendored xxhash). */
+#include "openzl/shared/xxhash.h"
+uint64_t ref_xxh3_64(const void* src, size_t len) { return XXH3_64bits(src, len); }

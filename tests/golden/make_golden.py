@@ -1,0 +1,107 @@
+"""Generates the golden frames under tests/golden/ with the reference library.
+
+Run in a container that holds the reference sources (it builds
+oracle/_ref/ with oracle/ref.mk first). Each case is the frame the reference
+compressor produced for a seeded input, plus a manifest entry holding the
+SHA-256 of that input. The tests decode the frames with the GPU library and
+with the CPU oracle and check both against the recorded input hash.
+
+    python tests/golden/make_golden.py
+"""
+import ctypes
+import hashlib
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+# recipe numbers follow oracle/ref_driver.c
+CASES = []
+
+
+def walk(rng, n, dtype, step, start=1000000):
+    s = rng.integers(-step, step + 1, n)
+    return (start + np.cumsum(s)).astype(dtype)
+
+
+def timestamps(rng, n):
+    inc = rng.geometric(1 / 1000, n).astype(np.int64)
+    out = rng.random(n) < 0.01
+    inc[out] = rng.integers(0, 2**32, int(out.sum()))
+    return (1700000000000000000 + np.cumsum(inc)).astype(np.int64)
+
+
+def build_cases():
+    rng = np.random.default_rng(20261203)
+    c = []
+    # the 1 MiB u32 random walk of the small numeric workload
+    c.append(("walk_u32_1mib_dz_tsplit_fse", 1, walk(rng, 262144, np.uint32, 100), 4))
+    c.append(("ts_i64_dz_bitpack_huf", 2, timestamps(rng, 100000), 8))
+    for w, dt in [(1, np.uint8), (2, np.uint16), (4, np.uint32), (8, np.uint64)]:
+        c.append(("walk_u%d_d_tsplit_fse" % (8 * w), 3, walk(rng, 70000 + 13 * w, dt, 3000), w))
+        c.append(("walk_u%d_d_bitpack_huf" % (8 * w), 4, walk(rng, 70001 + 7 * w, dt, 300), w))
+        c.append(("walk_u%d_delta_store" % (8 * w), 9, walk(rng, 5000 + w, dt, 100), w))
+        c.append(("walk_u%d_zigzag_store" % (8 * w), 10, walk(rng, 4000 + w, dt, 100), w))
+        c.append(("walk_u%d_bitpack_store" % (8 * w), 11, walk(rng, 3000 + w, dt, 100, start=500), w))
+        c.append(("walk_u%d_tsplit_store" % (8 * w), 12, walk(rng, 3333 + w, dt, 100), w))
+    keys = rng.integers(-2**31, 2**31, 10000).astype(np.int32)
+    z = (rng.zipf(1.1, 200000) - 1) % 10000
+    c.append(("tokenize_zipf_i32", 5, keys[z], 4))
+    c.append(("tokenize_small_alphabet_i32", 5, rng.choice(keys[:200], 50000), 4))
+    c.append(("tokenize_sorted_i32", 16, keys[z[:60000]], 4))
+    bf = rng.normal(0, 0.02, 300000).astype(np.float32).view(np.uint32)
+    c.append(("bf16_weights", 6, ((bf + 0x7FFF + ((bf >> 16) & 1)) >> 16).astype(np.uint16), 2))
+    c.append(("fse_serial_skewed", 7, (rng.zipf(1.3, 300000) % 256).astype(np.uint8), 0))
+    c.append(("fse_serial_small", 7, rng.integers(0, 4, 700).astype(np.uint8), 0))
+    c.append(("huf_serial_skewed", 8, (rng.zipf(1.3, 300000) % 256).astype(np.uint8), 0))
+    c.append(("huf_serial_uniform", 8, rng.integers(0, 256, 150000).astype(np.uint8), 0))
+    c.append(("huf_serial_1x", 8, rng.integers(0, 6, 900).astype(np.uint8), 0))
+    c.append(("constant_serial", 13, np.full(5000, 7, np.uint8), 0))
+    c.append(("flatpack_serial", 14, rng.integers(0, 37, 30000).astype(np.uint8), 0))
+    c.append(("bitpack_graph_serial", 15, rng.integers(0, 37, 30000).astype(np.uint8), 0))
+    c.append(("store_serial", 0, rng.integers(0, 256, 3000).astype(np.uint8), 0))
+    c.append(("empty_serial_fse", 7, np.zeros(0, np.uint8), 0))
+    c.append(("tiny_numeric_delta", 9, np.array([5], np.uint32), 4))
+    return c
+
+
+def main():
+    subprocess.check_call(["make", "-s", "-f", "oracle/ref.mk", "-j8"], cwd=ROOT)
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "ref_driver.so"))
+    lib.ref_compress.restype = ctypes.c_int64
+    lib.ref_compress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                 ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    lib.ref_compressBound.restype = ctypes.c_size_t
+    manifest = []
+    for name, recipe, arr, w in build_cases():
+        arr = np.ascontiguousarray(arr)
+        for cs in (1, 0):
+            if cs == 0 and recipe not in (1, 2, 3, 4, 5):
+                continue
+            cap = lib.ref_compressBound(arr.nbytes) + 4096
+            dst = np.zeros(cap, np.uint8)
+            n = arr.size if w else arr.nbytes
+            r = lib.ref_compress(recipe, arr.ctypes.data if arr.size else None, n, w, dst.ctypes.data, cap, cs, 0)
+            if r <= 0:
+                print("skip", name, cs, r)
+                continue
+            case = name + ("" if cs else "_nock")
+            with open(os.path.join(HERE, case + ".zl"), "wb") as f:
+                f.write(dst[:r].tobytes())
+            manifest.append({"case": case, "recipe": recipe, "elt_width": w, "n": int(arr.size),
+                             "checksums": cs, "frame_bytes": int(r),
+                             "sha256_in": hashlib.sha256(arr.tobytes()).hexdigest(),
+                             "sha256_frame": hashlib.sha256(dst[:r].tobytes()).hexdigest()})
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+    tot = sum(os.path.getsize(os.path.join(HERE, m["case"] + ".zl")) for m in manifest)
+    print(len(manifest), "cases,", tot, "bytes")
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,61 @@
+"""CPU oracle: pinned against the reference's golden frames (and, where the
+reference library is built in this container, against the reference itself)."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, read_frame
+from oracle import oracle
+
+REF_DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver.so")
+
+
+def test_oracle_decodes_every_golden_frame(manifest):
+    assert len(manifest) >= 40
+    for m in manifest:
+        out, t, w = oracle.decompress(read_frame(m["case"]))
+        assert hashlib.sha256(out.tobytes()).hexdigest() == m["sha256_in"], m["case"]
+
+
+def test_oracle_detects_checksum_corruption(manifest):
+    m = next(m for m in manifest if m["checksums"] and m["frame_bytes"] > 1000)
+    fr = bytearray(read_frame(m["case"]))
+    fr[len(fr) // 2] ^= 0x40
+    with pytest.raises(ValueError):
+        oracle.decompress(bytes(fr))
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
+def test_xxh3_every_length_class_matches_reference():
+    import ctypes
+
+    ref = ctypes.CDLL(REF_DRIVER)
+    ref.ref_xxh3_64.restype = ctypes.c_uint64
+    ref.ref_xxh3_64.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+    rng = np.random.default_rng(1)
+    for n in [0, 1, 3, 4, 8, 9, 16, 17, 100, 128, 129, 240, 241, 1024, 1025, 1088, 5000, 100000]:
+        b = rng.integers(0, 256, n).astype(np.uint8)
+        assert oracle.xxh3_64(b.tobytes()) == ref.ref_xxh3_64(b.ctypes.data, n), n
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
+def test_oracle_matches_reference_on_seeded_inputs():
+    import ctypes
+
+    ref = ctypes.CDLL(REF_DRIVER)
+    ref.ref_compress.restype = ctypes.c_int64
+    ref.ref_compress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(99)
+    for recipe, w, dt in [(1, 4, np.uint32), (2, 8, np.int64), (3, 2, np.uint16), (4, 8, np.uint64),
+                          (3, 1, np.uint8), (4, 4, np.uint32)]:
+        for n in (1, 2, 999, 1000, 33000, 150001):
+            arr = (500 + np.cumsum(rng.integers(-50, 51, n))).astype(dt)
+            cap = arr.nbytes * 2 + 4096
+            dst = np.zeros(cap, np.uint8)
+            r = ref.ref_compress(recipe, arr.ctypes.data, n, w, dst.ctypes.data, cap, 1, 0)
+            assert r > 0
+            out, _, _ = oracle.decompress(dst[:r].tobytes())
+            assert out.tobytes() == arr.tobytes(), (recipe, w, n)
