@@ -649,7 +649,8 @@ int DecodePlan::planBlock(int f, const uint8_t* src, size_t size, size_t start, 
     auto isNumView = [&](const PlanNode& nd_) {
         return !nd_.dead && signature(nd_.id).view;
     };
-    for (int u = nBase; u < int(nodes.size()); u++) {
+    // consumers before producers, so the outermost node absorbs the whole chain
+    for (int u = int(nodes.size()) - 1; u >= nBase; u--) {
         PlanNode& C = nodes[u];
         if (C.dead) continue;
         if (C.id != T_DELTA && C.id != T_ZIGZAG && C.id != T_TSPLIT && C.id != T_BITPACK_INT
@@ -817,6 +818,16 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         addrDone[s] = 1;
         return a;
     };
+
+    // every input of a live decoder must have a location by now
+    for (const PlanNode& nd : nodes) {
+        if (nd.dead) continue;
+        for (int s : nd.ins)
+            if (streams[s].loc == L_NONE) {
+                err = "planner: stream without a location (codec " + std::to_string(nd.id) + ")";
+                return 80;
+            }
+    }
 
     // ---- levels ------------------------------------------------------------
     std::vector<int> level(nodes.size(), 0);

@@ -1,0 +1,35 @@
+"""Decode planner (host logic, no GPU): every golden frame plans and lays out
+with every task's pointers and lengths inside the allocations they address."""
+import os
+import subprocess
+
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+
+@pytest.fixture(scope="module")
+def checker(tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("plan") / "plan_check")
+    cmd = ["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined", "-I",
+           os.path.join(ROOT, "openzl_gb300", "csrc"), os.path.join(ROOT, "tests", "native", "plan_check.cpp"),
+           os.path.join(ROOT, "openzl_gb300", "csrc", "dec_plan.cpp"), "-o", exe]
+    subprocess.check_call(cmd)
+    return exe
+
+
+def test_every_golden_layout_is_in_bounds(checker, manifest):
+    for m in manifest:
+        r = subprocess.run([checker, os.path.join(GOLDEN, m["case"] + ".zl")], capture_output=True, text=True)
+        assert r.returncode == 0 and "bad=0" in r.stdout, (m["case"], r.stdout[-2000:], r.stderr[-2000:])
+
+
+def test_fused_pipeline_shape(checker):
+    """delta <- zigzag <- view <- transpose fuse into one planes-sourced pass
+    that runs after the entropy level, and checksums run last."""
+    r = subprocess.run([checker, os.path.join(GOLDEN, "walk_u32_1mib_dz_tsplit_fse.zl")], capture_output=True,
+                       text=True)
+    out = r.stdout
+    assert "np n=262144 w=4 mode=1 zz=1 delta=1" in out
+    kinds = [l.split()[1] for l in out.splitlines() if l.strip().startswith("launch")]
+    assert kinds == ["kind=1", "kind=2", "kind=8", "kind=9"], kinds
