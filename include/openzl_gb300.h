@@ -146,6 +146,10 @@ const size_t* ozl_gpu_batch_sizes(const OZL_GpuBatch* b);
 /* Message describing the last error of this batch ("" when none). */
 const char* ozl_gpu_batch_error(const OZL_GpuBatch* b);
 
+/* XXH3-64 (seed 0), the hash behind OpenZL's checksums, of `len` bytes of
+ * device memory; computed on the GPU. Returns the hash in the report value. */
+ZL_Report ozl_gpu_xxh3_64(const void* d_data, size_t len, void* stream);
+
 /* Library build identification (for load checks). */
 const char* ozl_gpu_version(void);
 

@@ -10,6 +10,7 @@ from ._lib import (  # noqa: F401
     DCtx,
     GpuBatch,
     decompress,
+    xxh3_64_device,
     get_decompressed_size,
     get_compressed_size,
     library,

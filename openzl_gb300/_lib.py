@@ -53,6 +53,7 @@ def library():
         "ozl_gpu_batch_sizes": ([vp], ctypes.POINTER(ctypes.c_size_t)),
         "ozl_gpu_batch_error": ([vp], ctypes.c_char_p),
         "ozl_gpu_version": ([], ctypes.c_char_p),
+        "ozl_gpu_xxh3_64": ([vp, sz, vp], ZLReport),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -130,6 +131,11 @@ class DCtx:
         if rep.code:
             raise ZLError(rep.code, self._err(rep))
         return rep.value
+
+
+def xxh3_64_device(dev_ptr, length, stream=0):
+    """XXH3-64 of device memory, computed on the GPU."""
+    return _check(library().ozl_gpu_xxh3_64(dev_ptr, length, stream))
 
 
 def decompress(frame):

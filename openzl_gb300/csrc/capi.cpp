@@ -382,6 +382,21 @@ size_t ozl_gpu_batch_launches(const OZL_GpuBatch* b) { return b ? size_t(b->laun
 
 const size_t* ozl_gpu_batch_sizes(const OZL_GpuBatch* b) { return b ? b->sizes.data() : nullptr; }
 
+ZL_Report ozl_gpu_xxh3_64(const void* d_data, size_t len, void* stream)
+{
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    size_t const scratchBytes = 512 + (len / 1024 + 1) * 72;
+    uint8_t* scratch = nullptr;
+    if (cudaMalloc(&scratch, scratchBytes + 64) != cudaSuccess) return fail(ZL_ErrorCode_allocation);
+    cudaError_t e = ozl::xxh3Device(static_cast<const uint8_t*>(d_data), len,
+                                    reinterpret_cast<uint64_t*>(scratch + scratchBytes), scratch, scratchBytes, s);
+    uint64_t h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, scratch + scratchBytes, 8, cudaMemcpyDeviceToHost);
+    cudaFree(scratch);
+    if (e != cudaSuccess) return fail(ZL_ErrorCode_GENERIC);
+    return ok(size_t(h));
+}
+
 const char* ozl_gpu_batch_error(const OZL_GpuBatch* b) { return b ? b->err.c_str() : ""; }
 
 } // extern "C"

@@ -17,4 +17,9 @@ long runLaunches(const DeviceLayout& layout, uint8_t* dPool, uint8_t* dScratch, 
 // Call once per device before the first launch (and before graph capture).
 cudaError_t prepareKernels();
 
+// XXH3-64 of `len` device bytes at `data`; the hash lands in *dHashOut.
+// Needs 256 + 72 * ceil(len / 1 KiB) bytes of device scratch. Synchronizes `s`.
+cudaError_t xxh3Device(const uint8_t* data, uint64_t len, uint64_t* dHashOut, uint8_t* dScratch,
+                       uint64_t scratchBytes, cudaStream_t s);
+
 } // namespace ozl

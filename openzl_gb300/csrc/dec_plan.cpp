@@ -232,6 +232,7 @@ int DecodePlan::build(size_t nbFrames, const uint8_t* const* hFrames, const size
     streams.clear();
     nodes.clear();
     hashes.clear();
+    directCopies.clear();
     params.clear();
     arenaBytes = 0;
     totalOut = 0;
@@ -644,6 +645,10 @@ int DecodePlan::planBlock(int f, const uint8_t* src, size_t size, size_t start, 
     frames[f].outWidth = OUT.w;
     frames[f].outType = OUT.type;
     *outBytes = OUT.bytes();
+    if (OUT.producer < 0 && OUT.bytes()) {
+        // the frame stores its output verbatim: copy it into place
+        directCopies.push_back(PlanCopy{ f, OUT.off, outOffset, OUT.bytes() });
+    }
 
     // ---- fusion of numeric chains (delta <- zigzag <- view <- tsplit|bitpack)
     auto isNumView = [&](const PlanNode& nd_) {
@@ -874,6 +879,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         level[u] = lv;
         maxLevel = std::max(maxLevel, lv);
     }
+    if (!plan.directCopies.empty()) maxLevel = std::max(maxLevel, 1);
     int const hashLevel = maxLevel + 1;
 
     // ---- tasks per level ---------------------------------------------------
@@ -883,6 +889,10 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         if (!bytes) continue;
         CopyTask t{ addr(c.dst) + c.dstOff, addr(c.src), bytes, 0 };
         B[c.level].copy.push_back(t);
+    }
+    for (const PlanCopy& c : plan.directCopies) {
+        CopyTask t{ dOuts[c.frame] + c.outOff, dFrames[c.frame] + c.frameOff, c.bytes, 0 };
+        B[1].copy.push_back(t);
     }
     // pointer arrays (planes) live in the pool; collect them first
     std::vector<const uint8_t*> ptrs;
@@ -1012,7 +1022,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
             if (anyDelta) {
                 L.needsScan = true;
                 L.statusOff = scratch;
-                L.statusBytes = 64 + 16 * uint64_t(tiles.size());
+                L.statusBytes = 64 + 32 * uint64_t(tiles.size());
                 scratch += (L.statusBytes + 255) & ~uint64_t(255);
             }
         }

@@ -74,6 +74,12 @@ struct PlanHash {
     bool low8;          // frame-header checksum: compare the low 8 bits only
 };
 
+// Output bytes that a frame stores verbatim (no decoder regenerates them).
+struct PlanCopy {
+    int frame;
+    uint64_t frameOff, outOff, bytes;
+};
+
 struct FramePlan {
     uint64_t decodedSize = 0;
     uint64_t frameBytes = 0;  // compressed size including the end-of-frame byte
@@ -92,6 +98,7 @@ class DecodePlan {
     std::vector<PlanStream> streams;
     std::vector<PlanNode> nodes;
     std::vector<PlanHash> hashes;
+    std::vector<PlanCopy> directCopies;
     std::vector<uint8_t> params;  // host-decoded small streams (FSE normalized counts)
     uint64_t arenaBytes = 0;
     uint64_t totalOut = 0;

@@ -126,6 +126,7 @@ struct HashTask {
     uint32_t nbBlocks;     // full 1 KiB blocks accumulated in phase 1
     uint32_t low8;         // compare the low 8 bits only (frame-header checksum)
     uint32_t aligned8;     // data pointer is 8-byte aligned
+    uint64_t* hashOut;     // optional: receives the full 64-bit hash
 };
 
 // One tile of a tiled launch: task index and tile index within the task.

@@ -6,6 +6,7 @@
 // input sets the batch status word (first error wins) and the kernel moves
 // on. Every spin-wait is bounded.
 #include <cstdint>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -159,13 +160,26 @@ __device__ __forceinline__ uint64_t fetchSource(const NumPipeTask& t, uint64_t j
     }
 }
 
-// Look-back status per tile: word 0 = flag (0 none, 1 aggregate, 2 prefix), word 1 = value.
-__device__ __forceinline__ void publish(unsigned long long* st, uint32_t tile, uint64_t value, uint64_t flag)
+// Look-back status per tile, 4 words: flag (0 none, 1 aggregate ready,
+// 2 inclusive prefix ready), aggregate, inclusive prefix, unused. The two
+// values live in separate words so that a reader who saw flag 1 never reads
+// a value overwritten by the later inclusive publication.
+constexpr int kScanWords = 4;
+
+__device__ __forceinline__ void publishAggregate(unsigned long long* st, uint32_t tile, uint64_t agg)
 {
-    volatile unsigned long long* s = st + 2 * tile;
-    s[1] = value;
+    volatile unsigned long long* s = st + kScanWords * tile;
+    s[1] = agg;
     __threadfence();
-    s[0] = flag;
+    s[0] = 1;
+}
+
+__device__ __forceinline__ void publishInclusive(unsigned long long* st, uint32_t tile, uint64_t incl)
+{
+    volatile unsigned long long* s = st + kScanWords * tile;
+    s[2] = incl;
+    __threadfence();
+    s[0] = 2;
 }
 
 __global__ void __launch_bounds__(kNPThreads) kNumPipe(const NumPipeTask* __restrict__ tasks,
@@ -240,26 +254,29 @@ __global__ void __launch_bounds__(kNPThreads) kNumPipe(const NumPipeTask* __rest
             uint64_t prefix = 0;
             uint32_t const g = tileIdx;
             if (tr.tile == 0) {
-                publish(st, g, tileAgg, 2);
+                publishInclusive(st, g, tileAgg);
             } else {
-                publish(st, g, tileAgg, 1);
+                publishAggregate(st, g, tileAgg);
                 int64_t p = int64_t(g) - 1;
                 uint32_t spins = 0;
                 bool ok = true;
                 while (true) {
-                    volatile unsigned long long* s = st + 2 * p;
-                    unsigned long long f = s[0];
+                    volatile unsigned long long* s = st + kScanWords * p;
+                    unsigned long long const f = s[0];
                     if (f == 0) {
                         if (++spins > (1u << 26)) { ok = false; break; }
                         continue;
                     }
                     __threadfence();
+                    if (f == 2) {
+                        prefix += s[2];
+                        break;
+                    }
                     prefix += s[1];
-                    if (f == 2) break;
                     p--;
                 }
                 if (!ok) reportError(status, DERR_TIMEOUT);
-                publish(st, g, prefix + tileAgg, 2);
+                publishInclusive(st, g, prefix + tileAgg);
             }
             sPrefix = prefix;
         }
@@ -806,8 +823,9 @@ __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks
             r += fold128(a[2 * k] ^ secret64(11 + 16 * k), a[2 * k + 1] ^ secret64(11 + 16 * k + 8));
         h = xAvalanche(r);
     }
+    if (t.hashOut) *t.hashOut = h;
     bool const ok = t.low8 ? ((h & 255) == t.expected) : (uint32_t(h) == t.expected);
-    if (!ok) reportError(status, t.errCode);
+    if (!ok && t.errCode) reportError(status, t.errCode);
 }
 
 } // namespace ozl
@@ -901,4 +919,38 @@ long runLaunches(const DeviceLayout& L, uint8_t* dPool, uint8_t* dScratch, uint3
     return count;
 }
 
+} // namespace ozl
+
+// ---------------------------------------------------------------------------
+// standalone XXH3-64 of a device buffer
+namespace ozl {
+cudaError_t xxh3Device(const uint8_t* data, uint64_t len, uint64_t* dHashOut, uint8_t* dScratch,
+                       uint64_t scratchBytes, cudaStream_t s)
+{
+    uint32_t const nbBlocks = len > 240 ? uint32_t((len - 1) / kHashBlock) : 0;
+    size_t const need = 256 + size_t(nbBlocks) * (64 + sizeof(TileRef));
+    if (need > scratchBytes) return cudaErrorInvalidValue;
+    HashTask t{};
+    t.data = data;
+    t.len = len;
+    t.blockSums = reinterpret_cast<uint64_t*>(dScratch + 256);
+    t.nbBlocks = nbBlocks;
+    t.aligned8 = (reinterpret_cast<uintptr_t>(data) & 7) == 0;
+    t.hashOut = dHashOut;
+    HashTask* dTask = reinterpret_cast<HashTask*>(dScratch);
+    TileRef* dTiles = reinterpret_cast<TileRef*>(dScratch + 256 + size_t(nbBlocks) * 64);
+    cudaError_t e = cudaMemcpyAsync(dTask, &t, sizeof(t), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    if (nbBlocks) {
+        std::vector<TileRef> tiles(nbBlocks);
+        for (uint32_t k = 0; k < nbBlocks; k++) tiles[k] = TileRef{ 0, k };
+        e = cudaMemcpyAsync(dTiles, tiles.data(), nbBlocks * sizeof(TileRef), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
+        kHashBlocks<<<(nbBlocks * 32 + 255) / 256, 256, 0, s>>>(dTask, dTiles, nbBlocks);
+    }
+    kHashFinish<<<1, 32, 0, s>>>(dTask, 1, nullptr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
+}
 } // namespace ozl
