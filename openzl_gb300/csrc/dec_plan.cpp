@@ -404,6 +404,7 @@ int DecodePlan::planBlock(int f, const uint8_t* src, size_t size, size_t start, 
             s.loc = L_FRAME;
             s.frame = f;
             s.off = pos;
+            s.host = src + pos;
             pos += storedSize[st];
             st++;
         }
@@ -601,9 +602,23 @@ int DecodePlan::planBlock(int f, const uint8_t* src, size_t size, size_t start, 
                 case T_FSE: {
                     PlanStream& N = in(0);
                     if (N.w != 2) { err = "FSE counts width"; return E_CORRUPT; }
-                    if (N.loc != L_PARAM) { err = "FSE counts not from an ncount stream"; return E_LIMIT; }
                     if (N.n < 2 || N.n > 256) { err = "FSE symbol count"; return E_CORRUPT; }
-                    const int16_t* norm = reinterpret_cast<const int16_t*>(params.data() + N.off);
+                    // The counts are host-known: decoded from an ncount header
+                    // here, or stored raw in the frame (small alphabets).
+                    if (N.loc == L_PARAM) {
+                        nodeU.paramOff = N.off;
+                    } else if (N.host) {
+                        size_t const off = (params.size() + 15) & ~size_t(15);
+                        params.resize(off + 2 * N.n);
+                        std::memcpy(params.data() + off, N.host, 2 * N.n);
+                        nodeU.paramOff = off;
+                    } else {
+                        err = "FSE counts regenerated on the device";
+                        return E_LIMIT;
+                    }
+                    int16_t normBuf[256];
+                    std::memcpy(normBuf, params.data() + nodeU.paramOff, 2 * N.n);
+                    const int16_t* norm = normBuf;
                     unsigned sum = 0;
                     for (uint64_t i = 0; i < N.n; i++) {
                         if (norm[i] < -1) { err = "FSE counts"; return E_CORRUPT; }
@@ -634,6 +649,7 @@ int DecodePlan::planBlock(int f, const uint8_t* src, size_t size, size_t start, 
                     err = "unsupported codec";
                     return E_TRANSFORM;
             }
+            if (sg.view && in(0).host) O.host = in(0).host;
             nodes.push_back(std::move(nodeU));
             sidx += nbIn;
         }
@@ -964,7 +980,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
                 FseTask t{};
                 t.out = o;
                 t.bits = in(1);
-                t.norm = reinterpret_cast<const int16_t*>(in(0));
+                t.norm = reinterpret_cast<const int16_t*>(dParams + nd.paramOff);
                 t.bitsSize = uint32_t(streams[nd.ins[1]].n);
                 t.dstSize = uint32_t(O.n);
                 t.nbSym = uint16_t(streams[nd.ins[0]].n);

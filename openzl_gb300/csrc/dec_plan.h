@@ -49,6 +49,7 @@ struct PlanStream {
     int frame = -1;    // for L_FRAME / L_OUT
     int parent = -1;   // for L_SUB / L_ALIAS
     uint64_t off = 0;  // offset within the location
+    const uint8_t* host = nullptr; // host copy of the content, when known at plan time
     uint64_t bytes() const { return n * w; }
 };
 
@@ -63,6 +64,7 @@ struct PlanNode {
     int level = 0;
     // fused numeric pipeline parameters
     uint8_t srcMode = SRC_PLAIN, nbBits = 0, zigzag = 0, delta = 0;
+    uint64_t paramOff = 0;    // FSE: normalized counts in the parameter block
 };
 
 struct PlanHash {

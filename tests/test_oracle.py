@@ -59,3 +59,48 @@ def test_oracle_matches_reference_on_seeded_inputs():
             assert r > 0
             out, _, _ = oracle.decompress(dst[:r].tobytes())
             assert out.tobytes() == arr.tobytes(), (recipe, w, n)
+
+
+def test_oracle_encoder_reproduces_every_golden_frame(manifest):
+    """The CPU encoder restatement emits the reference's exact frame bytes."""
+    for m in manifest:
+        fr = read_frame(m["case"])
+        data, _, w = oracle.decompress(fr)
+        width = m["elt_width"]
+        arr = data.view({0: np.uint8, 1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[width])
+        got = oracle.compress(m["recipe"], arr, width, checksums=bool(m["checksums"]))
+        assert hashlib.sha256(got.tobytes()).hexdigest() == m["sha256_frame"], m["case"]
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
+def test_oracle_encoder_matches_reference_on_seeded_inputs():
+    import ctypes
+
+    ref = ctypes.CDLL(REF_DRIVER)
+    ref.ref_compress.restype = ctypes.c_int64
+    ref.ref_compress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(1234)
+    cases = []
+    for w, dt in [(1, np.uint8), (2, np.uint16), (4, np.uint32), (8, np.uint64)]:
+        for recipe in (1, 2, 3, 4, 9, 10, 11, 12):
+            for n in (1, 9, 999, 40000, 120000):
+                cases.append((recipe, (7000 + np.cumsum(rng.integers(-3000, 3001, n))).astype(dt), w))
+    for recipe in (7, 8):
+        for n in (2, 10, 1001, 100000, 140000):
+            for k in (2, 5, 256):
+                cases.append((recipe, (rng.zipf(1.2, n) % k).astype(np.uint8), 0))
+    keys = rng.integers(-2**31, 2**31, 1000).astype(np.int32)
+    cases.append((5, keys[(rng.zipf(1.1, 50000) - 1) % 1000], 4))
+    cases.append((16, keys[(rng.zipf(1.1, 50000) - 1) % 300], 4))
+    bf = rng.normal(0, 0.02, 70000).astype(np.float32).view(np.uint32)
+    cases.append((6, (bf >> 16).astype(np.uint16), 2))
+    for recipe, arr, w in cases:
+        for cs in (1, 0):
+            cap = arr.nbytes * 2 + 65536
+            dst = np.zeros(cap, np.uint8)
+            n = arr.size if w else arr.nbytes
+            r = ref.ref_compress(recipe, arr.ctypes.data, n, w, dst.ctypes.data, cap, cs, 0)
+            assert r > 0
+            got = oracle.compress(recipe, arr, w, checksums=bool(cs))
+            assert got.tobytes() == dst[:r].tobytes(), (recipe, w, arr.size, cs)
