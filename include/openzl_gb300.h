@@ -139,12 +139,64 @@ ZL_Report ozl_gpu_batch_run(OZL_GpuBatch* b, void* stream, int useGraph);
 /* Synchronizes `stream` and reports device-detected errors of the last run
  * (corruption, checksum mismatch). Returns the total decompressed size. */
 ZL_Report ozl_gpu_batch_check(OZL_GpuBatch* b, void* stream);
+/* Runs the planned decode launch by launch on `stream`, bracketing each with
+ * CUDA events. For launch i, writes its duration in milliseconds to
+ * ms[i], its codec family to kinds[i] (see ozl_gpu_kind_name) and the bytes
+ * it must read plus write to bytes[i], for i < capacity. Returns the number
+ * of launches. Synchronizes `stream`. */
+ZL_Report ozl_gpu_batch_profile(OZL_GpuBatch* b, void* stream, float* ms, int* kinds,
+                                uint64_t* bytes, size_t capacity);
+/* Name of a codec family reported by ozl_gpu_batch_profile. */
+const char* ozl_gpu_kind_name(int kind);
+/* Host-buffer run of a planned batch whose device frames sit back to back
+ * from d_frames[0] and whose outputs sit back to back from d_dsts[0] (as
+ * passed to ozl_gpu_batch_plan): copies h_in (inBytes) to the device, runs
+ * the decode, copies the outputs to h_out (outBytes) and synchronizes.
+ * Returns the total decompressed size. */
+ZL_Report ozl_gpu_batch_run_host(OZL_GpuBatch* b, const void* h_in, size_t inBytes, void* h_out,
+                                 size_t outBytes, void* stream, int useGraph);
 /* Number of kernel launches one run issues. */
 size_t ozl_gpu_batch_launches(const OZL_GpuBatch* b);
 /* Per-frame decoded sizes of the last plan (array of nbFrames). */
 const size_t* ozl_gpu_batch_sizes(const OZL_GpuBatch* b);
 /* Message describing the last error of this batch ("" when none). */
 const char* ozl_gpu_batch_error(const OZL_GpuBatch* b);
+
+/* Batched compression (no counterpart in the reference: the reference
+ * compresses one frame per call on the CPU). Each frame i compresses
+ * nbElts[i] elements of eltWidths[i] bytes (0 = serial bytes) at device
+ * address d_srcs[i] with the numeric graph recipes[i] (OZL_GRAPH_*) into
+ * d_dsts[i] (capacity dstCapacities[i], see ozl_gpu_compress_bound), format
+ * version 23. The frames are byte-identical to what the reference's
+ * ZL_CCtx_compressTypedRef emits for the same graph and parameters.
+ * frameSizes[i] receives each frame's size. Synchronizes `stream`. */
+typedef enum {
+    OZL_GRAPH_STORE = 0,            /* ZL_GRAPH_STORE */
+    OZL_GRAPH_DZ_TSPLIT_FSE = 1,    /* delta -> zigzag -> to-struct -> transpose-split(ZL_GRAPH_FSE) */
+    OZL_GRAPH_DZ_BITPACK_HUF = 2,   /* delta -> zigzag -> bitpack_int -> ZL_GRAPH_HUFFMAN */
+    OZL_GRAPH_D_TSPLIT_FSE = 3,     /* delta -> to-struct -> transpose-split(ZL_GRAPH_FSE) */
+    OZL_GRAPH_D_BITPACK_HUF = 4,    /* delta -> bitpack_int -> ZL_GRAPH_HUFFMAN */
+    OZL_GRAPH_FSE = 7,              /* ZL_GRAPH_FSE */
+    OZL_GRAPH_HUFFMAN = 8,          /* ZL_GRAPH_HUFFMAN */
+    OZL_GRAPH_DELTA_STORE = 9,      /* delta -> store */
+    OZL_GRAPH_ZIGZAG_STORE = 10,    /* zigzag -> store */
+    OZL_GRAPH_BITPACK_STORE = 11,   /* bitpack_int -> store */
+    OZL_GRAPH_TSPLIT_STORE = 12,    /* to-struct -> transpose-split(store) */
+    OZL_GRAPH_CONSTANT = 13,        /* ZL_GRAPH_CONSTANT */
+    OZL_GRAPH_FLATPACK = 14,        /* ZL_GRAPH_FLATPACK */
+    OZL_GRAPH_BITPACK = 15,         /* ZL_GRAPH_BITPACK */
+} OZL_GraphRecipe;
+
+typedef struct OZL_GpuEncoder_s OZL_GpuEncoder;
+OZL_GpuEncoder* ozl_gpu_encoder_create(void);
+void ozl_gpu_encoder_free(OZL_GpuEncoder* e);
+size_t ozl_gpu_compress_bound(size_t srcBytes);
+ZL_Report ozl_gpu_compress_batch(OZL_GpuEncoder* e, size_t nbFrames, const void* const* d_srcs,
+                                 const size_t* nbElts, const int* eltWidths, const int* recipes,
+                                 void* const* d_dsts, const size_t* dstCapacities, size_t* frameSizes,
+                                 int checksums, void* stream);
+/* Message describing the encoder's last error ("" when none). */
+const char* ozl_gpu_encoder_error(const OZL_GpuEncoder* e);
 
 /* XXH3-64 (seed 0), the hash behind OpenZL's checksums, of `len` bytes of
  * device memory; computed on the GPU. Returns the hash in the report value. */

@@ -9,6 +9,7 @@ from ._lib import (  # noqa: F401
     ZLError,
     DCtx,
     GpuBatch,
+    GpuEncoder,
     decompress,
     xxh3_64_device,
     get_decompressed_size,

@@ -54,6 +54,14 @@ def library():
         "ozl_gpu_batch_error": ([vp], ctypes.c_char_p),
         "ozl_gpu_version": ([], ctypes.c_char_p),
         "ozl_gpu_xxh3_64": ([vp, sz, vp], ZLReport),
+        "ozl_gpu_batch_profile": ([vp, vp, vp, vp, vp, sz], ZLReport),
+        "ozl_gpu_kind_name": ([ctypes.c_int], ctypes.c_char_p),
+        "ozl_gpu_batch_run_host": ([vp, vp, sz, vp, sz, vp, ctypes.c_int], ZLReport),
+        "ozl_gpu_encoder_create": ([], vp),
+        "ozl_gpu_encoder_free": ([vp], None),
+        "ozl_gpu_compress_bound": ([sz], sz),
+        "ozl_gpu_compress_batch": ([vp, sz, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, vp], ZLReport),
+        "ozl_gpu_encoder_error": ([vp], ctypes.c_char_p),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -188,9 +196,60 @@ class GpuBatch:
             self._raise(rep)
         return rep.value
 
+    def profile(self, stream=0, capacity=4096):
+        """Per-launch (kind name, milliseconds, algorithmic bytes), run one by one."""
+        ms = (ctypes.c_float * capacity)()
+        kinds = (ctypes.c_int * capacity)()
+        nb = (ctypes.c_uint64 * capacity)()
+        rep = self._lib.ozl_gpu_batch_profile(self._h, stream, ms, kinds, nb, capacity)
+        if rep.code:
+            self._raise(rep)
+        n = min(rep.value, capacity)
+        return [(self._lib.ozl_gpu_kind_name(kinds[i]).decode(), ms[i], nb[i]) for i in range(n)]
+
+    def run_host(self, h_in_ptr, in_bytes, h_out_ptr, out_bytes, stream=0, graph=True):
+        """Host buffers in and out around one planned run (copies included)."""
+        rep = self._lib.ozl_gpu_batch_run_host(self._h, h_in_ptr, in_bytes, h_out_ptr, out_bytes, stream,
+                                               1 if graph else 0)
+        if rep.code:
+            self._raise(rep)
+        return rep.value
+
     def launches(self):
         return self._lib.ozl_gpu_batch_launches(self._h)
 
     def sizes(self, n):
         p = self._lib.ozl_gpu_batch_sizes(self._h)
         return [p[i] for i in range(n)]
+
+
+class GpuEncoder:
+    """Batched compression on the device (frames identical to the reference's)."""
+
+    def __init__(self):
+        self._lib = library()
+        self._h = self._lib.ozl_gpu_encoder_create()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.ozl_gpu_encoder_free(h)
+            self._h = None
+
+    def bound(self, src_bytes):
+        return self._lib.ozl_gpu_compress_bound(src_bytes)
+
+    def compress_batch(self, src_ptrs, nb_elts, elt_widths, recipes, dst_ptrs, dst_caps, checksums=True, stream=0):
+        """Device pointers in and out; returns the list of frame sizes."""
+        n = len(src_ptrs)
+        sp = (ctypes.c_void_p * n)(*src_ptrs)
+        ne = (ctypes.c_size_t * n)(*nb_elts)
+        ew = (ctypes.c_int * n)(*elt_widths)
+        rc = (ctypes.c_int * n)(*recipes)
+        dp = (ctypes.c_void_p * n)(*dst_ptrs)
+        dc = (ctypes.c_size_t * n)(*dst_caps)
+        fs = (ctypes.c_size_t * n)()
+        rep = self._lib.ozl_gpu_compress_batch(self._h, n, sp, ne, ew, rc, dp, dc, fs, 1 if checksums else 0, stream)
+        if rep.code:
+            raise ZLError(rep.code, self._lib.ozl_gpu_encoder_error(self._h).decode())
+        return [fs[i] for i in range(n)]

@@ -14,6 +14,7 @@
 #include "../../include/openzl_gb300.h"
 #include "dec_exec.h"
 #include "dec_plan.h"
+#include "enc_engine.h"
 
 namespace {
 
@@ -184,6 +185,11 @@ struct ZL_DCtx_s {
     }
 };
 
+struct OZL_GpuEncoder_s {
+    ozl::EncodeBatch batch;
+    std::string err;
+};
+
 extern "C" {
 
 int ZL_isError(ZL_Report r) { return r._code != ZL_ErrorCode_no_error; }
@@ -211,6 +217,47 @@ const char* ZL_ErrorCode_toString(ZL_ErrorCode code)
         case ZL_ErrorCode_temporaryLibraryLimitation: return "Temporary library limitation";
         default: return "Error";
     }
+}
+
+OZL_GpuEncoder* ozl_gpu_encoder_create(void)
+{
+    try {
+        return new OZL_GpuEncoder_s();
+    } catch (...) {
+        return nullptr;
+    }
+}
+
+void ozl_gpu_encoder_free(OZL_GpuEncoder* e) { delete e; }
+
+size_t ozl_gpu_compress_bound(size_t srcBytes) { return ozl::encodeBound(srcBytes); }
+
+const char* ozl_gpu_encoder_error(const OZL_GpuEncoder* e) { return e ? e->err.c_str() : ""; }
+
+ZL_Report ozl_gpu_compress_batch(OZL_GpuEncoder* e, size_t n, const void* const* d_srcs, const size_t* nbElts,
+                                 const int* eltWidths, const int* recipes, void* const* d_dsts, const size_t* caps,
+                                 size_t* frameSizes, int checksums, void* stream)
+{
+    if (!e || (n && (!d_srcs || !nbElts || !eltWidths || !recipes || !d_dsts || !caps || !frameSizes)))
+        return fail(ZL_ErrorCode_parameter_invalid);
+    std::vector<ozl::EncFrameSpec> specs(n);
+    for (size_t i = 0; i < n; i++) {
+        int const w = eltWidths[i];
+        if (!(w == 0 || w == 1 || w == 2 || w == 4 || w == 8)) return fail(ZL_ErrorCode_parameter_invalid);
+        specs[i] = ozl::EncFrameSpec{ static_cast<const uint8_t*>(d_srcs[i]), nbElts[i], uint32_t(w ? w : 1), w == 0,
+                                      recipes[i] };
+    }
+    std::vector<size_t> sizes;
+    e->err.clear();
+    int rc = e->batch.compress(specs, reinterpret_cast<uint8_t* const*>(d_dsts), caps, checksums != 0,
+                               static_cast<cudaStream_t>(stream), sizes, e->err);
+    if (rc) return fail(rc);
+    size_t total = 0;
+    for (size_t i = 0; i < n; i++) {
+        frameSizes[i] = sizes[i];
+        total += sizes[i];
+    }
+    return ok(total);
 }
 
 const char* ozl_gpu_version(void) { return "openzl_gb300 0.1 (sm_103a)"; }
@@ -379,6 +426,58 @@ ZL_Report ozl_gpu_batch_check(OZL_GpuBatch* b, void* stream)
 }
 
 size_t ozl_gpu_batch_launches(const OZL_GpuBatch* b) { return b ? size_t(b->launches) : 0; }
+
+const char* ozl_gpu_kind_name(int kind)
+{
+    static const char* names[] = { "copy", "constant", "fse", "huffman", "flatpack", "tokenize",
+                                   "float_deconstruct", "transpose", "numeric_pipeline", "xxh3" };
+    return (kind >= 0 && kind < ozl::KIND_COUNT) ? names[kind] : "?";
+}
+
+ZL_Report ozl_gpu_batch_profile(OZL_GpuBatch* b, void* stream, float* ms, int* kinds, uint64_t* bytes,
+                                size_t capacity)
+{
+    if (!b) return fail(ZL_ErrorCode_parameter_invalid);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    size_t const n = b->layout.launches.size();
+    std::vector<cudaEvent_t> ev(n + 1);
+    for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return fail(ZL_ErrorCode_GENERIC);
+    bool okRun = cudaMemsetAsync(b->status.data(), 0, 4, s) == cudaSuccess;
+    cudaEventRecord(ev[0], s);
+    for (size_t i = 0; i < n && okRun; i++) {
+        okRun = ozl::runOneLaunch(b->layout, i, b->pool.data(), b->scratch.data(),
+                                  reinterpret_cast<uint32_t*>(b->status.data()), s) >= 0;
+        cudaEventRecord(ev[i + 1], s);
+    }
+    okRun = okRun && cudaStreamSynchronize(s) == cudaSuccess;
+    for (size_t i = 0; i < n && i < capacity && okRun; i++) {
+        float t = 0;
+        cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+        if (ms) ms[i] = t;
+        if (kinds) kinds[i] = b->layout.launches[i].kind;
+        if (bytes) bytes[i] = b->layout.launches[i].algoBytes;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (!okRun) return fail(ZL_ErrorCode_GENERIC);
+    return ok(n);
+}
+
+ZL_Report ozl_gpu_batch_run_host(OZL_GpuBatch* b, const void* h_in, size_t inBytes, void* h_out, size_t outBytes,
+                                 void* stream, int useGraph)
+{
+    if (!b || b->dFrames.empty()) return fail(ZL_ErrorCode_parameter_invalid);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (inBytes
+        && cudaMemcpyAsync(const_cast<uint8_t*>(b->dFrames[0]), h_in, inBytes, cudaMemcpyHostToDevice, s)
+                   != cudaSuccess)
+        return fail(ZL_ErrorCode_GENERIC);
+    ZL_Report r = b->run(s, useGraph != 0);
+    if (ZL_isError(r)) return r;
+    if (outBytes && cudaMemcpyAsync(h_out, b->dOuts[0], outBytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return fail(ZL_ErrorCode_GENERIC);
+    return b->check(s);
+}
 
 const size_t* ozl_gpu_batch_sizes(const OZL_GpuBatch* b) { return b ? b->sizes.data() : nullptr; }
 

@@ -17,6 +17,16 @@ long runLaunches(const DeviceLayout& layout, uint8_t* dPool, uint8_t* dScratch, 
 // Call once per device before the first launch (and before graph capture).
 cudaError_t prepareKernels();
 
+// Enqueues launch `i` of `layout` alone (the building block of runLaunches).
+// Returns the number of kernels it issued, or a negative value on failure.
+long runOneLaunch(const DeviceLayout& layout, size_t i, uint8_t* dPool, uint8_t* dScratch, uint32_t* dStatus,
+                  cudaStream_t stream);
+
+// Launch helpers shared with the encoder.
+void launchCopy(const CopyTask* tasks, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
+void launchHash(const HashTask* tasks, uint32_t nbTasks, const TileRef* blocks, uint32_t nbBlocks,
+                uint32_t* status, cudaStream_t s);
+
 // XXH3-64 of `len` device bytes at `data`; the hash lands in *dHashOut.
 // Needs 256 + 72 * ceil(len / 1 KiB) bytes of device scratch. Synchronizes `s`.
 cudaError_t xxh3Device(const uint8_t* data, uint64_t len, uint64_t* dHashOut, uint8_t* dScratch,

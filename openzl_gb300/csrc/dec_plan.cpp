@@ -810,6 +810,22 @@ struct Buckets {
 
 uint32_t ceilDiv(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }
 
+// Algorithmic bytes of one task: what it must read plus what it must write.
+uint64_t taskBytes(const CopyTask& t) { return 2 * t.bytes; }
+uint64_t taskBytes(const ConstTask& t) { return t.n * t.w + t.w; }
+uint64_t taskBytes(const FseTask& t) { return uint64_t(t.bitsSize) + t.dstSize + 2ull * t.nbSym; }
+uint64_t taskBytes(const HufTask& t) { return uint64_t(t.bitsSize) + t.dstSize + t.nbWeights; }
+uint64_t taskBytes(const FlatpackTask& t) { return t.n + (t.n * t.nbBits + 7) / 8 + t.alphabetSize; }
+uint64_t taskBytes(const TokenizeTask& t) { return t.n * (t.w + t.iw) + uint64_t(t.alphabetSize) * t.w; }
+uint64_t taskBytes(const FloatDecTask& t) { return t.n * (t.eltType == 0 ? 8 : 4); }
+uint64_t taskBytes(const TransposeTask& t) { return 2 * t.n * t.W; }
+uint64_t taskBytes(const NumPipeTask& t)
+{
+    uint64_t const ns = t.delta ? (t.n ? t.n - 1 : 0) : t.n;
+    uint64_t const src = t.srcMode == SRC_BITPACK ? (ns * t.nbBits + 7) / 8 : ns * t.w;
+    return src + t.n * t.w;
+}
+
 } // namespace
 
 int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* const* dOuts,
@@ -1028,6 +1044,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         Launch L{};
         L.kind = kind;
         L.level = lv;
+        for (auto& t : tasks) L.algoBytes += taskBytes(t);
         L.taskOff = pool.put(tasks);
         L.nbTasks = uint32_t(tasks.size());
         L.tileOff = pool.put(tiles);
@@ -1056,6 +1073,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
             for (auto& t : tasks) tlMax = std::max<uint32_t>(tlMax, t.tableLog);
             L.param0 = tlMax;
         }
+        for (auto& t : tasks) L.algoBytes += taskBytes(t);
         L.kind = kind;
         L.level = lv;
         L.taskOff = pool.put(tasks);
@@ -1095,6 +1113,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         scratch += ((uint64_t)blocks.size() * 64 + 255) & ~uint64_t(255);
         for (HashTask& t : ht) t.blockSums = reinterpret_cast<uint64_t*>(dScratch + sumsOff) + 8ull * t.blockBase;
         Launch L{};
+        for (const HashTask& t : ht) L.algoBytes += t.len;
         L.kind = KIND_HASH;
         L.level = hashLevel;
         L.taskOff = pool.put(ht);

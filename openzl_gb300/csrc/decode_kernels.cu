@@ -856,7 +856,20 @@ cudaError_t prepareKernels()
 long runLaunches(const DeviceLayout& L, uint8_t* dPool, uint8_t* dScratch, uint32_t* dStatus, cudaStream_t s)
 {
     long count = 0;
-    for (const Launch& l : L.launches) {
+    for (size_t i = 0; i < L.launches.size(); i++) {
+        long const n = runOneLaunch(L, i, dPool, dScratch, dStatus, s);
+        if (n < 0) return -1;
+        count += n;
+    }
+    return count;
+}
+
+long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dScratch, uint32_t* dStatus,
+                  cudaStream_t s)
+{
+    long count = 0;
+    {
+        const Launch& l = L.launches[li];
         const void* tasks = dPool + l.taskOff;
         const TileRef* tiles = reinterpret_cast<const TileRef*>(dPool + l.tileOff);
         switch (l.kind) {
@@ -922,8 +935,20 @@ long runLaunches(const DeviceLayout& L, uint8_t* dPool, uint8_t* dScratch, uint3
 } // namespace ozl
 
 // ---------------------------------------------------------------------------
-// standalone XXH3-64 of a device buffer
+// standalone XXH3-64 of a device buffer, and launch helpers for the encoder
 namespace ozl {
+void launchCopy(const CopyTask* tasks, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s)
+{
+    if (nbTiles) kCopy<<<nbTiles, 256, 0, s>>>(tasks, tiles);
+}
+
+void launchHash(const HashTask* tasks, uint32_t nbTasks, const TileRef* blocks, uint32_t nbBlocks, uint32_t* status,
+                cudaStream_t s)
+{
+    if (nbBlocks) kHashBlocks<<<(nbBlocks * 32 + 255) / 256, 256, 0, s>>>(tasks, blocks, nbBlocks);
+    if (nbTasks) kHashFinish<<<(nbTasks * 32 + 255) / 256, 256, 0, s>>>(tasks, nbTasks, status);
+}
+
 cudaError_t xxh3Device(const uint8_t* data, uint64_t len, uint64_t* dHashOut, uint8_t* dScratch,
                        uint64_t scratchBytes, cudaStream_t s)
 {

@@ -1,0 +1,1159 @@
+// Batched GPU compressor: host orchestration.
+//
+// One compress() call encodes many frames in a fixed sequence of phases, each
+// one batched across all frames:
+//   A. front end on the GPU: per-frame maximum (for bit packing), then
+//      delta/zigzag with byte planes, bit packing or plain output; content
+//      checksums of the inputs;
+//   B. graph discovery on the host: which streams enter an entropy graph and
+//      how they are chunked (sizes only);
+//   C. 256-bin histograms of every chunk on the GPU;
+//   D. per-chunk codec choice and coding tables on the host (the small,
+//      exactly-specified arithmetic of the reference);
+//   E. entropy bitstreams (FSE, Huffman, bit packing, flatpack) on the GPU;
+//   F. graph replay on the host, in the reference's node-creation order
+//      (src/openzl/compress/cctx.c:700-1230), giving each frame's decoder map,
+//      codec headers and stored streams (encode_frameheader.c:441-834);
+//   G. frame assembly and block/header checksums on the GPU.
+#include "enc_engine.h"
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+
+#include "dec_exec.h"
+#include "enc_exec.h"
+#include "enc_tables.h"
+#include "enc_tasks.h"
+
+namespace ozl {
+
+namespace {
+
+enum : int { T_SERIAL = 1, T_STRUCT = 2, T_NUMERIC = 4 };
+enum : uint32_t {
+    TR_DELTA = 1, TR_ZIGZAG = 3, TR_TSPLIT = 4, TR_CONV_STRUCT_TO_SERIAL = 6, TR_CONV_NUM_TO_STRUCT = 8,
+    TR_CONV_NUM_TO_SERIAL = 10, TR_BITPACK_SERIAL = 27, TR_BITPACK_INT = 28, TR_FLATPACK = 29, TR_SPLITN = 40,
+    TR_CONST_SERIAL = 44, TR_FSE = 49, TR_HUF = 50, TR_NCOUNT = 52,
+};
+constexpr uint64_t kMinStream = 10;   // ZL_MINSTREAMSIZE_DEFAULT
+constexpr uint64_t kChunk = 1 << 15;  // entropy chunk size
+constexpr uint64_t kMinChunking = 100000;
+
+struct DevBuf {
+    uint8_t* p = nullptr;
+    size_t cap = 0;
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+    bool reserve(size_t bytes)
+    {
+        bytes += 256;
+        if (bytes <= cap) return true;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) return false;
+        cap = bytes;
+        return true;
+    }
+    uint8_t* data() const { return p + 64; }
+};
+
+// bump allocator over a size pass / real pass
+struct Bump {
+    uint8_t* base = nullptr;
+    size_t used = 0;
+    uint8_t* take(size_t bytes, size_t align = 64)
+    {
+        used = (used + align - 1) & ~(align - 1);
+        uint8_t* r = base ? base + used : nullptr;
+        used += bytes;
+        return r;
+    }
+};
+
+struct Piece {
+    const uint8_t* dev = nullptr;
+    const uint8_t* host = nullptr;
+    uint64_t bytes = 0;
+};
+
+enum : int { M_FSE = 0, M_HUF, M_CONSTANT, M_FLATPACK, M_BITPACK };
+
+struct Job {
+    const uint8_t* dsrc = nullptr;    // device content
+    std::vector<uint8_t> hsrc;        // host content (Huffman weights)
+    const uint8_t* dstaged = nullptr; // device copy of hsrc
+    uint64_t n = 0;
+    int mode = M_FSE;
+    ent::Histo hist{};
+    int codec = ent::CC_STORE;
+    // FSE
+    int16_t norm[256];
+    unsigned tl = 0, nbStates = 2;
+    std::unique_ptr<ent::FseCTable> fct;
+    uint8_t ncount[600];
+    size_t ncountSize = 0;
+    // Huffman
+    std::unique_ptr<ent::HufCTable> hct;
+    std::vector<uint8_t> weights;
+    int weightsJob = -1;
+    bool x4 = false;
+    uint8_t jump[6];
+    // bit packing / flatpack
+    unsigned packBits = 0;
+    uint64_t packBytes = 0;
+    uint8_t map[256];
+    std::vector<uint8_t> alphabet;
+    uint8_t constVal = 0;
+    // device outputs and sizes
+    uint8_t* out = nullptr;
+    uint32_t sizeSlot = 0;
+    uint32_t sizes[4] = { 0, 0, 0, 0 };
+    const uint8_t* dTable = nullptr;
+};
+
+struct RStream {
+    int type;
+    uint32_t w;
+    uint64_t n;
+    std::vector<Piece> pieces; // content (contiguous device pointer is pieces[0] when single)
+    bool store = false;
+    uint64_t bytes() const { return n * w; }
+};
+
+struct RNode {
+    uint32_t trid;
+    uint8_t hdr[16];
+    size_t hsz = 0;
+    int in;
+    int outStart, nbOut, nbSO;
+};
+
+// Per-frame front-end plan (phase A).
+struct Front {
+    int mode = -1;            // -1 none, else EncOut
+    bool delta = false, zigzag = false;
+    uint8_t* out = nullptr;
+    uint64_t n = 0;           // output elements
+    uint64_t planeStride = 0;
+    unsigned nbBits = 0;
+    uint64_t outBytes = 0;
+    uint32_t maxSlot = 0;
+    bool needMax = false;
+};
+
+} // namespace
+
+struct EncodeBatch::Impl {
+    DevBuf bufA, bufE, bufF, bufSmall;
+    std::vector<Job> jobs;           // data chunks (discovery order), then nested weights jobs
+    size_t nbDataJobs = 0;
+    bool checksums = true;
+};
+
+EncodeBatch::EncodeBatch() : impl_(new Impl) {}
+EncodeBatch::~EncodeBatch() { delete impl_; }
+
+size_t encodeBound(size_t srcBytes) { return srcBytes + srcBytes / 16 + 4096; }
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Graph engine (one frame). In discovery mode entropy chunks are registered
+// as jobs; in replay mode their decisions and encoded outputs are used.
+struct Engine {
+    bool discover;
+    std::vector<Job>* jobs;
+    size_t* jobCursor;          // next data-job index (same order in both modes)
+    std::vector<RStream> s;
+    std::vector<RNode> nd;
+    const Front* front;
+    int err = 0;
+
+    int newStream(int type, uint32_t w, uint64_t n)
+    {
+        s.push_back(RStream{ type, w, n, {}, false });
+        return int(s.size() - 1);
+    }
+    RNode& newNode(uint32_t trid, int in, int nbSO)
+    {
+        RNode x{};
+        x.trid = trid;
+        x.in = in;
+        x.outStart = int(s.size());
+        x.nbSO = nbSO;
+        nd.push_back(x);
+        return nd.back();
+    }
+    static std::vector<Piece> slice(const std::vector<Piece>& p, uint64_t off, uint64_t len)
+    {
+        // contiguous single-piece sources only
+        std::vector<Piece> r;
+        if (p.empty()) return r;
+        Piece x = p[0];
+        if (x.dev) x.dev += off;
+        if (x.host) x.host += off;
+        x.bytes = len;
+        r.push_back(x);
+        return r;
+    }
+
+    int convNumToSerial(int in)
+    {
+        RNode& x = newNode(TR_CONV_NUM_TO_SERIAL, in, 1);
+        x.hdr[0] = uint8_t(ent::nextPow2Bits(s[in].w));
+        x.hsz = 1;
+        int o = newStream(T_SERIAL, 1, s[in].bytes());
+        s[o].pieces = s[in].pieces;
+        nd.back().nbOut = 1;
+        return o;
+    }
+    int convStructToSerial(int in)
+    {
+        RNode& x = newNode(TR_CONV_STRUCT_TO_SERIAL, in, 1);
+        uint64_t v = s[in].w;
+        size_t k = 0;
+        while (v >= 0x80) { x.hdr[k++] = uint8_t(v | 0x80); v >>= 7; }
+        x.hdr[k++] = uint8_t(v);
+        x.hsz = k;
+        int o = newStream(T_SERIAL, 1, s[in].bytes());
+        s[o].pieces = s[in].pieces;
+        nd.back().nbOut = 1;
+        return o;
+    }
+    int convNumToStruct(int in)
+    {
+        newNode(TR_CONV_NUM_TO_STRUCT, in, 1);
+        int o = newStream(T_STRUCT, s[in].w, s[in].n);
+        s[o].pieces = s[in].pieces;
+        nd.back().nbOut = 1;
+        return o;
+    }
+    // implicit conversion (src/openzl/compress/implicit_conversion.c:18-34)
+    int convertFor(int sid, int mask)
+    {
+        int const t = s[sid].type;
+        if (t & mask) return sid;
+        if ((t & T_NUMERIC) && (mask & T_STRUCT)) return convNumToStruct(sid);
+        if ((t & T_STRUCT) && (mask & T_SERIAL)) return convStructToSerial(sid);
+        if ((t & T_NUMERIC) && (mask & T_SERIAL)) return convNumToSerial(sid);
+        err = 43;
+        return sid;
+    }
+
+    // ---- graphs ----------------------------------------------------------
+    enum G {
+        G_STORE, G_SERIAL_STORE, G_FSE, G_HUF, G_CONSTANT, G_BITPACK, G_FLATPACK, G_NCOUNT, G_TSPLIT_FSE,
+        G_TSPLIT_STORE, G_BITPACK_HUF, G_JOB
+    };
+    struct Succ {
+        int g, sid, job;
+    };
+
+    void runSuccs(std::vector<Succ>& l)
+    {
+        // successors run in edge-creation (stream id) order (cctx.c:660-690)
+        std::stable_sort(l.begin(), l.end(), [](const Succ& a, const Succ& b) { return a.sid < b.sid; });
+        for (const Succ& x : l) {
+            if (err) return;
+            runSuccessor(x.g, x.sid, x.job);
+        }
+    }
+
+    // small single inputs are stored (cctx.c:1125-1140)
+    void runSuccessor(int g, int sid, int job = -1)
+    {
+        if (err) return;
+        if (g != G_SERIAL_STORE && s[sid].bytes() < kMinStream) g = G_STORE;
+        if (g == G_STORE && s[sid].bytes() < kMinStream) {
+            graph(G_SERIAL_STORE, sid, -1);
+            return;
+        }
+        graph(g, sid, job);
+    }
+
+    Job* jobFor(int sid, int mode, int explicitJob)
+    {
+        if (explicitJob >= 0) return &(*jobs)[size_t(explicitJob)];
+        size_t const j = (*jobCursor)++;
+        if (discover) {
+            Job job;
+            job.n = s[sid].n;
+            job.mode = mode;
+            job.dsrc = s[sid].pieces.empty() ? nullptr : s[sid].pieces[0].dev;
+            jobs->push_back(std::move(job));
+            return nullptr;
+        }
+        return &(*jobs)[j];
+    }
+
+    // entropyCompressChunk (encode_entropy_binding.c:602-762)
+    void entropyChunk(int sid, bool huf, std::vector<Succ>& succ, int explicitJob)
+    {
+        if (s[sid].n <= 1) {
+            succ.push_back({ G_STORE, sid, -1 });
+            return;
+        }
+        Job* j = jobFor(sid, huf ? M_HUF : M_FSE, explicitJob);
+        if (!j) return; // discovery
+        switch (j->codec) {
+            case ent::CC_STORE: succ.push_back({ G_STORE, sid, -1 }); return;
+            case ent::CC_CONSTANT: succ.push_back({ G_JOB, sid, int(j - jobs->data()) | (G_CONSTANT << 24) }); return;
+            case ent::CC_FLATPACK: succ.push_back({ G_JOB, sid, int(j - jobs->data()) | (G_FLATPACK << 24) }); return;
+            case ent::CC_BITPACK: succ.push_back({ G_JOB, sid, int(j - jobs->data()) | (G_BITPACK << 24) }); return;
+            case ent::CC_FSE: {
+                RNode& x = newNode(TR_FSE, sid, 2);
+                x.hdr[0] = uint8_t(j->nbStates);
+                size_t const nbBytes = size_t(ent::nextPow2Bits(j->n + 1) + 7) / 8;
+                for (size_t b = 0; b < nbBytes; b++) x.hdr[1 + b] = uint8_t(j->n >> (8 * b));
+                x.hsz = nbBytes + 1;
+                int ns = newStream(T_NUMERIC, 2, j->hist.maxSym + 1);
+                s[ns].pieces.push_back(Piece{ nullptr, reinterpret_cast<const uint8_t*>(j->norm), 2ull * (j->hist.maxSym + 1) });
+                int bs = newStream(T_SERIAL, 1, j->sizes[0]);
+                s[bs].pieces.push_back(Piece{ j->out, nullptr, j->sizes[0] });
+                nd.back().nbOut = 2;
+                succ.push_back({ G_NCOUNT, ns, int(j - jobs->data()) });
+                succ.push_back({ G_STORE, bs, -1 });
+                return;
+            }
+            case ent::CC_HUF: {
+                RNode& x = newNode(TR_HUF, sid, 2);
+                x.hdr[0] = uint8_t(j->x4 ? 1 : 0);
+                size_t const nbBytes = size_t(ent::nextPow2Bits(j->n + 1) + 7) / 8;
+                for (size_t b = 0; b < nbBytes; b++) x.hdr[1 + b] = uint8_t(j->n >> (8 * b));
+                x.hsz = nbBytes + 1;
+                int ws = newStream(T_NUMERIC, 1, j->weights.size());
+                s[ws].pieces.push_back(Piece{ nullptr, j->weights.data(), j->weights.size() });
+                uint64_t total = 0;
+                for (int k = 0; k < (j->x4 ? 4 : 1); k++) total += j->sizes[k];
+                int bs = newStream(T_SERIAL, 1, total + (j->x4 ? 6 : 0));
+                if (j->x4) {
+                    s[bs].pieces.push_back(Piece{ nullptr, j->jump, 6 });
+                    uint32_t const cap = hufEncStreamCap(uint32_t((j->n + 3) / 4));
+                    for (int k = 0; k < 4; k++) s[bs].pieces.push_back(Piece{ j->out + 16 + uint64_t(k) * cap, nullptr, j->sizes[k] });
+                } else {
+                    s[bs].pieces.push_back(Piece{ j->out, nullptr, j->sizes[0] });
+                }
+                nd.back().nbOut = 2;
+                succ.push_back({ G_FSE, ws, j->weightsJob });
+                succ.push_back({ G_STORE, bs, -1 });
+                return;
+            }
+        }
+    }
+
+    void entropyGraph(int sid, bool huf, int explicitJob)
+    {
+        std::vector<Succ> succ;
+        if (s[sid].w == 1 && s[sid].type != T_SERIAL)
+            sid = s[sid].type == T_NUMERIC ? convNumToSerial(sid) : convStructToSerial(sid);
+        if (s[sid].w != 1) { err = 81; return; }
+        uint64_t const n = s[sid].n;
+        if (n < kMinChunking) {
+            entropyChunk(sid, huf, succ, explicitJob);
+        } else {
+            uint64_t const nb = (n + kChunk - 1) / kChunk;
+            newNode(TR_SPLITN, sid, 0);
+            int const first = int(s.size());
+            uint64_t pos = 0;
+            std::vector<Piece> src = s[sid].pieces;
+            for (uint64_t k = 0; k < nb; k++) {
+                uint64_t const len = k + 1 < nb ? kChunk : n - pos;
+                int o = newStream(T_SERIAL, 1, len);
+                s[o].pieces = slice(src, pos, len);
+                pos += len;
+            }
+            nd.back().nbOut = int(nb);
+            for (uint64_t k = 0; k < nb; k++) entropyChunk(first + int(k), huf, succ, -1);
+        }
+        runSuccs(succ);
+    }
+
+    void graph(int g, int sid, int job)
+    {
+        std::vector<Succ> succ;
+        if (g == G_JOB) {
+            g = job >> 24;
+            job &= 0xffffff;
+        }
+        switch (g) {
+            case G_SERIAL_STORE:
+                sid = convertFor(sid, T_SERIAL);
+                s[sid].store = true;
+                return;
+            case G_STORE: runSuccessor(G_SERIAL_STORE, sid); return;
+            case G_FSE: sid = convertFor(sid, T_SERIAL); entropyGraph(sid, false, job); return;
+            case G_HUF: entropyGraph(sid, true, job); return;
+            case G_CONSTANT: {
+                Job& j = (*jobs)[size_t(job)];
+                RNode& x = newNode(TR_CONST_SERIAL, sid, 1);
+                uint64_t v = s[sid].n;
+                size_t k = 0;
+                while (v >= 0x80) { x.hdr[k++] = uint8_t(v | 0x80); v >>= 7; }
+                x.hdr[k++] = uint8_t(v);
+                x.hsz = k;
+                int o = newStream(T_SERIAL, 1, 1);
+                s[o].pieces.push_back(Piece{ nullptr, &j.constVal, 1 });
+                nd.back().nbOut = 1;
+                runSuccessor(G_SERIAL_STORE, o);
+                return;
+            }
+            case G_BITPACK: {
+                Job& j = (*jobs)[size_t(job)];
+                RNode& x = newNode(TR_BITPACK_SERIAL, sid, 1);
+                uint64_t const maxN = j.packBytes * 8 / j.packBits;
+                x.hdr[0] = uint8_t(j.packBits - 1);
+                x.hsz = 1;
+                if (maxN > j.n) { x.hdr[1] = uint8_t(maxN - j.n); x.hsz = 2; }
+                int o = newStream(T_SERIAL, 1, j.packBytes);
+                s[o].pieces.push_back(Piece{ j.out, nullptr, j.packBytes });
+                nd.back().nbOut = 1;
+                runSuccessor(G_SERIAL_STORE, o);
+                return;
+            }
+            case G_FLATPACK: {
+                Job& j = (*jobs)[size_t(job)];
+                sid = convertFor(sid, T_SERIAL);
+                newNode(TR_FLATPACK, sid, 2);
+                int a = newStream(T_SERIAL, 1, j.alphabet.size());
+                s[a].pieces.push_back(Piece{ nullptr, j.alphabet.data(), j.alphabet.size() });
+                int p = newStream(T_SERIAL, 1, j.packBytes);
+                s[p].pieces.push_back(Piece{ j.out, nullptr, j.packBytes });
+                nd.back().nbOut = 2;
+                succ.push_back({ G_SERIAL_STORE, a, -1 });
+                succ.push_back({ G_SERIAL_STORE, p, -1 });
+                runSuccs(succ);
+                return;
+            }
+            case G_NCOUNT: {
+                Job& j = (*jobs)[size_t(job)];
+                newNode(TR_NCOUNT, sid, 1);
+                int o = newStream(T_SERIAL, 1, j.ncountSize);
+                s[o].pieces.push_back(Piece{ nullptr, j.ncount, j.ncountSize });
+                nd.back().nbOut = 1;
+                runSuccessor(G_SERIAL_STORE, o);
+                return;
+            }
+            case G_TSPLIT_FSE:
+            case G_TSPLIT_STORE: {
+                sid = convertFor(sid, T_STRUCT);
+                uint32_t const W = s[sid].w;
+                uint64_t const m = s[sid].n;
+                newNode(TR_TSPLIT, sid, 0);
+                int const first = int(s.size());
+                for (uint32_t b = 0; b < W; b++) {
+                    int o = newStream(T_SERIAL, 1, m);
+                    if (front->mode == EOUT_PLANES) s[o].pieces.push_back(Piece{ front->out + b * front->planeStride, nullptr, m });
+                }
+                nd.back().nbOut = int(W);
+                for (uint32_t b = 0; b < W; b++) succ.push_back({ g == G_TSPLIT_FSE ? G_FSE : G_STORE, first + int(b), -1 });
+                runSuccs(succ);
+                return;
+            }
+            case G_BITPACK_HUF: {
+                sid = convertFor(sid, T_NUMERIC);
+                RNode& x = newNode(TR_BITPACK_INT, sid, 1);
+                static const uint8_t lg[9] = { 0, 0, 1, 0, 2, 0, 0, 0, 3 };
+                uint64_t const n = s[sid].n;
+                uint64_t const bytes = (n * front->nbBits + 7) / 8;
+                uint64_t const maxN = bytes * 8 / front->nbBits;
+                x.hdr[0] = uint8_t((lg[s[sid].w] << 6) | (front->nbBits - 1));
+                x.hsz = 1;
+                if (maxN > n) { x.hdr[1] = uint8_t(maxN - n); x.hsz = 2; }
+                int o = newStream(T_SERIAL, 1, bytes);
+                s[o].pieces.push_back(Piece{ front->out, nullptr, bytes });
+                nd.back().nbOut = 1;
+                runSuccessor(job == 1 ? G_STORE : G_HUF, o);
+                return;
+            }
+            default: err = 32; return;
+        }
+    }
+
+    // Pipeline steps of the numeric recipes, each hop a successor.
+    void pipeline(int recipe, int in)
+    {
+        int cur = in;
+        auto hop = [&](bool first) -> bool {
+            if (!first && s[cur].bytes() < kMinStream) {
+                runSuccessor(G_STORE, cur);
+                return false;
+            }
+            return true;
+        };
+        bool const delta = recipe == RC_DZ_TSPLIT_FSE || recipe == RC_DZ_BITPACK_HUF || recipe == RC_D_TSPLIT_FSE
+                || recipe == RC_D_BITPACK_HUF || recipe == RC_DELTA_STORE;
+        bool const zz = recipe == RC_DZ_TSPLIT_FSE || recipe == RC_DZ_BITPACK_HUF || recipe == RC_ZIGZAG_STORE;
+        bool first = true;
+        if (delta) {
+            RNode& x = newNode(TR_DELTA, cur, 1);
+            (void)x;
+            uint64_t const n = s[cur].n;
+            int o = newStream(T_NUMERIC, s[cur].w, n ? n - 1 : 0);
+            nd.back().nbOut = 1;
+            // delta output content: the front end writes it when it is the
+            // last step (plain) or when it is stored because it is small
+            if (front->mode == EOUT_PLAIN && !front->zigzag) s[o].pieces.push_back(Piece{ front->out, nullptr, front->outBytes });
+            cur = o;
+            first = false;
+            if (!hop(false)) return;
+        }
+        if (zz) {
+            if (!first && !hop(false)) return;
+            newNode(TR_ZIGZAG, cur, 1);
+            int o = newStream(T_NUMERIC, s[cur].w, s[cur].n);
+            nd.back().nbOut = 1;
+            if (front->mode == EOUT_PLAIN) s[o].pieces.push_back(Piece{ front->out, nullptr, front->outBytes });
+            cur = o;
+            first = false;
+        }
+        switch (recipe) {
+            case RC_DZ_TSPLIT_FSE:
+            case RC_D_TSPLIT_FSE: {
+                if (!hop(first)) return;
+                cur = convNumToStruct(cur);
+                runSuccessor(G_TSPLIT_FSE, cur);
+                return;
+            }
+            case RC_TSPLIT_STORE: {
+                if (!hop(first)) return;
+                cur = convNumToStruct(cur);
+                runSuccessor(G_TSPLIT_STORE, cur);
+                return;
+            }
+            case RC_DZ_BITPACK_HUF:
+            case RC_D_BITPACK_HUF: runSuccessor(G_BITPACK_HUF, cur, 0); return;
+            case RC_BITPACK_STORE: runSuccessor(G_BITPACK_HUF, cur, 1); return;
+            case RC_DELTA_STORE:
+            case RC_ZIGZAG_STORE: runSuccessor(G_STORE, cur); return;
+            default: err = 32; return;
+        }
+    }
+};
+
+uint8_t typeCode(int t) { return t == T_SERIAL ? 0 : (t == T_STRUCT ? 1 : 2); }
+
+void pushVarint(std::vector<uint8_t>& o, uint64_t v)
+{
+    while (v >= 0x80) {
+        o.push_back(uint8_t(v | 0x80));
+        v >>= 7;
+    }
+    o.push_back(uint8_t(v));
+}
+
+void pushBits(std::vector<uint8_t>& o, const std::vector<uint32_t>& v, int nbBits)
+{
+    size_t const base = o.size();
+    o.resize(base + (v.size() * size_t(nbBits) + 7) / 8, 0);
+    for (size_t i = 0; i < v.size(); i++) {
+        size_t bit = i * size_t(nbBits);
+        for (int b = 0; b < nbBits; b++, bit++)
+            if ((v[i] >> b) & 1) o[base + (bit >> 3)] |= uint8_t(1u << (bit & 7));
+    }
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* const* dOut, const size_t* caps,
+                          bool checksums, cudaStream_t st, std::vector<size_t>& sizes, std::string& err)
+{
+    Impl& I = *impl_;
+    launches_ = 0;
+    static bool prepared = false;
+    if (!prepared) {
+        if (prepareEncodeKernels() != cudaSuccess) { err = "kernel attributes"; return 1; }
+        prepared = true;
+    }
+    size_t const nf = frames.size();
+    sizes.assign(nf, 0);
+    std::vector<Front> fronts(nf);
+
+    // ---- phase A: front-end plan -------------------------------------------------
+    for (size_t f = 0; f < nf; f++) {
+        const EncFrameSpec& F = frames[f];
+        Front& fr = fronts[f];
+        uint64_t const inBytes = F.n * F.w;
+        int const r = F.recipe;
+        bool const hasDelta = r == RC_DZ_TSPLIT_FSE || r == RC_DZ_BITPACK_HUF || r == RC_D_TSPLIT_FSE
+                || r == RC_D_BITPACK_HUF || r == RC_DELTA_STORE;
+        bool const hasZz = r == RC_DZ_TSPLIT_FSE || r == RC_DZ_BITPACK_HUF || r == RC_ZIGZAG_STORE;
+        if (F.serial || inBytes < kMinStream) continue; // no numeric front end
+        uint64_t const m = hasDelta ? F.n - 1 : F.n;
+        if (hasDelta && m * F.w < kMinStream) {
+            fr.mode = EOUT_PLAIN; // small delta output: stored as is
+            fr.delta = true;
+            fr.n = m;
+            continue;
+        }
+        fr.delta = hasDelta;
+        fr.zigzag = hasZz;
+        fr.n = m;
+        if (r == RC_DZ_TSPLIT_FSE || r == RC_D_TSPLIT_FSE || r == RC_TSPLIT_STORE) fr.mode = EOUT_PLANES;
+        else if (r == RC_DZ_BITPACK_HUF || r == RC_D_BITPACK_HUF || r == RC_BITPACK_STORE) { fr.mode = EOUT_BITPACK; fr.needMax = true; }
+        else fr.mode = EOUT_PLAIN;
+    }
+    // maxima for bit packing
+    std::vector<EncNumTask> maxTasks;
+    std::vector<TileRef> maxTiles;
+    uint32_t nbMax = 0;
+    for (size_t f = 0; f < nf; f++) {
+        Front& fr = fronts[f];
+        if (!fr.needMax) continue;
+        fr.maxSlot = nbMax++;
+        EncNumTask t{};
+        t.src = frames[f].dIn;
+        t.n = fr.n;
+        t.w = frames[f].w;
+        t.delta = fr.delta;
+        t.zigzag = fr.zigzag;
+        t.maxSlot = fr.maxSlot;
+        for (uint32_t k = 0; k < (fr.n + kEncTile - 1) / kEncTile; k++) maxTiles.push_back(TileRef{ uint32_t(maxTasks.size()), k });
+        maxTasks.push_back(t);
+    }
+    // content checksums of the inputs, computed on the device now and
+    // written into the frames during assembly
+    std::vector<HashTask> contentHash;
+    std::vector<TileRef> contentBlocks;
+    {
+        size_t smallBytes = 4096 + maxTasks.size() * sizeof(EncNumTask) + maxTiles.size() * sizeof(TileRef)
+                + nbMax * 8 + nf * (sizeof(HashTask) + 8) + 64;
+        uint64_t blocks = 0;
+        for (size_t f = 0; f < nf; f++) {
+            uint64_t const len = frames[f].n * frames[f].w;
+            if (len > 240) blocks += (len - 1) / kHashBlock;
+        }
+        smallBytes += blocks * (64 + sizeof(TileRef)) + 1024;
+        if (!I.bufSmall.reserve(smallBytes)) { err = "device allocation failed"; return 70; }
+        Bump b{ I.bufSmall.data(), 0 };
+        auto* dMaxTasks = reinterpret_cast<EncNumTask*>(b.take(maxTasks.size() * sizeof(EncNumTask) + 1));
+        auto* dMaxTiles = reinterpret_cast<TileRef*>(b.take(maxTiles.size() * sizeof(TileRef) + 1));
+        auto* dMax = reinterpret_cast<unsigned long long*>(b.take(nbMax * 8 + 8));
+        auto* dHashOut = reinterpret_cast<uint64_t*>(b.take(nf * 8 + 8));
+        auto* dHashTasks = reinterpret_cast<HashTask*>(b.take(nf * sizeof(HashTask) + 1));
+        auto* dSums = reinterpret_cast<uint64_t*>(b.take(blocks * 64 + 64));
+        auto* dBlocks = reinterpret_cast<TileRef*>(b.take(blocks * sizeof(TileRef) + 8));
+        if (checksums) {
+            uint64_t bb = 0;
+            for (size_t f = 0; f < nf; f++) {
+                HashTask h{};
+                h.data = frames[f].dIn;
+                h.len = frames[f].n * frames[f].w;
+                h.aligned8 = (reinterpret_cast<uintptr_t>(h.data) & 7) == 0;
+                h.nbBlocks = h.len > 240 ? uint32_t((h.len - 1) / kHashBlock) : 0;
+                h.blockSums = dSums + 8 * bb;
+                h.hashOut = dHashOut + f;
+                for (uint32_t k = 0; k < h.nbBlocks; k++) contentBlocks.push_back(TileRef{ uint32_t(f), k });
+                bb += h.nbBlocks;
+                contentHash.push_back(h);
+            }
+        }
+        if (!maxTasks.empty()) {
+            cudaMemcpyAsync(dMaxTasks, maxTasks.data(), maxTasks.size() * sizeof(EncNumTask), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dMaxTiles, maxTiles.data(), maxTiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+            cudaMemsetAsync(dMax, 0, nbMax * 8, st);
+            launchEncMax(dMaxTasks, dMaxTiles, uint32_t(maxTiles.size()), dMax, st);
+            launches_++;
+        }
+        if (!contentHash.empty()) {
+            cudaMemcpyAsync(dHashTasks, contentHash.data(), contentHash.size() * sizeof(HashTask), cudaMemcpyHostToDevice, st);
+            if (!contentBlocks.empty())
+                cudaMemcpyAsync(dBlocks, contentBlocks.data(), contentBlocks.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+            launchHash(dHashTasks, uint32_t(contentHash.size()), dBlocks, uint32_t(contentBlocks.size()), nullptr, st);
+            launches_ += contentBlocks.empty() ? 1 : 2;
+        }
+        std::vector<unsigned long long> maxima(nbMax);
+        if (nbMax) cudaMemcpyAsync(maxima.data(), dMax, nbMax * 8, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in phase A"; return 1; }
+        for (size_t f = 0; f < nf; f++)
+            if (fronts[f].needMax) {
+                uint64_t const mx = maxima[fronts[f].maxSlot];
+                fronts[f].nbBits = 1 + (mx ? unsigned(63 - __builtin_clzll(mx)) : 0);
+            }
+        // keep the content hash outputs' addresses
+        for (size_t f = 0; f < contentHash.size(); f++) contentHash[f].hashOut = dHashOut + f;
+    }
+
+    // front-end outputs
+    {
+        Bump sizeB;
+        auto layoutA = [&](Bump& b) {
+            for (size_t f = 0; f < nf; f++) {
+                Front& fr = fronts[f];
+                if (fr.mode < 0) continue;
+                uint32_t const w = frames[f].w;
+                if (fr.mode == EOUT_PLANES) {
+                    fr.planeStride = (fr.n + 63) & ~uint64_t(63);
+                    fr.outBytes = fr.n; // per plane
+                    fr.out = b.take(fr.planeStride * w + 64, 64);
+                } else if (fr.mode == EOUT_BITPACK) {
+                    fr.outBytes = (fr.n * fr.nbBits + 7) / 8;
+                    fr.out = b.take(fr.outBytes + 64, 64);
+                } else {
+                    fr.outBytes = fr.n * w;
+                    fr.out = b.take(fr.outBytes + 64, 64);
+                }
+            }
+        };
+        layoutA(sizeB);
+        if (!I.bufA.reserve(sizeB.used)) { err = "device allocation failed"; return 70; }
+        Bump real{ I.bufA.data(), 0 };
+        layoutA(real);
+    }
+    {
+        std::vector<EncNumTask> tasks;
+        std::vector<TileRef> tiles;
+        for (size_t f = 0; f < nf; f++) {
+            Front& fr = fronts[f];
+            if (fr.mode < 0 || fr.n == 0) continue;
+            EncNumTask t{};
+            t.src = frames[f].dIn;
+            t.out = fr.out;
+            t.n = fr.n;
+            t.planeStride = fr.planeStride;
+            t.w = frames[f].w;
+            t.delta = fr.delta;
+            t.zigzag = fr.zigzag;
+            t.mode = uint8_t(fr.mode);
+            t.nbBits = uint8_t(fr.nbBits);
+            for (uint32_t k = 0; k < (fr.n + kEncTile - 1) / kEncTile; k++) tiles.push_back(TileRef{ uint32_t(tasks.size()), k });
+            tasks.push_back(t);
+        }
+        if (!tasks.empty()) {
+            size_t const bytes = tasks.size() * sizeof(EncNumTask) + tiles.size() * sizeof(TileRef) + 256;
+            if (!I.bufF.reserve(bytes)) { err = "device allocation failed"; return 70; }
+            Bump b{ I.bufF.data(), 0 };
+            auto* dT = reinterpret_cast<EncNumTask*>(b.take(tasks.size() * sizeof(EncNumTask)));
+            auto* dTi = reinterpret_cast<TileRef*>(b.take(tiles.size() * sizeof(TileRef)));
+            cudaMemcpyAsync(dT, tasks.data(), tasks.size() * sizeof(EncNumTask), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dTi, tiles.data(), tiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+            launchEncNum(dT, dTi, uint32_t(tiles.size()), st);
+            launches_++;
+            if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in front end"; return 1; }
+        }
+    }
+
+    // ---- phase B: discovery ------------------------------------------------------
+    I.jobs.clear();
+    auto runFrame = [&](size_t f, bool discover, size_t* cursor, Engine& E) {
+        const EncFrameSpec& F = frames[f];
+        E.discover = discover;
+        E.jobs = &I.jobs;
+        E.jobCursor = cursor;
+        E.front = &fronts[f];
+        int const in = E.newStream(F.serial ? T_SERIAL : T_NUMERIC, F.w, F.n);
+        E.s[in].pieces.push_back(Piece{ F.dIn, nullptr, F.n * F.w });
+        int const r = F.recipe;
+        if (E.s[in].bytes() < kMinStream || r == RC_STORE) { E.runSuccessor(Engine::G_STORE, in); return; }
+        switch (r) {
+            case RC_FSE: E.runSuccessor(Engine::G_FSE, in); break;
+            case RC_HUFFMAN: E.runSuccessor(Engine::G_HUF, in); break;
+            case RC_CONSTANT:
+            case RC_FLATPACK:
+            case RC_BITPACK: {
+                // the whole input is one forced-codec job
+                Job* j = E.jobFor(in, r == RC_CONSTANT ? M_CONSTANT : (r == RC_FLATPACK ? M_FLATPACK : M_BITPACK), -1);
+                if (j) {
+                    int const g = r == RC_CONSTANT ? Engine::G_CONSTANT : (r == RC_FLATPACK ? Engine::G_FLATPACK : Engine::G_BITPACK);
+                    E.graph(Engine::G_JOB, in, int(j - I.jobs.data()) | (g << 24));
+                }
+                break;
+            }
+            default: E.pipeline(r, in);
+        }
+    };
+    {
+        size_t cursor = 0;
+        for (size_t f = 0; f < nf; f++) {
+            Engine E;
+            runFrame(f, true, &cursor, E);
+            if (E.err) { err = "graph not supported on the GPU path"; return E.err; }
+        }
+        I.nbDataJobs = I.jobs.size();
+    }
+
+    // ---- phase C: histograms ------------------------------------------------------
+    size_t const nj = I.nbDataJobs;
+    std::vector<uint32_t> hists(nj * 256);
+    if (nj) {
+        std::vector<HistTask> ht(nj);
+        for (size_t j = 0; j < nj; j++) ht[j] = HistTask{ I.jobs[j].dsrc, uint32_t(I.jobs[j].n), uint32_t(j) };
+        size_t const bytes = nj * sizeof(HistTask) + nj * 1024 + 256;
+        if (!I.bufF.reserve(bytes)) { err = "device allocation failed"; return 70; }
+        Bump b{ I.bufF.data(), 0 };
+        auto* dHt = reinterpret_cast<HistTask*>(b.take(nj * sizeof(HistTask)));
+        auto* dH = reinterpret_cast<uint32_t*>(b.take(nj * 1024));
+        cudaMemcpyAsync(dHt, ht.data(), nj * sizeof(HistTask), cudaMemcpyHostToDevice, st);
+        launchHist(dHt, uint32_t(nj), dH, st);
+        launches_++;
+        cudaMemcpyAsync(hists.data(), dH, nj * 1024, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in histograms"; return 1; }
+    }
+
+    // ---- phase D: decisions and tables ------------------------------------------
+    auto decide = [&](Job& j) {
+        j.hist.n = j.n;
+        j.hist.finish();
+        if (j.mode == M_CONSTANT) j.codec = ent::CC_CONSTANT;
+        else if (j.mode == M_FLATPACK) j.codec = ent::CC_FLATPACK;
+        else if (j.mode == M_BITPACK) j.codec = ent::CC_BITPACK;
+        else j.codec = ent::chooseCodec(j.hist, j.mode == M_HUF);
+        switch (j.codec) {
+            case ent::CC_CONSTANT: j.constVal = uint8_t(j.hist.maxSym); break;
+            case ent::CC_BITPACK:
+                // computeNbBits (encode_bitpack_binding.c:51-72)
+                j.packBits = 1 + (j.hist.maxSym ? unsigned(31 - __builtin_clz(j.hist.maxSym)) : 0);
+                j.packBytes = (j.n * j.packBits + 7) / 8;
+                break;
+            case ent::CC_FLATPACK: {
+                j.alphabet.clear();
+                std::memset(j.map, 0, 256);
+                for (int s = 0; s < 256; s++)
+                    if (j.hist.count[s]) {
+                        j.map[s] = uint8_t(j.alphabet.size());
+                        j.alphabet.push_back(uint8_t(s));
+                    }
+                size_t const na = j.alphabet.size();
+                j.packBits = na <= 1 ? unsigned(na) : 1u + unsigned(31 - __builtin_clz(uint32_t(na - 1)));
+                j.packBytes = j.n ? 1 + (j.packBits * j.n) / 8 : 0;
+                break;
+            }
+            case ent::CC_FSE: {
+                j.nbStates = j.n < 1000 ? 2 : 4;
+                j.tl = ent::fseTableLog(11, j.n, j.hist.maxSym, 2);
+                ent::fseNormalize(j.norm, j.tl, j.hist.count, j.n, j.hist.maxSym);
+                j.fct.reset(new ent::FseCTable());
+                ent::fseBuildCTable(*j.fct, j.norm, j.hist.maxSym, j.tl);
+                j.ncountSize = ent::fseWriteNCount(j.ncount, j.norm, j.hist.maxSym, j.tl);
+                break;
+            }
+            case ent::CC_HUF: {
+                unsigned const tl0 = ent::fseTableLog(11, j.n, j.hist.maxSym, 1);
+                j.hct.reset(new ent::HufCTable());
+                unsigned const tl = ent::hufBuild(*j.hct, j.hist.count, j.hist.maxSym, tl0);
+                j.weights.resize(j.hist.maxSym + 1);
+                for (unsigned s = 0; s <= j.hist.maxSym; s++)
+                    j.weights[s] = uint8_t(j.hct->nbBits[s] ? tl + 1 - j.hct->nbBits[s] : 0);
+                j.x4 = j.n > 1000;
+                break;
+            }
+            default: break;
+        }
+    };
+    for (size_t j = 0; j < nj; j++) {
+        std::memcpy(I.jobs[j].hist.count, &hists[j * 256], 1024);
+        decide(I.jobs[j]);
+    }
+    // nested weights jobs (FSE graph of Huffman weights): decided on the host
+    // histogram of the weights, encoded on the device with the data jobs
+    for (size_t j = 0; j < nj; j++) {
+        Job& J = I.jobs[j];
+        if (J.codec != ent::CC_HUF) continue;
+        // weights stream: numeric u8; under 10 bytes it is stored, else the
+        // FSE graph gets it after a numeric->serial conversion
+        if (J.weights.size() < kMinStream) continue;
+        Job W;
+        W.hsrc = J.weights;
+        W.n = J.weights.size();
+        W.mode = M_FSE;
+        std::memset(W.hist.count, 0, sizeof(W.hist.count));
+        for (uint8_t x : W.hsrc) W.hist.count[x]++;
+        J.weightsJob = int(I.jobs.size());
+        I.jobs.push_back(std::move(W));
+        decide(I.jobs.back());
+    }
+
+    // ---- phase E: entropy bitstreams -----------------------------------------------
+    {
+        std::vector<FseEncTask> fseT;
+        std::vector<HufEncTask> hufT;
+        std::vector<PackTask> packT;
+        std::vector<TileRef> packTiles;
+        uint32_t nbSizes = 0;
+        auto layoutE = [&](Bump& b, bool real) {
+            nbSizes = 0;
+            for (size_t j = 0; j < I.jobs.size(); j++) {
+                Job& J = I.jobs[j];
+                if (!J.hsrc.empty()) {
+                    uint8_t* p = b.take(J.hsrc.size() + 16, 16);
+                    J.dstaged = p;
+                }
+                const uint8_t* src = J.hsrc.empty() ? J.dsrc : J.dstaged;
+                switch (J.codec) {
+                    case ent::CC_FSE: {
+                        J.out = b.take(J.n + J.n / 128 + 512, 16);
+                        J.dTable = b.take(sizeof(ent::FseCTable), 16);
+                        J.sizeSlot = nbSizes++;
+                        if (real) fseT.push_back(FseEncTask{ src, J.out, J.dTable, uint32_t(J.n), J.sizeSlot, J.nbStates, J.tl });
+                        break;
+                    }
+                    case ent::CC_HUF: {
+                        uint32_t const seg = uint32_t((J.n + 3) / 4);
+                        J.out = b.take(J.x4 ? 16 + 4ull * hufEncStreamCap(seg) : J.n + J.n / 8 + 64, 16);
+                        J.dTable = b.take(sizeof(ent::HufCTable), 16);
+                        J.sizeSlot = nbSizes;
+                        nbSizes += 4;
+                        if (real) hufT.push_back(HufEncTask{ src, J.out, J.dTable, uint32_t(J.n), J.sizeSlot, J.x4 ? 1u : 0u });
+                        break;
+                    }
+                    case ent::CC_BITPACK:
+                    case ent::CC_FLATPACK: {
+                        J.out = b.take(J.packBytes + 64, 16);
+                        uint8_t* map = J.codec == ent::CC_FLATPACK ? b.take(256, 16) : nullptr;
+                        J.dTable = map;
+                        if (real && J.n) {
+                            PackTask t{ src, J.out, map, J.n, J.packBits, 0 };
+                            for (uint32_t k = 0; k < (J.n + kEncTile - 1) / kEncTile; k++)
+                                packTiles.push_back(TileRef{ uint32_t(packT.size()), k });
+                            packT.push_back(t);
+                        }
+                        break;
+                    }
+                    default: break;
+                }
+            }
+        };
+        Bump sz;
+        layoutE(sz, false);
+        size_t const taskBytes = 4096 + I.jobs.size() * (sizeof(FseEncTask) + sizeof(HufEncTask) + sizeof(PackTask));
+        size_t tilesGuess = 0;
+        for (auto& J : I.jobs)
+            if (J.codec == ent::CC_BITPACK || J.codec == ent::CC_FLATPACK) tilesGuess += (J.n + kEncTile - 1) / kEncTile;
+        size_t const total = sz.used + taskBytes + tilesGuess * sizeof(TileRef) + (nbSizes + 16) * 4 + 1024;
+        if (!I.bufE.reserve(total)) { err = "device allocation failed"; return 70; }
+        Bump b{ I.bufE.data(), 0 };
+        layoutE(b, true);
+        auto* dFse = reinterpret_cast<FseEncTask*>(b.take(fseT.size() * sizeof(FseEncTask) + 1));
+        auto* dHuf = reinterpret_cast<HufEncTask*>(b.take(hufT.size() * sizeof(HufEncTask) + 1));
+        auto* dPack = reinterpret_cast<PackTask*>(b.take(packT.size() * sizeof(PackTask) + 1));
+        auto* dPackTiles = reinterpret_cast<TileRef*>(b.take(packTiles.size() * sizeof(TileRef) + 1));
+        auto* dSizes = reinterpret_cast<uint32_t*>(b.take((nbSizes + 1) * 4));
+        // uploads: staged weights, tables, maps, tasks
+        for (Job& J : I.jobs) {
+            if (!J.hsrc.empty()) cudaMemcpyAsync(const_cast<uint8_t*>(J.dstaged), J.hsrc.data(), J.hsrc.size(), cudaMemcpyHostToDevice, st);
+            if (J.codec == ent::CC_FSE) cudaMemcpyAsync(const_cast<uint8_t*>(J.dTable), J.fct.get(), sizeof(ent::FseCTable), cudaMemcpyHostToDevice, st);
+            if (J.codec == ent::CC_HUF) cudaMemcpyAsync(const_cast<uint8_t*>(J.dTable), J.hct.get(), sizeof(ent::HufCTable), cudaMemcpyHostToDevice, st);
+            if (J.codec == ent::CC_FLATPACK) cudaMemcpyAsync(const_cast<uint8_t*>(J.dTable), J.map, 256, cudaMemcpyHostToDevice, st);
+        }
+        if (!fseT.empty()) cudaMemcpyAsync(dFse, fseT.data(), fseT.size() * sizeof(FseEncTask), cudaMemcpyHostToDevice, st);
+        if (!hufT.empty()) cudaMemcpyAsync(dHuf, hufT.data(), hufT.size() * sizeof(HufEncTask), cudaMemcpyHostToDevice, st);
+        if (!packT.empty()) {
+            cudaMemcpyAsync(dPack, packT.data(), packT.size() * sizeof(PackTask), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dPackTiles, packTiles.data(), packTiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+        }
+        if (nbSizes) cudaMemsetAsync(dSizes, 0, nbSizes * 4, st);
+        launchFseEnc(dFse, uint32_t(fseT.size()), dSizes, st);
+        launchHufEnc(dHuf, uint32_t(hufT.size()), dSizes, st);
+        launchPack(dPack, dPackTiles, uint32_t(packTiles.size()), st);
+        launches_ += (fseT.empty() ? 0 : 1) + (hufT.empty() ? 0 : 1) + (packTiles.empty() ? 0 : 1);
+        std::vector<uint32_t> hs(nbSizes + 1);
+        if (nbSizes) cudaMemcpyAsync(hs.data(), dSizes, nbSizes * 4, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in entropy encoding"; return 1; }
+        for (Job& J : I.jobs) {
+            if (J.codec == ent::CC_FSE) J.sizes[0] = hs[J.sizeSlot];
+            if (J.codec == ent::CC_HUF) {
+                for (int k = 0; k < 4; k++) J.sizes[k] = hs[J.sizeSlot + k];
+                if (J.x4) {
+                    for (int k = 0; k < 3; k++) {
+                        J.jump[2 * k] = uint8_t(J.sizes[k]);
+                        J.jump[2 * k + 1] = uint8_t(J.sizes[k] >> 8);
+                    }
+                }
+            }
+        }
+    }
+
+    // ---- phase F: replay and frame layout --------------------------------------
+    struct FrameOut {
+        std::vector<uint8_t> head;     // frame header + chunk header + codec headers
+        std::vector<Piece> stored;     // stored streams in frame order
+        size_t headerBytes = 0;        // frame header length (before the block)
+        size_t total = 0;
+    };
+    std::vector<FrameOut> outs(nf);
+    {
+        size_t cursor = 0;
+        for (size_t f = 0; f < nf; f++) {
+            Engine E;
+            runFrame(f, false, &cursor, E);
+            if (E.err) { err = "graph replay failed"; return E.err; }
+            FrameOut& O = outs[f];
+            std::vector<uint8_t>& h = O.head;
+            const RStream& in0 = E.s[0];
+            uint32_t const magic = 0xD7B1A5C0u + 23;
+            for (int b = 0; b < 4; b++) h.push_back(uint8_t(magic >> (8 * b)));
+            h.push_back(uint8_t(checksums ? 3 : 0));
+            h.push_back(uint8_t(1 | (typeCode(in0.type) << 4)));
+            pushVarint(h, in0.bytes() + 1);
+            O.headerBytes = h.size(); // the header checksum byte follows when enabled
+            if (checksums) h.push_back(0);
+            size_t const nd = E.nd.size();
+            size_t nbStored = 0;
+            for (const RStream& x : E.s) nbStored += x.store;
+            pushVarint(h, nd + 1);
+            pushVarint(h, nbStored);
+            std::vector<uint32_t> a(nd, 0);
+            pushBits(h, a, 1);
+            for (size_t u = 0; u < nd; u++) a[u] = E.nd[nd - 1 - u].trid;
+            pushBits(h, a, ent::nextPow2Bits(63));
+            for (size_t u = 0; u < nd; u++) a[u] = E.nd[nd - 1 - u].hsz > 0;
+            pushBits(h, a, 1);
+            for (size_t u = 0; u < nd; u++)
+                if (E.nd[nd - 1 - u].hsz) pushVarint(h, E.nd[nd - 1 - u].hsz - 1);
+            for (size_t u = 0; u < nd; u++) a[u] = (E.nd[nd - 1 - u].nbOut - E.nd[nd - 1 - u].nbSO) > 0;
+            pushBits(h, a, 1);
+            for (size_t u = 0; u < nd; u++) {
+                const RNode& x = E.nd[nd - 1 - u];
+                if (x.nbOut - x.nbSO > 0) pushVarint(h, uint64_t(x.nbOut - x.nbSO - 1));
+            }
+            for (size_t u = 0; u < nd; u++) a[u] = 0;
+            pushBits(h, a, 1);
+            for (size_t u = 0; u < nd; u++) a[u] = uint32_t(E.nd[nd - 1 - u].outStart - E.nd[nd - 1 - u].in) - 1;
+            pushBits(h, a, ent::nextPow2Bits(nd + nbStored));
+            for (size_t i = E.s.size(); i-- > 0;)
+                if (E.s[i].store) pushVarint(h, E.s[i].bytes());
+            for (size_t u = 0; u < nd; u++) {
+                const RNode& x = E.nd[nd - 1 - u];
+                h.insert(h.end(), x.hdr, x.hdr + x.hsz);
+            }
+            for (size_t i = E.s.size(); i-- > 0;)
+                if (E.s[i].store) {
+                    uint64_t have = 0;
+                    for (const Piece& p : E.s[i].pieces) {
+                        O.stored.push_back(p);
+                        have += p.bytes;
+                    }
+                    if (have != E.s[i].bytes()) { err = "internal: stored stream without content"; return 80; }
+                }
+            uint64_t tot = h.size();
+            for (const Piece& p : O.stored) tot += p.bytes;
+            tot += checksums ? 8 : 0;
+            tot += 1;
+            O.total = tot;
+            if (tot > caps[f]) { err = "destination too small"; return 5; }
+            sizes[f] = tot;
+        }
+    }
+
+    // ---- phase G: assembly and checksums -----------------------------------------
+    {
+        // host bytes go through one staging upload
+        std::vector<uint8_t> stage;
+        std::vector<CopyTask> copies;
+        std::vector<std::pair<size_t, size_t>> hostCopies; // (stage offset, copy index)
+        auto stageBytes = [&](const uint8_t* p, uint64_t n) {
+            size_t const off = (stage.size() + 15) & ~size_t(15);
+            stage.resize(off + n);
+            if (n) std::memcpy(stage.data() + off, p, n);
+            return off;
+        };
+        for (size_t f = 0; f < nf; f++) {
+            FrameOut& O = outs[f];
+            uint64_t pos = 0;
+            size_t const so = stageBytes(O.head.data(), O.head.size());
+            copies.push_back(CopyTask{ dOut[f], nullptr, O.head.size(), 0 });
+            hostCopies.push_back({ so, copies.size() - 1 });
+            pos += O.head.size();
+            for (const Piece& p : O.stored) {
+                if (p.bytes) {
+                    if (p.host) {
+                        size_t const o2 = stageBytes(p.host, p.bytes);
+                        copies.push_back(CopyTask{ dOut[f] + pos, nullptr, p.bytes, 0 });
+                        hostCopies.push_back({ o2, copies.size() - 1 });
+                    } else {
+                        copies.push_back(CopyTask{ dOut[f] + pos, p.dev, p.bytes, 0 });
+                    }
+                }
+                pos += p.bytes;
+            }
+        }
+        std::vector<TileRef> tiles;
+        for (size_t i = 0; i < copies.size(); i++) {
+            copies[i].tileBase = uint32_t(tiles.size());
+            for (uint32_t k = 0; k < (copies[i].bytes + kTileBytes - 1) / kTileBytes; k++) tiles.push_back(TileRef{ uint32_t(i), k });
+        }
+        // checksum tasks: frame header (low 8 bits), block (content checksum
+        // included, so it runs after the content checksum is in place)
+        std::vector<HashTask> blockHash;
+        std::vector<TileRef> blockBlocks;
+        std::vector<PutTask> put1, put2;
+        uint64_t nbBlocks = 0;
+        if (checksums) {
+            for (size_t f = 0; f < nf; f++) {
+                FrameOut& O = outs[f];
+                uint64_t const blockStart = O.headerBytes + 1;
+                uint64_t const blockLen = O.total - 1 - 4 - blockStart;
+                HashTask hh{};
+                hh.data = dOut[f];
+                hh.len = O.headerBytes;
+                hh.aligned8 = (reinterpret_cast<uintptr_t>(dOut[f]) & 7) == 0;
+                blockHash.push_back(hh);
+                HashTask bh{};
+                bh.data = dOut[f] + blockStart;
+                bh.len = blockLen;
+                bh.aligned8 = (reinterpret_cast<uintptr_t>(bh.data) & 7) == 0;
+                bh.nbBlocks = blockLen > 240 ? uint32_t((blockLen - 1) / kHashBlock) : 0;
+                blockHash.push_back(bh);
+                nbBlocks += bh.nbBlocks;
+            }
+        }
+        size_t const bytes = stage.size() + copies.size() * sizeof(CopyTask) + tiles.size() * sizeof(TileRef)
+                + blockHash.size() * (sizeof(HashTask) + 8) + nbBlocks * (64 + sizeof(TileRef))
+                + 3 * nf * sizeof(PutTask) + 4096;
+        if (!I.bufF.reserve(bytes)) { err = "device allocation failed"; return 70; }
+        Bump b{ I.bufF.data(), 0 };
+        uint8_t* dStage = b.take(stage.size() + 16, 16);
+        for (auto& hc : hostCopies) copies[hc.second].src = dStage + hc.first;
+        auto* dCopies = reinterpret_cast<CopyTask*>(b.take(copies.size() * sizeof(CopyTask) + 1));
+        auto* dTiles = reinterpret_cast<TileRef*>(b.take(tiles.size() * sizeof(TileRef) + 1));
+        auto* dHT = reinterpret_cast<HashTask*>(b.take(blockHash.size() * sizeof(HashTask) + 1));
+        auto* dHOut = reinterpret_cast<uint64_t*>(b.take(blockHash.size() * 8 + 8));
+        auto* dSums = reinterpret_cast<uint64_t*>(b.take(nbBlocks * 64 + 64));
+        auto* dBB = reinterpret_cast<TileRef*>(b.take(nbBlocks * sizeof(TileRef) + 8));
+        auto* dPut1 = reinterpret_cast<PutTask*>(b.take(nf * sizeof(PutTask) + 1));
+        auto* dPut2 = reinterpret_cast<PutTask*>(b.take(2 * nf * sizeof(PutTask) + 1));
+        if (checksums) {
+            uint64_t bb = 0;
+            for (size_t i = 0; i < blockHash.size(); i++) {
+                blockHash[i].hashOut = dHOut + i;
+                blockHash[i].blockSums = dSums + 8 * bb;
+                for (uint32_t k = 0; k < blockHash[i].nbBlocks; k++) blockBlocks.push_back(TileRef{ uint32_t(i), k });
+                bb += blockHash[i].nbBlocks;
+            }
+            for (size_t f = 0; f < nf; f++) {
+                FrameOut& O = outs[f];
+                put1.push_back(PutTask{ dOut[f] + O.total - 1 - 8, contentHash[f].hashOut, 4 });
+                put2.push_back(PutTask{ dOut[f] + O.headerBytes, dHOut + 2 * f, 1 });
+                put2.push_back(PutTask{ dOut[f] + O.total - 1 - 4, dHOut + 2 * f + 1, 4 });
+            }
+        }
+        cudaMemcpyAsync(dStage, stage.data(), stage.size(), cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(dCopies, copies.data(), copies.size() * sizeof(CopyTask), cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(dTiles, tiles.data(), tiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+        if (checksums) {
+            cudaMemcpyAsync(dHT, blockHash.data(), blockHash.size() * sizeof(HashTask), cudaMemcpyHostToDevice, st);
+            if (!blockBlocks.empty())
+                cudaMemcpyAsync(dBB, blockBlocks.data(), blockBlocks.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dPut1, put1.data(), put1.size() * sizeof(PutTask), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dPut2, put2.data(), put2.size() * sizeof(PutTask), cudaMemcpyHostToDevice, st);
+        }
+        launchCopy(dCopies, dTiles, uint32_t(tiles.size()), st);
+        launches_++;
+        // end marker: a zero byte at the end of every frame
+        for (size_t f = 0; f < nf; f++) cudaMemsetAsync(dOut[f] + outs[f].total - 1, 0, 1, st);
+        if (checksums) {
+            launchPut(dPut1, uint32_t(put1.size()), st);
+            launchHash(dHT, uint32_t(blockHash.size()), dBB, uint32_t(blockBlocks.size()), nullptr, st);
+            launchPut(dPut2, uint32_t(put2.size()), st);
+            launches_ += 3 + (blockBlocks.empty() ? 0 : 1);
+        }
+        if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in frame assembly"; return 1; }
+    }
+    return 0;
+}
+
+} // namespace ozl

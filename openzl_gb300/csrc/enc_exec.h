@@ -1,0 +1,20 @@
+// Launchers of the encode kernels (encode_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "enc_tasks.h"
+
+namespace ozl {
+
+cudaError_t prepareEncodeKernels();
+uint32_t hufEncStreamCap(uint32_t segmentSize);
+void launchEncMax(const EncNumTask* t, const TileRef* tiles, uint32_t nbTiles, unsigned long long* maxima,
+                  cudaStream_t s);
+void launchEncNum(const EncNumTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
+void launchPack(const PackTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
+void launchHist(const HistTask* t, uint32_t n, uint32_t* hists, cudaStream_t s);
+void launchFseEnc(const FseEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);
+void launchHufEnc(const HufEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);
+void launchPut(const PutTask* t, uint32_t n, cudaStream_t s);
+
+} // namespace ozl

@@ -1,0 +1,66 @@
+// Host-side entropy decisions and coding tables for the GPU encoder.
+//
+// These are the small, per-chunk computations between the GPU histogram pass
+// and the GPU bitstream pass: OpenZL's chunk codec choice
+// (src/openzl/codecs/entropy/encode_entropy_binding.c:602-762) from 256-bin
+// histograms, FSE normalization and encoding tables
+// (src/openzl/fse/compress/fse_compress.c), and Huffman code lengths
+// (src/openzl/fse/compress/huf_compress.c). Their results must equal the
+// reference's bit for bit, so the arithmetic is restated exactly, including
+// the one double-precision entropy estimate (computed without FMA).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace ozl {
+namespace ent {
+
+enum ChunkCodec : int {
+    CC_STORE = 0,
+    CC_CONSTANT,
+    CC_FLATPACK,
+    CC_BITPACK,
+    CC_FSE,
+    CC_HUF,
+};
+
+struct Histo {
+    uint32_t count[256];
+    uint64_t n;
+    unsigned maxSym;
+    unsigned card;
+    void finish(); // fills maxSym and card from count
+};
+
+// Chunk codec choice for a serial chunk (huffman mode for the Huffman graph,
+// FSE mode for the FSE graph).
+ChunkCodec chooseCodec(const Histo& h, bool hufMode);
+
+// FSE: table log, normalized counts, encoding tables.
+unsigned fseTableLog(unsigned maxTableLog, uint64_t srcSize, unsigned maxSym, unsigned minus);
+bool fseNormalize(int16_t* norm, unsigned tableLog, const uint32_t* count, uint64_t total, unsigned maxSym);
+size_t fseWriteNCount(uint8_t* out, const int16_t* norm, unsigned maxSym, unsigned tableLog);
+
+// Device-ready FSE encoding table: next-state table sorted by symbol, and
+// per-symbol (deltaNbBits, deltaFindState).
+struct FseCTable {
+    uint16_t tableLog;
+    uint16_t maxSym;
+    uint32_t deltaNbBits[256];
+    int32_t deltaFindState[256];
+    uint16_t state[2048];
+};
+void fseBuildCTable(FseCTable& ct, const int16_t* norm, unsigned maxSym, unsigned tableLog);
+
+// Huffman: code lengths and canonical codes for a histogram.
+struct HufCTable {
+    uint16_t value[256];
+    uint8_t nbBits[256];
+    uint32_t tableLog;
+};
+unsigned hufBuild(HufCTable& ct, const uint32_t* count, unsigned maxSym, unsigned maxNbBits);
+
+int nextPow2Bits(uint64_t v);
+
+} // namespace ent
+} // namespace ozl

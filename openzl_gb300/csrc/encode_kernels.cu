@@ -1,0 +1,387 @@
+// sm_103a encode kernels for OpenZL's numeric codec graph.
+//
+// Data-parallel front ends (delta/zigzag with byte-split or bit packing),
+// per-chunk histograms, and the entropy bitstreams (FSE with 2/4 interleaved
+// states, Huffman 1X/4X). Bitstream kernels run one lane per chunk (FSE) or
+// per stream (Huffman) with that chunk's coding table in shared memory; the
+// bit order restates src/openzl/fse/bitstream.h (fields appended LSB-first,
+// a final 1 marker bit).
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "enc_exec.h"
+#include "enc_tables.h"
+#include "enc_tasks.h"
+
+namespace ozl {
+
+namespace {
+
+__device__ __forceinline__ uint64_t ldW(const uint8_t* p, uint32_t w)
+{
+    uint64_t v = 0;
+    if (w == 1) return *p;
+    if (w == 2 && !(reinterpret_cast<uintptr_t>(p) & 1)) return *reinterpret_cast<const uint16_t*>(p);
+    if (w == 4 && !(reinterpret_cast<uintptr_t>(p) & 3)) return *reinterpret_cast<const uint32_t*>(p);
+    if (w == 8 && !(reinterpret_cast<uintptr_t>(p) & 7)) return *reinterpret_cast<const uint64_t*>(p);
+    for (uint32_t b = 0; b < w; b++) v |= uint64_t(p[b]) << (8 * b);
+    return v;
+}
+
+__device__ __forceinline__ void stW(uint8_t* p, uint64_t v, uint32_t w)
+{
+    if (w == 1) { *p = uint8_t(v); return; }
+    if (w == 2 && !(reinterpret_cast<uintptr_t>(p) & 1)) { *reinterpret_cast<uint16_t*>(p) = uint16_t(v); return; }
+    if (w == 4 && !(reinterpret_cast<uintptr_t>(p) & 3)) { *reinterpret_cast<uint32_t*>(p) = uint32_t(v); return; }
+    if (w == 8 && !(reinterpret_cast<uintptr_t>(p) & 7)) { *reinterpret_cast<uint64_t*>(p) = v; return; }
+    for (uint32_t b = 0; b < w; b++) p[b] = uint8_t(v >> (8 * b));
+}
+
+__device__ __forceinline__ uint64_t transformed(const EncNumTask& t, uint64_t i)
+{
+    uint64_t const m = t.w >= 8 ? ~0ull : ((1ull << (8 * t.w)) - 1);
+    uint64_t v;
+    if (t.delta) v = (ldW(t.src + (i + 1) * t.w, t.w) - ldW(t.src + i * t.w, t.w)) & m;
+    else v = ldW(t.src + i * t.w, t.w);
+    if (t.zigzag) {
+        uint64_t const sign = (v >> (8 * t.w - 1)) & 1;
+        v = ((v << 1) ^ (0 - sign)) & m;
+    }
+    return v;
+}
+
+// Packs `cnt` fields of nbBits (LSB-first) that start at a 32-bit boundary of
+// `out`; complete words are stored whole, the final partial word bytewise.
+struct WordPacker {
+    uint8_t* out;
+    uint64_t acc = 0;
+    uint32_t nb = 0;
+    uint32_t pos = 0; // bytes written
+    __device__ explicit WordPacker(uint8_t* o) : out(o) {}
+    // invariant: nb < 32 between calls
+    __device__ __forceinline__ void put(uint64_t v, uint32_t bits)
+    {
+        if (bits > 32) {
+            put(v & 0xffffffffu, 32);
+            put(v >> 32, bits - 32);
+            return;
+        }
+        uint64_t const m = bits == 32 ? 0xffffffffull : ((1ull << bits) - 1);
+        acc |= (v & m) << nb;
+        nb += bits;
+        if (nb >= 32) {
+            *reinterpret_cast<uint32_t*>(out + pos) = uint32_t(acc);
+            pos += 4;
+            acc >>= 32;
+            nb -= 32;
+        }
+    }
+    __device__ __forceinline__ void finish(uint32_t totalBytes)
+    {
+        while (pos < totalBytes) {
+            out[pos++] = uint8_t(acc);
+            acc >>= 8;
+        }
+    }
+};
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+// per-task maximum of the transformed values (bit width of bitpack_int)
+__global__ void kEncMax(const EncNumTask* __restrict__ tasks, const TileRef* __restrict__ tiles,
+                        unsigned long long* __restrict__ maxima)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    EncNumTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kEncTile;
+    uint64_t const e1 = min(t.n, e0 + kEncTile);
+    uint64_t mx = 0;
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+        uint64_t const v = transformed(t, i);
+        mx = v > mx ? v : mx;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        uint64_t const x = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = x > mx ? x : mx;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(&maxima[t.maxSlot], (unsigned long long)mx);
+}
+
+// front end: delta/zigzag then plain, byte planes or bit packing.
+// 128 threads x 32 consecutive elements per tile.
+__global__ void __launch_bounds__(128) kEncNum(const EncNumTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    EncNumTask const t = tasks[tr.task];
+    uint64_t const i0 = uint64_t(tr.tile) * kEncTile + uint64_t(threadIdx.x) * 32;
+    if (i0 >= t.n) return;
+    uint32_t const cnt = uint32_t(min(uint64_t(32), t.n - i0));
+    if (t.mode == EOUT_PLAIN) {
+        for (uint32_t k = 0; k < cnt; k++) stW(t.out + (i0 + k) * t.w, transformed(t, i0 + k), t.w);
+    } else if (t.mode == EOUT_PLANES) {
+        uint64_t v[32];
+        for (uint32_t k = 0; k < cnt; k++) v[k] = transformed(t, i0 + k);
+        for (uint32_t b = 0; b < t.w; b++) {
+            uint8_t* const p = t.out + b * t.planeStride + i0;
+            if (cnt == 32 && !(reinterpret_cast<uintptr_t>(p) & 15)) {
+                uint32_t wds[8];
+                for (int q = 0; q < 8; q++) {
+                    uint32_t x = 0;
+                    for (int c = 0; c < 4; c++) x |= uint32_t((v[4 * q + c] >> (8 * b)) & 0xff) << (8 * c);
+                    wds[q] = x;
+                }
+                reinterpret_cast<uint4*>(p)[0] = make_uint4(wds[0], wds[1], wds[2], wds[3]);
+                reinterpret_cast<uint4*>(p)[1] = make_uint4(wds[4], wds[5], wds[6], wds[7]);
+            } else {
+                for (uint32_t k = 0; k < cnt; k++) p[k] = uint8_t(v[k] >> (8 * b));
+            }
+        }
+    } else {
+        // 32 fields start at bit 32*nbBits*(i0/32): a 4-byte boundary
+        WordPacker wp(t.out + (i0 / 32) * 4 * t.nbBits);
+        for (uint32_t k = 0; k < cnt; k++) wp.put(transformed(t, i0 + k), t.nbBits);
+        wp.finish(uint32_t((uint64_t(cnt) * t.nbBits + 7) / 8));
+    }
+}
+
+// serial bit packing / flatpack indices
+__global__ void __launch_bounds__(128) kPack(const PackTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    PackTask const t = tasks[tr.task];
+    uint64_t const i0 = uint64_t(tr.tile) * kEncTile + uint64_t(threadIdx.x) * 32;
+    if (i0 >= t.n) return;
+    uint32_t const cnt = uint32_t(min(uint64_t(32), t.n - i0));
+    WordPacker wp(t.out + (i0 / 32) * 4 * t.nbBits);
+    for (uint32_t k = 0; k < cnt; k++) {
+        uint32_t const s = t.src[i0 + k];
+        wp.put(t.map ? t.map[s] : s, t.nbBits);
+    }
+    uint32_t bits = cnt * t.nbBits;
+    if (t.map && i0 + cnt == t.n) {
+        wp.put(1, 1); // flatpack terminator
+        bits += 1;
+    }
+    wp.finish((bits + 7) / 8);
+}
+
+// 256-bin histogram of one chunk per CTA
+__global__ void __launch_bounds__(256) kHist(const HistTask* __restrict__ tasks, uint32_t* __restrict__ hists)
+{
+    __shared__ uint32_t h[8][256];
+    HistTask const t = tasks[blockIdx.x];
+    for (int k = threadIdx.x; k < 8 * 256; k += 256) (&h[0][0])[k] = 0;
+    __syncthreads();
+    uint32_t* const mine = h[threadIdx.x & 7];
+    uint32_t const n = t.n;
+    uint32_t i = threadIdx.x * 4;
+    bool const al = !(reinterpret_cast<uintptr_t>(t.src) & 3);
+    if (al) {
+        for (; i + 4 <= n; i += 1024) {
+            uint32_t const x = *reinterpret_cast<const uint32_t*>(t.src + i);
+            atomicAdd(&mine[x & 0xff], 1u);
+            atomicAdd(&mine[(x >> 8) & 0xff], 1u);
+            atomicAdd(&mine[(x >> 16) & 0xff], 1u);
+            atomicAdd(&mine[x >> 24], 1u);
+        }
+        for (uint32_t k = i; k < n && k < i + 4; k++) atomicAdd(&mine[t.src[k]], 1u);
+    } else {
+        for (uint32_t k = threadIdx.x; k < n; k += 256) atomicAdd(&mine[t.src[k]], 1u);
+    }
+    __syncthreads();
+    uint32_t s = 0;
+    for (int r = 0; r < 8; r++) s += h[r][threadIdx.x];
+    hists[uint64_t(t.outIndex) * 256 + threadIdx.x] = s;
+}
+
+// ---------------------------------------------------------------------------
+// forward bit writer into a 4-byte aligned buffer
+struct BitOut {
+    uint8_t* out;
+    uint64_t acc = 0;
+    uint32_t nb = 0;
+    uint32_t pos = 0;
+    __device__ explicit BitOut(uint8_t* o) : out(o) {}
+    __device__ __forceinline__ void add(uint32_t v, uint32_t bits)
+    {
+        acc |= uint64_t(v & ((1u << bits) - 1u)) << nb;
+        nb += bits;
+        if (nb >= 32) {
+            *reinterpret_cast<uint32_t*>(out + pos) = uint32_t(acc);
+            pos += 4;
+            acc >>= 32;
+            nb -= 32;
+        }
+    }
+    __device__ __forceinline__ uint32_t close()
+    {
+        add(1, 1);
+        while (nb > 0) {
+            out[pos++] = uint8_t(acc);
+            acc >>= 8;
+            nb = nb > 8 ? nb - 8 : 0;
+        }
+        return pos;
+    }
+};
+
+// FSE: one lane per chunk; the lane's table (2^tableLog next states and the
+// per-symbol transform) lives in shared memory.
+constexpr uint32_t kFseEncLanes = 16;
+constexpr uint32_t kFseLaneBytes = 2048 * 2 + 256 * 8;
+
+__global__ void __launch_bounds__(32) kFseEnc(const FseEncTask* __restrict__ tasks, uint32_t nbTasks,
+                                              uint32_t* __restrict__ sizes)
+{
+    extern __shared__ uint8_t smemFseEnc[];
+    uint32_t const lane = threadIdx.x;
+    uint32_t const ti = blockIdx.x * kFseEncLanes + lane;
+    if (lane >= kFseEncLanes || ti >= nbTasks) return;
+    FseEncTask const t = tasks[ti];
+    uint8_t* const base = smemFseEnc + size_t(lane) * kFseLaneBytes;
+    uint32_t* const dnb = reinterpret_cast<uint32_t*>(base);
+    int32_t* const dfs = reinterpret_cast<int32_t*>(base + 1024);
+    uint16_t* const st = reinterpret_cast<uint16_t*>(base + 2048);
+    const ent::FseCTable* ct = reinterpret_cast<const ent::FseCTable*>(t.ctable);
+    for (int s = 0; s < 256; s++) {
+        dnb[s] = ct->deltaNbBits[s];
+        dfs[s] = ct->deltaFindState[s];
+    }
+    uint32_t const size = 1u << t.tableLog;
+    for (uint32_t u = 0; u < size; u++) st[u] = ct->state[u];
+
+    uint32_t const n = t.n, ns = t.nbStates;
+    BitOut bo(t.out);
+    uint32_t v[4];
+    auto initState = [&](uint32_t sym) -> uint32_t {
+        uint32_t const nbOut = (dnb[sym] + (1u << 15)) >> 16;
+        uint32_t const x = (nbOut << 16) - dnb[sym];
+        return st[(x >> nbOut) + dfs[sym]];
+    };
+    auto encode = [&](uint32_t& state, uint32_t sym) {
+        uint32_t const nbOut = (state + dnb[sym]) >> 16;
+        bo.add(state, nbOut);
+        state = st[(state >> nbOut) + dfs[sym]];
+    };
+    int64_t ip = n;
+    uint32_t s = ns - (n % ns);
+    for (uint32_t k = 0; k < ns; k++) v[(s++) % ns] = initState(t.src[--ip]);
+    for (uint32_t k = 0; k < n % ns; k++) encode(v[(s++) % ns], t.src[--ip]);
+    if (ns == 4) {
+        while (ip > 0) {
+            encode(v[0], t.src[ip - 1]);
+            encode(v[1], t.src[ip - 2]);
+            encode(v[2], t.src[ip - 3]);
+            encode(v[3], t.src[ip - 4]);
+            ip -= 4;
+        }
+    } else {
+        while (ip > 0) {
+            encode(v[0], t.src[ip - 1]);
+            encode(v[1], t.src[ip - 2]);
+            ip -= 2;
+        }
+    }
+    for (uint32_t k = 0; k < ns; k++) bo.add(v[k], t.tableLog);
+    sizes[t.sizeSlot] = bo.close();
+}
+
+// Huffman: one lane per stream (4 per chunk for 4X); symbols are appended
+// from the end of the stream to its start. Each stream writes at its own
+// offset of the chunk buffer; the frame assembly joins them.
+constexpr uint32_t kHufEncChunks = 8;
+
+__device__ __forceinline__ uint32_t hufStreamCap(uint32_t seg) { return ((seg + (seg >> 3) + 64) + 15) & ~15u; }
+
+__global__ void __launch_bounds__(32) kHufEnc(const HufEncTask* __restrict__ tasks, uint32_t nbTasks,
+                                              uint32_t* __restrict__ sizes)
+{
+    __shared__ uint16_t val[kHufEncChunks][256];
+    __shared__ uint8_t nbb[kHufEncChunks][256];
+    uint32_t const c = threadIdx.x >> 2, k = threadIdx.x & 3;
+    uint32_t const ti = blockIdx.x * kHufEncChunks + c;
+    bool const active = ti < nbTasks;
+    HufEncTask t{};
+    if (active) {
+        t = tasks[ti];
+        const ent::HufCTable* ct = reinterpret_cast<const ent::HufCTable*>(t.ctable);
+        for (int s = k; s < 256; s += 4) {
+            val[c][s] = ct->value[s];
+            nbb[c][s] = ct->nbBits[s];
+        }
+    }
+    __syncwarp();
+    if (!active) return;
+    uint32_t start, len;
+    uint8_t* out;
+    if (t.x4) {
+        uint32_t const seg = (t.n + 3) / 4;
+        start = seg * k;
+        len = k < 3 ? seg : t.n - 3 * seg;
+        out = t.out + 16 + k * hufStreamCap(seg);
+    } else {
+        if (k) return;
+        start = 0;
+        len = t.n;
+        out = t.out;
+    }
+    BitOut bo(out);
+    const uint8_t* const src = t.src + start;
+    for (uint32_t i = len; i > 0; i--) {
+        uint32_t const s = src[i - 1];
+        bo.add(val[c][s], nbb[c][s]);
+    }
+    sizes[t.sizeSlot + k] = bo.close();
+}
+
+__global__ void kPut(const PutTask* __restrict__ tasks, uint32_t n)
+{
+    uint32_t const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PutTask const t = tasks[i];
+    uint64_t const h = *t.hash;
+    for (uint32_t b = 0; b < t.bytes; b++) t.dst[b] = uint8_t(h >> (8 * b));
+}
+
+// ---------------------------------------------------------------------------
+cudaError_t prepareEncodeKernels()
+{
+    return cudaFuncSetAttribute(kFseEnc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(kFseEncLanes * kFseLaneBytes));
+}
+
+uint32_t hufEncStreamCap(uint32_t seg) { return ((seg + (seg >> 3) + 64) + 15) & ~15u; }
+
+void launchEncMax(const EncNumTask* t, const TileRef* tiles, uint32_t nbTiles, unsigned long long* maxima,
+                  cudaStream_t s)
+{
+    if (nbTiles) kEncMax<<<nbTiles, 256, 0, s>>>(t, tiles, maxima);
+}
+void launchEncNum(const EncNumTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s)
+{
+    if (nbTiles) kEncNum<<<nbTiles, 128, 0, s>>>(t, tiles);
+}
+void launchPack(const PackTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s)
+{
+    if (nbTiles) kPack<<<nbTiles, 128, 0, s>>>(t, tiles);
+}
+void launchHist(const HistTask* t, uint32_t n, uint32_t* hists, cudaStream_t s)
+{
+    if (n) kHist<<<n, 256, 0, s>>>(t, hists);
+}
+void launchFseEnc(const FseEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s)
+{
+    if (n) kFseEnc<<<(n + kFseEncLanes - 1) / kFseEncLanes, 32, kFseEncLanes * kFseLaneBytes, s>>>(t, n, sizes);
+}
+void launchHufEnc(const HufEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s)
+{
+    if (n) kHufEnc<<<(n + kHufEncChunks - 1) / kHufEncChunks, 32, 0, s>>>(t, n, sizes);
+}
+void launchPut(const PutTask* t, uint32_t n, cudaStream_t s)
+{
+    if (n) kPut<<<(n + 127) / 128, 128, 0, s>>>(t, n);
+}
+
+} // namespace ozl

@@ -1,0 +1,80 @@
+"""GPU encoder parity: frames compressed on the device are byte-identical to
+the CPU oracle's (itself pinned to the reference's frames), and decode back
+on the device to the input."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _walk(rng, n, dt, step, start=1000000):
+    return (start + np.cumsum(rng.integers(-step, step + 1, n))).astype(dt)
+
+
+def _timestamps(rng, n):
+    inc = rng.geometric(1 / 1000, n).astype(np.int64)
+    o = rng.random(n) < 0.01
+    inc[o] = rng.integers(0, 2**32, int(o.sum()))
+    return (1700000000000000000 + np.cumsum(inc)).astype(np.int64)
+
+
+def _cases(seed):
+    rng = np.random.default_rng(seed)
+    c = [(1, _walk(rng, 262144, np.uint32, 100), 4), (2, _timestamps(rng, 150000), 8)]
+    for w, dt in [(1, np.uint8), (2, np.uint16), (4, np.uint32), (8, np.uint64)]:
+        for recipe in (1, 2, 3, 4, 9, 10, 11, 12):
+            for n in (1, 3, 9, 700, 20000 + 17 * w, 130000):
+                c.append((recipe, _walk(rng, n, dt, int(rng.integers(1, 6000))), w))
+    for recipe in (7, 8):
+        for n in (2, 9, 10, 999, 1001, 5000, 100000, 200000):
+            for k in (2, 3, 37, 256):
+                c.append((recipe, (rng.zipf(1.2, n) % k).astype(np.uint8), 0))
+    c.append((13, np.full(4000, 9, np.uint8), 0))
+    c.append((14, rng.integers(0, 37, 3000).astype(np.uint8), 0))
+    c.append((15, rng.integers(0, 37, 3000).astype(np.uint8), 0))
+    c.append((0, rng.integers(0, 256, 3000).astype(np.uint8), 0))
+    return c
+
+
+@pytest.mark.parametrize("checksums", [True, False])
+def test_gpu_frames_equal_oracle_frames(gpu_lib, checksums):
+    import torch
+    import openzl_gb300 as oz
+
+    cases = _cases(11 if checksums else 12)
+    enc = oz.GpuEncoder()
+    srcs = [torch.from_numpy(a.view(np.uint8).copy()).cuda() if a.size else torch.zeros(1, dtype=torch.uint8,
+            device="cuda") for _, a, _ in cases]
+    caps = [enc.bound(a.nbytes) for _, a, _ in cases]
+    dsts = [torch.zeros(c, dtype=torch.uint8, device="cuda") for c in caps]
+    sizes = enc.compress_batch([s.data_ptr() for s in srcs], [a.size if w else a.nbytes for _, a, w in cases],
+                               [w for _, _, w in cases], [r for r, _, _ in cases], [d.data_ptr() for d in dsts],
+                               caps, checksums=checksums)
+    bad = []
+    for (recipe, arr, w), d, sz in zip(cases, dsts, sizes):
+        want = oracle.compress(recipe, arr, w, checksums=checksums).tobytes()
+        got = d[:sz].cpu().numpy().tobytes()
+        if got != want:
+            bad.append((recipe, w, arr.size, len(got), len(want)))
+    assert not bad, bad[:10]
+
+
+def test_gpu_encode_then_gpu_decode(gpu_lib):
+    import torch
+    import openzl_gb300 as oz
+
+    rng = np.random.default_rng(5)
+    arrs = [(3, _walk(rng, 300000, np.uint16, 3000), 2), (4, _walk(rng, 250000, np.uint64, 60000), 8),
+            (1, _walk(rng, 262144, np.uint32, 100), 4), (2, _timestamps(rng, 400000), 8)]
+    enc = oz.GpuEncoder()
+    srcs = [torch.from_numpy(a.view(np.uint8).copy()).cuda() for _, a, _ in arrs]
+    caps = [enc.bound(a.nbytes) for _, a, _ in arrs]
+    dsts = [torch.zeros(c + 64, dtype=torch.uint8, device="cuda") for c in caps]
+    sizes = enc.compress_batch([s.data_ptr() for s in srcs], [a.size for _, a, _ in arrs], [w for _, _, w in arrs],
+                               [r for r, _, _ in arrs], [d.data_ptr() for d in dsts], caps)
+    d = oz.DCtx()
+    for (_, a, _), dst, sz in zip(arrs, dsts, sizes):
+        frame = dst[:sz].cpu().numpy()
+        assert d.decompress(frame).tobytes() == a.tobytes()
