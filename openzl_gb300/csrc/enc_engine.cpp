@@ -143,6 +143,8 @@ struct Front {
     uint64_t outBytes = 0;
     uint32_t maxSlot = 0;
     bool needMax = false;
+    bool needFirst = false;   // delta: the first element goes to the codec header
+    uint64_t first = 0;
 };
 
 } // namespace
@@ -490,7 +492,9 @@ struct Engine {
         bool first = true;
         if (delta) {
             RNode& x = newNode(TR_DELTA, cur, 1);
-            (void)x;
+            uint32_t const w = s[cur].w;
+            for (uint32_t b = 0; b < w; b++) x.hdr[b] = uint8_t(front->first >> (8 * b));
+            x.hsz = w;
             uint64_t const n = s[cur].n;
             int o = newStream(T_NUMERIC, s[cur].w, n ? n - 1 : 0);
             nd.back().nbOut = 1;
@@ -583,6 +587,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                 || r == RC_D_BITPACK_HUF || r == RC_DELTA_STORE;
         bool const hasZz = r == RC_DZ_TSPLIT_FSE || r == RC_DZ_BITPACK_HUF || r == RC_ZIGZAG_STORE;
         if (F.serial || inBytes < kMinStream) continue; // no numeric front end
+        fr.needFirst = hasDelta;
         uint64_t const m = hasDelta ? F.n - 1 : F.n;
         if (hasDelta && m * F.w < kMinStream) {
             fr.mode = EOUT_PLAIN; // small delta output: stored as is
@@ -621,7 +626,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
     std::vector<TileRef> contentBlocks;
     {
         size_t smallBytes = 4096 + maxTasks.size() * sizeof(EncNumTask) + maxTiles.size() * sizeof(TileRef)
-                + nbMax * 8 + nf * (sizeof(HashTask) + 8) + 64;
+                + nbMax * 8 + nf * (sizeof(HashTask) + 8) + 64 + nf * (8 + sizeof(CopyTask) + sizeof(TileRef)) + 256;
         uint64_t blocks = 0;
         for (size_t f = 0; f < nf; f++) {
             uint64_t const len = frames[f].n * frames[f].w;
@@ -637,6 +642,24 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         auto* dHashTasks = reinterpret_cast<HashTask*>(b.take(nf * sizeof(HashTask) + 1));
         auto* dSums = reinterpret_cast<uint64_t*>(b.take(blocks * 64 + 64));
         auto* dBlocks = reinterpret_cast<TileRef*>(b.take(blocks * sizeof(TileRef) + 8));
+        auto* dFirst = reinterpret_cast<uint64_t*>(b.take(nf * 8 + 8));
+        auto* dFirstCopies = reinterpret_cast<CopyTask*>(b.take(nf * sizeof(CopyTask) + 8));
+        auto* dFirstTiles = reinterpret_cast<TileRef*>(b.take(nf * sizeof(TileRef) + 8));
+        // first elements of the delta inputs, gathered into one array
+        std::vector<CopyTask> firstCopies;
+        std::vector<TileRef> firstTiles;
+        for (size_t f = 0; f < nf; f++)
+            if (fronts[f].needFirst) {
+                firstTiles.push_back(TileRef{ uint32_t(firstCopies.size()), 0 });
+                firstCopies.push_back(CopyTask{ reinterpret_cast<uint8_t*>(dFirst + f), frames[f].dIn, frames[f].w, 0 });
+            }
+        if (!firstCopies.empty()) {
+            cudaMemsetAsync(dFirst, 0, nf * 8, st);
+            cudaMemcpyAsync(dFirstCopies, firstCopies.data(), firstCopies.size() * sizeof(CopyTask), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dFirstTiles, firstTiles.data(), firstTiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+            launchCopy(dFirstCopies, dFirstTiles, uint32_t(firstTiles.size()), st);
+            launches_++;
+        }
         if (checksums) {
             uint64_t bb = 0;
             for (size_t f = 0; f < nf; f++) {
@@ -668,7 +691,11 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         }
         std::vector<unsigned long long> maxima(nbMax);
         if (nbMax) cudaMemcpyAsync(maxima.data(), dMax, nbMax * 8, cudaMemcpyDeviceToHost, st);
+        std::vector<uint64_t> firsts(firstCopies.empty() ? 0 : nf);
+        if (!firstCopies.empty()) cudaMemcpyAsync(firsts.data(), dFirst, nf * 8, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in phase A"; return 1; }
+        for (size_t f = 0; f < nf; f++)
+            if (fronts[f].needFirst) fronts[f].first = firsts[f];
         for (size_t f = 0; f < nf; f++)
             if (fronts[f].needMax) {
                 uint64_t const mx = maxima[fronts[f].maxSlot];
@@ -954,9 +981,18 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         if (nbSizes) cudaMemcpyAsync(hs.data(), dSizes, nbSizes * 4, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in entropy encoding"; return 1; }
         for (Job& J : I.jobs) {
-            if (J.codec == ent::CC_FSE) J.sizes[0] = hs[J.sizeSlot];
+            if (J.codec == ent::CC_FSE) {
+                J.sizes[0] = hs[J.sizeSlot];
+                if (J.sizes[0] > J.n + J.n / 128 + 512) { err = "FSE bitstream over capacity"; return 1; }
+            }
             if (J.codec == ent::CC_HUF) {
                 for (int k = 0; k < 4; k++) J.sizes[k] = hs[J.sizeSlot + k];
+                uint64_t const cap = J.x4 ? hufEncStreamCap(uint32_t((J.n + 3) / 4)) : J.n + J.n / 8 + 64;
+                for (int k = 0; k < (J.x4 ? 4 : 1); k++)
+                    if (J.sizes[k] > cap || (J.x4 && k < 3 && J.sizes[k] > 65535)) {
+                        err = "Huffman stream over capacity";
+                        return 1;
+                    }
                 if (J.x4) {
                     for (int k = 0; k < 3; k++) {
                         J.jump[2 * k] = uint8_t(J.sizes[k]);
@@ -1051,6 +1087,8 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             if (n) std::memcpy(stage.data() + off, p, n);
             return off;
         };
+        uint8_t const zero = 0;
+        size_t const zeroOff = stageBytes(&zero, 1);
         for (size_t f = 0; f < nf; f++) {
             FrameOut& O = outs[f];
             uint64_t pos = 0;
@@ -1070,6 +1108,9 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                 }
                 pos += p.bytes;
             }
+            // end-of-frame marker (a zero byte) after the block checksums
+            copies.push_back(CopyTask{ dOut[f] + O.total - 1, nullptr, 1, 0 });
+            hostCopies.push_back({ zeroOff, copies.size() - 1 });
         }
         std::vector<TileRef> tiles;
         for (size_t i = 0; i < copies.size(); i++) {
@@ -1143,8 +1184,6 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         }
         launchCopy(dCopies, dTiles, uint32_t(tiles.size()), st);
         launches_++;
-        // end marker: a zero byte at the end of every frame
-        for (size_t f = 0; f < nf; f++) cudaMemsetAsync(dOut[f] + outs[f].total - 1, 0, 1, st);
         if (checksums) {
             launchPut(dPut1, uint32_t(put1.size()), st);
             launchHash(dHT, uint32_t(blockHash.size()), dBB, uint32_t(blockBlocks.size()), nullptr, st);

@@ -197,19 +197,21 @@ __global__ void __launch_bounds__(256) kHist(const HistTask* __restrict__ tasks,
 }
 
 // ---------------------------------------------------------------------------
-// forward bit writer into a 4-byte aligned buffer
+// forward bit writer into a 4-byte aligned buffer of `cap` bytes; writes past
+// the capacity are dropped and reported through the returned size (> cap).
 struct BitOut {
     uint8_t* out;
+    uint32_t cap;
     uint64_t acc = 0;
     uint32_t nb = 0;
     uint32_t pos = 0;
-    __device__ explicit BitOut(uint8_t* o) : out(o) {}
+    __device__ BitOut(uint8_t* o, uint32_t c) : out(o), cap(c) {}
     __device__ __forceinline__ void add(uint32_t v, uint32_t bits)
     {
         acc |= uint64_t(v & ((1u << bits) - 1u)) << nb;
         nb += bits;
         if (nb >= 32) {
-            *reinterpret_cast<uint32_t*>(out + pos) = uint32_t(acc);
+            if (pos + 4 <= cap) *reinterpret_cast<uint32_t*>(out + pos) = uint32_t(acc);
             pos += 4;
             acc >>= 32;
             nb -= 32;
@@ -219,7 +221,8 @@ struct BitOut {
     {
         add(1, 1);
         while (nb > 0) {
-            out[pos++] = uint8_t(acc);
+            if (pos < cap) out[pos] = uint8_t(acc);
+            pos++;
             acc >>= 8;
             nb = nb > 8 ? nb - 8 : 0;
         }
@@ -253,7 +256,7 @@ __global__ void __launch_bounds__(32) kFseEnc(const FseEncTask* __restrict__ tas
     for (uint32_t u = 0; u < size; u++) st[u] = ct->state[u];
 
     uint32_t const n = t.n, ns = t.nbStates;
-    BitOut bo(t.out);
+    BitOut bo(t.out, t.n + t.n / 128 + 512);
     uint32_t v[4];
     auto initState = [&](uint32_t sym) -> uint32_t {
         uint32_t const nbOut = (dnb[sym] + (1u << 15)) >> 16;
@@ -327,7 +330,7 @@ __global__ void __launch_bounds__(32) kHufEnc(const HufEncTask* __restrict__ tas
         len = t.n;
         out = t.out;
     }
-    BitOut bo(out);
+    BitOut bo(out, t.x4 ? hufStreamCap((t.n + 3) / 4) : t.n + t.n / 8 + 64);
     const uint8_t* const src = t.src + start;
     for (uint32_t i = len; i > 0; i--) {
         uint32_t const s = src[i - 1];
