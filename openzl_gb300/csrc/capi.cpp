@@ -69,6 +69,7 @@ struct OZL_GpuBatch_s {
     std::vector<uint8_t*> dOuts;
     std::vector<size_t> sizes;
     long launches = 0;
+    bool uploaded = false;   // descriptors and parameters of the plan are on the device
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graphStream = nullptr;
     std::string err;
@@ -103,18 +104,30 @@ struct OZL_GpuBatch_s {
         rc = ozl::layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), scratch.data(),
                              pool.data(), layout, err);
         if (rc) return fail(rc);
+        uploaded = false;
+        launches = 0;
+        return ok(size_t(plan.totalOut));
+    }
+
+    // Copies the plan's descriptors and parameters to the device, ordered on
+    // the stream that runs the plan (the kernels read them).
+    ZL_Report upload(cudaStream_t s)
+    {
+        if (uploaded) return ok(0);
         if (!layout.pool.empty()
-            && cudaMemcpy(pool.data(), layout.pool.data(), layout.pool.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            && cudaMemcpyAsync(pool.data(), layout.pool.data(), layout.pool.size(), cudaMemcpyHostToDevice, s)
+                       != cudaSuccess) {
             err = "descriptor upload failed";
             return fail(ZL_ErrorCode_GENERIC);
         }
         if (!plan.params.empty()
-            && cudaMemcpy(params.data(), plan.params.data(), plan.params.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            && cudaMemcpyAsync(params.data(), plan.params.data(), plan.params.size(), cudaMemcpyHostToDevice, s)
+                       != cudaSuccess) {
             err = "parameter upload failed";
             return fail(ZL_ErrorCode_GENERIC);
         }
-        launches = 0;
-        return ok(size_t(plan.totalOut));
+        uploaded = true;
+        return ok(0);
     }
 
     ZL_Report enqueue(cudaStream_t s)
@@ -131,6 +144,8 @@ struct OZL_GpuBatch_s {
 
     ZL_Report run(cudaStream_t s, bool useGraph)
     {
+        ZL_Report const u = upload(s);
+        if (ZL_isError(u)) return u;
         if (!useGraph) return enqueue(s);
         if (s == nullptr) {
             err = "CUDA graph capture needs a non-default stream";
@@ -439,6 +454,8 @@ ZL_Report ozl_gpu_batch_profile(OZL_GpuBatch* b, void* stream, float* ms, int* k
 {
     if (!b) return fail(ZL_ErrorCode_parameter_invalid);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ZL_Report const u = b->upload(s);
+    if (ZL_isError(u)) return u;
     size_t const n = b->layout.launches.size();
     std::vector<cudaEvent_t> ev(n + 1);
     for (auto& e : ev)
@@ -490,7 +507,8 @@ ZL_Report ozl_gpu_xxh3_64(const void* d_data, size_t len, void* stream)
     cudaError_t e = ozl::xxh3Device(static_cast<const uint8_t*>(d_data), len,
                                     reinterpret_cast<uint64_t*>(scratch + scratchBytes), scratch, scratchBytes, s);
     uint64_t h = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(&h, scratch + scratchBytes, 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, scratch + scratchBytes, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaFree(scratch);
     if (e != cudaSuccess) return fail(ZL_ErrorCode_GENERIC);
     return ok(size_t(h));

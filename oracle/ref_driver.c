@@ -175,7 +175,8 @@ int64_t ref_decompress_into(const void* src, size_t srcSize, void* dst, size_t d
     ZL_DCtx* dc = ZL_DCtx_create();
     int64_t ret = -1;
     for (int i = 0; i < reps; i++) {
-        ZL_Report r = ZL_DCtx_decompress(dc, dst, dstCap, src, srcSize);
+        ZL_OutputInfo info;
+        ZL_Report r = ZL_DCtx_decompressTyped(dc, &info, dst, dstCap, src, srcSize);
         ret = ZL_isError(r) ? -(int64_t)ZL_errorCode(r) - 1000 : (int64_t)ZL_validResult(r);
         if (ret < 0) break;
     }
