@@ -379,73 +379,107 @@ __global__ void kFlatpack(const FlatpackTask* __restrict__ tasks, const TileRef*
 }
 
 // ---------------------------------------------------------------------------
-// Backward bit reader (FSE / Huffman bitstreams): reads fields most
+// Backward bit reader (FSE / Huffman bitstreams): fields are read most
 // significant bit first from the end of the stream towards its start.
-struct BitRev {
-    const uint8_t* base;
-    int64_t pos;     // unread bits
-    int64_t cbase;   // bit index of cont's least significant bit
-    uint64_t cont;
+//
+// The stream is read as aligned 32-bit words (a word holding at least one
+// byte of the stream never crosses a page), through the L1 cache, with the
+// next lower word loaded one word ahead and the cache line two lines below
+// prefetched whenever a line boundary is crossed. Positions are bit indices
+// above bit 0 of the aligned word that holds the stream's first byte.
+// Invariant between reads: cb + 32 < pos <= cb + 64, where the 64-bit
+// container c holds the words at bit indices [cb, cb + 64); fields are at most
+// 32 bits, so every field lies inside the container.
+struct BitIn {
+    const uint32_t* w;
+    int32_t pos;   // unread bits
+    int32_t end;   // position of the stream's first bit (0..24)
+    int32_t cb;    // bit index of c's least significant bit (multiple of 32)
+    uint64_t c;
+    uint32_t ahead; // the word below c
+
+    __device__ __forceinline__ static uint32_t word(const uint32_t* w, int32_t k) { return k >= 0 ? __ldg(w + k) : 0u; }
 
     __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size)
     {
-        base = p;
         if (size == 0) return false;
         uint8_t const last = p[size - 1];
         if (last == 0) return false;
-        pos = int64_t(size - 1) * 8 + (31 - __clz(uint32_t(last)));
-        refill();
+        uintptr_t const a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(3);
+        w = reinterpret_cast<const uint32_t*>(a);
+        end = int32_t(reinterpret_cast<uintptr_t>(p) - a) * 8;
+        pos = end + int32_t(size - 1) * 8 + (31 - __clz(uint32_t(last)));
+        int32_t const j = ((pos - 1) >> 5) - 1; // arithmetic shift: floor
+        cb = j * 32;
+        c = (uint64_t(word(w, j + 1)) << 32) | word(w, j);
+        ahead = word(w, j - 1);
         return true;
     }
-    __device__ __forceinline__ void refill()
+    __device__ __forceinline__ void renorm()
     {
-        int64_t b = ((pos + 7) >> 3) - 8;
-        if (b < 0) b = 0;
-        cbase = b * 8;
-        cont = ld64Any(base + b);
+        if (pos <= cb + 32) {
+            c = (c << 32) | ahead;
+            cb -= 32;
+            int32_t const k = (cb >> 5) - 1;
+            ahead = word(w, k);
+            if ((k & 31) == 0 && k >= 64) asm volatile("prefetch.global.L1 [%0];" ::"l"(w + k - 64));
+        }
     }
-    __device__ __forceinline__ uint32_t peek(unsigned nb) const
+    __device__ __forceinline__ uint32_t peek(uint32_t nb) const
     {
-        int64_t const sh = pos - int64_t(nb) - cbase;
-        uint64_t const v = sh >= 0 ? (cont >> sh) : (cont << (-sh));
-        return uint32_t(v) & ((1u << nb) - 1);
+        int32_t sh = pos - int32_t(nb) - cb;
+        // below 0 only on corrupt streams (caught by the end check); 64 only
+        // when nb is 0, where the mask clears the result
+        sh = sh < 0 ? 0 : (sh > 63 ? 63 : sh);
+        return uint32_t(c >> sh) & ((1u << nb) - 1u);
     }
-    __device__ __forceinline__ void skip(unsigned nb)
+    __device__ __forceinline__ void skip(uint32_t nb)
     {
-        pos -= nb;
-        if (pos - cbase < 32 && cbase > 0) refill();
+        pos -= int32_t(nb);
+        renorm();
     }
-    __device__ __forceinline__ uint32_t read(unsigned nb)
+    __device__ __forceinline__ uint32_t read(uint32_t nb)
     {
         uint32_t const v = peek(nb);
         skip(nb);
         return v;
     }
+    __device__ __forceinline__ bool finished() const { return pos == end; }
 };
 
 // ---------------------------------------------------------------------------
-// FSE: one lane per chunk, lane-private decoding table in shared memory.
-// Table entry: newState (16) | nbBits (8) | symbol (8).
+// FSE: one lane per chunk; kFseWarps warps per CTA share the SM's shared
+// memory, each lane with its own decoding table (entry: newState (16) |
+// nbBits (8) | symbol (8)) and build counters.
 //
 // Table construction restates src/openzl/fse/decompress/fse_decompress.c:
 // 73-171; decode order restates fse_decompress.c:255-337 (state i % nbStates
 // emits symbol i; the last symbol of each state has no transition).
-__global__ void kFse(const FseTask* __restrict__ tasks, uint32_t nbTasks, uint32_t lanesPerCta,
-                     uint32_t tableLogMax, uint32_t* __restrict__ status)
+constexpr uint32_t kFseWarps = 4;
+constexpr uint32_t kFseSmemMax = 227 * 1024;
+
+__device__ __forceinline__ uint32_t fseSlotBytes(uint32_t tlMax) { return (4u << tlMax) + 512u + 4u; }
+
+__global__ void __launch_bounds__(32 * kFseWarps) kFse(const FseTask* __restrict__ tasks, uint32_t nbTasks,
+                                                        uint32_t lanesPerWarp, uint32_t tableLogMax,
+                                                        uint32_t* __restrict__ status)
 {
-    extern __shared__ uint32_t smemFse[];
-    uint32_t const lane = threadIdx.x;
-    uint32_t const ti = blockIdx.x * lanesPerCta + lane;
-    if (lane >= lanesPerCta || ti >= nbTasks) return;
+    extern __shared__ __align__(16) uint8_t smemFse[];
+    uint32_t const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane >= lanesPerWarp) return;
+    uint32_t const slot = warp * lanesPerWarp + lane;
+    uint32_t const ti = blockIdx.x * (kFseWarps * lanesPerWarp) + slot;
+    if (ti >= nbTasks) return;
     FseTask const t = tasks[ti];
-    uint32_t* const dt = smemFse + (size_t(lane) << tableLogMax);
+    uint8_t* const base = smemFse + size_t(slot) * fseSlotBytes(tableLogMax);
+    uint32_t* const dt = reinterpret_cast<uint32_t*>(base);
+    uint16_t* const next = reinterpret_cast<uint16_t*>(base + (4u << tableLogMax));
     uint32_t const tl = t.tableLog;
     uint32_t const size = 1u << tl, mask = size - 1;
     uint32_t const step = (size >> 1) + (size >> 3) + 3;
     uint32_t high = size - 1;
-    uint16_t next[256];
     for (uint32_t s = 0; s < t.nbSym; s++) {
-        int16_t const c = t.norm[s];
+        int const c = t.norm[s];
         if (c == -1) {
             dt[high--] = s;
             next[s] = 1;
@@ -469,114 +503,146 @@ __global__ void kFse(const FseTask* __restrict__ tasks, uint32_t nbTasks, uint32
         dt[u] = s | (nb << 8) | (ns << 16);
     }
 
-    BitRev br;
+    BitIn br;
     if (!br.init(t.bits, t.bitsSize)) { reportError(status, DERR_CORRUPTION); return; }
     uint32_t const nst = t.nbStates;
     uint32_t st0 = br.read(tl), st1 = br.read(tl), st2 = 0, st3 = 0;
     if (nst == 4) { st2 = br.read(tl); st3 = br.read(tl); }
     uint32_t const n = t.dstSize;
-    uint32_t const lastTr = n - nst;
+    uint32_t const lastTr = n > nst ? n - nst : 0; // symbols [0, lastTr) have a transition
     uint8_t* const out = t.out;
-    // Bytes are packed four at a time into aligned 32-bit stores; the
-    // unaligned head and the last partial word go out as single bytes.
-    uint32_t const head = uint32_t((4 - (reinterpret_cast<uintptr_t>(out) & 3)) & 3);
-    uint32_t const bodyEnd = n < head ? n : head + ((n - head) & ~3u);
-    uint32_t word = 0;
-    uint32_t i = 0;
-    auto emit = [&](uint32_t idx, uint32_t sym) {
-        if (idx < head || idx >= bodyEnd) {
-            out[idx] = uint8_t(sym);
-            return;
-        }
-        uint32_t const q = (idx - head) & 3;
-        word |= sym << (8 * q);
-        if (q == 3) {
-            *reinterpret_cast<uint32_t*>(out + idx - 3) = word;
-            word = 0;
+    bool const aligned = !(reinterpret_cast<uintptr_t>(out) & 3);
+    auto put4 = [&](uint32_t i, uint32_t word) {
+        if (aligned) {
+            *reinterpret_cast<uint32_t*>(out + i) = word;
+        } else {
+            out[i] = uint8_t(word);
+            out[i + 1] = uint8_t(word >> 8);
+            out[i + 2] = uint8_t(word >> 16);
+            out[i + 3] = uint8_t(word >> 24);
         }
     };
+    uint32_t i = 0;
     if (nst == 4) {
         for (; i + 4 <= lastTr; i += 4) {
-            uint32_t e;
-            e = dt[st0]; emit(i, e & 0xff); st0 = (e >> 16) + br.read((e >> 8) & 0xff);
-            e = dt[st1]; emit(i + 1, e & 0xff); st1 = (e >> 16) + br.read((e >> 8) & 0xff);
-            e = dt[st2]; emit(i + 2, e & 0xff); st2 = (e >> 16) + br.read((e >> 8) & 0xff);
-            e = dt[st3]; emit(i + 3, e & 0xff); st3 = (e >> 16) + br.read((e >> 8) & 0xff);
+            uint32_t const e0 = dt[st0], e1 = dt[st1], e2 = dt[st2], e3 = dt[st3];
+            st0 = (e0 >> 16) + br.read((e0 >> 8) & 0xff);
+            st1 = (e1 >> 16) + br.read((e1 >> 8) & 0xff);
+            st2 = (e2 >> 16) + br.read((e2 >> 8) & 0xff);
+            st3 = (e3 >> 16) + br.read((e3 >> 8) & 0xff);
+            put4(i, (e0 & 0xff) | ((e1 & 0xff) << 8) | ((e2 & 0xff) << 16) | ((e3 & 0xff) << 24));
         }
     } else {
-        for (; i + 2 <= lastTr; i += 2) {
-            uint32_t e;
-            e = dt[st0]; emit(i, e & 0xff); st0 = (e >> 16) + br.read((e >> 8) & 0xff);
-            e = dt[st1]; emit(i + 1, e & 0xff); st1 = (e >> 16) + br.read((e >> 8) & 0xff);
+        for (; i + 4 <= lastTr; i += 4) {
+            uint32_t const e0 = dt[st0], e1 = dt[st1];
+            st0 = (e0 >> 16) + br.read((e0 >> 8) & 0xff);
+            st1 = (e1 >> 16) + br.read((e1 >> 8) & 0xff);
+            uint32_t const e2 = dt[st0], e3 = dt[st1];
+            st0 = (e2 >> 16) + br.read((e2 >> 8) & 0xff);
+            st1 = (e3 >> 16) + br.read((e3 >> 8) & 0xff);
+            put4(i, (e0 & 0xff) | ((e1 & 0xff) << 8) | ((e2 & 0xff) << 16) | ((e3 & 0xff) << 24));
         }
     }
+    // remaining symbols, state (i % nbStates) rotated into st0
     for (; i < n; i++) {
-        uint32_t const k = i % nst;
-        uint32_t& s = k == 0 ? st0 : (k == 1 ? st1 : (k == 2 ? st2 : st3));
-        uint32_t const e = dt[s];
-        emit(i, e & 0xff);
-        if (i < lastTr) s = (e >> 16) + br.read((e >> 8) & 0xff);
+        uint32_t const e = dt[st0];
+        out[i] = uint8_t(e);
+        uint32_t ns = st0;
+        if (i < lastTr) ns = (e >> 16) + br.read((e >> 8) & 0xff);
+        if (nst == 4) {
+            st0 = st1; st1 = st2; st2 = st3; st3 = ns;
+        } else {
+            st0 = st1; st1 = ns;
+        }
     }
-    if (br.pos != 0) reportError(status, DERR_CORRUPTION);
+    if (!br.finished()) reportError(status, DERR_CORRUPTION);
 }
 
 // ---------------------------------------------------------------------------
 // Huffman: weights -> canonical table (symbols ranked by weight then value;
 // weight w spans 2^(w-1) cells, nbBits = tableLog + 1 - w), after
-// src/openzl/fse/decompress/huf_decompress.c:342-454. One lane per stream;
-// the 4 streams of a 4X chunk share the chunk's table. Entry: symbol | nbBits<<8.
+// src/openzl/fse/decompress/huf_decompress.c:342-454. Four lanes per chunk
+// (one per stream of a 4X chunk; lane 0 alone for 1X) share the chunk's table
+// (entry: symbol | nbBits << 8). Lane 0 ranks the symbols; all four fill.
 constexpr uint32_t kHufTableLog = 12;
 
-__device__ bool hufBuild(uint16_t* dt, const uint8_t* weights, uint32_t nbW, uint32_t& tlOut)
-{
-    uint32_t counts[16];
-    for (int k = 0; k < 16; k++) counts[k] = 0;
-    uint32_t sum = 0;
-    for (uint32_t s = 0; s < nbW; s++) {
-        uint32_t const w = weights[s];
-        if (w > 12) return false;
-        counts[w]++;
-        sum += (1u << w) >> 1;
-    }
-    if (sum == 0 || (sum & (sum - 1))) return false;
-    uint32_t const tl = 31 - __clz(sum);
-    if (tl > 12 || nbW - counts[0] < 2) return false;
-    uint32_t start[16];
-    uint32_t p = 0;
-    for (uint32_t w = 1; w <= tl; w++) {
-        start[w] = p;
-        p += counts[w] << (w - 1);
-    }
-    for (uint32_t s = 0; s < nbW; s++) {
-        uint32_t const w = weights[s];
-        if (!w) continue;
-        uint32_t const len = 1u << (w - 1);
-        uint16_t const e = uint16_t(s | ((tl + 1 - w) << 8));
-        for (uint32_t u = 0; u < len; u++) dt[start[w] + u] = e;
-        start[w] += len;
-    }
-    tlOut = tl;
-    return true;
-}
+__device__ __forceinline__ uint32_t hufChunksPerCta(uint32_t tlMax) { return tlMax <= 11 ? 32u : 24u; }
+__device__ __forceinline__ uint32_t hufSlotBytes(uint32_t tlMax) { return (2u << tlMax) + 512u + 4u; }
 
-__global__ void kHuf(const HufTask* __restrict__ tasks, uint32_t nbTasks, uint32_t chunksPerCta,
-                     uint32_t* __restrict__ status)
+__global__ void __launch_bounds__(128) kHuf(const HufTask* __restrict__ tasks, uint32_t nbTasks, uint32_t tableLogMax,
+                                            uint32_t* __restrict__ status)
 {
-    extern __shared__ uint16_t smemHuf[];
+    extern __shared__ __align__(16) uint8_t smemHuf[];
     __shared__ uint32_t sTl[32];
     __shared__ uint8_t sOk[32];
+    uint32_t const chunks = hufChunksPerCta(tableLogMax);
     uint32_t const c = threadIdx.x >> 2;       // chunk slot in this CTA
     uint32_t const sIdx = threadIdx.x & 3;     // stream within the chunk
-    uint32_t const ti = blockIdx.x * chunksPerCta + c;
-    bool const active = c < chunksPerCta && ti < nbTasks;
-    uint16_t* const dt = smemHuf + (size_t(c) << kHufTableLog);
+    uint32_t const ti = blockIdx.x * chunks + c;
+    bool const active = c < chunks && ti < nbTasks;
+    uint8_t* const base = smemHuf + size_t(c < chunks ? c : 0) * hufSlotBytes(tableLogMax);
+    uint16_t* const dt = reinterpret_cast<uint16_t*>(base);
+    uint16_t* const first = reinterpret_cast<uint16_t*>(base + (2u << tableLogMax)); // first cell per symbol
     HufTask t{};
+    uint32_t nbW = 0;
     if (active) {
         t = tasks[ti];
+        nbW = t.nbWeights;
         if (sIdx == 0) {
+            // rank: weight class w starts after all cells of lower classes
+            uint32_t counts[13];
+#pragma unroll
+            for (int k = 0; k < 13; k++) counts[k] = 0;
+            uint32_t sum = 0;
+            bool ok = nbW <= 256;
+            for (uint32_t s = 0; s < nbW && ok; s++) {
+                uint32_t const w = t.weights[s];
+                if (w > 12) { ok = false; break; }
+#pragma unroll
+                for (int k = 1; k < 13; k++) counts[k] += (w == uint32_t(k));
+                sum += (1u << w) >> 1;
+            }
             uint32_t tl = 0;
-            sOk[c] = hufBuild(dt, t.weights, t.nbWeights, tl) ? 1 : 0;
+            if (ok) ok = sum != 0 && !(sum & (sum - 1));
+            if (ok) {
+                tl = 31 - __clz(sum);
+                ok = tl <= tableLogMax;
+            }
+            uint32_t nz = 0;
+#pragma unroll
+            for (int k = 1; k < 13; k++) nz += counts[k];
+            if (ok && nz < 2) ok = false;
+            if (ok) {
+                uint32_t start[13];
+                uint32_t p = 0;
+#pragma unroll
+                for (int k = 1; k < 13; k++) {
+                    start[k] = p;
+                    if (uint32_t(k) <= tl) p += counts[k] << (k - 1);
+                }
+                for (uint32_t s = 0; s < nbW; s++) {
+                    uint32_t const w = t.weights[s];
+                    uint32_t f = 0;
+#pragma unroll
+                    for (int k = 1; k < 13; k++)
+                        if (w == uint32_t(k)) { f = start[k]; start[k] += 1u << (k - 1); }
+                    first[s] = uint16_t(f);
+                }
+            }
+            sOk[c] = ok ? 1 : 0;
             sTl[c] = tl;
+        }
+    }
+    __syncthreads();
+    if (active && sOk[c]) {
+        uint32_t const tl = sTl[c];
+        for (uint32_t s = sIdx; s < nbW; s += 4) {
+            uint32_t const w = t.weights[s];
+            if (!w) continue;
+            uint32_t const len = 1u << (w - 1);
+            uint16_t const e = uint16_t(s | ((tl + 1 - w) << 8));
+            uint32_t const f = first[s];
+            for (uint32_t u = 0; u < len; u++) dt[f + u] = e;
         }
     }
     __syncthreads();
@@ -599,9 +665,10 @@ __global__ void kHuf(const HufTask* __restrict__ tasks, uint32_t nbTasks, uint32
         if (3ull * seg > t.dstSize) { if (sIdx == 0) reportError(status, DERR_CORRUPTION); return; }
         uint32_t const lens[4] = { l1, l2, l3, l4 };
         uint32_t off = 6;
-        for (uint32_t k = 0; k < sIdx; k++) off += lens[k];
+#pragma unroll
+        for (uint32_t k = 0; k < 3; k++) off += k < sIdx ? lens[k] : 0;
         sp = t.bits + off;
-        ssize = lens[sIdx];
+        ssize = sIdx == 0 ? l1 : (sIdx == 1 ? l2 : (sIdx == 2 ? l3 : l4));
         o0 = seg * sIdx;
         n = sIdx == 3 ? t.dstSize - 3 * seg : seg;
     } else {
@@ -611,15 +678,34 @@ __global__ void kHuf(const HufTask* __restrict__ tasks, uint32_t nbTasks, uint32
         o0 = 0;
         n = t.dstSize;
     }
-    BitRev br;
+    BitIn br;
     if (!br.init(sp, ssize)) { reportError(status, DERR_CORRUPTION); return; }
     uint8_t* const out = t.out + o0;
-    for (uint32_t i = 0; i < n; i++) {
+    uint32_t i = 0;
+    // unaligned head, then four symbols per 32-bit store
+    uint32_t const head = uint32_t((4 - (reinterpret_cast<uintptr_t>(out) & 3)) & 3);
+    for (; i < head && i < n; i++) {
         uint32_t const e = dt[br.peek(tl)];
-        out[i] = uint8_t(e & 0xff);
+        out[i] = uint8_t(e);
         br.skip(e >> 8);
     }
-    if (br.pos != 0) reportError(status, DERR_CORRUPTION);
+    for (; i + 4 <= n; i += 4) {
+        uint32_t const e0 = dt[br.peek(tl)];
+        br.skip(e0 >> 8);
+        uint32_t const e1 = dt[br.peek(tl)];
+        br.skip(e1 >> 8);
+        uint32_t const e2 = dt[br.peek(tl)];
+        br.skip(e2 >> 8);
+        uint32_t const e3 = dt[br.peek(tl)];
+        br.skip(e3 >> 8);
+        *reinterpret_cast<uint32_t*>(out + i) = (e0 & 0xff) | ((e1 & 0xff) << 8) | ((e2 & 0xff) << 16) | ((e3 & 0xff) << 24);
+    }
+    for (; i < n; i++) {
+        uint32_t const e = dt[br.peek(tl)];
+        out[i] = uint8_t(e);
+        br.skip(e >> 8);
+    }
+    if (!br.finished()) reportError(status, DERR_CORRUPTION);
 }
 
 // ---------------------------------------------------------------------------
@@ -835,22 +921,21 @@ __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks
 namespace ozl {
 
 namespace {
-constexpr uint32_t kFseSmemBudget = 96 * 1024;  // per CTA: two CTAs per SM
-constexpr uint32_t kHufChunksPerCta = 8;
-uint32_t fseLanes(uint32_t tlMax)
+uint32_t fseLanesPerWarp(uint32_t tlMax)
 {
-    uint32_t const per = 4u << tlMax;
-    uint32_t lanes = kFseSmemBudget / per;
+    uint32_t const per = (4u << tlMax) + 512u + 4u;
+    uint32_t lanes = kFseSmemMax / (kFseWarps * per);
     return lanes > 32 ? 32 : (lanes < 1 ? 1 : lanes);
 }
+uint32_t hufChunks(uint32_t tlMax) { return tlMax <= 11 ? 32u : 24u; }
+uint32_t hufSmem(uint32_t tlMax) { return hufChunks(tlMax) * ((2u << tlMax) + 512u + 4u); }
 } // namespace
 
 cudaError_t prepareKernels()
 {
-    cudaError_t e = cudaFuncSetAttribute(kFse, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFseSmemBudget));
+    cudaError_t e = cudaFuncSetAttribute(kFse, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFseSmemMax));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(kHuf, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(kHufChunksPerCta * (2u << kHufTableLog)));
+    return cudaFuncSetAttribute(kHuf, cudaFuncAttributeMaxDynamicSharedMemorySize, int(hufSmem(kHufTableLog)));
 }
 
 long runLaunches(const DeviceLayout& L, uint8_t* dPool, uint8_t* dScratch, uint32_t* dStatus, cudaStream_t s)
@@ -880,16 +965,20 @@ long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dSc
                 kConst<<<l.nbTiles, 256, 0, s>>>(static_cast<const ConstTask*>(tasks), tiles);
                 break;
             case KIND_FSE: {
-                uint32_t const lanes = fseLanes(l.param0);
-                uint32_t const grid = (l.nbTasks + lanes - 1) / lanes;
-                kFse<<<grid, 32, lanes * (4u << l.param0), s>>>(static_cast<const FseTask*>(tasks), l.nbTasks, lanes,
-                                                                 l.param0, dStatus);
+                uint32_t const lanes = fseLanesPerWarp(l.param0);
+                uint32_t const perCta = kFseWarps * lanes;
+                uint32_t const grid = (l.nbTasks + perCta - 1) / perCta;
+                uint32_t const smem = perCta * ((4u << l.param0) + 512u + 4u);
+                kFse<<<grid, 32 * kFseWarps, smem, s>>>(static_cast<const FseTask*>(tasks), l.nbTasks, lanes,
+                                                          l.param0, dStatus);
                 break;
             }
             case KIND_HUF: {
-                uint32_t const grid = (l.nbTasks + kHufChunksPerCta - 1) / kHufChunksPerCta;
-                kHuf<<<grid, 4 * kHufChunksPerCta, kHufChunksPerCta * (2u << kHufTableLog), s>>>(
-                        static_cast<const HufTask*>(tasks), l.nbTasks, kHufChunksPerCta, dStatus);
+                uint32_t const tlMax = l.param0 ? l.param0 : kHufTableLog;
+                uint32_t const chunks = hufChunks(tlMax);
+                uint32_t const grid = (l.nbTasks + chunks - 1) / chunks;
+                kHuf<<<grid, 4 * chunks, hufSmem(tlMax), s>>>(static_cast<const HufTask*>(tasks), l.nbTasks, tlMax,
+                                                              dStatus);
                 break;
             }
             case KIND_FLATPACK:

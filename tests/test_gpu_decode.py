@@ -93,3 +93,30 @@ def test_truncated_frame_is_rejected_on_host(gpu_lib):
     fr = read_frame("ts_i64_dz_bitpack_huf")
     with pytest.raises(oz.ZLError):
         oz.DCtx().decompress(fr[: len(fr) // 3])
+
+
+def test_device_api_side_stream_back_to_back(gpu_lib):
+    """Many frames of growing size decoded one call after another on a
+    non-blocking stream: each call's plan upload is ordered before its own
+    kernels (a plan uploaded off-stream raced the next frame's launch)."""
+    import torch
+    import openzl_gb300 as oz
+
+    rng = np.random.default_rng(5)
+    s = torch.cuda.Stream()
+    d = oz.DCtx()
+    cases = []
+    for k in range(24):
+        n = int(2000 * 1.5 ** k) // 8 + 1
+        a = (1000 + np.cumsum(rng.integers(-300, 301, n))).astype(np.uint32)
+        recipe = 3 if k % 2 else 4
+        cases.append((a, oracle.compress(recipe, a, 4)))
+    dfr = [_dev(torch, f.tobytes()) for _, f in cases]
+    outs = [torch.zeros(a.nbytes + 64, dtype=torch.uint8, device="cuda") for a, _ in cases]
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        for (a, f), df, o in zip(cases, dfr, outs):
+            d.decompress_device(f, df.data_ptr(), o.data_ptr(), a.nbytes, s.cuda_stream)
+    s.synchronize()
+    for (a, _), o in zip(cases, outs):
+        assert o[: a.nbytes].cpu().numpy().tobytes() == a.tobytes()
