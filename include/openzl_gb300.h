@@ -202,6 +202,21 @@ const char* ozl_gpu_encoder_error(const OZL_GpuEncoder* e);
  * device memory; computed on the GPU. Returns the hash in the report value. */
 ZL_Report ozl_gpu_xxh3_64(const void* d_data, size_t len, void* stream);
 
+/* Allocation-free variant of ozl_gpu_xxh3_64 (no counterpart in the
+ * reference), for callers that cannot call cudaMalloc: the same hash and
+ * kernels, with their scratch (task, block list, per-1 KiB block sums and the
+ * result) in one fixed file-scope device array of OZL_XXH3_STATIC_SCRATCH
+ * bytes per device instead of a per-call allocation. Accepts at most
+ * OZL_XXH3_STATIC_MAX_LEN bytes; longer inputs return
+ * ZL_ErrorCode_srcSize_tooLarge without touching the device. Calls no
+ * allocating routine. Every call on a device shares that array: calls whose
+ * work overlaps on the GPU (other streams, other host threads) race and must
+ * be serialized by the caller. Synchronizes `stream`; returns the hash in the
+ * report value. */
+#define OZL_XXH3_STATIC_MAX_LEN ((size_t)32 << 20)
+#define OZL_XXH3_STATIC_SCRATCH ((size_t)256 + ((size_t)32 << 10) * 72)
+ZL_Report ozl_gpu_xxh3_64_static(const void* d_data, size_t len, void* stream);
+
 /* Library build identification (for load checks). */
 const char* ozl_gpu_version(void);
 

@@ -12,6 +12,8 @@ from ._lib import (  # noqa: F401
     GpuEncoder,
     decompress,
     xxh3_64_device,
+    xxh3_64_device_static,
+    XXH3_STATIC_MAX_LEN,
     get_decompressed_size,
     get_compressed_size,
     library,

@@ -54,6 +54,7 @@ def library():
         "ozl_gpu_batch_error": ([vp], ctypes.c_char_p),
         "ozl_gpu_version": ([], ctypes.c_char_p),
         "ozl_gpu_xxh3_64": ([vp, sz, vp], ZLReport),
+        "ozl_gpu_xxh3_64_static": ([vp, sz, vp], ZLReport),
         "ozl_gpu_batch_profile": ([vp, vp, vp, vp, vp, sz], ZLReport),
         "ozl_gpu_kind_name": ([ctypes.c_int], ctypes.c_char_p),
         "ozl_gpu_batch_run_host": ([vp, vp, sz, vp, sz, vp, ctypes.c_int], ZLReport),
@@ -144,6 +145,18 @@ class DCtx:
 def xxh3_64_device(dev_ptr, length, stream=0):
     """XXH3-64 of device memory, computed on the GPU."""
     return _check(library().ozl_gpu_xxh3_64(dev_ptr, length, stream))
+
+
+XXH3_STATIC_MAX_LEN = 32 << 20
+
+
+def xxh3_64_device_static(dev_ptr, length, stream=0):
+    """XXH3-64 of device memory through the allocation-free entry point
+    (fixed device scratch shared by all calls; at most XXH3_STATIC_MAX_LEN
+    bytes; calls that overlap on the GPU race)."""
+    rep = library().ozl_gpu_xxh3_64_static(dev_ptr, length, stream)
+    _check(rep)
+    return rep.value
 
 
 def decompress(frame):

@@ -1068,3 +1068,95 @@ cudaError_t xxh3Device(const uint8_t* data, uint64_t len, uint64_t* dHashOut, ui
     return cudaStreamSynchronize(s);
 }
 } // namespace ozl
+
+// ---------------------------------------------------------------------------
+// Allocation-free XXH3 (ozl_gpu_xxh3_64_static): the hash kernels above, fed
+// from one file-scope device array instead of allocated scratch.
+//
+// Array layout: [0, 128) the task, [128, 136) the result, [256, ...) the
+// per-block sums (64 bytes per 1 KiB block), then the block list (8 bytes per
+// block). Nothing in it has to start at zero: each call writes the task, the
+// block list and every block sum it reads, and clears the result word first.
+// Calls that overlap on the GPU share the array and race.
+#include "../../include/openzl_gb300.h"
+
+#include <mutex>
+
+namespace {
+
+constexpr uint64_t kStaticMaxLen = OZL_XXH3_STATIC_MAX_LEN;
+constexpr uint32_t kStaticMaxBlocks = uint32_t(kStaticMaxLen / ozl::kHashBlock);
+constexpr size_t kStaticScratch = OZL_XXH3_STATIC_SCRATCH;
+static_assert(kStaticScratch >= 256 + size_t(kStaticMaxBlocks) * (64 + sizeof(ozl::TileRef)), "scratch layout");
+static_assert(sizeof(ozl::HashTask) <= 128, "task slot");
+
+static __device__ __align__(256) uint8_t gXxh3Scratch[kStaticScratch];
+
+// Writes the task and the block list into the array (one launch, no host copy).
+__global__ void kStageHashStatic(ozl::HashTask t, ozl::HashTask* dTask, ozl::TileRef* dBlocks, uint32_t nbBlocks,
+                                 uint64_t* dResult)
+{
+    uint32_t const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        *dTask = t;
+        *dResult = 0;
+    }
+    if (i < nbBlocks) dBlocks[i] = ozl::TileRef{ 0, i };
+}
+
+constexpr int kMaxDevices = 64;
+std::mutex gStaticMu;
+uint8_t* gStaticPtr[kMaxDevices] = {};
+
+// Device address of the array on the current device, looked up once per
+// device with that device current.
+cudaError_t staticScratch(uint8_t** out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(gStaticMu);
+    if (!gStaticPtr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, gXxh3Scratch);
+        if (e != cudaSuccess) return e;
+        gStaticPtr[dev] = static_cast<uint8_t*>(p);
+    }
+    *out = gStaticPtr[dev];
+    return cudaSuccess;
+}
+
+} // namespace
+
+extern "C" ZL_Report ozl_gpu_xxh3_64_static(const void* d_data, size_t len, void* stream)
+{
+    if (len > kStaticMaxLen) return ZL_Report{ ZL_ErrorCode_srcSize_tooLarge, 0 };
+    if (!d_data && len) return ZL_Report{ ZL_ErrorCode_parameter_invalid, 0 };
+    uint8_t* base = nullptr;
+    if (staticScratch(&base) != cudaSuccess) return ZL_Report{ ZL_ErrorCode_GENERIC, 0 };
+    cudaStream_t const s = static_cast<cudaStream_t>(stream);
+    uint32_t const nbBlocks = len > 240 ? uint32_t((len - 1) / ozl::kHashBlock) : 0;
+    auto* dTask = reinterpret_cast<ozl::HashTask*>(base);
+    auto* dResult = reinterpret_cast<uint64_t*>(base + 128);
+    auto* dSums = reinterpret_cast<uint64_t*>(base + 256);
+    auto* dBlocks = reinterpret_cast<ozl::TileRef*>(base + 256 + size_t(kStaticMaxBlocks) * 64);
+    ozl::HashTask t{};
+    t.data = static_cast<const uint8_t*>(d_data);
+    t.len = len;
+    t.blockSums = dSums;
+    t.nbBlocks = nbBlocks;
+    t.aligned8 = (reinterpret_cast<uintptr_t>(d_data) & 7) == 0;
+    t.hashOut = dResult;
+    uint32_t const stageThreads = nbBlocks > 0 ? nbBlocks : 1;
+    kStageHashStatic<<<(stageThreads + 255) / 256, 256, 0, s>>>(t, dTask, dBlocks, nbBlocks, dResult);
+    if (nbBlocks) ozl::kHashBlocks<<<(nbBlocks * 32 + 255) / 256, 256, 0, s>>>(dTask, dBlocks, nbBlocks);
+    ozl::kHashFinish<<<1, 32, 0, s>>>(dTask, 1, nullptr);
+    if (cudaGetLastError() != cudaSuccess) return ZL_Report{ ZL_ErrorCode_GENERIC, 0 };
+    uint64_t h = 0;
+    if (cudaMemcpyAsync(&h, dResult, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess
+        || cudaStreamSynchronize(s) != cudaSuccess)
+        return ZL_Report{ ZL_ErrorCode_GENERIC, 0 };
+    return ZL_Report{ ZL_ErrorCode_no_error, size_t(h) };
+}
+
