@@ -1063,22 +1063,39 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
     };
     auto addPlain = [&](int kind, int lv, auto& tasks) {
         if (tasks.empty()) return;
-        Launch L{};
+        auto emit = [&](auto& part, uint32_t param0) {
+            if (part.empty()) return;
+            Launch L{};
+            L.param0 = param0;
+            for (auto& t : part) L.algoBytes += taskBytes(t);
+            L.kind = kind;
+            L.level = lv;
+            L.taskOff = pool.put(part);
+            L.nbTasks = uint32_t(part.size());
+            out.launches.push_back(L);
+        };
         if constexpr (std::is_same_v<std::decay_t<decltype(tasks[0])>, FseTask>) {
-            // similar chunks side by side: largest tables first, then by length
-            std::sort(tasks.begin(), tasks.end(), [](const FseTask& a, const FseTask& b) {
-                return a.tableLog != b.tableLog ? a.tableLog > b.tableLog : a.dstSize > b.dstSize;
-            });
-            uint32_t tlMax = 5;
-            for (auto& t : tasks) tlMax = std::max<uint32_t>(tlMax, t.tableLog);
-            L.param0 = tlMax;
+            // Two launches by table size (a lane's table takes 3 << tableLog
+            // bytes of shared memory): small tables (Huffman weights and the
+            // like) run many lanes per CTA. Within each, longest chunks first.
+            std::vector<FseTask> small, large;
+            for (auto& t : tasks) (t.tableLog <= 8 ? small : large).push_back(t);
+            auto order = [](const FseTask& a, const FseTask& b) {
+                return a.dstSize != b.dstSize ? a.dstSize > b.dstSize : a.tableLog > b.tableLog;
+            };
+            std::sort(large.begin(), large.end(), order);
+            std::sort(small.begin(), small.end(), order);
+            uint32_t tlLarge = 9, tlSmall = 5;
+            for (auto& t : large) tlLarge = std::max<uint32_t>(tlLarge, t.tableLog);
+            for (auto& t : small) tlSmall = std::max<uint32_t>(tlSmall, t.tableLog);
+            emit(large, tlLarge);
+            emit(small, tlSmall);
+        } else {
+            if constexpr (std::is_same_v<std::decay_t<decltype(tasks[0])>, HufTask>)
+                std::stable_sort(tasks.begin(), tasks.end(),
+                                 [](const HufTask& a, const HufTask& b) { return a.dstSize > b.dstSize; });
+            emit(tasks, 0);
         }
-        for (auto& t : tasks) L.algoBytes += taskBytes(t);
-        L.kind = kind;
-        L.level = lv;
-        L.taskOff = pool.put(tasks);
-        L.nbTasks = uint32_t(tasks.size());
-        out.launches.push_back(L);
     };
     for (int lv = 0; lv <= maxLevel; lv++) {
         Buckets& b = B[lv];

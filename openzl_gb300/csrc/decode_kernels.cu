@@ -379,50 +379,65 @@ __global__ void kFlatpack(const FlatpackTask* __restrict__ tasks, const TileRef*
 }
 
 // ---------------------------------------------------------------------------
-// Backward bit reader (FSE / Huffman bitstreams): fields are read most
+// Backward bit readers (FSE / Huffman bitstreams): fields are read most
 // significant bit first from the end of the stream towards its start.
 //
-// The stream is read as aligned 32-bit words (a word holding at least one
-// byte of the stream never crosses a page), through the L1 cache, with the
-// next lower word loaded one word ahead and the cache line two lines below
-// prefetched whenever a line boundary is crossed. Positions are bit indices
-// above bit 0 of the aligned word that holds the stream's first byte.
-// Invariant between reads: cb + 32 < pos <= cb + 64, where the 64-bit
-// container c holds the words at bit indices [cb, cb + 64); fields are at most
-// 32 bits, so every field lies inside the container.
+// Streams are read as aligned 32-bit words (a word holding at least one byte
+// of the stream never crosses a page), never above the word that holds the
+// stream's last byte and never below its first. Three words below the window
+// are held in registers (loaded three refills before use) and the stream is
+// prefetched into L2 512 bytes ahead. Positions are bit indices above bit 0 of
+// the aligned word that holds the stream's first byte.
+__device__ __forceinline__ uint32_t streamWord(const uint32_t* w, int32_t k) { return k >= 0 ? __ldg(w + k) : 0u; }
+
+__device__ __forceinline__ void prefetchAhead(const uint32_t* w, int32_t k)
+{
+    // k: index of the word just loaded; every 32 words, touch the line 128 words below
+    if ((k & 31) == 0 && k >= 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(w + k - 128));
+}
+
+__device__ __forceinline__ bool streamStart(const uint8_t* p, uint32_t size, const uint32_t*& w, int32_t& pos,
+                                            int32_t& end)
+{
+    if (size == 0) return false;
+    uint8_t const last = p[size - 1];
+    if (last == 0) return false;
+    uintptr_t const a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(3);
+    w = reinterpret_cast<const uint32_t*>(a);
+    end = int32_t(reinterpret_cast<uintptr_t>(p) - a) * 8;
+    pos = end + int32_t(size - 1) * 8 + (31 - __clz(uint32_t(last)));
+    return true;
+}
+
+// 64-bit window (Huffman: one field at a time, at most 12 bits).
+// Invariant between reads: cb + 32 < pos <= cb + 64.
 struct BitIn {
     const uint32_t* w;
-    int32_t pos;   // unread bits
-    int32_t end;   // position of the stream's first bit (0..24)
-    int32_t cb;    // bit index of c's least significant bit (multiple of 32)
+    int32_t pos, end, cb;
     uint64_t c;
-    uint32_t ahead; // the word below c
-
-    __device__ __forceinline__ static uint32_t word(const uint32_t* w, int32_t k) { return k >= 0 ? __ldg(w + k) : 0u; }
+    uint32_t a1, a2, a3; // the three words below the window
 
     __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size)
     {
-        if (size == 0) return false;
-        uint8_t const last = p[size - 1];
-        if (last == 0) return false;
-        uintptr_t const a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(3);
-        w = reinterpret_cast<const uint32_t*>(a);
-        end = int32_t(reinterpret_cast<uintptr_t>(p) - a) * 8;
-        pos = end + int32_t(size - 1) * 8 + (31 - __clz(uint32_t(last)));
+        if (!streamStart(p, size, w, pos, end)) return false;
         int32_t const j = ((pos - 1) >> 5) - 1; // arithmetic shift: floor
         cb = j * 32;
-        c = (uint64_t(word(w, j + 1)) << 32) | word(w, j);
-        ahead = word(w, j - 1);
+        c = (uint64_t(streamWord(w, j + 1)) << 32) | streamWord(w, j);
+        a1 = streamWord(w, j - 1);
+        a2 = streamWord(w, j - 2);
+        a3 = streamWord(w, j - 3);
         return true;
     }
     __device__ __forceinline__ void renorm()
     {
         if (pos <= cb + 32) {
-            c = (c << 32) | ahead;
+            c = (c << 32) | a1;
+            a1 = a2;
+            a2 = a3;
             cb -= 32;
-            int32_t const k = (cb >> 5) - 1;
-            ahead = word(w, k);
-            if ((k & 31) == 0 && k >= 64) asm volatile("prefetch.global.L1 [%0];" ::"l"(w + k - 64));
+            int32_t const k = (cb >> 5) - 3;
+            a3 = streamWord(w, k);
+            prefetchAhead(w, k);
         }
     }
     __device__ __forceinline__ uint32_t peek(uint32_t nb) const
@@ -447,33 +462,92 @@ struct BitIn {
     __device__ __forceinline__ bool finished() const { return pos == end; }
 };
 
+// 128-bit window (FSE: four fields of at most 12 bits per group, their
+// offsets known from the table entries before any of them is read).
+// Invariant between groups: cb + 64 <= pos <= cb + 96, so the 48 bits below
+// pos lie in the window at shift pos - 48 - cb, between 16 and 48.
+struct BitWin {
+    const uint32_t* w;
+    int32_t pos, end, cb;
+    uint64_t lo, hi;
+    uint32_t a1, a2, a3;
+
+    __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size)
+    {
+        if (!streamStart(p, size, w, pos, end)) return false;
+        int32_t const jt = (pos - 1) >> 5; // word of the top unread bit
+        cb = (jt - 2) * 32;
+        lo = uint64_t(streamWord(w, jt - 2)) | (uint64_t(streamWord(w, jt - 1)) << 32);
+        hi = streamWord(w, jt);
+        a1 = streamWord(w, jt - 3);
+        a2 = streamWord(w, jt - 4);
+        a3 = streamWord(w, jt - 5);
+        return true;
+    }
+    __device__ __forceinline__ void shift()
+    {
+        hi = (hi << 32) | (lo >> 32);
+        lo = (lo << 32) | a1;
+        a1 = a2;
+        a2 = a3;
+        cb -= 32;
+        int32_t const k = (cb >> 5) - 3;
+        a3 = streamWord(w, k);
+        prefetchAhead(w, k);
+    }
+    __device__ __forceinline__ void renorm()
+    {
+        if (pos - cb < 64) {
+            shift();
+            if (pos - cb < 64) shift();
+        }
+    }
+    // the 64 bits starting 48 bits below pos
+    __device__ __forceinline__ uint64_t view() const
+    {
+        uint32_t const s = uint32_t(pos - 48 - cb); // 16..48
+        return (lo >> s) | (hi << (64 - s));
+    }
+    // one field of nb bits (nb <= 12) just below pos
+    __device__ __forceinline__ uint32_t read(uint32_t nb)
+    {
+        uint64_t const v = view();
+        uint32_t const r = uint32_t(v >> (48 - nb)) & ((1u << nb) - 1u);
+        pos -= int32_t(nb);
+        renorm();
+        return r;
+    }
+    __device__ __forceinline__ bool finished() const { return pos == end; }
+};
+
 // ---------------------------------------------------------------------------
-// FSE: one lane per chunk; kFseWarps warps per CTA share the SM's shared
-// memory, each lane with its own decoding table (entry: newState (16) |
-// nbBits (8) | symbol (8)) and build counters.
+// FSE: one lane per chunk, lanes per CTA sized so that four CTAs fit an SM.
+// Each lane keeps its decoding table in shared memory as two arrays: the
+// state cell (newState | nbBits << 12) and the symbol byte, plus the build
+// counters. Four symbols per step: the four table entries are loaded
+// together, and their fields' offsets follow from the code lengths, so the
+// four reads share one 64-bit view of the stream.
 //
 // Table construction restates src/openzl/fse/decompress/fse_decompress.c:
 // 73-171; decode order restates fse_decompress.c:255-337 (state i % nbStates
 // emits symbol i; the last symbol of each state has no transition).
-constexpr uint32_t kFseWarps = 4;
-constexpr uint32_t kFseSmemMax = 227 * 1024;
+constexpr uint32_t kFseCtaSmem = 56 * 1024; // four CTAs per SM
 
-__device__ __forceinline__ uint32_t fseSlotBytes(uint32_t tlMax) { return (4u << tlMax) + 512u + 4u; }
+__host__ __device__ __forceinline__ uint32_t fseSlotBytes(uint32_t tlMax) { return (3u << tlMax) + 512u + 4u; }
 
-__global__ void __launch_bounds__(32 * kFseWarps) kFse(const FseTask* __restrict__ tasks, uint32_t nbTasks,
-                                                        uint32_t lanesPerWarp, uint32_t tableLogMax,
-                                                        uint32_t* __restrict__ status)
+__global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, uint32_t nbTasks, uint32_t lanes,
+                                           uint32_t tableLogMax, uint32_t* __restrict__ status)
 {
     extern __shared__ __align__(16) uint8_t smemFse[];
-    uint32_t const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane >= lanesPerWarp) return;
-    uint32_t const slot = warp * lanesPerWarp + lane;
-    uint32_t const ti = blockIdx.x * (kFseWarps * lanesPerWarp) + slot;
+    uint32_t const lane = threadIdx.x;
+    if (lane >= lanes) return;
+    uint32_t const ti = blockIdx.x * lanes + lane;
     if (ti >= nbTasks) return;
     FseTask const t = tasks[ti];
-    uint8_t* const base = smemFse + size_t(slot) * fseSlotBytes(tableLogMax);
-    uint32_t* const dt = reinterpret_cast<uint32_t*>(base);
-    uint16_t* const next = reinterpret_cast<uint16_t*>(base + (4u << tableLogMax));
+    uint8_t* const base = smemFse + size_t(lane) * fseSlotBytes(tableLogMax);
+    uint16_t* const cell = reinterpret_cast<uint16_t*>(base);
+    uint8_t* const sym = base + (2u << tableLogMax);
+    uint16_t* const next = reinterpret_cast<uint16_t*>(base + (3u << tableLogMax));
     uint32_t const tl = t.tableLog;
     uint32_t const size = 1u << tl, mask = size - 1;
     uint32_t const step = (size >> 1) + (size >> 3) + 3;
@@ -481,7 +555,7 @@ __global__ void __launch_bounds__(32 * kFseWarps) kFse(const FseTask* __restrict
     for (uint32_t s = 0; s < t.nbSym; s++) {
         int const c = t.norm[s];
         if (c == -1) {
-            dt[high--] = s;
+            sym[high--] = uint8_t(s);
             next[s] = 1;
         } else {
             next[s] = uint16_t(c);
@@ -491,19 +565,19 @@ __global__ void __launch_bounds__(32 * kFseWarps) kFse(const FseTask* __restrict
     for (uint32_t s = 0; s < t.nbSym; s++) {
         int const c = t.norm[s];
         for (int i = 0; i < c; i++) {
-            dt[pos] = s;
+            sym[pos] = uint8_t(s);
             do { pos = (pos + step) & mask; } while (pos > high);
         }
     }
     for (uint32_t u = 0; u < size; u++) {
-        uint32_t const s = dt[u] & 0xff;
+        uint32_t const s = sym[u];
         uint32_t const x = next[s]++;
         uint32_t const nb = tl - (31 - __clz(x));
         uint32_t const ns = (x << nb) - size;
-        dt[u] = s | (nb << 8) | (ns << 16);
+        cell[u] = uint16_t(ns | (nb << 12));
     }
 
-    BitIn br;
+    BitWin br;
     if (!br.init(t.bits, t.bitsSize)) { reportError(status, DERR_CORRUPTION); return; }
     uint32_t const nst = t.nbStates;
     uint32_t st0 = br.read(tl), st1 = br.read(tl), st2 = 0, st3 = 0;
@@ -522,33 +596,49 @@ __global__ void __launch_bounds__(32 * kFseWarps) kFse(const FseTask* __restrict
             out[i + 3] = uint8_t(word >> 24);
         }
     };
+    // one step of two or four transitions on consecutive states
+    auto step4 = [&](uint32_t& sa, uint32_t& sb, uint32_t& sc, uint32_t& sd) -> uint32_t {
+        uint32_t const ca = cell[sa], cb = cell[sb], cc = cell[sc], cd = cell[sd];
+        uint32_t const ya = sym[sa], yb = sym[sb], yc = sym[sc], yd = sym[sd];
+        uint32_t const na = ca >> 12, nb = cb >> 12, nc = cc >> 12, nd = cd >> 12;
+        uint64_t const v = br.view();
+        uint32_t const oa = 48 - na, ob = oa - nb, oc = ob - nc, od = oc - nd;
+        sa = (ca & 0xfff) + (uint32_t(v >> oa) & ((1u << na) - 1u));
+        sb = (cb & 0xfff) + (uint32_t(v >> ob) & ((1u << nb) - 1u));
+        sc = (cc & 0xfff) + (uint32_t(v >> oc) & ((1u << nc) - 1u));
+        sd = (cd & 0xfff) + (uint32_t(v >> od) & ((1u << nd) - 1u));
+        br.pos -= int32_t(48 - od);
+        br.renorm();
+        return ya | (yb << 8) | (yc << 16) | (yd << 24);
+    };
+    auto step2 = [&](uint32_t& sa, uint32_t& sb) -> uint32_t {
+        uint32_t const ca = cell[sa], cb = cell[sb];
+        uint32_t const ya = sym[sa], yb = sym[sb];
+        uint32_t const na = ca >> 12, nb = cb >> 12;
+        uint64_t const v = br.view();
+        uint32_t const oa = 48 - na, ob = oa - nb;
+        sa = (ca & 0xfff) + (uint32_t(v >> oa) & ((1u << na) - 1u));
+        sb = (cb & 0xfff) + (uint32_t(v >> ob) & ((1u << nb) - 1u));
+        br.pos -= int32_t(48 - ob);
+        br.renorm();
+        return ya | (yb << 8);
+    };
     uint32_t i = 0;
     if (nst == 4) {
-        for (; i + 4 <= lastTr; i += 4) {
-            uint32_t const e0 = dt[st0], e1 = dt[st1], e2 = dt[st2], e3 = dt[st3];
-            st0 = (e0 >> 16) + br.read((e0 >> 8) & 0xff);
-            st1 = (e1 >> 16) + br.read((e1 >> 8) & 0xff);
-            st2 = (e2 >> 16) + br.read((e2 >> 8) & 0xff);
-            st3 = (e3 >> 16) + br.read((e3 >> 8) & 0xff);
-            put4(i, (e0 & 0xff) | ((e1 & 0xff) << 8) | ((e2 & 0xff) << 16) | ((e3 & 0xff) << 24));
-        }
+        for (; i + 4 <= lastTr; i += 4) put4(i, step4(st0, st1, st2, st3));
     } else {
         for (; i + 4 <= lastTr; i += 4) {
-            uint32_t const e0 = dt[st0], e1 = dt[st1];
-            st0 = (e0 >> 16) + br.read((e0 >> 8) & 0xff);
-            st1 = (e1 >> 16) + br.read((e1 >> 8) & 0xff);
-            uint32_t const e2 = dt[st0], e3 = dt[st1];
-            st0 = (e2 >> 16) + br.read((e2 >> 8) & 0xff);
-            st1 = (e3 >> 16) + br.read((e3 >> 8) & 0xff);
-            put4(i, (e0 & 0xff) | ((e1 & 0xff) << 8) | ((e2 & 0xff) << 16) | ((e3 & 0xff) << 24));
+            uint32_t const lo = step2(st0, st1);
+            uint32_t const hi2 = step2(st0, st1);
+            put4(i, lo | (hi2 << 16));
         }
     }
     // remaining symbols, state (i % nbStates) rotated into st0
     for (; i < n; i++) {
-        uint32_t const e = dt[st0];
-        out[i] = uint8_t(e);
+        uint32_t const c = cell[st0];
+        out[i] = sym[st0];
         uint32_t ns = st0;
-        if (i < lastTr) ns = (e >> 16) + br.read((e >> 8) & 0xff);
+        if (i < lastTr) ns = (c & 0xfff) + br.read(c >> 12);
         if (nst == 4) {
             st0 = st1; st1 = st2; st2 = st3; st3 = ns;
         } else {
@@ -561,97 +651,61 @@ __global__ void __launch_bounds__(32 * kFseWarps) kFse(const FseTask* __restrict
 // ---------------------------------------------------------------------------
 // Huffman: weights -> canonical table (symbols ranked by weight then value;
 // weight w spans 2^(w-1) cells, nbBits = tableLog + 1 - w), after
-// src/openzl/fse/decompress/huf_decompress.c:342-454. Four lanes per chunk
-// (one per stream of a 4X chunk; lane 0 alone for 1X) share the chunk's table
-// (entry: symbol | nbBits << 8). Lane 0 ranks the symbols; all four fill.
+// src/openzl/fse/decompress/huf_decompress.c:342-454. One warp per CTA
+// decodes eight chunks, four lanes per chunk (one per stream of a 4X chunk;
+// lane 0 alone for 1X) sharing the chunk's table (entry: symbol |
+// nbBits << 8). Table slots hold tableLog 11, the largest the reference's
+// encoder emits (encode_entropy_binding.c:222, HUF_TABLELOG_DEFAULT); chunks
+// with tableLog 12 take two adjacent slots and are decoded in a second round
+// when their neighbour's slot is busy.
 constexpr uint32_t kHufTableLog = 12;
+constexpr uint32_t kHufChunks = 8;
+constexpr uint32_t kHufSlotCells = 1u << 11;
+constexpr uint32_t kHufSlotBytes = kHufSlotCells * 2 + 512 + 4;
 
-__device__ __forceinline__ uint32_t hufChunksPerCta(uint32_t tlMax) { return tlMax <= 11 ? 32u : 24u; }
-__device__ __forceinline__ uint32_t hufSlotBytes(uint32_t tlMax) { return (2u << tlMax) + 512u + 4u; }
-
-__global__ void __launch_bounds__(128) kHuf(const HufTask* __restrict__ tasks, uint32_t nbTasks, uint32_t tableLogMax,
-                                            uint32_t* __restrict__ status)
+__device__ bool hufRank(const uint8_t* weights, uint32_t nbW, uint16_t* first, uint32_t& tlOut)
 {
-    extern __shared__ __align__(16) uint8_t smemHuf[];
-    __shared__ uint32_t sTl[32];
-    __shared__ uint8_t sOk[32];
-    uint32_t const chunks = hufChunksPerCta(tableLogMax);
-    uint32_t const c = threadIdx.x >> 2;       // chunk slot in this CTA
-    uint32_t const sIdx = threadIdx.x & 3;     // stream within the chunk
-    uint32_t const ti = blockIdx.x * chunks + c;
-    bool const active = c < chunks && ti < nbTasks;
-    uint8_t* const base = smemHuf + size_t(c < chunks ? c : 0) * hufSlotBytes(tableLogMax);
-    uint16_t* const dt = reinterpret_cast<uint16_t*>(base);
-    uint16_t* const first = reinterpret_cast<uint16_t*>(base + (2u << tableLogMax)); // first cell per symbol
-    HufTask t{};
-    uint32_t nbW = 0;
-    if (active) {
-        t = tasks[ti];
-        nbW = t.nbWeights;
-        if (sIdx == 0) {
-            // rank: weight class w starts after all cells of lower classes
-            uint32_t counts[13];
+    uint32_t counts[13];
 #pragma unroll
-            for (int k = 0; k < 13; k++) counts[k] = 0;
-            uint32_t sum = 0;
-            bool ok = nbW <= 256;
-            for (uint32_t s = 0; s < nbW && ok; s++) {
-                uint32_t const w = t.weights[s];
-                if (w > 12) { ok = false; break; }
+    for (int k = 0; k < 13; k++) counts[k] = 0;
+    uint32_t sum = 0;
+    if (nbW > 256) return false;
+    for (uint32_t s = 0; s < nbW; s++) {
+        uint32_t const w = weights[s];
+        if (w > 12) return false;
 #pragma unroll
-                for (int k = 1; k < 13; k++) counts[k] += (w == uint32_t(k));
-                sum += (1u << w) >> 1;
-            }
-            uint32_t tl = 0;
-            if (ok) ok = sum != 0 && !(sum & (sum - 1));
-            if (ok) {
-                tl = 31 - __clz(sum);
-                ok = tl <= tableLogMax;
-            }
-            uint32_t nz = 0;
-#pragma unroll
-            for (int k = 1; k < 13; k++) nz += counts[k];
-            if (ok && nz < 2) ok = false;
-            if (ok) {
-                uint32_t start[13];
-                uint32_t p = 0;
-#pragma unroll
-                for (int k = 1; k < 13; k++) {
-                    start[k] = p;
-                    if (uint32_t(k) <= tl) p += counts[k] << (k - 1);
-                }
-                for (uint32_t s = 0; s < nbW; s++) {
-                    uint32_t const w = t.weights[s];
-                    uint32_t f = 0;
-#pragma unroll
-                    for (int k = 1; k < 13; k++)
-                        if (w == uint32_t(k)) { f = start[k]; start[k] += 1u << (k - 1); }
-                    first[s] = uint16_t(f);
-                }
-            }
-            sOk[c] = ok ? 1 : 0;
-            sTl[c] = tl;
-        }
+        for (int k = 1; k < 13; k++) counts[k] += (w == uint32_t(k));
+        sum += (1u << w) >> 1;
     }
-    __syncthreads();
-    if (active && sOk[c]) {
-        uint32_t const tl = sTl[c];
-        for (uint32_t s = sIdx; s < nbW; s += 4) {
-            uint32_t const w = t.weights[s];
-            if (!w) continue;
-            uint32_t const len = 1u << (w - 1);
-            uint16_t const e = uint16_t(s | ((tl + 1 - w) << 8));
-            uint32_t const f = first[s];
-            for (uint32_t u = 0; u < len; u++) dt[f + u] = e;
-        }
+    if (sum == 0 || (sum & (sum - 1))) return false;
+    uint32_t const tl = 31 - __clz(sum);
+    if (tl > kHufTableLog) return false;
+    uint32_t nz = 0;
+#pragma unroll
+    for (int k = 1; k < 13; k++) nz += counts[k];
+    if (nz < 2) return false;
+    uint32_t start[13];
+    uint32_t p = 0;
+#pragma unroll
+    for (int k = 1; k < 13; k++) {
+        start[k] = p;
+        if (uint32_t(k) <= tl) p += counts[k] << (k - 1);
     }
-    __syncthreads();
-    if (!active) return;
-    if (!sOk[c]) {
-        if (sIdx == 0) reportError(status, DERR_CORRUPTION);
-        return;
+    for (uint32_t s = 0; s < nbW; s++) {
+        uint32_t const w = weights[s];
+        uint32_t f = 0;
+#pragma unroll
+        for (int k = 1; k < 13; k++)
+            if (w == uint32_t(k)) { f = start[k]; start[k] += 1u << (k - 1); }
+        first[s] = uint16_t(f);
     }
-    uint32_t const tl = sTl[c];
+    tlOut = tl;
+    return true;
+}
+
+__device__ __forceinline__ void hufDecodeStream(const HufTask& t, const uint16_t* dt, uint32_t tl, uint32_t sIdx,
+                                                uint32_t* status)
+{
     const uint8_t* sp;
     uint32_t ssize, n, o0;
     if (t.x4) {
@@ -663,10 +717,10 @@ __global__ void __launch_bounds__(128) kHuf(const HufTask* __restrict__ tasks, u
         uint32_t const l4 = t.bitsSize - 6 - l1 - l2 - l3;
         uint32_t const seg = (t.dstSize + 3) / 4;
         if (3ull * seg > t.dstSize) { if (sIdx == 0) reportError(status, DERR_CORRUPTION); return; }
-        uint32_t const lens[4] = { l1, l2, l3, l4 };
         uint32_t off = 6;
-#pragma unroll
-        for (uint32_t k = 0; k < 3; k++) off += k < sIdx ? lens[k] : 0;
+        off += sIdx > 0 ? l1 : 0;
+        off += sIdx > 1 ? l2 : 0;
+        off += sIdx > 2 ? l3 : 0;
         sp = t.bits + off;
         ssize = sIdx == 0 ? l1 : (sIdx == 1 ? l2 : (sIdx == 2 ? l3 : l4));
         o0 = seg * sIdx;
@@ -706,6 +760,73 @@ __global__ void __launch_bounds__(128) kHuf(const HufTask* __restrict__ tasks, u
         br.skip(e >> 8);
     }
     if (!br.finished()) reportError(status, DERR_CORRUPTION);
+}
+
+__global__ void __launch_bounds__(32) kHuf(const HufTask* __restrict__ tasks, uint32_t nbTasks,
+                                           uint32_t* __restrict__ status)
+{
+    extern __shared__ __align__(16) uint8_t smemHuf[];
+    __shared__ uint32_t sTl[kHufChunks];
+    __shared__ uint8_t sOk[kHufChunks];
+    uint32_t const c = threadIdx.x >> 2;       // chunk slot in this CTA
+    uint32_t const sIdx = threadIdx.x & 3;     // stream within the chunk
+    uint32_t const ti = blockIdx.x * kHufChunks + c;
+    bool const active = ti < nbTasks;
+    uint8_t* const slot = smemHuf + size_t(c) * kHufSlotBytes;
+    uint16_t* const first = reinterpret_cast<uint16_t*>(slot + kHufSlotCells * 2); // first cell per symbol
+    HufTask t{};
+    if (active) t = tasks[ti];
+    if (sIdx == 0) {
+        uint32_t tl = 0;
+        bool const ok = active && hufRank(t.weights, t.nbWeights, first, tl);
+        sOk[c] = ok ? 1 : 0;
+        sTl[c] = tl;
+        if (active && !ok) reportError(status, DERR_CORRUPTION);
+    }
+    __syncwarp();
+    // tableLog <= 11: each chunk in its own slot
+    uint32_t const tl = sTl[c];
+    bool const narrow = active && sOk[c] && tl <= 11;
+    uint16_t* const dt = reinterpret_cast<uint16_t*>(slot);
+    if (narrow) {
+        for (uint32_t s = sIdx; s < t.nbWeights; s += 4) {
+            uint32_t const w = t.weights[s];
+            if (!w) continue;
+            uint32_t const len = 1u << (w - 1);
+            uint16_t const e = uint16_t(s | ((tl + 1 - w) << 8));
+            uint32_t const f = first[s];
+            for (uint32_t u = 0; u < len; u++) dt[f + u] = e;
+        }
+    }
+    __syncwarp();
+    if (narrow) hufDecodeStream(t, dt, tl, sIdx, status);
+    __syncwarp();
+    // tableLog 12 (valid, but never emitted by the reference's encoder): one
+    // chunk at a time, its table across the first slots, ranks recomputed
+    // into the spare area after the slots
+    uint16_t* const wideFirst = reinterpret_cast<uint16_t*>(smemHuf + size_t(kHufChunks) * kHufSlotBytes);
+    uint16_t* const wide = reinterpret_cast<uint16_t*>(smemHuf);
+    for (uint32_t k = 0; k < kHufChunks; k++) {
+        if (!(sOk[k] && sTl[k] > 11)) continue; // warp-uniform
+        HufTask const tk = tasks[blockIdx.x * kHufChunks + k];
+        if (threadIdx.x == 0) {
+            uint32_t tlk = 0;
+            hufRank(tk.weights, tk.nbWeights, wideFirst, tlk);
+        }
+        __syncwarp();
+        uint32_t const tlk = sTl[k];
+        for (uint32_t s = threadIdx.x; s < tk.nbWeights; s += 32) {
+            uint32_t const w = tk.weights[s];
+            if (!w) continue;
+            uint32_t const len = 1u << (w - 1);
+            uint16_t const e = uint16_t(s | ((tlk + 1 - w) << 8));
+            uint32_t const f = wideFirst[s];
+            for (uint32_t u = 0; u < len; u++) wide[f + u] = e;
+        }
+        __syncwarp();
+        if (threadIdx.x < 4) hufDecodeStream(tk, wide, tlk, threadIdx.x, status);
+        __syncwarp();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -838,31 +959,97 @@ __device__ uint64_t xxh3Short(const uint8_t* in, uint64_t len, bool al)
     return xAvalanche(acc);
 }
 
-// Phase 1: one warp per 1 KiB block; lane = (stripe group g, accumulator i).
-__global__ void kHashBlocks(const HashTask* __restrict__ tasks, const TileRef* __restrict__ blocks, uint32_t nbBlocks)
+// Phase 1: one warp per 1 KiB block. Lane L holds 16 bytes of each half
+// block (stripe L/4 (+8), words 2(L%4) and 2(L%4)+1), read as one aligned
+// 16-byte load; for data that is not 16-byte aligned the lane funnels its
+// aligned chunk with the next lane's (the last lane loads one more chunk,
+// which holds at least one byte of the task's data). Each lane adds both
+// words' increments (acc[i] += data[i^1] + lo32(data[i]^key[i]) * hi32(...))
+// and the warp reduces over stripes.
+__device__ __forceinline__ uint4 funnel16(uint4 c, uint4 n, uint32_t off)
 {
+    uint32_t const q = off >> 2, r = (off & 3) * 8;
+    uint32_t w[4];
+    switch (q) {
+        case 0:
+            w[0] = __funnelshift_r(c.x, c.y, r); w[1] = __funnelshift_r(c.y, c.z, r);
+            w[2] = __funnelshift_r(c.z, c.w, r); w[3] = __funnelshift_r(c.w, n.x, r);
+            break;
+        case 1:
+            w[0] = __funnelshift_r(c.y, c.z, r); w[1] = __funnelshift_r(c.z, c.w, r);
+            w[2] = __funnelshift_r(c.w, n.x, r); w[3] = __funnelshift_r(n.x, n.y, r);
+            break;
+        case 2:
+            w[0] = __funnelshift_r(c.z, c.w, r); w[1] = __funnelshift_r(c.w, n.x, r);
+            w[2] = __funnelshift_r(n.x, n.y, r); w[3] = __funnelshift_r(n.y, n.z, r);
+            break;
+        default:
+            w[0] = __funnelshift_r(c.w, n.x, r); w[1] = __funnelshift_r(n.x, n.y, r);
+            w[2] = __funnelshift_r(n.y, n.z, r); w[3] = __funnelshift_r(n.z, n.w, r);
+            break;
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__global__ void __launch_bounds__(256) kHashBlocks(const HashTask* __restrict__ tasks,
+                                                   const TileRef* __restrict__ blocks, uint32_t nbBlocks)
+{
+    __shared__ uint64_t sKey[24]; // secret words at byte offsets 0, 8, ..., 184
+    if (threadIdx.x < 24) sKey[threadIdx.x] = secret64(int(8 * threadIdx.x));
+    __syncthreads();
     uint32_t const warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint32_t const lane = threadIdx.x & 31;
     if (warp >= nbBlocks) return;
     TileRef const br = blocks[warp];
     HashTask const t = tasks[br.task];
     const uint8_t* const blk = t.data + uint64_t(br.tile) * kHashBlock;
-    uint32_t const i = lane & 7, g = lane >> 3;
-    bool const al = t.aligned8 != 0;
-    uint64_t s = 0;
-    for (uint32_t st = g; st < 16; st += 4) {
-        const uint8_t* const stripe = blk + 64 * st;
-        uint64_t const v = ldData(stripe + 8 * i, al);
-        uint64_t const vx = ldData(stripe + 8 * (i ^ 1), al);
-        uint64_t const k = v ^ secret64(int(8 * st + 8 * i));
-        s += vx + uint64_t(uint32_t(k)) * (k >> 32);
+    uintptr_t const base = reinterpret_cast<uintptr_t>(blk) & ~uintptr_t(15);
+    uint32_t const off = uint32_t(reinterpret_cast<uintptr_t>(blk) - base);
+    const uint4* const A = reinterpret_cast<const uint4*>(base);
+    uint32_t const j = lane & 3, sl = lane >> 2;
+    uint4 c[2];
+    c[0] = __ldg(A + lane);
+    c[1] = __ldg(A + 32 + lane);
+    if (off) {
+        uint4 const ext = lane == 31 ? __ldg(A + 64) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            uint4 n;
+            n.x = __shfl_down_sync(0xffffffffu, c[r].x, 1);
+            n.y = __shfl_down_sync(0xffffffffu, c[r].y, 1);
+            n.z = __shfl_down_sync(0xffffffffu, c[r].z, 1);
+            n.w = __shfl_down_sync(0xffffffffu, c[r].w, 1);
+            // lane 31's next chunk: round 0 -> lane 0 of round 1; round 1 -> ext
+            uint32_t const x = __shfl_sync(0xffffffffu, c[1].x, 0), y = __shfl_sync(0xffffffffu, c[1].y, 0);
+            uint32_t const z = __shfl_sync(0xffffffffu, c[1].z, 0), w = __shfl_sync(0xffffffffu, c[1].w, 0);
+            if (lane == 31) n = r == 0 ? make_uint4(x, y, z, w) : ext;
+            c[r] = funnel16(c[r], n, off);
+        }
     }
-    s += __shfl_xor_sync(0xffffffffu, s, 8);
-    s += __shfl_xor_sync(0xffffffffu, s, 16);
-    if (lane < 8) t.blockSums[8ull * br.tile + lane] = s;
+    uint64_t a0 = 0, a1 = 0;
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        uint32_t const st = sl + 8 * r;
+        uint64_t const w0 = uint64_t(c[r].x) | (uint64_t(c[r].y) << 32);
+        uint64_t const w1 = uint64_t(c[r].z) | (uint64_t(c[r].w) << 32);
+        uint64_t const k0 = w0 ^ sKey[st + 2 * j], k1 = w1 ^ sKey[st + 2 * j + 1];
+        a0 += w1 + uint64_t(uint32_t(k0)) * (k0 >> 32);
+        a1 += w0 + uint64_t(uint32_t(k1)) * (k1 >> 32);
+    }
+#pragma unroll
+    for (int m = 4; m < 32; m <<= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, m);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, m);
+    }
+    if (lane < 4) {
+        t.blockSums[8ull * br.tile + 2 * lane] = a0;
+        t.blockSums[8ull * br.tile + 2 * lane + 1] = a1;
+    }
 }
 
-// Phase 2: one warp per task.
+// Phase 2: one warp per task. Lanes 0..7 run the block chain for their
+// accumulator (loads four blocks ahead), then the trailing partial stripes
+// and the final stripe, and lane 0 merges.
 __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks, uint32_t* __restrict__ status)
 {
     uint32_t const ti = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -875,39 +1062,53 @@ __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks
         if (lane != 0) return;
         h = xxh3Short(t.data, t.len, al);
     } else {
-        uint64_t const init[8] = { XP32_3, XP64_1, XP64_2, XP64_3, XP64_4, XP32_2, XP64_5, XP32_1 };
         uint32_t const i = lane & 7;
-        uint64_t acc = init[i];
+        uint64_t const init = i == 0 ? XP32_3 : i == 1 ? XP64_1 : i == 2 ? XP64_2 : i == 3 ? XP64_3
+                            : i == 4 ? XP64_4 : i == 5 ? XP32_2 : i == 6 ? XP64_5 : XP32_1;
+        uint64_t acc = init;
         uint64_t const key = secret64(int(192 - 64 + 8 * i));
-        for (uint32_t b = 0; b < t.nbBlocks; b++) {
-            acc += t.blockSums[8ull * b + i];
+        const uint64_t* const bs = t.blockSums + i;
+        uint32_t const nb = t.nbBlocks;
+        uint32_t b = 0;
+        for (; b + 4 <= nb; b += 4) {
+            uint64_t const v0 = bs[8ull * b], v1 = bs[8ull * (b + 1)], v2 = bs[8ull * (b + 2)], v3 = bs[8ull * (b + 3)];
+            acc += v0; acc ^= acc >> 47; acc ^= key; acc *= XP32_1;
+            acc += v1; acc ^= acc >> 47; acc ^= key; acc *= XP32_1;
+            acc += v2; acc ^= acc >> 47; acc ^= key; acc *= XP32_1;
+            acc += v3; acc ^= acc >> 47; acc ^= key; acc *= XP32_1;
+        }
+        for (; b < nb; b++) {
+            acc += bs[8ull * b];
             acc ^= acc >> 47;
             acc ^= key;
             acc *= XP32_1;
         }
-        uint64_t a[8];
-        for (int k = 0; k < 8; k++) a[k] = __shfl_sync(0xffffffffu, acc, k);
-        if (lane != 0) return;
         uint64_t const len = t.len;
-        uint64_t const nbStripes = ((len - 1) - uint64_t(kHashBlock) * t.nbBlocks) / 64;
-        const uint8_t* const last = t.data + uint64_t(kHashBlock) * t.nbBlocks;
-        for (uint64_t st = 0; st < nbStripes; st++)
-            for (int k = 0; k < 8; k++) {
-                uint64_t const v = ldData(last + 64 * st + 8 * k, al);
-                uint64_t const x = v ^ secret64(int(8 * st + 8 * k));
-                a[k ^ 1] += v;
-                a[k] += uint64_t(uint32_t(x)) * (x >> 32);
-            }
-        for (int k = 0; k < 8; k++) {
-            uint64_t const v = ldData(t.data + len - 64 + 8 * k, al);
-            uint64_t const x = v ^ secret64(192 - 64 - 7 + 8 * k);
-            a[k ^ 1] += v;
-            a[k] += uint64_t(uint32_t(x)) * (x >> 32);
+        uint64_t const nbStripes = ((len - 1) - uint64_t(kHashBlock) * nb) / 64;
+        const uint8_t* const last = t.data + uint64_t(kHashBlock) * nb;
+        for (uint64_t st = 0; st < nbStripes; st++) {
+            uint64_t const v = ldData(last + 64 * st + 8 * i, al);
+            uint64_t const vx = __shfl_xor_sync(0xffffffffu, v, 1);
+            uint64_t const x = v ^ secret64(int(8 * st + 8 * i));
+            acc += vx + uint64_t(uint32_t(x)) * (x >> 32);
         }
-        uint64_t r = len * XP64_1;
-        for (int k = 0; k < 4; k++)
-            r += fold128(a[2 * k] ^ secret64(11 + 16 * k), a[2 * k + 1] ^ secret64(11 + 16 * k + 8));
-        h = xAvalanche(r);
+        {
+            uint64_t const v = ldData(t.data + len - 64 + 8 * i, al);
+            uint64_t const vx = __shfl_xor_sync(0xffffffffu, v, 1);
+            uint64_t const x = v ^ secret64(192 - 64 - 7 + 8 * int(i));
+            acc += vx + uint64_t(uint32_t(x)) * (x >> 32);
+        }
+        // merge: pairs (2k, 2k+1) folded with secret words at 11 + 16k
+        uint64_t const odd = __shfl_xor_sync(0xffffffffu, acc, 1);
+        uint64_t part = 0;
+        if (!(i & 1)) {
+            int const k = int(i >> 1);
+            part = fold128(acc ^ secret64(11 + 16 * k), odd ^ secret64(11 + 16 * k + 8));
+        }
+        part += __shfl_xor_sync(0xffffffffu, part, 2);
+        part += __shfl_xor_sync(0xffffffffu, part, 4);
+        if (lane != 0) return;
+        h = xAvalanche(len * XP64_1 + part);
     }
     if (t.hashOut) *t.hashOut = h;
     bool const ok = t.low8 ? ((h & 255) == t.expected) : (uint32_t(h) == t.expected);
@@ -921,21 +1122,20 @@ __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks
 namespace ozl {
 
 namespace {
-uint32_t fseLanesPerWarp(uint32_t tlMax)
+uint32_t fseLanes(uint32_t tlMax)
 {
-    uint32_t const per = (4u << tlMax) + 512u + 4u;
-    uint32_t lanes = kFseSmemMax / (kFseWarps * per);
+    uint32_t lanes = kFseCtaSmem / fseSlotBytes(tlMax);
     return lanes > 32 ? 32 : (lanes < 1 ? 1 : lanes);
 }
-uint32_t hufChunks(uint32_t tlMax) { return tlMax <= 11 ? 32u : 24u; }
-uint32_t hufSmem(uint32_t tlMax) { return hufChunks(tlMax) * ((2u << tlMax) + 512u + 4u); }
+constexpr uint32_t kHufSmem = kHufChunks * kHufSlotBytes + 512;
+static_assert(kHufChunks * kHufSlotBytes >= (2u << kHufTableLog), "a tableLog-12 table fits the slots");
 } // namespace
 
 cudaError_t prepareKernels()
 {
-    cudaError_t e = cudaFuncSetAttribute(kFse, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFseSmemMax));
+    cudaError_t e = cudaFuncSetAttribute(kFse, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFseCtaSmem));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(kHuf, cudaFuncAttributeMaxDynamicSharedMemorySize, int(hufSmem(kHufTableLog)));
+    return cudaFuncSetAttribute(kHuf, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kHufSmem));
 }
 
 long runLaunches(const DeviceLayout& L, uint8_t* dPool, uint8_t* dScratch, uint32_t* dStatus, cudaStream_t s)
@@ -965,20 +1165,15 @@ long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dSc
                 kConst<<<l.nbTiles, 256, 0, s>>>(static_cast<const ConstTask*>(tasks), tiles);
                 break;
             case KIND_FSE: {
-                uint32_t const lanes = fseLanesPerWarp(l.param0);
-                uint32_t const perCta = kFseWarps * lanes;
-                uint32_t const grid = (l.nbTasks + perCta - 1) / perCta;
-                uint32_t const smem = perCta * ((4u << l.param0) + 512u + 4u);
-                kFse<<<grid, 32 * kFseWarps, smem, s>>>(static_cast<const FseTask*>(tasks), l.nbTasks, lanes,
-                                                          l.param0, dStatus);
+                uint32_t const lanes = fseLanes(l.param0);
+                uint32_t const grid = (l.nbTasks + lanes - 1) / lanes;
+                kFse<<<grid, 32, lanes * fseSlotBytes(l.param0), s>>>(static_cast<const FseTask*>(tasks), l.nbTasks,
+                                                                     lanes, l.param0, dStatus);
                 break;
             }
             case KIND_HUF: {
-                uint32_t const tlMax = l.param0 ? l.param0 : kHufTableLog;
-                uint32_t const chunks = hufChunks(tlMax);
-                uint32_t const grid = (l.nbTasks + chunks - 1) / chunks;
-                kHuf<<<grid, 4 * chunks, hufSmem(tlMax), s>>>(static_cast<const HufTask*>(tasks), l.nbTasks, tlMax,
-                                                              dStatus);
+                uint32_t const grid = (l.nbTasks + kHufChunks - 1) / kHufChunks;
+                kHuf<<<grid, 32, kHufSmem, s>>>(static_cast<const HufTask*>(tasks), l.nbTasks, dStatus);
                 break;
             }
             case KIND_FLATPACK:
