@@ -127,38 +127,19 @@ __global__ void kConst(const ConstTask* __restrict__ tasks, const TileRef* __res
 }
 
 // ---------------------------------------------------------------------------
-// Fused numeric pipeline with decoupled look-back prefix sum.
+// Fused numeric pipeline: source (plain elements, byte planes or LSB-first
+// bit-packed fields) -> optional zigzag -> optional delta -> output elements.
 //
-// Tile = kTileElems output elements, 256 threads, 32 elements per thread.
-// y[0] = first value, y[i] = source[i-1] for delta tasks; out = inclusive
-// prefix sum of y modulo 2^(8w). Non-delta tasks write y directly.
-
+// Delta decoding is an exclusive prefix sum: out[i] = first + sum(src[0..i))
+// modulo 2^(8w), src holding n-1 elements (decode_delta_kernel.c:232). A tile
+// is 4096 output elements; thread t owns the 16 consecutive elements
+// 16t..16t+15 of its tile and loads exactly their sources (16-byte loads per
+// plane, 16w-byte loads for plain elements, aligned words for packed fields).
+// Tiles of a task are combined by a decoupled look-back done by one warp,
+// over up to 32 predecessors at a time; tiles are taken in launch order from
+// a counter, so a tile only waits on tiles that were taken before it.
 constexpr int kNPThreads = 256;
-constexpr int kNPPer = kTileElems / kNPThreads; // 32
-
-__device__ __forceinline__ uint64_t fetchSource(const NumPipeTask& t, uint64_t j)
-{
-    switch (t.srcMode) {
-        case SRC_PLAIN: return ldElem(t.src + j * t.w, t.w);
-        case SRC_PLANES: {
-            uint64_t v = 0;
-            for (uint32_t b = 0; b < t.w; b++) v |= uint64_t(t.planes[b][j]) << (8 * b);
-            return v;
-        }
-        default: {
-            uint64_t const bit = j * t.nbBits;
-            const uint8_t* p = t.src + (bit >> 3);
-            unsigned const sh = unsigned(bit & 7);
-            uintptr_t const a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(7);
-            unsigned const s = unsigned(reinterpret_cast<uintptr_t>(p) - a) * 8u + sh; // < 64
-            uint64_t const lo = *reinterpret_cast<const uint64_t*>(a);
-            uint64_t const hi = *reinterpret_cast<const uint64_t*>(a + 8);
-            uint64_t v = s ? ((lo >> s) | (hi << (64u - s))) : lo;
-            if (t.nbBits < 64) v &= (1ull << t.nbBits) - 1;
-            return v;
-        }
-    }
-}
+constexpr int kNPPer = kTileElems / kNPThreads; // 16
 
 // Look-back status per tile, 4 words: flag (0 none, 1 aggregate ready,
 // 2 inclusive prefix ready), aggregate, inclusive prefix, unused. The two
@@ -182,119 +163,263 @@ __device__ __forceinline__ void publishInclusive(unsigned long long* st, uint32_
     s[0] = 2;
 }
 
+// Exclusive prefix of tile g (index `tileInTask` within its task) from its
+// predecessors in the same task; called by all 32 lanes of one warp. Returns
+// false when a predecessor never published (bounded wait).
+__device__ __forceinline__ bool lookBack(unsigned long long* st, uint32_t g, uint32_t tileInTask, uint64_t& prefixOut)
+{
+    uint32_t const lane = threadIdx.x & 31;
+    uint64_t prefix = 0;
+    int64_t const lowest = int64_t(g) - int64_t(tileInTask); // the task's first tile
+    int64_t p = int64_t(g) - 1 - lane;
+    uint32_t spins = 0;
+    while (true) {
+        bool const valid = p >= lowest;
+        unsigned long long f = 0;
+        volatile unsigned long long* s = st + kScanWords * (valid ? p : 0);
+        while (true) {
+            f = valid ? s[0] : 2ull;
+            if (!__any_sync(0xffffffffu, f == 0)) break;
+            if (++spins > (1u << 24)) { prefixOut = prefix; return false; }
+        }
+        __threadfence();
+        uint64_t const v = valid ? (f == 2 ? s[2] : s[1]) : 0;
+        unsigned const incl = __ballot_sync(0xffffffffu, valid && f == 2);
+        // lanes up to (and including) the nearest inclusive predecessor count
+        unsigned const upto = incl ? (__ffs(incl) - 1) : 31;
+        uint64_t x = lane <= upto ? v : 0;
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1) x += __shfl_xor_sync(0xffffffffu, x, m);
+        prefix += x;
+        if (incl) break;
+        p -= 32;
+    }
+    prefixOut = prefix;
+    return true;
+}
+
+template <int W> struct NPVal { using T = uint32_t; };
+template <> struct NPVal<8> { using T = uint64_t; };
+
+template <int W>
+__device__ __forceinline__ typename NPVal<W>::T npMask(typename NPVal<W>::T v)
+{
+    if constexpr (W == 1) return v & 0xffu;
+    else if constexpr (W == 2) return v & 0xffffu;
+    else return v;
+}
+
+// Loads source elements j0..j0+15 (those below nSrc; the rest read as 0).
+template <int W, int MODE>
+__device__ __forceinline__ void npLoad(const NumPipeTask& t, uint64_t j0, uint64_t nSrc,
+                                       typename NPVal<W>::T (&v)[kNPPer])
+{
+    using T = typename NPVal<W>::T;
+    bool const full = j0 + kNPPer <= nSrc;
+    if constexpr (MODE == SRC_PLANES) {
+#pragma unroll
+        for (int k = 0; k < kNPPer; k++) v[k] = 0;
+#pragma unroll
+        for (int b = 0; b < W; b++) {
+            const uint8_t* const pl = t.planes[b] + j0;
+            if (full && !(reinterpret_cast<uintptr_t>(pl) & 15)) {
+                uint4 const q = __ldg(reinterpret_cast<const uint4*>(pl));
+                uint32_t const wd[4] = { q.x, q.y, q.z, q.w };
+#pragma unroll
+                for (int k = 0; k < kNPPer; k++) v[k] |= T((wd[k >> 2] >> (8 * (k & 3))) & 0xffu) << (8 * b);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kNPPer; k++)
+                    if (j0 + k < nSrc) v[k] |= T(pl[k]) << (8 * b);
+            }
+        }
+    } else if constexpr (MODE == SRC_PLAIN) {
+        const uint8_t* const p = t.src + j0 * W;
+        if (full && !(reinterpret_cast<uintptr_t>(p) & 15)) {
+#pragma unroll
+            for (int q = 0; q < W; q++) {
+                uint4 const x = __ldg(reinterpret_cast<const uint4*>(p) + q);
+                uint32_t const wd[4] = { x.x, x.y, x.z, x.w };
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    if constexpr (W == 8) {
+                        if (m & 1) v[q * 2 + (m >> 1)] |= uint64_t(wd[m]) << 32;
+                        else v[q * 2 + (m >> 1)] = wd[m];
+                    } else if constexpr (W == 4) {
+                        v[q * 4 + m] = wd[m];
+                    } else if constexpr (W == 2) {
+                        v[q * 8 + 2 * m] = wd[m] & 0xffffu;
+                        v[q * 8 + 2 * m + 1] = wd[m] >> 16;
+                    } else {
+#pragma unroll
+                        for (int y = 0; y < 4; y++) v[q * 16 + 4 * m + y] = (wd[m] >> (8 * y)) & 0xffu;
+                    }
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kNPPer; k++) {
+                T x = 0;
+                if (j0 + k < nSrc)
+                    for (int y = 0; y < W; y++) x |= T(p[k * W + y]) << (8 * y);
+                v[k] = x;
+            }
+        }
+    } else {
+        // LSB-first fields of nbBits (1..64) over aligned 32-bit words
+        uint32_t const nb = t.nbBits;
+        uintptr_t const a = reinterpret_cast<uintptr_t>(t.src) & ~uintptr_t(3);
+        const uint32_t* const wds = reinterpret_cast<const uint32_t*>(a);
+        uint64_t const bit0 = (reinterpret_cast<uintptr_t>(t.src) - a) * 8 + j0 * nb;
+#pragma unroll
+        for (int k = 0; k < kNPPer; k++) {
+            T x = 0;
+            if (j0 + k < nSrc) {
+                uint64_t const bit = bit0 + uint64_t(k) * nb;
+                uint64_t const q = bit >> 5;
+                uint32_t const r = uint32_t(bit & 31);
+                uint32_t const w0 = __ldg(wds + q);
+                uint32_t const w1 = (r + nb > 32) ? __ldg(wds + q + 1) : 0u;
+                uint64_t lo = __funnelshift_r(w0, w1, r);
+                if (r + nb > 64) {
+                    uint32_t const w2 = __ldg(wds + q + 2);
+                    lo |= uint64_t(__funnelshift_r(w1, w2, r)) << 32;
+                } else if (nb > 32) {
+                    lo |= uint64_t(w1 >> r) << 32;
+                }
+                if (nb < 64) lo &= (1ull << nb) - 1;
+                x = T(lo);
+            }
+            v[k] = x;
+        }
+    }
+}
+
+template <int W>
+__device__ __forceinline__ void npStore(uint8_t* out, uint32_t cnt, const typename NPVal<W>::T (&v)[kNPPer])
+{
+    if (cnt == kNPPer && !(reinterpret_cast<uintptr_t>(out) & 15)) {
+#pragma unroll
+        for (int q = 0; q < W; q++) {
+            uint32_t wd[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+                if constexpr (W == 8) {
+                    wd[m] = (m & 1) ? uint32_t(v[q * 2 + (m >> 1)] >> 32) : uint32_t(v[q * 2 + (m >> 1)]);
+                } else if constexpr (W == 4) {
+                    wd[m] = v[q * 4 + m];
+                } else if constexpr (W == 2) {
+                    wd[m] = (v[q * 8 + 2 * m] & 0xffffu) | (v[q * 8 + 2 * m + 1] << 16);
+                } else {
+                    wd[m] = (v[q * 16 + 4 * m] & 0xffu) | ((v[q * 16 + 4 * m + 1] & 0xffu) << 8)
+                            | ((v[q * 16 + 4 * m + 2] & 0xffu) << 16) | (v[q * 16 + 4 * m + 3] << 24);
+                }
+            }
+            reinterpret_cast<uint4*>(out)[q] = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kNPPer; k++)
+            if (uint32_t(k) < cnt)
+                for (int y = 0; y < W; y++) out[k * W + y] = uint8_t(uint64_t(v[k]) >> (8 * y));
+    }
+}
+
+template <int W, int MODE>
+__device__ __forceinline__ void npTile(const NumPipeTask& t, const TileRef& tr, uint32_t g, unsigned long long* scan,
+                                       uint32_t* status)
+{
+    using T = typename NPVal<W>::T;
+    __shared__ uint64_t warpTot[kNPThreads / 32];
+    __shared__ uint64_t sPrefix;
+    uint32_t const tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint64_t const e0 = uint64_t(tr.tile) * kTileElems + uint64_t(tid) * kNPPer;
+    uint32_t const cnt = e0 < t.n ? uint32_t(umin64(kNPPer, t.n - e0)) : 0;
+    uint64_t const nSrc = t.delta ? (t.n ? t.n - 1 : 0) : t.n;
+    T v[kNPPer];
+    npLoad<W, MODE>(t, e0, nSrc, v);
+    if (t.zigzag) {
+#pragma unroll
+        for (int k = 0; k < kNPPer; k++) v[k] = npMask<W>((v[k] >> 1) ^ (T(0) - (v[k] & 1)));
+    }
+    if (t.delta) {
+        // exclusive scan within the thread
+        T acc = 0;
+#pragma unroll
+        for (int k = 0; k < kNPPer; k++) {
+            T const x = v[k];
+            v[k] = acc;
+            acc += x;
+        }
+        // exclusive scan of thread totals within the warp
+        uint64_t incl = acc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t const y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= uint32_t(o)) incl += y;
+        }
+        if (lane == 31) warpTot[wid] = incl;
+        __syncthreads();
+        uint64_t warpPre = 0, tileAgg = 0;
+#pragma unroll
+        for (int w2 = 0; w2 < kNPThreads / 32; w2++) {
+            uint64_t const x = warpTot[w2];
+            warpPre += uint32_t(w2) < wid ? x : 0;
+            tileAgg += x;
+        }
+        if (wid == 0) {
+            unsigned long long* const st = scan + 8; // header: tile counter (+ padding)
+            uint64_t prefix = 0;
+            if (tr.tile == 0) {
+                if (lane == 0) publishInclusive(st, g, tileAgg);
+            } else {
+                if (lane == 0) publishAggregate(st, g, tileAgg);
+                if (!lookBack(st, g, tr.tile, prefix) && lane == 0) reportError(status, DERR_TIMEOUT);
+                if (lane == 0) publishInclusive(st, g, prefix + tileAgg);
+            }
+            if (lane == 0) sPrefix = prefix;
+        }
+        __syncthreads();
+        T const add = T(t.first + sPrefix + warpPre + (incl - acc));
+#pragma unroll
+        for (int k = 0; k < kNPPer; k++) v[k] = npMask<W>(T(v[k] + add));
+    }
+    if (cnt) npStore<W>(t.out + e0 * W, cnt, v);
+}
+
+template <int W>
+__device__ __forceinline__ void npTileW(const NumPipeTask& t, const TileRef& tr, uint32_t g, unsigned long long* scan,
+                                        uint32_t* status)
+{
+    switch (t.srcMode) {
+        case SRC_PLAIN: npTile<W, SRC_PLAIN>(t, tr, g, scan, status); break;
+        case SRC_PLANES: npTile<W, SRC_PLANES>(t, tr, g, scan, status); break;
+        default: npTile<W, SRC_BITPACK>(t, tr, g, scan, status); break;
+    }
+}
+
 __global__ void __launch_bounds__(kNPThreads) kNumPipe(const NumPipeTask* __restrict__ tasks,
                                                        const TileRef* __restrict__ tiles,
                                                        unsigned long long* __restrict__ scan,
                                                        uint32_t* __restrict__ status)
 {
-    __shared__ uint64_t sv[kTileElems + kTileElems / 32];
-    __shared__ uint64_t warpTot[kNPThreads / 32];
     __shared__ uint32_t sTile;
-    __shared__ uint64_t sPrefix;
-    uint32_t tileIdx;
+    uint32_t g;
     if (scan) {
         // dynamic tile order: a tile only waits on tiles acquired before it
         if (threadIdx.x == 0) sTile = atomicAdd(reinterpret_cast<unsigned int*>(scan), 1u);
         __syncthreads();
-        tileIdx = sTile;
+        g = sTile;
     } else {
-        tileIdx = blockIdx.x;
+        g = blockIdx.x;
     }
-    TileRef const tr = tiles[tileIdx];
+    TileRef const tr = tiles[g];
     NumPipeTask const t = tasks[tr.task];
-    uint64_t const e0 = uint64_t(tr.tile) * kTileElems;
-    uint32_t const cnt = uint32_t(umin64(kTileElems, t.n - e0));
-    uint64_t const mask = widthMask(t.w);
-    auto sidx = [](uint32_t i) { return i + (i >> 5); };
-
-    // 1. striped, coalesced source reads -> shared memory
-    for (uint32_t k = threadIdx.x; k < cnt; k += kNPThreads) {
-        uint64_t const i = e0 + k;
-        uint64_t y;
-        if (t.delta && i == 0) {
-            y = t.first;
-        } else {
-            uint64_t const j = t.delta ? i - 1 : i;
-            y = fetchSource(t, j);
-            if (t.zigzag) y = (y >> 1) ^ (0 - (y & 1));
-        }
-        sv[sidx(k)] = y & mask;
-    }
-    __syncthreads();
-
-    if (t.delta) {
-        // 2. per-thread serial scan over a blocked segment of 32 elements
-        uint32_t const b = threadIdx.x * kNPPer;
-        uint64_t acc = 0;
-        for (int q = 0; q < kNPPer; q++) {
-            uint32_t const k = b + q;
-            if (k < cnt) {
-                acc += sv[sidx(k)];
-                sv[sidx(k)] = acc;
-            }
-        }
-        // 3. block exclusive scan of thread totals
-        uint64_t incl = acc;
-        unsigned const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-        for (int o = 1; o < 32; o <<= 1) {
-            uint64_t const v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= unsigned(o)) incl += v;
-        }
-        if (lane == 31) warpTot[wid] = incl;
-        __syncthreads();
-        uint64_t warpPre = 0, tileAgg = 0;
-        for (unsigned w2 = 0; w2 < kNPThreads / 32; w2++) {
-            if (w2 < wid) warpPre += warpTot[w2];
-            tileAgg += warpTot[w2];
-        }
-        uint64_t const threadPre = warpPre + incl - acc;
-        // 4. decoupled look-back across the task's tiles
-        if (threadIdx.x == 0) {
-            unsigned long long* st = scan + 8; // header: counter (+ padding)
-            uint64_t prefix = 0;
-            uint32_t const g = tileIdx;
-            if (tr.tile == 0) {
-                publishInclusive(st, g, tileAgg);
-            } else {
-                publishAggregate(st, g, tileAgg);
-                int64_t p = int64_t(g) - 1;
-                uint32_t spins = 0;
-                bool ok = true;
-                while (true) {
-                    volatile unsigned long long* s = st + kScanWords * p;
-                    unsigned long long const f = s[0];
-                    if (f == 0) {
-                        if (++spins > (1u << 26)) { ok = false; break; }
-                        continue;
-                    }
-                    __threadfence();
-                    if (f == 2) {
-                        prefix += s[2];
-                        break;
-                    }
-                    prefix += s[1];
-                    p--;
-                }
-                if (!ok) reportError(status, DERR_TIMEOUT);
-                publishInclusive(st, g, prefix + tileAgg);
-            }
-            sPrefix = prefix;
-        }
-        __syncthreads();
-        uint64_t const add = sPrefix + threadPre;
-        for (int q = 0; q < kNPPer; q++) {
-            uint32_t const k = b + q;
-            if (k < cnt) sv[sidx(k)] += add;
-        }
-        __syncthreads();
-    }
-
-    // 5. striped stores
-    uint8_t* const out = t.out + e0 * t.w;
-    if (t.w == 1) {
-        for (uint32_t k = threadIdx.x; k < cnt; k += kNPThreads) out[k] = uint8_t(sv[sidx(k)]);
-    } else {
-        for (uint32_t k = threadIdx.x; k < cnt; k += kNPThreads) stElem(out + uint64_t(k) * t.w, sv[sidx(k)], t.w);
+    switch (t.w) {
+        case 1: npTileW<1>(t, tr, g, scan, status); break;
+        case 2: npTileW<2>(t, tr, g, scan, status); break;
+        case 4: npTileW<4>(t, tr, g, scan, status); break;
+        default: npTileW<8>(t, tr, g, scan, status); break;
     }
 }
 
