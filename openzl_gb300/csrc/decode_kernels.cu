@@ -135,68 +135,12 @@ __global__ void kConst(const ConstTask* __restrict__ tasks, const TileRef* __res
 // is 4096 output elements; thread t owns the 16 consecutive elements
 // 16t..16t+15 of its tile and loads exactly their sources (16-byte loads per
 // plane, 16w-byte loads for plain elements, aligned words for packed fields).
-// Tiles of a task are combined by a decoupled look-back done by one warp,
-// over up to 32 predecessors at a time; tiles are taken in launch order from
-// a counter, so a tile only waits on tiles that were taken before it.
+// Delta tasks take three launches, none of which waits on another CTA: the
+// sum of every tile's sources, an exclusive scan of those sums per task (one
+// warp per task), then the final pass that scans inside the tile and adds
+// the tile's prefix. The sources are read twice; nothing is latency-bound.
 constexpr int kNPThreads = 256;
 constexpr int kNPPer = kTileElems / kNPThreads; // 16
-
-// Look-back status per tile, 4 words: flag (0 none, 1 aggregate ready,
-// 2 inclusive prefix ready), aggregate, inclusive prefix, unused. The two
-// values live in separate words so that a reader who saw flag 1 never reads
-// a value overwritten by the later inclusive publication.
-constexpr int kScanWords = 4;
-
-__device__ __forceinline__ void publishAggregate(unsigned long long* st, uint32_t tile, uint64_t agg)
-{
-    volatile unsigned long long* s = st + kScanWords * tile;
-    s[1] = agg;
-    __threadfence();
-    s[0] = 1;
-}
-
-__device__ __forceinline__ void publishInclusive(unsigned long long* st, uint32_t tile, uint64_t incl)
-{
-    volatile unsigned long long* s = st + kScanWords * tile;
-    s[2] = incl;
-    __threadfence();
-    s[0] = 2;
-}
-
-// Exclusive prefix of tile g (index `tileInTask` within its task) from its
-// predecessors in the same task; called by all 32 lanes of one warp. Returns
-// false when a predecessor never published (bounded wait).
-__device__ __forceinline__ bool lookBack(unsigned long long* st, uint32_t g, uint32_t tileInTask, uint64_t& prefixOut)
-{
-    uint32_t const lane = threadIdx.x & 31;
-    uint64_t prefix = 0;
-    int64_t const lowest = int64_t(g) - int64_t(tileInTask); // the task's first tile
-    int64_t p = int64_t(g) - 1 - lane;
-    uint32_t spins = 0;
-    while (true) {
-        bool const valid = p >= lowest;
-        unsigned long long f = 0;
-        volatile unsigned long long* s = st + kScanWords * (valid ? p : 0);
-        while (true) {
-            f = valid ? s[0] : 2ull;
-            if (!__any_sync(0xffffffffu, f == 0)) break;
-            if (++spins > (1u << 24)) { prefixOut = prefix; return false; }
-        }
-        __threadfence();
-        uint64_t const v = valid ? (f == 2 ? s[2] : s[1]) : 0;
-        unsigned const incl = __ballot_sync(0xffffffffu, valid && f == 2);
-        // lanes up to (and including) the nearest inclusive predecessor count
-        unsigned const upto = incl ? (__ffs(incl) - 1) : 31;
-        uint64_t x = lane <= upto ? v : 0;
-#pragma unroll
-        for (int m = 16; m > 0; m >>= 1) x += __shfl_xor_sync(0xffffffffu, x, m);
-        prefix += x;
-        if (incl) break;
-        p -= 32;
-    }
-    prefixOut = prefix;
-    return true;
-}
 
 template <int W> struct NPVal { using T = uint32_t; };
 template <> struct NPVal<8> { using T = uint64_t; };
@@ -326,12 +270,39 @@ __device__ __forceinline__ void npStore(uint8_t* out, uint32_t cnt, const typena
 }
 
 template <int W, int MODE>
-__device__ __forceinline__ void npTile(const NumPipeTask& t, const TileRef& tr, uint32_t g, unsigned long long* scan,
-                                       uint32_t* status)
+__device__ __forceinline__ void npReduceTile(const NumPipeTask& t, const TileRef& tr, uint64_t* sums, uint32_t g)
+{
+    using T = typename NPVal<W>::T;
+    __shared__ uint64_t warpSum[kNPThreads / 32];
+    uint32_t const tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint64_t const e0 = uint64_t(tr.tile) * kTileElems + uint64_t(tid) * kNPPer;
+    uint64_t const nSrc = t.n ? t.n - 1 : 0;
+    T v[kNPPer];
+    npLoad<W, MODE>(t, e0, nSrc, v);
+    uint64_t acc = 0;
+#pragma unroll
+    for (int k = 0; k < kNPPer; k++) {
+        T x = v[k];
+        if (t.zigzag) x = npMask<W>((x >> 1) ^ (T(0) - (x & 1)));
+        acc += x;
+    }
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+    if (lane == 0) warpSum[wid] = acc;
+    __syncthreads();
+    if (tid == 0) {
+        uint64_t tot = 0;
+#pragma unroll
+        for (int w2 = 0; w2 < kNPThreads / 32; w2++) tot += warpSum[w2];
+        sums[g] = tot;
+    }
+}
+
+template <int W, int MODE>
+__device__ __forceinline__ void npTile(const NumPipeTask& t, const TileRef& tr, uint32_t g, const uint64_t* prefix)
 {
     using T = typename NPVal<W>::T;
     __shared__ uint64_t warpTot[kNPThreads / 32];
-    __shared__ uint64_t sPrefix;
     uint32_t const tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     uint64_t const e0 = uint64_t(tr.tile) * kTileElems + uint64_t(tid) * kNPPer;
     uint32_t const cnt = e0 < t.n ? uint32_t(umin64(kNPPer, t.n - e0)) : 0;
@@ -351,7 +322,7 @@ __device__ __forceinline__ void npTile(const NumPipeTask& t, const TileRef& tr, 
             v[k] = acc;
             acc += x;
         }
-        // exclusive scan of thread totals within the warp
+        // exclusive scan of thread totals within the warp, then across warps
         uint64_t incl = acc;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -360,27 +331,10 @@ __device__ __forceinline__ void npTile(const NumPipeTask& t, const TileRef& tr, 
         }
         if (lane == 31) warpTot[wid] = incl;
         __syncthreads();
-        uint64_t warpPre = 0, tileAgg = 0;
+        uint64_t warpPre = 0;
 #pragma unroll
-        for (int w2 = 0; w2 < kNPThreads / 32; w2++) {
-            uint64_t const x = warpTot[w2];
-            warpPre += uint32_t(w2) < wid ? x : 0;
-            tileAgg += x;
-        }
-        if (wid == 0) {
-            unsigned long long* const st = scan + 8; // header: tile counter (+ padding)
-            uint64_t prefix = 0;
-            if (tr.tile == 0) {
-                if (lane == 0) publishInclusive(st, g, tileAgg);
-            } else {
-                if (lane == 0) publishAggregate(st, g, tileAgg);
-                if (!lookBack(st, g, tr.tile, prefix) && lane == 0) reportError(status, DERR_TIMEOUT);
-                if (lane == 0) publishInclusive(st, g, prefix + tileAgg);
-            }
-            if (lane == 0) sPrefix = prefix;
-        }
-        __syncthreads();
-        T const add = T(t.first + sPrefix + warpPre + (incl - acc));
+        for (int w2 = 0; w2 < kNPThreads / 32; w2++) warpPre += uint32_t(w2) < wid ? warpTot[w2] : 0;
+        T const add = T(t.first + prefix[g] + warpPre + (incl - acc));
 #pragma unroll
         for (int k = 0; k < kNPPer; k++) v[k] = npMask<W>(T(v[k] + add));
     }
@@ -388,38 +342,80 @@ __device__ __forceinline__ void npTile(const NumPipeTask& t, const TileRef& tr, 
 }
 
 template <int W>
-__device__ __forceinline__ void npTileW(const NumPipeTask& t, const TileRef& tr, uint32_t g, unsigned long long* scan,
-                                        uint32_t* status)
+__device__ __forceinline__ void npTileW(const NumPipeTask& t, const TileRef& tr, uint32_t g, const uint64_t* prefix)
 {
     switch (t.srcMode) {
-        case SRC_PLAIN: npTile<W, SRC_PLAIN>(t, tr, g, scan, status); break;
-        case SRC_PLANES: npTile<W, SRC_PLANES>(t, tr, g, scan, status); break;
-        default: npTile<W, SRC_BITPACK>(t, tr, g, scan, status); break;
+        case SRC_PLAIN: npTile<W, SRC_PLAIN>(t, tr, g, prefix); break;
+        case SRC_PLANES: npTile<W, SRC_PLANES>(t, tr, g, prefix); break;
+        default: npTile<W, SRC_BITPACK>(t, tr, g, prefix); break;
     }
 }
 
+template <int W>
+__device__ __forceinline__ void npReduceW(const NumPipeTask& t, const TileRef& tr, uint64_t* sums, uint32_t g)
+{
+    switch (t.srcMode) {
+        case SRC_PLAIN: npReduceTile<W, SRC_PLAIN>(t, tr, sums, g); break;
+        case SRC_PLANES: npReduceTile<W, SRC_PLANES>(t, tr, sums, g); break;
+        default: npReduceTile<W, SRC_BITPACK>(t, tr, sums, g); break;
+    }
+}
+
+// pass 1 (delta tasks): sum of each tile's sources
+__global__ void __launch_bounds__(kNPThreads) kNumReduce(const NumPipeTask* __restrict__ tasks,
+                                                         const TileRef* __restrict__ tiles,
+                                                         uint64_t* __restrict__ sums)
+{
+    uint32_t const g = blockIdx.x;
+    TileRef const tr = tiles[g];
+    NumPipeTask const t = tasks[tr.task];
+    if (!t.delta) return;
+    switch (t.w) {
+        case 1: npReduceW<1>(t, tr, sums, g); break;
+        case 2: npReduceW<2>(t, tr, sums, g); break;
+        case 4: npReduceW<4>(t, tr, sums, g); break;
+        default: npReduceW<8>(t, tr, sums, g); break;
+    }
+}
+
+// pass 2: exclusive scan of tile sums per task, one warp per task
+__global__ void __launch_bounds__(256) kNumPrefix(const NumPipeTask* __restrict__ tasks, uint32_t nbTasks,
+                                                  const uint64_t* __restrict__ sums, uint64_t* __restrict__ prefix)
+{
+    uint32_t const ti = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t const lane = threadIdx.x & 31;
+    if (ti >= nbTasks) return;
+    NumPipeTask const t = tasks[ti];
+    if (!t.delta) return;
+    uint32_t const nT = uint32_t((t.n + kTileElems - 1) / kTileElems);
+    uint64_t running = 0;
+    for (uint32_t k0 = 0; k0 < nT; k0 += 32) {
+        uint32_t const k = k0 + lane;
+        uint64_t const x = k < nT ? sums[t.tileBase + k] : 0;
+        uint64_t incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t const y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= uint32_t(o)) incl += y;
+        }
+        if (k < nT) prefix[t.tileBase + k] = running + incl - x;
+        running += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
+// pass 3: the output
 __global__ void __launch_bounds__(kNPThreads) kNumPipe(const NumPipeTask* __restrict__ tasks,
                                                        const TileRef* __restrict__ tiles,
-                                                       unsigned long long* __restrict__ scan,
-                                                       uint32_t* __restrict__ status)
+                                                       const uint64_t* __restrict__ prefix)
 {
-    __shared__ uint32_t sTile;
-    uint32_t g;
-    if (scan) {
-        // dynamic tile order: a tile only waits on tiles acquired before it
-        if (threadIdx.x == 0) sTile = atomicAdd(reinterpret_cast<unsigned int*>(scan), 1u);
-        __syncthreads();
-        g = sTile;
-    } else {
-        g = blockIdx.x;
-    }
+    uint32_t const g = blockIdx.x;
     TileRef const tr = tiles[g];
     NumPipeTask const t = tasks[tr.task];
     switch (t.w) {
-        case 1: npTileW<1>(t, tr, g, scan, status); break;
-        case 2: npTileW<2>(t, tr, g, scan, status); break;
-        case 4: npTileW<4>(t, tr, g, scan, status); break;
-        default: npTileW<8>(t, tr, g, scan, status); break;
+        case 1: npTileW<1>(t, tr, g, prefix); break;
+        case 2: npTileW<2>(t, tr, g, prefix); break;
+        case 4: npTileW<4>(t, tr, g, prefix); break;
+        default: npTileW<8>(t, tr, g, prefix); break;
     }
 }
 
@@ -507,28 +503,58 @@ __global__ void kFlatpack(const FlatpackTask* __restrict__ tasks, const TileRef*
 // Backward bit readers (FSE / Huffman bitstreams): fields are read most
 // significant bit first from the end of the stream towards its start.
 //
-// Streams are read as aligned 32-bit words (a word holding at least one byte
-// of the stream never crosses a page), never above the word that holds the
-// stream's last byte and never below its first. Three words below the window
-// are held in registers (loaded three refills before use) and the stream is
-// prefetched into L2 512 bytes ahead. Positions are bit indices above bit 0 of
-// the aligned word that holds the stream's first byte.
-__device__ __forceinline__ uint32_t streamWord(const uint32_t* w, int32_t k) { return k >= 0 ? __ldg(w + k) : 0u; }
+// Each lane stages its stream through a small ring of 16-byte chunks in
+// shared memory, filled by asynchronous copies (cp.async) issued AHEAD chunks
+// before they are needed; the bit window in registers refills from the ring.
+// Chunks are the 16-byte-aligned blocks of global memory that hold at least
+// one byte of the stream (such a block never crosses a page), counted from
+// the block holding the stream's first byte. Positions are bit indices above
+// bit 0 of that block.
+template <int RING, int AHEAD>
+struct StreamRing {
+    static_assert((RING & (RING - 1)) == 0 && AHEAD + 1 <= RING, "ring shape");
+    const uint8_t* g16;  // 16-byte aligned block holding the stream's first byte
+    uint32_t* ring;      // RING * 4 words of shared memory, 16-byte aligned
+    int32_t low;         // lowest chunk whose words have been read
 
-__device__ __forceinline__ void prefetchAhead(const uint32_t* w, int32_t k)
-{
-    // k: index of the word just loaded; every 32 words, touch the line 128 words below
-    if ((k & 31) == 0 && k >= 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(w + k - 128));
-}
+    __device__ __forceinline__ void issue(int32_t m)
+    {
+        if (m >= 0) {
+            uint32_t const dst = uint32_t(__cvta_generic_to_shared(ring + 4 * (m & (RING - 1))));
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(g16 + 16 * size_t(m)) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    // Starts the ring for a stream whose top bit is at position pos (> 0).
+    __device__ __forceinline__ void start(int32_t pos)
+    {
+        int32_t const mt = (pos - 1) >> 7;
+        for (int32_t m = mt; m >= mt - AHEAD; m--) issue(m);
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        low = mt;
+    }
+    // Word k (descending order after start(); k may be negative: 0).
+    __device__ __forceinline__ uint32_t word(int32_t k)
+    {
+        if (k < 0) return 0u;
+        int32_t const m = k >> 2;
+        if (m < low) {
+            low = m;
+            issue(m - AHEAD);
+            asm volatile("cp.async.wait_group %0;" ::"n"(AHEAD) : "memory");
+        }
+        return ring[k & (4 * RING - 1)];
+    }
+};
 
-__device__ __forceinline__ bool streamStart(const uint8_t* p, uint32_t size, const uint32_t*& w, int32_t& pos,
+__device__ __forceinline__ bool streamStart(const uint8_t* p, uint32_t size, const uint8_t*& g16, int32_t& pos,
                                             int32_t& end)
 {
     if (size == 0) return false;
     uint8_t const last = p[size - 1];
     if (last == 0) return false;
-    uintptr_t const a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(3);
-    w = reinterpret_cast<const uint32_t*>(a);
+    uintptr_t const a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(15);
+    g16 = reinterpret_cast<const uint8_t*>(a);
     end = int32_t(reinterpret_cast<uintptr_t>(p) - a) * 8;
     pos = end + int32_t(size - 1) * 8 + (31 - __clz(uint32_t(last)));
     return true;
@@ -536,33 +562,28 @@ __device__ __forceinline__ bool streamStart(const uint8_t* p, uint32_t size, con
 
 // 64-bit window (Huffman: one field at a time, at most 12 bits).
 // Invariant between reads: cb + 32 < pos <= cb + 64.
+template <int RING, int AHEAD>
 struct BitIn {
-    const uint32_t* w;
+    StreamRing<RING, AHEAD> r;
     int32_t pos, end, cb;
     uint64_t c;
-    uint32_t a1, a2, a3; // the three words below the window
 
-    __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size)
+    __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size, uint32_t* ring)
     {
-        if (!streamStart(p, size, w, pos, end)) return false;
+        if (!streamStart(p, size, r.g16, pos, end)) return false;
+        r.ring = ring;
+        r.start(pos);
         int32_t const j = ((pos - 1) >> 5) - 1; // arithmetic shift: floor
         cb = j * 32;
-        c = (uint64_t(streamWord(w, j + 1)) << 32) | streamWord(w, j);
-        a1 = streamWord(w, j - 1);
-        a2 = streamWord(w, j - 2);
-        a3 = streamWord(w, j - 3);
+        uint32_t const top = r.word(j + 1);
+        c = (uint64_t(top) << 32) | r.word(j);
         return true;
     }
     __device__ __forceinline__ void renorm()
     {
         if (pos <= cb + 32) {
-            c = (c << 32) | a1;
-            a1 = a2;
-            a2 = a3;
             cb -= 32;
-            int32_t const k = (cb >> 5) - 3;
-            a3 = streamWord(w, k);
-            prefetchAhead(w, k);
+            c = (c << 32) | r.word(cb >> 5);
         }
     }
     __device__ __forceinline__ uint32_t peek(uint32_t nb) const
@@ -591,34 +612,29 @@ struct BitIn {
 // offsets known from the table entries before any of them is read).
 // Invariant between groups: cb + 64 <= pos <= cb + 96, so the 48 bits below
 // pos lie in the window at shift pos - 48 - cb, between 16 and 48.
+template <int RING, int AHEAD>
 struct BitWin {
-    const uint32_t* w;
+    StreamRing<RING, AHEAD> r;
     int32_t pos, end, cb;
     uint64_t lo, hi;
-    uint32_t a1, a2, a3;
 
-    __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size)
+    __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size, uint32_t* ring)
     {
-        if (!streamStart(p, size, w, pos, end)) return false;
+        if (!streamStart(p, size, r.g16, pos, end)) return false;
+        r.ring = ring;
+        r.start(pos);
         int32_t const jt = (pos - 1) >> 5; // word of the top unread bit
         cb = (jt - 2) * 32;
-        lo = uint64_t(streamWord(w, jt - 2)) | (uint64_t(streamWord(w, jt - 1)) << 32);
-        hi = streamWord(w, jt);
-        a1 = streamWord(w, jt - 3);
-        a2 = streamWord(w, jt - 4);
-        a3 = streamWord(w, jt - 5);
+        hi = r.word(jt);
+        uint32_t const mid = r.word(jt - 1);
+        lo = uint64_t(r.word(jt - 2)) | (uint64_t(mid) << 32);
         return true;
     }
     __device__ __forceinline__ void shift()
     {
         hi = (hi << 32) | (lo >> 32);
-        lo = (lo << 32) | a1;
-        a1 = a2;
-        a2 = a3;
         cb -= 32;
-        int32_t const k = (cb >> 5) - 3;
-        a3 = streamWord(w, k);
-        prefetchAhead(w, k);
+        lo = (lo << 32) | r.word(cb >> 5);
     }
     __device__ __forceinline__ void renorm()
     {
@@ -637,10 +653,10 @@ struct BitWin {
     __device__ __forceinline__ uint32_t read(uint32_t nb)
     {
         uint64_t const v = view();
-        uint32_t const r = uint32_t(v >> (48 - nb)) & ((1u << nb) - 1u);
+        uint32_t const x = uint32_t(v >> (48 - nb)) & ((1u << nb) - 1u);
         pos -= int32_t(nb);
         renorm();
-        return r;
+        return x;
     }
     __device__ __forceinline__ bool finished() const { return pos == end; }
 };
@@ -658,7 +674,17 @@ struct BitWin {
 // emits symbol i; the last symbol of each state has no transition).
 constexpr uint32_t kFseCtaSmem = 56 * 1024; // four CTAs per SM
 
+constexpr int kFseRing = 16, kFseAhead = 12; // stream ring: 256 bytes per lane, 192 bytes ahead
+
 __host__ __device__ __forceinline__ uint32_t fseSlotBytes(uint32_t tlMax) { return (3u << tlMax) + 512u + 4u; }
+__host__ __device__ __forceinline__ uint32_t fseRingOffset(uint32_t lanes, uint32_t tlMax)
+{
+    return (lanes * fseSlotBytes(tlMax) + 15u) & ~15u;
+}
+__host__ __device__ __forceinline__ uint32_t fseSmemBytes(uint32_t lanes, uint32_t tlMax)
+{
+    return fseRingOffset(lanes, tlMax) + lanes * 16u * kFseRing;
+}
 
 __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, uint32_t nbTasks, uint32_t lanes,
                                            uint32_t tableLogMax, uint32_t* __restrict__ status)
@@ -702,8 +728,9 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
         cell[u] = uint16_t(ns | (nb << 12));
     }
 
-    BitWin br;
-    if (!br.init(t.bits, t.bitsSize)) { reportError(status, DERR_CORRUPTION); return; }
+    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemFse + fseRingOffset(lanes, tableLogMax)) + lane * 4 * kFseRing;
+    BitWin<kFseRing, kFseAhead> br;
+    if (!br.init(t.bits, t.bitsSize, ring)) { reportError(status, DERR_CORRUPTION); return; }
     uint32_t const nst = t.nbStates;
     uint32_t st0 = br.read(tl), st1 = br.read(tl), st2 = 0, st3 = 0;
     if (nst == 4) { st2 = br.read(tl); st3 = br.read(tl); }
@@ -828,8 +855,11 @@ __device__ bool hufRank(const uint8_t* weights, uint32_t nbW, uint16_t* first, u
     return true;
 }
 
+constexpr int kHufRing = 8, kHufAhead = 6; // stream ring: 128 bytes per lane, 96 bytes ahead
+constexpr uint32_t kHufRingOff = kHufChunks * kHufSlotBytes + 512;     // after the slots and the spare ranks
+
 __device__ __forceinline__ void hufDecodeStream(const HufTask& t, const uint16_t* dt, uint32_t tl, uint32_t sIdx,
-                                                uint32_t* status)
+                                                uint32_t* ring, uint32_t* status)
 {
     const uint8_t* sp;
     uint32_t ssize, n, o0;
@@ -857,8 +887,8 @@ __device__ __forceinline__ void hufDecodeStream(const HufTask& t, const uint16_t
         o0 = 0;
         n = t.dstSize;
     }
-    BitIn br;
-    if (!br.init(sp, ssize)) { reportError(status, DERR_CORRUPTION); return; }
+    BitIn<kHufRing, kHufAhead> br;
+    if (!br.init(sp, ssize, ring)) { reportError(status, DERR_CORRUPTION); return; }
     uint8_t* const out = t.out + o0;
     uint32_t i = 0;
     // unaligned head, then four symbols per 32-bit store
@@ -924,7 +954,8 @@ __global__ void __launch_bounds__(32) kHuf(const HufTask* __restrict__ tasks, ui
         }
     }
     __syncwarp();
-    if (narrow) hufDecodeStream(t, dt, tl, sIdx, status);
+    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemHuf + kHufRingOff) + threadIdx.x * 4 * kHufRing;
+    if (narrow) hufDecodeStream(t, dt, tl, sIdx, ring, status);
     __syncwarp();
     // tableLog 12 (valid, but never emitted by the reference's encoder): one
     // chunk at a time, its table across the first slots, ranks recomputed
@@ -949,7 +980,7 @@ __global__ void __launch_bounds__(32) kHuf(const HufTask* __restrict__ tasks, ui
             for (uint32_t u = 0; u < len; u++) wide[f + u] = e;
         }
         __syncwarp();
-        if (threadIdx.x < 4) hufDecodeStream(tk, wide, tlk, threadIdx.x, status);
+        if (threadIdx.x < 4) hufDecodeStream(tk, wide, tlk, threadIdx.x, ring, status);
         __syncwarp();
     }
 }
@@ -1249,10 +1280,12 @@ namespace ozl {
 namespace {
 uint32_t fseLanes(uint32_t tlMax)
 {
-    uint32_t lanes = kFseCtaSmem / fseSlotBytes(tlMax);
-    return lanes > 32 ? 32 : (lanes < 1 ? 1 : lanes);
+    uint32_t lanes = 32;
+    while (lanes > 1 && fseSmemBytes(lanes, tlMax) > kFseCtaSmem) lanes--;
+    return lanes;
 }
-constexpr uint32_t kHufSmem = kHufChunks * kHufSlotBytes + 512;
+constexpr uint32_t kHufSmem = kHufRingOff + 32 * 16 * kHufRing;
+static_assert(kHufRingOff % 16 == 0, "ring alignment");
 static_assert(kHufChunks * kHufSlotBytes >= (2u << kHufTableLog), "a tableLog-12 table fits the slots");
 } // namespace
 
@@ -1292,7 +1325,7 @@ long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dSc
             case KIND_FSE: {
                 uint32_t const lanes = fseLanes(l.param0);
                 uint32_t const grid = (l.nbTasks + lanes - 1) / lanes;
-                kFse<<<grid, 32, lanes * fseSlotBytes(l.param0), s>>>(static_cast<const FseTask*>(tasks), l.nbTasks,
+                kFse<<<grid, 32, fseSmemBytes(lanes, l.param0), s>>>(static_cast<const FseTask*>(tasks), l.nbTasks,
                                                                      lanes, l.param0, dStatus);
                 break;
             }
@@ -1314,12 +1347,16 @@ long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dSc
                 kTranspose<<<l.nbTiles, 256, 0, s>>>(static_cast<const TransposeTask*>(tasks), tiles);
                 break;
             case KIND_NUMPIPE: {
-                unsigned long long* scan = nullptr;
+                const NumPipeTask* const np = static_cast<const NumPipeTask*>(tasks);
+                uint64_t* prefix = nullptr;
                 if (l.needsScan) {
-                    scan = reinterpret_cast<unsigned long long*>(dScratch + l.statusOff);
-                    if (cudaMemsetAsync(scan, 0, l.statusBytes, s) != cudaSuccess) return -1;
+                    uint64_t* const sums = reinterpret_cast<uint64_t*>(dScratch + l.statusOff);
+                    prefix = sums + l.nbTiles;
+                    kNumReduce<<<l.nbTiles, kNPThreads, 0, s>>>(np, tiles, sums);
+                    kNumPrefix<<<(l.nbTasks * 32 + 255) / 256, 256, 0, s>>>(np, l.nbTasks, sums, prefix);
+                    count += 2;
                 }
-                kNumPipe<<<l.nbTiles, kNPThreads, 0, s>>>(static_cast<const NumPipeTask*>(tasks), tiles, scan, dStatus);
+                kNumPipe<<<l.nbTiles, kNPThreads, 0, s>>>(np, tiles, prefix);
                 break;
             }
             case KIND_HASH: {
