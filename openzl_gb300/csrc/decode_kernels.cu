@@ -560,58 +560,10 @@ __device__ __forceinline__ bool streamStart(const uint8_t* p, uint32_t size, con
     return true;
 }
 
-// 64-bit window (Huffman: one field at a time, at most 12 bits).
-// Invariant between reads: cb + 32 < pos <= cb + 64.
-template <int RING, int AHEAD>
-struct BitIn {
-    StreamRing<RING, AHEAD> r;
-    int32_t pos, end, cb;
-    uint64_t c;
-
-    __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size, uint32_t* ring)
-    {
-        if (!streamStart(p, size, r.g16, pos, end)) return false;
-        r.ring = ring;
-        r.start(pos);
-        int32_t const j = ((pos - 1) >> 5) - 1; // arithmetic shift: floor
-        cb = j * 32;
-        uint32_t const top = r.word(j + 1);
-        c = (uint64_t(top) << 32) | r.word(j);
-        return true;
-    }
-    __device__ __forceinline__ void renorm()
-    {
-        if (pos <= cb + 32) {
-            cb -= 32;
-            c = (c << 32) | r.word(cb >> 5);
-        }
-    }
-    __device__ __forceinline__ uint32_t peek(uint32_t nb) const
-    {
-        int32_t sh = pos - int32_t(nb) - cb;
-        // below 0 only on corrupt streams (caught by the end check); 64 only
-        // when nb is 0, where the mask clears the result
-        sh = sh < 0 ? 0 : (sh > 63 ? 63 : sh);
-        return uint32_t(c >> sh) & ((1u << nb) - 1u);
-    }
-    __device__ __forceinline__ void skip(uint32_t nb)
-    {
-        pos -= int32_t(nb);
-        renorm();
-    }
-    __device__ __forceinline__ uint32_t read(uint32_t nb)
-    {
-        uint32_t const v = peek(nb);
-        skip(nb);
-        return v;
-    }
-    __device__ __forceinline__ bool finished() const { return pos == end; }
-};
-
-// 128-bit window (FSE: four fields of at most 12 bits per group, their
-// offsets known from the table entries before any of them is read).
-// Invariant between groups: cb + 64 <= pos <= cb + 96, so the 48 bits below
-// pos lie in the window at shift pos - 48 - cb, between 16 and 48.
+// 128-bit window over the stream, refilled 64 bits at a time from the ring.
+// Between steps cb + 64 <= pos <= cb + 128 (cb: bit index of lo's bit 0), so
+// up to 48 bits below pos can be read without refilling: four FSE fields of
+// at most 12 bits, or four Huffman peeks of at most 12 bits.
 template <int RING, int AHEAD>
 struct BitWin {
     StreamRing<RING, AHEAD> r;
@@ -624,7 +576,63 @@ struct BitWin {
         r.ring = ring;
         r.start(pos);
         int32_t const jt = (pos - 1) >> 5; // word of the top unread bit
-        cb = (jt - 2) * 32;
+        cb = (jt - 3) * 32;                // pos - cb in (96, 128]
+        uint32_t const w3 = r.word(jt), w2 = r.word(jt - 1), w1 = r.word(jt - 2), w0 = r.word(jt - 3);
+        hi = (uint64_t(w3) << 32) | w2;
+        lo = (uint64_t(w1) << 32) | w0;
+        return true;
+    }
+    __device__ __forceinline__ void renorm()
+    {
+        if (pos - cb < 64) {
+            cb -= 64;
+            hi = lo;
+            int32_t const k = cb >> 5;
+            uint32_t const w1 = r.word(k + 1), w0 = r.word(k);
+            lo = (uint64_t(w1) << 32) | w0;
+        }
+    }
+    // the 64 bits starting at bit b (b - cb between 0 and 127)
+    __device__ __forceinline__ uint64_t bitsAt(int32_t b) const
+    {
+        int32_t const s = b - cb;
+        if (s >= 64) return hi >> ((s - 64) & 63); // s = 128 only for an empty field (masked to 0)
+        if (s <= 0) return lo; // only on corrupt streams (caught by the end check)
+        return (lo >> s) | (hi << (64 - s));
+    }
+    // the 64 bits starting 48 bits below pos
+    __device__ __forceinline__ uint64_t view() const { return bitsAt(pos - 48); }
+    __device__ __forceinline__ uint32_t peek(uint32_t nb) const
+    {
+        return uint32_t(bitsAt(pos - int32_t(nb))) & ((1u << nb) - 1u);
+    }
+    // one field of nb bits (nb <= 12) just below pos
+    __device__ __forceinline__ uint32_t read(uint32_t nb)
+    {
+        uint32_t const x = peek(nb);
+        pos -= int32_t(nb);
+        renorm();
+        return x;
+    }
+    __device__ __forceinline__ bool finished() const { return pos == end; }
+};
+
+// 128-bit window refilled 32 bits at a time (FSE groups). Between groups
+// cb + 64 <= pos <= cb + 96, so the 48 bits below pos lie in the window at
+// shift pos - 48 - cb, between 16 and 48 (no boundary cases in the view).
+template <int RING, int AHEAD>
+struct BitWin32 {
+    StreamRing<RING, AHEAD> r;
+    int32_t pos, end, cb;
+    uint64_t lo, hi;
+
+    __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size, uint32_t* ring)
+    {
+        if (!streamStart(p, size, r.g16, pos, end)) return false;
+        r.ring = ring;
+        r.start(pos);
+        int32_t const jt = (pos - 1) >> 5; // word of the top unread bit
+        cb = (jt - 2) * 32;                // pos - cb in (64, 96]
         hi = r.word(jt);
         uint32_t const mid = r.word(jt - 1);
         lo = uint64_t(r.word(jt - 2)) | (uint64_t(mid) << 32);
@@ -729,7 +737,7 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
     }
 
     uint32_t* const ring = reinterpret_cast<uint32_t*>(smemFse + fseRingOffset(lanes, tableLogMax)) + lane * 4 * kFseRing;
-    BitWin<kFseRing, kFseAhead> br;
+    BitWin32<kFseRing, kFseAhead> br;
     if (!br.init(t.bits, t.bitsSize, ring)) { reportError(status, DERR_CORRUPTION); return; }
     uint32_t const nst = t.nbStates;
     uint32_t st0 = br.read(tl), st1 = br.read(tl), st2 = 0, st3 = 0;
@@ -855,7 +863,7 @@ __device__ bool hufRank(const uint8_t* weights, uint32_t nbW, uint16_t* first, u
     return true;
 }
 
-constexpr int kHufRing = 8, kHufAhead = 6; // stream ring: 128 bytes per lane, 96 bytes ahead
+constexpr int kHufRing = 8, kHufAhead = 5; // stream ring: 128 bytes per lane, 80 bytes ahead
 constexpr uint32_t kHufRingOff = kHufChunks * kHufSlotBytes + 512;     // after the slots and the spare ranks
 
 __device__ __forceinline__ void hufDecodeStream(const HufTask& t, const uint16_t* dt, uint32_t tl, uint32_t sIdx,
@@ -887,32 +895,36 @@ __device__ __forceinline__ void hufDecodeStream(const HufTask& t, const uint16_t
         o0 = 0;
         n = t.dstSize;
     }
-    BitIn<kHufRing, kHufAhead> br;
+    BitWin<kHufRing, kHufAhead> br;
     if (!br.init(sp, ssize, ring)) { reportError(status, DERR_CORRUPTION); return; }
     uint8_t* const out = t.out + o0;
     uint32_t i = 0;
-    // unaligned head, then four symbols per 32-bit store
+    // unaligned head, then four symbols (at most 48 bits) per refill check
+    // and per 32-bit store
     uint32_t const head = uint32_t((4 - (reinterpret_cast<uintptr_t>(out) & 3)) & 3);
     for (; i < head && i < n; i++) {
         uint32_t const e = dt[br.peek(tl)];
         out[i] = uint8_t(e);
-        br.skip(e >> 8);
+        br.pos -= int32_t(e >> 8);
+        br.renorm();
     }
     for (; i + 4 <= n; i += 4) {
         uint32_t const e0 = dt[br.peek(tl)];
-        br.skip(e0 >> 8);
+        br.pos -= int32_t(e0 >> 8);
         uint32_t const e1 = dt[br.peek(tl)];
-        br.skip(e1 >> 8);
+        br.pos -= int32_t(e1 >> 8);
         uint32_t const e2 = dt[br.peek(tl)];
-        br.skip(e2 >> 8);
+        br.pos -= int32_t(e2 >> 8);
         uint32_t const e3 = dt[br.peek(tl)];
-        br.skip(e3 >> 8);
+        br.pos -= int32_t(e3 >> 8);
+        br.renorm();
         *reinterpret_cast<uint32_t*>(out + i) = (e0 & 0xff) | ((e1 & 0xff) << 8) | ((e2 & 0xff) << 16) | ((e3 & 0xff) << 24);
     }
     for (; i < n; i++) {
         uint32_t const e = dt[br.peek(tl)];
         out[i] = uint8_t(e);
-        br.skip(e >> 8);
+        br.pos -= int32_t(e >> 8);
+        br.renorm();
     }
     if (!br.finished()) reportError(status, DERR_CORRUPTION);
 }
