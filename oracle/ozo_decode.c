@@ -3,6 +3,8 @@
  * compared against. Each function cites the reference code it restates. */
 #include <stdio.h>
 
+#include <string.h>
+
 #include "ozo_internal.h"
 
 typedef struct {
@@ -44,16 +46,33 @@ static void ost_ref(OStream* s, int type, size_t w, size_t n, const uint8_t* p)
  * common_bitpack_kernel.c). Element i occupies bits [i*nbBits, (i+1)*nbBits)
  * of the little-endian byte stream. Returns bytes consumed.
  * ------------------------------------------------------------------- */
+static uint64_t le64_at(const uint8_t* p)
+{
+    uint64_t v;
+    memcpy(&v, p, 8);
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_BIG_ENDIAN__
+    v = __builtin_bswap64(v);
+#endif
+    return v;
+}
+
 static size_t bitunpack(uint64_t* dst, size_t n, const uint8_t* src, size_t srcSize, int nbBits)
 {
     size_t const need = (n * (size_t)nbBits + 7) / 8;
     if (need > srcSize) return (size_t)-1;
+    uint64_t const mask = nbBits >= 64 ? ~0ull : ((1ull << nbBits) - 1);
     for (size_t i = 0; i < n; i++) {
-        size_t bit = i * (size_t)nbBits;
+        size_t const bit = i * (size_t)nbBits;
+        size_t const b = bit >> 3;
+        unsigned const sh = (unsigned)(bit & 7);
+        if (sh + (unsigned)nbBits <= 64 && b + 8 <= srcSize) {
+            dst[i] = (le64_at(src + b) >> sh) & mask;
+            continue;
+        }
         uint64_t v = 0;
-        for (int b = 0; b < nbBits; b++) {
-            size_t q = bit + (size_t)b;
-            v |= (uint64_t)((src[q >> 3] >> (q & 7)) & 1) << b;
+        for (int k = 0; k < nbBits; k++) {
+            size_t q = bit + (size_t)k;
+            v |= (uint64_t)((src[q >> 3] >> (q & 7)) & 1) << k;
         }
         dst[i] = v;
     }
@@ -68,6 +87,7 @@ static size_t bitunpack(uint64_t* dst, size_t n, const uint8_t* src, size_t srcS
  * ------------------------------------------------------------------- */
 typedef struct {
     const uint8_t* src;
+    size_t size;
     int64_t pos; /* number of unread bits */
 } BRd;
 
@@ -77,11 +97,18 @@ static int brd_init(BRd* r, const uint8_t* src, size_t size)
     uint8_t last = src[size - 1];
     if (last == 0) return -1;
     r->src = src;
+    r->size = size;
     r->pos = (int64_t)(size - 1) * 8 + ozo_highbit32(last);
     return 0;
 }
 static uint32_t brd_peek(const BRd* r, int nb)
 {
+    int64_t const start = r->pos - nb;
+    if (nb == 0) return 0;
+    if (start >= 0 && (size_t)(start >> 3) + 8 <= r->size) {
+        uint64_t const w = le64_at(r->src + (start >> 3));
+        return (uint32_t)((w >> (start & 7)) & ((1ull << nb) - 1));
+    }
     uint32_t v = 0;
     for (int i = 0; i < nb; i++) {
         int64_t q = r->pos - 1 - i;
@@ -95,6 +122,51 @@ static uint32_t brd_read(BRd* r, int nb)
     uint32_t v = brd_peek(r, nb);
     r->pos -= nb;
     return v;
+}
+
+/* Container form of the same reader for the entropy loops: 64 bits of the
+ * stream starting at bit index `base` are held in `cont`; fields below
+ * position 0 read as zero. */
+typedef struct {
+    const uint8_t* src;
+    size_t size;
+    int64_t pos;
+    int64_t base;
+    uint64_t cont;
+} BCont;
+
+static inline void bc_fill(BCont* r)
+{
+    int64_t b = ((r->pos + 7) >> 3) - 8;
+    if (b < 0) b = 0;
+    r->base = b * 8;
+    if ((size_t)b + 8 <= r->size) {
+        r->cont = le64_at(r->src + b);
+    } else {
+        uint64_t v = 0;
+        for (size_t k = 0; (size_t)b + k < r->size && k < 8; k++) v |= (uint64_t)r->src[b + k] << (8 * k);
+        r->cont = v;
+    }
+}
+static inline int bc_init(BCont* r, const uint8_t* src, size_t size)
+{
+    if (size == 0 || src[size - 1] == 0) return -1;
+    r->src = src;
+    r->size = size;
+    r->pos = (int64_t)(size - 1) * 8 + ozo_highbit32(src[size - 1]);
+    bc_fill(r);
+    return 0;
+}
+static inline uint32_t bc_peek(const BCont* r, int nb)
+{
+    int64_t const sh = r->pos - nb - r->base;
+    uint64_t const v = sh >= 0 ? (r->cont >> sh) : (r->cont << -sh);
+    return (uint32_t)(v & ((1ull << nb) - 1));
+}
+static inline void bc_skip(BCont* r, int nb)
+{
+    r->pos -= nb;
+    if (r->pos - r->base < 32 && r->base > 0) bc_fill(r);
 }
 
 /* ---------------------------------------------------------------------
@@ -205,17 +277,23 @@ static int fse_build_dtable(FseD* dt, const int16_t* norm, unsigned maxSV, unsig
 static int fse_decode(uint8_t* dst, size_t dstSize, const uint8_t* src, size_t srcSize,
                       const FseD* dt, unsigned tableLog, unsigned nbStates)
 {
-    BRd r;
-    if (brd_init(&r, src, srcSize)) return -OZO_ERR_CORRUPTION;
+    BCont r;
+    if (bc_init(&r, src, srcSize)) return -OZO_ERR_CORRUPTION;
     uint32_t st[4];
-    for (unsigned k = 0; k < nbStates; k++) st[k] = brd_read(&r, (int)tableLog);
+    for (unsigned k = 0; k < nbStates; k++) {
+        st[k] = bc_peek(&r, (int)tableLog);
+        bc_skip(&r, (int)tableLog);
+    }
     if (dstSize < nbStates) return -OZO_ERR_CORRUPTION;
     size_t const lastTransition = dstSize - nbStates;
     for (size_t i = 0; i < dstSize; i++) {
         unsigned const k = (unsigned)(i % nbStates);
         FseD const e = dt[st[k]];
         dst[i] = e.symbol;
-        if (i < lastTransition) st[k] = e.newState + brd_read(&r, e.nbBits);
+        if (i < lastTransition) {
+            st[k] = e.newState + bc_peek(&r, e.nbBits);
+            bc_skip(&r, e.nbBits);
+        }
     }
     if (r.pos != 0) return -OZO_ERR_CORRUPTION;
     return 0;
@@ -266,12 +344,12 @@ static int huf_build_dtable(HufD* dt, unsigned* tableLogOut, const uint8_t* weig
 static int huf_decode_stream(uint8_t* dst, size_t n, const uint8_t* src, size_t size,
                              const HufD* dt, unsigned tableLog)
 {
-    BRd r;
-    if (brd_init(&r, src, size)) return -OZO_ERR_CORRUPTION;
+    BCont r;
+    if (bc_init(&r, src, size)) return -OZO_ERR_CORRUPTION;
     for (size_t i = 0; i < n; i++) {
-        HufD const e = dt[brd_peek(&r, (int)tableLog)];
+        HufD const e = dt[bc_peek(&r, (int)tableLog)];
         dst[i] = e.symbol;
-        r.pos -= e.nbBits;
+        bc_skip(&r, e.nbBits);
     }
     if (r.pos != 0) return -OZO_ERR_CORRUPTION;
     return 0;
@@ -392,10 +470,30 @@ static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, s
             if (n) {
                 uint64_t const m = w == 8 ? ~0ull : ((1ull << (8 * w)) - 1);
                 uint64_t v = ozo_rdN(hdr, w);
-                for (size_t i = 0; i < n; i++) {
-                    if (i) v = (v + ozo_rdN(in[0]->p + (i - 1) * w, w)) & m;
-                    for (size_t b = 0; b < w; b++) o[i * w + b] = (uint8_t)(v >> (8 * b));
+                const uint8_t* const d = in[0]->p;
+#define OZO_DELTA_W(T)                                                            \
+    {                                                                             \
+        T acc = (T)v;                                                             \
+        memcpy(o, &acc, sizeof(T));                                               \
+        for (size_t i = 1; i < n; i++) {                                          \
+            T x;                                                                  \
+            memcpy(&x, d + (i - 1) * sizeof(T), sizeof(T));                       \
+            acc = (T)(acc + x);                                                   \
+            memcpy(o + i * sizeof(T), &acc, sizeof(T));                           \
+        }                                                                         \
+    }
+                switch (w) {
+                    case 1: OZO_DELTA_W(uint8_t) break;
+                    case 2: OZO_DELTA_W(uint16_t) break;
+                    case 4: OZO_DELTA_W(uint32_t) break;
+                    case 8: OZO_DELTA_W(uint64_t) break;
+                    default:
+                        for (size_t i = 0; i < n; i++) {
+                            if (i) v = (v + ozo_rdN(d + (i - 1) * w, w)) & m;
+                            for (size_t b = 0; b < w; b++) o[i * w + b] = (uint8_t)(v >> (8 * b));
+                        }
                 }
+#undef OZO_DELTA_W
             }
             return 0;
         }
@@ -416,8 +514,11 @@ static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, s
             for (size_t i = 0; i < nbIn; i++)
                 if (in[i]->type != OZO_TYPE_SERIAL || in[i]->n != n) return -OZO_ERR_CORRUPTION;
             uint8_t* o = ost_alloc(out, OZO_TYPE_STRUCT, W, n);
-            for (size_t e = 0; e < n; e++)
-                for (size_t b = 0; b < W; b++) o[e * W + b] = in[b]->p[e];
+            for (size_t b = 0; b < W; b++) {
+                const uint8_t* const pl = in[b]->p;
+                uint8_t* const ob = o + b;
+                for (size_t e = 0; e < n; e++) ob[e * W] = pl[e];
+            }
             return 0;
         }
         case TR_CONV_NUM_TO_STRUCT_LE: { /* decode_conversion_binding.c:190-225 */
@@ -472,8 +573,12 @@ static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, s
             uint8_t* o = ost_alloc(out, sg.outType, w, n);
             uint64_t* tmp = (uint64_t*)malloc((n + 1) * 8);
             bitunpack(tmp, n, in[0]->p, srcSize, nbBits);
-            for (size_t i = 0; i < n; i++)
-                for (size_t b = 0; b < w; b++) o[i * w + b] = (uint8_t)(tmp[i] >> (8 * b));
+            switch (w) {
+                case 1: for (size_t i = 0; i < n; i++) o[i] = (uint8_t)tmp[i]; break;
+                case 2: for (size_t i = 0; i < n; i++) { uint16_t x = (uint16_t)tmp[i]; ozo_wr16(o + 2 * i, x); } break;
+                case 4: for (size_t i = 0; i < n; i++) ozo_wr32(o + 4 * i, (uint32_t)tmp[i]); break;
+                default: for (size_t i = 0; i < n; i++) ozo_wr64(o + 8 * i, tmp[i]); break;
+            }
             free(tmp);
             return 0;
         }

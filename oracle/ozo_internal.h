@@ -43,26 +43,54 @@ enum {
 
 #define OZO_MAGIC_BASE 0xD7B1A5C0u
 
+/* Little-endian loads (the oracle runs on little-endian hosts; the
+ * byte-swap keeps it correct elsewhere). */
+static inline uint64_t ozo_le(uint64_t v, size_t n)
+{
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_BIG_ENDIAN__
+    v = __builtin_bswap64(v) >> (64 - 8 * n);
+#else
+    (void)n;
+#endif
+    return v;
+}
 static inline uint16_t ozo_rd16(const uint8_t* p) { return (uint16_t)(p[0] | (p[1] << 8)); }
 static inline uint32_t ozo_rd32(const uint8_t* p)
 {
-    return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+    uint32_t v;
+    memcpy(&v, p, 4);
+    return (uint32_t)ozo_le(v, 4);
 }
-static inline uint64_t ozo_rd64(const uint8_t* p) { return (uint64_t)ozo_rd32(p) | ((uint64_t)ozo_rd32(p + 4) << 32); }
+static inline uint64_t ozo_rd64(const uint8_t* p)
+{
+    uint64_t v;
+    memcpy(&v, p, 8);
+    return ozo_le(v, 8);
+}
 static inline uint64_t ozo_rdN(const uint8_t* p, size_t n)
 {
-    uint64_t v = 0;
-    for (size_t i = 0; i < n; i++) v |= (uint64_t)p[i] << (8 * i);
-    return v;
+    switch (n) {
+        case 1: return p[0];
+        case 2: return ozo_rd16(p);
+        case 4: return ozo_rd32(p);
+        case 8: return ozo_rd64(p);
+        default: {
+            uint64_t v = 0;
+            for (size_t i = 0; i < n; i++) v |= (uint64_t)p[i] << (8 * i);
+            return v;
+        }
+    }
 }
 static inline void ozo_wr16(uint8_t* p, uint16_t v) { p[0] = (uint8_t)v; p[1] = (uint8_t)(v >> 8); }
 static inline void ozo_wr32(uint8_t* p, uint32_t v)
 {
-    for (int i = 0; i < 4; i++) p[i] = (uint8_t)(v >> (8 * i));
+    v = (uint32_t)ozo_le(v, 4);
+    memcpy(p, &v, 4);
 }
 static inline void ozo_wr64(uint8_t* p, uint64_t v)
 {
-    for (int i = 0; i < 8; i++) p[i] = (uint8_t)(v >> (8 * i));
+    v = ozo_le(v, 8);
+    memcpy(p, &v, 8);
 }
 static inline int ozo_highbit32(uint32_t v) { return 31 - __builtin_clz(v); }
 static inline int ozo_highbit64(uint64_t v) { return 63 - __builtin_clzll(v); }
