@@ -15,6 +15,7 @@
 #ifndef OPENZL_GB300_H
 #define OPENZL_GB300_H
 
+#include <stdbool.h>
 #include <stddef.h>
 #include <stdint.h>
 
@@ -41,10 +42,13 @@ typedef enum {
     ZL_ErrorCode_corruption = 12,
     ZL_ErrorCode_compressedChecksumWrong = 13,
     ZL_ErrorCode_contentChecksumWrong = 14,
+    ZL_ErrorCode_compressionParameter_invalid = 20,
     ZL_ErrorCode_parameter_invalid = 21,
     ZL_ErrorCode_invalidRequest_singleOutputFrameOnly = 23,
     ZL_ErrorCode_graph_invalid = 30,
     ZL_ErrorCode_invalidTransform = 32,
+    ZL_ErrorCode_node_unexpected_input_type = 54,
+    ZL_ErrorCode_node_invalid = 56,
     ZL_ErrorCode_formatVersion_unsupported = 60,
     ZL_ErrorCode_formatVersion_notSet = 61,
     ZL_ErrorCode_allocation = 70,
@@ -106,6 +110,148 @@ ZL_Report ZL_DCtx_decompress(ZL_DCtx* dctx, void* dst, size_t dstCapacity,
                              const void* compressed, size_t cSize);
 /* zl_decompress.h:32: one-shot variant with an internal context. */
 ZL_Report ZL_decompress(void* dst, size_t dstCapacity, const void* compressed, size_t cSize);
+
+/* ------------------------------------------------------------------ */
+/* Typed decompression (include/openzl/zl_decompress.h:358-599). */
+typedef struct {
+    ZL_Type type;                  /* type of the output */
+    uint32_t fixedWidth;           /* element width in bytes */
+    uint64_t decompressedByteSize; /* decompressed size in bytes */
+    uint64_t numElts;              /* number of elements */
+} ZL_OutputInfo;
+
+/* zl_decompress.h:388: single typed output into a caller buffer. */
+ZL_Report ZL_DCtx_decompressTyped(ZL_DCtx* dctx, ZL_OutputInfo* outputInfo, void* dst, size_t dstByteCapacity,
+                                  const void* compressed, size_t cSize);
+
+typedef struct ZL_TypedBuffer_s ZL_TypedBuffer;
+/* zl_decompress.h:418-599 */
+ZL_TypedBuffer* ZL_TypedBuffer_create(void);
+void ZL_TypedBuffer_free(ZL_TypedBuffer* tbuffer);
+ZL_TypedBuffer* ZL_TypedBuffer_createWrapSerial(void* buffer, size_t bufferCapacity);
+ZL_TypedBuffer* ZL_TypedBuffer_createWrapStruct(void* structBuffer, size_t structWidth, size_t numStructs);
+ZL_TypedBuffer* ZL_TypedBuffer_createWrapNumeric(void* numArray, size_t numWidth, size_t numCapacity);
+ZL_Type ZL_TypedBuffer_type(const ZL_TypedBuffer* tbuffer);
+size_t ZL_TypedBuffer_byteSize(const ZL_TypedBuffer* tbuffer);
+const void* ZL_TypedBuffer_rPtr(const ZL_TypedBuffer* tbuffer);
+size_t ZL_TypedBuffer_numElts(const ZL_TypedBuffer* tbuffer);
+size_t ZL_TypedBuffer_eltWidth(const ZL_TypedBuffer* tbuffer);
+/* zl_decompress.h:505 */
+ZL_Report ZL_DCtx_decompressTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* output, const void* compressed, size_t cSize);
+/* zl_decompress.h:527: frames here have one output, so nbOutputs must be 1. */
+ZL_Report ZL_DCtx_decompressMultiTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* outputs[], size_t nbOutputs,
+                                         const void* compressed, size_t cSize);
+
+typedef struct ZL_FrameInfo_s ZL_FrameInfo;
+/* zl_decompress.h:290-342 */
+ZL_FrameInfo* ZL_FrameInfo_create(const void* compressed, size_t cSize);
+void ZL_FrameInfo_free(ZL_FrameInfo* fi);
+ZL_Report ZL_FrameInfo_getFormatVersion(const ZL_FrameInfo* fi);
+ZL_Report ZL_FrameInfo_getNumOutputs(const ZL_FrameInfo* fi);
+ZL_Report ZL_FrameInfo_getOutputType(const ZL_FrameInfo* fi, int outputID);
+ZL_Report ZL_FrameInfo_getDecompressedSize(const ZL_FrameInfo* fi, int outputID);
+ZL_Report ZL_FrameInfo_getNumElts(const ZL_FrameInfo* fi, int outputID);
+
+/* ------------------------------------------------------------------ */
+/* Graph building and compression (include/openzl/zl_compressor.h,
+ * zl_compress.h, zl_opaque_types.h, zl_nodes.h, zl_graphs.h). Node and
+ * graph identifiers keep the reference's numeric values, so code written
+ * against the reference's headers runs unchanged. Compression runs on the
+ * GPU; a graph the GPU encoder does not implement is rejected with
+ * ZL_ErrorCode_graph_invalid (there is no CPU path). Frames are format
+ * version 23. */
+typedef unsigned ZL_IDType;
+typedef struct { ZL_IDType nid; } ZL_NodeID;   /* zl_opaque_types.h:28-30 */
+typedef struct { ZL_IDType gid; } ZL_GraphID;  /* zl_opaque_types.h:32-34 */
+#if defined(__cplusplus)
+#define ZL_MAKE_NODE_ID(id) (ZL_NodeID{ (id) })
+#define ZL_MAKE_GRAPH_ID(id) (ZL_GraphID{ (id) })
+#else
+#define ZL_MAKE_NODE_ID(id) ((ZL_NodeID){ .nid = (id) })
+#define ZL_MAKE_GRAPH_ID(id) ((ZL_GraphID){ .gid = (id) })
+#endif
+/* standard nodes (zl_nodes.h, codecs/zl_*.h, compress/private_nodes.h) */
+#define ZL_NODE_DELTA_INT ZL_MAKE_NODE_ID(2)
+#define ZL_NODE_TRANSPOSE_SPLIT ZL_MAKE_NODE_ID(3)
+#define ZL_NODE_ZIGZAG ZL_MAKE_NODE_ID(4)
+#define ZL_NODE_BFLOAT16_DECONSTRUCT ZL_MAKE_NODE_ID(7)
+#define ZL_NODE_CONVERT_TOKEN_TO_SERIAL ZL_MAKE_NODE_ID(10)
+#define ZL_NODE_CONVERT_NUM_TO_TOKEN ZL_MAKE_NODE_ID(11)
+#define ZL_NODE_CONVERT_NUM_TO_SERIAL ZL_MAKE_NODE_ID(12)
+#define ZL_NODE_BITPACK_INT ZL_MAKE_NODE_ID(53)
+/* standard graphs (zl_graphs.h, codecs/zl_*.h) */
+#define ZL_GRAPH_ILLEGAL ZL_MAKE_GRAPH_ID(0)
+#define ZL_GRAPH_STORE ZL_MAKE_GRAPH_ID(2)
+#define ZL_GRAPH_FSE ZL_MAKE_GRAPH_ID(3)
+#define ZL_GRAPH_HUFFMAN ZL_MAKE_GRAPH_ID(4)
+#define ZL_GRAPH_ENTROPY ZL_MAKE_GRAPH_ID(5)
+#define ZL_GRAPH_CONSTANT ZL_MAKE_GRAPH_ID(6)
+#define ZL_GRAPH_BITPACK ZL_MAKE_GRAPH_ID(8)
+#define ZL_GRAPH_FLATPACK ZL_MAKE_GRAPH_ID(9)
+
+/* zl_compress.h:64-150 */
+typedef enum {
+    ZL_CParam_stickyParameters = 1,
+    ZL_CParam_compressionLevel = 2,
+    ZL_CParam_decompressionLevel = 3,
+    ZL_CParam_formatVersion = 4,
+    ZL_CParam_permissiveCompression = 5,
+    ZL_CParam_compressedChecksum = 6,
+    ZL_CParam_contentChecksum = 7,
+    ZL_CParam_minStreamSize = 11,
+} ZL_CParam;
+
+typedef struct ZL_Compressor_s ZL_Compressor;
+typedef struct ZL_CCtx_s ZL_CCtx;
+typedef struct ZL_TypedRef_s ZL_TypedRef;
+
+/* zl_compressor.h:69, :78 */
+ZL_Compressor* ZL_Compressor_create(void);
+void ZL_Compressor_free(ZL_Compressor* compressor);
+/* zl_compressor.h:151, :162 */
+ZL_Report ZL_Compressor_setParameter(ZL_Compressor* compressor, ZL_CParam gcparam, int value);
+int ZL_Compressor_getParameter(const ZL_Compressor* compressor, ZL_CParam gcparam);
+/* zl_compressor.h:232, :249, :281 */
+ZL_GraphID ZL_Compressor_registerStaticGraph_fromNode1o(ZL_Compressor* compressor, ZL_NodeID headNode,
+                                                        ZL_GraphID dstGraph);
+ZL_GraphID ZL_Compressor_registerStaticGraph_fromPipelineNodes1o(ZL_Compressor* compressor, const ZL_NodeID* nodes,
+                                                                 size_t nbNodes, ZL_GraphID dstGraph);
+ZL_GraphID ZL_Compressor_registerStaticGraph_fromNode(ZL_Compressor* compressor, ZL_NodeID headNode,
+                                                      const ZL_GraphID* dstGraphs, size_t nbDstGraphs);
+/* codecs/zl_transpose.h:43 */
+ZL_GraphID ZL_Compressor_registerTransposeSplitGraph(ZL_Compressor* cgraph, ZL_GraphID successor);
+/* codecs/zl_tokenize.h:67 */
+ZL_GraphID ZL_Compressor_registerTokenizeGraph(ZL_Compressor* compressor, ZL_Type inputType, bool sort,
+                                               ZL_GraphID alphabetGraph, ZL_GraphID indicesGraph);
+/* zl_compressor.h:555 */
+ZL_Report ZL_Compressor_selectStartingGraphID(ZL_Compressor* compressor, ZL_GraphID graph);
+
+/* zl_compress.h:39-53 */
+#define ZL_COMPRESSBOUND(s) (((s) * 2) + 512 + 8)
+size_t ZL_compressBound(size_t totalSrcSize);
+/* zl_compress.h:60-61 */
+ZL_CCtx* ZL_CCtx_create(void);
+void ZL_CCtx_free(ZL_CCtx* cctx);
+/* zl_compress.h:152, :161, :168 */
+ZL_Report ZL_CCtx_setParameter(ZL_CCtx* cctx, ZL_CParam gcparam, int value);
+int ZL_CCtx_getParameter(const ZL_CCtx* cctx, ZL_CParam gcparam);
+ZL_Report ZL_CCtx_resetParameters(ZL_CCtx* cctx);
+/* zl_compressor.h:597 */
+ZL_Report ZL_CCtx_refCompressor(ZL_CCtx* cctx, const ZL_Compressor* compressor);
+/* zl_compress.h:194: serial input */
+ZL_Report ZL_CCtx_compress(ZL_CCtx* cctx, void* dst, size_t dstCapacity, const void* src, size_t srcSize);
+/* zl_compress.h:213 */
+const char* ZL_CCtx_getErrorContextString(const ZL_CCtx* cctx, ZL_Report report);
+/* zl_compress.h:274 */
+ZL_Report ZL_CCtx_compressTypedRef(ZL_CCtx* cctx, void* dst, size_t dstCapacity, const ZL_TypedRef* input);
+/* zl_compress.h:295: one input per frame here (nbInputs must be 1) */
+ZL_Report ZL_CCtx_compressMultiTypedRef(ZL_CCtx* cctx, void* dst, size_t dstCapacity, const ZL_TypedRef* inputs[],
+                                        size_t nbInputs);
+/* zl_compress.h:313-394 */
+ZL_TypedRef* ZL_TypedRef_createSerial(const void* src, size_t srcSize);
+ZL_TypedRef* ZL_TypedRef_createStruct(const void* start, size_t structWidth, size_t structCount);
+ZL_TypedRef* ZL_TypedRef_createNumeric(const void* start, size_t numWidth, size_t numCount);
+void ZL_TypedRef_free(ZL_TypedRef* tref);
 
 /* ------------------------------------------------------------------ */
 /* GPU additions (no counterpart in the reference; the reference has no

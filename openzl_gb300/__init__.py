@@ -8,6 +8,9 @@ and raises if either is missing.
 from ._lib import (  # noqa: F401
     ZLError,
     DCtx,
+    CCtx,
+    Compressor,
+    FrameInfo,
     GpuBatch,
     GpuEncoder,
     decompress,
@@ -19,3 +22,4 @@ from ._lib import (  # noqa: F401
     library,
     library_path,
 )
+from . import _lib as api  # noqa: F401  (constants: NODE_*, GRAPH_*, CPARAM_*, TYPE_*)

@@ -13,6 +13,19 @@ class ZLReport(ctypes.Structure):
     _fields_ = [("code", ctypes.c_int), ("value", ctypes.c_size_t)]
 
 
+class NodeID(ctypes.Structure):
+    _fields_ = [("nid", ctypes.c_uint)]
+
+
+class GraphID(ctypes.Structure):
+    _fields_ = [("gid", ctypes.c_uint)]
+
+
+class OutputInfo(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int), ("fixedWidth", ctypes.c_uint32), ("decompressedByteSize", ctypes.c_uint64),
+                ("numElts", ctypes.c_uint64)]
+
+
 class ZLError(RuntimeError):
     def __init__(self, code, msg=""):
         super().__init__("openzl_gb300 error %d: %s" % (code, msg))
@@ -63,6 +76,51 @@ def library():
         "ozl_gpu_compress_bound": ([sz], sz),
         "ozl_gpu_compress_batch": ([vp, sz, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, vp], ZLReport),
         "ozl_gpu_encoder_error": ([vp], ctypes.c_char_p),
+        "ZL_DCtx_decompressTyped": ([vp, ctypes.POINTER(OutputInfo), vp, sz, vp, sz], ZLReport),
+        "ZL_TypedBuffer_create": ([], vp),
+        "ZL_TypedBuffer_free": ([vp], None),
+        "ZL_TypedBuffer_createWrapSerial": ([vp, sz], vp),
+        "ZL_TypedBuffer_createWrapStruct": ([vp, sz, sz], vp),
+        "ZL_TypedBuffer_createWrapNumeric": ([vp, sz, sz], vp),
+        "ZL_TypedBuffer_type": ([vp], ctypes.c_int),
+        "ZL_TypedBuffer_byteSize": ([vp], sz),
+        "ZL_TypedBuffer_rPtr": ([vp], vp),
+        "ZL_TypedBuffer_numElts": ([vp], sz),
+        "ZL_TypedBuffer_eltWidth": ([vp], sz),
+        "ZL_DCtx_decompressTBuffer": ([vp, vp, vp, sz], ZLReport),
+        "ZL_DCtx_decompressMultiTBuffer": ([vp, vp, sz, vp, sz], ZLReport),
+        "ZL_FrameInfo_create": ([vp, sz], vp),
+        "ZL_FrameInfo_free": ([vp], None),
+        "ZL_FrameInfo_getFormatVersion": ([vp], ZLReport),
+        "ZL_FrameInfo_getNumOutputs": ([vp], ZLReport),
+        "ZL_FrameInfo_getOutputType": ([vp, ctypes.c_int], ZLReport),
+        "ZL_FrameInfo_getDecompressedSize": ([vp, ctypes.c_int], ZLReport),
+        "ZL_FrameInfo_getNumElts": ([vp, ctypes.c_int], ZLReport),
+        "ZL_Compressor_create": ([], vp),
+        "ZL_Compressor_free": ([vp], None),
+        "ZL_Compressor_setParameter": ([vp, ctypes.c_int, ctypes.c_int], ZLReport),
+        "ZL_Compressor_getParameter": ([vp, ctypes.c_int], ctypes.c_int),
+        "ZL_Compressor_registerStaticGraph_fromNode1o": ([vp, NodeID, GraphID], GraphID),
+        "ZL_Compressor_registerStaticGraph_fromPipelineNodes1o": ([vp, ctypes.POINTER(NodeID), sz, GraphID], GraphID),
+        "ZL_Compressor_registerStaticGraph_fromNode": ([vp, NodeID, ctypes.POINTER(GraphID), sz], GraphID),
+        "ZL_Compressor_registerTransposeSplitGraph": ([vp, GraphID], GraphID),
+        "ZL_Compressor_registerTokenizeGraph": ([vp, ctypes.c_int, ctypes.c_bool, GraphID, GraphID], GraphID),
+        "ZL_Compressor_selectStartingGraphID": ([vp, GraphID], ZLReport),
+        "ZL_compressBound": ([sz], sz),
+        "ZL_CCtx_create": ([], vp),
+        "ZL_CCtx_free": ([vp], None),
+        "ZL_CCtx_setParameter": ([vp, ctypes.c_int, ctypes.c_int], ZLReport),
+        "ZL_CCtx_getParameter": ([vp, ctypes.c_int], ctypes.c_int),
+        "ZL_CCtx_resetParameters": ([vp], ZLReport),
+        "ZL_CCtx_refCompressor": ([vp, vp], ZLReport),
+        "ZL_CCtx_compress": ([vp, vp, sz, vp, sz], ZLReport),
+        "ZL_CCtx_getErrorContextString": ([vp, ZLReport], ctypes.c_char_p),
+        "ZL_CCtx_compressTypedRef": ([vp, vp, sz, vp], ZLReport),
+        "ZL_CCtx_compressMultiTypedRef": ([vp, vp, sz, vp, sz], ZLReport),
+        "ZL_TypedRef_createSerial": ([vp, sz], vp),
+        "ZL_TypedRef_createStruct": ([vp, sz, sz], vp),
+        "ZL_TypedRef_createNumeric": ([vp, sz, sz], vp),
+        "ZL_TypedRef_free": ([vp], None),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -123,12 +181,28 @@ class DCtx:
         return self._lib.ZL_DCtx_getErrorContextString(self._h, rep).decode()
 
     def decompress(self, frame, out=None):
-        """Host frame in, host bytes out (numpy uint8)."""
+        """ZL_DCtx_decompressTyped: host frame in, host bytes out (numpy uint8)."""
+        data, _, _ = self.decompress_typed(frame, out)
+        return data
+
+    def decompress_typed(self, frame, out=None):
+        """Returns (bytes as numpy uint8, ZL_Type value, element width)."""
         f = _as_u8(frame)
         n = get_decompressed_size(f)
         if out is None:
             out = np.empty(max(n, 1), np.uint8)
-        rep = self._lib.ZL_DCtx_decompress(self._h, out.ctypes.data, out.nbytes, f.ctypes.data, f.size)
+        info = OutputInfo()
+        rep = self._lib.ZL_DCtx_decompressTyped(self._h, ctypes.byref(info), out.ctypes.data, out.nbytes,
+                                                f.ctypes.data, f.size)
+        if rep.code:
+            raise ZLError(rep.code, self._err(rep))
+        return out[: rep.value], info.type, info.fixedWidth
+
+    def decompress_serial(self, frame, capacity):
+        """ZL_DCtx_decompress (serial outputs only, as in the reference)."""
+        f = _as_u8(frame)
+        out = np.empty(max(capacity, 1), np.uint8)
+        rep = self._lib.ZL_DCtx_decompress(self._h, out.ctypes.data, capacity, f.ctypes.data, f.size)
         if rep.code:
             raise ZLError(rep.code, self._err(rep))
         return out[: rep.value]
@@ -266,3 +340,148 @@ class GpuEncoder:
         if rep.code:
             raise ZLError(rep.code, self._lib.ozl_gpu_encoder_error(self._h).decode())
         return [fs[i] for i in range(n)]
+
+
+# ---------------------------------------------------------------------------
+# Compression (ZL_Compressor / ZL_CCtx), mirroring the reference's C API.
+
+NODE_DELTA_INT = 2
+NODE_TRANSPOSE_SPLIT = 3
+NODE_ZIGZAG = 4
+NODE_BFLOAT16_DECONSTRUCT = 7
+NODE_CONVERT_NUM_TO_TOKEN = 11
+NODE_BITPACK_INT = 53
+GRAPH_ILLEGAL = 0
+GRAPH_STORE = 2
+GRAPH_FSE = 3
+GRAPH_HUFFMAN = 4
+GRAPH_CONSTANT = 6
+GRAPH_BITPACK = 8
+GRAPH_FLATPACK = 9
+CPARAM_STICKY = 1
+CPARAM_FORMAT_VERSION = 4
+CPARAM_COMPRESSED_CHECKSUM = 6
+CPARAM_CONTENT_CHECKSUM = 7
+TYPE_SERIAL, TYPE_STRUCT, TYPE_NUMERIC = 1, 2, 4
+
+
+class Compressor:
+    """ZL_Compressor: a graph registry (ids are plain ints here)."""
+
+    def __init__(self):
+        self._lib = library()
+        self._h = self._lib.ZL_Compressor_create()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.ZL_Compressor_free(h)
+            self._h = None
+
+    def set_parameter(self, p, v):
+        _check(self._lib.ZL_Compressor_setParameter(self._h, p, v))
+
+    def pipeline(self, nodes, dst):
+        arr = (NodeID * len(nodes))(*[NodeID(n) for n in nodes])
+        return self._lib.ZL_Compressor_registerStaticGraph_fromPipelineNodes1o(self._h, arr, len(nodes),
+                                                                               GraphID(dst)).gid
+
+    def node(self, node, dst):
+        return self._lib.ZL_Compressor_registerStaticGraph_fromNode1o(self._h, NodeID(node), GraphID(dst)).gid
+
+    def node_multi(self, node, dsts):
+        arr = (GraphID * len(dsts))(*[GraphID(g) for g in dsts])
+        return self._lib.ZL_Compressor_registerStaticGraph_fromNode(self._h, NodeID(node), arr, len(dsts)).gid
+
+    def transpose_split(self, succ):
+        return self._lib.ZL_Compressor_registerTransposeSplitGraph(self._h, GraphID(succ)).gid
+
+    def tokenize(self, typ, sort, alphabet, indices):
+        return self._lib.ZL_Compressor_registerTokenizeGraph(self._h, typ, sort, GraphID(alphabet),
+                                                             GraphID(indices)).gid
+
+    def select(self, gid):
+        _check(self._lib.ZL_Compressor_selectStartingGraphID(self._h, GraphID(gid)))
+
+
+class CCtx:
+    """ZL_CCtx: compression context; compresses on the GPU."""
+
+    def __init__(self):
+        self._lib = library()
+        self._h = self._lib.ZL_CCtx_create()
+        self._comp = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.ZL_CCtx_free(h)
+            self._h = None
+
+    def set_parameter(self, p, v):
+        _check(self._lib.ZL_CCtx_setParameter(self._h, p, v))
+
+    def ref_compressor(self, comp):
+        self._comp = comp
+        _check(self._lib.ZL_CCtx_refCompressor(self._h, comp._h))
+
+    def _raise(self, rep):
+        raise ZLError(rep.code, self._lib.ZL_CCtx_getErrorContextString(self._h, rep).decode())
+
+    def compress(self, data, capacity=None):
+        """ZL_CCtx_compress: serial input."""
+        b = _as_u8(data)
+        cap = capacity if capacity is not None else self._lib.ZL_compressBound(b.size)
+        out = np.empty(max(cap, 1), np.uint8)
+        rep = self._lib.ZL_CCtx_compress(self._h, out.ctypes.data, cap, b.ctypes.data if b.size else None, b.size)
+        if rep.code:
+            self._raise(rep)
+        return out[: rep.value].copy()
+
+    def compress_numeric(self, arr, capacity=None):
+        """ZL_CCtx_compressTypedRef with a numeric ZL_TypedRef."""
+        a = np.ascontiguousarray(arr)
+        ref = self._lib.ZL_TypedRef_createNumeric(a.ctypes.data if a.size else None, a.itemsize, a.size)
+        if not ref:
+            raise ZLError(21, "ZL_TypedRef_createNumeric failed")
+        cap = capacity if capacity is not None else self._lib.ZL_compressBound(a.nbytes)
+        out = np.empty(max(cap, 1), np.uint8)
+        try:
+            rep = self._lib.ZL_CCtx_compressTypedRef(self._h, out.ctypes.data, cap, ref)
+        finally:
+            self._lib.ZL_TypedRef_free(ref)
+        if rep.code:
+            self._raise(rep)
+        return out[: rep.value].copy()
+
+
+class FrameInfo:
+    """ZL_FrameInfo over a host frame (header only)."""
+
+    def __init__(self, frame):
+        self._lib = library()
+        self._f = _as_u8(frame)
+        self._h = self._lib.ZL_FrameInfo_create(self._f.ctypes.data, self._f.size)
+        if not self._h:
+            raise ZLError(12, "ZL_FrameInfo_create failed")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.ZL_FrameInfo_free(h)
+            self._h = None
+
+    def format_version(self):
+        return _check(self._lib.ZL_FrameInfo_getFormatVersion(self._h))
+
+    def num_outputs(self):
+        return _check(self._lib.ZL_FrameInfo_getNumOutputs(self._h))
+
+    def output_type(self, i=0):
+        return _check(self._lib.ZL_FrameInfo_getOutputType(self._h, i))
+
+    def decompressed_size(self, i=0):
+        return _check(self._lib.ZL_FrameInfo_getDecompressedSize(self._h, i))
+
+    def num_elts(self, i=0):
+        return _check(self._lib.ZL_FrameInfo_getNumElts(self._h, i))

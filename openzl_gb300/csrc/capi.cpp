@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -225,6 +226,11 @@ const char* ZL_ErrorCode_toString(ZL_ErrorCode code)
         case ZL_ErrorCode_compressedChecksumWrong: return "Compressed checksum mismatch";
         case ZL_ErrorCode_contentChecksumWrong: return "Content checksum mismatch";
         case ZL_ErrorCode_parameter_invalid: return "Invalid parameter";
+        case ZL_ErrorCode_compressionParameter_invalid: return "Invalid compression parameter";
+        case ZL_ErrorCode_graph_invalid: return "Graph invalid";
+        case ZL_ErrorCode_node_unexpected_input_type: return "Unexpected input type for node";
+        case ZL_ErrorCode_node_invalid: return "Node invalid";
+        case ZL_ErrorCode_invalidRequest_singleOutputFrameOnly: return "Only single-output frames are supported";
         case ZL_ErrorCode_invalidTransform: return "Codec not on the GPU path";
         case ZL_ErrorCode_formatVersion_unsupported: return "Format version unsupported";
         case ZL_ErrorCode_formatVersion_notSet: return "Format version not set";
@@ -356,13 +362,16 @@ ZL_Report ozl_gpu_decompress(ZL_DCtx* dctx, void* d_dst, size_t dstCap, const vo
     return r;
 }
 
-ZL_Report ZL_DCtx_decompress(ZL_DCtx* dctx, void* dst, size_t dstCap, const void* src, size_t cSize)
+// Host buffers in and out: one frame decoded on the DCtx's stream. Fills the
+// output's type and element width. Does not reset parameters.
+static ZL_Report decodeToHost(ZL_DCtx* dctx, void* dst, size_t dstCap, const void* src, size_t cSize, int* type,
+                              uint32_t* width)
 {
-    if (!dctx || !src) return fail(ZL_ErrorCode_parameter_invalid);
+    if (!dctx || !src || (dstCap && !dst)) return fail(ZL_ErrorCode_parameter_invalid);
     ZL_Report ds = ZL_getDecompressedSize(src, cSize);
-    if (ZL_isError(ds)) { resetParams(dctx); return ds; }
+    if (ZL_isError(ds)) return ds;
     size_t const outSize = ZL_validResult(ds);
-    if (outSize > dstCap) { resetParams(dctx); return fail(ZL_ErrorCode_dstCapacity_tooSmall); }
+    if (outSize > dstCap) return fail(ZL_ErrorCode_dstCapacity_tooSmall);
     if (!dctx->stream && cudaStreamCreateWithFlags(&dctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
         dctx->err = "no CUDA device";
         return fail(ZL_ErrorCode_GENERIC);
@@ -384,9 +393,42 @@ ZL_Report ZL_DCtx_decompress(ZL_DCtx* dctx, void* dst, size_t dstCap, const void
         && cudaMemcpyAsync(dst, dctx->out.data(), outSize, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         r = fail(ZL_ErrorCode_GENERIC);
     if (!ZL_isError(r)) r = dctx->batch.check(s);
-    if (ZL_isError(r)) dctx->err = dctx->batch.err;
-    resetParams(dctx);
-    return ZL_isError(r) ? r : ok(outSize);
+    if (ZL_isError(r)) {
+        dctx->err = dctx->batch.err;
+        return r;
+    }
+    if (type) *type = dctx->batch.plan.frames[0].outType;
+    if (width) *width = dctx->batch.plan.frames[0].outWidth;
+    return ok(outSize);
+}
+
+ZL_Report ZL_DCtx_decompress(ZL_DCtx* dctx, void* dst, size_t dstCap, const void* src, size_t cSize)
+{
+    int type = 0;
+    ZL_Report r = decodeToHost(dctx, dst, dstCap, src, cSize, &type, nullptr);
+    if (!ZL_isError(r) && type != ZL_Type_serial) {
+        // decompress2.c:1850-1856: typed outputs go through ZL_DCtx_decompressTyped
+        dctx->err = "ZL_DCtx_decompress is only compatible with serialized output";
+        r = fail(ZL_ErrorCode_GENERIC);
+    }
+    if (dctx) resetParams(dctx);
+    return r;
+}
+
+ZL_Report ZL_DCtx_decompressTyped(ZL_DCtx* dctx, ZL_OutputInfo* info, void* dst, size_t dstCap, const void* src,
+                                  size_t cSize)
+{
+    int type = 0;
+    uint32_t width = 1;
+    ZL_Report r = decodeToHost(dctx, dst, dstCap, src, cSize, &type, &width);
+    if (!ZL_isError(r) && info) {
+        info->type = ZL_Type(type);
+        info->fixedWidth = type == ZL_Type_serial ? 1 : width;
+        info->decompressedByteSize = ZL_validResult(r);
+        info->numElts = ZL_validResult(r) / (info->fixedWidth ? info->fixedWidth : 1);
+    }
+    if (dctx) resetParams(dctx);
+    return r;
 }
 
 ZL_Report ZL_decompress(void* dst, size_t dstCap, const void* src, size_t cSize)
@@ -515,5 +557,148 @@ ZL_Report ozl_gpu_xxh3_64(const void* d_data, size_t len, void* stream)
 }
 
 const char* ozl_gpu_batch_error(const OZL_GpuBatch* b) { return b ? b->err.c_str() : ""; }
+
+
+// ---------------------------------------------------------------------------
+// Typed buffers (zl_decompress.h:418-599): either wrapping caller memory of a
+// stated type and capacity, or filled by the DCtx (host allocation).
+struct ZL_TypedBuffer_s {
+    bool wrap = false;
+    ZL_Type type = ZL_Type_serial;
+    size_t width = 1;       // element width (wrap: declared; else from the frame)
+    size_t capacity = 0;    // wrap: bytes available
+    void* wrapped = nullptr;
+    std::vector<uint8_t> own;
+    size_t bytes = 0;
+};
+
+ZL_TypedBuffer* ZL_TypedBuffer_create(void) { return new (std::nothrow) ZL_TypedBuffer_s(); }
+void ZL_TypedBuffer_free(ZL_TypedBuffer* t) { delete t; }
+
+static ZL_TypedBuffer* wrapBuffer(ZL_Type type, void* p, size_t width, size_t bytes)
+{
+    ZL_TypedBuffer_s* t = new (std::nothrow) ZL_TypedBuffer_s();
+    if (!t) return nullptr;
+    t->wrap = true;
+    t->type = type;
+    t->width = width;
+    t->capacity = bytes;
+    t->wrapped = p;
+    return t;
+}
+ZL_TypedBuffer* ZL_TypedBuffer_createWrapSerial(void* buffer, size_t cap)
+{
+    return wrapBuffer(ZL_Type_serial, buffer, 1, cap);
+}
+ZL_TypedBuffer* ZL_TypedBuffer_createWrapStruct(void* buffer, size_t width, size_t n)
+{
+    return width ? wrapBuffer(ZL_Type_struct, buffer, width, width * n) : nullptr;
+}
+ZL_TypedBuffer* ZL_TypedBuffer_createWrapNumeric(void* buffer, size_t width, size_t n)
+{
+    if (!(width == 1 || width == 2 || width == 4 || width == 8)) return nullptr;
+    return wrapBuffer(ZL_Type_numeric, buffer, width, width * n);
+}
+ZL_Type ZL_TypedBuffer_type(const ZL_TypedBuffer* t) { return t ? t->type : ZL_Type_serial; }
+size_t ZL_TypedBuffer_byteSize(const ZL_TypedBuffer* t) { return t ? t->bytes : 0; }
+const void* ZL_TypedBuffer_rPtr(const ZL_TypedBuffer* t)
+{
+    if (!t) return nullptr;
+    return t->wrap ? t->wrapped : static_cast<const void*>(t->own.data());
+}
+size_t ZL_TypedBuffer_numElts(const ZL_TypedBuffer* t) { return t && t->width ? t->bytes / t->width : 0; }
+size_t ZL_TypedBuffer_eltWidth(const ZL_TypedBuffer* t) { return t ? t->width : 0; }
+
+ZL_Report ZL_DCtx_decompressTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* out, const void* src, size_t cSize)
+{
+    if (!dctx || !out || !src) return fail(ZL_ErrorCode_parameter_invalid);
+    ZL_Report ds = ZL_getDecompressedSize(src, cSize);
+    if (ZL_isError(ds)) { resetParams(dctx); return ds; }
+    size_t const outSize = ZL_validResult(ds);
+    void* dst;
+    size_t cap;
+    if (out->wrap) {
+        dst = out->wrapped;
+        cap = out->capacity;
+    } else {
+        try {
+            out->own.resize(outSize + 1);
+        } catch (...) {
+            resetParams(dctx);
+            return fail(ZL_ErrorCode_allocation);
+        }
+        dst = out->own.data();
+        cap = outSize;
+    }
+    int type = 0;
+    uint32_t width = 1;
+    ZL_Report r = decodeToHost(dctx, dst, cap, src, cSize, &type, &width);
+    if (!ZL_isError(r)) {
+        size_t const w = type == ZL_Type_serial ? 1 : width;
+        if (out->wrap && (ZL_Type(type) != out->type || (type != ZL_Type_serial && w != out->width))) {
+            dctx->err = "the wrapped buffer's type or width differs from the frame's output";
+            r = fail(ZL_ErrorCode_GENERIC);
+        } else {
+            out->type = ZL_Type(type);
+            out->width = w;
+            out->bytes = ZL_validResult(r);
+        }
+    }
+    resetParams(dctx);
+    return r;
+}
+
+ZL_Report ZL_DCtx_decompressMultiTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* outputs[], size_t nbOutputs,
+                                         const void* src, size_t cSize)
+{
+    if (!dctx || !outputs || nbOutputs != 1) return fail(ZL_ErrorCode_invalidRequest_singleOutputFrameOnly);
+    return ZL_DCtx_decompressTBuffer(dctx, outputs[0], src, cSize);
+}
+
+// ---------------------------------------------------------------------------
+// Frame information from the frame header (decode_frameheader.c:290-470).
+struct ZL_FrameInfo_s {
+    unsigned version;
+    ZL_Type type;
+    uint64_t size;
+};
+
+ZL_FrameInfo* ZL_FrameInfo_create(const void* src, size_t cSize)
+{
+    ZL_Report ds = ZL_getDecompressedSize(src, cSize);
+    if (ZL_isError(ds)) return nullptr;
+    const uint8_t* p = static_cast<const uint8_t*>(src);
+    static const ZL_Type map[4] = { ZL_Type_serial, ZL_Type_struct, ZL_Type_numeric, ZL_Type_string };
+    ZL_FrameInfo_s* fi = new (std::nothrow) ZL_FrameInfo_s();
+    if (!fi) return nullptr;
+    uint32_t const magic = uint32_t(p[0]) | (uint32_t(p[1]) << 8) | (uint32_t(p[2]) << 16) | (uint32_t(p[3]) << 24);
+    fi->version = magic - 0xD7B1A5C0u;
+    fi->type = map[(p[5] >> 4) & 3];
+    fi->size = ZL_validResult(ds);
+    return fi;
+}
+void ZL_FrameInfo_free(ZL_FrameInfo* fi) { delete fi; }
+ZL_Report ZL_FrameInfo_getFormatVersion(const ZL_FrameInfo* fi)
+{
+    return fi ? ok(fi->version) : fail(ZL_ErrorCode_parameter_invalid);
+}
+ZL_Report ZL_FrameInfo_getNumOutputs(const ZL_FrameInfo* fi) { return fi ? ok(1) : fail(ZL_ErrorCode_parameter_invalid); }
+ZL_Report ZL_FrameInfo_getOutputType(const ZL_FrameInfo* fi, int id)
+{
+    if (!fi || id != 0) return fail(ZL_ErrorCode_parameter_invalid);
+    return ok(size_t(fi->type));
+}
+ZL_Report ZL_FrameInfo_getDecompressedSize(const ZL_FrameInfo* fi, int id)
+{
+    if (!fi || id != 0) return fail(ZL_ErrorCode_parameter_invalid);
+    return ok(size_t(fi->size));
+}
+ZL_Report ZL_FrameInfo_getNumElts(const ZL_FrameInfo* fi, int id)
+{
+    if (!fi || id != 0) return fail(ZL_ErrorCode_parameter_invalid);
+    // decode_frameheader.c:455-467: counts known for serial outputs only
+    if (fi->type == ZL_Type_struct || fi->type == ZL_Type_numeric) return fail(ZL_ErrorCode_temporaryLibraryLimitation);
+    return ok(size_t(fi->size));
+}
 
 } // extern "C"

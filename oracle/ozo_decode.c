@@ -91,16 +91,6 @@ typedef struct {
     int64_t pos; /* number of unread bits */
 } BRd;
 
-static int brd_init(BRd* r, const uint8_t* src, size_t size)
-{
-    if (size == 0) return -1;
-    uint8_t last = src[size - 1];
-    if (last == 0) return -1;
-    r->src = src;
-    r->size = size;
-    r->pos = (int64_t)(size - 1) * 8 + ozo_highbit32(last);
-    return 0;
-}
 static uint32_t brd_peek(const BRd* r, int nb)
 {
     int64_t const start = r->pos - nb;
@@ -115,12 +105,6 @@ static uint32_t brd_peek(const BRd* r, int nb)
         uint32_t bit = q >= 0 ? ((r->src[q >> 3] >> (q & 7)) & 1) : 0;
         v = (v << 1) | bit;
     }
-    return v;
-}
-static uint32_t brd_read(BRd* r, int nb)
-{
-    uint32_t v = brd_peek(r, nb);
-    r->pos -= nb;
     return v;
 }
 

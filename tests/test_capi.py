@@ -69,3 +69,67 @@ def test_inspection_errors_without_gpu(lib):
     trunc = read_frame("walk_u32_1mib_dz_tsplit_fse")[:100]
     with pytest.raises(oz.ZLError):
         oz.get_compressed_size(trunc)
+
+
+def test_frame_info_on_golden_frames(lib, manifest):
+    """ZL_FrameInfo (header only, no GPU): version, outputs, type, size."""
+    import openzl_gb300 as oz
+
+    types = {"serial": 1, "struct": 2, "numeric": 4}
+    for m in manifest:
+        fi = oz.FrameInfo(read_frame(m["case"]))
+        assert fi.format_version() == 23
+        assert fi.num_outputs() == 1
+        width = m["elt_width"] or 1
+        assert fi.decompressed_size() == m["n"] * width, m["case"]
+        t = fi.output_type()
+        assert t in types.values()
+        if t == 1:
+            assert fi.num_elts() == m["n"] * width
+        else:
+            # decode_frameheader.c:455-467: not known for struct/numeric outputs
+            with pytest.raises(oz.ZLError) as e:
+                fi.num_elts()
+            assert e.value.code == 81
+
+
+def test_compress_api_errors_before_any_device_work(lib):
+    """Parameter and graph errors of ZL_CCtx are reported before any device
+    work, with the reference's error codes."""
+    import numpy as np
+    import openzl_gb300 as oz
+    from openzl_gb300 import api
+
+    data = np.arange(1000, dtype=np.uint32)
+    comp = oz.Compressor()
+    g = comp.node(api.NODE_DELTA_INT, api.GRAPH_STORE)
+    comp.select(g)
+    cctx = oz.CCtx()
+    cctx.ref_compressor(comp)
+    with pytest.raises(oz.ZLError) as e:  # formatVersion not set
+        cctx.compress_numeric(data)
+    assert e.value.code == 61
+    cctx.set_parameter(api.CPARAM_FORMAT_VERSION, 22)
+    with pytest.raises(oz.ZLError) as e:  # the GPU encoder writes version 23
+        cctx.compress_numeric(data)
+    assert e.value.code == 60
+    cctx.set_parameter(api.CPARAM_FORMAT_VERSION, 23)
+    with pytest.raises(oz.ZLError) as e:  # delta takes numeric input
+        cctx.compress(data.tobytes())
+    assert e.value.code == 54
+    # a graph shape the GPU encoder does not implement
+    comp2 = oz.Compressor()
+    comp2.select(comp2.node(api.NODE_ZIGZAG, api.GRAPH_FSE))
+    cctx2 = oz.CCtx()
+    cctx2.ref_compressor(comp2)
+    cctx2.set_parameter(api.CPARAM_FORMAT_VERSION, 23)
+    with pytest.raises(oz.ZLError) as e:
+        cctx2.compress_numeric(data)
+    assert e.value.code == 30
+    # parameters are not sticky by default: formatVersion is gone again
+    with pytest.raises(oz.ZLError) as e:
+        cctx2.compress_numeric(data)
+    assert e.value.code == 61
+    # unknown successor graphs are rejected at registration
+    assert comp.node(api.NODE_DELTA_INT, 12345) == api.GRAPH_ILLEGAL
+    assert lib.ZL_compressBound(1000) == 2 * 1000 + 520
