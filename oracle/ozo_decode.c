@@ -85,32 +85,8 @@ static size_t bitunpack(uint64_t* dst, size_t n, const uint8_t* src, size_t srcS
  * bit of the last byte is an end marker; fields are read most significant
  * bit first. Bits below position 0 read as zero.
  * ------------------------------------------------------------------- */
-typedef struct {
-    const uint8_t* src;
-    size_t size;
-    int64_t pos; /* number of unread bits */
-} BRd;
-
-static uint32_t brd_peek(const BRd* r, int nb)
-{
-    int64_t const start = r->pos - nb;
-    if (nb == 0) return 0;
-    if (start >= 0 && (size_t)(start >> 3) + 8 <= r->size) {
-        uint64_t const w = le64_at(r->src + (start >> 3));
-        return (uint32_t)((w >> (start & 7)) & ((1ull << nb) - 1));
-    }
-    uint32_t v = 0;
-    for (int i = 0; i < nb; i++) {
-        int64_t q = r->pos - 1 - i;
-        uint32_t bit = q >= 0 ? ((r->src[q >> 3] >> (q & 7)) & 1) : 0;
-        v = (v << 1) | bit;
-    }
-    return v;
-}
-
-/* Container form of the same reader for the entropy loops: 64 bits of the
- * stream starting at bit index `base` are held in `cont`; fields below
- * position 0 read as zero. */
+/* The reader keeps 64 bits of the stream starting at bit index `base` in
+ * `cont`; fields below position 0 read as zero. */
 typedef struct {
     const uint8_t* src;
     size_t size;
