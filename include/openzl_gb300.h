@@ -363,6 +363,33 @@ ZL_Report ozl_gpu_xxh3_64(const void* d_data, size_t len, void* stream);
 #define OZL_XXH3_STATIC_SCRATCH ((size_t)256 + ((size_t)32 << 10) * 72)
 ZL_Report ozl_gpu_xxh3_64_static(const void* d_data, size_t len, void* stream);
 
+/* Serving loop (no counterpart in the reference): continuous batching of
+ * decompress and compress requests with host buffers on the current device.
+ * `hbmBudget` bytes of device memory are split into one resident arena per
+ * worker; each worker (its own CUDA stream) takes the oldest queued requests
+ * of one kind that fit its arena together and runs them as one batch, so
+ * batches of different workers overlap on the GPU. `checksums` selects
+ * whether frames carry (compress) and have verified (decompress) both
+ * checksums. Host buffers must stay valid until the request completes; a
+ * request larger than one arena completes with ZL_ErrorCode_srcSize_tooLarge. */
+typedef struct OZL_Server_s OZL_Server;
+OZL_Server* ozl_server_create(size_t hbmBudget, int nbWorkers, int checksums);
+/* Drains the queue, then stops the workers. */
+void ozl_server_free(OZL_Server* server);
+/* Returns the request id (> 0), or 0 when the arguments are invalid. */
+uint64_t ozl_server_submit_decompress(OZL_Server* server, const void* frame, size_t frameSize, void* dst,
+                                      size_t dstCapacity);
+/* eltWidth 0 = serial bytes; recipe: OZL_GRAPH_* */
+uint64_t ozl_server_submit_compress(OZL_Server* server, const void* src, size_t nbElts, int eltWidth, int recipe,
+                                    void* dst, size_t dstCapacity);
+/* Completed requests, oldest first: up to `max` ids, results (decoded or
+ * frame size, or an error) and latencies from submission in microseconds.
+ * Waits up to waitMs for a first completion. Returns the count. */
+size_t ozl_server_poll(OZL_Server* server, uint64_t* ids, ZL_Report* results, double* latencyUs, size_t max,
+                       int waitMs);
+/* Requests submitted and not yet returned by ozl_server_poll. */
+size_t ozl_server_in_flight(OZL_Server* server);
+
 /* Library build identification (for load checks). */
 const char* ozl_gpu_version(void);
 

@@ -13,6 +13,7 @@ from ._lib import (  # noqa: F401
     FrameInfo,
     GpuBatch,
     GpuEncoder,
+    Server,
     decompress,
     xxh3_64_device,
     xxh3_64_device_static,

@@ -485,3 +485,74 @@ class FrameInfo:
 
     def num_elts(self, i=0):
         return _check(self._lib.ZL_FrameInfo_getNumElts(self._h, i))
+
+
+class Server:
+    """Serving loop (ozl_server_*): continuous batching of decompress and
+    compress requests with host buffers. Buffers are kept alive until their
+    request has been polled."""
+
+    def __init__(self, hbm_budget, workers=4, checksums=True):
+        self._lib = library()
+        L = self._lib
+        if not getattr(L, "_server_sigs", False):
+            vp, sz = ctypes.c_void_p, ctypes.c_size_t
+            for name, args, res in [
+                ("ozl_server_create", [sz, ctypes.c_int, ctypes.c_int], vp),
+                ("ozl_server_free", [vp], None),
+                ("ozl_server_submit_decompress", [vp, vp, sz, vp, sz], ctypes.c_uint64),
+                ("ozl_server_submit_compress", [vp, vp, sz, ctypes.c_int, ctypes.c_int, vp, sz], ctypes.c_uint64),
+                ("ozl_server_poll", [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ZLReport),
+                                     ctypes.POINTER(ctypes.c_double), sz, ctypes.c_int], sz),
+                ("ozl_server_in_flight", [vp], sz),
+            ]:
+                f = getattr(L, name)
+                f.argtypes = args
+                f.restype = res
+            L._server_sigs = True
+        self._h = L.ozl_server_create(hbm_budget, workers, 1 if checksums else 0)
+        if not self._h:
+            raise ZLError(70, "ozl_server_create failed")
+        self._keep = {}
+
+    def submit_decompress(self, frame, out):
+        f = _as_u8(frame)
+        i = self._lib.ozl_server_submit_decompress(self._h, f.ctypes.data, f.size, out.ctypes.data, out.nbytes)
+        if not i:
+            raise ZLError(21, "submit failed")
+        self._keep[i] = (f, out)
+        return i
+
+    def submit_compress(self, arr, elt_width, recipe, out):
+        a = np.ascontiguousarray(arr)
+        n = a.size if elt_width else a.nbytes
+        i = self._lib.ozl_server_submit_compress(self._h, a.ctypes.data if a.size else None, n, elt_width, recipe,
+                                                 out.ctypes.data, out.nbytes)
+        if not i:
+            raise ZLError(21, "submit failed")
+        self._keep[i] = (a, out)
+        return i
+
+    def poll(self, max_items=4096, wait_ms=0):
+        """[(id, code, value, latency_us)] of completed requests."""
+        ids = (ctypes.c_uint64 * max_items)()
+        res = (ZLReport * max_items)()
+        lat = (ctypes.c_double * max_items)()
+        k = self._lib.ozl_server_poll(self._h, ids, res, lat, max_items, wait_ms)
+        out = []
+        for j in range(k):
+            self._keep.pop(ids[j], None)
+            out.append((ids[j], res[j].code, res[j].value, lat[j]))
+        return out
+
+    def in_flight(self):
+        return self._lib.ozl_server_in_flight(self._h)
+
+    def close(self):
+        if self._h:
+            self._lib.ozl_server_free(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        self.close()

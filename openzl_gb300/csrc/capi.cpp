@@ -15,6 +15,7 @@
 #include "../../include/openzl_gb300.h"
 #include "dec_exec.h"
 #include "dec_plan.h"
+#include "decode_batch.h"
 #include "enc_engine.h"
 
 namespace {
@@ -22,177 +23,25 @@ namespace {
 ZL_Report ok(size_t v) { return ZL_Report{ ZL_ErrorCode_no_error, v }; }
 ZL_Report fail(int code) { return ZL_Report{ ZL_ErrorCode(code), 0 }; }
 
-// Grow-only device allocation with slack so that kernels may read whole
-// aligned words around the ends of the streams they hold.
-struct DevBuf {
-    uint8_t* p = nullptr;
-    size_t cap = 0;
-    ~DevBuf() { release(); }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-    bool reserve(size_t bytes)
-    {
-        size_t const want = bytes + 256;
-        if (want <= cap) return true;
-        release();
-        if (cudaMalloc(&p, want) != cudaSuccess) {
-            p = nullptr;
-            return false;
-        }
-        cap = want;
-        return true;
-    }
-    uint8_t* data() const { return p ? p + 64 : nullptr; } // 64 bytes of slack in front
-};
-
-std::once_flag gPrepOnce;
-cudaError_t gPrepErr = cudaSuccess;
-cudaError_t prepare()
-{
-    std::call_once(gPrepOnce, [] { gPrepErr = ozl::prepareKernels(); });
-    return gPrepErr;
-}
-
 } // namespace
 
-// A planned decode of one or more frames, with its device resources.
-struct OZL_GpuBatch_s {
-    bool checkContent = true;
-    bool checkCompressed = true;
-    ozl::DecodePlan plan;
-    ozl::DeviceLayout layout;
-    DevBuf pool, scratch, arena, params, status;
-    std::vector<const uint8_t*> dFrames;
-    std::vector<uint8_t*> dOuts;
-    std::vector<size_t> sizes;
-    long launches = 0;
-    bool uploaded = false;   // descriptors and parameters of the plan are on the device
-    cudaGraphExec_t graph = nullptr;
-    cudaStream_t graphStream = nullptr;
-    std::string err;
+namespace ozl {
+cudaError_t prepareOnce()
+{
+    static std::once_flag once;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [] { err = prepareKernels(); });
+    return err;
+}
+} // namespace ozl
 
-    ~OZL_GpuBatch_s() { dropGraph(); }
-    void dropGraph()
-    {
-        if (graph) cudaGraphExecDestroy(graph);
-        graph = nullptr;
-    }
-
-    ZL_Report makePlan(size_t n, const void* const* hF, const size_t* fs, const void* const* dF,
-                       void* const* dO, const size_t* caps)
-    {
-        dropGraph();
-        if (prepare() != cudaSuccess) { err = "kernel attributes could not be set"; return fail(ZL_ErrorCode_GENERIC); }
-        int rc = plan.build(n, reinterpret_cast<const uint8_t* const*>(hF), fs, caps, checkContent,
-                            checkCompressed, err);
-        if (rc) return fail(rc);
-        dFrames.assign(reinterpret_cast<const uint8_t* const*>(dF), reinterpret_cast<const uint8_t* const*>(dF) + n);
-        dOuts.assign(reinterpret_cast<uint8_t* const*>(dO), reinterpret_cast<uint8_t* const*>(dO) + n);
-        sizes.resize(n);
-        for (size_t i = 0; i < n; i++) sizes[i] = size_t(plan.frames[i].decodedSize);
-        // size pass, allocate, then the real layout
-        rc = ozl::layoutPlan(plan, dFrames.data(), dOuts.data(), nullptr, nullptr, nullptr, nullptr, layout, err);
-        if (rc) return fail(rc);
-        if (!pool.reserve(layout.pool.size()) || !scratch.reserve(layout.scratchBytes)
-            || !arena.reserve(plan.arenaBytes) || !params.reserve(plan.params.size()) || !status.reserve(64)) {
-            err = "device allocation failed";
-            return fail(ZL_ErrorCode_allocation);
-        }
-        rc = ozl::layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), scratch.data(),
-                             pool.data(), layout, err);
-        if (rc) return fail(rc);
-        uploaded = false;
-        launches = 0;
-        return ok(size_t(plan.totalOut));
-    }
-
-    // Copies the plan's descriptors and parameters to the device, ordered on
-    // the stream that runs the plan (the kernels read them).
-    ZL_Report upload(cudaStream_t s)
-    {
-        if (uploaded) return ok(0);
-        if (!layout.pool.empty()
-            && cudaMemcpyAsync(pool.data(), layout.pool.data(), layout.pool.size(), cudaMemcpyHostToDevice, s)
-                       != cudaSuccess) {
-            err = "descriptor upload failed";
-            return fail(ZL_ErrorCode_GENERIC);
-        }
-        if (!plan.params.empty()
-            && cudaMemcpyAsync(params.data(), plan.params.data(), plan.params.size(), cudaMemcpyHostToDevice, s)
-                       != cudaSuccess) {
-            err = "parameter upload failed";
-            return fail(ZL_ErrorCode_GENERIC);
-        }
-        uploaded = true;
-        return ok(0);
-    }
-
-    ZL_Report enqueue(cudaStream_t s)
-    {
-        if (cudaMemsetAsync(status.data(), 0, 4, s) != cudaSuccess) return fail(ZL_ErrorCode_GENERIC);
-        long n = ozl::runLaunches(layout, pool.data(), scratch.data(), reinterpret_cast<uint32_t*>(status.data()), s);
-        if (n < 0) {
-            err = std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError());
-            return fail(ZL_ErrorCode_GENERIC);
-        }
-        launches = n;
-        return ok(0);
-    }
-
-    ZL_Report run(cudaStream_t s, bool useGraph)
-    {
-        ZL_Report const u = upload(s);
-        if (ZL_isError(u)) return u;
-        if (!useGraph) return enqueue(s);
-        if (s == nullptr) {
-            err = "CUDA graph capture needs a non-default stream";
-            return fail(ZL_ErrorCode_parameter_invalid);
-        }
-        if (!graph || graphStream != s) {
-            dropGraph();
-            cudaGraph_t g = nullptr;
-            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-                err = "stream capture failed";
-                return fail(ZL_ErrorCode_GENERIC);
-            }
-            ZL_Report r = enqueue(s);
-            cudaError_t e = cudaStreamEndCapture(s, &g);
-            if (ZL_isError(r)) { if (g) cudaGraphDestroy(g); return r; }
-            if (e != cudaSuccess) { err = "stream capture failed"; return fail(ZL_ErrorCode_GENERIC); }
-            e = cudaGraphInstantiate(&graph, g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) { graph = nullptr; err = "graph instantiation failed"; return fail(ZL_ErrorCode_GENERIC); }
-            graphStream = s;
-        }
-        if (cudaGraphLaunch(graph, s) != cudaSuccess) { err = "graph launch failed"; return fail(ZL_ErrorCode_GENERIC); }
-        return ok(0);
-    }
-
-    ZL_Report check(cudaStream_t s)
-    {
-        uint32_t st = 0;
-        if (cudaMemcpyAsync(&st, status.data(), 4, cudaMemcpyDeviceToHost, s) != cudaSuccess
-            || cudaStreamSynchronize(s) != cudaSuccess) {
-            err = std::string("device error: ") + cudaGetErrorString(cudaGetLastError());
-            return fail(ZL_ErrorCode_GENERIC);
-        }
-        if (st) {
-            err = st == 13 ? "compressed checksum mismatch"
-                           : st == 14 ? "content checksum mismatch" : st == 80 ? "device wait timed out" : "corruption";
-            return fail(int(st));
-        }
-        return ok(size_t(plan.totalOut));
-    }
-};
+// A planned decode of one or more frames (the C handle).
+struct OZL_GpuBatch_s : ozl::DecodeBatch {};
 
 struct ZL_DCtx_s {
-    OZL_GpuBatch_s batch;
+    ozl::DecodeBatch batch;
     bool sticky = false;
-    DevBuf frame, out;
+    ozl::DevBuf frame, out;
     cudaStream_t stream = nullptr;
     std::string err;
     ~ZL_DCtx_s()

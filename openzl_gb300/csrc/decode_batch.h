@@ -1,0 +1,179 @@
+// Batched decode of planned frames on the device, shared by the C entry
+// points (capi.cpp) and the serving loop (server.cpp).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/openzl_gb300.h"
+#include "dec_exec.h"
+#include "dec_plan.h"
+
+namespace ozl {
+
+inline ZL_Report reportOk(size_t v) { return ZL_Report{ ZL_ErrorCode_no_error, v }; }
+inline ZL_Report reportFail(int code) { return ZL_Report{ ZL_ErrorCode(code), 0 }; }
+
+// Grow-only device allocation with slack so that kernels may read whole
+// aligned words around the ends of the streams they hold.
+struct DevBuf {
+    uint8_t* p = nullptr;
+    size_t cap = 0;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    bool reserve(size_t bytes)
+    {
+        size_t const want = bytes + 256;
+        if (want <= cap) return true;
+        release();
+        if (cudaMalloc(&p, want) != cudaSuccess) {
+            p = nullptr;
+            return false;
+        }
+        cap = want;
+        return true;
+    }
+    uint8_t* data() const { return p ? p + 64 : nullptr; } // 64 bytes of slack in front
+};
+
+// Kernel attributes, set once per process.
+cudaError_t prepareOnce();
+
+// A planned decode of one or more frames, with its device resources.
+struct DecodeBatch {
+    bool checkContent = true;
+    bool checkCompressed = true;
+    DecodePlan plan;
+    DeviceLayout layout;
+    DevBuf pool, scratch, arena, params, status;
+    std::vector<const uint8_t*> dFrames;
+    std::vector<uint8_t*> dOuts;
+    std::vector<size_t> sizes;
+    long launches = 0;
+    bool uploaded = false;   // descriptors and parameters of the plan are on the device
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t graphStream = nullptr;
+    std::string err;
+
+    ~DecodeBatch() { dropGraph(); }
+    void dropGraph()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+
+    ZL_Report makePlan(size_t n, const void* const* hF, const size_t* fs, const void* const* dF,
+                       void* const* dO, const size_t* caps)
+    {
+        dropGraph();
+        if (prepareOnce() != cudaSuccess) { err = "kernel attributes could not be set"; return reportFail(ZL_ErrorCode_GENERIC); }
+        int rc = plan.build(n, reinterpret_cast<const uint8_t* const*>(hF), fs, caps, checkContent,
+                            checkCompressed, err);
+        if (rc) return reportFail(rc);
+        dFrames.assign(reinterpret_cast<const uint8_t* const*>(dF), reinterpret_cast<const uint8_t* const*>(dF) + n);
+        dOuts.assign(reinterpret_cast<uint8_t* const*>(dO), reinterpret_cast<uint8_t* const*>(dO) + n);
+        sizes.resize(n);
+        for (size_t i = 0; i < n; i++) sizes[i] = size_t(plan.frames[i].decodedSize);
+        // size pass, allocate, then the real layout
+        rc = layoutPlan(plan, dFrames.data(), dOuts.data(), nullptr, nullptr, nullptr, nullptr, layout, err);
+        if (rc) return reportFail(rc);
+        if (!pool.reserve(layout.pool.size()) || !scratch.reserve(layout.scratchBytes)
+            || !arena.reserve(plan.arenaBytes) || !params.reserve(plan.params.size()) || !status.reserve(64)) {
+            err = "device allocation failed";
+            return reportFail(ZL_ErrorCode_allocation);
+        }
+        rc = layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), scratch.data(),
+                             pool.data(), layout, err);
+        if (rc) return reportFail(rc);
+        uploaded = false;
+        launches = 0;
+        return reportOk(size_t(plan.totalOut));
+    }
+
+    // Copies the plan's descriptors and parameters to the device, ordered on
+    // the stream that runs the plan (the kernels read them).
+    ZL_Report upload(cudaStream_t s)
+    {
+        if (uploaded) return reportOk(0);
+        if (!layout.pool.empty()
+            && cudaMemcpyAsync(pool.data(), layout.pool.data(), layout.pool.size(), cudaMemcpyHostToDevice, s)
+                       != cudaSuccess) {
+            err = "descriptor upload failed";
+            return reportFail(ZL_ErrorCode_GENERIC);
+        }
+        if (!plan.params.empty()
+            && cudaMemcpyAsync(params.data(), plan.params.data(), plan.params.size(), cudaMemcpyHostToDevice, s)
+                       != cudaSuccess) {
+            err = "parameter upload failed";
+            return reportFail(ZL_ErrorCode_GENERIC);
+        }
+        uploaded = true;
+        return reportOk(0);
+    }
+
+    ZL_Report enqueue(cudaStream_t s)
+    {
+        if (cudaMemsetAsync(status.data(), 0, 4, s) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
+        long n = runLaunches(layout, pool.data(), scratch.data(), reinterpret_cast<uint32_t*>(status.data()), s);
+        if (n < 0) {
+            err = std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError());
+            return reportFail(ZL_ErrorCode_GENERIC);
+        }
+        launches = n;
+        return reportOk(0);
+    }
+
+    ZL_Report run(cudaStream_t s, bool useGraph)
+    {
+        ZL_Report const u = upload(s);
+        if (ZL_isError(u)) return u;
+        if (!useGraph) return enqueue(s);
+        if (s == nullptr) {
+            err = "CUDA graph capture needs a non-default stream";
+            return reportFail(ZL_ErrorCode_parameter_invalid);
+        }
+        if (!graph || graphStream != s) {
+            dropGraph();
+            cudaGraph_t g = nullptr;
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                err = "stream capture failed";
+                return reportFail(ZL_ErrorCode_GENERIC);
+            }
+            ZL_Report r = enqueue(s);
+            cudaError_t e = cudaStreamEndCapture(s, &g);
+            if (ZL_isError(r)) { if (g) cudaGraphDestroy(g); return r; }
+            if (e != cudaSuccess) { err = "stream capture failed"; return reportFail(ZL_ErrorCode_GENERIC); }
+            e = cudaGraphInstantiate(&graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { graph = nullptr; err = "graph instantiation failed"; return reportFail(ZL_ErrorCode_GENERIC); }
+            graphStream = s;
+        }
+        if (cudaGraphLaunch(graph, s) != cudaSuccess) { err = "graph launch failed"; return reportFail(ZL_ErrorCode_GENERIC); }
+        return reportOk(0);
+    }
+
+    ZL_Report check(cudaStream_t s)
+    {
+        uint32_t st = 0;
+        if (cudaMemcpyAsync(&st, status.data(), 4, cudaMemcpyDeviceToHost, s) != cudaSuccess
+            || cudaStreamSynchronize(s) != cudaSuccess) {
+            err = std::string("device error: ") + cudaGetErrorString(cudaGetLastError());
+            return reportFail(ZL_ErrorCode_GENERIC);
+        }
+        if (st) {
+            err = st == 13 ? "compressed checksum mismatch"
+                           : st == 14 ? "content checksum mismatch" : st == 80 ? "device wait timed out" : "corruption";
+            return reportFail(int(st));
+        }
+        return reportOk(size_t(plan.totalOut));
+    }
+};
+
+} // namespace ozl

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <mutex>
 
 #include "dec_exec.h"
 #include "enc_exec.h"
@@ -568,11 +569,10 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
 {
     Impl& I = *impl_;
     launches_ = 0;
-    static bool prepared = false;
-    if (!prepared) {
-        if (prepareEncodeKernels() != cudaSuccess) { err = "kernel attributes"; return 1; }
-        prepared = true;
-    }
+    static std::once_flag prepOnce;
+    static cudaError_t prepErr = cudaSuccess;
+    std::call_once(prepOnce, [] { prepErr = prepareEncodeKernels(); });
+    if (prepErr != cudaSuccess) { err = "kernel attributes"; return 1; }
     size_t const nf = frames.size();
     sizes.assign(nf, 0);
     std::vector<Front> fronts(nf);

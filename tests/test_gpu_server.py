@@ -1,0 +1,110 @@
+"""Serving loop: requests of mixed kinds and sizes give the same bytes when
+run alone (one request in the system at a time) and in the mix (all queued
+at once over several workers), and both equal the expected result (decoded
+input; the reference's frame through the oracle). Errors stay with their own
+request."""
+import time
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(seed=7):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(48):
+        w = int(rng.choice([1, 2, 4, 8]))
+        n = int(np.exp(rng.uniform(np.log(300), np.log(400000)))) // w + 1
+        dt = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[w]
+        a = (1000 + np.cumsum(rng.integers(-int(rng.integers(1, 5000)), 5000, n))).astype(dt)
+        recipe = 3 if k % 3 else 4
+        if k % 5 == 0:
+            reqs.append(("c", a, w, recipe, oracle.compress(recipe, a, w)))
+        else:
+            reqs.append(("d", oracle.compress(recipe, a, w), w, recipe, a))
+    return reqs
+
+
+def _submit(srv, r):
+    kind, x, w, recipe, want = r
+    if kind == "d":
+        out = np.zeros(max(want.nbytes, 1), np.uint8)
+        return srv.submit_decompress(x, out), out
+    out = np.zeros(2 * x.nbytes + 1024, np.uint8)
+    return srv.submit_compress(x, w, recipe, out), out
+
+
+def _collect(srv, n, timeout=120):
+    got = {}
+    t0 = time.time()
+    while len(got) < n and time.time() - t0 < timeout:
+        for i, code, val, lat in srv.poll(wait_ms=100):
+            got[i] = (code, val, lat)
+    return got
+
+
+def test_alone_equals_mix_equals_expected(gpu_lib):
+    import openzl_gb300 as oz
+
+    reqs = _requests()
+    srv = oz.Server(hbm_budget=1 << 30, workers=3)
+    alone = []
+    for r in reqs:
+        i, out = _submit(srv, r)
+        res = _collect(srv, 1)
+        code, val, lat = res[i]
+        assert code == 0, (r[0], code)
+        alone.append(out[:val].tobytes())
+    ids, outs = [], []
+    for r in reqs:
+        i, out = _submit(srv, r)
+        ids.append(i)
+        outs.append(out)
+    res = _collect(srv, len(reqs))
+    srv.close()
+    assert len(res) == len(reqs)
+    for r, i, out, a in zip(reqs, ids, outs, alone):
+        code, val, lat = res[i]
+        assert code == 0
+        mix = out[:val].tobytes()
+        assert mix == a  # tolerance 0: bit-exact alone and in the mix
+        kind, x, w, recipe, want = r
+        assert mix == want.tobytes()
+        assert lat > 0
+
+
+def test_errors_stay_with_their_request(gpu_lib):
+    import openzl_gb300 as oz
+
+    reqs = _requests(9)[:12]
+    srv = oz.Server(hbm_budget=64 << 20, workers=2)
+    ids = []
+    outs = []
+    for k, r in enumerate(reqs):
+        kind, x, w, recipe, want = r
+        if kind == "d" and k == 3:
+            bad = x.copy()
+            bad[len(bad) // 2] ^= 0x5A
+            out = np.zeros(want.nbytes, np.uint8)
+            ids.append(srv.submit_decompress(bad, out))
+        else:
+            i, out = _submit(srv, r)
+            ids.append(i)
+        outs.append(out)
+    big = np.zeros(40 << 20, np.uint8)
+    big_out = np.zeros(1, np.uint8)
+    big_id = srv.submit_compress(big, 0, 0, big_out)  # larger than one 32 MiB arena
+    res = _collect(srv, len(ids) + 1)
+    srv.close()
+    assert res[big_id][0] == 4  # srcSize_tooLarge
+    for k, (r, i, out) in enumerate(zip(reqs, ids, outs)):
+        code, val, _ = res[i]
+        if k == 3 and r[0] == "d":
+            assert code != 0
+        else:
+            assert code == 0
+            assert out[:val].tobytes() == r[4].tobytes()
