@@ -43,6 +43,7 @@ METRIC = "decompressed GB/s on 1 GB300 (bit-exact): batched vs plain, %HBM peak;
 WORKLOAD = "mixed_frames_4096"
 RECIPE_TSPLIT_FSE = 3   # delta -> to-struct -> transpose-split(FSE)
 RECIPE_BITPACK_HUF = 4  # delta -> bitpack_int -> Huffman
+RECIPE_DZ_BITPACK_HUF = 2  # delta -> zigzag -> bitpack_int -> Huffman
 OUT_ALIGN = 256
 FRAME_ALIGN = 16
 
@@ -58,6 +59,10 @@ def parse_args():
     p.add_argument("--cpu-threads", type=int, default=0, help="0 = all host cores")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--no-plain", action="store_true", help="skip the per-frame plain path")
+    p.add_argument("--no-serve", action="store_true", help="skip the serving-loop run")
+    p.add_argument("--no-single", action="store_true", help="skip the single 256 MiB array run")
+    p.add_argument("--serve-rates", default="1000,5000,20000,50000", help="request rates (req/s) for the serving run")
+    p.add_argument("--serve-seconds", type=float, default=1.0, help="seconds of arrivals per rate")
     return p.parse_args()
 
 
@@ -277,6 +282,181 @@ def build_workload_host(spec, threads):
     with ThreadPoolExecutor(threads) as ex:
         list(ex.map(gen, range(len(spec)), chunksize=8))
     return host_in, ooffs, osizes, obytes
+
+
+# ---------------------------------------------------------------------------
+# single large array (256 MiB int64 timestamps, delta -> zigzag -> bitpack ->
+# Huffman), decoded by the plain per-frame path
+
+
+def timestamps(seed, n):
+    rng = np.random.default_rng(seed)
+    inc = rng.geometric(1 / 1000, n).astype(np.int64)
+    out = rng.random(n) < 0.01
+    inc[out] = rng.integers(0, 1 << 32, int(out.sum()))
+    return (1700000000000000000 + np.cumsum(inc)).astype(np.int64)
+
+
+def run_single_array(oz, torch, dev, sptr, seed):
+    n = 256 << 17  # 33,554,432 int64 values = 256 MiB
+    a = timestamps(seed + 2, n)
+    d_in = torch.from_numpy(a.view(np.uint8)).to(dev)
+    enc = oz.GpuEncoder()
+    cap = enc.bound(a.nbytes)
+    d_fr = torch.empty(cap, dtype=torch.uint8, device=dev)
+    fs = enc.compress_batch([d_in.data_ptr()], [n], [8], [RECIPE_DZ_BITPACK_HUF], [d_fr.data_ptr()], [cap],
+                            checksums=True, stream=sptr)[0]
+    torch.cuda.synchronize()
+    frame_h = d_fr[:fs].cpu().numpy()
+    d_out = torch.empty(a.nbytes, dtype=torch.uint8, device=dev)
+    dctx = oz.DCtx()
+    for _ in range(2):
+        dctx.decompress_device(frame_h, d_fr.data_ptr(), d_out.data_ptr(), a.nbytes, stream=sptr)
+    torch.cuda.synchronize()
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        dctx.decompress_device(frame_h, d_fr.data_ptr(), d_out.data_ptr(), a.nbytes, stream=sptr)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    if not torch.equal(d_out, d_in):
+        raise RuntimeError("single-array decode differs from the input")
+    return {"workload": "timestamps_int64_256mib", "graph": "delta->zigzag->bitpack->Huffman",
+            "decoded_bytes": int(a.nbytes), "compressed_bytes": int(fs), "ratio": round(a.nbytes / fs, 3),
+            "plain_gbs": round(a.nbytes / dt / 1e9, 2), "ms": round(dt * 1e3, 3)}
+
+
+# ---------------------------------------------------------------------------
+# serving loop: Poisson arrivals of decompress (80 %) and compress (20 %)
+# requests, payloads log-normal (median 256 KiB, sigma 1.5, clipped to
+# 1 KiB..64 MiB) from the timestamp and random-walk generators
+
+
+def serving_pool(seed, count):
+    rng = np.random.default_rng(seed + 11)
+    sizes = np.clip(np.exp(rng.normal(np.log(256 << 10), 1.5, count)), 1 << 10, 64 << 20).astype(np.int64)
+    pool = []
+    for i, b in enumerate(sizes):
+        if i % 2 == 0:
+            a = timestamps(seed + 100 + i, max(int(b) // 8, 1))
+            pool.append((a.view(np.uint8), 8, RECIPE_DZ_BITPACK_HUF))
+        else:
+            w = int(rng.choice([1, 2, 4, 8]))
+            f = dict(n=max(int(b) // w, 1), w=w, step=int(np.exp(rng.uniform(0, np.log(65536)))),
+                     recipe=int(rng.choice([RECIPE_TSPLIT_FSE, RECIPE_BITPACK_HUF])),
+                     start=int(rng.integers(0, 1 << 40)), seed=int(rng.integers(0, 1 << 62)))
+            pool.append((make_frame_input(f), w, f["recipe"]))
+    return pool
+
+
+def run_serving(oz, torch, dev, sptr, args):
+    pool = serving_pool(args.seed, 96)
+    enc = oz.GpuEncoder()
+    # frames of every pool entry, compressed on the device
+    d_in = [torch.from_numpy(p[0].copy()).to(dev) for p in pool]
+    caps = [enc.bound(p[0].nbytes) for p in pool]
+    d_fr = [torch.empty(c, dtype=torch.uint8, device=dev) for c in caps]
+    fs = enc.compress_batch([d.data_ptr() for d in d_in], [p[0].nbytes // p[1] for p in pool], [p[1] for p in pool],
+                            [p[2] for p in pool], [d.data_ptr() for d in d_fr], caps, checksums=True, stream=sptr)
+    torch.cuda.synchronize()
+    frames = [d_fr[i][:fs[i]].cpu().numpy() for i in range(len(pool))]
+    del d_in, d_fr
+
+    def pinned(nbytes):
+        return torch.empty(max(nbytes, 1), dtype=torch.uint8, pin_memory=True).numpy()
+
+    frames_p, src_p = [], []
+    for i, p in enumerate(pool):
+        f = pinned(frames[i].size)
+        f[:frames[i].size] = frames[i]
+        frames_p.append(f[:frames[i].size])
+        x = pinned(p[0].nbytes)
+        x[:p[0].nbytes] = p[0]
+        src_p.append(x[:p[0].nbytes])
+    slots = 4
+    outs_d = [[pinned(p[0].nbytes) for _ in range(slots)] for p in pool]
+    outs_c = [[pinned(caps[i]) for _ in range(slots)] for i in range(len(pool))]
+    rng = np.random.default_rng(args.seed + 5)
+    srv = oz.Server(hbm_budget=40 << 30, workers=4, checksums=True)
+    results = []
+    rates = [int(r) for r in args.serve_rates.split(",") if r]
+    for rate in rates:
+        nreq = max(50, int(rate * args.serve_seconds))
+        gaps = rng.exponential(1.0 / rate, nreq)
+        kinds = rng.random(nreq) < 0.8
+        which = rng.integers(0, len(pool), nreq)
+        lat, nbytes, done = [], 0, 0
+        t0 = time.perf_counter()
+        due = t0
+        last_poll = t0
+        for k in range(nreq):
+            due += gaps[k]
+            while True:  # wait for the arrival time, draining completions every 0.2 ms
+                now = time.perf_counter()
+                if now - last_poll > 2e-4:
+                    for _, code, val, lus in srv.poll(wait_ms=0):
+                        if code:
+                            raise RuntimeError("serving request failed (%d)" % code)
+                        lat.append(lus)
+                        done += 1
+                    last_poll = now
+                if now >= due:
+                    break
+            i = int(which[k])
+            if kinds[k]:
+                srv.submit_decompress(frames_p[i], outs_d[i][k % slots])
+            else:
+                srv.submit_compress(src_p[i], pool[i][1], pool[i][2], outs_c[i][k % slots])
+            nbytes += pool[i][0].nbytes
+        while done < nreq:
+            for _, code, val, lus in srv.poll(wait_ms=50):
+                if code:
+                    raise RuntimeError("serving request failed (%d)" % code)
+                lat.append(lus)
+                done += 1
+        wall = time.perf_counter() - t0
+        lat = np.sort(np.array(lat)) / 1e3
+        results.append({"rate": rate, "requests": nreq, "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                        "p99_ms": round(float(np.percentile(lat, 99)), 3), "gbs": round(nbytes / wall / 1e9, 2),
+                        "offered_gbs": round(nbytes / (gaps.sum()) / 1e9, 2)})
+    srv.close()
+    # plain per-request path: the same kind of requests one call at a time
+    # through the reference-style API (ZL_DCtx_decompressTyped /
+    # ZL_CCtx_compressTypedRef with host buffers)
+    d = oz.DCtx()
+    comps = {}
+    for r in (RECIPE_TSPLIT_FSE, RECIPE_BITPACK_HUF, RECIPE_DZ_BITPACK_HUF):
+        c = oz.Compressor()
+        a = oz.api
+        if r == RECIPE_TSPLIT_FSE:
+            g = c.pipeline([a.NODE_DELTA_INT, a.NODE_CONVERT_NUM_TO_TOKEN], c.transpose_split(a.GRAPH_FSE))
+        elif r == RECIPE_BITPACK_HUF:
+            g = c.node(a.NODE_DELTA_INT, c.node(a.NODE_BITPACK_INT, a.GRAPH_HUFFMAN))
+        else:
+            g = c.pipeline([a.NODE_DELTA_INT, a.NODE_ZIGZAG], c.node(a.NODE_BITPACK_INT, a.GRAPH_HUFFMAN))
+        c.select(g)
+        cc = oz.CCtx()
+        cc.ref_compressor(c)
+        cc.set_parameter(a.CPARAM_STICKY, 1)
+        cc.set_parameter(a.CPARAM_FORMAT_VERSION, 23)
+        comps[r] = (c, cc)
+    npl = 300
+    kinds = rng.random(npl) < 0.8
+    which = rng.integers(0, len(pool), npl)
+    nbytes = 0
+    t0 = time.perf_counter()
+    for k in range(npl):
+        i = int(which[k])
+        if kinds[k]:
+            d.decompress_typed(frames_p[i], outs_d[i][0])
+        else:
+            _, w, r = pool[i]
+            comps[r][1].compress_numeric(src_p[i].view({1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[w]))
+        nbytes += pool[i][0].nbytes
+    plain_gbs = nbytes / (time.perf_counter() - t0) / 1e9
+    return {"workers": 4, "hbm_budget_gb": 40, "mix": "80% decompress / 20% compress",
+            "payload": "log-normal, median 256 KiB, sigma 1.5, clipped 1 KiB..64 MiB", "pool": len(pool),
+            "host_buffers": "pinned", "rates": results, "plain_per_request_gbs": round(plain_gbs, 3)}
 
 
 # ---------------------------------------------------------------------------
@@ -523,6 +703,14 @@ def main():
         plain = {"value": round(total_out / plain_s / 1e9, 3), "unit": "GB/s", "ms": round(plain_s * 1e3, 2),
                  "batched_over_plain": round(value / ws / (total_out / plain_s / 1e9), 2)}
 
+    # ---- the single large array and the serving loop (rank 0, N=1 only)
+    single = None
+    serving = None
+    if rank == 0 and ws == 1 and not args.no_single:
+        single = run_single_array(oz, torch, dev, sptr, args.seed)
+    if rank == 0 and ws == 1 and not args.no_serve:
+        serving = run_serving(oz, torch, dev, sptr, args)
+
     # ---- CPU baseline (rank 0, N=1 only): the same frames on the host cores
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -558,6 +746,8 @@ def main():
         "p50_ms": round(statistics.median(step_ms), 4),
         "p99_ms": round(srt[min(len(srt) - 1, int(round(0.99 * (len(srt) - 1))))], 4),
         "plain": plain,
+        "single_array": single,
+        "serving": serving,
         "encode": {"value": round(enc_gbs, 3), "unit": "GB/s", "note": "batched compress, host decisions included"},
         "roofline": roofline,
         "cpu_baseline": cpu,

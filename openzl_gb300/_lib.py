@@ -525,7 +525,9 @@ class Server:
 
     def submit_compress(self, arr, elt_width, recipe, out):
         a = np.ascontiguousarray(arr)
-        n = a.size if elt_width else a.nbytes
+        if elt_width and a.nbytes % elt_width:
+            raise ZLError(21, "input size is not a multiple of the element width")
+        n = a.nbytes // elt_width if elt_width else a.nbytes
         i = self._lib.ozl_server_submit_compress(self._h, a.ctypes.data if a.size else None, n, elt_width, recipe,
                                                  out.ctypes.data, out.nbytes)
         if not i:
@@ -533,12 +535,16 @@ class Server:
         self._keep[i] = (a, out)
         return i
 
-    def poll(self, max_items=4096, wait_ms=0):
+    _POLL = 4096
+
+    def poll(self, wait_ms=0):
         """[(id, code, value, latency_us)] of completed requests."""
-        ids = (ctypes.c_uint64 * max_items)()
-        res = (ZLReport * max_items)()
-        lat = (ctypes.c_double * max_items)()
-        k = self._lib.ozl_server_poll(self._h, ids, res, lat, max_items, wait_ms)
+        if not hasattr(self, "_ids"):
+            self._ids = (ctypes.c_uint64 * self._POLL)()
+            self._res = (ZLReport * self._POLL)()
+            self._lat = (ctypes.c_double * self._POLL)()
+        ids, res, lat = self._ids, self._res, self._lat
+        k = self._lib.ozl_server_poll(self._h, ids, res, lat, self._POLL, wait_ms)
         out = []
         for j in range(k):
             self._keep.pop(ids[j], None)
