@@ -115,7 +115,25 @@ struct ZL_Compressor_s {
                 if (!flatten(g.succ[0], out, depth + 1)) return false;
                 out += ")";
                 return true;
-            default: return false; // tokenize and multi-output nodes: not on the GPU encoder yet
+            case TOKENIZE: {
+                if (g.type != ZL_Type_numeric || g.sort) return false; // numeric, first-occurrence order
+                out += "tokenize(";
+                if (!flatten(g.succ[0], out, depth + 1)) return false;
+                out += ",";
+                if (!flatten(g.succ[1], out, depth + 1)) return false;
+                out += ")";
+                return true;
+            }
+            case MULTI: {
+                if (g.nodes[0] != N_BF16 || g.succ.size() != 2) return false;
+                out += "bf16(";
+                if (!flatten(g.succ[0], out, depth + 1)) return false;
+                out += ",";
+                if (!flatten(g.succ[1], out, depth + 1)) return false;
+                out += ")";
+                return true;
+            }
+            default: return false;
         }
     }
 };
@@ -169,6 +187,8 @@ int recipeOf(const std::string& chain)
         { "CONSTANT", ozl::RC_CONSTANT },
         { "FLATPACK", ozl::RC_FLATPACK },
         { "BITPACK", ozl::RC_BITPACK },
+        { "tokenize(STORE,bitpack>HUFFMAN)", ozl::RC_TOKENIZE },
+        { "bf16(STORE,FSE)", ozl::RC_BF16 },
     };
     auto it = table.find(chain);
     return it == table.end() ? -1 : it->second;
@@ -178,7 +198,7 @@ bool numericRecipe(int r)
 {
     return r == ozl::RC_DZ_TSPLIT_FSE || r == ozl::RC_DZ_BITPACK_HUF || r == ozl::RC_D_TSPLIT_FSE
             || r == ozl::RC_D_BITPACK_HUF || r == ozl::RC_DELTA_STORE || r == ozl::RC_ZIGZAG_STORE
-            || r == ozl::RC_BITPACK_STORE || r == ozl::RC_TSPLIT_STORE;
+            || r == ozl::RC_BITPACK_STORE || r == ozl::RC_TSPLIT_STORE || r == ozl::RC_TOKENIZE || r == ozl::RC_BF16;
 }
 
 ZL_Report compressOne(ZL_CCtx* c, void* dst, size_t cap, const ZL_TypedRef& in)

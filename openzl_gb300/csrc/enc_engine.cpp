@@ -35,7 +35,8 @@ enum : int { T_SERIAL = 1, T_STRUCT = 2, T_NUMERIC = 4 };
 enum : uint32_t {
     TR_DELTA = 1, TR_ZIGZAG = 3, TR_TSPLIT = 4, TR_CONV_STRUCT_TO_SERIAL = 6, TR_CONV_NUM_TO_STRUCT = 8,
     TR_CONV_NUM_TO_SERIAL = 10, TR_BITPACK_SERIAL = 27, TR_BITPACK_INT = 28, TR_FLATPACK = 29, TR_SPLITN = 40,
-    TR_CONST_SERIAL = 44, TR_FSE = 49, TR_HUF = 50, TR_NCOUNT = 52,
+    TR_CONST_SERIAL = 44, TR_FSE = 49, TR_HUF = 50, TR_NCOUNT = 52, TR_FLOAT_DECONSTRUCT = 33,
+    TR_TOKENIZE_NUMERIC = 37,
 };
 constexpr uint64_t kMinStream = 10;   // ZL_MINSTREAMSIZE_DEFAULT
 constexpr uint64_t kChunk = 1 << 15;  // entropy chunk size
@@ -146,12 +147,18 @@ struct Front {
     bool needMax = false;
     bool needFirst = false;   // delta: the first element goes to the codec header
     uint64_t first = 0;
+    int special = 0;          // 1: bf16 deconstruct, 2: tokenize
+    uint8_t* signFrac = nullptr, *exponent = nullptr;  // bf16 outputs
+    uint8_t* alphabet = nullptr, *idx = nullptr;       // tokenize outputs
+    uint32_t iw = 0;          // tokenize index width
+    uint64_t na = 0;          // tokenize alphabet size
+    uint32_t tokSlot = 0;
 };
 
 } // namespace
 
 struct EncodeBatch::Impl {
-    DevBuf bufA, bufE, bufF, bufSmall;
+    DevBuf bufA, bufE, bufF, bufSmall, bufT;
     std::vector<Job> jobs;           // data chunks (discovery order), then nested weights jobs
     size_t nbDataJobs = 0;
     bool checksums = true;
@@ -250,7 +257,7 @@ struct Engine {
     // ---- graphs ----------------------------------------------------------
     enum G {
         G_STORE, G_SERIAL_STORE, G_FSE, G_HUF, G_CONSTANT, G_BITPACK, G_FLATPACK, G_NCOUNT, G_TSPLIT_FSE,
-        G_TSPLIT_STORE, G_BITPACK_HUF, G_JOB
+        G_TSPLIT_STORE, G_BITPACK_HUF, G_JOB, G_TOKENIZE, G_BF16
     };
     struct Succ {
         int g, sid, job;
@@ -456,6 +463,35 @@ struct Engine {
                 runSuccs(succ);
                 return;
             }
+            case G_TOKENIZE: { // encode_tokenize_binding.c:423 (numeric, first-occurrence order)
+                sid = convertFor(sid, T_NUMERIC);
+                newNode(TR_TOKENIZE_NUMERIC, sid, 2);
+                int const a = newStream(s[sid].type, s[sid].w, front->na);
+                s[a].pieces.push_back(Piece{ front->alphabet, nullptr, front->na * s[sid].w });
+                int const o = newStream(T_NUMERIC, front->iw, s[sid].n);
+                s[o].pieces.push_back(Piece{ front->idx, nullptr, s[sid].n * front->iw });
+                nd.back().nbOut = 2;
+                succ.push_back({ G_STORE, a, -1 });
+                succ.push_back({ G_BITPACK_HUF, o, -1 });
+                runSuccs(succ);
+                return;
+            }
+            case G_BF16: { // encode_float_deconstruct_binding.c:14-80
+                sid = convertFor(sid, T_NUMERIC);
+                RNode& x = newNode(TR_FLOAT_DECONSTRUCT, sid, 2);
+                x.hdr[0] = 1; // bfloat16
+                x.hsz = 1;
+                uint64_t const n = s[sid].n;
+                int const sf = newStream(T_STRUCT, 1, n);
+                s[sf].pieces.push_back(Piece{ front->signFrac, nullptr, n });
+                int const ex = newStream(T_SERIAL, 1, n);
+                s[ex].pieces.push_back(Piece{ front->exponent, nullptr, n });
+                nd.back().nbOut = 2;
+                succ.push_back({ G_STORE, sf, -1 });
+                succ.push_back({ G_FSE, ex, -1 });
+                runSuccs(succ);
+                return;
+            }
             case G_BITPACK_HUF: {
                 sid = convertFor(sid, T_NUMERIC);
                 RNode& x = newNode(TR_BITPACK_INT, sid, 1);
@@ -587,6 +623,19 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                 || r == RC_D_BITPACK_HUF || r == RC_DELTA_STORE;
         bool const hasZz = r == RC_DZ_TSPLIT_FSE || r == RC_DZ_BITPACK_HUF || r == RC_ZIGZAG_STORE;
         if (F.serial || inBytes < kMinStream) continue; // no numeric front end
+        if (r == RC_BF16) {
+            if (F.w != 2) { err = "bf16 deconstruct takes 2-byte elements"; return 54; }
+            fr.special = 1;
+            fr.n = F.n;
+            continue;
+        }
+        if (r == RC_TOKENIZE) {
+            if (F.n >= (1ull << 32)) { err = "tokenize input too large"; return 4; }
+            fr.special = 2;
+            fr.n = F.n;
+            fr.mode = EOUT_BITPACK; // the indices, bit-packed
+            continue;
+        }
         fr.needFirst = hasDelta;
         uint64_t const m = hasDelta ? F.n - 1 : F.n;
         if (hasDelta && m * F.w < kMinStream) {
@@ -705,14 +754,99 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         for (size_t f = 0; f < contentHash.size(); f++) contentHash[f].hashOut = dHashOut + f;
     }
 
+    // tokenize: distinct values in first-occurrence order, counted then emitted
+    {
+        std::vector<size_t> tokFrames;
+        for (size_t f = 0; f < nf; f++)
+            if (fronts[f].special == 2) tokFrames.push_back(f);
+        if (!tokFrames.empty()) {
+            std::vector<TokTask> tt(tokFrames.size());
+            std::vector<TileRef> tiles;
+            uint8_t *dTasks = nullptr, *dTiles = nullptr, *dSums = nullptr, *dPre = nullptr, *dCnt = nullptr;
+            auto layoutT = [&](Bump& b) {
+                tiles.clear();
+                for (size_t k = 0; k < tokFrames.size(); k++) {
+                    size_t const f = tokFrames[k];
+                    uint64_t const n = frames[f].n;
+                    uint32_t const w = frames[f].w;
+                    uint64_t cap = 1024;
+                    while (cap < 2 * n) cap <<= 1;
+                    TokTask& t = tt[k];
+                    t = TokTask{};
+                    t.src = frames[f].dIn;
+                    t.n = n;
+                    t.w = w;
+                    t.capMask = cap - 1;
+                    t.state = reinterpret_cast<uint32_t*>(b.take(4 * cap));
+                    t.key = reinterpret_cast<uint64_t*>(b.take(8 * cap));
+                    t.first = reinterpret_cast<uint32_t*>(b.take(4 * cap));
+                    t.slotOf = reinterpret_cast<uint32_t*>(b.take(4 * n + 64));
+                    t.rank = reinterpret_cast<uint32_t*>(b.take(4 * n + 64));
+                    t.alphabet = b.take(uint64_t(w) * n + 64);
+                    t.idx = b.take(4 * n + 64);
+                    t.tileBase = uint32_t(tiles.size());
+                    for (uint32_t j = 0; j < (n + kEncTile - 1) / kEncTile; j++) tiles.push_back(TileRef{ uint32_t(k), j });
+                    fronts[f].tokSlot = uint32_t(k);
+                }
+                dTasks = b.take(tt.size() * sizeof(TokTask));
+                dTiles = b.take(tiles.size() * sizeof(TileRef));
+                dSums = b.take(tiles.size() * 8 + 8);
+                dPre = b.take(tiles.size() * 8 + 8);
+                dCnt = b.take(tt.size() * 4 + 8); // counts, then the error count
+            };
+            Bump sizeT;
+            layoutT(sizeT);
+            if (!I.bufT.reserve(sizeT.used)) { err = "device allocation failed"; return 70; }
+            Bump realT{ I.bufT.data(), 0 };
+            layoutT(realT);
+            for (const TokTask& t : tt) {
+                cudaMemsetAsync(t.state, 0, 4 * (t.capMask + 1), st);
+                cudaMemsetAsync(t.first, 0xff, 4 * (t.capMask + 1), st);
+            }
+            uint32_t* const counts = reinterpret_cast<uint32_t*>(dCnt);
+            uint32_t* const errors = counts + tt.size();
+            cudaMemsetAsync(dCnt, 0, tt.size() * 4 + 8, st);
+            cudaMemcpyAsync(dTasks, tt.data(), tt.size() * sizeof(TokTask), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dTiles, tiles.data(), tiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+            launchTokCount(reinterpret_cast<const TokTask*>(dTasks), uint32_t(tt.size()),
+                           reinterpret_cast<const TileRef*>(dTiles), uint32_t(tiles.size()),
+                           reinterpret_cast<uint64_t*>(dSums), reinterpret_cast<uint64_t*>(dPre), counts, errors, st);
+            launches_ += 4;
+            std::vector<uint32_t> hc(tt.size() + 1);
+            cudaMemcpyAsync(hc.data(), dCnt, (tt.size() + 1) * 4, cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in tokenize"; return 1; }
+            if (hc[tt.size()]) { err = "tokenize table overflow"; return 1; }
+            for (size_t k = 0; k < tt.size(); k++) {
+                Front& fr = fronts[tokFrames[k]];
+                uint64_t const na = hc[k];
+                fr.na = na;
+                fr.iw = na <= 256 ? 1 : (na <= 65536 ? 2 : 4); // encode_tokenize_binding.c:195-205
+                uint64_t const mx = na ? na - 1 : 0;
+                fr.nbBits = 1 + (mx ? unsigned(63 - __builtin_clzll(mx)) : 0);
+                fr.alphabet = tt[k].alphabet;
+                fr.idx = tt[k].idx;
+                tt[k].iw = fr.iw;
+            }
+            cudaMemcpyAsync(dTasks, tt.data(), tt.size() * sizeof(TokTask), cudaMemcpyHostToDevice, st);
+            launchTokEmit(reinterpret_cast<const TokTask*>(dTasks), reinterpret_cast<const TileRef*>(dTiles),
+                          uint32_t(tiles.size()), st);
+            launches_++;
+        }
+    }
+
     // front-end outputs
     {
         Bump sizeB;
         auto layoutA = [&](Bump& b) {
             for (size_t f = 0; f < nf; f++) {
                 Front& fr = fronts[f];
+                if (fr.special == 1) {
+                    fr.signFrac = b.take(fr.n + 64, 64);
+                    fr.exponent = b.take(fr.n + 64, 64);
+                    continue;
+                }
                 if (fr.mode < 0) continue;
-                uint32_t const w = frames[f].w;
+                uint32_t const w = fr.special == 2 ? fr.iw : frames[f].w;
                 if (fr.mode == EOUT_PLANES) {
                     fr.planeStride = (fr.n + 63) & ~uint64_t(63);
                     fr.outBytes = fr.n; // per plane
@@ -738,11 +872,11 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             Front& fr = fronts[f];
             if (fr.mode < 0 || fr.n == 0) continue;
             EncNumTask t{};
-            t.src = frames[f].dIn;
+            t.src = fr.special == 2 ? fr.idx : frames[f].dIn;
             t.out = fr.out;
             t.n = fr.n;
             t.planeStride = fr.planeStride;
-            t.w = frames[f].w;
+            t.w = fr.special == 2 ? fr.iw : frames[f].w;
             t.delta = fr.delta;
             t.zigzag = fr.zigzag;
             t.mode = uint8_t(fr.mode);
@@ -750,16 +884,35 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             for (uint32_t k = 0; k < (fr.n + kEncTile - 1) / kEncTile; k++) tiles.push_back(TileRef{ uint32_t(tasks.size()), k });
             tasks.push_back(t);
         }
-        if (!tasks.empty()) {
-            size_t const bytes = tasks.size() * sizeof(EncNumTask) + tiles.size() * sizeof(TileRef) + 256;
+        std::vector<Bf16Task> bt;
+        std::vector<TileRef> btiles;
+        for (size_t f = 0; f < nf; f++) {
+            Front& fr = fronts[f];
+            if (fr.special != 1 || fr.n == 0) continue;
+            for (uint32_t k = 0; k < (fr.n + kEncTile - 1) / kEncTile; k++) btiles.push_back(TileRef{ uint32_t(bt.size()), k });
+            bt.push_back(Bf16Task{ frames[f].dIn, fr.signFrac, fr.exponent, fr.n });
+        }
+        if (!tasks.empty() || !bt.empty()) {
+            size_t const bytes = tasks.size() * sizeof(EncNumTask) + tiles.size() * sizeof(TileRef)
+                    + bt.size() * sizeof(Bf16Task) + btiles.size() * sizeof(TileRef) + 1024;
             if (!I.bufF.reserve(bytes)) { err = "device allocation failed"; return 70; }
             Bump b{ I.bufF.data(), 0 };
             auto* dT = reinterpret_cast<EncNumTask*>(b.take(tasks.size() * sizeof(EncNumTask)));
             auto* dTi = reinterpret_cast<TileRef*>(b.take(tiles.size() * sizeof(TileRef)));
-            cudaMemcpyAsync(dT, tasks.data(), tasks.size() * sizeof(EncNumTask), cudaMemcpyHostToDevice, st);
-            cudaMemcpyAsync(dTi, tiles.data(), tiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
-            launchEncNum(dT, dTi, uint32_t(tiles.size()), st);
-            launches_++;
+            auto* dB = reinterpret_cast<Bf16Task*>(b.take(bt.size() * sizeof(Bf16Task)));
+            auto* dBi = reinterpret_cast<TileRef*>(b.take(btiles.size() * sizeof(TileRef)));
+            if (!tasks.empty()) {
+                cudaMemcpyAsync(dT, tasks.data(), tasks.size() * sizeof(EncNumTask), cudaMemcpyHostToDevice, st);
+                cudaMemcpyAsync(dTi, tiles.data(), tiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+                launchEncNum(dT, dTi, uint32_t(tiles.size()), st);
+                launches_++;
+            }
+            if (!bt.empty()) {
+                cudaMemcpyAsync(dB, bt.data(), bt.size() * sizeof(Bf16Task), cudaMemcpyHostToDevice, st);
+                cudaMemcpyAsync(dBi, btiles.data(), btiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+                launchBf16(dB, dBi, uint32_t(btiles.size()), st);
+                launches_++;
+            }
             if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in front end"; return 1; }
         }
     }
@@ -778,6 +931,8 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         if (E.s[in].bytes() < kMinStream || r == RC_STORE) { E.runSuccessor(Engine::G_STORE, in); return; }
         switch (r) {
             case RC_FSE: E.runSuccessor(Engine::G_FSE, in); break;
+            case RC_TOKENIZE: E.runSuccessor(Engine::G_TOKENIZE, in); break;
+            case RC_BF16: E.runSuccessor(Engine::G_BF16, in); break;
             case RC_HUFFMAN: E.runSuccessor(Engine::G_HUF, in); break;
             case RC_CONSTANT:
             case RC_FLATPACK:

@@ -17,6 +17,8 @@ enum Recipe : int {
     RC_DZ_BITPACK_HUF = 2,  // delta -> zigzag -> bitpack_int -> Huffman
     RC_D_TSPLIT_FSE = 3,    // delta -> to-struct -> transpose split -> FSE per plane
     RC_D_BITPACK_HUF = 4,   // delta -> bitpack_int -> Huffman
+    RC_TOKENIZE = 5,        // tokenize (numeric, first-occurrence order): alphabet -> store, indices -> bitpack_int -> Huffman
+    RC_BF16 = 6,            // bf16 deconstruct: sign|fraction -> store, exponent -> FSE
     RC_FSE = 7,
     RC_HUFFMAN = 8,
     RC_DELTA_STORE = 9,

@@ -16,5 +16,11 @@ void launchHist(const HistTask* t, uint32_t n, uint32_t* hists, cudaStream_t s);
 void launchFseEnc(const FseEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);
 void launchHufEnc(const HufEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);
 void launchPut(const PutTask* t, uint32_t n, cudaStream_t s);
+void launchBf16(const Bf16Task* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
+// Tokenize, up to the per-task distinct counts (counts[task], errors[0]).
+void launchTokCount(const TokTask* t, uint32_t nbTasks, const TileRef* tiles, uint32_t nbTiles, uint64_t* tileSums,
+                    uint64_t* tilePrefix, uint32_t* counts, uint32_t* errors, cudaStream_t s);
+// Tokenize, the alphabet and the indices (iw set in the tasks).
+void launchTokEmit(const TokTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
 
 } // namespace ozl

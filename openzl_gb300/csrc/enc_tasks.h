@@ -70,6 +70,36 @@ struct PutTask {
     uint32_t bytes;          // 4 (low 32 bits) or 1 (low 8 bits)
 };
 
+// bf16 deconstruct (encode_float_deconstruct_kernel.c): per element, the
+// sign|fraction byte (sign in bit 0, the 7 fraction bits above it) and the
+// exponent byte.
+struct Bf16Task {
+    const uint8_t* src;
+    uint8_t* signFrac;
+    uint8_t* exponent;
+    uint64_t n;
+};
+
+// Tokenize with the alphabet in first-occurrence order: a per-frame
+// open-addressing table keeps each distinct value's first index; marking the
+// elements that are first occurrences and prefix-summing the marks gives each
+// value its alphabet rank.
+struct TokTask {
+    const uint8_t* src;   // n elements of width w
+    uint64_t n;
+    uint32_t w;
+    uint32_t iw;          // index width (1, 2 or 4), known after counting
+    uint64_t capMask;     // table capacity - 1 (a power of two)
+    uint32_t* state;      // 0 empty, 1 being written, 2 ready
+    uint64_t* key;
+    uint32_t* first;      // first element index of the slot's value
+    uint32_t* slotOf;     // per element: the slot of its value
+    uint32_t* rank;       // per element: marks, then exclusive rank of the marks
+    uint8_t* alphabet;    // distinct values, width w
+    uint8_t* idx;         // per element: alphabet index, width iw
+    uint32_t tileBase;    // first tile of this task in its launch
+};
+
 constexpr uint32_t kEncTile = 4096; // elements per numeric/pack tile (32 per thread)
 
 } // namespace ozl

@@ -349,6 +349,190 @@ __global__ void kPut(const PutTask* __restrict__ tasks, uint32_t n)
 }
 
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// bf16 deconstruct: 4096 elements per tile
+__global__ void __launch_bounds__(256) kBf16(const Bf16Task* __restrict__ tasks, const TileRef* __restrict__ tiles)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    Bf16Task const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kEncTile;
+    uint64_t const e1 = e0 + kEncTile < t.n ? e0 + kEncTile : t.n;
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+        uint32_t const x = uint32_t(t.src[2 * i]) | (uint32_t(t.src[2 * i + 1]) << 8);
+        t.signFrac[i] = uint8_t(((x >> 15) & 1) | ((x & 0x7f) << 1));
+        t.exponent[i] = uint8_t(x >> 7);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// tokenize: open-addressing table of distinct values with their first index
+__device__ __forceinline__ uint64_t tokHash(uint64_t k)
+{
+    // splitmix64 finalizer
+    k ^= k >> 30;
+    k *= 0xbf58476d1ce4e5b9ull;
+    k ^= k >> 27;
+    k *= 0x94d049bb133111ebull;
+    return k ^ (k >> 31);
+}
+
+__global__ void __launch_bounds__(256) kTokInsert(const TokTask* __restrict__ tasks, const TileRef* __restrict__ tiles,
+                                                  uint32_t* __restrict__ errors)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    TokTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kEncTile;
+    uint64_t const e1 = e0 + kEncTile < t.n ? e0 + kEncTile : t.n;
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+        uint64_t const k = ldW(t.src + i * t.w, t.w);
+        uint64_t h = tokHash(k) & t.capMask;
+        bool placed = false;
+        for (uint64_t probe = 0; probe <= t.capMask && !placed; probe++) {
+            volatile uint32_t* const st = t.state + h;
+            uint32_t s = *st;
+            if (s == 0) {
+                if (atomicCAS(t.state + h, 0u, 1u) == 0u) {
+                    t.key[h] = k;
+                    __threadfence();
+                    atomicExch(t.state + h, 2u);
+                    atomicMin(t.first + h, uint32_t(i));
+                    placed = true;
+                    break;
+                }
+                s = *st;
+            }
+            // another element is writing this slot: wait (bounded) for its key
+            uint32_t spins = 0;
+            while (s == 1 && spins < (1u << 22)) {
+                s = *st;
+                spins++;
+            }
+            if (s != 2) break;
+            __threadfence();
+            if (*reinterpret_cast<volatile uint64_t*>(t.key + h) == k) {
+                atomicMin(t.first + h, uint32_t(i));
+                placed = true;
+                break;
+            }
+            h = (h + 1) & t.capMask;
+        }
+        if (!placed) atomicAdd(errors, 1u);
+    }
+}
+
+// Marks first occurrences (rank[i] = 1) and records each element's slot;
+// per-tile mark counts go to tileSums.
+__global__ void __launch_bounds__(256) kTokMark(const TokTask* __restrict__ tasks, const TileRef* __restrict__ tiles,
+                                                uint64_t* __restrict__ tileSums, uint32_t* __restrict__ errors)
+{
+    __shared__ uint32_t warpCnt[8];
+    TileRef const tr = tiles[blockIdx.x];
+    TokTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kEncTile;
+    uint64_t const e1 = e0 + kEncTile < t.n ? e0 + kEncTile : t.n;
+    uint32_t cnt = 0;
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+        uint64_t const k = ldW(t.src + i * t.w, t.w);
+        uint64_t h = tokHash(k) & t.capMask;
+        uint64_t probe = 0;
+        while (probe <= t.capMask && !(t.state[h] == 2 && t.key[h] == k)) {
+            h = (h + 1) & t.capMask;
+            probe++;
+        }
+        if (probe > t.capMask) {
+            atomicAdd(errors, 1u);
+            t.slotOf[i] = 0;
+            t.rank[i] = 0;
+            continue;
+        }
+        t.slotOf[i] = uint32_t(h);
+        uint32_t const m = t.first[h] == uint32_t(i) ? 1u : 0u;
+        t.rank[i] = m;
+        cnt += m;
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) warpCnt[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t tot = 0;
+        for (int w = 0; w < 8; w++) tot += warpCnt[w];
+        tileSums[blockIdx.x] = tot;
+    }
+}
+
+// one warp per task: exclusive scan of its tiles' mark counts; the total is
+// the alphabet size
+__global__ void __launch_bounds__(256) kTokPrefix(const TokTask* __restrict__ tasks, uint32_t nbTasks,
+                                                  const uint64_t* __restrict__ tileSums,
+                                                  uint64_t* __restrict__ tilePrefix, uint32_t* __restrict__ counts)
+{
+    uint32_t const ti = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t const lane = threadIdx.x & 31;
+    if (ti >= nbTasks) return;
+    TokTask const t = tasks[ti];
+    uint32_t const nT = uint32_t((t.n + kEncTile - 1) / kEncTile);
+    uint64_t running = 0;
+    for (uint32_t k0 = 0; k0 < nT; k0 += 32) {
+        uint32_t const k = k0 + lane;
+        uint64_t const x = k < nT ? tileSums[t.tileBase + k] : 0;
+        uint64_t incl = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t const y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= uint32_t(o)) incl += y;
+        }
+        if (k < nT) tilePrefix[t.tileBase + k] = running + incl - x;
+        running += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) counts[ti] = uint32_t(running);
+}
+
+// marks -> exclusive ranks, 16 consecutive elements per thread
+__global__ void __launch_bounds__(256) kTokRank(const TokTask* __restrict__ tasks, const TileRef* __restrict__ tiles,
+                                                const uint64_t* __restrict__ tilePrefix)
+{
+    __shared__ uint32_t warpTot[8];
+    TileRef const tr = tiles[blockIdx.x];
+    TokTask const t = tasks[tr.task];
+    uint32_t const tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint64_t const base = uint64_t(tr.tile) * kEncTile + uint64_t(tid) * 16;
+    uint32_t v[16];
+    uint32_t acc = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        uint32_t const m = base + k < t.n ? t.rank[base + k] : 0u;
+        v[k] = acc;
+        acc += m;
+    }
+    uint32_t incl = acc;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t const y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= uint32_t(o)) incl += y;
+    }
+    if (lane == 31) warpTot[wid] = incl;
+    __syncthreads();
+    uint32_t pre = 0;
+    for (uint32_t w = 0; w < wid; w++) pre += warpTot[w];
+    uint32_t const add = uint32_t(tilePrefix[blockIdx.x]) + pre + (incl - acc);
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+        if (base + k < t.n) t.rank[base + k] = v[k] + add;
+}
+
+// indices and alphabet
+__global__ void __launch_bounds__(256) kTokEmit(const TokTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    TokTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kEncTile;
+    uint64_t const e1 = e0 + kEncTile < t.n ? e0 + kEncTile : t.n;
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+        uint32_t const f = t.first[t.slotOf[i]];
+        uint32_t const r = t.rank[f];
+        stW(t.idx + i * t.iw, r, t.iw);
+        if (f == uint32_t(i)) stW(t.alphabet + uint64_t(r) * t.w, ldW(t.src + i * t.w, t.w), t.w);
+    }
+}
+
 cudaError_t prepareEncodeKernels()
 {
     return cudaFuncSetAttribute(kFseEnc, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -385,6 +569,27 @@ void launchHufEnc(const HufEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t
 void launchPut(const PutTask* t, uint32_t n, cudaStream_t s)
 {
     if (n) kPut<<<(n + 127) / 128, 128, 0, s>>>(t, n);
+}
+
+
+void launchBf16(const Bf16Task* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s)
+{
+    if (nbTiles) kBf16<<<nbTiles, 256, 0, s>>>(t, tiles);
+}
+
+void launchTokCount(const TokTask* t, uint32_t nbTasks, const TileRef* tiles, uint32_t nbTiles, uint64_t* tileSums,
+                    uint64_t* tilePrefix, uint32_t* counts, uint32_t* errors, cudaStream_t s)
+{
+    if (!nbTiles) return;
+    kTokInsert<<<nbTiles, 256, 0, s>>>(t, tiles, errors);
+    kTokMark<<<nbTiles, 256, 0, s>>>(t, tiles, tileSums, errors);
+    kTokPrefix<<<(nbTasks * 32 + 255) / 256, 256, 0, s>>>(t, nbTasks, tileSums, tilePrefix, counts);
+    kTokRank<<<nbTiles, 256, 0, s>>>(t, tiles, tilePrefix);
+}
+
+void launchTokEmit(const TokTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s)
+{
+    if (nbTiles) kTokEmit<<<nbTiles, 256, 0, s>>>(t, tiles);
 }
 
 } // namespace ozl

@@ -31,6 +31,15 @@ def _cases(seed):
         for n in (2, 9, 10, 999, 1001, 5000, 100000, 200000):
             for k in (2, 3, 37, 256):
                 c.append((recipe, (rng.zipf(1.2, n) % k).astype(np.uint8), 0))
+    keys = rng.integers(0, 2**31, 10000).astype(np.int32)
+    for n in (3, 700, 20000, 300000):
+        idx = (rng.zipf(1.1, n) - 1) % keys.size
+        c.append((5, keys[idx].astype(np.uint32), 4))
+    c.append((5, (rng.integers(0, 200, 50000)).astype(np.uint16), 2))
+    c.append((5, (rng.integers(0, 2**40, 3000)).astype(np.uint64), 8))
+    for n in (4, 900, 70000):
+        bf = (rng.normal(0, 0.02, n).astype(np.float32).view(np.uint32) >> 16).astype(np.uint16)
+        c.append((6, bf, 2))
     c.append((13, np.full(4000, 9, np.uint8), 0))
     c.append((14, rng.integers(0, 37, 3000).astype(np.uint8), 0))
     c.append((15, rng.integers(0, 37, 3000).astype(np.uint8), 0))
