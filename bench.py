@@ -61,6 +61,7 @@ def parse_args():
     p.add_argument("--no-plain", action="store_true", help="skip the per-frame plain path")
     p.add_argument("--no-serve", action="store_true", help="skip the serving-loop run")
     p.add_argument("--no-single", action="store_true", help="skip the single 256 MiB array run")
+    p.add_argument("--no-columnar", action="store_true", help="skip the columnar/bf16 round trip")
     p.add_argument("--serve-rates", default="1000,5000,20000,50000", help="request rates (req/s) for the serving run")
     p.add_argument("--serve-seconds", type=float, default=1.0, help="seconds of arrivals per rate")
     return p.parse_args()
@@ -324,6 +325,72 @@ def run_single_array(oz, torch, dev, sptr, seed):
     return {"workload": "timestamps_int64_256mib", "graph": "delta->zigzag->bitpack->Huffman",
             "decoded_bytes": int(a.nbytes), "compressed_bytes": int(fs), "ratio": round(a.nbytes / fs, 3),
             "plain_gbs": round(a.nbytes / dt / 1e9, 2), "ms": round(dt * 1e3, 3)}
+
+
+# ---------------------------------------------------------------------------
+# columnar and weight-like data: a 64M-row int32 column (Zipf 1.1 over 10,000
+# random keys) through tokenize -> {alphabet: store, indices: bitpack ->
+# Huffman}, and 2 GiB of bf16 matrices (4096x4096, 4096x11008, 11008x4096,
+# N(0, 0.02)) through bf16 deconstruct -> {sign|fraction: store, exponent:
+# FSE}; all frames encoded in one batched call and decoded in one batched
+# graph launch, checked bit-exact
+
+
+RECIPE_TOKENIZE = 5
+RECIPE_BF16 = 6
+
+
+def run_columnar(oz, torch, dev, sptr, seed):
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed + 41)
+    rows = 64 << 20
+    keys = torch.randint(0, 2**31 - 1, (10000,), device=dev, generator=g, dtype=torch.int64).to(torch.int32)
+    p = 1.0 / torch.arange(1, 10001, device=dev, dtype=torch.float64) ** 1.1
+    cdf = torch.cumsum(p / p.sum(), 0)
+    u = torch.rand(rows, device=dev, generator=g, dtype=torch.float64)
+    col = keys[torch.searchsorted(cdf, u).clamp_(max=9999)].contiguous()
+    shapes = [(4096, 4096), (4096, 11008), (11008, 4096)] * 10
+    mats = [(torch.randn(r, c, device=dev, generator=g) * 0.02).to(torch.bfloat16).contiguous() for r, c in shapes]
+    srcs = [col] + mats
+    nbytes = [t.numel() * t.element_size() for t in srcs]
+    elts = [t.numel() for t in srcs]
+    widths = [4] + [2] * len(mats)
+    recipes = [RECIPE_TOKENIZE] + [RECIPE_BF16] * len(mats)
+    enc = oz.GpuEncoder()
+    caps = [enc.bound(b) for b in nbytes]
+    offs, tot = layout(caps, OUT_ALIGN)
+    d_fr = torch.empty(tot, dtype=torch.uint8, device=dev)
+    fptr = [d_fr.data_ptr() + o for o in offs]
+    enc.compress_batch([t.data_ptr() for t in srcs], elts, widths, recipes, fptr, caps, checksums=True, stream=sptr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fs = enc.compress_batch([t.data_ptr() for t in srcs], elts, widths, recipes, fptr, caps, checksums=True,
+                            stream=sptr)
+    torch.cuda.synchronize()
+    enc_s = time.perf_counter() - t0
+    frames_h = [d_fr[o:o + f].cpu().numpy() for o, f in zip(offs, fs)]
+    ooffs, obytes = layout(nbytes, OUT_ALIGN)
+    d_out = torch.zeros(obytes, dtype=torch.uint8, device=dev)
+    batch = oz.GpuBatch()
+    batch.plan(frames_h, fptr, [d_out.data_ptr() + o for o in ooffs], nbytes)
+    for _ in range(3):
+        batch.run(sptr, graph=True)
+    batch.check(sptr)
+    reps = 10
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        batch.run(sptr, graph=True)
+    batch.check(sptr)
+    dec_s = (time.perf_counter() - t0) / reps
+    ok = all(torch.equal(d_out[o:o + n], t.view(torch.uint8).reshape(-1)) for o, n, t in zip(ooffs, nbytes, srcs))
+    if not ok:
+        raise RuntimeError("columnar round trip differs")
+    total = sum(nbytes)
+    return {"column_rows": rows, "column_ratio": round(nbytes[0] / fs[0], 3), "bf16_bytes": sum(nbytes[1:]),
+            "bf16_ratio": round(sum(nbytes[1:]) / sum(fs[1:]), 3), "frames": len(srcs),
+            "encode_gbs": round(total / enc_s / 1e9, 2), "decode_gbs": round(total / dec_s / 1e9, 2),
+            "bit_exact": True}
 
 
 # ---------------------------------------------------------------------------
@@ -710,6 +777,9 @@ def main():
         single = run_single_array(oz, torch, dev, sptr, args.seed)
     if rank == 0 and ws == 1 and not args.no_serve:
         serving = run_serving(oz, torch, dev, sptr, args)
+    columnar = None
+    if rank == 0 and ws == 1 and not args.no_columnar:
+        columnar = run_columnar(oz, torch, dev, sptr, args.seed)
 
     # ---- CPU baseline (rank 0, N=1 only): the same frames on the host cores
     cpu = None
@@ -748,6 +818,7 @@ def main():
         "plain": plain,
         "single_array": single,
         "serving": serving,
+        "columnar": columnar,
         "encode": {"value": round(enc_gbs, 3), "unit": "GB/s", "note": "batched compress, host decisions included"},
         "roofline": roofline,
         "cpu_baseline": cpu,
