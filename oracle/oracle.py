@@ -36,6 +36,14 @@ def lib():
                                    ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
         l.ozo_compress_bound.restype = ctypes.c_size_t
         l.ozo_compress_bound.argtypes = [ctypes.c_size_t]
+        l.ozo_decode_transform.restype = ctypes.c_int64
+        l.ozo_decode_transform.argtypes = [ctypes.c_uint, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
+        l.ozo_tokenize.restype = ctypes.c_int64
+        l.ozo_tokenize.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         l.ozo_xxh3_64.restype = ctypes.c_uint64
         l.ozo_xxh3_64.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
         _lib = l
@@ -71,3 +79,38 @@ def compress(recipe, arr, elt_width, checksums=True):
 def xxh3_64(buf):
     b = np.frombuffer(bytes(buf), np.uint8)
     return lib().ozo_xxh3_64(b.ctypes.data, b.size)
+
+
+TYPE_SERIAL, TYPE_STRUCT, TYPE_NUMERIC = 1, 2, 4
+
+
+def decode_transform(trid, header, inputs, out_cap=1 << 20):
+    """One decoder on explicit streams: inputs = [(type, width, bytes)] in the
+    decoder's order. Returns (output bytes, type, width, count)."""
+    n = len(inputs)
+    bufs = [np.frombuffer(bytes(b), np.uint8).copy() if len(b) else np.zeros(1, np.uint8) for _, _, b in inputs]
+    types = (ctypes.c_int * max(n, 1))(*[t for t, _, _ in inputs])
+    widths = (ctypes.c_size_t * max(n, 1))(*[w for _, w, _ in inputs])
+    counts = (ctypes.c_size_t * max(n, 1))(*[len(b) // w for _, w, b in inputs])
+    ptrs = (ctypes.c_void_p * max(n, 1))(*[b.ctypes.data for b in bufs])
+    h = np.frombuffer(bytes(header), np.uint8).copy() if header else np.zeros(1, np.uint8)
+    out = np.empty(out_cap, np.uint8)
+    t, w, c = ctypes.c_int(), ctypes.c_size_t(), ctypes.c_size_t()
+    r = lib().ozo_decode_transform(trid, h.ctypes.data, len(header), n, types, widths, counts, ptrs, out.ctypes.data,
+                                   out_cap, ctypes.byref(t), ctypes.byref(w), ctypes.byref(c))
+    if r < 0:
+        raise ValueError("oracle: decoder failed (%d)" % r)
+    return out[:r].copy(), t.value, w.value, c.value
+
+
+def tokenize(arr, sorted_alphabet=False):
+    """The tokenize node alone: (alphabet array, indices array)."""
+    a = np.ascontiguousarray(arr)
+    alpha = np.empty(max(a.size, 1), a.dtype)
+    idx = np.empty(max(a.size, 1) * 4, np.uint8)
+    iw = ctypes.c_int()
+    na = lib().ozo_tokenize(a.ctypes.data, a.size, a.itemsize, 1 if sorted_alphabet else 0, alpha.ctypes.data,
+                            idx.ctypes.data, ctypes.byref(iw))
+    dt = {1: np.uint8, 2: np.uint16, 4: np.uint32}[iw.value]
+    return alpha[:na].copy(), idx[: a.size * iw.value].view(dt).copy()
+

@@ -49,6 +49,14 @@ int64_t ozo_compress(int recipe, const void* src, size_t nbElts, int eltWidth,
 
 size_t ozo_compress_bound(size_t srcSize);
 
+/* Test entry points (known-answer vectors): one decoder on caller streams
+ * (inputs in the decoder's order; returns output bytes), and the tokenize
+ * node alone (returns the alphabet size). */
+int64_t ozo_decode_transform(unsigned id, const uint8_t* hdr, size_t hsz, size_t nbIn, const int* types,
+                             const size_t* widths, const size_t* counts, const uint8_t* const* data, void* out,
+                             size_t outCap, int* outType, size_t* outW, size_t* outN);
+int64_t ozo_tokenize(const void* src, size_t n, int w, int sorted, void* alphaOut, void* idxOut, int* iwOut);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1043,3 +1043,33 @@ int64_t ozo_decompress(const void* srcv, size_t size, void* dst, size_t dstCap, 
     if (outEltWidth) *outEltWidth = (int)(ws[0] ? ws[0] : 1);
     return (int64_t)lens[0];
 }
+
+/* Test entry point: runs one decoder on caller streams (codec-level known
+ * answers). Inputs are given in the decoder's own order. */
+int64_t ozo_decode_transform(unsigned id, const uint8_t* hdr, size_t hsz, size_t nbIn, const int* types,
+                             const size_t* widths, const size_t* counts, const uint8_t* const* data, void* out,
+                             size_t outCap, int* outType, size_t* outW, size_t* outN)
+{
+    OStream ins[16];
+    OStream* pin[16];
+    if (nbIn > 16) return -OZO_ERR_UNSUPPORTED;
+    for (size_t i = 0; i < nbIn; i++) {
+        memset(&ins[i], 0, sizeof(ins[i]));
+        ost_ref(&ins[i], types[i], widths[i], counts[i], data[i]);
+        pin[i] = &ins[i];
+    }
+    OStream o;
+    memset(&o, 0, sizeof(o));
+    int rc = dec_run(id, pin, nbIn, hdr, hsz, &o);
+    if (rc < 0) return rc;
+    size_t const bytes = o.n * o.w;
+    int64_t ret = (int64_t)bytes;
+    if (bytes > outCap) ret = -OZO_ERR_DST_SIZE;
+    else if (bytes) memcpy(out, o.p, bytes);
+    if (outType) *outType = o.type;
+    if (outW) *outW = o.w;
+    if (outN) *outN = o.n;
+    ost_free(&o);
+    return ret;
+}
+

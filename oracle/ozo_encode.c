@@ -1369,3 +1369,23 @@ int64_t ozo_compress(int recipe, const void* src, size_t nbElts, int eltWidth, v
     free(c.nd);
     return ret;
 }
+
+/* Test entry point: the tokenize node alone (encoder known answers):
+ * alphabet (na values of width w) and indices (n of width *iw). */
+int64_t ozo_tokenize(const void* src, size_t n, int w, int sorted, void* alphaOut, void* idxOut, int* iwOut)
+{
+    ECtx ctx;
+    ECtx* const c = &ctx;
+    memset(c, 0, sizeof(*c));
+    int in = new_stream(c, OZO_TYPE_NUMERIC, (size_t)w, n, (const uint8_t*)src);
+    int a = node_tokenize(c, in, sorted);
+    size_t const na = S(a)->n;
+    memcpy(alphaOut, S(a)->data, na * (size_t)w);
+    memcpy(idxOut, S(a + 1)->data, n * S(a + 1)->w);
+    *iwOut = (int)S(a + 1)->w;
+    for (size_t i = 0; i < c->ns; i++) free(c->s[i].data);
+    free(c->s);
+    free(c->nd);
+    return (int64_t)na;
+}
+
