@@ -664,6 +664,12 @@ def main():
                          [d_out.data_ptr() + o for o in ooffs], osizes)
     assert planned == total_out, (planned, total_out)
 
+    # autotuner: launch shapes (chunks per CTA of the FSE and Huffman launches)
+    prof0 = sum(ms for _, ms, _ in batch.profile(sptr, capacity=256))
+    shapes = batch.autotune(sptr, reps=2)
+    prof1 = sum(ms for _, ms, _ in batch.profile(sptr, capacity=256))
+    tuned = {"shapes": shapes, "profile_ms_before": round(prof0, 3), "profile_ms_after": round(prof1, 3)}
+
     # warm-up (graph capture happens on the first run)
     for _ in range(args.warmup):
         batch.run(sptr, graph=True)
@@ -820,6 +826,7 @@ def main():
         "serving": serving,
         "columnar": columnar,
         "encode": {"value": round(enc_gbs, 3), "unit": "GB/s", "note": "batched compress, host decisions included"},
+        "autotune": tuned,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,

@@ -294,6 +294,13 @@ ZL_Report ozl_gpu_batch_profile(OZL_GpuBatch* b, void* stream, float* ms, int* k
                                 uint64_t* bytes, size_t capacity);
 /* Name of a codec family reported by ozl_gpu_batch_profile. */
 const char* ozl_gpu_kind_name(int kind);
+/* Autotuner: times the candidate launch shapes (chunks per CTA of the FSE
+ * and Huffman launches) of the planned batch on `stream`, best of `reps`,
+ * after one full run; keeps the fastest per launch for the following runs
+ * (the next graph run recaptures). Writes the chosen shape of launch i to
+ * shapes[i] (0 = not tunable) for i < capacity. Returns the number of
+ * planned launches. Results do not depend on the shapes. */
+ZL_Report ozl_gpu_batch_autotune(OZL_GpuBatch* b, void* stream, int reps, uint32_t* shapes, size_t capacity);
 /* Host-buffer run of a planned batch whose device frames sit back to back
  * from d_frames[0] and whose outputs sit back to back from d_dsts[0] (as
  * passed to ozl_gpu_batch_plan): copies h_in (inBytes) to the device, runs

@@ -71,6 +71,7 @@ def library():
         "ozl_gpu_batch_profile": ([vp, vp, vp, vp, vp, sz], ZLReport),
         "ozl_gpu_kind_name": ([ctypes.c_int], ctypes.c_char_p),
         "ozl_gpu_batch_run_host": ([vp, vp, sz, vp, sz, vp, ctypes.c_int], ZLReport),
+        "ozl_gpu_batch_autotune": ([vp, vp, ctypes.c_int, vp, sz], ZLReport),
         "ozl_gpu_encoder_create": ([], vp),
         "ozl_gpu_encoder_free": ([vp], None),
         "ozl_gpu_compress_bound": ([sz], sz),
@@ -301,6 +302,15 @@ class GpuBatch:
         if rep.code:
             self._raise(rep)
         return rep.value
+
+    def autotune(self, stream=0, reps=2, capacity=256):
+        """Picks the launch shapes (chunks per CTA) by timing; returns the
+        chosen shape per launch (0 = not tunable)."""
+        shapes = (ctypes.c_uint32 * capacity)()
+        rep = self._lib.ozl_gpu_batch_autotune(self._h, stream, reps, shapes, capacity)
+        if rep.code:
+            self._raise(rep)
+        return list(shapes)[: min(rep.value, capacity)]
 
     def launches(self):
         return self._lib.ozl_gpu_batch_launches(self._h)

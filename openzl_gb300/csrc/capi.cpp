@@ -371,6 +371,15 @@ ZL_Report ozl_gpu_batch_profile(OZL_GpuBatch* b, void* stream, float* ms, int* k
     return ok(n);
 }
 
+ZL_Report ozl_gpu_batch_autotune(OZL_GpuBatch* b, void* stream, int reps, uint32_t* shapes, size_t capacity)
+{
+    if (!b || b->dFrames.empty()) return fail(ZL_ErrorCode_parameter_invalid);
+    ZL_Report r = b->autotune(static_cast<cudaStream_t>(stream), reps < 1 ? 1 : reps);
+    if (ZL_isError(r)) return r;
+    for (size_t i = 0; shapes && i < capacity && i < b->layout.launches.size(); i++) shapes[i] = b->layout.launches[i].tune;
+    return ok(b->layout.launches.size());
+}
+
 ZL_Report ozl_gpu_batch_run_host(OZL_GpuBatch* b, const void* h_in, size_t inBytes, void* h_out, size_t outBytes,
                                  void* stream, int useGraph)
 {

@@ -16,6 +16,8 @@ long runLaunches(const DeviceLayout& layout, uint8_t* dPool, uint8_t* dScratch, 
 // Applies the shared-memory carve-out attributes the entropy kernels need.
 // Call once per device before the first launch (and before graph capture).
 cudaError_t prepareKernels();
+// Launch shapes the autotuner may try for a launch (chunks per CTA); 0 if none.
+uint32_t tuneCandidates(const Launch& l, uint32_t* out, uint32_t cap);
 
 // Enqueues launch `i` of `layout` alone (the building block of runLaunches).
 // Returns the number of kernels it issued, or a negative value on failure.

@@ -35,6 +35,7 @@ struct Launch {
     size_t statusBytes;
     bool needsScan;
     uint32_t param0;  // kind-specific launch shape (FSE: max table log)
+    uint32_t tune;    // chunks per CTA chosen by the autotuner (FSE, Huffman); 0 = default
     uint64_t algoBytes; // bytes the launch must read plus write (roofline numerator)
 };
 

@@ -159,6 +159,51 @@ struct DecodeBatch {
         return reportOk(0);
     }
 
+    // Times every candidate launch shape of the tunable launches (one launch
+    // at a time, CUDA events on `s`, best of `reps`) after one full run that
+    // produces every launch's inputs, keeps the fastest per launch and drops
+    // the captured graph. Returns the number of launches tuned.
+    ZL_Report autotune(cudaStream_t s, int reps)
+    {
+        ZL_Report r = upload(s);
+        if (ZL_isError(r)) return r;
+        r = enqueue(s);
+        if (ZL_isError(r)) return r;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
+        size_t tuned = 0;
+        for (size_t li = 0; li < layout.launches.size(); li++) {
+            uint32_t cand[8];
+            uint32_t const nc = tuneCandidates(layout.launches[li], cand, 8);
+            if (nc < 2) continue;
+            float best = 1e30f;
+            uint32_t bestC = 0;
+            for (uint32_t k = 0; k < nc; k++) {
+                layout.launches[li].tune = cand[k];
+                float t = 1e30f;
+                for (int rep = 0; rep < reps; rep++) {
+                    cudaEventRecord(a, s);
+                    if (runOneLaunch(layout, li, pool.data(), scratch.data(), reinterpret_cast<uint32_t*>(status.data()), s) < 0)
+                        break;
+                    cudaEventRecord(b, s);
+                    cudaEventSynchronize(b);
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, a, b);
+                    t = ms < t ? ms : t;
+                }
+                if (t < best) { best = t; bestC = cand[k]; }
+            }
+            layout.launches[li].tune = bestC;
+            tuned++;
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        dropGraph();
+        if (cudaStreamSynchronize(s) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
+        return reportOk(tuned);
+    }
+
     ZL_Report check(cudaStream_t s)
     {
         uint32_t st = 0;

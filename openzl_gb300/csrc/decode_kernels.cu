@@ -864,7 +864,8 @@ __device__ bool hufRank(const uint8_t* weights, uint32_t nbW, uint16_t* first, u
 }
 
 constexpr int kHufRing = 8, kHufAhead = 5; // stream ring: 128 bytes per lane, 80 bytes ahead
-constexpr uint32_t kHufRingOff = kHufChunks * kHufSlotBytes + 512;     // after the slots and the spare ranks
+// rings after the slots and the spare ranks
+__host__ __device__ __forceinline__ uint32_t hufRingOff(uint32_t chunks) { return (chunks * kHufSlotBytes + 512 + 15) & ~15u; }
 
 __device__ __forceinline__ void hufDecodeStream(const HufTask& t, const uint16_t* dt, uint32_t tl, uint32_t sIdx,
                                                 uint32_t* ring, uint32_t* status)
@@ -929,7 +930,7 @@ __device__ __forceinline__ void hufDecodeStream(const HufTask& t, const uint16_t
     if (!br.finished()) reportError(status, DERR_CORRUPTION);
 }
 
-__global__ void __launch_bounds__(32) kHuf(const HufTask* __restrict__ tasks, uint32_t nbTasks,
+__global__ void __launch_bounds__(32) kHuf(const HufTask* __restrict__ tasks, uint32_t nbTasks, uint32_t chunks,
                                            uint32_t* __restrict__ status)
 {
     extern __shared__ __align__(16) uint8_t smemHuf[];
@@ -937,7 +938,7 @@ __global__ void __launch_bounds__(32) kHuf(const HufTask* __restrict__ tasks, ui
     __shared__ uint8_t sOk[kHufChunks];
     uint32_t const c = threadIdx.x >> 2;       // chunk slot in this CTA
     uint32_t const sIdx = threadIdx.x & 3;     // stream within the chunk
-    uint32_t const ti = blockIdx.x * kHufChunks + c;
+    uint32_t const ti = blockIdx.x * chunks + c;
     bool const active = ti < nbTasks;
     uint8_t* const slot = smemHuf + size_t(c) * kHufSlotBytes;
     uint16_t* const first = reinterpret_cast<uint16_t*>(slot + kHufSlotCells * 2); // first cell per symbol
@@ -966,17 +967,17 @@ __global__ void __launch_bounds__(32) kHuf(const HufTask* __restrict__ tasks, ui
         }
     }
     __syncwarp();
-    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemHuf + kHufRingOff) + threadIdx.x * 4 * kHufRing;
+    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemHuf + hufRingOff(chunks)) + threadIdx.x * 4 * kHufRing;
     if (narrow) hufDecodeStream(t, dt, tl, sIdx, ring, status);
     __syncwarp();
     // tableLog 12 (valid, but never emitted by the reference's encoder): one
     // chunk at a time, its table across the first slots, ranks recomputed
     // into the spare area after the slots
-    uint16_t* const wideFirst = reinterpret_cast<uint16_t*>(smemHuf + size_t(kHufChunks) * kHufSlotBytes);
+    uint16_t* const wideFirst = reinterpret_cast<uint16_t*>(smemHuf + size_t(chunks) * kHufSlotBytes);
     uint16_t* const wide = reinterpret_cast<uint16_t*>(smemHuf);
-    for (uint32_t k = 0; k < kHufChunks; k++) {
+    for (uint32_t k = 0; k < chunks; k++) {
         if (!(sOk[k] && sTl[k] > 11)) continue; // warp-uniform
-        HufTask const tk = tasks[blockIdx.x * kHufChunks + k];
+        HufTask const tk = tasks[blockIdx.x * chunks + k];
         if (threadIdx.x == 0) {
             uint32_t tlk = 0;
             hufRank(tk.weights, tk.nbWeights, wideFirst, tlk);
@@ -1296,16 +1297,29 @@ uint32_t fseLanes(uint32_t tlMax)
     while (lanes > 1 && fseSmemBytes(lanes, tlMax) > kFseCtaSmem) lanes--;
     return lanes;
 }
-constexpr uint32_t kHufSmem = kHufRingOff + 32 * 16 * kHufRing;
-static_assert(kHufRingOff % 16 == 0, "ring alignment");
-static_assert(kHufChunks * kHufSlotBytes >= (2u << kHufTableLog), "a tableLog-12 table fits the slots");
+uint32_t hufSmem(uint32_t chunks) { return hufRingOff(chunks) + 4 * chunks * 16 * kHufRing; }
+static_assert(2 * kHufSlotBytes >= (2u << kHufTableLog), "a tableLog-12 table fits two slots");
 } // namespace
 
 cudaError_t prepareKernels()
 {
     cudaError_t e = cudaFuncSetAttribute(kFse, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFseCtaSmem));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(kHuf, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kHufSmem));
+    return cudaFuncSetAttribute(kHuf, cudaFuncAttributeMaxDynamicSharedMemorySize, int(hufSmem(kHufChunks)));
+}
+
+uint32_t tuneCandidates(const Launch& l, uint32_t* out, uint32_t cap)
+{
+    uint32_t n = 0;
+    if (l.kind == KIND_FSE) {
+        uint32_t const mx = fseLanes(l.param0);
+        for (uint32_t c : { 32u, 16u, 8u, 6u, 4u, 2u })
+            if (c <= mx && n < cap) out[n++] = c;
+    } else if (l.kind == KIND_HUF) {
+        for (uint32_t c : { 8u, 6u, 4u, 2u })
+            if (n < cap) out[n++] = c;
+    }
+    return n;
 }
 
 long runLaunches(const DeviceLayout& L, uint8_t* dPool, uint8_t* dScratch, uint32_t* dStatus, cudaStream_t s)
@@ -1335,15 +1349,18 @@ long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dSc
                 kConst<<<l.nbTiles, 256, 0, s>>>(static_cast<const ConstTask*>(tasks), tiles);
                 break;
             case KIND_FSE: {
-                uint32_t const lanes = fseLanes(l.param0);
+                uint32_t const maxLanes = fseLanes(l.param0);
+                uint32_t const lanes = l.tune && l.tune < maxLanes ? l.tune : maxLanes;
                 uint32_t const grid = (l.nbTasks + lanes - 1) / lanes;
                 kFse<<<grid, 32, fseSmemBytes(lanes, l.param0), s>>>(static_cast<const FseTask*>(tasks), l.nbTasks,
                                                                      lanes, l.param0, dStatus);
                 break;
             }
             case KIND_HUF: {
-                uint32_t const grid = (l.nbTasks + kHufChunks - 1) / kHufChunks;
-                kHuf<<<grid, 32, kHufSmem, s>>>(static_cast<const HufTask*>(tasks), l.nbTasks, dStatus);
+                uint32_t const chunks = l.tune && l.tune <= kHufChunks ? l.tune : kHufChunks;
+                uint32_t const grid = (l.nbTasks + chunks - 1) / chunks;
+                kHuf<<<grid, 4 * chunks, hufSmem(chunks), s>>>(static_cast<const HufTask*>(tasks), l.nbTasks, chunks,
+                                                               dStatus);
                 break;
             }
             case KIND_FLATPACK:

@@ -120,3 +120,29 @@ def test_device_api_side_stream_back_to_back(gpu_lib):
     s.synchronize()
     for (a, _), o in zip(cases, outs):
         assert o[: a.nbytes].cpu().numpy().tobytes() == a.tobytes()
+
+
+def test_autotuned_shapes_keep_results(gpu_lib, manifest):
+    """The autotuner changes only launch shapes: the batch decodes the same
+    bytes before and after, through the captured graph."""
+    import torch
+    import openzl_gb300 as oz
+
+    frames = [read_frame(m["case"]) for m in manifest]
+    dfr = [_dev(torch, f) for f in frames]
+    sizes = [oz.get_decompressed_size(f) for f in frames]
+    outs = [torch.zeros(max(n, 1) + 64, dtype=torch.uint8, device="cuda") for n in sizes]
+    s = torch.cuda.Stream()
+    b = oz.GpuBatch()
+    b.plan(frames, [d.data_ptr() for d in dfr], [o.data_ptr() for o in outs], sizes)
+    torch.cuda.synchronize()
+    shapes = b.autotune(s.cuda_stream, reps=1)
+    assert len(shapes) > 0 and any(x > 0 for x in shapes)
+    for o in outs:
+        o.zero_()
+    torch.cuda.synchronize()
+    b.run(s.cuda_stream, graph=True)
+    b.check(s.cuda_stream)
+    for m, n, o in zip(manifest, sizes, outs):
+        h = hashlib.sha256(o[:n].cpu().numpy().tobytes()).hexdigest()
+        assert h == m["sha256_in"], m["case"]
