@@ -347,14 +347,16 @@ ZL_Report ozl_gpu_batch_profile(OZL_GpuBatch* b, void* stream, float* ms, int* k
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ZL_Report const u = b->upload(s);
     if (ZL_isError(u)) return u;
-    size_t const n = b->layout.launches.size();
+    size_t const n = b->nbLaunches();
     std::vector<cudaEvent_t> ev(n + 1);
     for (auto& e : ev)
         if (cudaEventCreate(&e) != cudaSuccess) return fail(ZL_ErrorCode_GENERIC);
     bool okRun = cudaMemsetAsync(b->status.data(), 0, 4, s) == cudaSuccess;
     cudaEventRecord(ev[0], s);
     for (size_t i = 0; i < n && okRun; i++) {
-        okRun = ozl::runOneLaunch(b->layout, i, b->pool.data(), b->scratch.data(),
+        size_t p = 0, li = 0;
+        b->locate(i, p, li);
+        okRun = ozl::runOneLaunch(b->parts[p].layout, li, b->parts[p].pool.data(), b->parts[p].scratch.data(),
                                   reinterpret_cast<uint32_t*>(b->status.data()), s) >= 0;
         cudaEventRecord(ev[i + 1], s);
     }
@@ -362,9 +364,11 @@ ZL_Report ozl_gpu_batch_profile(OZL_GpuBatch* b, void* stream, float* ms, int* k
     for (size_t i = 0; i < n && i < capacity && okRun; i++) {
         float t = 0;
         cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+        size_t p = 0, li = 0;
+        b->locate(i, p, li);
         if (ms) ms[i] = t;
-        if (kinds) kinds[i] = b->layout.launches[i].kind;
-        if (bytes) bytes[i] = b->layout.launches[i].algoBytes;
+        if (kinds) kinds[i] = b->parts[p].layout.launches[li].kind;
+        if (bytes) bytes[i] = b->parts[p].layout.launches[li].algoBytes;
     }
     for (auto& e : ev) cudaEventDestroy(e);
     if (!okRun) return fail(ZL_ErrorCode_GENERIC);
@@ -376,8 +380,12 @@ ZL_Report ozl_gpu_batch_autotune(OZL_GpuBatch* b, void* stream, int reps, uint32
     if (!b || b->dFrames.empty()) return fail(ZL_ErrorCode_parameter_invalid);
     ZL_Report r = b->autotune(static_cast<cudaStream_t>(stream), reps < 1 ? 1 : reps);
     if (ZL_isError(r)) return r;
-    for (size_t i = 0; shapes && i < capacity && i < b->layout.launches.size(); i++) shapes[i] = b->layout.launches[i].tune;
-    return ok(b->layout.launches.size());
+    for (size_t i = 0; shapes && i < capacity && i < b->nbLaunches(); i++) {
+        size_t p = 0, li = 0;
+        b->locate(i, p, li);
+        shapes[i] = b->parts[p].layout.launches[li].tune;
+    }
+    return ok(b->nbLaunches());
 }
 
 ZL_Report ozl_gpu_batch_run_host(OZL_GpuBatch* b, const void* h_in, size_t inBytes, void* h_out, size_t outBytes,

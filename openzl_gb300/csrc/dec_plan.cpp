@@ -830,8 +830,9 @@ uint64_t taskBytes(const NumPipeTask& t)
 
 int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* const* dOuts,
                uint8_t* dArena, uint8_t* dParams, uint8_t* dScratch, uint8_t* dPool,
-               DeviceLayout& out, std::string& err)
+               DeviceLayout& out, std::string& err, const std::vector<char>* frameMask)
 {
+    auto inPart = [&](int frame) { return !frameMask || (frame >= 0 && (*frameMask)[size_t(frame)]); };
     const auto& streams = plan.streams;
     const auto& nodes = plan.nodes;
     std::vector<uint8_t*> addrMemo(streams.size(), nullptr);
@@ -858,7 +859,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
 
     // every input of a live decoder must have a location by now
     for (const PlanNode& nd : nodes) {
-        if (nd.dead) continue;
+        if (nd.dead || !inPart(nd.frame)) continue;
         for (int s : nd.ins)
             if (streams[s].loc == L_NONE) {
                 err = "planner: stream without a location (codec " + std::to_string(nd.id) + ")";
@@ -872,7 +873,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         int p = streams[s].producer;
         return (p >= 0 && !nodes[p].dead) ? level[p] : 0;
     };
-    struct CopyReq { int src, dst; uint64_t dstOff; int level; };
+    struct CopyReq { int src, dst; uint64_t dstOff; int level; int frame; };
     std::vector<CopyReq> copies;
     int maxLevel = 0;
     for (size_t u = 0; u < nodes.size(); u++) {
@@ -889,7 +890,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
                 lv = streamLevel(I);
             } else {
                 lv = streamLevel(I) + 1;
-                copies.push_back(CopyReq{ I, nd.out, 0, lv });
+                copies.push_back(CopyReq{ I, nd.out, 0, lv, nd.frame });
             }
         } else if (isConcat) {
             uint64_t off = 0;
@@ -899,7 +900,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
                     lv = std::max(lv, streamLevel(I));
                 } else {
                     int const cl = streamLevel(I) + 1;
-                    copies.push_back(CopyReq{ I, nd.out, off, cl });
+                    copies.push_back(CopyReq{ I, nd.out, off, cl, nd.frame });
                     lv = std::max(lv, cl);
                 }
                 off += IS.bytes();
@@ -917,12 +918,14 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
     // ---- tasks per level ---------------------------------------------------
     std::vector<Buckets> B(size_t(hashLevel) + 1);
     for (const CopyReq& c : copies) {
+        if (!inPart(c.frame)) continue;
         uint64_t bytes = streams[c.src].bytes();
         if (!bytes) continue;
         CopyTask t{ addr(c.dst) + c.dstOff, addr(c.src), bytes, 0 };
         B[c.level].copy.push_back(t);
     }
     for (const PlanCopy& c : plan.directCopies) {
+        if (!inPart(c.frame)) continue;
         CopyTask t{ dOuts[c.frame] + c.outOff, dFrames[c.frame] + c.frameOff, c.bytes, 0 };
         B[1].copy.push_back(t);
     }
@@ -933,7 +936,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
     std::vector<PendingPlanes> pend;
     for (size_t u = 0; u < nodes.size(); u++) {
         const PlanNode& nd = nodes[u];
-        if (nd.dead) continue;
+        if (nd.dead || !inPart(nd.frame)) continue;
         int const lv = level[u];
         const PlanStream& O = streams[nd.out];
         uint8_t* o = addr(nd.out);
@@ -1110,10 +1113,13 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         addTiled(KIND_NUMPIPE, lv, b.num, [](const NumPipeTask& t) { return ceilDiv(t.n, kTileElems); });
     }
     // checksums: one launch after everything else
-    if (!plan.hashes.empty()) {
+    bool anyHash = false;
+    for (const PlanHash& h : plan.hashes) anyHash |= inPart(h.frame);
+    if (anyHash) {
         std::vector<HashTask> ht;
         std::vector<TileRef> blocks;
         for (const PlanHash& h : plan.hashes) {
+            if (!inPart(h.frame)) continue;
             HashTask t{};
             t.data = h.inOutput ? dOuts[h.frame] + h.off : dFrames[h.frame] + h.off;
             t.len = h.len;

@@ -125,8 +125,10 @@ struct DeviceLayout {
 };
 
 // Produces task descriptors with absolute device addresses.
+// With `frameMask`, only the work of the frames it marks is laid out (the
+// plan's arena and parameter placements are shared by all such parts).
 int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* const* dOuts,
                uint8_t* dArena, uint8_t* dParams, uint8_t* dScratch, uint8_t* dPool,
-               DeviceLayout& out, std::string& err);
+               DeviceLayout& out, std::string& err, const std::vector<char>* frameMask = nullptr);
 
 } // namespace ozl

@@ -617,65 +617,72 @@ struct BitWin {
     __device__ __forceinline__ bool finished() const { return pos == end; }
 };
 
-// 128-bit window refilled 32 bits at a time (FSE groups). Between groups
-// cb + 64 <= pos <= cb + 96, so the 48 bits below pos lie in the window at
-// shift pos - 48 - cb, between 16 and 48 (no boundary cases in the view).
+// Backward bit reader of the FSE decoder: two stream words in registers, a
+// (bits [cb + 32, cb + 64)) above b (bits [cb, cb + 32)), cb = 32 * kb, and
+// g = cb + 64 - pos. Before each group of fields of at most 32 bits in total
+// g <= 32, so the 32 bits just below pos, most significant first, are one
+// funnel shift of (a, b). A refill takes the next word from the ring without
+// a branch; prepare(), once per two groups, makes the next two words of the
+// ring readable. Words below the stream are never consumed by a valid stream
+// (finished() checks that the stream ends exactly at its first bit), so the
+// ring's stale contents may stand in for them.
 template <int RING, int AHEAD>
-struct BitWin32 {
+struct FseWin {
     StreamRing<RING, AHEAD> r;
-    int32_t pos, end, cb;
-    uint64_t lo, hi;
+    uint32_t a, b;
+    int32_t kb, g, end;
 
     __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size, uint32_t* ring)
     {
+        int32_t pos;
         if (!streamStart(p, size, r.g16, pos, end)) return false;
         r.ring = ring;
         r.start(pos);
         int32_t const jt = (pos - 1) >> 5; // word of the top unread bit
-        cb = (jt - 2) * 32;                // pos - cb in (64, 96]
-        hi = r.word(jt);
-        uint32_t const mid = r.word(jt - 1);
-        lo = uint64_t(r.word(jt - 2)) | (uint64_t(mid) << 32);
+        a = r.word(jt);
+        b = r.word(jt - 1);
+        kb = jt - 1;
+        g = (kb + 2) * 32 - pos; // in [0, 32)
         return true;
     }
-    __device__ __forceinline__ void shift()
+    __device__ __forceinline__ void prepare()
     {
-        hi = (hi << 32) | (lo >> 32);
-        cb -= 32;
-        lo = (lo << 32) | r.word(cb >> 5);
-    }
-    __device__ __forceinline__ void renorm()
-    {
-        if (pos - cb < 64) {
-            shift();
-            if (pos - cb < 64) shift();
+        int32_t const m = (kb - 2) >> 2;
+        if (m < r.low) {
+            r.low = m;
+            r.issue(m - AHEAD);
+            asm volatile("cp.async.wait_group %0;" ::"n"(AHEAD) : "memory");
         }
     }
-    // the 64 bits starting 48 bits below pos
-    __device__ __forceinline__ uint64_t view() const
+    __device__ __forceinline__ uint32_t window() const { return __funnelshift_lc(b, a, uint32_t(g)); }
+    __device__ __forceinline__ void refill()
     {
-        uint32_t const s = uint32_t(pos - 48 - cb); // 16..48
-        return (lo >> s) | (hi << (64 - s));
+        uint32_t const nw = r.ring[(kb - 1) & (4 * RING - 1)];
+        bool const need = g > 32;
+        a = need ? b : a;
+        b = need ? nw : b;
+        kb -= need ? 1 : 0;
+        g -= need ? 32 : 0;
     }
     // one field of nb bits (nb <= 12) just below pos
     __device__ __forceinline__ uint32_t read(uint32_t nb)
     {
-        uint64_t const v = view();
-        uint32_t const x = uint32_t(v >> (48 - nb)) & ((1u << nb) - 1u);
-        pos -= int32_t(nb);
-        renorm();
-        return x;
+        prepare();
+        uint32_t const f = __funnelshift_rc(window(), 0u, 32u - nb);
+        g += int32_t(nb);
+        refill();
+        return f;
     }
-    __device__ __forceinline__ bool finished() const { return pos == end; }
+    __device__ __forceinline__ bool finished() const { return (kb + 2) * 32 - g == end; }
 };
 
 // ---------------------------------------------------------------------------
 // FSE: one lane per chunk, lanes per CTA sized so that four CTAs fit an SM.
-// Each lane keeps its decoding table in shared memory as two arrays: the
-// state cell (newState | nbBits << 12) and the symbol byte, plus the build
-// counters. Four symbols per step: the four table entries are loaded
-// together, and their fields' offsets follow from the code lengths, so the
-// four reads share one 64-bit view of the stream.
+// Each lane keeps its decoding table in shared memory, one 32-bit entry per
+// cell: the symbol (bits 0-7), 32 - nbBits (bits 8-15) and the shared-memory
+// byte offset of the cell newStateBase (bits 16-31). A decoder state is the
+// byte offset of its cell, so a transition is one load, and the fields of a
+// pair of transitions come out of one 32-bit window by shifts.
 //
 // Table construction restates src/openzl/fse/decompress/fse_decompress.c:
 // 73-171; decode order restates fse_decompress.c:255-337 (state i % nbStates
@@ -684,15 +691,13 @@ constexpr uint32_t kFseCtaSmem = 56 * 1024; // four CTAs per SM
 
 constexpr int kFseRing = 16, kFseAhead = 12; // stream ring: 256 bytes per lane, 192 bytes ahead
 
-__host__ __device__ __forceinline__ uint32_t fseSlotBytes(uint32_t tlMax) { return (3u << tlMax) + 512u + 4u; }
-__host__ __device__ __forceinline__ uint32_t fseRingOffset(uint32_t lanes, uint32_t tlMax)
-{
-    return (lanes * fseSlotBytes(tlMax) + 15u) & ~15u;
-}
+// per lane: table (4 << tableLog), build counters (512), stream ring
+__host__ __device__ __forceinline__ uint32_t fseSlotBytes(uint32_t tlMax) { return (4u << tlMax) + 512u + 16u * kFseRing; }
 __host__ __device__ __forceinline__ uint32_t fseSmemBytes(uint32_t lanes, uint32_t tlMax)
 {
-    return fseRingOffset(lanes, tlMax) + lanes * 16u * kFseRing;
+    return lanes * fseSlotBytes(tlMax);
 }
+static_assert(kFseCtaSmem <= 65536, "FSE states are 16-bit shared-memory offsets");
 
 __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, uint32_t nbTasks, uint32_t lanes,
                                            uint32_t tableLogMax, uint32_t* __restrict__ status)
@@ -703,108 +708,107 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
     uint32_t const ti = blockIdx.x * lanes + lane;
     if (ti >= nbTasks) return;
     FseTask const t = tasks[ti];
-    uint8_t* const base = smemFse + size_t(lane) * fseSlotBytes(tableLogMax);
-    uint16_t* const cell = reinterpret_cast<uint16_t*>(base);
-    uint8_t* const sym = base + (2u << tableLogMax);
-    uint16_t* const next = reinterpret_cast<uint16_t*>(base + (3u << tableLogMax));
+    uint32_t const slot = lane * fseSlotBytes(tableLogMax);
+    uint32_t* const tab = reinterpret_cast<uint32_t*>(smemFse + slot);
+    uint16_t* const next = reinterpret_cast<uint16_t*>(smemFse + slot + (4u << tableLogMax));
+    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemFse + slot + (4u << tableLogMax) + 512u);
     uint32_t const tl = t.tableLog;
     uint32_t const size = 1u << tl, mask = size - 1;
     uint32_t const step = (size >> 1) + (size >> 3) + 3;
-    uint32_t high = size - 1;
-    for (uint32_t s = 0; s < t.nbSym; s++) {
-        int const c = t.norm[s];
-        if (c == -1) {
-            sym[high--] = uint8_t(s);
-            next[s] = 1;
-        } else {
-            next[s] = uint16_t(c);
-        }
+    uint32_t const nbSym = t.nbSym;
+    // normalized counts (16-byte aligned in the parameter block, which has
+    // slack after its end) into the build counters
+    {
+        const uint4* const src = reinterpret_cast<const uint4*>(t.norm);
+        uint4* const dst = reinterpret_cast<uint4*>(next);
+        uint32_t const nv = (nbSym * 2 + 15) >> 4;
+#pragma unroll 8
+        for (uint32_t v = 0; v < nv; v++) dst[v] = __ldg(src + v);
     }
+    uint32_t high = size - 1;
+    for (uint32_t s = 0; s < nbSym; s++)
+        if (next[s] == 0xffffu) tab[high--] = s;
     uint32_t pos = 0;
-    for (uint32_t s = 0; s < t.nbSym; s++) {
-        int const c = t.norm[s];
+    for (uint32_t s = 0; s < nbSym; s++) {
+        int const c = int16_t(next[s]);
+        if (c == -1) {
+            next[s] = 1;
+            continue;
+        }
         for (int i = 0; i < c; i++) {
-            sym[pos] = uint8_t(s);
+            tab[pos] = s;
             do { pos = (pos + step) & mask; } while (pos > high);
         }
     }
     for (uint32_t u = 0; u < size; u++) {
-        uint32_t const s = sym[u];
+        uint32_t const s = tab[u] & 0xffu;
         uint32_t const x = next[s]++;
         uint32_t const nb = tl - (31 - __clz(x));
         uint32_t const ns = (x << nb) - size;
-        cell[u] = uint16_t(ns | (nb << 12));
+        tab[u] = s | ((32u - nb) << 8) | ((slot + 4u * ns) << 16);
     }
 
-    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemFse + fseRingOffset(lanes, tableLogMax)) + lane * 4 * kFseRing;
-    BitWin32<kFseRing, kFseAhead> br;
+    FseWin<kFseRing, kFseAhead> br;
     if (!br.init(t.bits, t.bitsSize, ring)) { reportError(status, DERR_CORRUPTION); return; }
     uint32_t const nst = t.nbStates;
-    uint32_t st0 = br.read(tl), st1 = br.read(tl), st2 = 0, st3 = 0;
-    if (nst == 4) { st2 = br.read(tl); st3 = br.read(tl); }
+    uint32_t st0 = slot + 4u * br.read(tl), st1 = slot + 4u * br.read(tl), st2 = 0, st3 = 0;
+    if (nst == 4) {
+        st2 = slot + 4u * br.read(tl);
+        st3 = slot + 4u * br.read(tl);
+    }
     uint32_t const n = t.dstSize;
     uint32_t const lastTr = n > nst ? n - nst : 0; // symbols [0, lastTr) have a transition
     uint8_t* const out = t.out;
-    bool const aligned = !(reinterpret_cast<uintptr_t>(out) & 3);
-    auto put4 = [&](uint32_t i, uint32_t word) {
-        if (aligned) {
-            *reinterpret_cast<uint32_t*>(out + i) = word;
-        } else {
-            out[i] = uint8_t(word);
-            out[i + 1] = uint8_t(word >> 8);
-            out[i + 2] = uint8_t(word >> 16);
-            out[i + 3] = uint8_t(word >> 24);
-        }
+    auto ent = [&](uint32_t st) -> uint32_t { return *reinterpret_cast<const uint32_t*>(smemFse + st); };
+    auto rsOf = [](uint32_t e) -> uint32_t { return __byte_perm(e, 0u, 0x4441); };
+    auto nextOf = [](uint32_t e, uint32_t f) -> uint32_t { return (e >> 16) + (f << 2); };
+    // two transitions whose fields lie in one window (at most 24 bits)
+    auto pair = [&](uint32_t ea, uint32_t eb, uint32_t& sa, uint32_t& sb) {
+        uint32_t const w = br.window();
+        uint32_t const ra = rsOf(ea), rb = rsOf(eb);
+        uint32_t const fa = __funnelshift_rc(w, 0u, ra);
+        uint32_t const fb = __funnelshift_rc(w << (32u - ra), 0u, rb);
+        sa = nextOf(ea, fa);
+        sb = nextOf(eb, fb);
+        br.g += 64 - int32_t(ra + rb);
+        br.refill();
     };
-    // one step of two or four transitions on consecutive states
-    auto step4 = [&](uint32_t& sa, uint32_t& sb, uint32_t& sc, uint32_t& sd) -> uint32_t {
-        uint32_t const ca = cell[sa], cb = cell[sb], cc = cell[sc], cd = cell[sd];
-        uint32_t const ya = sym[sa], yb = sym[sb], yc = sym[sc], yd = sym[sd];
-        uint32_t const na = ca >> 12, nb = cb >> 12, nc = cc >> 12, nd = cd >> 12;
-        uint64_t const v = br.view();
-        uint32_t const oa = 48 - na, ob = oa - nb, oc = ob - nc, od = oc - nd;
-        sa = (ca & 0xfff) + (uint32_t(v >> oa) & ((1u << na) - 1u));
-        sb = (cb & 0xfff) + (uint32_t(v >> ob) & ((1u << nb) - 1u));
-        sc = (cc & 0xfff) + (uint32_t(v >> oc) & ((1u << nc) - 1u));
-        sd = (cd & 0xfff) + (uint32_t(v >> od) & ((1u << nd) - 1u));
-        br.pos -= int32_t(48 - od);
-        br.renorm();
-        return ya | (yb << 8) | (yc << 16) | (yd << 24);
-    };
-    auto step2 = [&](uint32_t& sa, uint32_t& sb) -> uint32_t {
-        uint32_t const ca = cell[sa], cb = cell[sb];
-        uint32_t const ya = sym[sa], yb = sym[sb];
-        uint32_t const na = ca >> 12, nb = cb >> 12;
-        uint64_t const v = br.view();
-        uint32_t const oa = 48 - na, ob = oa - nb;
-        sa = (ca & 0xfff) + (uint32_t(v >> oa) & ((1u << na) - 1u));
-        sb = (cb & 0xfff) + (uint32_t(v >> ob) & ((1u << nb) - 1u));
-        br.pos -= int32_t(48 - ob);
-        br.renorm();
-        return ya | (yb << 8);
-    };
-    uint32_t i = 0;
-    if (nst == 4) {
-        for (; i + 4 <= lastTr; i += 4) put4(i, step4(st0, st1, st2, st3));
-    } else {
-        for (; i + 4 <= lastTr; i += 4) {
-            uint32_t const lo = step2(st0, st1);
-            uint32_t const hi2 = step2(st0, st1);
-            put4(i, lo | (hi2 << 16));
-        }
-    }
-    // remaining symbols, state (i % nbStates) rotated into st0
-    for (; i < n; i++) {
-        uint32_t const c = cell[st0];
-        out[i] = sym[st0];
+    // one symbol from st0, then the states rotate
+    auto single = [&](uint32_t i) {
+        uint32_t const e = ent(st0);
+        out[i] = uint8_t(e);
         uint32_t ns = st0;
-        if (i < lastTr) ns = (c & 0xfff) + br.read(c >> 12);
+        if (i < lastTr) ns = nextOf(e, br.read(32u - rsOf(e)));
         if (nst == 4) {
             st0 = st1; st1 = st2; st2 = st3; st3 = ns;
         } else {
             st0 = st1; st1 = ns;
         }
+    };
+    uint32_t i = 0;
+    uint32_t const head = min(n, uint32_t((4 - (reinterpret_cast<uintptr_t>(out) & 3)) & 3));
+    for (; i < head; i++) single(i);
+    if (nst == 4) {
+        for (; i + 4 <= lastTr; i += 4) {
+            br.prepare();
+            uint32_t const ea = ent(st0), eb = ent(st1), ec = ent(st2), ed = ent(st3);
+            pair(ea, eb, st0, st1);
+            pair(ec, ed, st2, st3);
+            *reinterpret_cast<uint32_t*>(out + i) =
+                __byte_perm(__byte_perm(ea, eb, 0x0040), __byte_perm(ec, ed, 0x0040), 0x5410);
+        }
+    } else {
+        for (; i + 4 <= lastTr; i += 4) {
+            br.prepare();
+            uint32_t const ea = ent(st0), eb = ent(st1);
+            pair(ea, eb, st0, st1);
+            uint32_t const ec = ent(st0), ed = ent(st1);
+            pair(ec, ed, st0, st1);
+            *reinterpret_cast<uint32_t*>(out + i) =
+                __byte_perm(__byte_perm(ea, eb, 0x0040), __byte_perm(ec, ed, 0x0040), 0x5410);
+        }
     }
+    for (; i < n; i++) single(i);
     if (!br.finished()) reportError(status, DERR_CORRUPTION);
 }
 
@@ -1313,7 +1317,7 @@ uint32_t tuneCandidates(const Launch& l, uint32_t* out, uint32_t cap)
     uint32_t n = 0;
     if (l.kind == KIND_FSE) {
         uint32_t const mx = fseLanes(l.param0);
-        for (uint32_t c : { 32u, 16u, 8u, 6u, 4u, 2u })
+        for (uint32_t c : { 32u, 16u, 8u, 6u, 5u, 4u, 3u, 2u })
             if (c <= mx && n < cap) out[n++] = c;
     } else if (l.kind == KIND_HUF) {
         for (uint32_t c : { 8u, 6u, 4u, 2u })
