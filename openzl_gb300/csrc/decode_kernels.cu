@@ -82,22 +82,48 @@ __device__ __forceinline__ uint64_t widthMask(uint32_t w)
 // ---------------------------------------------------------------------------
 // copy / constant: tiles of kTileBytes output bytes
 
-__global__ void kCopy(const CopyTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
+// 16 bytes starting `off` bytes (1..15) into the 32 bytes (u0, u1); q and r
+// are off / 4 and (off % 4) * 8, uniform across the block
+__device__ __forceinline__ uint4 shiftCombine(uint4 u0, uint4 u1, uint32_t q, uint32_t r)
+{
+    uint32_t y0, y1, y2, y3, y4;
+    switch (q) {
+        case 0: y0 = u0.x; y1 = u0.y; y2 = u0.z; y3 = u0.w; y4 = u1.x; break;
+        case 1: y0 = u0.y; y1 = u0.z; y2 = u0.w; y3 = u1.x; y4 = u1.y; break;
+        case 2: y0 = u0.z; y1 = u0.w; y2 = u1.x; y3 = u1.y; y4 = u1.z; break;
+        default: y0 = u0.w; y1 = u1.x; y2 = u1.y; y3 = u1.z; y4 = u1.w; break;
+    }
+    return make_uint4(__funnelshift_r(y0, y1, r), __funnelshift_r(y1, y2, r), __funnelshift_r(y2, y3, r),
+                      __funnelshift_r(y3, y4, r));
+}
+
+// Copies one tile: bytes up to the destination's 16-byte boundary, then
+// 16-byte stores, each from the two aligned 16-byte source blocks that hold
+// its bytes (both blocks hold bytes of the source, so nothing outside the
+// source's blocks is read), then the tail bytes.
+__global__ void __launch_bounds__(256) kCopy(const CopyTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
 {
     TileRef const tr = tiles[blockIdx.x];
     CopyTask const t = tasks[tr.task];
     uint64_t const b0 = uint64_t(tr.tile) * kTileBytes;
     uint64_t const b1 = min(t.bytes, b0 + kTileBytes);
-    bool const vec = !((reinterpret_cast<uintptr_t>(t.dst + b0) | reinterpret_cast<uintptr_t>(t.src + b0)) & 15);
-    if (vec) {
-        uint64_t const nv = (b1 - b0) / 16;
-        const uint4* s = reinterpret_cast<const uint4*>(t.src + b0);
-        uint4* d = reinterpret_cast<uint4*>(t.dst + b0);
-        for (uint64_t i = threadIdx.x; i < nv; i += blockDim.x) d[i] = s[i];
-        for (uint64_t i = b0 + nv * 16 + threadIdx.x; i < b1; i += blockDim.x) t.dst[i] = t.src[i];
+    uint64_t const head = min(b1 - b0, uint64_t((16 - (reinterpret_cast<uintptr_t>(t.dst + b0) & 15)) & 15));
+    for (uint64_t i = b0 + threadIdx.x; i < b0 + head; i += blockDim.x) t.dst[i] = t.src[i];
+    uint64_t const a0 = b0 + head;
+    uint64_t const nv = (b1 - a0) / 16;
+    uint4* const d = reinterpret_cast<uint4*>(t.dst + a0);
+    uintptr_t const sa = reinterpret_cast<uintptr_t>(t.src + a0);
+    uint32_t const off = uint32_t(sa & 15);
+    const uint4* const s = reinterpret_cast<const uint4*>(sa - off);
+    if (off == 0) {
+#pragma unroll 4
+        for (uint64_t i = threadIdx.x; i < nv; i += blockDim.x) d[i] = __ldg(s + i);
     } else {
-        for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) t.dst[i] = t.src[i];
+        uint32_t const q = off >> 2, r = (off & 3) * 8;
+#pragma unroll 4
+        for (uint64_t i = threadIdx.x; i < nv; i += blockDim.x) d[i] = shiftCombine(__ldg(s + i), __ldg(s + i + 1), q, r);
     }
+    for (uint64_t i = a0 + nv * 16 + threadIdx.x; i < b1; i += blockDim.x) t.dst[i] = t.src[i];
 }
 
 __global__ void kConst(const ConstTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
@@ -560,76 +586,21 @@ __device__ __forceinline__ bool streamStart(const uint8_t* p, uint32_t size, con
     return true;
 }
 
-// 128-bit window over the stream, refilled 64 bits at a time from the ring.
-// Between steps cb + 64 <= pos <= cb + 128 (cb: bit index of lo's bit 0), so
-// up to 48 bits below pos can be read without refilling: four FSE fields of
-// at most 12 bits, or four Huffman peeks of at most 12 bits.
+// Backward bit reader (FSE and Huffman decoders): three stream words in
+// registers, a (bits [cb + 64, cb + 96)) above b and c (bits [cb, cb + 32)),
+// cb = 32 * kb, and g = cb + 96 - pos. At the start of a step g <= 32, so the
+// 32 bits that start o <= 56 bits below the top of the window
+// (pos - o - 32 .. pos - o) are one funnel shift of (a, b) or (b, c): a step
+// reads two windows, one per pair of fields (at most 24 bits each), without
+// waiting for a refill, and refills once at its end by one or two words,
+// without a branch. prepare(), once per step, makes the next two words of
+// the ring readable. Words below the stream are never consumed by a valid
+// stream (finished() checks that the stream ends exactly at its first bit),
+// so the ring's stale contents may stand in for them.
 template <int RING, int AHEAD>
-struct BitWin {
+struct BitWin3 {
     StreamRing<RING, AHEAD> r;
-    int32_t pos, end, cb;
-    uint64_t lo, hi;
-
-    __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size, uint32_t* ring)
-    {
-        if (!streamStart(p, size, r.g16, pos, end)) return false;
-        r.ring = ring;
-        r.start(pos);
-        int32_t const jt = (pos - 1) >> 5; // word of the top unread bit
-        cb = (jt - 3) * 32;                // pos - cb in (96, 128]
-        uint32_t const w3 = r.word(jt), w2 = r.word(jt - 1), w1 = r.word(jt - 2), w0 = r.word(jt - 3);
-        hi = (uint64_t(w3) << 32) | w2;
-        lo = (uint64_t(w1) << 32) | w0;
-        return true;
-    }
-    __device__ __forceinline__ void renorm()
-    {
-        if (pos - cb < 64) {
-            cb -= 64;
-            hi = lo;
-            int32_t const k = cb >> 5;
-            uint32_t const w1 = r.word(k + 1), w0 = r.word(k);
-            lo = (uint64_t(w1) << 32) | w0;
-        }
-    }
-    // the 64 bits starting at bit b (b - cb between 0 and 127)
-    __device__ __forceinline__ uint64_t bitsAt(int32_t b) const
-    {
-        int32_t const s = b - cb;
-        if (s >= 64) return hi >> ((s - 64) & 63); // s = 128 only for an empty field (masked to 0)
-        if (s <= 0) return lo; // only on corrupt streams (caught by the end check)
-        return (lo >> s) | (hi << (64 - s));
-    }
-    // the 64 bits starting 48 bits below pos
-    __device__ __forceinline__ uint64_t view() const { return bitsAt(pos - 48); }
-    __device__ __forceinline__ uint32_t peek(uint32_t nb) const
-    {
-        return uint32_t(bitsAt(pos - int32_t(nb))) & ((1u << nb) - 1u);
-    }
-    // one field of nb bits (nb <= 12) just below pos
-    __device__ __forceinline__ uint32_t read(uint32_t nb)
-    {
-        uint32_t const x = peek(nb);
-        pos -= int32_t(nb);
-        renorm();
-        return x;
-    }
-    __device__ __forceinline__ bool finished() const { return pos == end; }
-};
-
-// Backward bit reader of the FSE decoder: two stream words in registers, a
-// (bits [cb + 32, cb + 64)) above b (bits [cb, cb + 32)), cb = 32 * kb, and
-// g = cb + 64 - pos. Before each group of fields of at most 32 bits in total
-// g <= 32, so the 32 bits just below pos, most significant first, are one
-// funnel shift of (a, b). A refill takes the next word from the ring without
-// a branch; prepare(), once per two groups, makes the next two words of the
-// ring readable. Words below the stream are never consumed by a valid stream
-// (finished() checks that the stream ends exactly at its first bit), so the
-// ring's stale contents may stand in for them.
-template <int RING, int AHEAD>
-struct FseWin {
-    StreamRing<RING, AHEAD> r;
-    uint32_t a, b;
+    uint32_t a, b, c;
     int32_t kb, g, end;
 
     __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size, uint32_t* ring)
@@ -641,8 +612,9 @@ struct FseWin {
         int32_t const jt = (pos - 1) >> 5; // word of the top unread bit
         a = r.word(jt);
         b = r.word(jt - 1);
-        kb = jt - 1;
-        g = (kb + 2) * 32 - pos; // in [0, 32)
+        c = r.word(jt - 2);
+        kb = jt - 2;
+        g = (kb + 3) * 32 - pos; // in [0, 32)
         return true;
     }
     __device__ __forceinline__ void prepare()
@@ -654,35 +626,48 @@ struct FseWin {
             asm volatile("cp.async.wait_group %0;" ::"n"(AHEAD) : "memory");
         }
     }
-    __device__ __forceinline__ uint32_t window() const { return __funnelshift_lc(b, a, uint32_t(g)); }
-    __device__ __forceinline__ void refill()
+    // the 32 bits starting o bits below the top of the window (o <= 56)
+    __device__ __forceinline__ uint32_t window(int32_t o) const
     {
-        uint32_t const nw = r.ring[(kb - 1) & (4 * RING - 1)];
-        bool const need = g > 32;
-        a = need ? b : a;
-        b = need ? nw : b;
-        kb -= need ? 1 : 0;
-        g -= need ? 32 : 0;
+        uint32_t const hiPair = __funnelshift_l(b, a, uint32_t(o));      // o < 32
+        uint32_t const loPair = __funnelshift_l(c, b, uint32_t(o - 32)); // 32 <= o <= 56
+        return o < 32 ? hiPair : loPair;
+    }
+    // drops the n bits read since the start of the step (g + n <= 96)
+    __device__ __forceinline__ void advance(int32_t n)
+    {
+        uint32_t const w1 = r.ring[(kb - 1) & (4 * RING - 1)];
+        uint32_t const w2 = r.ring[(kb - 2) & (4 * RING - 1)];
+        g += n;
+        bool const one = g > 32, two = g > 64;
+        uint32_t const na = two ? c : (one ? b : a);
+        uint32_t const nb = two ? w1 : (one ? c : b);
+        uint32_t const nc = two ? w2 : (one ? w1 : c);
+        a = na;
+        b = nb;
+        c = nc;
+        int32_t const k = int32_t(one) + int32_t(two);
+        kb -= k;
+        g -= 32 * k;
     }
     // one field of nb bits (nb <= 12) just below pos
     __device__ __forceinline__ uint32_t read(uint32_t nb)
     {
         prepare();
-        uint32_t const f = __funnelshift_rc(window(), 0u, 32u - nb);
-        g += int32_t(nb);
-        refill();
+        uint32_t const f = __funnelshift_l(window(g), 0u, nb);
+        advance(int32_t(nb));
         return f;
     }
-    __device__ __forceinline__ bool finished() const { return (kb + 2) * 32 - g == end; }
+    __device__ __forceinline__ bool finished() const { return (kb + 3) * 32 - g == end; }
 };
 
 // ---------------------------------------------------------------------------
 // FSE: one lane per chunk, lanes per CTA sized so that four CTAs fit an SM.
 // Each lane keeps its decoding table in shared memory, one 32-bit entry per
-// cell: the symbol (bits 0-7), 32 - nbBits (bits 8-15) and the shared-memory
-// byte offset of the cell newStateBase (bits 16-31). A decoder state is the
-// byte offset of its cell, so a transition is one load, and the fields of a
-// pair of transitions come out of one 32-bit window by shifts.
+// cell: the symbol (bits 0-7), nbBits (bits 8-15) and the shared-memory byte
+// offset of the cell newStateBase (bits 16-31). A decoder state is the byte
+// offset of its cell, so a transition is one load, and the fields of a pair
+// of transitions come out of one 32-bit window by funnel shifts.
 //
 // Table construction restates src/openzl/fse/decompress/fse_decompress.c:
 // 73-171; decode order restates fse_decompress.c:255-337 (state i % nbStates
@@ -745,10 +730,10 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
         uint32_t const x = next[s]++;
         uint32_t const nb = tl - (31 - __clz(x));
         uint32_t const ns = (x << nb) - size;
-        tab[u] = s | ((32u - nb) << 8) | ((slot + 4u * ns) << 16);
+        tab[u] = s | (nb << 8) | ((slot + 4u * ns) << 16);
     }
 
-    FseWin<kFseRing, kFseAhead> br;
+    BitWin3<kFseRing, kFseAhead> br;
     if (!br.init(t.bits, t.bitsSize, ring)) { reportError(status, DERR_CORRUPTION); return; }
     uint32_t const nst = t.nbStates;
     uint32_t st0 = slot + 4u * br.read(tl), st1 = slot + 4u * br.read(tl), st2 = 0, st3 = 0;
@@ -760,25 +745,23 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
     uint32_t const lastTr = n > nst ? n - nst : 0; // symbols [0, lastTr) have a transition
     uint8_t* const out = t.out;
     auto ent = [&](uint32_t st) -> uint32_t { return *reinterpret_cast<const uint32_t*>(smemFse + st); };
-    auto rsOf = [](uint32_t e) -> uint32_t { return __byte_perm(e, 0u, 0x4441); };
+    auto nbOf = [](uint32_t e) -> uint32_t { return __byte_perm(e, 0u, 0x4441); };
     auto nextOf = [](uint32_t e, uint32_t f) -> uint32_t { return (e >> 16) + (f << 2); };
-    // two transitions whose fields lie in one window (at most 24 bits)
-    auto pair = [&](uint32_t ea, uint32_t eb, uint32_t& sa, uint32_t& sb) {
-        uint32_t const w = br.window();
-        uint32_t const ra = rsOf(ea), rb = rsOf(eb);
-        uint32_t const fa = __funnelshift_rc(w, 0u, ra);
-        uint32_t const fb = __funnelshift_rc(w << (32u - ra), 0u, rb);
-        sa = nextOf(ea, fa);
-        sb = nextOf(eb, fb);
-        br.g += 64 - int32_t(ra + rb);
-        br.refill();
+    // two transitions whose fields (at most 24 bits) start o bits below the
+    // top of the window; returns the bits they read
+    auto pair = [&](int32_t o, uint32_t ea, uint32_t eb, uint32_t& sa, uint32_t& sb) -> uint32_t {
+        uint32_t const w = br.window(o);
+        uint32_t const na = nbOf(ea), nb = nbOf(eb);
+        sa = nextOf(ea, __funnelshift_l(w, 0u, na));
+        sb = nextOf(eb, __funnelshift_l(w << na, 0u, nb));
+        return na + nb;
     };
     // one symbol from st0, then the states rotate
     auto single = [&](uint32_t i) {
         uint32_t const e = ent(st0);
         out[i] = uint8_t(e);
         uint32_t ns = st0;
-        if (i < lastTr) ns = nextOf(e, br.read(32u - rsOf(e)));
+        if (i < lastTr) ns = nextOf(e, br.read(nbOf(e)));
         if (nst == 4) {
             st0 = st1; st1 = st2; st2 = st3; st3 = ns;
         } else {
@@ -792,8 +775,9 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
         for (; i + 4 <= lastTr; i += 4) {
             br.prepare();
             uint32_t const ea = ent(st0), eb = ent(st1), ec = ent(st2), ed = ent(st3);
-            pair(ea, eb, st0, st1);
-            pair(ec, ed, st2, st3);
+            uint32_t const n1 = pair(br.g, ea, eb, st0, st1);
+            uint32_t const n2 = pair(br.g + int32_t(n1), ec, ed, st2, st3);
+            br.advance(int32_t(n1 + n2));
             *reinterpret_cast<uint32_t*>(out + i) =
                 __byte_perm(__byte_perm(ea, eb, 0x0040), __byte_perm(ec, ed, 0x0040), 0x5410);
         }
@@ -801,9 +785,10 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
         for (; i + 4 <= lastTr; i += 4) {
             br.prepare();
             uint32_t const ea = ent(st0), eb = ent(st1);
-            pair(ea, eb, st0, st1);
+            uint32_t const n1 = pair(br.g, ea, eb, st0, st1);
             uint32_t const ec = ent(st0), ed = ent(st1);
-            pair(ec, ed, st0, st1);
+            uint32_t const n2 = pair(br.g + int32_t(n1), ec, ed, st0, st1);
+            br.advance(int32_t(n1 + n2));
             *reinterpret_cast<uint32_t*>(out + i) =
                 __byte_perm(__byte_perm(ea, eb, 0x0040), __byte_perm(ec, ed, 0x0040), 0x5410);
         }
@@ -900,37 +885,42 @@ __device__ __forceinline__ void hufDecodeStream(const HufTask& t, const uint16_t
         o0 = 0;
         n = t.dstSize;
     }
-    BitWin<kHufRing, kHufAhead> br;
+    BitWin3<kHufRing, kHufAhead> br;
     if (!br.init(sp, ssize, ring)) { reportError(status, DERR_CORRUPTION); return; }
     uint8_t* const out = t.out + o0;
+    uint32_t const sh = 32u - tl;
     uint32_t i = 0;
-    // unaligned head, then four symbols (at most 48 bits) per refill check
-    // and per 32-bit store
-    uint32_t const head = uint32_t((4 - (reinterpret_cast<uintptr_t>(out) & 3)) & 3);
-    for (; i < head && i < n; i++) {
-        uint32_t const e = dt[br.peek(tl)];
-        out[i] = uint8_t(e);
-        br.pos -= int32_t(e >> 8);
-        br.renorm();
-    }
+    // one symbol; its code is at most tl <= 12 bits
+    auto single = [&]() -> uint32_t {
+        br.prepare();
+        uint32_t const e = dt[__funnelshift_lc(br.b, br.a, uint32_t(br.g)) >> sh];
+        br.advance(int32_t(e >> 8));
+        return e;
+    };
+    // unaligned head, then four symbols per refill and per 32-bit store: the
+    // 64 bits below pos, left-aligned in (hi, lo), hold the four codes
+    uint32_t const head = min(n, uint32_t((4 - (reinterpret_cast<uintptr_t>(out) & 3)) & 3));
+    for (; i < head; i++) out[i] = uint8_t(single());
     for (; i + 4 <= n; i += 4) {
-        uint32_t const e0 = dt[br.peek(tl)];
-        br.pos -= int32_t(e0 >> 8);
-        uint32_t const e1 = dt[br.peek(tl)];
-        br.pos -= int32_t(e1 >> 8);
-        uint32_t const e2 = dt[br.peek(tl)];
-        br.pos -= int32_t(e2 >> 8);
-        uint32_t const e3 = dt[br.peek(tl)];
-        br.pos -= int32_t(e3 >> 8);
-        br.renorm();
-        *reinterpret_cast<uint32_t*>(out + i) = (e0 & 0xff) | ((e1 & 0xff) << 8) | ((e2 & 0xff) << 16) | ((e3 & 0xff) << 24);
+        br.prepare();
+        uint32_t hi = __funnelshift_lc(br.b, br.a, uint32_t(br.g));
+        uint32_t lo = __funnelshift_lc(br.c, br.b, uint32_t(br.g));
+        uint32_t const e0 = dt[hi >> sh];
+        uint32_t const n0 = e0 >> 8;
+        hi = __funnelshift_l(lo, hi, n0);
+        lo <<= n0;
+        uint32_t const e1 = dt[hi >> sh];
+        uint32_t const n1 = e1 >> 8;
+        hi = __funnelshift_l(lo, hi, n1);
+        lo <<= n1;
+        uint32_t const e2 = dt[hi >> sh];
+        uint32_t const n2 = e2 >> 8;
+        hi = __funnelshift_l(lo, hi, n2);
+        uint32_t const e3 = dt[hi >> sh];
+        br.advance(int32_t(n0 + n1 + n2 + (e3 >> 8)));
+        *reinterpret_cast<uint32_t*>(out + i) = __byte_perm(__byte_perm(e0, e1, 0x0040), __byte_perm(e2, e3, 0x0040), 0x5410);
     }
-    for (; i < n; i++) {
-        uint32_t const e = dt[br.peek(tl)];
-        out[i] = uint8_t(e);
-        br.pos -= int32_t(e >> 8);
-        br.renorm();
-    }
+    for (; i < n; i++) out[i] = uint8_t(single());
     if (!br.finished()) reportError(status, DERR_CORRUPTION);
 }
 
