@@ -1210,8 +1210,8 @@ __global__ void __launch_bounds__(256) kHashBlocks(const HashTask* __restrict__ 
     }
 }
 
-// Phase 2: one warp per task. Lanes 0..7 run the block chain for their
-// accumulator (loads four blocks ahead), then the trailing partial stripes
+// Phase 2: one warp per task. Lane i (and its copies i + 8, i + 16, i + 24)
+// runs the block chain of accumulator i, then the trailing partial stripes
 // and the final stripe, and lane 0 merges.
 __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks, uint32_t* __restrict__ status)
 {
@@ -1230,21 +1230,39 @@ __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks
                             : i == 4 ? XP64_4 : i == 5 ? XP32_2 : i == 6 ? XP64_5 : XP32_1;
         uint64_t acc = init;
         uint64_t const key = secret64(int(192 - 64 + 8 * i));
-        const uint64_t* const bs = t.blockSums + i;
+        // The block chain acc = scramble(acc + sum) is serial; its inputs are
+        // not. The warp loads the sums of 32 blocks at a time (coalesced, the
+        // next batch while the current one runs), and lane i takes the value
+        // of block k for accumulator i from lane 8 * (k % 4) + i.
+        const uint64_t* const bs = t.blockSums;
         uint32_t const nb = t.nbBlocks;
-        uint32_t b = 0;
-        for (; b + 4 <= nb; b += 4) {
-            uint64_t const v0 = bs[8ull * b], v1 = bs[8ull * (b + 1)], v2 = bs[8ull * (b + 2)], v3 = bs[8ull * (b + 3)];
-            acc += v0; acc ^= acc >> 47; acc ^= key; acc *= XP32_1;
-            acc += v1; acc ^= acc >> 47; acc ^= key; acc *= XP32_1;
-            acc += v2; acc ^= acc >> 47; acc ^= key; acc *= XP32_1;
-            acc += v3; acc ^= acc >> 47; acc ^= key; acc *= XP32_1;
+        uint64_t const total = 8ull * nb;
+        uint64_t cur[8];
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            uint64_t const idx = uint64_t(lane) + 32u * m;
+            cur[m] = idx < total ? __ldg(bs + idx) : 0;
         }
-        for (; b < nb; b++) {
-            acc += bs[8ull * b];
-            acc ^= acc >> 47;
-            acc ^= key;
-            acc *= XP32_1;
+        for (uint32_t b0 = 0; b0 < nb; b0 += 32) {
+            uint64_t nxt[8];
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                uint64_t const idx = 8ull * (b0 + 32) + lane + 32u * m;
+                nxt[m] = idx < total ? __ldg(bs + idx) : 0;
+            }
+            uint32_t const cnt = min(32u, nb - b0);
+#pragma unroll
+            for (int k = 0; k < 32; k++) {
+                uint64_t const v = __shfl_sync(0xffffffffu, cur[k >> 2], int(8 * (k & 3) + i));
+                if (uint32_t(k) < cnt) {
+                    acc += v;
+                    acc ^= acc >> 47;
+                    acc ^= key;
+                    acc *= XP32_1;
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < 8; m++) cur[m] = nxt[m];
         }
         uint64_t const len = t.len;
         uint64_t const nbStripes = ((len - 1) - uint64_t(kHashBlock) * nb) / 64;
