@@ -684,54 +684,120 @@ __host__ __device__ __forceinline__ uint32_t fseSmemBytes(uint32_t lanes, uint32
 }
 static_assert(kFseCtaSmem <= 65536, "FSE states are 16-bit shared-memory offsets");
 
-__global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, uint32_t nbTasks, uint32_t lanes,
-                                           uint32_t tableLogMax, uint32_t* __restrict__ status)
+// Builds the decoding table of task t in the slot at byte `slot` of the CTA's
+// shared memory with all 32 lanes of the warp (every lane calls it).
+//  - Counts: the normalized counts go to the slot's counters; a warp scan of
+//    the positive counts gives each symbol's first occurrence (cum), and the
+//    count -1 symbols take the top cells in symbol order.
+//  - Spread: occurrence k (symbols in order, each repeated count times) goes
+//    to the k-th cell of the sequence 0, step, 2 step, ... (mod size) that is
+//    not a top cell; 32 sequence positions per round, ranked by a ballot.
+//  - Cells, 32 per round in increasing order: a cell's state x is its
+//    symbol's counter plus the number of lower lanes of the round holding
+//    the same symbol (__match_any_sync); the highest such lane advances the
+//    counter.
+// The result equals the serial construction of fse_decompress.c:73-171.
+__device__ __forceinline__ void fseBuildWarp(const FseTask& t, uint8_t* smem, uint32_t slot, uint32_t tlMax,
+                                             uint16_t* cum)
 {
-    extern __shared__ __align__(16) uint8_t smemFse[];
     uint32_t const lane = threadIdx.x;
-    if (lane >= lanes) return;
-    uint32_t const ti = blockIdx.x * lanes + lane;
-    if (ti >= nbTasks) return;
-    FseTask const t = tasks[ti];
-    uint32_t const slot = lane * fseSlotBytes(tableLogMax);
-    uint32_t* const tab = reinterpret_cast<uint32_t*>(smemFse + slot);
-    uint16_t* const next = reinterpret_cast<uint16_t*>(smemFse + slot + (4u << tableLogMax));
-    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemFse + slot + (4u << tableLogMax) + 512u);
+    uint32_t const lt = (1u << lane) - 1u;
+    uint32_t* const tab = reinterpret_cast<uint32_t*>(smem + slot);
+    uint16_t* const next = reinterpret_cast<uint16_t*>(smem + slot + (4u << tlMax));
     uint32_t const tl = t.tableLog;
     uint32_t const size = 1u << tl, mask = size - 1;
     uint32_t const step = (size >> 1) + (size >> 3) + 3;
     uint32_t const nbSym = t.nbSym;
     // normalized counts (16-byte aligned in the parameter block, which has
-    // slack after its end) into the build counters
-    {
-        const uint4* const src = reinterpret_cast<const uint4*>(t.norm);
-        uint4* const dst = reinterpret_cast<uint4*>(next);
-        uint32_t const nv = (nbSym * 2 + 15) >> 4;
-#pragma unroll 8
-        for (uint32_t v = 0; v < nv; v++) dst[v] = __ldg(src + v);
+    // slack after its end) into the counters: at most 32 16-byte blocks
+    uint32_t const nv = (nbSym * 2 + 15) >> 4;
+    if (lane < nv) reinterpret_cast<uint4*>(next)[lane] = __ldg(reinterpret_cast<const uint4*>(t.norm) + lane);
+    __syncwarp();
+    // lane j: symbols 8j .. 8j + 7
+    int v[8];
+    uint32_t sumC = 0, sumNeg = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t const sy = 8 * lane + k;
+        v[k] = sy < nbSym ? int(int16_t(next[sy])) : 0;
+        sumC += v[k] > 0 ? uint32_t(v[k]) : 0u;
+        sumNeg += v[k] == -1 ? 1u : 0u;
     }
-    uint32_t high = size - 1;
-    for (uint32_t s = 0; s < nbSym; s++)
-        if (next[s] == 0xffffu) tab[high--] = s;
-    uint32_t pos = 0;
-    for (uint32_t s = 0; s < nbSym; s++) {
-        int const c = int16_t(next[s]);
-        if (c == -1) {
-            next[s] = 1;
-            continue;
-        }
-        for (int i = 0; i < c; i++) {
-            tab[pos] = s;
-            do { pos = (pos + step) & mask; } while (pos > high);
+    uint32_t inC = sumC, inNeg = sumNeg;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t const yc = __shfl_up_sync(0xffffffffu, inC, o), yn = __shfl_up_sync(0xffffffffu, inNeg, o);
+        if (lane >= uint32_t(o)) {
+            inC += yc;
+            inNeg += yn;
         }
     }
-    for (uint32_t u = 0; u < size; u++) {
-        uint32_t const s = tab[u] & 0xffu;
-        uint32_t const x = next[s]++;
+    uint32_t const totalNeg = __shfl_sync(0xffffffffu, inNeg, 31);
+    uint32_t const high = size - 1 - totalNeg;
+    uint32_t c0 = inC - sumC, n0 = inNeg - sumNeg;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t const sy = 8 * lane + k;
+        cum[sy] = uint16_t(c0);
+        c0 += v[k] > 0 ? uint32_t(v[k]) : 0u;
+        if (v[k] == -1) {
+            tab[size - 1 - n0] = sy;
+            next[sy] = 1;
+            n0++;
+        }
+    }
+    if (lane == 31) cum[256] = uint16_t(c0);
+    __syncwarp();
+    // spread
+    uint32_t sCur = 0, cumNext = cum[1], occBase = 0;
+    for (uint32_t b0 = 0; b0 < size; b0 += 32) {
+        uint32_t const pos = ((b0 + lane) * step) & mask;
+        bool const valid = totalNeg < size && pos <= high; // all cells are top cells when every count is -1
+        uint32_t const bal = __ballot_sync(0xffffffffu, valid);
+        if (valid) {
+            uint32_t const occ = occBase + __popc(bal & lt);
+            while (occ >= cumNext && sCur < 255) cumNext = cum[++sCur + 1];
+            tab[pos] = sCur;
+        }
+        occBase += __popc(bal);
+    }
+    __syncwarp();
+    // cells
+    for (uint32_t b0 = 0; b0 < size; b0 += 32) {
+        uint32_t const u = b0 + lane;
+        uint32_t const sy = tab[u] & 0xffu;
+        uint32_t const m = __match_any_sync(0xffffffffu, sy);
+        uint32_t const base = next[sy];
+        __syncwarp();
+        if (lane == 31u - __clz(m)) next[sy] = uint16_t(base + __popc(m));
+        uint32_t const x = base + __popc(m & lt);
         uint32_t const nb = tl - (31 - __clz(x));
         uint32_t const ns = (x << nb) - size;
-        tab[u] = s | (nb << 8) | ((slot + 4u * ns) << 16);
+        tab[u] = sy | (nb << 8) | ((slot + 4u * ns) << 16);
+        __syncwarp();
     }
+}
+
+__global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, uint32_t nbTasks, uint32_t lanes,
+                                           uint32_t tableLogMax, uint32_t* __restrict__ status)
+{
+    extern __shared__ __align__(16) uint8_t smemFse[];
+    __shared__ uint16_t sCum[260];
+    uint32_t const lane = threadIdx.x;
+    // every lane of the warp builds every table of the CTA, one at a time
+    for (uint32_t k = 0; k < lanes; k++) {
+        uint32_t const tk = blockIdx.x * lanes + k;
+        if (tk >= nbTasks) break;
+        FseTask const tt = tasks[tk];
+        fseBuildWarp(tt, smemFse, k * fseSlotBytes(tableLogMax), tableLogMax, sCum);
+    }
+    if (lane >= lanes) return;
+    uint32_t const ti = blockIdx.x * lanes + lane;
+    if (ti >= nbTasks) return;
+    FseTask const t = tasks[ti];
+    uint32_t const slot = lane * fseSlotBytes(tableLogMax);
+    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemFse + slot + (4u << tableLogMax) + 512u);
+    uint32_t const tl = t.tableLog;
 
     BitWin3<kFseRing, kFseAhead> br;
     if (!br.init(t.bits, t.bitsSize, ring)) { reportError(status, DERR_CORRUPTION); return; }
