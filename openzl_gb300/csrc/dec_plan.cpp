@@ -1110,7 +1110,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         addTiled(KIND_TOKENIZE, lv, b.tok, [](const TokenizeTask& t) { return ceilDiv(t.n, kTileElems); });
         addTiled(KIND_FLOATDEC, lv, b.flt, [](const FloatDecTask& t) { return ceilDiv(t.n, kTileElems); });
         addTiled(KIND_TRANSPOSE, lv, b.tr, [](const TransposeTask& t) { return ceilDiv(t.n, kTileElems); });
-        addTiled(KIND_NUMPIPE, lv, b.num, [](const NumPipeTask& t) { return ceilDiv(t.n, kTileElems); });
+        addTiled(KIND_NUMPIPE, lv, b.num, [](const NumPipeTask& t) { return ceilDiv(t.n, kNumTileBytes / t.w); });
     }
     // checksums: one launch after everything else
     bool anyHash = false;

@@ -136,6 +136,7 @@ struct TileRef {
 };
 
 constexpr uint32_t kTileElems = 4096;     // element tile of the element-wise kernels
+constexpr uint32_t kNumTileBytes = 16384; // numeric-pipeline tile: kNumTileBytes / w output elements
 constexpr uint32_t kTileBytes = 65536;    // byte-oriented tile
 constexpr uint32_t kHashBlock = 1024;     // XXH3 block length
 

@@ -158,232 +158,412 @@ __global__ void kConst(const ConstTask* __restrict__ tasks, const TileRef* __res
 //
 // Delta decoding is an exclusive prefix sum: out[i] = first + sum(src[0..i))
 // modulo 2^(8w), src holding n-1 elements (decode_delta_kernel.c:232). A tile
-// is 4096 output elements; thread t owns the 16 consecutive elements
-// 16t..16t+15 of its tile and loads exactly their sources (16-byte loads per
-// plane, 16w-byte loads for plain elements, aligned words for packed fields).
-// Delta tasks take three launches, none of which waits on another CTA: the
-// sum of every tile's sources, an exclusive scan of those sums per task (one
-// warp per task), then the final pass that scans inside the tile and adds
-// the tile's prefix. The sources are read twice; nothing is latency-bound.
+// is kNumTileBytes of output (kNumTileBytes / w elements); thread t owns the
+// 64 output bytes 64t..64t+63 of its tile and holds them as 16 words of
+// little-endian elements, so every width keeps 64 bytes of loads in flight
+// per thread. Byte and 16-bit elements are zigzagged and scanned four or two
+// to a word with SIMD byte/halfword adds. Plain sources and planes are read
+// with 16- or 8-byte loads (shifted into place when misaligned); bit-packed
+// sources are staged through shared memory with coalesced loads, one pad
+// word after every 32 so that the threads' field reads spread over the
+// banks. Delta tasks take three launches, none of which waits on another
+// CTA: the sum of every tile's sources, an exclusive scan of those sums per
+// task (one warp per task), then the final pass that scans inside the tile
+// and adds the tile's prefix.
 constexpr int kNPThreads = 256;
-constexpr int kNPPer = kTileElems / kNPThreads; // 16
+constexpr int kNW = 16;                                   // words per thread
+constexpr uint32_t kNPBytes = 4 * kNW;                    // 64 output bytes per thread
+static_assert(kNPBytes * kNPThreads == kNumTileBytes, "tile = threads x bytes per thread");
+constexpr uint32_t kNPStageWords = kNumTileBytes / 4 + 8; // the fields of a tile plus partial blocks at both ends
+constexpr uint32_t kNPStagePadded = kNPStageWords + kNPStageWords / 32 + 1;
 
-template <int W> struct NPVal { using T = uint32_t; };
-template <> struct NPVal<8> { using T = uint64_t; };
+__device__ __forceinline__ uint32_t npPad(uint32_t q) { return q + (q >> 5); }
 
-template <int W>
-__device__ __forceinline__ typename NPVal<W>::T npMask(typename NPVal<W>::T v)
+// NQ 16-byte blocks from p (any alignment; every block read holds bytes of
+// the range) into w[0 .. 4 NQ)
+template <int NQ>
+__device__ __forceinline__ void npLdq(const uint8_t* p, uint32_t* w)
 {
-    if constexpr (W == 1) return v & 0xffu;
-    else if constexpr (W == 2) return v & 0xffffu;
-    else return v;
+    uintptr_t const a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(15);
+    uint32_t const off = uint32_t(reinterpret_cast<uintptr_t>(p) - a);
+    const uint4* const s = reinterpret_cast<const uint4*>(a);
+    if (off == 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            uint4 const u = __ldg(s + q);
+            w[4 * q] = u.x; w[4 * q + 1] = u.y; w[4 * q + 2] = u.z; w[4 * q + 3] = u.w;
+        }
+    } else {
+        uint32_t const qq = off >> 2, r = (off & 3) * 8;
+        uint4 prev = __ldg(s);
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            uint4 const nxt = __ldg(s + q + 1);
+            uint4 const u = shiftCombine(prev, nxt, qq, r);
+            w[4 * q] = u.x; w[4 * q + 1] = u.y; w[4 * q + 2] = u.z; w[4 * q + 3] = u.w;
+            prev = nxt;
+        }
+    }
 }
 
-// Loads source elements j0..j0+15 (those below nSrc; the rest read as 0).
-template <int W, int MODE>
-__device__ __forceinline__ void npLoad(const NumPipeTask& t, uint64_t j0, uint64_t nSrc,
-                                       typename NPVal<W>::T (&v)[kNPPer])
+// 8 bytes from p (any alignment) into w[0], w[1], from the aligned 8-byte
+// words that hold them
+__device__ __forceinline__ void npLd8(const uint8_t* p, uint32_t* w)
 {
-    using T = typename NPVal<W>::T;
-    bool const full = j0 + kNPPer <= nSrc;
-    if constexpr (MODE == SRC_PLANES) {
+    uintptr_t const a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(7);
+    uint32_t const off = uint32_t(reinterpret_cast<uintptr_t>(p) - a);
+    const uint2* const s = reinterpret_cast<const uint2*>(a);
+    uint2 const u0 = __ldg(s);
+    if (off == 0) {
+        w[0] = u0.x;
+        w[1] = u0.y;
+    } else {
+        uint2 const u1 = __ldg(s + 1);
+        uint32_t const r = (off & 3) * 8;
+        uint32_t const x0 = off < 4 ? u0.x : u0.y, x1 = off < 4 ? u0.y : u1.x, x2 = off < 4 ? u1.x : u1.y;
+        w[0] = __funnelshift_r(x0, x1, r);
+        w[1] = __funnelshift_r(x1, x2, r);
+    }
+}
+
+// Loads the thread's source elements j0 .. j0 + 64/W (those below nSrc; the
+// rest read as 0) as 16 words of little-endian elements. `stage` holds the
+// tile's bit-packed words (padded) for SRC_BITPACK, bit `sbit` being the
+// first field of the tile.
+template <int W, int MODE>
+__device__ __forceinline__ void npLoad(const NumPipeTask& t, uint64_t j0, uint64_t nSrc, const uint32_t* stage,
+                                       uint32_t sbit, uint32_t tileRel, uint32_t (&w)[kNW])
+{
+    constexpr uint32_t E = kNPBytes / W;
+    uint32_t const cs = j0 < nSrc ? uint32_t(umin64(E, nSrc - j0)) : 0u;
+    if constexpr (MODE == SRC_PLAIN) {
+        if (cs == E) {
+            npLdq<kNW / 4>(t.src + j0 * W, w);
+        } else {
+            const uint8_t* const p = t.src + j0 * W;
 #pragma unroll
-        for (int k = 0; k < kNPPer; k++) v[k] = 0;
+            for (int m = 0; m < kNW; m++) {
+                uint32_t x = 0;
 #pragma unroll
-        for (int b = 0; b < W; b++) {
-            const uint8_t* const pl = t.planes[b] + j0;
-            if (full && !(reinterpret_cast<uintptr_t>(pl) & 15)) {
-                uint4 const q = __ldg(reinterpret_cast<const uint4*>(pl));
-                uint32_t const wd[4] = { q.x, q.y, q.z, q.w };
-#pragma unroll
-                for (int k = 0; k < kNPPer; k++) v[k] |= T((wd[k >> 2] >> (8 * (k & 3))) & 0xffu) << (8 * b);
-            } else {
-#pragma unroll
-                for (int k = 0; k < kNPPer; k++)
-                    if (j0 + k < nSrc) v[k] |= T(pl[k]) << (8 * b);
+                for (int y = 0; y < 4; y++)
+                    if (uint32_t(4 * m + y) < cs * W) x |= uint32_t(p[4 * m + y]) << (8 * y);
+                w[m] = x;
             }
         }
-    } else if constexpr (MODE == SRC_PLAIN) {
-        const uint8_t* const p = t.src + j0 * W;
-        if (full && !(reinterpret_cast<uintptr_t>(p) & 15)) {
+    } else if constexpr (MODE == SRC_PLANES) {
+        constexpr int PW = int(E / 4); // words per plane
+        uint32_t raw[kNW];
+        if (cs == E) {
 #pragma unroll
-            for (int q = 0; q < W; q++) {
-                uint4 const x = __ldg(reinterpret_cast<const uint4*>(p) + q);
-                uint32_t const wd[4] = { x.x, x.y, x.z, x.w };
-#pragma unroll
-                for (int m = 0; m < 4; m++) {
-                    if constexpr (W == 8) {
-                        if (m & 1) v[q * 2 + (m >> 1)] |= uint64_t(wd[m]) << 32;
-                        else v[q * 2 + (m >> 1)] = wd[m];
-                    } else if constexpr (W == 4) {
-                        v[q * 4 + m] = wd[m];
-                    } else if constexpr (W == 2) {
-                        v[q * 8 + 2 * m] = wd[m] & 0xffffu;
-                        v[q * 8 + 2 * m + 1] = wd[m] >> 16;
-                    } else {
-#pragma unroll
-                        for (int y = 0; y < 4; y++) v[q * 16 + 4 * m + y] = (wd[m] >> (8 * y)) & 0xffu;
-                    }
-                }
+            for (int b = 0; b < W; b++) {
+                if constexpr (PW >= 4) npLdq<PW / 4>(t.planes[b] + j0, raw + PW * b);
+                else npLd8(t.planes[b] + j0, raw + PW * b);
             }
         } else {
 #pragma unroll
-            for (int k = 0; k < kNPPer; k++) {
-                T x = 0;
-                if (j0 + k < nSrc)
-                    for (int y = 0; y < W; y++) x |= T(p[k * W + y]) << (8 * y);
-                v[k] = x;
+            for (int b = 0; b < W; b++) {
+                const uint8_t* const pl = t.planes[b] + j0;
+#pragma unroll
+                for (int m = 0; m < PW; m++) {
+                    uint32_t x = 0;
+#pragma unroll
+                    for (int y = 0; y < 4; y++)
+                        if (uint32_t(4 * m + y) < cs) x |= uint32_t(pl[4 * m + y]) << (8 * y);
+                    raw[PW * b + m] = x;
+                }
+            }
+        }
+        if constexpr (W == 1) {
+#pragma unroll
+            for (int m = 0; m < kNW; m++) w[m] = raw[m];
+        } else if constexpr (W == 2) {
+#pragma unroll
+            for (int m = 0; m < kNW; m++) w[m] = __byte_perm(raw[m >> 1], raw[PW + (m >> 1)], (m & 1) ? 0x7362 : 0x5140);
+        } else {
+            // 4x4 byte transposes of planes 0-3 (and 4-7 for the high words)
+#pragma unroll
+            for (int h = 0; h < W / 4; h++) {
+#pragma unroll
+                for (int g = 0; g < PW; g++) {
+                    uint32_t const* const pl = raw + PW * (4 * h);
+                    uint32_t const p0 = pl[g], p1 = pl[PW + g], p2 = pl[2 * PW + g], p3 = pl[3 * PW + g];
+                    uint32_t const t0 = __byte_perm(p0, p1, 0x5140), t1 = __byte_perm(p0, p1, 0x7362);
+                    uint32_t const t2 = __byte_perm(p2, p3, 0x5140), t3 = __byte_perm(p2, p3, 0x7362);
+                    uint32_t const e[4] = { __byte_perm(t0, t2, 0x5410), __byte_perm(t0, t2, 0x7632),
+                                            __byte_perm(t1, t3, 0x5410), __byte_perm(t1, t3, 0x7632) };
+#pragma unroll
+                    for (int j = 0; j < 4; j++) w[(W / 4) * (4 * g + j) + h] = e[j];
+                }
             }
         }
     } else {
-        // LSB-first fields of nbBits (1..64) over aligned 32-bit words
+        // LSB-first fields of nbBits (1..8W) from the staged words
         uint32_t const nb = t.nbBits;
-        uintptr_t const a = reinterpret_cast<uintptr_t>(t.src) & ~uintptr_t(3);
-        const uint32_t* const wds = reinterpret_cast<const uint32_t*>(a);
-        uint64_t const bit0 = (reinterpret_cast<uintptr_t>(t.src) - a) * 8 + j0 * nb;
 #pragma unroll
-        for (int k = 0; k < kNPPer; k++) {
-            T x = 0;
-            if (j0 + k < nSrc) {
-                uint64_t const bit = bit0 + uint64_t(k) * nb;
-                uint64_t const q = bit >> 5;
-                uint32_t const r = uint32_t(bit & 31);
-                uint32_t const w0 = __ldg(wds + q);
-                uint32_t const w1 = (r + nb > 32) ? __ldg(wds + q + 1) : 0u;
-                uint64_t lo = __funnelshift_r(w0, w1, r);
-                if (r + nb > 64) {
-                    uint32_t const w2 = __ldg(wds + q + 2);
-                    lo |= uint64_t(__funnelshift_r(w1, w2, r)) << 32;
-                } else if (nb > 32) {
-                    lo |= uint64_t(w1 >> r) << 32;
-                }
-                if (nb < 64) lo &= (1ull << nb) - 1;
-                x = T(lo);
+        for (int m = 0; m < kNW; m++) w[m] = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < E; k++) {
+            uint64_t x = 0;
+            if (k < cs) {
+                uint32_t const bit = sbit + (tileRel + k) * nb;
+                uint32_t const q = bit >> 5, r = bit & 31;
+                uint32_t const w0 = stage[npPad(q)];
+                uint32_t const w1 = (r + nb > 32) ? stage[npPad(q + 1)] : 0u;
+                x = __funnelshift_r(w0, w1, r);
+                if (r + nb > 64) x |= uint64_t(__funnelshift_r(w1, stage[npPad(q + 2)], r)) << 32;
+                else if (nb > 32) x |= uint64_t(w1 >> r) << 32;
+                if (nb < 64) x &= (1ull << nb) - 1;
             }
-            v[k] = x;
+            if constexpr (W == 1) w[k >> 2] |= uint32_t(x) << (8 * (k & 3));
+            else if constexpr (W == 2) w[k >> 1] |= uint32_t(x) << (16 * (k & 1));
+            else if constexpr (W == 4) w[k] = uint32_t(x);
+            else {
+                w[2 * k] = uint32_t(x);
+                w[2 * k + 1] = uint32_t(x >> 32);
+            }
         }
     }
 }
 
 template <int W>
-__device__ __forceinline__ void npStore(uint8_t* out, uint32_t cnt, const typename NPVal<W>::T (&v)[kNPPer])
+__device__ __forceinline__ void npZigzag(uint32_t (&w)[kNW])
 {
-    if (cnt == kNPPer && !(reinterpret_cast<uintptr_t>(out) & 15)) {
 #pragma unroll
-        for (int q = 0; q < W; q++) {
-            uint32_t wd[4];
+    for (int m = 0; m < kNW; m++) {
+        uint32_t const x = w[m];
+        if constexpr (W == 1) w[m] = ((x >> 1) & 0x7f7f7f7fu) ^ ((x & 0x01010101u) * 0xffu);
+        else if constexpr (W == 2) w[m] = ((x >> 1) & 0x7fff7fffu) ^ ((x & 0x00010001u) * 0xffffu);
+        else if constexpr (W == 4) w[m] = (x >> 1) ^ (0u - (x & 1u));
+    }
+    if constexpr (W == 8) {
 #pragma unroll
-            for (int m = 0; m < 4; m++) {
-                if constexpr (W == 8) {
-                    wd[m] = (m & 1) ? uint32_t(v[q * 2 + (m >> 1)] >> 32) : uint32_t(v[q * 2 + (m >> 1)]);
-                } else if constexpr (W == 4) {
-                    wd[m] = v[q * 4 + m];
-                } else if constexpr (W == 2) {
-                    wd[m] = (v[q * 8 + 2 * m] & 0xffffu) | (v[q * 8 + 2 * m + 1] << 16);
-                } else {
-                    wd[m] = (v[q * 16 + 4 * m] & 0xffu) | ((v[q * 16 + 4 * m + 1] & 0xffu) << 8)
-                            | ((v[q * 16 + 4 * m + 2] & 0xffu) << 16) | (v[q * 16 + 4 * m + 3] << 24);
-                }
-            }
-            reinterpret_cast<uint4*>(out)[q] = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+        for (int m = 0; m < kNW; m += 2) {
+            uint64_t const v = uint64_t(w[m]) | (uint64_t(w[m + 1]) << 32);
+            uint64_t const z = (v >> 1) ^ (0ull - (v & 1ull));
+            w[m] = uint32_t(z);
+            w[m + 1] = uint32_t(z >> 32);
         }
-    } else {
-#pragma unroll
-        for (int k = 0; k < kNPPer; k++)
-            if (uint32_t(k) < cnt)
-                for (int y = 0; y < W; y++) out[k * W + y] = uint8_t(uint64_t(v[k]) >> (8 * y));
     }
 }
 
-template <int W, int MODE>
-__device__ __forceinline__ void npReduceTile(const NumPipeTask& t, const TileRef& tr, uint64_t* sums, uint32_t g)
+// sum of the thread's elements (modulo 2^(8W) after masking)
+template <int W>
+__device__ __forceinline__ uint64_t npSum(const uint32_t (&w)[kNW])
 {
-    using T = typename NPVal<W>::T;
-    __shared__ uint64_t warpSum[kNPThreads / 32];
-    uint32_t const tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    uint64_t const e0 = uint64_t(tr.tile) * kTileElems + uint64_t(tid) * kNPPer;
-    uint64_t const nSrc = t.n ? t.n - 1 : 0;
-    T v[kNPPer];
-    npLoad<W, MODE>(t, e0, nSrc, v);
-    uint64_t acc = 0;
+    if constexpr (W == 1) {
+        uint32_t acc = 0;
 #pragma unroll
-    for (int k = 0; k < kNPPer; k++) {
-        T x = v[k];
-        if (t.zigzag) x = npMask<W>((x >> 1) ^ (T(0) - (x & 1)));
-        acc += x;
+        for (int m = 0; m < kNW; m++) acc = __vadd4(acc, w[m]);
+        return (acc & 0xff) + ((acc >> 8) & 0xff) + ((acc >> 16) & 0xff) + (acc >> 24);
+    } else if constexpr (W == 2) {
+        uint32_t acc = 0;
+#pragma unroll
+        for (int m = 0; m < kNW; m++) acc = __vadd2(acc, w[m]);
+        return (acc & 0xffff) + (acc >> 16);
+    } else if constexpr (W == 4) {
+        uint32_t acc = 0;
+#pragma unroll
+        for (int m = 0; m < kNW; m++) acc += w[m];
+        return acc;
+    } else {
+        uint64_t acc = 0;
+#pragma unroll
+        for (int m = 0; m < kNW; m += 2) acc += uint64_t(w[m]) | (uint64_t(w[m + 1]) << 32);
+        return acc;
     }
+}
+
+// exclusive scan of the thread's elements in place
+template <int W>
+__device__ __forceinline__ void npScan(uint32_t (&w)[kNW])
+{
+    if constexpr (W == 1) {
+        uint32_t c = 0;
+#pragma unroll
+        for (int m = 0; m < kNW; m++) {
+            uint32_t p = __vadd4(w[m], w[m] << 8);
+            p = __vadd4(p, p << 16);
+            w[m] = __vadd4(p << 8, c * 0x01010101u);
+            c = (c + (p >> 24)) & 0xffu;
+        }
+    } else if constexpr (W == 2) {
+        uint32_t c = 0;
+#pragma unroll
+        for (int m = 0; m < kNW; m++) {
+            uint32_t const p = __vadd2(w[m], w[m] << 16);
+            w[m] = __vadd2(p << 16, c * 0x00010001u);
+            c = (c + (p >> 16)) & 0xffffu;
+        }
+    } else if constexpr (W == 4) {
+        uint32_t c = 0;
+#pragma unroll
+        for (int m = 0; m < kNW; m++) {
+            uint32_t const x = w[m];
+            w[m] = c;
+            c += x;
+        }
+    } else {
+        uint64_t c = 0;
+#pragma unroll
+        for (int m = 0; m < kNW; m += 2) {
+            uint64_t const x = uint64_t(w[m]) | (uint64_t(w[m + 1]) << 32);
+            w[m] = uint32_t(c);
+            w[m + 1] = uint32_t(c >> 32);
+            c += x;
+        }
+    }
+}
+
+// adds `add` (modulo 2^(8W)) to every element
+template <int W>
+__device__ __forceinline__ void npAdd(uint32_t (&w)[kNW], uint64_t add)
+{
+    if constexpr (W == 1) {
+        uint32_t const a = uint32_t(add & 0xff) * 0x01010101u;
+#pragma unroll
+        for (int m = 0; m < kNW; m++) w[m] = __vadd4(w[m], a);
+    } else if constexpr (W == 2) {
+        uint32_t const a = uint32_t(add & 0xffff) * 0x00010001u;
+#pragma unroll
+        for (int m = 0; m < kNW; m++) w[m] = __vadd2(w[m], a);
+    } else if constexpr (W == 4) {
+#pragma unroll
+        for (int m = 0; m < kNW; m++) w[m] += uint32_t(add);
+    } else {
+#pragma unroll
+        for (int m = 0; m < kNW; m += 2) {
+            uint64_t const v = (uint64_t(w[m]) | (uint64_t(w[m + 1]) << 32)) + add;
+            w[m] = uint32_t(v);
+            w[m + 1] = uint32_t(v >> 32);
+        }
+    }
+}
+
+// Stages the tile's bit-packed source in shared memory (padded words): the
+// 16-byte blocks from the one holding the tile's first field to the one
+// holding its last source bit. Returns the bit offset of the first field.
+__device__ __forceinline__ uint32_t npStage(const NumPipeTask& t, uint64_t e0, uint64_t nSrc, uint32_t te,
+                                            uint32_t* stage)
+{
+    uint64_t const firstBit = uint64_t(reinterpret_cast<uintptr_t>(t.src) & 15) * 8 + e0 * t.nbBits;
+    uintptr_t const a = (reinterpret_cast<uintptr_t>(t.src) & ~uintptr_t(15)) + (firstBit >> 7) * 16;
+    uint32_t const sbit = uint32_t(firstBit & 127);
+    uint64_t const nFields = e0 < nSrc ? umin64(te, nSrc - e0) : 0;
+    uint32_t const nq = nFields ? uint32_t((sbit + nFields * t.nbBits + 127) >> 7) : 0u;
+    const uint4* const src = reinterpret_cast<const uint4*>(a);
+    for (uint32_t q = threadIdx.x; q < nq; q += kNPThreads) {
+        uint4 const u = __ldg(src + q);
+        uint32_t const d = npPad(4 * q); // a block never straddles a pad word
+        stage[d] = u.x;
+        stage[d + 1] = u.y;
+        stage[d + 2] = u.z;
+        stage[d + 3] = u.w;
+    }
+    __syncthreads();
+    return sbit;
+}
+
+template <int W>
+__device__ __forceinline__ void npStore(uint8_t* out, uint32_t cnt, const uint32_t (&w)[kNW])
+{
+    constexpr uint32_t E = kNPBytes / W;
+    if (cnt == E && !(reinterpret_cast<uintptr_t>(out) & 15)) {
+#pragma unroll
+        for (int q = 0; q < kNW / 4; q++)
+            reinterpret_cast<uint4*>(out)[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < int(kNPBytes); k++)
+            if (uint32_t(k) < cnt * W) out[k] = uint8_t(w[k >> 2] >> (8 * (k & 3)));
+    }
+}
+
+// shared scratch of one tile
+struct NPShared {
+    uint32_t stage[kNPStagePadded];
+    uint64_t warpVal[kNPThreads / 32];
+};
+
+template <int W, int MODE>
+__device__ __forceinline__ void npReduceTile(const NumPipeTask& t, const TileRef& tr, uint64_t* sums, uint32_t g,
+                                             NPShared& sh)
+{
+    constexpr uint32_t TE = kNumTileBytes / W, E = kNPBytes / W;
+    uint32_t const tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint64_t const e0 = uint64_t(tr.tile) * TE;
+    uint64_t const nSrc = t.n ? t.n - 1 : 0;
+    uint32_t sbit = 0;
+    if constexpr (MODE == SRC_BITPACK) sbit = npStage(t, e0, nSrc, TE, sh.stage);
+    uint32_t w[kNW];
+    npLoad<W, MODE>(t, e0 + uint64_t(tid) * E, nSrc, sh.stage, sbit, tid * E, w);
+    if (t.zigzag) npZigzag<W>(w);
+    uint64_t acc = npSum<W>(w);
 #pragma unroll
     for (int m = 16; m > 0; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
-    if (lane == 0) warpSum[wid] = acc;
+    if (lane == 0) sh.warpVal[wid] = acc;
     __syncthreads();
     if (tid == 0) {
         uint64_t tot = 0;
 #pragma unroll
-        for (int w2 = 0; w2 < kNPThreads / 32; w2++) tot += warpSum[w2];
+        for (int w2 = 0; w2 < kNPThreads / 32; w2++) tot += sh.warpVal[w2];
         sums[g] = tot;
     }
 }
 
 template <int W, int MODE>
-__device__ __forceinline__ void npTile(const NumPipeTask& t, const TileRef& tr, uint32_t g, const uint64_t* prefix)
+__device__ __forceinline__ void npTile(const NumPipeTask& t, const TileRef& tr, uint32_t g, const uint64_t* prefix,
+                                       NPShared& sh)
 {
-    using T = typename NPVal<W>::T;
-    __shared__ uint64_t warpTot[kNPThreads / 32];
+    constexpr uint32_t TE = kNumTileBytes / W, E = kNPBytes / W;
     uint32_t const tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    uint64_t const e0 = uint64_t(tr.tile) * kTileElems + uint64_t(tid) * kNPPer;
-    uint32_t const cnt = e0 < t.n ? uint32_t(umin64(kNPPer, t.n - e0)) : 0;
+    uint64_t const e0 = uint64_t(tr.tile) * TE;
+    uint64_t const j0 = e0 + uint64_t(tid) * E;
+    uint32_t const cnt = j0 < t.n ? uint32_t(umin64(E, t.n - j0)) : 0;
     uint64_t const nSrc = t.delta ? (t.n ? t.n - 1 : 0) : t.n;
-    T v[kNPPer];
-    npLoad<W, MODE>(t, e0, nSrc, v);
-    if (t.zigzag) {
-#pragma unroll
-        for (int k = 0; k < kNPPer; k++) v[k] = npMask<W>((v[k] >> 1) ^ (T(0) - (v[k] & 1)));
-    }
+    uint32_t sbit = 0;
+    if constexpr (MODE == SRC_BITPACK) sbit = npStage(t, e0, nSrc, TE, sh.stage);
+    uint32_t w[kNW];
+    npLoad<W, MODE>(t, j0, nSrc, sh.stage, sbit, tid * E, w);
+    if (t.zigzag) npZigzag<W>(w);
     if (t.delta) {
-        // exclusive scan within the thread
-        T acc = 0;
-#pragma unroll
-        for (int k = 0; k < kNPPer; k++) {
-            T const x = v[k];
-            v[k] = acc;
-            acc += x;
-        }
+        uint64_t const tot = npSum<W>(w);
+        npScan<W>(w);
         // exclusive scan of thread totals within the warp, then across warps
-        uint64_t incl = acc;
+        uint64_t incl = tot;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             uint64_t const y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= uint32_t(o)) incl += y;
         }
-        if (lane == 31) warpTot[wid] = incl;
+        if (lane == 31) sh.warpVal[wid] = incl;
         __syncthreads();
         uint64_t warpPre = 0;
 #pragma unroll
-        for (int w2 = 0; w2 < kNPThreads / 32; w2++) warpPre += uint32_t(w2) < wid ? warpTot[w2] : 0;
-        T const add = T(t.first + prefix[g] + warpPre + (incl - acc));
-#pragma unroll
-        for (int k = 0; k < kNPPer; k++) v[k] = npMask<W>(T(v[k] + add));
+        for (int w2 = 0; w2 < kNPThreads / 32; w2++) warpPre += uint32_t(w2) < wid ? sh.warpVal[w2] : 0;
+        npAdd<W>(w, t.first + prefix[g] + warpPre + (incl - tot));
     }
-    if (cnt) npStore<W>(t.out + e0 * W, cnt, v);
+    if (cnt) npStore<W>(t.out + j0 * W, cnt, w);
 }
 
 template <int W>
-__device__ __forceinline__ void npTileW(const NumPipeTask& t, const TileRef& tr, uint32_t g, const uint64_t* prefix)
+__device__ __forceinline__ void npTileW(const NumPipeTask& t, const TileRef& tr, uint32_t g, const uint64_t* prefix,
+                                        NPShared& sh)
 {
     switch (t.srcMode) {
-        case SRC_PLAIN: npTile<W, SRC_PLAIN>(t, tr, g, prefix); break;
-        case SRC_PLANES: npTile<W, SRC_PLANES>(t, tr, g, prefix); break;
-        default: npTile<W, SRC_BITPACK>(t, tr, g, prefix); break;
+        case SRC_PLAIN: npTile<W, SRC_PLAIN>(t, tr, g, prefix, sh); break;
+        case SRC_PLANES: npTile<W, SRC_PLANES>(t, tr, g, prefix, sh); break;
+        default: npTile<W, SRC_BITPACK>(t, tr, g, prefix, sh); break;
     }
 }
 
 template <int W>
-__device__ __forceinline__ void npReduceW(const NumPipeTask& t, const TileRef& tr, uint64_t* sums, uint32_t g)
+__device__ __forceinline__ void npReduceW(const NumPipeTask& t, const TileRef& tr, uint64_t* sums, uint32_t g,
+                                          NPShared& sh)
 {
     switch (t.srcMode) {
-        case SRC_PLAIN: npReduceTile<W, SRC_PLAIN>(t, tr, sums, g); break;
-        case SRC_PLANES: npReduceTile<W, SRC_PLANES>(t, tr, sums, g); break;
-        default: npReduceTile<W, SRC_BITPACK>(t, tr, sums, g); break;
+        case SRC_PLAIN: npReduceTile<W, SRC_PLAIN>(t, tr, sums, g, sh); break;
+        case SRC_PLANES: npReduceTile<W, SRC_PLANES>(t, tr, sums, g, sh); break;
+        default: npReduceTile<W, SRC_BITPACK>(t, tr, sums, g, sh); break;
     }
 }
 
@@ -392,15 +572,16 @@ __global__ void __launch_bounds__(kNPThreads) kNumReduce(const NumPipeTask* __re
                                                          const TileRef* __restrict__ tiles,
                                                          uint64_t* __restrict__ sums)
 {
+    __shared__ NPShared sh;
     uint32_t const g = blockIdx.x;
     TileRef const tr = tiles[g];
     NumPipeTask const t = tasks[tr.task];
     if (!t.delta) return;
     switch (t.w) {
-        case 1: npReduceW<1>(t, tr, sums, g); break;
-        case 2: npReduceW<2>(t, tr, sums, g); break;
-        case 4: npReduceW<4>(t, tr, sums, g); break;
-        default: npReduceW<8>(t, tr, sums, g); break;
+        case 1: npReduceW<1>(t, tr, sums, g, sh); break;
+        case 2: npReduceW<2>(t, tr, sums, g, sh); break;
+        case 4: npReduceW<4>(t, tr, sums, g, sh); break;
+        default: npReduceW<8>(t, tr, sums, g, sh); break;
     }
 }
 
@@ -413,7 +594,8 @@ __global__ void __launch_bounds__(256) kNumPrefix(const NumPipeTask* __restrict_
     if (ti >= nbTasks) return;
     NumPipeTask const t = tasks[ti];
     if (!t.delta) return;
-    uint32_t const nT = uint32_t((t.n + kTileElems - 1) / kTileElems);
+    uint32_t const te = kNumTileBytes / t.w;
+    uint32_t const nT = uint32_t((t.n + te - 1) / te);
     uint64_t running = 0;
     for (uint32_t k0 = 0; k0 < nT; k0 += 32) {
         uint32_t const k = k0 + lane;
@@ -434,14 +616,15 @@ __global__ void __launch_bounds__(kNPThreads) kNumPipe(const NumPipeTask* __rest
                                                        const TileRef* __restrict__ tiles,
                                                        const uint64_t* __restrict__ prefix)
 {
+    __shared__ NPShared sh;
     uint32_t const g = blockIdx.x;
     TileRef const tr = tiles[g];
     NumPipeTask const t = tasks[tr.task];
     switch (t.w) {
-        case 1: npTileW<1>(t, tr, g, prefix); break;
-        case 2: npTileW<2>(t, tr, g, prefix); break;
-        case 4: npTileW<4>(t, tr, g, prefix); break;
-        default: npTileW<8>(t, tr, g, prefix); break;
+        case 1: npTileW<1>(t, tr, g, prefix, sh); break;
+        case 2: npTileW<2>(t, tr, g, prefix, sh); break;
+        case 4: npTileW<4>(t, tr, g, prefix, sh); break;
+        default: npTileW<8>(t, tr, g, prefix, sh); break;
     }
 }
 
