@@ -685,19 +685,56 @@ __global__ void kFloatDec(const FloatDecTask* __restrict__ tasks, const TileRef*
 
 // ---------------------------------------------------------------------------
 // flatpack: alphabet + LSB-first indices terminated by a 1 bit
-__global__ void kFlatpack(const FlatpackTask* __restrict__ tasks, const TileRef* __restrict__ tiles,
-                          uint32_t* __restrict__ status)
+// Flatpack: out[i] = alphabet[field i], fields of nbBits (1..8) LSB-first.
+// The alphabet sits in shared memory; each thread decodes 8 consecutive
+// fields from a 64-bit window (three aligned words of the packed stream,
+// funnel-shifted) and stores them with one 8-byte store. Only words that hold
+// bytes of the packed stream are read (its last word holds the terminator).
+__global__ void __launch_bounds__(256) kFlatpack(const FlatpackTask* __restrict__ tasks,
+                                                 const TileRef* __restrict__ tiles, uint32_t* __restrict__ status)
 {
+    __shared__ uint8_t sAlpha[256];
     TileRef const tr = tiles[blockIdx.x];
     FlatpackTask const t = tasks[tr.task];
+    uint32_t const as = min(t.alphabetSize, 256u);
+    for (uint32_t i = threadIdx.x; i < as; i += blockDim.x) sAlpha[i] = t.alphabet[i];
+    __syncthreads();
+    uint32_t const nb = t.nbBits, mask = (1u << nb) - 1u;
+    const uint32_t* const pw = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(t.packed) & ~uintptr_t(3));
+    uint64_t const sb = (reinterpret_cast<uintptr_t>(t.packed) & 3) * 8;
+    uint64_t const qLast = (sb + t.n * nb) >> 5;
     uint64_t const e0 = uint64_t(tr.tile) * kTileBytes;
     uint64_t const e1 = umin64(t.n, e0 + kTileBytes);
     bool bad = false;
-    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
-        uint64_t const bit = i * t.nbBits;
-        uint32_t v = uint32_t(ld64Any(t.packed + (bit >> 3)) >> (bit & 7)) & ((1u << t.nbBits) - 1);
-        if (v >= t.alphabetSize) { bad = true; v = 0; }
-        t.out[i] = t.alphabet[v];
+    for (uint64_t k0 = e0 + 8ull * threadIdx.x; k0 < e1; k0 += 8ull * blockDim.x) {
+        uint32_t const cnt = uint32_t(umin64(8, e1 - k0));
+        uint64_t const bit = sb + k0 * nb;
+        uint64_t const q = bit >> 5;
+        uint32_t const r = uint32_t(bit & 31);
+        uint32_t const w0 = __ldg(pw + q);
+        uint32_t const w1 = q + 1 <= qLast ? __ldg(pw + q + 1) : 0u;
+        uint32_t const w2 = q + 2 <= qLast ? __ldg(pw + q + 2) : 0u;
+        uint32_t const lo = __funnelshift_r(w0, w1, r), hi = __funnelshift_r(w1, w2, r);
+        uint32_t o[2] = { 0u, 0u };
+#pragma unroll
+        for (uint32_t j = 0; j < 8; j++) {
+            uint32_t const sh = j * nb;
+            uint32_t const f = (sh < 32 ? __funnelshift_r(lo, hi, sh) : hi >> (sh - 32)) & mask;
+            uint32_t v = 0;
+            if (j < cnt) {
+                if (f < as) v = sAlpha[f];
+                else bad = true;
+            }
+            o[j >> 2] |= v << (8 * (j & 3));
+        }
+        uint8_t* const dst = t.out + k0;
+        if (cnt == 8 && !(reinterpret_cast<uintptr_t>(dst) & 7)) {
+            *reinterpret_cast<uint2*>(dst) = make_uint2(o[0], o[1]);
+        } else {
+#pragma unroll
+            for (uint32_t j = 0; j < 8; j++)
+                if (j < cnt) dst[j] = uint8_t(o[j >> 2] >> (8 * (j & 3)));
+        }
     }
     if (tr.tile == 0 && threadIdx.x == 0) {
         // terminator: the bit after the last index is set and is the last set bit
@@ -1403,16 +1440,9 @@ __device__ __forceinline__ uint4 funnel16(uint4 c, uint4 n, uint32_t off)
     return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
-__global__ void __launch_bounds__(256) kHashBlocks(const HashTask* __restrict__ tasks,
-                                                   const TileRef* __restrict__ blocks, uint32_t nbBlocks)
+__device__ __forceinline__ void hashBlock(const HashTask* __restrict__ tasks, TileRef const br, const uint64_t* sKey,
+                                          uint32_t lane)
 {
-    __shared__ uint64_t sKey[24]; // secret words at byte offsets 0, 8, ..., 184
-    if (threadIdx.x < 24) sKey[threadIdx.x] = secret64(int(8 * threadIdx.x));
-    __syncthreads();
-    uint32_t const warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t const lane = threadIdx.x & 31;
-    if (warp >= nbBlocks) return;
-    TileRef const br = blocks[warp];
     HashTask const t = tasks[br.task];
     const uint8_t* const blk = t.data + uint64_t(br.tile) * kHashBlock;
     uintptr_t const base = reinterpret_cast<uintptr_t>(blk) & ~uintptr_t(15);
@@ -1458,6 +1488,21 @@ __global__ void __launch_bounds__(256) kHashBlocks(const HashTask* __restrict__ 
         t.blockSums[8ull * br.tile + 2 * lane + 1] = a1;
     }
 }
+
+__global__ void __launch_bounds__(256) kHashBlocks(const HashTask* __restrict__ tasks,
+                                                   const TileRef* __restrict__ blocks, uint32_t nbBlocks)
+{
+    __shared__ uint64_t sKey[24]; // secret words at byte offsets 0, 8, ..., 184
+    if (threadIdx.x < 24) sKey[threadIdx.x] = secret64(int(8 * threadIdx.x));
+    __syncthreads();
+    uint32_t const lane = threadIdx.x & 31;
+    // grid-stride over the blocks, one warp per block at a time: the secret
+    // is staged once per CTA
+    uint32_t const nw = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); warp < nbBlocks; warp += nw)
+        hashBlock(tasks, blocks[warp], sKey, lane);
+}
+
 
 // Phase 2: one warp per task. Lane i (and its copies i + 8, i + 16, i + 24)
 // runs the block chain of accumulator i, then the trailing partial stripes
@@ -1559,6 +1604,21 @@ uint32_t fseLanes(uint32_t tlMax)
     return lanes;
 }
 uint32_t hufSmem(uint32_t chunks) { return hufRingOff(chunks) + 4 * chunks * 16 * kHufRing; }
+// kHashBlocks grid: one warp per block up to eight full CTAs per SM, then
+// grid-stride (any grid size is correct)
+uint32_t hashGrid(uint32_t nbBlocks)
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0, n = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+            sms = n;
+        if (sms <= 0) sms = 152;
+    }
+    uint32_t const want = (nbBlocks + 7) / 8;
+    uint32_t const cap = uint32_t(sms) * 8;
+    return want < cap ? (want ? want : 1) : cap;
+}
 static_assert(2 * kHufSlotBytes >= (2u << kHufTableLog), "a tableLog-12 table fits two slots");
 } // namespace
 
@@ -1651,8 +1711,8 @@ long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dSc
             }
             case KIND_HASH: {
                 if (l.nbTiles) {
-                    uint32_t const grid = (l.nbTiles * 32 + 255) / 256;
-                    kHashBlocks<<<grid, 256, 0, s>>>(static_cast<const HashTask*>(tasks), tiles, l.nbTiles);
+                    kHashBlocks<<<hashGrid(l.nbTiles), 256, 0, s>>>(static_cast<const HashTask*>(tasks), tiles,
+                                                                   l.nbTiles);
                     count++;
                 }
                 uint32_t const grid = (l.nbTasks * 32 + 255) / 256;
@@ -1681,7 +1741,7 @@ void launchCopy(const CopyTask* tasks, const TileRef* tiles, uint32_t nbTiles, c
 void launchHash(const HashTask* tasks, uint32_t nbTasks, const TileRef* blocks, uint32_t nbBlocks, uint32_t* status,
                 cudaStream_t s)
 {
-    if (nbBlocks) kHashBlocks<<<(nbBlocks * 32 + 255) / 256, 256, 0, s>>>(tasks, blocks, nbBlocks);
+    if (nbBlocks) kHashBlocks<<<hashGrid(nbBlocks), 256, 0, s>>>(tasks, blocks, nbBlocks);
     if (nbTasks) kHashFinish<<<(nbTasks * 32 + 255) / 256, 256, 0, s>>>(tasks, nbTasks, status);
 }
 
@@ -1707,7 +1767,7 @@ cudaError_t xxh3Device(const uint8_t* data, uint64_t len, uint64_t* dHashOut, ui
         for (uint32_t k = 0; k < nbBlocks; k++) tiles[k] = TileRef{ 0, k };
         e = cudaMemcpyAsync(dTiles, tiles.data(), nbBlocks * sizeof(TileRef), cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) return e;
-        kHashBlocks<<<(nbBlocks * 32 + 255) / 256, 256, 0, s>>>(dTask, dTiles, nbBlocks);
+        kHashBlocks<<<hashGrid(nbBlocks), 256, 0, s>>>(dTask, dTiles, nbBlocks);
     }
     kHashFinish<<<1, 32, 0, s>>>(dTask, 1, nullptr);
     e = cudaGetLastError();
@@ -1797,7 +1857,7 @@ extern "C" ZL_Report ozl_gpu_xxh3_64_static(const void* d_data, size_t len, void
     t.hashOut = dResult;
     uint32_t const stageThreads = nbBlocks > 0 ? nbBlocks : 1;
     kStageHashStatic<<<(stageThreads + 255) / 256, 256, 0, s>>>(t, dTask, dBlocks, nbBlocks, dResult);
-    if (nbBlocks) ozl::kHashBlocks<<<(nbBlocks * 32 + 255) / 256, 256, 0, s>>>(dTask, dBlocks, nbBlocks);
+    if (nbBlocks) ozl::kHashBlocks<<<ozl::hashGrid(nbBlocks), 256, 0, s>>>(dTask, dBlocks, nbBlocks);
     ozl::kHashFinish<<<1, 32, 0, s>>>(dTask, 1, nullptr);
     if (cudaGetLastError() != cudaSuccess) return ZL_Report{ ZL_ErrorCode_GENERIC, 0 };
     uint64_t h = 0;
