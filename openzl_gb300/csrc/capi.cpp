@@ -392,16 +392,7 @@ ZL_Report ozl_gpu_batch_run_host(OZL_GpuBatch* b, const void* h_in, size_t inByt
                                  void* stream, int useGraph)
 {
     if (!b || b->dFrames.empty()) return fail(ZL_ErrorCode_parameter_invalid);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (inBytes
-        && cudaMemcpyAsync(const_cast<uint8_t*>(b->dFrames[0]), h_in, inBytes, cudaMemcpyHostToDevice, s)
-                   != cudaSuccess)
-        return fail(ZL_ErrorCode_GENERIC);
-    ZL_Report r = b->run(s, useGraph != 0);
-    if (ZL_isError(r)) return r;
-    if (outBytes && cudaMemcpyAsync(h_out, b->dOuts[0], outBytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
-        return fail(ZL_ErrorCode_GENERIC);
-    return b->check(s);
+    return b->runHost(h_in, inBytes, h_out, outBytes, static_cast<cudaStream_t>(stream), useGraph != 0);
 }
 
 const size_t* ozl_gpu_batch_sizes(const OZL_GpuBatch* b) { return b ? b->sizes.data() : nullptr; }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -79,6 +80,49 @@ struct DecodeBatch {
     cudaEvent_t fork = nullptr, join[kMaxParts] = {};
     std::string err;
 
+    // Host-buffer runs (ozl_gpu_batch_run_host): the frames split into
+    // rounds of contiguous frames. Each round's frames go up on one copy
+    // stream, the round decodes on its own stream as soon as they are in
+    // (rounds share the SMs), and its outputs go down on a second copy stream
+    // as soon as it is done, so both copy directions overlap the decode.
+    struct HostPipe {
+        static constexpr int kRounds = 8;
+        std::vector<Part> rounds;
+        std::vector<size_t> inOff, outOff; // round boundaries in the input / output images
+        bool ready = false, uploaded = false;
+        cudaStream_t sIn = nullptr, sOut = nullptr, rs[kRounds] = {};
+        cudaEvent_t start = nullptr, inEv[kRounds] = {}, decEv[kRounds] = {}, outDone = nullptr;
+        cudaGraphExec_t graph = nullptr;
+        const void* gIn = nullptr;
+        void* gOut = nullptr;
+        size_t gInBytes = 0, gOutBytes = 0;
+        cudaStream_t gStream = nullptr;
+        void dropGraph()
+        {
+            if (graph) cudaGraphExecDestroy(graph);
+            graph = nullptr;
+        }
+        void reset()
+        {
+            dropGraph();
+            rounds.clear();
+            ready = uploaded = false;
+        }
+        ~HostPipe()
+        {
+            dropGraph();
+            if (sIn) cudaStreamDestroy(sIn);
+            if (sOut) cudaStreamDestroy(sOut);
+            for (int r = 0; r < kRounds; r++) {
+                if (rs[r]) cudaStreamDestroy(rs[r]);
+                if (inEv[r]) cudaEventDestroy(inEv[r]);
+                if (decEv[r]) cudaEventDestroy(decEv[r]);
+            }
+            if (start) cudaEventDestroy(start);
+            if (outDone) cudaEventDestroy(outDone);
+        }
+    } host;
+
     ~DecodeBatch()
     {
         dropGraph();
@@ -118,6 +162,7 @@ struct DecodeBatch {
                        void* const* dO, const size_t* caps)
     {
         dropGraph();
+        host.reset();
         if (prepareOnce() != cudaSuccess) { err = "kernel attributes could not be set"; return reportFail(ZL_ErrorCode_GENERIC); }
         int rc = plan.build(n, reinterpret_cast<const uint8_t* const*>(hF), fs, caps, checkContent,
                             checkCompressed, err);
@@ -191,7 +236,10 @@ struct DecodeBatch {
 
     ZL_Report enqueue(cudaStream_t s)
     {
-        if (cudaMemsetAsync(status.data(), 0, 4, s) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
+        if (cudaMemsetAsync(status.data(), 0, 4, s) != cudaSuccess) {
+            err = "status reset failed";
+            return reportFail(ZL_ErrorCode_GENERIC);
+        }
         uint32_t* const st = reinterpret_cast<uint32_t*>(status.data());
         size_t const np = parts.size();
         if (np > 1) {
@@ -298,6 +346,177 @@ struct DecodeBatch {
         dropGraph();
         if (cudaStreamSynchronize(s) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
         return reportOk(tuned);
+    }
+
+    // Rounds for host-buffer runs: frames must be laid out in order in both
+    // images (increasing device addresses inside [0, inBytes) and
+    // [0, outBytes)); otherwise returns false and the caller runs the copies
+    // and the decode one after another.
+    bool buildRounds(size_t inBytes, size_t outBytes)
+    {
+        size_t const n = dFrames.size();
+        if (n < 2) return false;
+        for (size_t i = 0; i < n; i++) {
+            size_t const fi = size_t(dFrames[i] - dFrames[0]), oi = size_t(dOuts[i] - dOuts[0]);
+            if (dFrames[i] < dFrames[0] || dOuts[i] < dOuts[0] || fi >= inBytes || oi + sizes[i] > outBytes) return false;
+            if (i && (dFrames[i] < dFrames[i - 1] || dOuts[i] < dOuts[i - 1] + sizes[i - 1])) return false;
+        }
+        if (host.ready) return true;
+        int const K = int(std::min<size_t>(HostPipe::kRounds, n));
+        uint64_t const target = (plan.totalOut + K - 1) / K;
+        std::vector<size_t> first{ 0 };
+        uint64_t acc = 0;
+        for (size_t i = 0; i + 1 < n && int(first.size()) < K; i++) {
+            acc += sizes[i];
+            if (acc >= target * first.size()) first.push_back(i + 1);
+        }
+        first.push_back(n);
+        size_t const nr = first.size() - 1;
+        host.rounds.assign(nr, Part{});
+        host.inOff.assign(nr + 1, 0);
+        host.outOff.assign(nr + 1, 0);
+        for (size_t r = 0; r < nr; r++) {
+            Part& p = host.rounds[r];
+            p.mask.assign(n, 0);
+            for (size_t i = first[r]; i < first[r + 1]; i++) p.mask[i] = 1;
+            int rc = layoutPlan(plan, dFrames.data(), dOuts.data(), nullptr, nullptr, nullptr, nullptr, p.layout, err,
+                                &p.mask);
+            if (rc) return false;
+            if (!p.pool.reserve(p.layout.pool.size()) || !p.scratch.reserve(p.layout.scratchBytes)) return false;
+            rc = layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), p.scratch.data(),
+                            p.pool.data(), p.layout, err, &p.mask);
+            if (rc) return false;
+            host.inOff[r] = size_t(dFrames[first[r]] - dFrames[0]);
+            host.outOff[r] = size_t(dOuts[first[r]] - dOuts[0]);
+        }
+        host.inOff[nr] = inBytes;
+        host.outOff[nr] = outBytes;
+        // earlier rounds decode at higher stream priority, so they finish
+        // first and their outputs start down while later rounds fill the SMs
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) least = greatest = 0;
+        auto mkStream = [](cudaStream_t& x, int prio) {
+            return x || cudaStreamCreateWithPriority(&x, cudaStreamNonBlocking, prio) == cudaSuccess;
+        };
+        auto mkEvent = [](cudaEvent_t& x) { return x || cudaEventCreateWithFlags(&x, cudaEventDisableTiming) == cudaSuccess; };
+        bool ok = mkStream(host.sIn, greatest) && mkStream(host.sOut, greatest) && mkEvent(host.start)
+                  && mkEvent(host.outDone);
+        for (size_t r = 0; r < nr && ok; r++) {
+            int const prio = nr > 1 ? greatest + int((int64_t(least) - greatest) * int64_t(r) / int64_t(nr - 1)) : greatest;
+            ok = mkStream(host.rs[r], prio) && mkEvent(host.inEv[r]) && mkEvent(host.decEv[r]);
+        }
+        if (!ok) return false;
+        host.ready = true;
+        host.uploaded = false;
+        return true;
+    }
+
+    ZL_Report enqueueHost(const void* hIn, void* hOut, cudaStream_t s)
+    {
+        size_t const nr = host.rounds.size();
+        uint8_t* const dIn = const_cast<uint8_t*>(dFrames[0]);
+        uint32_t* const st = reinterpret_cast<uint32_t*>(status.data());
+        bool ok = cudaMemsetAsync(st, 0, 4, s) == cudaSuccess && cudaEventRecord(host.start, s) == cudaSuccess
+                  && cudaStreamWaitEvent(host.sIn, host.start, 0) == cudaSuccess
+                  && cudaStreamWaitEvent(host.sOut, host.start, 0) == cudaSuccess;
+        for (size_t r = 0; r < nr && ok; r++) {
+            size_t const a = host.inOff[r], b = host.inOff[r + 1];
+            if (b > a)
+                ok = cudaMemcpyAsync(dIn + a, static_cast<const uint8_t*>(hIn) + a, b - a, cudaMemcpyHostToDevice,
+                                     host.sIn) == cudaSuccess;
+            ok = ok && cudaEventRecord(host.inEv[r], host.sIn) == cudaSuccess;
+        }
+        for (size_t r = 0; r < nr && ok; r++) {
+            Part& p = host.rounds[r];
+            ok = cudaStreamWaitEvent(host.rs[r], host.inEv[r], 0) == cudaSuccess
+                 && runLaunches(p.layout, p.pool.data(), p.scratch.data(), st, host.rs[r]) >= 0
+                 && cudaEventRecord(host.decEv[r], host.rs[r]) == cudaSuccess;
+        }
+        for (size_t r = 0; r < nr && ok; r++) {
+            size_t const a = host.outOff[r], b = host.outOff[r + 1];
+            ok = cudaStreamWaitEvent(host.sOut, host.decEv[r], 0) == cudaSuccess;
+            if (ok && b > a)
+                ok = cudaMemcpyAsync(static_cast<uint8_t*>(hOut) + a, dOuts[0] + a, b - a, cudaMemcpyDeviceToHost,
+                                     host.sOut) == cudaSuccess;
+        }
+        ok = ok && cudaEventRecord(host.outDone, host.sOut) == cudaSuccess
+             && cudaStreamWaitEvent(s, host.outDone, 0) == cudaSuccess
+             && cudaStreamWaitEvent(s, host.inEv[nr - 1], 0) == cudaSuccess;
+        for (size_t r = 0; r < nr && ok; r++) ok = cudaStreamWaitEvent(s, host.decEv[r], 0) == cudaSuccess;
+        if (!ok) {
+            err = std::string("host pipeline launch failed: ") + cudaGetErrorString(cudaGetLastError());
+            return reportFail(ZL_ErrorCode_GENERIC);
+        }
+        return reportOk(0);
+    }
+
+    // Copies the frames in from hIn, decodes and copies the outputs out to
+    // hOut, overlapped by rounds when the frames are laid out in order.
+    ZL_Report runHost(const void* hIn, size_t inBytes, void* hOut, size_t outBytes, cudaStream_t s, bool useGraph)
+    {
+        if (!buildRounds(inBytes, outBytes)) {
+            cudaError_t e = inBytes ? cudaMemcpyAsync(const_cast<uint8_t*>(dFrames[0]), hIn, inBytes,
+                                                      cudaMemcpyHostToDevice, s)
+                                    : cudaSuccess;
+            if (e != cudaSuccess) {
+                err = std::string("frame upload failed: ") + cudaGetErrorString(e);
+                return reportFail(ZL_ErrorCode_GENERIC);
+            }
+            ZL_Report r = run(s, useGraph);
+            if (ZL_isError(r)) return r;
+            e = outBytes ? cudaMemcpyAsync(hOut, dOuts[0], outBytes, cudaMemcpyDeviceToHost, s) : cudaSuccess;
+            if (e != cudaSuccess) {
+                err = std::string("output download failed: ") + cudaGetErrorString(e);
+                return reportFail(ZL_ErrorCode_GENERIC);
+            }
+            return check(s);
+        }
+        ZL_Report u = upload(s);
+        if (ZL_isError(u)) return u;
+        if (!host.uploaded) {
+            for (Part& p : host.rounds) {
+                if (p.layout.pool.empty()) continue;
+                cudaError_t const e = cudaMemcpyAsync(p.pool.data(), p.layout.pool.data(), p.layout.pool.size(),
+                                                      cudaMemcpyHostToDevice, s);
+                if (e != cudaSuccess) {
+                    err = std::string("round descriptor upload failed: ") + cudaGetErrorString(e);
+                    return reportFail(ZL_ErrorCode_GENERIC);
+                }
+            }
+            host.uploaded = true;
+        }
+        if (!useGraph) {
+            ZL_Report r = enqueueHost(hIn, hOut, s);
+            if (ZL_isError(r)) return r;
+            return check(s);
+        }
+        if (s == nullptr) {
+            err = "CUDA graph capture needs a non-default stream";
+            return reportFail(ZL_ErrorCode_parameter_invalid);
+        }
+        if (!host.graph || host.gIn != hIn || host.gOut != hOut || host.gInBytes != inBytes || host.gOutBytes != outBytes
+            || host.gStream != s) {
+            host.dropGraph();
+            cudaGraph_t g = nullptr;
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                err = "stream capture failed";
+                return reportFail(ZL_ErrorCode_GENERIC);
+            }
+            ZL_Report r = enqueueHost(hIn, hOut, s);
+            cudaError_t e = cudaStreamEndCapture(s, &g);
+            if (ZL_isError(r)) { if (g) cudaGraphDestroy(g); return r; }
+            if (e != cudaSuccess) { err = "stream capture failed"; return reportFail(ZL_ErrorCode_GENERIC); }
+            e = cudaGraphInstantiate(&host.graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { host.graph = nullptr; err = "graph instantiation failed"; return reportFail(ZL_ErrorCode_GENERIC); }
+            host.gIn = hIn;
+            host.gOut = hOut;
+            host.gInBytes = inBytes;
+            host.gOutBytes = outBytes;
+            host.gStream = s;
+        }
+        if (cudaGraphLaunch(host.graph, s) != cudaSuccess) { err = "graph launch failed"; return reportFail(ZL_ErrorCode_GENERIC); }
+        return check(s);
     }
 
     ZL_Report check(cudaStream_t s)

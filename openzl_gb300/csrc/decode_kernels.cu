@@ -1080,6 +1080,7 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
         }
     }
     for (; i < n; i++) single(i);
+    asm volatile("cp.async.wait_all;" ::: "memory"); // no copy outlives the lane
     if (!br.finished()) reportError(status, DERR_CORRUPTION);
 }
 
@@ -1207,6 +1208,7 @@ __device__ __forceinline__ void hufDecodeStream(const HufTask& t, const uint16_t
         *reinterpret_cast<uint32_t*>(out + i) = __byte_perm(__byte_perm(e0, e1, 0x0040), __byte_perm(e2, e3, 0x0040), 0x5410);
     }
     for (; i < n; i++) out[i] = uint8_t(single());
+    asm volatile("cp.async.wait_all;" ::: "memory"); // no copy outlives the lane
     if (!br.finished()) reportError(status, DERR_CORRUPTION);
 }
 

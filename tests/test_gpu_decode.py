@@ -146,3 +146,59 @@ def test_autotuned_shapes_keep_results(gpu_lib, manifest):
     for m, n, o in zip(manifest, sizes, outs):
         h = hashlib.sha256(o[:n].cpu().numpy().tobytes()).hexdigest()
         assert h == m["sha256_in"], m["case"]
+
+
+def _layout(sizes, align):
+    offs, o = [], 0
+    for s in sizes:
+        offs.append(o)
+        o += (s + align - 1) // align * align
+    return offs, o
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_run_host_pipelined(gpu_lib, manifest, graph):
+    """ozl_gpu_batch_run_host with host images of frames and outputs laid out
+    in order: the copies in, the decode and the copies out run in overlapped
+    rounds, and the host output equals the reference's inputs; frames whose
+    addresses do not increase with their index take the serial path with the
+    same result; a corrupted frame is reported."""
+    import torch
+    import openzl_gb300 as oz
+
+    frames = [read_frame(m["case"]) for m in manifest] * 3
+    want = [m["sha256_in"] for m in manifest] * 3
+    sizes = [oz.get_decompressed_size(f) for f in frames]
+    foffs, fbytes = _layout([len(f) for f in frames], 16)
+    ooffs, obytes = _layout([max(s, 1) for s in sizes], 256)
+    fbytes += 64
+    h_in = torch.zeros(fbytes, dtype=torch.uint8, pin_memory=True)
+    for f, o in zip(frames, foffs):
+        h_in[o:o + len(f)].copy_(torch.from_numpy(np.frombuffer(f, np.uint8).copy()))
+    d_in = torch.zeros(fbytes, dtype=torch.uint8, device="cuda")
+    d_out = torch.zeros(obytes, dtype=torch.uint8, device="cuda")
+    h_out = torch.zeros(obytes, dtype=torch.uint8, pin_memory=True)
+    s = torch.cuda.Stream()
+    for order in ("increasing", "swapped"):
+        idx = list(range(len(frames)))
+        if order == "swapped":
+            # frames 1 and 2 planned in swapped order: the image still starts
+            # at the first frame, but the addresses no longer increase
+            idx[1], idx[2] = idx[2], idx[1]
+        b = oz.GpuBatch()
+        b.plan([frames[i] for i in idx], [d_in.data_ptr() + foffs[i] for i in idx],
+               [d_out.data_ptr() + ooffs[i] for i in idx], [sizes[i] for i in idx])
+        for rep in range(3):
+            h_out.fill_(0xAB)
+            b.run_host(h_in.data_ptr(), fbytes, h_out.data_ptr(), obytes, s.cuda_stream, graph=graph)
+            for i in range(len(frames)):
+                got = h_out[ooffs[i]:ooffs[i] + sizes[i]].numpy().tobytes()
+                assert hashlib.sha256(got).hexdigest() == want[i], (order, rep, i)
+    # a corrupted payload byte in one frame of the image is reported
+    b = oz.GpuBatch()
+    b.plan(frames, [d_in.data_ptr() + o for o in foffs], [d_out.data_ptr() + o for o in ooffs], sizes)
+    k = next(i for i, m in enumerate(manifest) if m["case"] == "walk_u32_1mib_dz_tsplit_fse")
+    bad = h_in.clone().pin_memory()
+    bad[foffs[k] + len(frames[k]) // 2] ^= 0x01  # inside a stored FSE bitstream
+    with pytest.raises(oz.ZLError):
+        b.run_host(bad.data_ptr(), fbytes, h_out.data_ptr(), obytes, s.cuda_stream, graph=graph)
