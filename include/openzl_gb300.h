@@ -305,7 +305,10 @@ ZL_Report ozl_gpu_batch_autotune(OZL_GpuBatch* b, void* stream, int reps, uint32
  * from d_frames[0] and whose outputs sit back to back from d_dsts[0] (as
  * passed to ozl_gpu_batch_plan): copies h_in (inBytes) to the device, runs
  * the decode, copies the outputs to h_out (outBytes) and synchronizes.
- * Returns the total decompressed size. */
+ * When both images hold the frames in increasing order, the copies in, the
+ * decode and the copies out overlap in rounds of contiguous frames (pinned
+ * h_in / h_out make the copies asynchronous); otherwise they run one after
+ * another. Returns the total decompressed size. */
 ZL_Report ozl_gpu_batch_run_host(OZL_GpuBatch* b, const void* h_in, size_t inBytes, void* h_out,
                                  size_t outBytes, void* stream, int useGraph);
 /* Number of kernel launches one run issues. */
