@@ -336,7 +336,7 @@ size_t ozl_gpu_batch_launches(const OZL_GpuBatch* b) { return b ? size_t(b->laun
 const char* ozl_gpu_kind_name(int kind)
 {
     static const char* names[] = { "copy", "constant", "fse", "huffman", "flatpack", "tokenize",
-                                   "float_deconstruct", "transpose", "numeric_pipeline", "xxh3" };
+                                   "float_deconstruct", "transpose", "numeric_pipeline", "xxh3", "huffman16" };
     return (kind >= 0 && kind < ozl::KIND_COUNT) ? names[kind] : "?";
 }
 

@@ -49,6 +49,7 @@ enum : uint32_t {
     T_SPLITN_NUM = 48,
     T_FSE = 49,
     T_HUF = 50,
+    T_HUF16 = 51,
     T_NCOUNT = 52,
     T_ID_END = 63,
 };
@@ -93,6 +94,7 @@ Sig signature(uint32_t id)
         case T_CONST_FIXED: return { true, 1, { TY_STRUCT, 0 }, 0, TY_STRUCT, false, false };
         case T_FSE:
         case T_HUF: return { true, 2, { TY_NUMERIC, TY_SERIAL }, 0, TY_SERIAL, false, false };
+        case T_HUF16: return { true, 2, { TY_NUMERIC, TY_SERIAL }, 0, TY_STRUCT, false, false };
         case T_NCOUNT: return { true, 1, { TY_SERIAL, 0 }, 0, TY_NUMERIC, false, false };
         default: return { false, 0, { 0, 0 }, 0, 0, false, false };
     }
@@ -645,6 +647,41 @@ int DecodePlan::planBlock(int f, const uint8_t* src, size_t size, size_t start, 
                     O.w = 1; O.n = dstSize;
                     break;
                 }
+                case T_HUF16: {
+                    // decode_entropy_binding.c:415-467, decode_huffman_kernel.c:196-290
+                    if (in(0).w != 1) { err = "Huffman weights width"; return E_CORRUPT; }
+                    if (in(0).n < 2 || in(0).n > 65536) { err = "Huffman weights count"; return E_CORRUPT; }
+                    if (hs < 2 || hs > 9) { err = "Huffman header"; return E_CORRUPT; }
+                    uint64_t dstSize = readLEn(h + 1, hs - 1);
+                    if (dstSize < 2 || dstSize >= (1ull << 32)) { err = "Huffman size"; return E_CORRUPT; }
+                    PlanStream& I = in(1);
+                    if (I.loc != L_FRAME) { err = "16-bit Huffman over a regenerated bitstream"; return E_LIMIT; }
+                    // the stream table: symbol count and byte size (LE32) before each stream
+                    uint32_t const nbStreams = (h[0] & 1) ? 4u : 1u;
+                    uint32_t tab[16] = { 0 };
+                    uint64_t pos = 0, done = 0;
+                    const uint8_t* const b = src + I.off;
+                    for (uint32_t k = 0; k < nbStreams; k++) {
+                        if (pos + 8 > I.n) { err = "Huffman stream table"; return E_CORRUPT; }
+                        uint32_t const cnt = uint32_t(readLEn(b + pos, 4)), sz = uint32_t(readLEn(b + pos + 4, 4));
+                        pos += 8;
+                        if (pos + sz > I.n || done + cnt > dstSize || sz == 0) { err = "Huffman stream table"; return E_CORRUPT; }
+                        tab[k] = uint32_t(pos);
+                        tab[4 + k] = sz;
+                        tab[8 + k] = cnt;
+                        tab[12 + k] = uint32_t(done);
+                        pos += sz;
+                        done += cnt;
+                    }
+                    if (pos != I.n || done != dstSize) { err = "Huffman stream table"; return E_CORRUPT; }
+                    size_t const off = (params.size() + 15) & ~size_t(15);
+                    params.resize(off + sizeof(tab));
+                    std::memcpy(params.data() + off, tab, sizeof(tab));
+                    nodeU.paramOff = off;
+                    nodeU.nbBits = uint8_t(nbStreams);
+                    O.w = 2; O.n = dstSize;
+                    break;
+                }
                 default:
                     err = "unsupported codec";
                     return E_TRANSFORM;
@@ -803,6 +840,7 @@ struct Buckets {
     std::vector<ConstTask> cst;
     std::vector<FseTask> fse;
     std::vector<HufTask> huf;
+    std::vector<Huf16Task> huf16;
     std::vector<TokenizeTask> tok;
     std::vector<FloatDecTask> flt;
     std::vector<FlatpackTask> flat;
@@ -815,6 +853,12 @@ uint64_t taskBytes(const CopyTask& t) { return 2 * t.bytes; }
 uint64_t taskBytes(const ConstTask& t) { return t.n * t.w + t.w; }
 uint64_t taskBytes(const FseTask& t) { return uint64_t(t.bitsSize) + t.dstSize + 2ull * t.nbSym; }
 uint64_t taskBytes(const HufTask& t) { return uint64_t(t.bitsSize) + t.dstSize + t.nbWeights; }
+uint64_t taskBytes(const Huf16Task& t)
+{
+    uint64_t b = t.nbWeights;
+    for (uint32_t k = 0; k < t.nbStreams; k++) b += uint64_t(t.streamSize[k]) + 2ull * t.count[k];
+    return b;
+}
 uint64_t taskBytes(const FlatpackTask& t) { return t.n + (t.n * t.nbBits + 7) / 8 + t.alphabetSize; }
 uint64_t taskBytes(const TokenizeTask& t) { return t.n * (t.w + t.iw) + uint64_t(t.alphabetSize) * t.w; }
 uint64_t taskBytes(const FloatDecTask& t) { return t.n * (t.eltType == 0 ? 8 : 4); }
@@ -1020,6 +1064,23 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
                 B[lv].huf.push_back(t);
                 break;
             }
+            case 51: {
+                Huf16Task t{};
+                t.out = o;
+                t.weights = in(0);
+                t.nbWeights = uint32_t(streams[nd.ins[0]].n);
+                uint32_t tab[16];
+                std::memcpy(tab, plan.params.data() + nd.paramOff, sizeof(tab));
+                t.nbStreams = nd.nbBits;
+                for (uint32_t k = 0; k < t.nbStreams; k++) {
+                    t.stream[k] = in(1) + tab[k];
+                    t.streamSize[k] = tab[4 + k];
+                    t.count[k] = tab[8 + k];
+                    t.dstOff[k] = tab[12 + k];
+                }
+                B[lv].huf16.push_back(t);
+                break;
+            }
             default:
                 err = "layout: unexpected codec " + std::to_string(nd.id);
                 return 32;
@@ -1106,6 +1167,11 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         addTiled(KIND_CONST, lv, b.cst, [](const ConstTask& t) { return ceilDiv(t.n * t.w, kTileBytes); });
         addPlain(KIND_FSE, lv, b.fse);
         addPlain(KIND_HUF, lv, b.huf);
+        for (Huf16Task& t : b.huf16) {
+            t.sorted = reinterpret_cast<uint16_t*>(dScratch + scratch);
+            scratch += (2ull * t.nbWeights + 255) & ~uint64_t(255);
+        }
+        addPlain(KIND_HUF16, lv, b.huf16);
         addTiled(KIND_FLATPACK, lv, b.flat, [](const FlatpackTask& t) { return ceilDiv(t.n, kTileBytes); });
         addTiled(KIND_TOKENIZE, lv, b.tok, [](const TokenizeTask& t) { return ceilDiv(t.n, kTileElems); });
         addTiled(KIND_FLOATDEC, lv, b.flt, [](const FloatDecTask& t) { return ceilDiv(t.n, kTileElems); });

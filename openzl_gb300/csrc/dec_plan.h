@@ -21,6 +21,7 @@ enum Kind : int {
     KIND_TRANSPOSE,
     KIND_NUMPIPE,
     KIND_HASH,
+    KIND_HUF16, // launched after KIND_HUF within a level
     KIND_COUNT
 };
 

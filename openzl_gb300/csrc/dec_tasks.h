@@ -75,6 +75,21 @@ struct FseTask {
     uint8_t tableLog;
 };
 
+// 16-bit-symbol Huffman (huffman_struct_v2): one or four backward streams
+// whose byte ranges and symbol counts the planner read from the stored
+// bitstream; `sorted` is scratch for the symbols ranked by (weight, value).
+struct Huf16Task {
+    uint8_t* out;              // dstSize 16-bit symbols
+    const uint8_t* weights;    // nbWeights bytes
+    uint16_t* sorted;          // nbWeights entries of scratch
+    const uint8_t* stream[4];
+    uint32_t streamSize[4];
+    uint32_t count[4];         // symbols per stream
+    uint32_t dstOff[4];        // first symbol of each stream
+    uint32_t nbWeights;
+    uint32_t nbStreams;
+};
+
 struct HufTask {
     uint8_t* out;
     const uint8_t* bits;

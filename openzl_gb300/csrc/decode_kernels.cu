@@ -1280,6 +1280,172 @@ __global__ void __launch_bounds__(32) kHuf(const HufTask* __restrict__ tasks, ui
     }
 }
 
+// Backward bit reader of the 16-bit Huffman decoder. The window is the three
+// stream words kb + 2 (top), kb + 1 and kb, loaded through the read-only data
+// cache at each step (a lane walks down one 128-byte line every few dozen
+// steps, so nearly all loads hit L1), and g = 32 * (kb + 3) - pos in
+// [0, 32): the 64 bits just below pos, most significant first, are two
+// funnel shifts of them. A step reads at most 48 bits; advance() drops them
+// with three integer operations. Word indices are clamped at 0, the 16-byte
+// block that holds the stream's first byte: words below the stream are never
+// consumed by a valid stream (finished() checks that the stream ends exactly
+// at its first bit), so any word may stand in for them, and nothing outside
+// the stream's blocks is read.
+struct BitLdg {
+    const uint32_t* base; // the 16-byte block holding the stream's first byte
+    int32_t kb, g, end;
+
+    __device__ __forceinline__ bool init(const uint8_t* p, uint32_t size)
+    {
+        int32_t pos;
+        const uint8_t* g16;
+        if (!streamStart(p, size, g16, pos, end)) return false;
+        base = reinterpret_cast<const uint32_t*>(g16);
+        int32_t const jt = (pos - 1) >> 5;
+        kb = jt - 2;
+        g = (kb + 3) * 32 - pos;
+        return true;
+    }
+    // the 64 bits below pos, most significant first
+    __device__ __forceinline__ void window(uint32_t& hi, uint32_t& lo) const
+    {
+        uint32_t const c = __ldg(base + max(kb, 0)), b = __ldg(base + max(kb + 1, 0)), a = __ldg(base + max(kb + 2, 0));
+        hi = __funnelshift_l(b, a, uint32_t(g));
+        lo = __funnelshift_l(c, b, uint32_t(g));
+    }
+    __device__ __forceinline__ void advance(uint32_t n)
+    {
+        g += int32_t(n);
+        kb -= g >> 5;
+        g &= 31;
+    }
+    // one field of nb bits (nb <= 12) just below pos
+    __device__ __forceinline__ uint32_t read(uint32_t nb)
+    {
+        uint32_t hi, lo;
+        window(hi, lo);
+        advance(nb);
+        return __funnelshift_l(hi, 0u, nb);
+    }
+    __device__ __forceinline__ bool finished() const { return (kb + 3) * 32 - g == end; }
+};
+
+// ---------------------------------------------------------------------------
+// 16-bit-symbol Huffman (huffman_struct_v2), one CTA per chunk. Tables reach
+// 2^20 cells (tableLog <= 20), so instead of a cell table the CTA keeps, per
+// weight, the first cell and the first index into the symbols sorted by
+// (weight, value): the cell range of weight w spans count[w] << (w - 1)
+// cells, weight 1 (the longest code) first, and a symbol of weight w spans
+// 2^(w-1) consecutive cells and codes on tableLog + 1 - w bits
+// (decode_huffman_kernel.c:35-71). Decoding a symbol peeks tableLog bits,
+// finds the weight whose cell range holds them (binary search over at most
+// 20 ranks) and indexes the sorted symbols. The validity rules of
+// decode_entropy_binding.c:349-412 apply: weights at most 20, at least two
+// of them non-zero, the sum of 2^(w-1) a power of two. One lane decodes each
+// of the one or four streams; like the reference, a stream is not required
+// to end exactly at its first bit (the planner checked that the stream table
+// fills the input exactly).
+__global__ void __launch_bounds__(128) kHuf16(const Huf16Task* __restrict__ tasks, uint32_t* __restrict__ status)
+{
+    __shared__ uint32_t sCount[32], sStart[32], sBase[32], sNext[32];
+    __shared__ uint32_t sTl, sOk;
+    __shared__ unsigned long long sSum;
+    Huf16Task const t = tasks[blockIdx.x];
+    uint32_t const tid = threadIdx.x, lane = tid & 31;
+    if (tid < 32) sCount[tid] = 0;
+    if (tid == 0) {
+        sSum = 0;
+        sOk = 1;
+    }
+    __syncthreads();
+    unsigned long long part = 0;
+    bool bad = false;
+    for (uint32_t s = tid; s < t.nbWeights; s += blockDim.x) {
+        uint32_t const w = t.weights[s];
+        if (w > 20) {
+            bad = true;
+        } else if (w) {
+            atomicAdd(&sCount[w], 1u);
+            part += 1ull << (w - 1);
+        }
+    }
+    if (bad) sOk = 0;
+    if (part) atomicAdd(&sSum, part);
+    __syncthreads();
+    if (tid == 0) {
+        uint64_t const sum = sSum;
+        uint32_t nz = 0;
+        for (int w = 1; w <= 20; w++) nz += sCount[w];
+        uint32_t tl = 0;
+        while (tl < 63 && (2ull << tl) <= sum) tl++;
+        bool const ok = sOk && nz >= 2 && sum != 0 && !(sum & (sum - 1)) && tl <= 20;
+        if (ok) {
+            uint32_t pos = 0, base = 0;
+            for (uint32_t w = 1; w <= tl; w++) {
+                sStart[w] = pos;
+                sBase[w] = base;
+                sNext[w] = base;
+                pos += sCount[w] << (w - 1);
+                base += sCount[w];
+            }
+            sStart[tl + 1] = 1u << tl;
+        }
+        sTl = tl;
+        sOk = ok ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!sOk) {
+        if (tid == 0) reportError(status, DERR_CORRUPTION);
+        return;
+    }
+    uint32_t const tl = sTl;
+    // symbols sorted by (weight, value): 32 at a time, ranked among the lanes
+    // holding the same weight
+    if (tid < 32) {
+        for (uint32_t b0 = 0; b0 < t.nbWeights; b0 += 32) {
+            uint32_t const s = b0 + lane;
+            uint32_t const w = s < t.nbWeights ? t.weights[s] : 0u;
+            uint32_t const m = __match_any_sync(0xffffffffu, w);
+            uint32_t const base = w ? sNext[w] : 0u;
+            __syncwarp();
+            if (w) {
+                if (lane == 31u - __clz(m)) sNext[w] = base + __popc(m);
+                t.sorted[base + __popc(m & ((1u << lane) - 1u))] = uint16_t(s);
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    if (tid >= t.nbStreams) return;
+    BitLdg br;
+    if (!br.init(t.stream[tid], t.streamSize[tid])) {
+        reportError(status, DERR_CORRUPTION);
+        return;
+    }
+    uint8_t* const out = t.out + 2ull * t.dstOff[tid];
+    bool const al = !(reinterpret_cast<uintptr_t>(out) & 1);
+    uint32_t const n = t.count[tid];
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t hi, lo;
+        br.window(hi, lo);
+        uint32_t const v = hi >> (32 - tl);
+        uint32_t a = 1, b = tl;
+        while (a < b) {
+            uint32_t const mid = (a + b + 1) >> 1;
+            if (sStart[mid] <= v) a = mid;
+            else b = mid - 1;
+        }
+        uint32_t const sym = t.sorted[sBase[a] + ((v - sStart[a]) >> (a - 1))];
+        if (al) {
+            reinterpret_cast<uint16_t*>(out)[i] = uint16_t(sym);
+        } else {
+            out[2 * i] = uint8_t(sym);
+            out[2 * i + 1] = uint8_t(sym >> 8);
+        }
+        br.advance(tl + 1 - a);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // XXH3-64 checksums. Phase 1: per 1 KiB block, the 16-stripe sum of every
 // accumulator lane's increments (they commute within a block). Phase 2: per
@@ -1688,6 +1854,9 @@ long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dSc
             }
             case KIND_FLATPACK:
                 kFlatpack<<<l.nbTiles, 256, 0, s>>>(static_cast<const FlatpackTask*>(tasks), tiles, dStatus);
+                break;
+            case KIND_HUF16:
+                if (l.nbTasks) kHuf16<<<l.nbTasks, 128, 0, s>>>(static_cast<const Huf16Task*>(tasks), dStatus);
                 break;
             case KIND_TOKENIZE:
                 kTokenize<<<l.nbTiles, 256, 0, s>>>(static_cast<const TokenizeTask*>(tasks), tiles, dStatus);

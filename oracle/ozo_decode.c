@@ -336,6 +336,84 @@ static int huf_decode_4x(uint8_t* dst, size_t n, const uint8_t* src, size_t size
 }
 
 /* ---------------------------------------------------------------------
+ * 16-bit-symbol Huffman (huffman_struct_v2,
+ * src/openzl/codecs/entropy/decode_entropy_binding.c:349-467 and
+ * src/openzl/codecs/entropy/decode_huffman_kernel.c:35-290). Up to 65536
+ * weights, at least two non-zero, weights and tableLog at most 20, the sum
+ * of 2^(w-1) a power of two. Cells are ranked by weight (weight 1, the
+ * longest code, first) then by symbol; a symbol of weight w spans 2^(w-1)
+ * cells and codes on tableLog+1-w bits. The bitstream holds one stream, or
+ * four in sequence, each prefixed by its symbol count and its byte size
+ * (LE32 each); the streams together must fill the input exactly.
+ * ------------------------------------------------------------------- */
+typedef struct {
+    uint16_t symbol;
+    uint8_t nbBits;
+} Huf16D;
+
+static int huf16_build_dtable(Huf16D** dtOut, unsigned* tableLogOut, const uint8_t* weights, size_t nbWeights)
+{
+    if (nbWeights < 2 || nbWeights > 65536) return -1;
+    size_t nz = 0;
+    uint64_t sum = 0;
+    unsigned counts[21] = { 0 };
+    for (size_t i = 0; i < nbWeights; i++) {
+        if (weights[i] > 20) return -1;
+        nz += weights[i] != 0;
+        sum += ((uint64_t)1 << weights[i]) >> 1;
+        counts[weights[i]]++;
+    }
+    if (nz < 2 || sum == 0 || (sum & (sum - 1))) return -1;
+    unsigned tableLog = 0;
+    while (((uint64_t)1 << (tableLog + 1)) <= sum) tableLog++;
+    if (tableLog > 20) return -1;
+    Huf16D* dt = (Huf16D*)malloc(sizeof(Huf16D) << tableLog);
+    if (!dt) return -1;
+    size_t start[22];
+    size_t pos = 0;
+    for (unsigned w = 1; w <= tableLog; w++) {
+        start[w] = pos;
+        pos += (size_t)counts[w] << (w - 1);
+    }
+    for (size_t s = 0; s < nbWeights; s++) {
+        unsigned const w = weights[s];
+        if (!w) continue;
+        size_t const len = (size_t)1 << (w - 1);
+        for (size_t u = 0; u < len; u++) {
+            dt[start[w] + u].symbol = (uint16_t)s;
+            dt[start[w] + u].nbBits = (uint8_t)(tableLog + 1 - w);
+        }
+        start[w] += len;
+    }
+    *dtOut = dt;
+    *tableLogOut = tableLog;
+    return 0;
+}
+
+/* one stream: symbol count and byte size (LE32 each), then the backward
+ * bitstream; decodes its symbols as 16-bit little-endian values */
+static int huf16_decode_stream(uint8_t* dst, size_t cap, size_t* done, const uint8_t** src, size_t* avail,
+                               const Huf16D* dt, unsigned tableLog)
+{
+    if (*avail < 8) return -OZO_ERR_CORRUPTION;
+    size_t const n = ozo_rd32(*src), size = ozo_rd32(*src + 4);
+    *src += 8;
+    *avail -= 8;
+    if (size > *avail || *done + n > cap) return -OZO_ERR_CORRUPTION;
+    BCont r;
+    if (bc_init(&r, *src, size)) return -OZO_ERR_CORRUPTION;
+    for (size_t i = 0; i < n; i++) {
+        Huf16D const e = dt[bc_peek(&r, (int)tableLog)];
+        ozo_wr16(dst + 2 * (*done + i), e.symbol);
+        bc_skip(&r, e.nbBits);
+    }
+    *src += size;
+    *avail -= size;
+    *done += n;
+    return 0;
+}
+
+/* ---------------------------------------------------------------------
  * Decoder signatures (src/openzl/codecs/decoder_registry.c:88-161 and the
  * graph macros it names): number of singleton inputs with their types,
  * whether variable inputs are accepted, and the regenerated type.
@@ -400,6 +478,9 @@ static DecSig sig_of(unsigned id)
         case TR_HUFFMAN_V2:
             d.nbSO = 2; d.soTypes[0] = OZO_TYPE_NUMERIC; d.soTypes[1] = OZO_TYPE_SERIAL;
             d.outType = OZO_TYPE_SERIAL; break;
+        case TR_HUFFMAN_STRUCT_V2:
+            d.nbSO = 2; d.soTypes[0] = OZO_TYPE_NUMERIC; d.soTypes[1] = OZO_TYPE_SERIAL;
+            d.outType = OZO_TYPE_STRUCT; break;
         case TR_FSE_NCOUNT:
             d.nbSO = 1; d.soTypes[0] = OZO_TYPE_SERIAL; d.outType = OZO_TYPE_NUMERIC; break;
         default:
@@ -703,6 +784,27 @@ static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, s
             uint8_t* o = ost_alloc(out, OZO_TYPE_SERIAL, 1, dstSize);
             return x4 ? huf_decode_4x(o, dstSize, bits->p, bits->n, dt, tl)
                       : huf_decode_stream(o, dstSize, bits->p, bits->n, dt, tl);
+        }
+        case TR_HUFFMAN_STRUCT_V2: { /* decode_entropy_binding.c:415-467 */
+            const OStream* wS = in[0];
+            const OStream* bits = in[1];
+            if (wS->w != 1) return -OZO_ERR_CORRUPTION;
+            if (hsz < 2 || hsz > 9) return -OZO_ERR_CORRUPTION;
+            int const x4 = hdr[0] & 1;
+            size_t const dstSize = (size_t)ozo_rdN(hdr + 1, hsz - 1);
+            if (dstSize < 2) return -OZO_ERR_CORRUPTION;
+            Huf16D* dt = NULL;
+            unsigned tl;
+            if (huf16_build_dtable(&dt, &tl, wS->p, wS->n)) return -OZO_ERR_CORRUPTION;
+            uint8_t* o = ost_alloc(out, OZO_TYPE_STRUCT, 2, dstSize);
+            const uint8_t* p = bits->p;
+            size_t avail = bits->n, done = 0;
+            int rc = 0;
+            for (int k = 0; k < (x4 ? 4 : 1) && !rc; k++) rc = huf16_decode_stream(o, dstSize, &done, &p, &avail, dt, tl);
+            free(dt);
+            if (rc) return rc;
+            if (done != dstSize || avail != 0) return -OZO_ERR_CORRUPTION;
+            return 0;
         }
         default:
             return -OZO_ERR_UNSUPPORTED;

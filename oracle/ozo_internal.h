@@ -37,6 +37,7 @@ enum {
     TR_SPLITN_NUM = 48,
     TR_FSE_V2 = 49,
     TR_HUFFMAN_V2 = 50,
+    TR_HUFFMAN_STRUCT_V2 = 51,
     TR_FSE_NCOUNT = 52,
     TR_END = 63,
 };

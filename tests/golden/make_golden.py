@@ -4,7 +4,8 @@ Run in a container that holds the reference sources (it builds
 oracle/_ref/ with oracle/ref.mk first). Each case is the frame the reference
 compressor produced for a seeded input, plus a manifest entry holding the
 SHA-256 of that input. The tests decode the frames with the GPU library and
-with the CPU oracle and check both against the recorded input hash.
+with the CPU oracle and check both against the recorded input hash; the
+encoders re-create every frame not marked decode_only.
 
     python tests/golden/make_golden.py
 """
@@ -67,6 +68,12 @@ def build_cases():
     c.append(("store_serial", 0, rng.integers(0, 256, 3000).astype(np.uint8), 0))
     c.append(("empty_serial_fse", 7, np.zeros(0, np.uint8), 0))
     c.append(("tiny_numeric_delta", 9, np.array([5], np.uint32), 4))
+    # 16-bit-symbol Huffman (huffman_struct_v2): u16 columns whose alphabet is
+    # too wide for tokenize, through ZL_GRAPH_HUFFMAN. Decode-only cases: the
+    # encoders here do not build 16-bit Huffman tables.
+    c.append(("huf16_zipf_u16", 8, (rng.zipf(1.3, 200000) % 3000).astype(np.uint16), 2, True))
+    c.append(("huf16_x1_u16", 8, (rng.zipf(1.2, 900) % 1000).astype(np.uint16), 2, True))
+    c.append(("huf16_wide_u16", 8, np.minimum(rng.geometric(1 / 3000, 150000), 65535).astype(np.uint16), 2, True))
     return c
 
 
@@ -78,7 +85,8 @@ def main():
                                  ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
     lib.ref_compressBound.restype = ctypes.c_size_t
     manifest = []
-    for name, recipe, arr, w in build_cases():
+    for name, recipe, arr, w, *flags in build_cases():
+        decode_only = bool(flags and flags[0])
         arr = np.ascontiguousarray(arr)
         for cs in (1, 0):
             if cs == 0 and recipe not in (1, 2, 3, 4, 5):
@@ -96,7 +104,8 @@ def main():
             manifest.append({"case": case, "recipe": recipe, "elt_width": w, "n": int(arr.size),
                              "checksums": cs, "frame_bytes": int(r),
                              "sha256_in": hashlib.sha256(arr.tobytes()).hexdigest(),
-                             "sha256_frame": hashlib.sha256(dst[:r].tobytes()).hexdigest()})
+                             "sha256_frame": hashlib.sha256(dst[:r].tobytes()).hexdigest(),
+                             **({"decode_only": True} if decode_only else {})})
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
     tot = sum(os.path.getsize(os.path.join(HERE, m["case"] + ".zl")) for m in manifest)

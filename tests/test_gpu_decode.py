@@ -202,3 +202,27 @@ def test_batch_run_host_pipelined(gpu_lib, manifest, graph):
     bad[foffs[k] + len(frames[k]) // 2] ^= 0x01  # inside a stored FSE bitstream
     with pytest.raises(oz.ZLError):
         b.run_host(bad.data_ptr(), fbytes, h_out.data_ptr(), obytes, s.cuda_stream, graph=graph)
+
+
+def test_huffman16_frames_run_the_16bit_kernel(gpu_lib, manifest):
+    """The 16-bit-symbol Huffman fixtures (huffman_struct_v2, transform 51)
+    decode through the GPU's 16-bit Huffman launch, bit-exactly."""
+    import torch
+    import openzl_gb300 as oz
+
+    cases = [m for m in manifest if m["case"].startswith("huf16_")]
+    assert len(cases) >= 3
+    frames = [read_frame(m["case"]) for m in cases]
+    dfr = [_dev(torch, f) for f in frames]
+    sizes = [oz.get_decompressed_size(f) for f in frames]
+    outs = [torch.zeros(max(n, 1) + 64, dtype=torch.uint8, device="cuda") for n in sizes]
+    s = torch.cuda.Stream()
+    b = oz.GpuBatch()
+    b.plan(frames, [d.data_ptr() for d in dfr], [o.data_ptr() for o in outs], sizes)
+    torch.cuda.synchronize()
+    kinds = [k for k, _, _ in b.profile(s.cuda_stream, capacity=64)]
+    assert "huffman16" in kinds, kinds
+    b.run(s.cuda_stream, graph=True)
+    b.check(s.cuda_stream)
+    for m, n, o in zip(cases, sizes, outs):
+        assert hashlib.sha256(o[:n].cpu().numpy().tobytes()).hexdigest() == m["sha256_in"], m["case"]

@@ -64,6 +64,8 @@ def test_oracle_matches_reference_on_seeded_inputs():
 def test_oracle_encoder_reproduces_every_golden_frame(manifest):
     """The CPU encoder restatement emits the reference's exact frame bytes."""
     for m in manifest:
+        if m.get("decode_only"):
+            continue
         fr = read_frame(m["case"])
         data, _, w = oracle.decompress(fr)
         width = m["elt_width"]
