@@ -341,6 +341,7 @@ typedef enum {
     OZL_GRAPH_CONSTANT = 13,        /* ZL_GRAPH_CONSTANT */
     OZL_GRAPH_FLATPACK = 14,        /* ZL_GRAPH_FLATPACK */
     OZL_GRAPH_BITPACK = 15,         /* ZL_GRAPH_BITPACK */
+    OZL_GRAPH_ENTROPY = 17,         /* ZL_GRAPH_ENTROPY (FSE or Huffman per chunk) */
 } OZL_GraphRecipe;
 
 typedef struct OZL_GpuEncoder_s OZL_GpuEncoder;

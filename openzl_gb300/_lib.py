@@ -365,6 +365,7 @@ GRAPH_ILLEGAL = 0
 GRAPH_STORE = 2
 GRAPH_FSE = 3
 GRAPH_HUFFMAN = 4
+GRAPH_ENTROPY = 5
 GRAPH_CONSTANT = 6
 GRAPH_BITPACK = 8
 GRAPH_FLATPACK = 9

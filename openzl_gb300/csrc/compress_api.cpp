@@ -91,6 +91,7 @@ struct ZL_Compressor_s {
                 case G_STORE: out += "STORE"; return true;
                 case G_FSE: out += "FSE"; return true;
                 case G_HUFFMAN: out += "HUFFMAN"; return true;
+                case G_ENTROPY: out += "ENTROPY"; return true;
                 case G_CONSTANT: out += "CONSTANT"; return true;
                 case G_BITPACK: out += "BITPACK"; return true;
                 case G_FLATPACK: out += "FLATPACK"; return true;
@@ -180,6 +181,7 @@ int recipeOf(const std::string& chain)
         { "delta>bitpack>HUFFMAN", ozl::RC_D_BITPACK_HUF },
         { "FSE", ozl::RC_FSE },
         { "HUFFMAN", ozl::RC_HUFFMAN },
+        { "ENTROPY", ozl::RC_ENTROPY },
         { "delta>STORE", ozl::RC_DELTA_STORE },
         { "zigzag>STORE", ozl::RC_ZIGZAG_STORE },
         { "bitpack>STORE", ozl::RC_BITPACK_STORE },

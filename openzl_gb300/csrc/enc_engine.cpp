@@ -82,7 +82,7 @@ struct Piece {
     uint64_t bytes = 0;
 };
 
-enum : int { M_FSE = 0, M_HUF, M_CONSTANT, M_FLATPACK, M_BITPACK };
+enum : int { M_FSE = 0, M_HUF, M_CONSTANT, M_FLATPACK, M_BITPACK, M_ANY };
 
 struct Job {
     const uint8_t* dsrc = nullptr;    // device content
@@ -256,7 +256,7 @@ struct Engine {
 
     // ---- graphs ----------------------------------------------------------
     enum G {
-        G_STORE, G_SERIAL_STORE, G_FSE, G_HUF, G_CONSTANT, G_BITPACK, G_FLATPACK, G_NCOUNT, G_TSPLIT_FSE,
+        G_STORE, G_SERIAL_STORE, G_FSE, G_HUF, G_ENTROPY, G_CONSTANT, G_BITPACK, G_FLATPACK, G_NCOUNT, G_TSPLIT_FSE,
         G_TSPLIT_STORE, G_BITPACK_HUF, G_JOB, G_TOKENIZE, G_BF16
     };
     struct Succ {
@@ -301,13 +301,13 @@ struct Engine {
     }
 
     // entropyCompressChunk (encode_entropy_binding.c:602-762)
-    void entropyChunk(int sid, bool huf, std::vector<Succ>& succ, int explicitJob)
+    void entropyChunk(int sid, int mode, std::vector<Succ>& succ, int explicitJob)
     {
         if (s[sid].n <= 1) {
             succ.push_back({ G_STORE, sid, -1 });
             return;
         }
-        Job* j = jobFor(sid, huf ? M_HUF : M_FSE, explicitJob);
+        Job* j = jobFor(sid, mode, explicitJob);
         if (!j) return; // discovery
         switch (j->codec) {
             case ent::CC_STORE: succ.push_back({ G_STORE, sid, -1 }); return;
@@ -355,7 +355,7 @@ struct Engine {
         }
     }
 
-    void entropyGraph(int sid, bool huf, int explicitJob)
+    void entropyGraph(int sid, int mode, int explicitJob)
     {
         std::vector<Succ> succ;
         if (s[sid].w == 1 && s[sid].type != T_SERIAL)
@@ -363,7 +363,7 @@ struct Engine {
         if (s[sid].w != 1) { err = 81; return; }
         uint64_t const n = s[sid].n;
         if (n < kMinChunking) {
-            entropyChunk(sid, huf, succ, explicitJob);
+            entropyChunk(sid, mode, succ, explicitJob);
         } else {
             uint64_t const nb = (n + kChunk - 1) / kChunk;
             newNode(TR_SPLITN, sid, 0);
@@ -377,7 +377,7 @@ struct Engine {
                 pos += len;
             }
             nd.back().nbOut = int(nb);
-            for (uint64_t k = 0; k < nb; k++) entropyChunk(first + int(k), huf, succ, -1);
+            for (uint64_t k = 0; k < nb; k++) entropyChunk(first + int(k), mode, succ, -1);
         }
         runSuccs(succ);
     }
@@ -395,8 +395,9 @@ struct Engine {
                 s[sid].store = true;
                 return;
             case G_STORE: runSuccessor(G_SERIAL_STORE, sid); return;
-            case G_FSE: sid = convertFor(sid, T_SERIAL); entropyGraph(sid, false, job); return;
-            case G_HUF: entropyGraph(sid, true, job); return;
+            case G_FSE: sid = convertFor(sid, T_SERIAL); entropyGraph(sid, M_FSE, job); return;
+            case G_HUF: entropyGraph(sid, M_HUF, job); return;
+            case G_ENTROPY: entropyGraph(sid, M_ANY, job); return;
             case G_CONSTANT: {
                 Job& j = (*jobs)[size_t(job)];
                 RNode& x = newNode(TR_CONST_SERIAL, sid, 1);
@@ -934,6 +935,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             case RC_TOKENIZE: E.runSuccessor(Engine::G_TOKENIZE, in); break;
             case RC_BF16: E.runSuccessor(Engine::G_BF16, in); break;
             case RC_HUFFMAN: E.runSuccessor(Engine::G_HUF, in); break;
+            case RC_ENTROPY: E.runSuccessor(Engine::G_ENTROPY, in); break;
             case RC_CONSTANT:
             case RC_FLATPACK:
             case RC_BITPACK: {
@@ -983,7 +985,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         if (j.mode == M_CONSTANT) j.codec = ent::CC_CONSTANT;
         else if (j.mode == M_FLATPACK) j.codec = ent::CC_FLATPACK;
         else if (j.mode == M_BITPACK) j.codec = ent::CC_BITPACK;
-        else j.codec = ent::chooseCodec(j.hist, j.mode == M_HUF);
+        else j.codec = ent::chooseCodec(j.hist, j.mode == M_HUF ? ent::EM_HUF : (j.mode == M_ANY ? ent::EM_ANY : ent::EM_FSE));
         switch (j.codec) {
             case ent::CC_CONSTANT: j.constVal = uint8_t(j.hist.maxSym); break;
             case ent::CC_BITPACK:

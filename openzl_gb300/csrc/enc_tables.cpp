@@ -66,23 +66,25 @@ void Histo::finish()
 
 // entropyCompressChunk's codec choice for serial chunks
 // (encode_entropy_binding.c:664-736).
-ChunkCodec chooseCodec(const Histo& h, bool hufMode)
+// DataStatsU8_estimateHuffmanSizeFast (data_stats.c:287-301)
+static uint64_t hufSizeFast(double e, uint64_t n)
+{
+    if (e > 7) return n;
+    double const e1 = e < 1 ? 1 : e;
+    volatile double prod = e1 * double(n);
+    volatile double q = prod / 8;
+    return uint64_t(q);
+}
+
+ChunkCodec chooseCodec(const Histo& h, int mode)
 {
     uint64_t const n = h.n;
     if (n <= 1) return CC_STORE;
     if (h.card == 1) return CC_CONSTANT;
     uint64_t entropySize;
     double const e = entropyBits(h.count, n);
-    if (hufMode) {
-        // DataStatsU8_estimateHuffmanSizeFast (data_stats.c:287-301)
-        if (e > 7) {
-            entropySize = n;
-        } else {
-            double const e1 = e < 1 ? 1 : e;
-            volatile double prod = e1 * double(n);
-            volatile double q = prod / 8;
-            entropySize = uint64_t(q);
-        }
+    if (mode == EM_HUF) {
+        entropySize = hufSizeFast(e, n);
     } else {
         volatile double prod = e * double(n);
         volatile double sum = prod + 7;
@@ -99,7 +101,10 @@ ChunkCodec chooseCodec(const Histo& h, bool hufMode)
         return CC_BITPACK;
     }
     if (n <= baseline) return CC_STORE;
-    return hufMode ? CC_HUF : CC_FSE;
+    // resolveMode (encode_entropy_binding.c:527-548): the FSE size is the
+    // entropy estimate above
+    if (mode == EM_ANY) return entropySize + n / 32 < hufSizeFast(e, n) ? CC_FSE : CC_HUF;
+    return mode == EM_HUF ? CC_HUF : CC_FSE;
 }
 
 // FSE_optimalTableLog_internal (fse_compress.c:379-396)

@@ -32,9 +32,12 @@ struct Histo {
     void finish(); // fills maxSym and card from count
 };
 
-// Chunk codec choice for a serial chunk (huffman mode for the Huffman graph,
-// FSE mode for the FSE graph).
-ChunkCodec chooseCodec(const Histo& h, bool hufMode);
+// Entropy backend modes: the FSE graph, the Huffman graph, the entropy graph.
+enum : int { EM_FSE = 0, EM_HUF = 1, EM_ANY = 2 };
+
+// Chunk codec choice for a serial chunk under a backend mode
+// (entropyCompressChunk, encode_entropy_binding.c:602-762).
+ChunkCodec chooseCodec(const Histo& h, int mode);
 
 // FSE: table log, normalized counts, encoding tables.
 unsigned fseTableLog(unsigned maxTableLog, uint64_t srcSize, unsigned maxSym, unsigned minus);

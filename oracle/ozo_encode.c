@@ -24,12 +24,14 @@ enum {
     R_D_BITPACK_HUF = 4, R_TOKENIZE = 5, R_BF16 = 6, R_FSE = 7, R_HUFFMAN = 8,
     R_DELTA_STORE = 9, R_ZIGZAG_STORE = 10, R_BITPACK_STORE = 11, R_TSPLIT_STORE = 12,
     R_CONSTANT = 13, R_FLATPACK = 14, R_BITPACK_GRAPH = 15, R_TOKENIZE_SORTED = 16,
+    R_ENTROPY = 17,
 };
 
 /* graphs of the engine */
 enum {
     G_STORE, G_SERIAL_STORE, G_FSE, G_HUF, G_CONSTANT, G_BITPACK, G_FLATPACK, G_FSE_NCOUNT,
     G_TSPLIT_FSE, G_TSPLIT_STORE, G_BITPACK_HUF, G_CHAIN, G_TOKENIZE, G_TOKENIZE_SORTED, G_BF16,
+    G_ENTROPY,
 };
 
 typedef struct {
@@ -1058,7 +1060,9 @@ static int node_bf16(ECtx* c, int in)
     return sf;
 }
 
-/* entropyCompressChunk for serial chunks (encode_entropy_binding.c:602-762) */
+/* entropyCompressChunk for serial chunks (encode_entropy_binding.c:602-762).
+ * mode: 0 FSE graph (EBM_fse), 1 Huffman graph (EBM_huf), 2 entropy graph
+ * (EBM_any: FSE or Huffman by resolveMode, encode_entropy_binding.c:527-548). */
 static int entropy_chunk(ECtx* c, int sid, int hufMode, SuccList* succ)
 {
     size_t const n = S(sid)->n;
@@ -1067,7 +1071,7 @@ static int entropy_chunk(ECtx* c, int sid, int hufMode, SuccList* succ)
     stats_init(&st, S(sid)->data, n);
     if (st.card == 1) { succ_add(succ, G_CONSTANT, sid, NULL); return 0; }
     size_t entropySize;
-    if (hufMode) {
+    if (hufMode == 1) {
         entropySize = stats_huf_fast(&st);
     } else {
         volatile double e = stats_entropy(&st);
@@ -1086,6 +1090,10 @@ static int entropy_chunk(ECtx* c, int sid, int hufMode, SuccList* succ)
         return 0;
     }
     if (n <= baseline) { succ_add(succ, G_STORE, sid, NULL); return 0; }
+    if (hufMode == 2) {
+        /* the FSE size is the entropy estimate above */
+        hufMode = entropySize + n / 32 < stats_huf_fast(&st) ? 0 : 1;
+    }
     if (hufMode) {
         int w = node_huf(c, sid, &st);
         succ_add(succ, G_FSE, w, NULL);
@@ -1138,6 +1146,8 @@ static int run_graph(ECtx* c, int g, int sid, const void* arg)
             return graph_entropy(c, sid, 0);
         case G_HUF:
             return graph_entropy(c, sid, 1);
+        case G_ENTROPY:
+            return graph_entropy(c, sid, 2);
         case G_CONSTANT: {
             int o = node_constant(c, sid);
             return run_successor(c, G_SERIAL_STORE, o, NULL);
@@ -1352,6 +1362,7 @@ int64_t ozo_compress(int recipe, const void* src, size_t nbElts, int eltWidth, v
         case R_TOKENIZE_SORTED: rc = run_successor(&c, G_TOKENIZE_SORTED, in, NULL); break;
         case R_BF16: rc = run_successor(&c, G_BF16, in, NULL); break;
         case R_HUFFMAN: rc = run_successor(&c, G_HUF, in, NULL); break;
+        case R_ENTROPY: rc = run_successor(&c, G_ENTROPY, in, NULL); break;
         case R_DELTA_STORE: rc = run_successor(&c, G_CHAIN, in, chainD_ST); break;
         case R_ZIGZAG_STORE: rc = run_successor(&c, G_CHAIN, in, chainZ_ST); break;
         case R_BITPACK_STORE: rc = run_successor(&c, G_CHAIN, in, chainB_ST); break;

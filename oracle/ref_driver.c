@@ -44,6 +44,7 @@ enum {
     R_FLATPACK         = 14, /* flatpack graph */
     R_BITPACK_GRAPH    = 15, /* public bitpack graph */
     R_TOKENIZE_SORTED  = 16, /* tokenize(numeric, sorted) alphabet->STORE, idx->bitpack->HUF */
+    R_ENTROPY          = 17, /* ENTROPY graph directly (FSE or Huffman per chunk) */
 };
 
 static ZL_GraphID build(ZL_Compressor* c, int recipe, int eltWidth)
@@ -89,6 +90,8 @@ static ZL_GraphID build(ZL_Compressor* c, int recipe, int eltWidth)
             return ZL_GRAPH_FSE;
         case R_HUFFMAN:
             return ZL_GRAPH_HUFFMAN;
+        case R_ENTROPY:
+            return ZL_GRAPH_ENTROPY;
         case R_DELTA_STORE:
             return ZL_Compressor_registerStaticGraph_fromNode1o(c, ZL_NODE_DELTA_INT, ZL_GRAPH_STORE);
         case R_ZIGZAG_STORE:

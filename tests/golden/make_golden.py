@@ -74,6 +74,14 @@ def build_cases():
     c.append(("huf16_zipf_u16", 8, (rng.zipf(1.3, 200000) % 3000).astype(np.uint16), 2, True))
     c.append(("huf16_x1_u16", 8, (rng.zipf(1.2, 900) % 1000).astype(np.uint16), 2, True))
     c.append(("huf16_wide_u16", 8, np.minimum(rng.geometric(1 / 3000, 150000), 65535).astype(np.uint16), 2, True))
+    # ZL_GRAPH_ENTROPY (EBM_any): per chunk FSE, Huffman, flatpack, bitpack,
+    # constant or store
+    lowent = np.where(rng.random(260000) < 0.98, 0, rng.integers(1, 256, 260000)).astype(np.uint8)
+    c.append(("entropy_serial_lowent_fse", 17, lowent, 0))
+    c.append(("entropy_serial_skewed_huf", 17, (rng.zipf(1.3, 300000) % 256).astype(np.uint8), 0))
+    c.append(("entropy_serial_geom_mixed", 17, np.minimum(rng.geometric(0.2, 250000), 255).astype(np.uint8), 0))
+    c.append(("entropy_serial_small_alpha", 17, rng.integers(0, 37, 30000).astype(np.uint8), 0))
+    c.append(("entropy_serial_uniform_store", 17, rng.integers(0, 256, 50000).astype(np.uint8), 0))
     return c
 
 

@@ -43,6 +43,8 @@ def _graph(oz, comp, recipe):
         return a.GRAPH_FLATPACK
     if recipe == 15:
         return a.GRAPH_BITPACK
+    if recipe == 17:
+        return a.GRAPH_ENTROPY
     if recipe == 5:
         return comp.tokenize(a.TYPE_NUMERIC, False, a.GRAPH_STORE, comp.node(a.NODE_BITPACK_INT, a.GRAPH_HUFFMAN))
     if recipe == 6:
@@ -68,6 +70,11 @@ def _cases():
             if recipe == 13:
                 a[:] = 7
             c.append((recipe, a))
+    # the entropy graph: Huffman, FSE (low entropy), flatpack and store chunks
+    for n in (3, 5000, 120000, 260000):
+        c.append((17, (rng.zipf(1.3, n) % 41).astype(np.uint8)))
+        c.append((17, np.where(rng.random(n) < 0.98, 0, rng.integers(1, 256, n)).astype(np.uint8)))
+    c.append((17, rng.integers(0, 256, 40000).astype(np.uint8)))
     return c
 
 
@@ -86,7 +93,7 @@ def test_cctx_frames_equal_reference_frames(gpu_lib, checksums):
         if not checksums:
             cctx.set_parameter(a.CPARAM_CONTENT_CHECKSUM, 2)
             cctx.set_parameter(a.CPARAM_COMPRESSED_CHECKSUM, 2)
-        serial = recipe in (0, 7, 8, 13, 14, 15)
+        serial = recipe in (0, 7, 8, 13, 14, 15, 17)
         got = cctx.compress(arr.tobytes()) if serial else cctx.compress_numeric(arr)
         want = oracle.compress(recipe, arr, 0 if serial else arr.itemsize, checksums=checksums)
         if got.tobytes() != want.tobytes():

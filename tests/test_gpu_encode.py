@@ -43,6 +43,11 @@ def _cases(seed):
     c.append((13, np.full(4000, 9, np.uint8), 0))
     c.append((14, rng.integers(0, 37, 3000).astype(np.uint8), 0))
     c.append((15, rng.integers(0, 37, 3000).astype(np.uint8), 0))
+    # the entropy graph (FSE or Huffman per chunk)
+    for n in (2, 999, 5000, 100000, 300000):
+        for k in (3, 37, 256):
+            c.append((17, (rng.zipf(1.2, n) % k).astype(np.uint8), 0))
+        c.append((17, np.where(rng.random(n) < 0.98, 0, rng.integers(1, 256, n)).astype(np.uint8), 0))
     c.append((0, rng.integers(0, 256, 3000).astype(np.uint8), 0))
     return c
 
