@@ -134,21 +134,12 @@ const char* ozl_gpu_version(void) { return "openzl_gb300 0.1 (sm_103a)"; }
 
 ZL_Report ZL_getDecompressedSize(const void* src, size_t size)
 {
-    if (!src || size < 7) return fail(ZL_ErrorCode_srcSize_tooSmall);
-    const uint8_t* p = static_cast<const uint8_t*>(src);
-    uint32_t const magic = uint32_t(p[0]) | (uint32_t(p[1]) << 8) | (uint32_t(p[2]) << 16) | (uint32_t(p[3]) << 24);
-    if (magic < 0xD7B1A5C0u + 21 || magic > 0xD7B1A5C0u + 23) return fail(ZL_ErrorCode_formatVersion_unsupported);
-    if ((p[5] & 15) != 1) return fail(ZL_ErrorCode_invalidRequest_singleOutputFrameOnly);
-    uint64_t v = 0;
-    size_t i = 6;
-    for (int sh = 0; sh < 70; sh += 7) {
-        if (i >= size) return fail(ZL_ErrorCode_srcSize_tooSmall);
-        uint8_t b = p[i++];
-        v |= uint64_t(b & 0x7f) << sh;
-        if (!(b & 0x80)) break;
-    }
-    if (v == 0) return fail(ZL_ErrorCode_temporaryLibraryLimitation);
-    return ok(size_t(v - 1));
+    if (!src) return fail(ZL_ErrorCode_srcSize_tooSmall);
+    ozl::FrameHeader h;
+    std::string err;
+    int rc = ozl::parseFrameHeader(static_cast<const uint8_t*>(src), size, h, err);
+    if (rc) return fail(rc);
+    return ok(size_t(h.outSize));
 }
 
 ZL_Report ZL_getCompressedSize(const void* src, size_t size)
@@ -522,16 +513,15 @@ struct ZL_FrameInfo_s {
 
 ZL_FrameInfo* ZL_FrameInfo_create(const void* src, size_t cSize)
 {
-    ZL_Report ds = ZL_getDecompressedSize(src, cSize);
-    if (ZL_isError(ds)) return nullptr;
-    const uint8_t* p = static_cast<const uint8_t*>(src);
-    static const ZL_Type map[4] = { ZL_Type_serial, ZL_Type_struct, ZL_Type_numeric, ZL_Type_string };
+    if (!src) return nullptr;
+    ozl::FrameHeader h;
+    std::string err;
+    if (ozl::parseFrameHeader(static_cast<const uint8_t*>(src), cSize, h, err)) return nullptr;
     ZL_FrameInfo_s* fi = new (std::nothrow) ZL_FrameInfo_s();
     if (!fi) return nullptr;
-    uint32_t const magic = uint32_t(p[0]) | (uint32_t(p[1]) << 8) | (uint32_t(p[2]) << 16) | (uint32_t(p[3]) << 24);
-    fi->version = magic - 0xD7B1A5C0u;
-    fi->type = map[(p[5] >> 4) & 3];
-    fi->size = ZL_validResult(ds);
+    fi->version = h.version;
+    fi->type = ZL_Type(h.outType); // the planner's type codes are ZL_Type's values
+    fi->size = h.outSize;
     return fi;
 }
 void ZL_FrameInfo_free(ZL_FrameInfo* fi) { delete fi; }
@@ -553,6 +543,8 @@ ZL_Report ZL_FrameInfo_getDecompressedSize(const ZL_FrameInfo* fi, int id)
 ZL_Report ZL_FrameInfo_getNumElts(const ZL_FrameInfo* fi, int id)
 {
     if (!fi || id != 0) return fail(ZL_ErrorCode_parameter_invalid);
+    // decode_frameheader.c:448-453: frames before v21 carry no element counts
+    if (fi->version < 21) return fail(ZL_ErrorCode_GENERIC);
     // decode_frameheader.c:455-467: counts known for serial outputs only
     if (fi->type == ZL_Type_struct || fi->type == ZL_Type_numeric) return fail(ZL_ErrorCode_temporaryLibraryLimitation);
     return ok(size_t(fi->size));

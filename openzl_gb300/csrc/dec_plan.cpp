@@ -108,6 +108,7 @@ enum : int {
     E_HEADER = 10,
     E_CORRUPT = 12,
     E_CK_COMPRESSED = 13,
+    E_SINGLE_OUTPUT = 23,
     E_VERSION = 60,
     E_LIMIT = 81,
     E_TRANSFORM = 32,
@@ -250,77 +251,136 @@ int DecodePlan::build(size_t nbFrames, const uint8_t* const* hFrames, const size
     return 0;
 }
 
-// Frame header (src/openzl/decompress/decode_frameheader.c:237-340).
-int DecodePlan::planFrame(int f, const uint8_t* src, size_t size, size_t dstCap, bool ckContent,
-                          bool ckCompressed, std::string& err)
+// Frame header. Versions 21+ open with a flags byte and store the output
+// count, types and varint sizes after it (decode_frameheader.c:94-107,
+// 148-173, 193-250, 270-370); versions 8..20 pack the count and types into
+// byte 4 onwards, store LE32 sizes and keep the checksum flags in the block
+// header (decode_frameheader.c:58-92, 110-147, 177-190).
+int parseFrameHeader(const uint8_t* src, size_t size, FrameHeader& h, std::string& err)
 {
-    if (size < 9) { err = "frame too small"; return E_SRC_SMALL; }
+    h = FrameHeader();
+    if (size < 8) { err = "frame too small"; return E_SRC_SMALL; }
     uint32_t const magic = readLE32(src);
-    if (magic < 0xD7B1A5C0u + 21 || magic > 0xD7B1A5C0u + 23) {
+    // ZL_MIN_FORMAT_VERSION .. ZL_MAX_FORMAT_VERSION (include/openzl/zl_version.h:49-57)
+    if (magic < 0xD7B1A5C0u + 8 || magic > 0xD7B1A5C0u + 23) {
         err = "unsupported format version or bad magic";
         return E_VERSION;
     }
     unsigned const version = magic - 0xD7B1A5C0u;
-    size_t pos = 4;
-    uint8_t const flags = src[pos++];
-    bool const hasContentCk = flags & 1, hasCompressedCk = (flags >> 1) & 1, hasComment = (flags >> 2) & 1;
-    uint8_t const t1 = src[pos++];
-    size_t const nbOut = t1 & 15;
-    if (nbOut != 1) { err = "only single-output frames are supported"; return E_LIMIT; }
+    h.version = version;
     static const int typeMap[4] = { TY_SERIAL, TY_STRUCT, TY_NUMERIC, TY_STRING };
-    int const outType = typeMap[(t1 >> 4) & 3];
-    if (outType == TY_STRING) { err = "string outputs are not supported"; return E_LIMIT; }
-    Reader rd{ src + pos, src + size };
-    uint64_t sz1;
-    if (!rd.varint(sz1) || sz1 == 0) { err = "unknown decompressed size"; return E_LIMIT; }
-    uint64_t const outSize = sz1 - 1;
-    if (outSize > dstCap) { err = "destination too small"; return E_DST_SMALL; }
-    if (version >= 22 && hasComment) {
-        uint64_t c;
-        if (!rd.varint(c) || c == 0 || c > size_t(rd.end - rd.p)) { err = "bad comment"; return E_CORRUPT; }
-        rd.p += c;
+    if (version < 21) {
+        size_t pos = 4 + (version >= 14);
+        if (version >= 15 && (src[4] >> 6) != 0) {
+            err = "only single-output frames are supported";
+            return E_SINGLE_OUTPUT;
+        }
+        h.outType = version >= 14 ? typeMap[src[4] & 3] : TY_SERIAL;
+        if (pos + 4 > size) { err = "truncated frame header"; return E_SRC_SMALL; }
+        h.outSize = readLE32(src + pos);
+        h.end = pos + 4;
+    } else {
+        if (size < 9) { err = "frame too small"; return E_SRC_SMALL; }
+        uint8_t const flags = src[4];
+        h.hasContentCk = flags & 1;
+        h.hasCompressedCk = (flags >> 1) & 1;
+        bool const hasComment = (flags >> 2) & 1;
+        uint8_t const t1 = src[5];
+        if ((t1 & 15) != 1) { err = "only single-output frames are supported"; return E_SINGLE_OUTPUT; }
+        h.outType = typeMap[(t1 >> 4) & 3];
+        Reader rd{ src + 6, src + size };
+        uint64_t sz1;
+        if (!rd.varint(sz1)) { err = "truncated frame header"; return E_SRC_SMALL; }
+        if (sz1 == 0) { err = "unknown decompressed size"; return E_LIMIT; }
+        h.outSize = sz1 - 1;
+        if (version >= 22 && hasComment) {
+            uint64_t c;
+            if (!rd.varint(c) || c == 0 || c > size_t(rd.end - rd.p)) { err = "bad comment"; return E_CORRUPT; }
+            rd.p += c;
+        }
+        h.end = size_t(rd.p - src);
+        if (h.hasCompressedCk) {
+            if (h.end + 1 > size) { err = "truncated header"; return E_SRC_SMALL; }
+            h.hdrCk = true;
+            h.end++;
+        }
     }
-    pos = size_t(rd.p - src);
-    if (hasCompressedCk) {
-        if (pos + 1 > size) { err = "truncated header"; return E_SRC_SMALL; }
-        // header checksum byte: low 8 bits of XXH3 over the header; verified on
-        // the device together with the block checksums.
-        if (ckCompressed)
-            hashes.push_back(PlanHash{ f, false, 0, pos, src[pos], E_CK_COMPRESSED, true });
-        pos++;
-    }
-    frames[f].outType = outType;
+    if (h.outType == TY_STRING) { err = "string outputs are not supported"; return E_LIMIT; }
+    return 0;
+}
+
+int DecodePlan::planFrame(int f, const uint8_t* src, size_t size, size_t dstCap, bool ckContent,
+                          bool ckCompressed, std::string& err)
+{
+    FrameHeader h;
+    int rc = parseFrameHeader(src, size, h, err);
+    if (rc) return rc;
+    if (h.outSize > dstCap) { err = "destination too small"; return E_DST_SMALL; }
+    size_t pos = h.end;
+    // header checksum byte: low 8 bits of XXH3 over the header; verified on
+    // the device together with the block checksums.
+    if (h.hdrCk && ckCompressed)
+        hashes.push_back(PlanHash{ f, false, 0, pos - 1, src[pos - 1], E_CK_COMPRESSED, true });
+    frames[f].outType = h.outType;
     uint64_t produced = 0;
     for (;;) {
-        if (pos >= size) { err = "missing end-of-frame marker"; return E_SRC_SMALL; }
-        if (src[pos] == 0) break;
+        // versions before 21 hold one block and no end-of-frame marker
+        // (decompress2.c:1689-1714)
+        if (h.version >= 21) {
+            if (pos >= size) { err = "missing end-of-frame marker"; return E_SRC_SMALL; }
+            if (src[pos] == 0) { pos++; break; }
+        }
         size_t consumed = 0;
         uint64_t blockBytes = 0;
-        int rc = planBlock(f, src, size, pos, &consumed, hasContentCk, hasCompressedCk, ckContent,
-                           ckCompressed, nbOut, produced, &blockBytes, err);
+        rc = planBlock(f, h.version, src, size, pos, &consumed, h.hasContentCk, h.hasCompressedCk, ckContent,
+                       ckCompressed, 1, produced, &blockBytes, err);
         if (rc) return rc;
         pos += consumed;
         produced += blockBytes;
+        if (h.version < 21) break;
     }
-    if (produced != outSize) { err = "decoded size does not match the frame header"; return E_CORRUPT; }
-    frames[f].decodedSize = outSize;
-    frames[f].frameBytes = pos + 1;
+    if (produced != h.outSize) { err = "decoded size does not match the frame header"; return E_CORRUPT; }
+    frames[f].decodedSize = h.outSize;
+    frames[f].frameBytes = pos;
     return 0;
 }
 
 // One block: chunk header (src/openzl/decompress/decode_frameheader.c:938-1171),
 // stored streams (src/openzl/decompress/decompress2.c:632-834), checksums
 // (decompress2.c:1478-1570).
-int DecodePlan::planBlock(int f, const uint8_t* src, size_t size, size_t start, size_t* consumed,
-                          bool hasContentCk, bool hasCompressedCk, bool ckContent, bool ckCompressed,
-                          size_t nbOutputs, uint64_t outOffset, uint64_t* outBytes, std::string& err)
+int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t size, size_t start,
+                          size_t* consumed, bool hasContentCk, bool hasCompressedCk, bool ckContent,
+                          bool ckCompressed, size_t nbOutputs, uint64_t outOffset, uint64_t* outBytes,
+                          std::string& err)
 {
     Reader rd{ src + start, src + size };
     uint64_t nd, ns;
-    if (!rd.varint(nd) || nd == 0) { err = "bad decoder count"; return E_CORRUPT; }
-    nd--;
-    if (!rd.varint(ns)) { err = "bad stored-stream count"; return E_CORRUPT; }
-    if (nd >= 20000 || ns >= 110000) { err = "graph too large"; return E_LIMIT; }
+    // counts: single bytes before v9, varints after; the decoder count is
+    // stored +1 from v21 (decode_frameheader.c:954-972)
+    if (version < 9) {
+        if (rd.end - rd.p < 2) { err = "truncated block header"; return E_SRC_SMALL; }
+        nd = rd.p[0];
+        ns = rd.p[1];
+        rd.p += 2;
+    } else {
+        if (!rd.varint(nd)) { err = "bad decoder count"; return E_CORRUPT; }
+        if (version >= 21) {
+            if (nd == 0) { err = "bad decoder count"; return E_CORRUPT; }
+            nd--;
+        }
+        if (!rd.varint(ns)) { err = "bad stored-stream count"; return E_CORRUPT; }
+    }
+    // ZL_runtimeNodeLimit / ZL_runtimeStreamLimit (src/openzl/common/limits.c:18-46)
+    uint64_t const nodeLimit = version < 9 ? 256 : version < 20 ? 10000 : 20000;
+    uint64_t const streamLimit = version < 9 ? 256 : version < 16 ? 10000 : 110000;
+    if (nd >= nodeLimit || ns >= streamLimit) { err = "graph too large"; return E_LIMIT; }
+    // before v21 the checksum flags open the block header (decode_frameheader.c:1002-1011)
+    if (version < 21) {
+        if (rd.p >= rd.end) { err = "truncated block header"; return E_SRC_SMALL; }
+        hasContentCk = rd.p[0] & 1;
+        hasCompressedCk = (rd.p[0] >> 1) & 1;
+        rd.p++;
+    }
     std::vector<uint64_t> trt, ids, hflags, vflags, rflags;
     if (!rd.unpack(trt, nd, 1)) { err = "truncated codec types"; return E_SRC_SMALL; }
     for (uint64_t t : trt)
@@ -346,7 +406,12 @@ int DecodePlan::planBlock(int f, const uint8_t* src, size_t size, size_t start, 
             if (!rd.varint(v)) { err = "bad VO count"; return E_CORRUPT; }
             nbVO[u] = v + 1;
         }
-    if (!rd.unpack(rflags, nd, 1)) { err = "truncated regen counts"; return E_SRC_SMALL; }
+    // one regenerated stream per decoder before v16 (decode_frameheader.c:1068-1082)
+    if (version >= 16) {
+        if (!rd.unpack(rflags, nd, 1)) { err = "truncated regen counts"; return E_SRC_SMALL; }
+    } else {
+        rflags.assign(nd, 0);
+    }
     uint64_t totalRegen = 0;
     for (size_t u = 0; u < nd; u++) {
         if (rflags[u]) {
@@ -420,8 +485,12 @@ int DecodePlan::planBlock(int f, const uint8_t* src, size_t size, size_t start, 
     }
     if (hasCompressedCk) {
         if (pos + 4 > size) { err = "truncated checksum"; return E_SRC_SMALL; }
-        if (ckCompressed)
-            hashes.push_back(PlanHash{ f, false, start, pos - start, readLE32(src + pos), E_CK_COMPRESSED, false });
+        if (ckCompressed) {
+            // versions before 21 hash the frame from its first byte, later
+            // ones the block only (decompress2.c:1494-1500)
+            size_t const hs = version < 21 ? 0 : start;
+            hashes.push_back(PlanHash{ f, false, hs, pos - hs, readLE32(src + pos), E_CK_COMPRESSED, false });
+        }
         pos += 4;
     }
 

@@ -87,10 +87,28 @@ struct PlanCopy {
 
 struct FramePlan {
     uint64_t decodedSize = 0;
-    uint64_t frameBytes = 0;  // compressed size including the end-of-frame byte
+    uint64_t frameBytes = 0;  // compressed size, with the end-of-frame byte (v21+)
     int outType = 0;
     uint32_t outWidth = 1;
 };
+
+// Frame-header fields shared by the planner and the frame-information calls.
+// Format versions 8..23; single-output frames only.
+struct FrameHeader {
+    unsigned version = 0;
+    bool hasContentCk = false;    // v21+; older frames carry the flags per block
+    bool hasCompressedCk = false;
+    int outType = 0;              // TY_* of the one output
+    uint64_t outSize = 0;         // its decompressed size in bytes
+    size_t end = 0;               // first byte after the header
+    bool hdrCk = false;           // v21+: header checksum byte at end - 1
+};
+
+// Parses the frame header (src/openzl/decompress/decode_frameheader.c:58-190,
+// 270-370). Returns 0 or a ZL error code: formatVersion_unsupported (60),
+// srcSize_tooSmall (3), invalidRequest_singleOutputFrameOnly (23),
+// temporaryLibraryLimitation (81) for unknown sizes, corruption (12).
+int parseFrameHeader(const uint8_t* src, size_t size, FrameHeader& h, std::string& err);
 
 class DecodePlan {
   public:
@@ -111,7 +129,7 @@ class DecodePlan {
   private:
     int planFrame(int f, const uint8_t* src, size_t size, size_t dstCap, bool ckContent,
                   bool ckCompressed, std::string& err);
-    int planBlock(int f, const uint8_t* src, size_t size, size_t start, size_t* consumed,
+    int planBlock(int f, unsigned version, const uint8_t* src, size_t size, size_t start, size_t* consumed,
                   bool hasContentCk, bool hasCompressedCk, bool ckContent, bool ckCompressed,
                   size_t nbOutputs, uint64_t outOffset, uint64_t* outBytes, std::string& err);
 };

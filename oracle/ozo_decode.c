@@ -831,13 +831,72 @@ static int decode_type(unsigned t)
     return m[t & 3];
 }
 
+/* Frame header of format versions 8..20: no flags byte (the checksum flags
+ * sit in the chunk header), the output count and types packed into byte 4
+ * onwards, sizes as LE32, no comment, no header checksum
+ * (decode_frameheader.c:58-92 count, 110-147 types, 177-190 sizes). */
+static int64_t parse_frame_header_v20(FrameHdr* fh, const uint8_t* src, size_t size)
+{
+    unsigned const v = fh->version;
+    size_t pos = 4, nbOut = 1;
+    if (v >= 15) {
+        if (size < pos + 1 + 4) return -OZO_ERR_SRC_SIZE;
+        nbOut = (size_t)(src[pos++] >> 6) + 1;
+        if (nbOut == 4) {
+            if (pos >= size) return -OZO_ERR_SRC_SIZE;
+            nbOut = (size_t)(src[pos++] >> 4) + 4;
+        }
+        if (nbOut == 19) {
+            if (pos >= size) return -OZO_ERR_SRC_SIZE;
+            nbOut = (size_t)src[pos++] + 19;
+        }
+        if (nbOut == 274) {
+            if (pos + 2 > size) return -OZO_ERR_SRC_SIZE;
+            nbOut = (size_t)ozo_rd16(src + pos) + 274;
+            pos += 2;
+        }
+    } else if (v == 14) {
+        pos++; /* the type byte */
+    }
+    if (nbOut > 14) return -OZO_ERR_UNSUPPORTED;
+    fh->nbOutputs = nbOut;
+    if (v < 14) {
+        fh->types[0] = OZO_TYPE_SERIAL;
+    } else {
+        if (size < 5) return -OZO_ERR_SRC_SIZE;
+        for (size_t n = 0; n < nbOut && n < 3; n++) fh->types[n] = decode_type(src[4] >> (2 * n));
+        if (nbOut > 3) {
+            if (size < 6) return -OZO_ERR_SRC_SIZE;
+            for (size_t n = 3; n < nbOut && n < 5; n++) fh->types[n] = decode_type(src[5] >> (2 * (n - 3)));
+        }
+        uint8_t tok = 0;
+        for (size_t n = 5; n < nbOut; n++) {
+            size_t const sh = ((n - 5) % 4) * 2;
+            if (sh == 0) {
+                if (pos >= size) return -OZO_ERR_SRC_SIZE;
+                tok = src[pos++];
+            }
+            fh->types[n] = decode_type(tok >> sh);
+        }
+    }
+    if (pos + 4 * nbOut > size) return -OZO_ERR_SRC_SIZE;
+    for (size_t n = 0; n < nbOut; n++) fh->sizes[n] = ozo_rd32(src + pos + 4 * n);
+    pos += 4 * nbOut;
+    for (size_t n = 0; n < nbOut; n++)
+        if (fh->types[n] == OZO_TYPE_STRING) return -OZO_ERR_UNSUPPORTED;
+    fh->headerSize = pos;
+    return (int64_t)pos;
+}
+
 static int64_t parse_frame_header(FrameHdr* fh, const uint8_t* src, size_t size)
 {
     memset(fh, 0, sizeof(*fh));
     if (size < 9) return -OZO_ERR_SRC_SIZE;
     uint32_t const magic = ozo_rd32(src);
-    if (magic < OZO_MAGIC_BASE + 21 || magic > OZO_MAGIC_BASE + 23) return -OZO_ERR_VERSION;
+    /* ZL_MIN_FORMAT_VERSION .. ZL_MAX_FORMAT_VERSION (openzl/zl_version.h) */
+    if (magic < OZO_MAGIC_BASE + 8 || magic > OZO_MAGIC_BASE + 23) return -OZO_ERR_VERSION;
     fh->version = magic - OZO_MAGIC_BASE;
+    if (fh->version < 21) return parse_frame_header_v20(fh, src, size);
     size_t pos = 4;
     uint8_t const flags = src[pos++];
     fh->hasContentCk = flags & 1;
@@ -898,11 +957,36 @@ static int64_t decode_block(const FrameHdr* fh, const uint8_t* src, size_t size,
 {
     const uint8_t* p = src + start;
     const uint8_t* const end = src + size;
+    unsigned const ver = fh->version;
     uint64_t nbDec, nbStored;
-    if (ozo_varint_dec(&p, end, &nbDec) || nbDec == 0) return -OZO_ERR_CORRUPTION;
-    nbDec--;
-    if (ozo_varint_dec(&p, end, &nbStored)) return -OZO_ERR_CORRUPTION;
-    if (nbDec >= 20000 || nbStored >= 110000) return -OZO_ERR_CORRUPTION;
+    /* counts: single bytes before v9, varints after; the decoder count is
+     * stored +1 from v21 (decode_frameheader.c:954-972) */
+    if (ver < 9) {
+        if (end - p < 2) return -OZO_ERR_SRC_SIZE;
+        nbDec = p[0];
+        nbStored = p[1];
+        p += 2;
+    } else {
+        if (ozo_varint_dec(&p, end, &nbDec)) return -OZO_ERR_CORRUPTION;
+        if (ver >= 21) {
+            if (nbDec == 0) return -OZO_ERR_CORRUPTION;
+            nbDec--;
+        }
+        if (ozo_varint_dec(&p, end, &nbStored)) return -OZO_ERR_CORRUPTION;
+    }
+    /* ZL_runtimeNodeLimit / ZL_runtimeStreamLimit (common/limits.c:18-46) */
+    uint64_t const nodeLimit = ver < 9 ? 256 : ver < 20 ? 10000 : 20000;
+    uint64_t const streamLimit = ver < 9 ? 256 : ver < 16 ? 10000 : 110000;
+    if (nbDec >= nodeLimit || nbStored >= streamLimit) return -OZO_ERR_CORRUPTION;
+    /* before v21 the checksum flags open the chunk header
+     * (decode_frameheader.c:1002-1011) */
+    int hasContentCk = fh->hasContentCk, hasCompressedCk = fh->hasCompressedCk;
+    if (ver < 21) {
+        if (p >= end) return -OZO_ERR_SRC_SIZE;
+        hasContentCk = p[0] & 1;
+        hasCompressedCk = (p[0] >> 1) & 1;
+        p++;
+    }
     size_t const nd = (size_t)nbDec, ns = (size_t)nbStored;
     DNode* nodes = (DNode*)calloc(nd + 1, sizeof(DNode));
     uint64_t* tmp = (uint64_t*)calloc(nd + ns + 8, 8);
@@ -953,10 +1037,15 @@ static int64_t decode_block(const FrameHdr* fh, const uint8_t* src, size_t size,
             nodes[u].nbVOs = (size_t)v + 1;
         }
     }
-    /* number of regenerated streams: 1-bit flags, then varint(n-2) */
-    r = bitunpack(tmp, nd, p, (size_t)(end - p), 1);
-    if (r == (size_t)-1) FAIL(OZO_ERR_SRC_SIZE);
-    p += r;
+    /* number of regenerated streams: 1-bit flags, then varint(n-2); every
+     * decoder regenerates one stream before v16 (decode_frameheader.c:1068-1082) */
+    if (ver >= 16) {
+        r = bitunpack(tmp, nd, p, (size_t)(end - p), 1);
+        if (r == (size_t)-1) FAIL(OZO_ERR_SRC_SIZE);
+        p += r;
+    } else {
+        memset(tmp, 0, nd * sizeof(tmp[0]));
+    }
     size_t totalRegens = 0;
     for (size_t u = 0; u < nd; u++) {
         nodes[u].nbRegens = 1;
@@ -1020,15 +1109,18 @@ static int64_t decode_block(const FrameHdr* fh, const uint8_t* src, size_t size,
         free(isRegen);
         if (st != ns) FAIL(OZO_ERR_CORRUPTION);
         uint32_t contentCk = 0;
-        if (fh->hasContentCk) {
+        if (hasContentCk) {
             if (pos + 4 > size) FAIL(OZO_ERR_SRC_SIZE);
             contentCk = ozo_rd32(src + pos);
             pos += 4;
         }
-        if (fh->hasCompressedCk) {
+        if (hasCompressedCk) {
+            /* versions before 21 hash the frame from its first byte, later
+             * ones the current block only (decompress2.c:1494-1500) */
+            size_t const hs = ver < 21 ? 0 : start;
             if (pos + 4 > size) FAIL(OZO_ERR_SRC_SIZE);
             uint32_t const want = ozo_rd32(src + pos);
-            if ((uint32_t)ozo_xxh3_64(src + start, pos - start) != want) FAIL(OZO_ERR_CHECKSUM);
+            if ((uint32_t)ozo_xxh3_64(src + hs, pos - hs) != want) FAIL(OZO_ERR_CHECKSUM);
             pos += 4;
         }
         /* run decoders in order */
@@ -1084,7 +1176,7 @@ static int64_t decode_block(const FrameHdr* fh, const uint8_t* src, size_t size,
                 if (outType[o] == 0) { outType[o] = s->type; outW[o] = s->w; }
                 else if (outType[o] != s->type || outW[o] != s->w) { free(cat); FAIL(OZO_ERR_CORRUPTION); }
             }
-            if (fh->hasContentCk && (uint32_t)ozo_xxh3_64(cat, catLen) != contentCk) {
+            if (hasContentCk && (uint32_t)ozo_xxh3_64(cat, catLen) != contentCk) {
                 free(cat);
                 FAIL(OZO_ERR_CHECKSUM);
             }
@@ -1131,11 +1223,16 @@ int64_t ozo_decompress(const void* srcv, size_t size, void* dst, size_t dstCap, 
     int types[1] = { 0 };
     size_t ws[1] = { 0 };
     for (;;) {
-        if (pos >= size) { free(bufs[0]); return -OZO_ERR_SRC_SIZE; }
-        if (src[pos] == 0) { pos++; break; }
+        /* versions before 21 hold exactly one block and no end marker
+         * (decompress2.c:1689-1714) */
+        if (fh.version >= 21) {
+            if (pos >= size) { free(bufs[0]); return -OZO_ERR_SRC_SIZE; }
+            if (src[pos] == 0) { pos++; break; }
+        }
         int64_t b = decode_block(&fh, src, size, pos, bufs, lens, types, ws);
         if (b < 0) { free(bufs[0]); return b; }
         pos += (size_t)b;
+        if (fh.version < 21) break;
     }
     if (lens[0] != fh.sizes[0]) { free(bufs[0]); return -OZO_ERR_CORRUPTION; }
     if (lens[0] > dstCap) { free(bufs[0]); return -OZO_ERR_DST_SIZE; }

@@ -82,6 +82,33 @@ def build_cases():
     c.append(("entropy_serial_geom_mixed", 17, np.minimum(rng.geometric(0.2, 250000), 255).astype(np.uint8), 0))
     c.append(("entropy_serial_small_alpha", 17, rng.integers(0, 37, 30000).astype(np.uint8), 0))
     c.append(("entropy_serial_uniform_store", 17, rng.integers(0, 256, 50000).astype(np.uint8), 0))
+    # older wire formats, written by the reference at a pinned format version
+    # (decode-only: the encoders here write the newest version). Versions
+    # 16..20 differ from 21+ in the frame and block headers only; 15 also
+    # lacks the per-decoder regenerated-stream counts; 14 has no output
+    # count; 8..13 have untyped outputs (serial only) and byte-sized block
+    # counts before 9. Entropy-coded frames start at 15 (fse_v2/huffman_v2).
+    for v in (20, 16, 15):
+        c.append(("v%d_walk_u32_dz_tsplit_fse" % v, 1, walk(rng, 20000, np.uint32, 100), 4, True, v))
+        c.append(("v%d_ts_i64_dz_bitpack_huf" % v, 2, timestamps(rng, 6000), 8, True, v))
+        c.append(("v%d_walk_u16_d_tsplit_fse" % v, 3, walk(rng, 15001, np.uint16, 3000), 2, True, v))
+        c.append(("v%d_walk_u64_d_bitpack_huf" % v, 4, walk(rng, 4003, np.uint64, 300), 8, True, v))
+        c.append(("v%d_tokenize_zipf_i32" % v, 5, keys[(rng.zipf(1.1, 20000) - 1) % 10000], 4, True, v))
+        c.append(("v%d_fse_serial_skewed" % v, 7, (rng.zipf(1.3, 20000) % 256).astype(np.uint8), 0, True, v))
+        c.append(("v%d_huf_serial_skewed" % v, 8, (rng.zipf(1.3, 20000) % 256).astype(np.uint8), 0, True, v))
+        c.append(("v%d_huf16_zipf_u16" % v, 8, (rng.zipf(1.3, 12000) % 3000).astype(np.uint16), 2, True, v))
+        c.append(("v%d_entropy_serial_geom" % v, 17, np.minimum(rng.geometric(0.2, 20000), 255).astype(np.uint8), 0, True, v))
+        c.append(("v%d_walk_u32_zigzag_store" % v, 10, walk(rng, 3001, np.uint32, 100), 4, True, v))
+    for v in (14, 13, 9, 8):
+        if v == 14:
+            c.append(("v14_walk_u32_delta_store", 9, walk(rng, 3002, np.uint32, 100), 4, True, v))
+            c.append(("v14_walk_u16_bitpack_store", 11, walk(rng, 2001, np.uint16, 100, start=500), 2, True, v))
+            c.append(("v14_walk_u64_tsplit_store", 12, walk(rng, 1003, np.uint64, 100), 8, True, v))
+        if v >= 11:
+            c.append(("v%d_constant_serial" % v, 13, np.full(3000, 9, np.uint8), 0, True, v))
+        c.append(("v%d_flatpack_serial" % v, 14, rng.integers(0, 37, 9000).astype(np.uint8), 0, True, v))
+        c.append(("v%d_bitpack_graph_serial" % v, 15, rng.integers(0, 21, 9000).astype(np.uint8), 0, True, v))
+        c.append(("v%d_store_serial" % v, 0, rng.integers(0, 256, 1500).astype(np.uint8), 0, True, v))
     return c
 
 
@@ -95,6 +122,7 @@ def main():
     manifest = []
     for name, recipe, arr, w, *flags in build_cases():
         decode_only = bool(flags and flags[0])
+        version = flags[1] if len(flags) > 1 else 0  # 0: the newest format
         arr = np.ascontiguousarray(arr)
         for cs in (1, 0):
             if cs == 0 and recipe not in (1, 2, 3, 4, 5):
@@ -102,7 +130,8 @@ def main():
             cap = lib.ref_compressBound(arr.nbytes) + 4096
             dst = np.zeros(cap, np.uint8)
             n = arr.size if w else arr.nbytes
-            r = lib.ref_compress(recipe, arr.ctypes.data if arr.size else None, n, w, dst.ctypes.data, cap, cs, 0)
+            r = lib.ref_compress(recipe, arr.ctypes.data if arr.size else None, n, w, dst.ctypes.data, cap, cs,
+                                 version)
             if r <= 0:
                 print("skip", name, cs, r)
                 continue
@@ -113,7 +142,8 @@ def main():
                              "checksums": cs, "frame_bytes": int(r),
                              "sha256_in": hashlib.sha256(arr.tobytes()).hexdigest(),
                              "sha256_frame": hashlib.sha256(dst[:r].tobytes()).hexdigest(),
-                             **({"decode_only": True} if decode_only else {})})
+                             **({"decode_only": True} if decode_only else {}),
+                             **({"format_version": version} if version else {})})
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
     tot = sum(os.path.getsize(os.path.join(HERE, m["case"] + ".zl")) for m in manifest)

@@ -77,14 +77,23 @@ def test_frame_info_on_golden_frames(lib, manifest):
 
     types = {"serial": 1, "struct": 2, "numeric": 4}
     for m in manifest:
-        fi = oz.FrameInfo(read_frame(m["case"]))
-        assert fi.format_version() == 23
+        fr = read_frame(m["case"])
+        fi = oz.FrameInfo(fr)
+        v = m.get("format_version", 23)
+        assert fi.format_version() == v
         assert fi.num_outputs() == 1
         width = m["elt_width"] or 1
         assert fi.decompressed_size() == m["n"] * width, m["case"]
+        assert oz.get_decompressed_size(fr) == m["n"] * width, m["case"]
+        assert oz.get_compressed_size(fr) == len(fr), m["case"]
         t = fi.output_type()
         assert t in types.values()
-        if t == 1:
+        if v < 21:
+            # decode_frameheader.c:448-453: no element counts before v21
+            with pytest.raises(oz.ZLError) as e:
+                fi.num_elts()
+            assert e.value.code == 1
+        elif t == 1:
             assert fi.num_elts() == m["n"] * width
         else:
             # decode_frameheader.c:455-467: not known for struct/numeric outputs

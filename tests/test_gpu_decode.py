@@ -226,3 +226,34 @@ def test_huffman16_frames_run_the_16bit_kernel(gpu_lib, manifest):
     b.check(s.cuda_stream)
     for m, n, o in zip(cases, sizes, outs):
         assert hashlib.sha256(o[:n].cpu().numpy().tobytes()).hexdigest() == m["sha256_in"], m["case"]
+
+
+def test_older_format_versions_on_the_gpu(gpu_lib, manifest):
+    """Frames of format versions 8..20 decode bit-exactly through the batch
+    API, with their checksums verified on the device; a payload byte flipped
+    in a v20 frame fails the compressed checksum, which before v21 spans the
+    frame from its first byte."""
+    import torch
+    import openzl_gb300 as oz
+
+    cases = [m for m in manifest if m.get("format_version", 23) < 21]
+    assert len(cases) >= 40
+    frames = [read_frame(m["case"]) for m in cases]
+    dfr = [_dev(torch, f) for f in frames]
+    sizes = [oz.get_decompressed_size(f) for f in frames]
+    outs = [torch.zeros(max(n, 1) + 64, dtype=torch.uint8, device="cuda") for n in sizes]
+    s = torch.cuda.Stream()
+    b = oz.GpuBatch()
+    b.plan(frames, [d.data_ptr() for d in dfr], [o.data_ptr() for o in outs], sizes)
+    torch.cuda.synchronize()
+    kinds = {k for k, _, _ in b.profile(s.cuda_stream, capacity=256)}
+    assert {"fse", "huffman", "huffman16"} <= kinds, kinds
+    b.run(s.cuda_stream, graph=True)
+    b.check(s.cuda_stream)
+    for m, n, o in zip(cases, sizes, outs):
+        assert hashlib.sha256(o[:n].cpu().numpy().tobytes()).hexdigest() == m["sha256_in"], m["case"]
+    fr = bytearray(read_frame("v20_walk_u32_dz_tsplit_fse"))
+    fr[len(fr) // 2] ^= 0x01
+    with pytest.raises(oz.ZLError) as e:
+        oz.DCtx().decompress(bytes(fr))
+    assert e.value.code in (12, 13, 14)

@@ -27,6 +27,51 @@ def test_oracle_detects_checksum_corruption(manifest):
         oracle.decompress(bytes(fr))
 
 
+def test_oracle_older_format_versions(manifest):
+    """Frames of format versions 8..20 (header-only differences, one block,
+    checksums over the whole frame) decode, and a payload byte flipped in a
+    v20 frame fails its compressed checksum, which spans the frame from its
+    first byte."""
+    old = [m for m in manifest if m.get("format_version", 23) < 21]
+    assert {m["format_version"] for m in old} >= {8, 14, 15, 16, 20}
+    for m in old:
+        out, _, _ = oracle.decompress(read_frame(m["case"]))
+        assert hashlib.sha256(out.tobytes()).hexdigest() == m["sha256_in"], m["case"]
+    m = next(m for m in old if m["case"] == "v20_walk_u32_dz_tsplit_fse")
+    fr = bytearray(read_frame(m["case"]))
+    fr[len(fr) // 2] ^= 0x40
+    with pytest.raises(ValueError):
+        oracle.decompress(bytes(fr))
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
+def test_oracle_matches_reference_at_older_format_versions():
+    """Seeded inputs compressed by the reference at every format version from
+    15 to 20 (and 14 for graphs without entropy coding) decode in the oracle."""
+    import ctypes
+
+    ref = ctypes.CDLL(REF_DRIVER)
+    ref.ref_compress.restype = ctypes.c_int64
+    ref.ref_compress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(7)
+    cases = [(1, 4, np.uint32), (2, 8, np.int64), (3, 2, np.uint16), (4, 1, np.uint8), (9, 4, np.uint32),
+             (10, 8, np.uint64), (11, 2, np.uint16), (12, 4, np.uint32)]
+    for v in range(14, 21):
+        for recipe, w, dt in cases:
+            if v == 14 and recipe < 9:
+                continue  # entropy coding before v15 uses the deprecated codecs
+            for n in (1, 1000, 40001):
+                arr = (500 + np.cumsum(rng.integers(-50, 51, n))).astype(dt)
+                cap = arr.nbytes * 2 + 4096
+                dst = np.zeros(cap, np.uint8)
+                for cs in (0, 1):
+                    r = ref.ref_compress(recipe, arr.ctypes.data, n, w, dst.ctypes.data, cap, cs, v)
+                    assert r > 0, (v, recipe, n)
+                    out, _, _ = oracle.decompress(dst[:r].tobytes())
+                    assert out.tobytes() == arr.tobytes(), (v, recipe, n, cs)
+
+
 @pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
 def test_xxh3_every_length_class_matches_reference():
     import ctypes
