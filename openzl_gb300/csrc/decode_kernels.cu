@@ -882,31 +882,33 @@ struct BitWin3 {
 };
 
 // ---------------------------------------------------------------------------
-// FSE: one lane per chunk, lanes per CTA sized so that four CTAs fit an SM.
-// Each lane keeps its decoding table in shared memory, one 32-bit entry per
-// cell: the symbol (bits 0-7), nbBits (bits 8-15) and the shared-memory byte
-// offset of the cell newStateBase (bits 16-31). A decoder state is the byte
-// offset of its cell, so a transition is one load, and the fields of a pair
-// of transitions come out of one 32-bit window by funnel shifts.
+// FSE: one lane per chunk. Each lane keeps its decoding table in shared
+// memory as two arrays over the cells: a 16-bit entry holding the cell's
+// newStateBase (bits 4-15) and nbBits (bits 0-3), and the cell's symbol byte.
+// Three bytes a cell (6 KiB at tableLog 11) let about 32 chunks reside per
+// SM. A decoder state is a cell index: a transition is one 16-bit load, the
+// symbol one byte load, and the fields of a pair of transitions come out of
+// one 32-bit window by funnel shifts.
 //
 // Table construction restates src/openzl/fse/decompress/fse_decompress.c:
 // 73-171; decode order restates fse_decompress.c:255-337 (state i % nbStates
 // emits symbol i; the last symbol of each state has no transition).
-constexpr uint32_t kFseCtaSmem = 56 * 1024; // four CTAs per SM
+constexpr uint32_t kFseCtaSmem = 56 * 1024; // at most eight tableLog-11 lanes per CTA
 
 constexpr int kFseRing = 16, kFseAhead = 12; // stream ring: 256 bytes per lane, 192 bytes ahead
 
-// per lane: table (4 << tableLog), build counters (512), stream ring
-__host__ __device__ __forceinline__ uint32_t fseSlotBytes(uint32_t tlMax) { return (4u << tlMax) + 512u + 16u * kFseRing; }
+// per lane: 16-bit entries (2 << tableLog), symbols (1 << tableLog), stream
+// ring (16-byte aligned for tableLog >= 4)
+__host__ __device__ __forceinline__ uint32_t fseSlotBytes(uint32_t tlMax) { return (3u << tlMax) + 16u * kFseRing; }
 __host__ __device__ __forceinline__ uint32_t fseSmemBytes(uint32_t lanes, uint32_t tlMax)
 {
     return lanes * fseSlotBytes(tlMax);
 }
-static_assert(kFseCtaSmem <= 65536, "FSE states are 16-bit shared-memory offsets");
 
 // Builds the decoding table of task t in the slot at byte `slot` of the CTA's
-// shared memory with all 32 lanes of the warp (every lane calls it).
-//  - Counts: the normalized counts go to the slot's counters; a warp scan of
+// shared memory with all 32 lanes of the warp (every lane calls it); `cum`
+// and `next` are the CTA's build scratch (257 and 256 entries).
+//  - Counts: the normalized counts go to the counters; a warp scan of
 //    the positive counts gives each symbol's first occurrence (cum), and the
 //    count -1 symbols take the top cells in symbol order.
 //  - Spread: occurrence k (symbols in order, each repeated count times) goes
@@ -918,12 +920,12 @@ static_assert(kFseCtaSmem <= 65536, "FSE states are 16-bit shared-memory offsets
 //    counter.
 // The result equals the serial construction of fse_decompress.c:73-171.
 __device__ __forceinline__ void fseBuildWarp(const FseTask& t, uint8_t* smem, uint32_t slot, uint32_t tlMax,
-                                             uint16_t* cum)
+                                             uint16_t* cum, uint16_t* next)
 {
     uint32_t const lane = threadIdx.x;
     uint32_t const lt = (1u << lane) - 1u;
-    uint32_t* const tab = reinterpret_cast<uint32_t*>(smem + slot);
-    uint16_t* const next = reinterpret_cast<uint16_t*>(smem + slot + (4u << tlMax));
+    uint16_t* const tab = reinterpret_cast<uint16_t*>(smem + slot);
+    uint8_t* const symOf = smem + slot + (2u << tlMax);
     uint32_t const tl = t.tableLog;
     uint32_t const size = 1u << tl, mask = size - 1;
     uint32_t const step = (size >> 1) + (size >> 3) + 3;
@@ -961,7 +963,7 @@ __device__ __forceinline__ void fseBuildWarp(const FseTask& t, uint8_t* smem, ui
         cum[sy] = uint16_t(c0);
         c0 += v[k] > 0 ? uint32_t(v[k]) : 0u;
         if (v[k] == -1) {
-            tab[size - 1 - n0] = sy;
+            symOf[size - 1 - n0] = uint8_t(sy);
             next[sy] = 1;
             n0++;
         }
@@ -977,7 +979,7 @@ __device__ __forceinline__ void fseBuildWarp(const FseTask& t, uint8_t* smem, ui
         if (valid) {
             uint32_t const occ = occBase + __popc(bal & lt);
             while (occ >= cumNext && sCur < 255) cumNext = cum[++sCur + 1];
-            tab[pos] = sCur;
+            symOf[pos] = uint8_t(sCur);
         }
         occBase += __popc(bal);
     }
@@ -985,7 +987,7 @@ __device__ __forceinline__ void fseBuildWarp(const FseTask& t, uint8_t* smem, ui
     // cells
     for (uint32_t b0 = 0; b0 < size; b0 += 32) {
         uint32_t const u = b0 + lane;
-        uint32_t const sy = tab[u] & 0xffu;
+        uint32_t const sy = symOf[u];
         uint32_t const m = __match_any_sync(0xffffffffu, sy);
         uint32_t const base = next[sy];
         __syncwarp();
@@ -993,7 +995,7 @@ __device__ __forceinline__ void fseBuildWarp(const FseTask& t, uint8_t* smem, ui
         uint32_t const x = base + __popc(m & lt);
         uint32_t const nb = tl - (31 - __clz(x));
         uint32_t const ns = (x << nb) - size;
-        tab[u] = sy | (nb << 8) | ((slot + 4u * ns) << 16);
+        tab[u] = uint16_t((ns << 4) | nb);
         __syncwarp();
     }
 }
@@ -1003,36 +1005,40 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
 {
     extern __shared__ __align__(16) uint8_t smemFse[];
     __shared__ uint16_t sCum[260];
+    __shared__ __align__(16) uint16_t sNext[256];
     uint32_t const lane = threadIdx.x;
     // every lane of the warp builds every table of the CTA, one at a time
     for (uint32_t k = 0; k < lanes; k++) {
         uint32_t const tk = blockIdx.x * lanes + k;
         if (tk >= nbTasks) break;
         FseTask const tt = tasks[tk];
-        fseBuildWarp(tt, smemFse, k * fseSlotBytes(tableLogMax), tableLogMax, sCum);
+        fseBuildWarp(tt, smemFse, k * fseSlotBytes(tableLogMax), tableLogMax, sCum, sNext);
     }
     if (lane >= lanes) return;
     uint32_t const ti = blockIdx.x * lanes + lane;
     if (ti >= nbTasks) return;
     FseTask const t = tasks[ti];
     uint32_t const slot = lane * fseSlotBytes(tableLogMax);
-    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemFse + slot + (4u << tableLogMax) + 512u);
+    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemFse + slot + (3u << tableLogMax));
+    const uint16_t* const tab = reinterpret_cast<const uint16_t*>(smemFse + slot);
+    const uint8_t* const symOf = smemFse + slot + (2u << tableLogMax);
     uint32_t const tl = t.tableLog;
 
     BitWin3<kFseRing, kFseAhead> br;
     if (!br.init(t.bits, t.bitsSize, ring)) { reportError(status, DERR_CORRUPTION); return; }
     uint32_t const nst = t.nbStates;
-    uint32_t st0 = slot + 4u * br.read(tl), st1 = slot + 4u * br.read(tl), st2 = 0, st3 = 0;
+    uint32_t st0 = br.read(tl), st1 = br.read(tl), st2 = 0, st3 = 0;
     if (nst == 4) {
-        st2 = slot + 4u * br.read(tl);
-        st3 = slot + 4u * br.read(tl);
+        st2 = br.read(tl);
+        st3 = br.read(tl);
     }
     uint32_t const n = t.dstSize;
     uint32_t const lastTr = n > nst ? n - nst : 0; // symbols [0, lastTr) have a transition
     uint8_t* const out = t.out;
-    auto ent = [&](uint32_t st) -> uint32_t { return *reinterpret_cast<const uint32_t*>(smemFse + st); };
-    auto nbOf = [](uint32_t e) -> uint32_t { return __byte_perm(e, 0u, 0x4441); };
-    auto nextOf = [](uint32_t e, uint32_t f) -> uint32_t { return (e >> 16) + (f << 2); };
+    auto ent = [&](uint32_t st) -> uint32_t { return tab[st]; };
+    auto sym = [&](uint32_t st) -> uint32_t { return symOf[st]; };
+    auto nbOf = [](uint32_t e) -> uint32_t { return e & 15u; };
+    auto nextOf = [](uint32_t e, uint32_t f) -> uint32_t { return (e >> 4) + f; };
     // two transitions whose fields (at most 24 bits) start o bits below the
     // top of the window; returns the bits they read
     auto pair = [&](int32_t o, uint32_t ea, uint32_t eb, uint32_t& sa, uint32_t& sb) -> uint32_t {
@@ -1045,7 +1051,7 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
     // one symbol from st0, then the states rotate
     auto single = [&](uint32_t i) {
         uint32_t const e = ent(st0);
-        out[i] = uint8_t(e);
+        out[i] = uint8_t(sym(st0));
         uint32_t ns = st0;
         if (i < lastTr) ns = nextOf(e, br.read(nbOf(e)));
         if (nst == 4) {
@@ -1061,22 +1067,25 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
         for (; i + 4 <= lastTr; i += 4) {
             br.prepare();
             uint32_t const ea = ent(st0), eb = ent(st1), ec = ent(st2), ed = ent(st3);
+            uint32_t const ya = sym(st0), yb = sym(st1), yc = sym(st2), yd = sym(st3);
             uint32_t const n1 = pair(br.g, ea, eb, st0, st1);
             uint32_t const n2 = pair(br.g + int32_t(n1), ec, ed, st2, st3);
             br.advance(int32_t(n1 + n2));
             *reinterpret_cast<uint32_t*>(out + i) =
-                __byte_perm(__byte_perm(ea, eb, 0x0040), __byte_perm(ec, ed, 0x0040), 0x5410);
+                __byte_perm(__byte_perm(ya, yb, 0x0040), __byte_perm(yc, yd, 0x0040), 0x5410);
         }
     } else {
         for (; i + 4 <= lastTr; i += 4) {
             br.prepare();
             uint32_t const ea = ent(st0), eb = ent(st1);
+            uint32_t const ya = sym(st0), yb = sym(st1);
             uint32_t const n1 = pair(br.g, ea, eb, st0, st1);
             uint32_t const ec = ent(st0), ed = ent(st1);
+            uint32_t const yc = sym(st0), yd = sym(st1);
             uint32_t const n2 = pair(br.g + int32_t(n1), ec, ed, st0, st1);
             br.advance(int32_t(n1 + n2));
             *reinterpret_cast<uint32_t*>(out + i) =
-                __byte_perm(__byte_perm(ea, eb, 0x0040), __byte_perm(ec, ed, 0x0040), 0x5410);
+                __byte_perm(__byte_perm(ya, yb, 0x0040), __byte_perm(yc, yd, 0x0040), 0x5410);
         }
     }
     for (; i < n; i++) single(i);
