@@ -36,7 +36,8 @@ enum : uint32_t {
     TR_DELTA = 1, TR_ZIGZAG = 3, TR_TSPLIT = 4, TR_CONV_STRUCT_TO_SERIAL = 6, TR_CONV_NUM_TO_STRUCT = 8,
     TR_CONV_NUM_TO_SERIAL = 10, TR_BITPACK_SERIAL = 27, TR_BITPACK_INT = 28, TR_FLATPACK = 29, TR_SPLITN = 40,
     TR_CONST_SERIAL = 44, TR_FSE = 49, TR_HUF = 50, TR_NCOUNT = 52, TR_FLOAT_DECONSTRUCT = 33,
-    TR_TOKENIZE_NUMERIC = 37,
+    TR_TOKENIZE_NUMERIC = 37, TR_CONV_STRUCT_TO_NUM = 7, TR_TOKENIZE_FIXED = 36, TR_CONST_FIXED = 45,
+    TR_SPLITN_STRUCT = 47, TR_HUF16 = 51,
 };
 constexpr uint64_t kMinStream = 10;   // ZL_MINSTREAMSIZE_DEFAULT
 constexpr uint64_t kChunk = 1 << 15;  // entropy chunk size
@@ -115,6 +116,30 @@ struct Job {
     uint32_t sizeSlot = 0;
     uint32_t sizes[4] = { 0, 0, 0, 0 };
     const uint8_t* dTable = nullptr;
+    // 16-bit chunks (struct of 2-byte values)
+    bool wide = false;
+    unsigned maxSym16 = 0, card16 = 0;
+    std::vector<uint32_t> count16, first16; // values 0..maxSym16
+    uint8_t const16[2] = { 0, 0 };
+    // huffman_struct_v2
+    int tl16 = 0;
+    std::vector<uint16_t> code16;
+    std::vector<uint8_t> nbBits16;
+    uint32_t streamCap = 0;
+    uint32_t full[4] = { 0, 0, 0, 0 };      // whole bytes of each bitstream
+    const uint8_t* dNbBits = nullptr;
+    // tokenize: alphabet in first-occurrence order, sorted lookup, indices
+    std::vector<uint8_t> alphabet16;        // little-endian 2-byte values
+    std::vector<uint16_t> tokKeys;
+    std::vector<uint8_t> tokIds;
+    int idxJob = -1;                        // Huffman-graph job of the indices
+    uint8_t* idxOut = nullptr;
+    const uint8_t* dKeys = nullptr;
+    const uint8_t* dIds = nullptr;
+    unsigned alphaBits = 0;                 // bit packing of the alphabet
+    uint64_t alphaBytes = 0;
+    const uint8_t* alphaStaged = nullptr;
+    uint8_t* alphaOut = nullptr;
 };
 
 struct RStream {
@@ -158,7 +183,7 @@ struct Front {
 } // namespace
 
 struct EncodeBatch::Impl {
-    DevBuf bufA, bufE, bufF, bufSmall, bufT;
+    DevBuf bufA, bufE, bufF, bufSmall, bufT, bufW;
     std::vector<Job> jobs;           // data chunks (discovery order), then nested weights jobs
     size_t nbDataJobs = 0;
     bool checksums = true;
@@ -234,6 +259,15 @@ struct Engine {
         nd.back().nbOut = 1;
         return o;
     }
+    // ZL_NODE_INTERPRET_TOKEN_AS_LE (encode_conversion_binding.c:179-189)
+    int convStructToNum(int in)
+    {
+        newNode(TR_CONV_STRUCT_TO_NUM, in, 1);
+        int o = newStream(T_NUMERIC, s[in].w, s[in].n);
+        s[o].pieces = s[in].pieces;
+        nd.back().nbOut = 1;
+        return o;
+    }
     int convNumToStruct(int in)
     {
         newNode(TR_CONV_NUM_TO_STRUCT, in, 1);
@@ -257,7 +291,7 @@ struct Engine {
     // ---- graphs ----------------------------------------------------------
     enum G {
         G_STORE, G_SERIAL_STORE, G_FSE, G_HUF, G_ENTROPY, G_CONSTANT, G_BITPACK, G_FLATPACK, G_NCOUNT, G_TSPLIT_FSE,
-        G_TSPLIT_STORE, G_BITPACK_HUF, G_JOB, G_TOKENIZE, G_BF16
+        G_TSPLIT_STORE, G_BITPACK_HUF, G_JOB, G_TOKENIZE, G_BF16, G_BITPACK16, G_ALPHAPACK
     };
     struct Succ {
         int g, sid, job;
@@ -294,6 +328,7 @@ struct Engine {
             job.n = s[sid].n;
             job.mode = mode;
             job.dsrc = s[sid].pieces.empty() ? nullptr : s[sid].pieces[0].dev;
+            job.wide = s[sid].w == 2;
             jobs->push_back(std::move(job));
             return nullptr;
         }
@@ -309,6 +344,10 @@ struct Engine {
         }
         Job* j = jobFor(sid, mode, explicitJob);
         if (!j) return; // discovery
+        if (j->wide) {
+            wideChunk(sid, *j, succ);
+            return;
+        }
         switch (j->codec) {
             case ent::CC_STORE: succ.push_back({ G_STORE, sid, -1 }); return;
             case ent::CC_CONSTANT: succ.push_back({ G_JOB, sid, int(j - jobs->data()) | (G_CONSTANT << 24) }); return;
@@ -355,25 +394,84 @@ struct Engine {
         }
     }
 
+    // the 2-byte branch of entropyCompressChunk (encode_entropy_binding.c:
+    // 612-681), from the decision taken on the chunk's statistics
+    void wideChunk(int sid, Job& j, std::vector<Succ>& succ)
+    {
+        int const ji = int(&j - jobs->data());
+        switch (j.codec) {
+            case ent::CC_STORE: succ.push_back({ G_STORE, sid, -1 }); return;
+            case ent::CC_CONSTANT: succ.push_back({ G_JOB, sid, ji | (G_CONSTANT << 24) }); return;
+            case ent::CC_BITPACK: {
+                int const o = convStructToNum(sid);
+                succ.push_back({ G_JOB, o, ji | (G_BITPACK16 << 24) });
+                return;
+            }
+            case ent::CC_TOK16: { // tokenize_struct (first-occurrence order)
+                newNode(TR_TOKENIZE_FIXED, sid, 2);
+                size_t const na = j.alphabet16.size() / 2;
+                int const a = newStream(T_STRUCT, 2, na);
+                s[a].pieces.push_back(Piece{ nullptr, j.alphabet16.data(), j.alphabet16.size() });
+                int const o = newStream(T_NUMERIC, 1, j.n);
+                s[o].pieces.push_back(Piece{ j.idxOut, nullptr, j.n });
+                nd.back().nbOut = 2;
+                if (ent::nextPow2Bits(uint64_t(j.maxSym16) + 1) < 16) {
+                    int const c = convStructToNum(a);
+                    succ.push_back({ G_JOB, c, ji | (G_ALPHAPACK << 24) });
+                } else {
+                    succ.push_back({ G_STORE, a, -1 });
+                }
+                succ.push_back({ G_HUF, o, j.idxJob });
+                return;
+            }
+            case ent::CC_HUF16: { // EI_huffman_struct_v2 (encode_entropy_binding.c:287-367)
+                RNode& x = newNode(TR_HUF16, sid, 2);
+                x.hdr[0] = uint8_t(j.x4 ? 1 : 0);
+                size_t const nbBytes = size_t(ent::nextPow2Bits(j.n + 1) + 7) / 8;
+                for (size_t b = 0; b < nbBytes; b++) x.hdr[1 + b] = uint8_t(j.n >> (8 * b));
+                x.hsz = nbBytes + 1;
+                int const ws = newStream(T_NUMERIC, 1, j.weights.size());
+                s[ws].pieces.push_back(Piece{ nullptr, j.weights.data(), j.weights.size() });
+                uint64_t total = 0;
+                int const ns = j.x4 ? 4 : 1;
+                for (int k = 0; k < ns; k++) total += 8 + j.sizes[k];
+                int const bs = newStream(T_SERIAL, 1, total);
+                for (int k = 0; k < ns; k++)
+                    s[bs].pieces.push_back(Piece{ j.out + uint64_t(k) * j.streamCap, nullptr, 8ull + j.sizes[k] });
+                nd.back().nbOut = 2;
+                succ.push_back({ G_FSE, ws, j.weightsJob });
+                succ.push_back({ G_STORE, bs, -1 });
+                return;
+            }
+            default: err = 32; return;
+        }
+    }
+
     void entropyGraph(int sid, int mode, int explicitJob)
     {
         std::vector<Succ> succ;
+        // doEntropyConversion (encode_entropy_binding.c:764-810): width 1 to
+        // serial, numeric width 2 to struct
         if (s[sid].w == 1 && s[sid].type != T_SERIAL)
             sid = s[sid].type == T_NUMERIC ? convNumToSerial(sid) : convStructToSerial(sid);
-        if (s[sid].w != 1) { err = 81; return; }
+        else if (s[sid].w == 2 && s[sid].type == T_NUMERIC)
+            sid = convNumToStruct(sid);
+        if (s[sid].w != 1 && s[sid].w != 2) { err = 81; return; }
         uint64_t const n = s[sid].n;
         if (n < kMinChunking) {
             entropyChunk(sid, mode, succ, explicitJob);
         } else {
             uint64_t const nb = (n + kChunk - 1) / kChunk;
-            newNode(TR_SPLITN, sid, 0);
+            uint32_t const w = s[sid].w;
+            int const type = s[sid].type;
+            newNode(type == T_STRUCT ? TR_SPLITN_STRUCT : TR_SPLITN, sid, 0);
             int const first = int(s.size());
             uint64_t pos = 0;
             std::vector<Piece> src = s[sid].pieces;
             for (uint64_t k = 0; k < nb; k++) {
                 uint64_t const len = k + 1 < nb ? kChunk : n - pos;
-                int o = newStream(T_SERIAL, 1, len);
-                s[o].pieces = slice(src, pos, len);
+                int o = newStream(type, w, len);
+                s[o].pieces = slice(src, pos * w, len * w);
                 pos += len;
             }
             nd.back().nbOut = int(nb);
@@ -400,14 +498,15 @@ struct Engine {
             case G_ENTROPY: entropyGraph(sid, M_ANY, job); return;
             case G_CONSTANT: {
                 Job& j = (*jobs)[size_t(job)];
-                RNode& x = newNode(TR_CONST_SERIAL, sid, 1);
+                bool const fixed = s[sid].type != T_SERIAL; // 2-byte struct chunks
+                RNode& x = newNode(fixed ? TR_CONST_FIXED : TR_CONST_SERIAL, sid, 1);
                 uint64_t v = s[sid].n;
                 size_t k = 0;
                 while (v >= 0x80) { x.hdr[k++] = uint8_t(v | 0x80); v >>= 7; }
                 x.hdr[k++] = uint8_t(v);
                 x.hsz = k;
-                int o = newStream(T_SERIAL, 1, 1);
-                s[o].pieces.push_back(Piece{ nullptr, &j.constVal, 1 });
+                int o = newStream(s[sid].type, s[sid].w, 1);
+                s[o].pieces.push_back(Piece{ nullptr, fixed ? j.const16 : &j.constVal, s[sid].w });
                 nd.back().nbOut = 1;
                 runSuccessor(G_SERIAL_STORE, o);
                 return;
@@ -421,6 +520,24 @@ struct Engine {
                 if (maxN > j.n) { x.hdr[1] = uint8_t(maxN - j.n); x.hsz = 2; }
                 int o = newStream(T_SERIAL, 1, j.packBytes);
                 s[o].pieces.push_back(Piece{ j.out, nullptr, j.packBytes });
+                nd.back().nbOut = 1;
+                runSuccessor(G_SERIAL_STORE, o);
+                return;
+            }
+            case G_BITPACK16:
+            case G_ALPHAPACK: { // ZL_GRAPH_BITPACK on 2-byte numbers (TR_BITPACK_INT)
+                Job& j = (*jobs)[size_t(job)];
+                bool const alpha = g == G_ALPHAPACK;
+                unsigned const bits = alpha ? j.alphaBits : j.packBits;
+                uint64_t const bytes = alpha ? j.alphaBytes : j.packBytes;
+                uint64_t const n = s[sid].n;
+                RNode& x = newNode(TR_BITPACK_INT, sid, 1);
+                uint64_t const maxN = bytes * 8 / bits;
+                x.hdr[0] = uint8_t((1u << 6) | (bits - 1));
+                x.hsz = 1;
+                if (maxN > n) { x.hdr[1] = uint8_t(maxN - n); x.hsz = 2; }
+                int o = newStream(T_SERIAL, 1, bytes);
+                s[o].pieces.push_back(Piece{ alpha ? j.alphaOut : j.out, nullptr, bytes });
                 nd.back().nbOut = 1;
                 runSuccessor(G_SERIAL_STORE, o);
                 return;
@@ -624,6 +741,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                 || r == RC_D_BITPACK_HUF || r == RC_DELTA_STORE;
         bool const hasZz = r == RC_DZ_TSPLIT_FSE || r == RC_DZ_BITPACK_HUF || r == RC_ZIGZAG_STORE;
         if (F.serial || inBytes < kMinStream) continue; // no numeric front end
+        if (r == RC_FSE || r == RC_HUFFMAN || r == RC_ENTROPY) continue; // the graphs read the input itself
         if (r == RC_BF16) {
             if (F.w != 2) { err = "bf16 deconstruct takes 2-byte elements"; return 54; }
             fr.special = 1;
@@ -963,19 +1081,65 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
     // ---- phase C: histograms ------------------------------------------------------
     size_t const nj = I.nbDataJobs;
     std::vector<uint32_t> hists(nj * 256);
-    if (nj) {
-        std::vector<HistTask> ht(nj);
-        for (size_t j = 0; j < nj; j++) ht[j] = HistTask{ I.jobs[j].dsrc, uint32_t(I.jobs[j].n), uint32_t(j) };
-        size_t const bytes = nj * sizeof(HistTask) + nj * 1024 + 256;
+    std::vector<HistTask> ht;
+    for (size_t j = 0; j < nj; j++)
+        if (!I.jobs[j].wide) ht.push_back(HistTask{ I.jobs[j].dsrc, uint32_t(I.jobs[j].n), uint32_t(j) });
+    if (!ht.empty()) {
+        size_t const bytes = ht.size() * sizeof(HistTask) + nj * 1024 + 256;
         if (!I.bufF.reserve(bytes)) { err = "device allocation failed"; return 70; }
         Bump b{ I.bufF.data(), 0 };
-        auto* dHt = reinterpret_cast<HistTask*>(b.take(nj * sizeof(HistTask)));
+        auto* dHt = reinterpret_cast<HistTask*>(b.take(ht.size() * sizeof(HistTask)));
         auto* dH = reinterpret_cast<uint32_t*>(b.take(nj * 1024));
-        cudaMemcpyAsync(dHt, ht.data(), nj * sizeof(HistTask), cudaMemcpyHostToDevice, st);
-        launchHist(dHt, uint32_t(nj), dH, st);
+        cudaMemcpyAsync(dHt, ht.data(), ht.size() * sizeof(HistTask), cudaMemcpyHostToDevice, st);
+        launchHist(dHt, uint32_t(ht.size()), dH, st);
         launches_++;
         cudaMemcpyAsync(hists.data(), dH, nj * 1024, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in histograms"; return 1; }
+    }
+    // 16-bit chunks: value counts, first occurrences and maxima on the
+    // device; the counts of values up to each chunk's maximum come back
+    {
+        std::vector<size_t> wide;
+        for (size_t j = 0; j < nj; j++)
+            if (I.jobs[j].wide) wide.push_back(j);
+        if (!wide.empty()) {
+            size_t const nw = wide.size();
+            std::vector<Hist16Task> tasks(nw);
+            std::vector<TileRef> tiles;
+            for (size_t k = 0; k < nw; k++)
+                for (uint32_t t = 0; t < (I.jobs[wide[k]].n + kEncTile - 1) / kEncTile; t++) tiles.push_back(TileRef{ uint32_t(k), t });
+            size_t const bytes = nw * (2ull * 65536 * 4 + 256) + nw * sizeof(Hist16Task) + tiles.size() * sizeof(TileRef) + 1024;
+            if (!I.bufW.reserve(bytes)) { err = "device allocation failed"; return 70; }
+            Bump b{ I.bufW.data(), 0 };
+            auto* dCount = reinterpret_cast<uint32_t*>(b.take(nw * 65536ull * 4));
+            auto* dFirst = reinterpret_cast<uint32_t*>(b.take(nw * 65536ull * 4));
+            auto* dMax = reinterpret_cast<uint32_t*>(b.take(nw * 4 + 4));
+            auto* dTasks = reinterpret_cast<Hist16Task*>(b.take(nw * sizeof(Hist16Task)));
+            auto* dTiles = reinterpret_cast<TileRef*>(b.take(tiles.size() * sizeof(TileRef) + 4));
+            for (size_t k = 0; k < nw; k++) {
+                const Job& J = I.jobs[wide[k]];
+                tasks[k] = Hist16Task{ J.dsrc, uint32_t(J.n), dCount + k * 65536, dFirst + k * 65536, dMax + k };
+            }
+            cudaMemsetAsync(dCount, 0, nw * 65536ull * 4, st);
+            cudaMemsetAsync(dFirst, 0xff, nw * 65536ull * 4, st);
+            cudaMemsetAsync(dMax, 0, nw * 4, st);
+            cudaMemcpyAsync(dTasks, tasks.data(), nw * sizeof(Hist16Task), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dTiles, tiles.data(), tiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+            launchHist16(dTasks, dTiles, uint32_t(tiles.size()), st);
+            launches_++;
+            std::vector<uint32_t> mx(nw);
+            cudaMemcpyAsync(mx.data(), dMax, nw * 4, cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in 16-bit histograms"; return 1; }
+            for (size_t k = 0; k < nw; k++) {
+                Job& J = I.jobs[wide[k]];
+                J.maxSym16 = mx[k];
+                J.count16.resize(size_t(mx[k]) + 1);
+                J.first16.resize(size_t(mx[k]) + 1);
+                cudaMemcpyAsync(J.count16.data(), dCount + k * 65536, J.count16.size() * 4, cudaMemcpyDeviceToHost, st);
+                cudaMemcpyAsync(J.first16.data(), dFirst + k * 65536, J.first16.size() * 4, cudaMemcpyDeviceToHost, st);
+            }
+            if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in 16-bit histograms"; return 1; }
+        }
     }
 
     // ---- phase D: decisions and tables ------------------------------------------
@@ -1028,15 +1192,84 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             default: break;
         }
     };
+    // 16-bit chunks (encode_entropy_binding.c:612-681); tokenize adds the
+    // Huffman-graph job of the indices, whose histogram follows from the
+    // value counts
+    auto decide16 = [&](size_t ji) -> bool {
+        Job& J = I.jobs[ji];
+        unsigned const m = J.maxSym16;
+        J.card16 = 0;
+        for (uint32_t c : J.count16) J.card16 += c != 0;
+        J.codec = ent::chooseCodec16(J.count16.data(), m, J.n, J.card16);
+        switch (J.codec) {
+            case ent::CC_CONSTANT:
+                J.const16[0] = uint8_t(m);
+                J.const16[1] = uint8_t(m >> 8);
+                return true;
+            case ent::CC_BITPACK:
+                J.packBits = 1 + (m ? unsigned(31 - __builtin_clz(m)) : 0);
+                J.packBytes = (J.n * J.packBits + 7) / 8;
+                return true;
+            case ent::CC_TOK16: {
+                std::vector<uint32_t> vals;
+                for (unsigned v = 0; v <= m; v++)
+                    if (J.count16[v]) vals.push_back(v);
+                std::vector<uint32_t> order = vals;
+                std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return J.first16[a] < J.first16[b]; });
+                std::vector<uint8_t> rank(size_t(m) + 1, 0);
+                J.alphabet16.clear();
+                for (size_t k = 0; k < order.size(); k++) {
+                    rank[order[k]] = uint8_t(k);
+                    J.alphabet16.push_back(uint8_t(order[k]));
+                    J.alphabet16.push_back(uint8_t(order[k] >> 8));
+                }
+                J.tokKeys.clear();
+                J.tokIds.clear();
+                for (uint32_t v : vals) {
+                    J.tokKeys.push_back(uint16_t(v));
+                    J.tokIds.push_back(rank[v]);
+                }
+                J.alphaBits = 1 + (m ? unsigned(31 - __builtin_clz(m)) : 0);
+                J.alphaBytes = (order.size() * J.alphaBits + 7) / 8;
+                Job W;
+                W.n = J.n;
+                W.mode = M_HUF;
+                std::memset(W.hist.count, 0, sizeof(W.hist.count));
+                for (size_t k = 0; k < order.size(); k++) W.hist.count[k] = J.count16[order[k]];
+                decide(W);
+                I.jobs.push_back(std::move(W));
+                I.jobs[ji].idxJob = int(I.jobs.size() - 1);
+                return true;
+            }
+            case ent::CC_HUF16: {
+                J.code16.assign(size_t(m) + 1, 0);
+                J.nbBits16.assign(size_t(m) + 1, 0);
+                J.tl16 = ent::huf16Build(J.code16.data(), J.nbBits16.data(), J.count16.data(), m);
+                if (J.tl16 < 0) return false;
+                J.weights.resize(size_t(m) + 1);
+                for (unsigned v = 0; v <= m; v++)
+                    J.weights[v] = uint8_t(J.nbBits16[v] ? J.tl16 + 1 - J.nbBits16[v] : 0);
+                J.x4 = J.n > 1000;
+                uint64_t const maxLen = J.x4 ? J.n / 4 + 1 : J.n;
+                J.streamCap = uint32_t(((8 + (maxLen * 20 + 8) / 8 + 16) + 15) & ~uint64_t(15));
+                return true;
+            }
+            default: return true;
+        }
+    };
     for (size_t j = 0; j < nj; j++) {
+        if (I.jobs[j].wide) {
+            if (!decide16(j)) { err = "16-bit Huffman table construction failed"; return 1; }
+            continue;
+        }
         std::memcpy(I.jobs[j].hist.count, &hists[j * 256], 1024);
         decide(I.jobs[j]);
     }
     // nested weights jobs (FSE graph of Huffman weights): decided on the host
     // histogram of the weights, encoded on the device with the data jobs
-    for (size_t j = 0; j < nj; j++) {
+    for (size_t j = 0; j < I.jobs.size(); j++) {
         Job& J = I.jobs[j];
-        if (J.codec != ent::CC_HUF) continue;
+        if (J.codec != ent::CC_HUF && J.codec != ent::CC_HUF16) continue;
         // weights stream: numeric u8; under 10 bytes it is stored, else the
         // FSE graph gets it after a numeric->serial conversion
         if (J.weights.size() < kMinStream) continue;
@@ -1057,11 +1290,68 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         std::vector<HufEncTask> hufT;
         std::vector<PackTask> packT;
         std::vector<TileRef> packTiles;
+        std::vector<Tok16Task> tok16T;
+        std::vector<TileRef> tok16Tiles;
+        std::vector<EncNumTask> wideNumT; // bit packing of 2-byte numbers
+        std::vector<TileRef> wideNumTiles;
+        std::vector<Huf16EncTask> huf16T;
         uint32_t nbSizes = 0;
+        auto addWideNum = [&](const uint8_t* src, uint8_t* out, uint64_t n, unsigned bits) {
+            EncNumTask t{};
+            t.src = src;
+            t.out = out;
+            t.n = n;
+            t.w = 2;
+            t.mode = EOUT_BITPACK;
+            t.nbBits = uint8_t(bits);
+            for (uint32_t k = 0; k < (n + kEncTile - 1) / kEncTile; k++) wideNumTiles.push_back(TileRef{ uint32_t(wideNumT.size()), k });
+            wideNumT.push_back(t);
+        };
         auto layoutE = [&](Bump& b, bool real) {
             nbSizes = 0;
             for (size_t j = 0; j < I.jobs.size(); j++) {
                 Job& J = I.jobs[j];
+                if (J.wide) {
+                    switch (J.codec) {
+                        case ent::CC_BITPACK:
+                            J.out = b.take(J.packBytes + 64, 16);
+                            if (real) addWideNum(J.dsrc, J.out, J.n, J.packBits);
+                            break;
+                        case ent::CC_TOK16: {
+                            size_t const na = J.tokKeys.size();
+                            J.idxOut = b.take(J.n + 64, 16);
+                            J.dKeys = b.take(2 * 256, 16);
+                            J.dIds = b.take(256, 16);
+                            I.jobs[size_t(J.idxJob)].dsrc = J.idxOut;
+                            if (real) {
+                                Tok16Task t{ J.dsrc, J.idxOut, reinterpret_cast<const uint16_t*>(J.dKeys), J.dIds, uint32_t(J.n),
+                                             uint32_t(na) };
+                                for (uint32_t k = 0; k < (J.n + kEncTile - 1) / kEncTile; k++)
+                                    tok16Tiles.push_back(TileRef{ uint32_t(tok16T.size()), k });
+                                tok16T.push_back(t);
+                            }
+                            if (ent::nextPow2Bits(uint64_t(J.maxSym16) + 1) < 16) {
+                                J.alphaStaged = b.take(2 * na + 16, 16);
+                                J.alphaOut = b.take(J.alphaBytes + 64, 16);
+                                if (real) addWideNum(J.alphaStaged, J.alphaOut, na, J.alphaBits);
+                            }
+                            break;
+                        }
+                        case ent::CC_HUF16: {
+                            J.out = b.take(uint64_t(J.x4 ? 4 : 1) * J.streamCap, 16);
+                            J.dTable = b.take(2 * J.code16.size() + 16, 16);
+                            J.dNbBits = b.take(J.nbBits16.size() + 16, 16);
+                            J.sizeSlot = nbSizes;
+                            nbSizes += 8;
+                            if (real)
+                                huf16T.push_back(Huf16EncTask{ J.dsrc, J.out, reinterpret_cast<const uint16_t*>(J.dTable), J.dNbBits,
+                                                               uint32_t(J.n), J.streamCap, J.sizeSlot, J.x4 ? 1u : 0u });
+                            break;
+                        }
+                        default: break;
+                    }
+                    continue;
+                }
                 if (!J.hsrc.empty()) {
                     uint8_t* p = b.take(J.hsrc.size() + 16, 16);
                     J.dstaged = p;
@@ -1103,10 +1393,13 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         };
         Bump sz;
         layoutE(sz, false);
-        size_t const taskBytes = 4096 + I.jobs.size() * (sizeof(FseEncTask) + sizeof(HufEncTask) + sizeof(PackTask));
+        size_t const taskBytes = 4096 + I.jobs.size() * (sizeof(FseEncTask) + sizeof(HufEncTask) + sizeof(PackTask)
+                                                         + sizeof(Tok16Task) + 2 * sizeof(EncNumTask) + sizeof(Huf16EncTask));
         size_t tilesGuess = 0;
-        for (auto& J : I.jobs)
+        for (auto& J : I.jobs) {
             if (J.codec == ent::CC_BITPACK || J.codec == ent::CC_FLATPACK) tilesGuess += (J.n + kEncTile - 1) / kEncTile;
+            if (J.codec == ent::CC_TOK16) tilesGuess += 2 * ((J.n + kEncTile - 1) / kEncTile) + 1;
+        }
         size_t const total = sz.used + taskBytes + tilesGuess * sizeof(TileRef) + (nbSizes + 16) * 4 + 1024;
         if (!I.bufE.reserve(total)) { err = "device allocation failed"; return 70; }
         Bump b{ I.bufE.data(), 0 };
@@ -1116,8 +1409,26 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         auto* dPack = reinterpret_cast<PackTask*>(b.take(packT.size() * sizeof(PackTask) + 1));
         auto* dPackTiles = reinterpret_cast<TileRef*>(b.take(packTiles.size() * sizeof(TileRef) + 1));
         auto* dSizes = reinterpret_cast<uint32_t*>(b.take((nbSizes + 1) * 4));
+        auto* dTok16 = reinterpret_cast<Tok16Task*>(b.take(tok16T.size() * sizeof(Tok16Task) + 1));
+        auto* dTok16Tiles = reinterpret_cast<TileRef*>(b.take(tok16Tiles.size() * sizeof(TileRef) + 1));
+        auto* dWideNum = reinterpret_cast<EncNumTask*>(b.take(wideNumT.size() * sizeof(EncNumTask) + 1));
+        auto* dWideNumTiles = reinterpret_cast<TileRef*>(b.take(wideNumTiles.size() * sizeof(TileRef) + 1));
+        auto* dHuf16 = reinterpret_cast<Huf16EncTask*>(b.take(huf16T.size() * sizeof(Huf16EncTask) + 1));
         // uploads: staged weights, tables, maps, tasks
         for (Job& J : I.jobs) {
+            if (J.wide) {
+                if (J.codec == ent::CC_TOK16) {
+                    cudaMemcpyAsync(const_cast<uint8_t*>(J.dKeys), J.tokKeys.data(), 2 * J.tokKeys.size(), cudaMemcpyHostToDevice, st);
+                    cudaMemcpyAsync(const_cast<uint8_t*>(J.dIds), J.tokIds.data(), J.tokIds.size(), cudaMemcpyHostToDevice, st);
+                    if (J.alphaStaged)
+                        cudaMemcpyAsync(const_cast<uint8_t*>(J.alphaStaged), J.alphabet16.data(), J.alphabet16.size(), cudaMemcpyHostToDevice, st);
+                }
+                if (J.codec == ent::CC_HUF16) {
+                    cudaMemcpyAsync(const_cast<uint8_t*>(J.dTable), J.code16.data(), 2 * J.code16.size(), cudaMemcpyHostToDevice, st);
+                    cudaMemcpyAsync(const_cast<uint8_t*>(J.dNbBits), J.nbBits16.data(), J.nbBits16.size(), cudaMemcpyHostToDevice, st);
+                }
+                continue;
+            }
             if (!J.hsrc.empty()) cudaMemcpyAsync(const_cast<uint8_t*>(J.dstaged), J.hsrc.data(), J.hsrc.size(), cudaMemcpyHostToDevice, st);
             if (J.codec == ent::CC_FSE) cudaMemcpyAsync(const_cast<uint8_t*>(J.dTable), J.fct.get(), sizeof(ent::FseCTable), cudaMemcpyHostToDevice, st);
             if (J.codec == ent::CC_HUF) cudaMemcpyAsync(const_cast<uint8_t*>(J.dTable), J.hct.get(), sizeof(ent::HufCTable), cudaMemcpyHostToDevice, st);
@@ -1130,6 +1441,25 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             cudaMemcpyAsync(dPackTiles, packTiles.data(), packTiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
         }
         if (nbSizes) cudaMemsetAsync(dSizes, 0, nbSizes * 4, st);
+        // 16-bit chunks first: the tokenize indices feed their Huffman-graph
+        // jobs below
+        if (!tok16T.empty()) {
+            cudaMemcpyAsync(dTok16, tok16T.data(), tok16T.size() * sizeof(Tok16Task), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dTok16Tiles, tok16Tiles.data(), tok16Tiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+            launchTok16(dTok16, dTok16Tiles, uint32_t(tok16Tiles.size()), st);
+            launches_++;
+        }
+        if (!wideNumT.empty()) {
+            cudaMemcpyAsync(dWideNum, wideNumT.data(), wideNumT.size() * sizeof(EncNumTask), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dWideNumTiles, wideNumTiles.data(), wideNumTiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+            launchEncNum(dWideNum, dWideNumTiles, uint32_t(wideNumTiles.size()), st);
+            launches_++;
+        }
+        if (!huf16T.empty()) {
+            cudaMemcpyAsync(dHuf16, huf16T.data(), huf16T.size() * sizeof(Huf16EncTask), cudaMemcpyHostToDevice, st);
+            launchHuf16Enc(dHuf16, uint32_t(huf16T.size()), dSizes, st);
+            launches_++;
+        }
         launchFseEnc(dFse, uint32_t(fseT.size()), dSizes, st);
         launchHufEnc(dHuf, uint32_t(hufT.size()), dSizes, st);
         launchPack(dPack, dPackTiles, uint32_t(packTiles.size()), st);
@@ -1138,6 +1468,23 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         if (nbSizes) cudaMemcpyAsync(hs.data(), dSizes, nbSizes * 4, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in entropy encoding"; return 1; }
         for (Job& J : I.jobs) {
+            if (J.wide && J.codec == ent::CC_HUF16) {
+                // the reference writes the streams into 2n + 32 bytes; each
+                // stream takes 8 header bytes and fails once its whole bytes
+                // reach its remaining room less 16 (encode_huffman_kernel.c:
+                // 437-488, encode_entropy_binding.c:351)
+                uint64_t avail = 2 * J.n + 32;
+                for (int k = 0; k < (J.x4 ? 4 : 1); k++) {
+                    J.sizes[k] = hs[J.sizeSlot + k];
+                    J.full[k] = hs[J.sizeSlot + 4 + k];
+                    if (avail < 8 || avail - 8 <= 8 || J.full[k] >= avail - 16 || 8ull + J.sizes[k] > J.streamCap) {
+                        err = "16-bit Huffman stream over capacity";
+                        return 1;
+                    }
+                    avail -= 8 + J.sizes[k];
+                }
+                continue;
+            }
             if (J.codec == ent::CC_FSE) {
                 J.sizes[0] = hs[J.sizeSlot];
                 if (J.sizes[0] > J.n + J.n / 128 + 512) { err = "FSE bitstream over capacity"; return 1; }

@@ -20,6 +20,12 @@ void launchBf16(const Bf16Task* t, const TileRef* tiles, uint32_t nbTiles, cudaS
 // Tokenize, up to the per-task distinct counts (counts[task], errors[0]).
 void launchTokCount(const TokTask* t, uint32_t nbTasks, const TileRef* tiles, uint32_t nbTiles, uint64_t* tileSums,
                     uint64_t* tilePrefix, uint32_t* counts, uint32_t* errors, cudaStream_t s);
+// 16-bit chunks: value counts, first occurrences and maxima.
+void launchHist16(const Hist16Task* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
+// 16-bit chunks: tokenize indices.
+void launchTok16(const Tok16Task* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
+// 16-bit-symbol Huffman streams, one thread per stream.
+void launchHuf16Enc(const Huf16EncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);
 // Tokenize, the alphabet and the indices (iw set in the tasks).
 void launchTokEmit(const TokTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
 

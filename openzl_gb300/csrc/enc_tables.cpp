@@ -3,6 +3,8 @@
 
 #include <cmath>
 #include <cstring>
+#include <vector>
+#include <algorithm>
 
 namespace ozl {
 namespace ent {
@@ -23,13 +25,14 @@ struct Log2Table {
 };
 const Log2Table kLog2;
 
-// ZL_calculateEntropy (src/openzl/shared/data_stats.c:46-79).
-double entropyBits(const uint32_t* count, uint64_t total)
+// ZL_calculateEntropy (src/openzl/shared/data_stats.c:46-79) over values
+// 0..maxValue.
+double entropyBits(const uint32_t* count, uint64_t total, unsigned maxValue = 255)
 {
     if (total == 0) return 0;
     int64_t acc = 0;
     int64_t const normalize = (int64_t(1) << 62) / int64_t(total);
-    for (int i = 0; i < 256; i++) {
+    for (unsigned i = 0; i <= maxValue; i++) {
         int64_t const c = count[i];
         int64_t idx = c * normalize;
         int const clz = __builtin_clzll(uint64_t(idx) | (1u << 9));
@@ -495,6 +498,146 @@ unsigned hufBuild(HufCTable& ct, const uint32_t* count, unsigned maxSym, unsigne
     for (unsigned n = 0; n <= maxSym; n++) ct.value[n] = valRank[ct.nbBits[n]]++;
     ct.tableLog = maxBits;
     return maxBits;
+}
+
+// ---------------------------------------------------------------------------
+// 16-bit chunks
+
+ChunkCodec chooseCodec16(const uint32_t* count, unsigned maxSym, uint64_t n, unsigned card)
+{
+    if (count[maxSym] == n) return CC_CONSTANT;
+    double entropy = entropyBits(count, n, maxSym);
+    if (1 > entropy) entropy = 1;
+    volatile double prod = entropy * double(n);
+    volatile double sum = prod + 7;
+    uint64_t const entropySize = uint64_t(sum) / 8;
+    uint64_t const header = maxSym / 4 > 100 ? maxSym / 4 : 100;
+    uint64_t const huffSize = entropySize + header, storeSize = 2 * n;
+    uint64_t const nbBits = uint64_t(nextPow2Bits(uint64_t(maxSym) + 1));
+    uint64_t const bitpackSize = (n * nbBits + 7) / 8 + 2;
+    if (bitpackSize <= huffSize && bitpackSize < storeSize) return CC_BITPACK;
+    if (entropy > 15 || huffSize >= storeSize) return CC_STORE;
+    if (card < 256) return CC_TOK16;
+    return CC_HUF16;
+}
+
+namespace {
+
+struct LNode {
+    uint32_t count, parent;
+    uint16_t symbol, nbBits;
+};
+
+// ZS_largeHuffmanSetMaxHeight (encode_huffman_kernel.c:34-151)
+int huf16MaxHeight(LNode* node, int last, int maxNbBits)
+{
+    int const largest = node[last].nbBits;
+    if (largest <= maxNbBits) return largest;
+    int totalCost = 0;
+    int const baseCost = 1 << (largest - maxNbBits);
+    int n;
+    for (n = last; node[n].nbBits > maxNbBits; --n) {
+        totalCost += baseCost - (1 << (largest - node[n].nbBits));
+        node[n].nbBits = uint16_t(maxNbBits);
+    }
+    while (node[n].nbBits == maxNbBits) --n;
+    totalCost >>= (largest - maxNbBits);
+    uint32_t const noSym = 0xF0F0F0F0u;
+    uint32_t rankLast[22];
+    for (uint32_t& r : rankLast) r = noSym;
+    {
+        int cur = maxNbBits;
+        for (int pos = n; pos >= 0; pos--) {
+            if (node[pos].nbBits >= cur) continue;
+            cur = node[pos].nbBits;
+            rankLast[maxNbBits - cur] = uint32_t(pos);
+        }
+    }
+    while (totalCost > 0) {
+        int nb = highbit32(uint32_t(totalCost)) + 1;
+        while (nb > 1 && rankLast[nb] == noSym) --nb;
+        for (; nb > 1; nb--) {
+            uint32_t const hi = rankLast[nb], lo = rankLast[nb - 1];
+            if (hi == noSym || lo == noSym) break;
+            if (node[hi].count <= 2 * node[lo].count) break;
+        }
+        while (nb <= 20 && rankLast[nb] == noSym) nb++;
+        if (nb > 21 || rankLast[nb] == noSym) return -1;
+        totalCost -= 1 << (nb - 1);
+        if (rankLast[nb - 1] == noSym) rankLast[nb - 1] = rankLast[nb];
+        node[rankLast[nb]].nbBits++;
+        if (rankLast[nb] == 0) {
+            rankLast[nb] = noSym;
+        } else {
+            rankLast[nb]--;
+            if (node[rankLast[nb]].nbBits != maxNbBits - nb) rankLast[nb] = noSym;
+        }
+    }
+    while (totalCost < 0) {
+        if (rankLast[1] == noSym) {
+            while (node[n].nbBits == maxNbBits) n--;
+            node[n + 1].nbBits--;
+            rankLast[1] = uint32_t(n + 1);
+            totalCost++;
+            continue;
+        }
+        node[rankLast[1] + 1].nbBits--;
+        rankLast[1]++;
+        totalCost++;
+    }
+    return maxNbBits;
+}
+
+} // namespace
+
+int huf16Build(uint16_t* code, uint8_t* nbBits, const uint32_t* count, unsigned maxSym)
+{
+    int maxNbBits = 20;
+    int const bound = nextPow2Bits(uint64_t(maxSym) + 1);
+    if (bound + 3 < maxNbBits) maxNbBits = bound + 3;
+    std::vector<LNode> all(2 * size_t(maxSym) + 3, LNode{ 0, 0, 0, 0 });
+    LNode* const node = all.data() + 1;
+    for (unsigned s = 0; s <= maxSym; s++) node[s] = LNode{ count[s], 0, uint16_t(s), 0 };
+    // ZS_largeHuffmanSort (encode_huffman_kernel.c:153-229): decreasing
+    // counts; the reference's partition by highest set bit is stable, so
+    // equal counts keep symbol order
+    std::stable_sort(node, node + maxSym + 1, [](const LNode& a, const LNode& b) { return a.count > b.count; });
+    // ZS_largeHuffmanBuildTree (encode_huffman_kernel.c:231-290); node[-1]
+    // is the sentinel
+    int nonNull = int(maxSym);
+    while (node[nonNull].count == 0) nonNull--;
+    int const startNode = int(maxSym) + 1;
+    int nodeNb = startNode, lowS = nonNull, lowN = nodeNb;
+    int const nodeRoot = nodeNb + lowS - 1;
+    node[nodeNb].count = node[lowS].count + node[lowS - 1].count;
+    node[lowS].parent = node[lowS - 1].parent = uint32_t(nodeNb);
+    nodeNb++;
+    lowS -= 2;
+    for (int k = nodeNb; k <= nodeRoot; k++) node[k].count = 1u << 30;
+    node[-1].count = 1u << 31;
+    for (; nodeNb <= nodeRoot; nodeNb++) {
+        int const n1 = node[lowS].count < node[lowN].count ? lowS-- : lowN++;
+        int const n2 = node[lowS].count < node[lowN].count ? lowS-- : lowN++;
+        node[nodeNb].count = node[n1].count + node[n2].count;
+        node[n1].parent = node[n2].parent = uint32_t(nodeNb);
+    }
+    node[nodeRoot].nbBits = 0;
+    for (int k = nodeRoot - 1; k >= startNode; k--) node[k].nbBits = uint16_t(node[node[k].parent].nbBits + 1);
+    for (int k = 0; k <= nonNull; k++) node[k].nbBits = uint16_t(node[node[k].parent].nbBits + 1);
+    maxNbBits = huf16MaxHeight(node, nonNull, maxNbBits);
+    if (maxNbBits < 0 || maxNbBits > 20) return -1;
+    // canonical codes (ZS_largeHuffmanBuildCTableFromTree, 16-bit arithmetic)
+    uint16_t nbPerRank[21] = { 0 }, valPerRank[21] = { 0 };
+    for (int k = 0; k <= nonNull; k++) nbPerRank[node[k].nbBits]++;
+    uint16_t mn = 0;
+    for (int k = maxNbBits; k > 0; k--) {
+        valPerRank[k] = mn;
+        mn = uint16_t(mn + nbPerRank[k]);
+        mn >>= 1;
+    }
+    for (unsigned k = 0; k <= maxSym; k++) nbBits[node[k].symbol] = uint8_t(node[k].nbBits);
+    for (unsigned s = 0; s <= maxSym; s++) code[s] = valPerRank[nbBits[s]]++;
+    return maxNbBits;
 }
 
 } // namespace ent

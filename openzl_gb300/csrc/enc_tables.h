@@ -22,6 +22,8 @@ enum ChunkCodec : int {
     CC_BITPACK,
     CC_FSE,
     CC_HUF,
+    CC_TOK16, // 16-bit chunk: tokenize (alphabet + 8-bit indices)
+    CC_HUF16, // 16-bit chunk: huffman_struct_v2
 };
 
 struct Histo {
@@ -62,6 +64,17 @@ struct HufCTable {
     uint32_t tableLog;
 };
 unsigned hufBuild(HufCTable& ct, const uint32_t* count, unsigned maxSym, unsigned maxNbBits);
+
+// Chunk codec choice for a 16-bit struct chunk (the 2-byte branch of
+// entropyCompressChunk, encode_entropy_binding.c:612-681), whatever the
+// backend mode: CC_CONSTANT, CC_BITPACK (read as little-endian numbers),
+// CC_STORE, CC_TOK16 or CC_HUF16. `count` holds values 0..maxSym.
+ChunkCodec chooseCodec16(const uint32_t* count, unsigned maxSym, uint64_t n, unsigned card);
+
+// 16-bit-symbol Huffman code (ZS_largeHuffmanBuildCTable with maxNbBits 0,
+// src/openzl/codecs/entropy/encode_huffman_kernel.c:34-374): code and length
+// of each value 0..maxSym. Returns the table log, or -1.
+int huf16Build(uint16_t* code, uint8_t* nbBits, const uint32_t* count, unsigned maxSym);
 
 int nextPow2Bits(uint64_t v);
 

@@ -100,6 +100,38 @@ struct TokTask {
     uint32_t tileBase;    // first tile of this task in its launch
 };
 
+// 16-bit chunk statistics: per 2-byte value its count and the index of its
+// first occurrence (initialised to 0xffffffff), and the largest value.
+struct Hist16Task {
+    const uint8_t* src;   // n little-endian 2-byte values
+    uint32_t n;
+    uint32_t* count;      // 65536 slots
+    uint32_t* first;      // 65536 slots
+    uint32_t* maxOut;     // one word, initialised to 0
+};
+
+// Tokenize indices of a 16-bit chunk with fewer than 256 distinct values:
+// `keys` holds the values in increasing order and `ids` their alphabet index.
+struct Tok16Task {
+    const uint8_t* src;
+    uint8_t* idx;
+    const uint16_t* keys;
+    const uint8_t* ids;
+    uint32_t n, na;
+};
+
+// 16-bit-symbol Huffman (huffman_struct_v2) streams of one chunk: stream k
+// (k < 4 when x4, else 0) is written at out + k * streamCap as LE32 symbol
+// count, LE32 bitstream size, bitstream; its bitstream size goes to
+// sizes[sizeSlot + k].
+struct Huf16EncTask {
+    const uint8_t* src;
+    uint8_t* out;
+    const uint16_t* code;   // per value 0..maxSym
+    const uint8_t* nbBits;
+    uint32_t n, streamCap, sizeSlot, x4;
+};
+
 constexpr uint32_t kEncTile = 4096; // elements per numeric/pack tile (32 per thread)
 
 } // namespace ozl

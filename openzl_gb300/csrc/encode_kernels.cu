@@ -339,6 +339,92 @@ __global__ void __launch_bounds__(32) kHufEnc(const HufEncTask* __restrict__ tas
     sizes[t.sizeSlot + k] = bo.close();
 }
 
+// 16-bit chunk statistics (the counts ZS_Histogram_count16 takes,
+// src/openzl/shared/histogram.c:37-80, plus first occurrences for tokenize):
+// one tile of kEncTile values per CTA, global atomics per value; the maximum
+// is reduced per warp first.
+__global__ void __launch_bounds__(256) kHist16(const Hist16Task* __restrict__ tasks,
+                                               const TileRef* __restrict__ tiles)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    Hist16Task const t = tasks[tr.task];
+    uint32_t const i0 = tr.tile * kEncTile;
+    uint32_t mx = 0;
+    for (uint32_t k = threadIdx.x; k < kEncTile; k += 256) {
+        uint32_t const i = i0 + k;
+        if (i >= t.n) break;
+        uint32_t const v = uint32_t(t.src[2 * i]) | (uint32_t(t.src[2 * i + 1]) << 8);
+        atomicAdd(&t.count[v], 1u);
+        atomicMin(&t.first[v], i);
+        mx = max(mx, v);
+    }
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if ((threadIdx.x & 31) == 0) atomicMax(t.maxOut, mx);
+}
+
+// tokenize indices: binary search of each value among the chunk's sorted
+// distinct values (fewer than 256, staged in shared memory)
+__global__ void __launch_bounds__(256) kTok16(const Tok16Task* __restrict__ tasks, const TileRef* __restrict__ tiles)
+{
+    __shared__ uint16_t keys[256];
+    __shared__ uint8_t ids[256];
+    TileRef const tr = tiles[blockIdx.x];
+    Tok16Task const t = tasks[tr.task];
+    for (uint32_t k = threadIdx.x; k < t.na; k += 256) {
+        keys[k] = t.keys[k];
+        ids[k] = t.ids[k];
+    }
+    __syncthreads();
+    uint32_t const i0 = tr.tile * kEncTile;
+    for (uint32_t k = threadIdx.x; k < kEncTile; k += 256) {
+        uint32_t const i = i0 + k;
+        if (i >= t.n) break;
+        uint32_t const v = uint32_t(t.src[2 * i]) | (uint32_t(t.src[2 * i + 1]) << 8);
+        uint32_t lo = 0, hi = t.na; // first key >= v
+        while (lo < hi) {
+            uint32_t const mid = (lo + hi) >> 1;
+            if (keys[mid] < v) lo = mid + 1;
+            else hi = mid;
+        }
+        t.idx[i] = ids[lo < t.na ? lo : 0];
+    }
+}
+
+// 16-bit-symbol Huffman streams (ZS_largeHuffmanEncodeUsingCTable and its 4X
+// split, src/openzl/codecs/entropy/encode_huffman_kernel.c:413-508): stream k
+// of a 4X chunk holds size/4 + 1 symbols, the last one the rest; symbols are
+// appended from the end of the stream to its start, then a 1 bit closes it.
+// sizes[sizeSlot + k] gets the bitstream's size, sizes[sizeSlot + 4 + k] its
+// whole bytes (the reference's writer fails once these reach its capacity
+// less 8 bytes).
+__global__ void __launch_bounds__(128) kHuf16Enc(const Huf16EncTask* __restrict__ tasks, uint32_t nbTasks,
+                                                 uint32_t* __restrict__ sizes)
+{
+    uint32_t const g = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t const ti = g >> 2, k = g & 3;
+    if (ti >= nbTasks) return;
+    Huf16EncTask const t = tasks[ti];
+    if (!t.x4 && k) return;
+    uint32_t const chunk = t.x4 ? t.n / 4 + 1 : t.n;
+    uint32_t const start = min(t.n, k * chunk);
+    uint32_t const len = min(chunk, t.n - start);
+    uint8_t* const out = t.out + uint64_t(k) * t.streamCap;
+    BitOut bo(out + 8, t.streamCap - 8);
+    const uint8_t* const src = t.src + 2ull * start;
+    uint64_t bits = 1;
+    for (uint32_t i = len; i > 0; i--) {
+        uint32_t const v = uint32_t(src[2 * (i - 1)]) | (uint32_t(src[2 * (i - 1) + 1]) << 8);
+        uint32_t const nb = __ldg(t.nbBits + v);
+        bo.add(__ldg(t.code + v), nb);
+        bits += nb;
+    }
+    uint32_t const size = bo.close();
+    *reinterpret_cast<uint32_t*>(out) = len;
+    *reinterpret_cast<uint32_t*>(out + 4) = size;
+    sizes[t.sizeSlot + k] = size;
+    sizes[t.sizeSlot + 4 + k] = uint32_t(bits / 8);
+}
+
 __global__ void kPut(const PutTask* __restrict__ tasks, uint32_t n)
 {
     uint32_t const i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -585,6 +671,19 @@ void launchTokCount(const TokTask* t, uint32_t nbTasks, const TileRef* tiles, ui
     kTokMark<<<nbTiles, 256, 0, s>>>(t, tiles, tileSums, errors);
     kTokPrefix<<<(nbTasks * 32 + 255) / 256, 256, 0, s>>>(t, nbTasks, tileSums, tilePrefix, counts);
     kTokRank<<<nbTiles, 256, 0, s>>>(t, tiles, tilePrefix);
+}
+
+void launchHist16(const Hist16Task* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s)
+{
+    if (nbTiles) kHist16<<<nbTiles, 256, 0, s>>>(t, tiles);
+}
+void launchTok16(const Tok16Task* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s)
+{
+    if (nbTiles) kTok16<<<nbTiles, 256, 0, s>>>(t, tiles);
+}
+void launchHuf16Enc(const Huf16EncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s)
+{
+    if (n) kHuf16Enc<<<(4 * n + 127) / 128, 128, 0, s>>>(t, n, sizes);
 }
 
 void launchTokEmit(const TokTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s)

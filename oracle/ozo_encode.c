@@ -694,6 +694,171 @@ static size_t huf_compress4x(uint8_t* dst, size_t cap, const uint8_t* src, size_
 }
 
 /* ------------------------------------------------------------------ */
+/* 16-bit-symbol Huffman (src/openzl/codecs/entropy/encode_huffman_kernel.c) */
+typedef struct {
+    uint32_t count, parent;
+    uint16_t symbol, nbBits;
+} LNode;
+
+/* ZS_largeHuffmanSort (encode_huffman_kernel.c:153-229): counts in
+ * decreasing order. The reference's partition by highest set bit, recursing
+ * into each partition on the remaining bits, is stable, so equal counts stay
+ * in symbol order. */
+static int lnode_cmp(const void* a, const void* b)
+{
+    const LNode* x = (const LNode*)a;
+    const LNode* y = (const LNode*)b;
+    if (x->count != y->count) return x->count > y->count ? -1 : 1;
+    return (int)x->symbol - (int)y->symbol;
+}
+
+/* ZS_largeHuffmanBuildTree (encode_huffman_kernel.c:231-290); node[-1] is the
+ * sentinel slot. */
+static int lhuf_build_tree(LNode* node, int maxSV)
+{
+    int nonNull = maxSV;
+    while (node[nonNull].count == 0) nonNull--;
+    int const startNode = maxSV + 1;
+    int nodeNb = startNode, lowS = nonNull, lowN = nodeNb;
+    int const nodeRoot = nodeNb + lowS - 1;
+    node[nodeNb].count = node[lowS].count + node[lowS - 1].count;
+    node[lowS].parent = node[lowS - 1].parent = (uint32_t)nodeNb;
+    nodeNb++;
+    lowS -= 2;
+    for (int n = nodeNb; n <= nodeRoot; n++) node[n].count = 1u << 30;
+    node[-1].count = 1u << 31;
+    for (; nodeNb <= nodeRoot; nodeNb++) {
+        int const n1 = node[lowS].count < node[lowN].count ? lowS-- : lowN++;
+        int const n2 = node[lowS].count < node[lowN].count ? lowS-- : lowN++;
+        node[nodeNb].count = node[n1].count + node[n2].count;
+        node[n1].parent = node[n2].parent = (uint32_t)nodeNb;
+    }
+    node[nodeRoot].nbBits = 0;
+    for (int n = nodeRoot - 1; n >= startNode; n--) node[n].nbBits = (uint16_t)(node[node[n].parent].nbBits + 1);
+    for (int n = 0; n <= nonNull; n++) node[n].nbBits = (uint16_t)(node[node[n].parent].nbBits + 1);
+    return nonNull;
+}
+
+/* ZS_largeHuffmanSetMaxHeight (encode_huffman_kernel.c:34-151) */
+static int lhuf_set_max_height(LNode* node, int last, int maxNbBits)
+{
+    int const largest = node[last].nbBits;
+    if (largest <= maxNbBits) return largest;
+    int totalCost = 0;
+    int const baseCost = 1 << (largest - maxNbBits);
+    int n;
+    for (n = last; node[n].nbBits > maxNbBits; --n) {
+        totalCost += baseCost - (1 << (largest - node[n].nbBits));
+        node[n].nbBits = (uint16_t)maxNbBits;
+    }
+    while (node[n].nbBits == maxNbBits) --n;
+    totalCost >>= (largest - maxNbBits);
+    uint32_t const noSym = 0xF0F0F0F0u;
+    uint32_t rankLast[22];
+    for (int i = 0; i < 22; i++) rankLast[i] = noSym;
+    {
+        int cur = maxNbBits;
+        for (int pos = n; pos >= 0; pos--) {
+            if (node[pos].nbBits >= cur) continue;
+            cur = node[pos].nbBits;
+            rankLast[maxNbBits - cur] = (uint32_t)pos;
+        }
+    }
+    while (totalCost > 0) {
+        int nb = ozo_highbit32((uint32_t)totalCost) + 1;
+        while (nb > 1 && rankLast[nb] == noSym) --nb;
+        for (; nb > 1; nb--) {
+            uint32_t const highPos = rankLast[nb], lowPos = rankLast[nb - 1];
+            if (highPos == noSym || lowPos == noSym) break;
+            if (node[highPos].count <= 2 * node[lowPos].count) break;
+        }
+        while (nb <= 20 && rankLast[nb] == noSym) nb++;
+        if (nb > 21 || rankLast[nb] == noSym) return -1;
+        totalCost -= 1 << (nb - 1);
+        if (rankLast[nb - 1] == noSym) rankLast[nb - 1] = rankLast[nb];
+        node[rankLast[nb]].nbBits++;
+        if (rankLast[nb] == 0) {
+            rankLast[nb] = noSym;
+        } else {
+            rankLast[nb]--;
+            if (node[rankLast[nb]].nbBits != maxNbBits - nb) rankLast[nb] = noSym;
+        }
+    }
+    while (totalCost < 0) {
+        if (rankLast[1] == noSym) {
+            while (node[n].nbBits == maxNbBits) n--;
+            node[n + 1].nbBits--;
+            rankLast[1] = (uint32_t)(n + 1);
+            totalCost++;
+            continue;
+        }
+        node[rankLast[1] + 1].nbBits--;
+        rankLast[1]++;
+        totalCost++;
+    }
+    return maxNbBits;
+}
+
+/* ZS_largeHuffmanBuildCTable with maxNbBits 0 (encode_huffman_kernel.c:292-374):
+ * code lengths and canonical codes per symbol (16-bit code arithmetic, as in
+ * the reference). Returns the table log, or -1. */
+static int lhuf_build_ctable(uint16_t* code, uint16_t* nbBits, const unsigned* count, unsigned maxSV)
+{
+    int maxNbBits = 20;
+    int const bound = ozo_nextpow2((uint64_t)maxSV + 1);
+    if (bound + 3 < maxNbBits) maxNbBits = bound + 3;
+    LNode* all = (LNode*)calloc(2 * (size_t)maxSV + 3, sizeof(LNode));
+    LNode* node = all + 1;
+    for (unsigned s = 0; s <= maxSV; s++) {
+        node[s].count = count[s];
+        node[s].symbol = (uint16_t)s;
+    }
+    qsort(node, (size_t)maxSV + 1, sizeof(LNode), lnode_cmp);
+    int const nonNull = lhuf_build_tree(node, (int)maxSV);
+    maxNbBits = lhuf_set_max_height(node, nonNull, maxNbBits);
+    if (maxNbBits < 0 || maxNbBits > 20) { free(all); return -1; }
+    uint16_t nbPerRank[21] = { 0 }, valPerRank[21] = { 0 };
+    for (int k = 0; k <= nonNull; k++) nbPerRank[node[k].nbBits]++;
+    {
+        uint16_t min = 0;
+        for (int k = maxNbBits; k > 0; k--) {
+            valPerRank[k] = min;
+            min = (uint16_t)(min + nbPerRank[k]);
+            min >>= 1;
+        }
+    }
+    for (unsigned k = 0; k <= maxSV; k++) nbBits[node[k].symbol] = node[k].nbBits;
+    for (unsigned s = 0; s <= maxSV; s++) code[s] = valPerRank[nbBits[s]]++;
+    free(all);
+    return maxNbBits;
+}
+
+/* ZS_largeHuffmanEncodeUsingCTable (encode_huffman_kernel.c:413-488): the
+ * symbol count and the stream size as LE32, then the symbols from last to
+ * first, codes appended LSB-first, closed by a 1 bit. The bit writer gives up
+ * (0) once its output reaches 8 bytes before the end of the capacity. */
+static size_t lhuf_stream(uint8_t* dst, size_t cap, const uint8_t* src, size_t n, const uint16_t* code,
+                          const uint16_t* nbBits)
+{
+    if (cap < 8) return 0;
+    ozo_wr32(dst, (uint32_t)n);
+    size_t const bcap = cap - 8;
+    if (bcap <= 8) return 0;
+    BW b = { dst + 8, bcap, 0, 0, 0 };
+    for (size_t i = n; i > 0; i--) {
+        uint16_t const s = ozo_rd16(src + 2 * (i - 1));
+        bw_add(&b, code[s], nbBits[s]);
+    }
+    bw_add(&b, 1, 1);
+    size_t const full = b.pos;
+    if (full >= bcap - 8) return 0;
+    size_t const sz = full + (b.nb > 0);
+    if (b.nb) dst[8 + full] = (uint8_t)b.acc;
+    ozo_wr32(dst + 4, (uint32_t)sz);
+    return 8 + sz;
+}
+
+/* ------------------------------------------------------------------ */
 /* engine: graph runs */
 static int run_successor(ECtx* c, int g, int sid, const void* arg);
 
@@ -758,6 +923,16 @@ static int node_conv_num_to_struct(ECtx* c, int in)
 {
     ENode* nd = new_node(c, TR_CONV_NUM_TO_STRUCT_LE, in, 1);
     int o = new_stream(c, OZO_TYPE_STRUCT, S(in)->w, S(in)->n, S(in)->data);
+    nd->nbOut = 1;
+    return o;
+}
+
+/* ZL_NODE_INTERPRET_TOKEN_AS_LE: struct tokens read as little-endian
+ * numbers, no codec header (encode_conversion_binding.c:179-189) */
+static int node_conv_struct_to_num(ECtx* c, int in)
+{
+    ENode* nd = new_node(c, TR_CONV_STRUCT_TO_NUM_LE, in, 1);
+    int o = new_stream(c, OZO_TYPE_NUMERIC, S(in)->w, S(in)->n, S(in)->data);
     nd->nbOut = 1;
     return o;
 }
@@ -857,10 +1032,14 @@ static int node_tsplit(ECtx* c, int in)
     return first;
 }
 
-/* EI_splitN over fixed chunk sizes (encode_splitN_binding.c:105-160) */
+/* EI_splitN over fixed chunk sizes (encode_splitN_binding.c:105-160); the
+ * transform follows the stream type (getSplitNNodeID,
+ * encode_splitN_binding.c:163-176) */
 static int node_splitn(ECtx* c, int in, const size_t* sizes, size_t nb)
 {
-    ENode* nd = new_node(c, TR_SPLITN, in, 0);
+    int const t = S(in)->type;
+    ENode* nd = new_node(c, t == OZO_TYPE_STRUCT ? TR_SPLITN_STRUCT : t == OZO_TYPE_NUMERIC ? TR_SPLITN_NUM : TR_SPLITN,
+                         in, 0);
     size_t pos = 0;
     int first = -1;
     for (size_t k = 0; k < nb; k++) {
@@ -986,6 +1165,50 @@ static int node_huf(ECtx* c, int in, const Stats* st)
     return ws;
 }
 
+/* EI_huffman_struct_v2 (encode_entropy_binding.c:287-367): weights (numeric
+ * u8) and the stream table of 1 (up to 1000 symbols) or 4 streams; the
+ * four streams hold size/4 + 1 symbols each, the last the rest
+ * (encode_huffman_kernel.c:490-508). */
+static int node_huf16(ECtx* c, int in, const unsigned* count, unsigned maxSV)
+{
+    size_t const n = S(in)->n;
+    uint16_t* code = (uint16_t*)calloc((size_t)maxSV + 1, 2);
+    uint16_t* nbb = (uint16_t*)calloc((size_t)maxSV + 1, 2);
+    int const tl = lhuf_build_ctable(code, nbb, count, maxSV);
+    if (tl < 0) c->err = OZO_ERR_GENERIC;
+    ENode* nd = new_node(c, TR_HUFFMAN_STRUCT_V2, in, 2);
+    int ws = new_stream(c, OZO_TYPE_NUMERIC, 1, (size_t)maxSV + 1, NULL);
+    for (unsigned v = 0; v <= maxSV; v++) S(ws)->data[v] = (uint8_t)(nbb[v] == 0 ? 0 : tl + 1 - nbb[v]);
+    int const x4 = n > 1000;
+    size_t const nbBytes = (size_t)(ozo_nextpow2(n + 1) + 7) / 8;
+    nd->hdr[0] = (uint8_t)(x4 ? 1 : 0);
+    for (size_t b = 0; b < nbBytes; b++) nd->hdr[1 + b] = (uint8_t)(n >> (8 * b));
+    nd->hsz = nbBytes + 1;
+    size_t const cap = 2 * n + 32;
+    uint8_t* tmp = (uint8_t*)malloc(cap);
+    const uint8_t* const src = S(in)->data;
+    size_t sz = 0;
+    if (x4) {
+        size_t off = 0, const_chunk = n / 4 + 1;
+        for (int k = 0; k < 4 && tl >= 0; k++) {
+            size_t const len = const_chunk < n - off ? const_chunk : n - off;
+            size_t const r = lhuf_stream(tmp + sz, cap - sz, src + 2 * off, len, code, nbb);
+            if (r == 0) { c->err = OZO_ERR_GENERIC; break; }
+            sz += r;
+            off += len;
+        }
+    } else if (tl >= 0) {
+        sz = lhuf_stream(tmp, cap, src, n, code, nbb);
+        if (sz == 0) c->err = OZO_ERR_GENERIC;
+    }
+    new_stream(c, OZO_TYPE_SERIAL, 1, sz, tmp);
+    nd->nbOut = 2;
+    free(tmp);
+    free(code);
+    free(nbb);
+    return ws;
+}
+
 /* tokenizeImpl (encode_tokenize_binding.c:127-215): alphabet in order of
  * first occurrence (ascending unsigned order when sorted), indices of 1, 2
  * or 4 bytes by alphabet size. */
@@ -1030,7 +1253,8 @@ static int node_tokenize(ECtx* c, int in, int sorted)
         free(remap);
     }
     size_t const iw = na <= 256 ? 1 : (na <= 65536 ? 2 : 4);
-    ENode* nd = new_node(c, TR_TOKENIZE_NUMERIC, in, 2);
+    /* struct input: tokenize_struct, first-occurrence order only */
+    ENode* nd = new_node(c, S(in)->type == OZO_TYPE_STRUCT ? TR_TOKENIZE_FIXED : TR_TOKENIZE_NUMERIC, in, 2);
     int a = new_stream(c, S(in)->type, w, na, NULL);
     for (size_t k = 0; k < na; k++) wr(S(a)->data + k * w, alpha[k], w);
     int o = new_stream(c, OZO_TYPE_NUMERIC, iw, n, NULL);
@@ -1106,18 +1330,70 @@ static int entropy_chunk(ECtx* c, int sid, int hufMode, SuccList* succ)
     return 0;
 }
 
-/* entropyDynamicGraph (encode_entropy_binding.c:765-868) for FSE / Huffman */
+/* entropyCompressChunk for 16-bit struct chunks (encode_entropy_binding.c:
+ * 612-681): constant, bitpack, store, tokenize (fewer than 256 distinct
+ * values) or huffman_struct_v2, whatever the graph's backend mode. */
+static int entropy_chunk16(ECtx* c, int sid, SuccList* succ)
+{
+    size_t const n = S(sid)->n;
+    if (n <= 1) { succ_add(succ, G_STORE, sid, NULL); return 0; }
+    unsigned* count = (unsigned*)calloc(65536, sizeof(unsigned));
+    unsigned maxSym = 0;
+    for (size_t i = 0; i < n; i++) {
+        unsigned const v = ozo_rd16(S(sid)->data + 2 * i);
+        count[v]++;
+        if (v > maxSym) maxSym = v;
+    }
+    if (count[maxSym] == n) { free(count); succ_add(succ, G_CONSTANT, sid, NULL); return 0; }
+    size_t card = 0;
+    for (unsigned v = 0; v <= maxSym; v++) card += count[v] > 0;
+    double entropy = calc_entropy(count, maxSym, n);
+    if (1 > entropy) entropy = 1;
+    volatile double prod = entropy * (double)n;
+    volatile double sum = prod + 7;
+    size_t const entropySize = (size_t)sum / 8;
+    size_t const header = maxSym / 4 > 100 ? maxSym / 4 : 100;
+    size_t const huffSize = entropySize + header, storeSize = 2 * n;
+    size_t const nbBits = (size_t)ozo_nextpow2((uint64_t)maxSym + 1);
+    size_t const bitpackSize = (n * nbBits + 7) / 8 + 2;
+    if (bitpackSize <= huffSize && bitpackSize < storeSize) {
+        /* runBitpack: interpret the tokens as little-endian numbers */
+        succ_add(succ, G_BITPACK, node_conv_struct_to_num(c, sid), NULL);
+    } else if (entropy > 15 || huffSize >= storeSize) {
+        succ_add(succ, G_STORE, sid, NULL);
+    } else if (card < 256) {
+        int const a = node_tokenize(c, sid, 0);
+        if (nbBits < 16) succ_add(succ, G_BITPACK, node_conv_struct_to_num(c, a), NULL);
+        else succ_add(succ, G_STORE, a, NULL);
+        succ_add(succ, G_HUF, a + 1, NULL);
+    } else {
+        int const w = node_huf16(c, sid, count, maxSym);
+        succ_add(succ, G_FSE, w, NULL);
+        succ_add(succ, G_STORE, w + 1, NULL);
+    }
+    free(count);
+    return 0;
+}
+
+/* entropyDynamicGraph (encode_entropy_binding.c:765-868) for FSE / Huffman
+ * / entropy */
 static int graph_entropy(ECtx* c, int sid, int hufMode)
 {
     SuccList succ = { 0 };
-    /* doEntropyConversion: eltWidth 1 goes to serial */
+    /* doEntropyConversion (encode_entropy_binding.c:764-810): eltWidth 1
+     * goes to serial, numeric eltWidth 2 to struct; other widths are
+     * rejected */
     if (S(sid)->w == 1 && S(sid)->type != OZO_TYPE_SERIAL)
         sid = S(sid)->type == OZO_TYPE_NUMERIC ? node_conv_num_to_serial(c, sid) : node_conv_struct_to_serial(c, sid);
-    if (S(sid)->w != 1) { c->err = OZO_ERR_UNSUPPORTED; return -1; }
+    else if (S(sid)->w == 2 && S(sid)->type == OZO_TYPE_NUMERIC)
+        sid = node_conv_num_to_struct(c, sid);
+    if (S(sid)->w != 1 && S(sid)->w != 2) { c->err = OZO_ERR_UNSUPPORTED; return -1; }
+    int const wide = S(sid)->w == 2;
     size_t const n = S(sid)->n;
     size_t const kChunk = 1 << 15;
     if (n < 100000) {
-        entropy_chunk(c, sid, hufMode, &succ);
+        if (wide) entropy_chunk16(c, sid, &succ);
+        else entropy_chunk(c, sid, hufMode, &succ);
     } else {
         size_t const nb = (n + kChunk - 1) / kChunk;
         size_t* sizes = (size_t*)malloc(nb * sizeof(size_t));
@@ -1125,7 +1401,10 @@ static int graph_entropy(ECtx* c, int sid, int hufMode)
         sizes[nb - 1] = n - (nb - 1) * kChunk;
         int first = node_splitn(c, sid, sizes, nb);
         free(sizes);
-        for (size_t i = 0; i < nb; i++) entropy_chunk(c, first + (int)i, hufMode, &succ);
+        for (size_t i = 0; i < nb; i++) {
+            if (wide) entropy_chunk16(c, first + (int)i, &succ);
+            else entropy_chunk(c, first + (int)i, hufMode, &succ);
+        }
     }
     return run_succs(c, &succ);
 }

@@ -69,11 +69,10 @@ def build_cases():
     c.append(("empty_serial_fse", 7, np.zeros(0, np.uint8), 0))
     c.append(("tiny_numeric_delta", 9, np.array([5], np.uint32), 4))
     # 16-bit-symbol Huffman (huffman_struct_v2): u16 columns whose alphabet is
-    # too wide for tokenize, through ZL_GRAPH_HUFFMAN. Decode-only cases: the
-    # encoders here do not build 16-bit Huffman tables.
-    c.append(("huf16_zipf_u16", 8, (rng.zipf(1.3, 200000) % 3000).astype(np.uint16), 2, True))
-    c.append(("huf16_x1_u16", 8, (rng.zipf(1.2, 900) % 1000).astype(np.uint16), 2, True))
-    c.append(("huf16_wide_u16", 8, np.minimum(rng.geometric(1 / 3000, 150000), 65535).astype(np.uint16), 2, True))
+    # too wide for tokenize, through ZL_GRAPH_HUFFMAN
+    c.append(("huf16_zipf_u16", 8, (rng.zipf(1.3, 200000) % 3000).astype(np.uint16), 2))
+    c.append(("huf16_x1_u16", 8, (rng.zipf(1.2, 900) % 1000).astype(np.uint16), 2))
+    c.append(("huf16_wide_u16", 8, np.minimum(rng.geometric(1 / 3000, 150000), 65535).astype(np.uint16), 2))
     # ZL_GRAPH_ENTROPY (EBM_any): per chunk FSE, Huffman, flatpack, bitpack,
     # constant or store
     lowent = np.where(rng.random(260000) < 0.98, 0, rng.integers(1, 256, 260000)).astype(np.uint8)

@@ -107,6 +107,39 @@ def test_cctx_frames_equal_reference_frames(gpu_lib, checksums):
     assert not bad, bad[:10]
 
 
+def test_cctx_2byte_numbers_through_huffman_and_entropy_graphs(gpu_lib):
+    """ZL_GRAPH_HUFFMAN and ZL_GRAPH_ENTROPY on 2-byte numeric input: the
+    16-bit chunk path (tokenize, bit packing, store, constant or
+    huffman_struct_v2) gives the reference's frames, and they decode back to
+    typed numeric output."""
+    import openzl_gb300 as oz
+
+    a = oz.api
+    rng = np.random.default_rng(41)
+    arrs = []
+    for n in (3, 1001, 50000, 150000):
+        arrs.append((rng.zipf(1.3, n) % 3000).astype(np.uint16))
+        arrs.append((rng.zipf(1.2, n) % 150).astype(np.uint16))
+        arrs.append(rng.integers(0, 30, n).astype(np.uint16))
+    arrs.append(np.full(4000, 1234, np.uint16))
+    arrs.append(rng.integers(0, 65536, 9000).astype(np.uint16))
+    bad = []
+    for recipe in (8, 17):
+        for arr in arrs:
+            comp = oz.Compressor()
+            comp.select(_graph(oz, comp, recipe))
+            cctx = oz.CCtx()
+            cctx.ref_compressor(comp)
+            cctx.set_parameter(a.CPARAM_FORMAT_VERSION, 23)
+            got = cctx.compress_numeric(arr)
+            want = oracle.compress(recipe, arr, 2)
+            if got.tobytes() != want.tobytes():
+                bad.append((recipe, arr.size, got.size, want.size))
+            data, typ, width = oz.DCtx().decompress_typed(got)
+            assert data.tobytes() == arr.tobytes() and typ == a.TYPE_NUMERIC and width == 2, (recipe, arr.size)
+    assert not bad, bad
+
+
 def test_decompress_rejects_typed_outputs_like_the_reference(gpu_lib):
     import openzl_gb300 as oz
 

@@ -49,6 +49,17 @@ def _cases(seed):
             c.append((17, (rng.zipf(1.2, n) % k).astype(np.uint8), 0))
         c.append((17, np.where(rng.random(n) < 0.98, 0, rng.integers(1, 256, n)).astype(np.uint8), 0))
     c.append((0, rng.integers(0, 256, 3000).astype(np.uint8), 0))
+    # 2-byte input to the Huffman and entropy graphs: per chunk constant,
+    # bit packing, store, tokenize (fewer than 256 values) or
+    # huffman_struct_v2 (1 or 4 streams), chunked from 100000 elements
+    for recipe in (8, 17):
+        for n in (2, 3, 999, 1001, 40000, 140000):
+            c.append((recipe, (rng.zipf(1.3, n) % 3000).astype(np.uint16), 2))
+            c.append((recipe, (rng.zipf(1.2, n) % 200).astype(np.uint16), 2))
+            c.append((recipe, np.minimum(rng.geometric(1 / 3000, n), 65535).astype(np.uint16), 2))
+            c.append((recipe, rng.integers(0, 40, n).astype(np.uint16), 2))
+        c.append((recipe, np.full(5000, 777, np.uint16), 2))
+        c.append((recipe, rng.integers(0, 65536, 20000).astype(np.uint16), 2))
     return c
 
 

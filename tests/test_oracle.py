@@ -73,6 +73,31 @@ def test_oracle_matches_reference_at_older_format_versions():
 
 
 @pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
+def test_oracle_matches_reference_on_2byte_entropy_graphs():
+    """2-byte numbers through the Huffman and entropy graphs (the 16-bit
+    branch of the entropy chunk: constant, bit packing, store, tokenize or
+    huffman_struct_v2, chunked from 100000 elements): the oracle's frames
+    equal the reference's."""
+    import ctypes
+
+    ref = ctypes.CDLL(REF_DRIVER)
+    ref.ref_compress.restype = ctypes.c_int64
+    ref.ref_compress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(3)
+    for recipe in (8, 17):
+        for n in (2, 3, 100, 999, 1001, 5000, 40000, 99999, 100000, 140000):
+            for a in ((rng.zipf(1.3, n) % 3000).astype(np.uint16), (rng.zipf(1.2, n) % 200).astype(np.uint16),
+                      np.minimum(rng.geometric(1 / 3000, n), 65535).astype(np.uint16),
+                      rng.integers(0, 65536, n).astype(np.uint16), rng.integers(0, 40, n).astype(np.uint16),
+                      np.full(n, 77, np.uint16), rng.choice(np.array([5, 60000], np.uint16), n)):
+                dst = np.zeros(4 * n + 4096, np.uint8)
+                r = ref.ref_compress(recipe, a.ctypes.data, n, 2, dst.ctypes.data, dst.size, 1, 0)
+                assert r > 0
+                assert oracle.compress(recipe, a, 2).tobytes() == dst[:r].tobytes(), (recipe, n)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
 def test_xxh3_every_length_class_matches_reference():
     import ctypes
 
