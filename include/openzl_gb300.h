@@ -37,6 +37,7 @@ typedef enum {
     ZL_ErrorCode_srcSize_tooSmall = 3,
     ZL_ErrorCode_srcSize_tooLarge = 4,
     ZL_ErrorCode_dstCapacity_tooSmall = 5,
+    ZL_ErrorCode_userBuffers_invalidNum = 8,
     ZL_ErrorCode_header_unknown = 10,
     ZL_ErrorCode_frameParameter_unsupported = 11,
     ZL_ErrorCode_corruption = 12,
@@ -44,6 +45,7 @@ typedef enum {
     ZL_ErrorCode_contentChecksumWrong = 14,
     ZL_ErrorCode_compressionParameter_invalid = 20,
     ZL_ErrorCode_parameter_invalid = 21,
+    ZL_ErrorCode_outputID_invalid = 22,
     ZL_ErrorCode_invalidRequest_singleOutputFrameOnly = 23,
     ZL_ErrorCode_graph_invalid = 30,
     ZL_ErrorCode_invalidTransform = 32,
@@ -138,7 +140,8 @@ size_t ZL_TypedBuffer_numElts(const ZL_TypedBuffer* tbuffer);
 size_t ZL_TypedBuffer_eltWidth(const ZL_TypedBuffer* tbuffer);
 /* zl_decompress.h:505 */
 ZL_Report ZL_DCtx_decompressTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* output, const void* compressed, size_t cSize);
-/* zl_decompress.h:527: frames here have one output, so nbOutputs must be 1. */
+/* zl_decompress.h:527: nbOutputs must equal the frame's output count
+ * (userBuffers_invalidNum otherwise); returns the number of outputs. */
 ZL_Report ZL_DCtx_decompressMultiTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* outputs[], size_t nbOutputs,
                                          const void* compressed, size_t cSize);
 
@@ -270,12 +273,22 @@ ZL_Report ozl_gpu_decompress(ZL_DCtx* dctx, void* d_dst, size_t dstCapacity,
 typedef struct OZL_GpuBatch_s OZL_GpuBatch;
 OZL_GpuBatch* ozl_gpu_batch_create(void);
 void ozl_gpu_batch_free(OZL_GpuBatch* b);
+/* Output layout of one frame for the batch API (no counterpart in the
+ * reference; its ZL_FrameInfo gives counts, types and sizes but not element
+ * widths, which sit in the block headers). Plans the frame on the host and
+ * writes, for the first `capacity` outputs, the offset in the destination,
+ * the size in bytes, the type and the element width. Returns the number of
+ * outputs; the destination needs offsets[n-1] + sizes[n-1] bytes. */
+ZL_Report ozl_frame_outputs(const void* frame, size_t frameSize, size_t capacity, uint64_t* offsets,
+                            uint64_t* sizes, int* types, uint32_t* widths);
 /* Sets a DParam for subsequent plans (same meaning as ZL_DCtx_setParameter). */
 ZL_Report ozl_gpu_batch_setParameter(OZL_GpuBatch* b, ZL_DParam param, int value);
 /* Plans the decode of nbFrames frames. h_frames[i]: host copy (planning);
  * d_frames[i]: device copy; d_dsts[i]/dstCapacities[i]: device outputs.
- * Returns the total decompressed size. Allocates device scratch sized for
- * the plan; reuses it across runs. */
+ * A frame with several outputs writes them one after another into its
+ * destination, each at a 16-byte-aligned offset (ozl_frame_outputs gives the
+ * layout). Returns the total destination bytes. Allocates device scratch
+ * sized for the plan; reuses it across runs. */
 ZL_Report ozl_gpu_batch_plan(OZL_GpuBatch* b, size_t nbFrames,
                              const void* const* h_frames, const size_t* frameSizes,
                              const void* const* d_frames, void* const* d_dsts,

@@ -20,6 +20,7 @@ from ._lib import (  # noqa: F401
     XXH3_STATIC_MAX_LEN,
     get_decompressed_size,
     get_compressed_size,
+    frame_outputs,
     library,
     library_path,
 )

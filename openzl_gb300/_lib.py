@@ -48,6 +48,7 @@ def library():
     sig = {
         "ZL_getDecompressedSize": ([vp, sz], ZLReport),
         "ZL_getCompressedSize": ([vp, sz], ZLReport),
+        "ozl_frame_outputs": ([vp, sz, sz, vp, vp, vp, vp], ZLReport),
         "ZL_DCtx_create": ([], vp),
         "ZL_DCtx_free": ([vp], None),
         "ZL_DCtx_setParameter": ([vp, ctypes.c_int, ctypes.c_int], ZLReport),
@@ -154,6 +155,19 @@ def get_compressed_size(frame):
     return _check(library().ZL_getCompressedSize(f.ctypes.data, f.size))
 
 
+def frame_outputs(frame):
+    """ozl_frame_outputs: per output its offset in a batch destination, size
+    in bytes, ZL_Type value and element width, as a list of dicts."""
+    f = _as_u8(frame)
+    n = _check(library().ozl_frame_outputs(f.ctypes.data, f.size, 0, None, None, None, None))
+    offs = (ctypes.c_uint64 * max(n, 1))()
+    sizes = (ctypes.c_uint64 * max(n, 1))()
+    types = (ctypes.c_int * max(n, 1))()
+    widths = (ctypes.c_uint32 * max(n, 1))()
+    _check(library().ozl_frame_outputs(f.ctypes.data, f.size, n, offs, sizes, types, widths))
+    return [{"offset": offs[o], "size": sizes[o], "type": types[o], "width": widths[o]} for o in range(n)]
+
+
 # DParam values (include/openzl_gb300.h)
 DPARAM_STICKY = 1
 DPARAM_CHECK_COMPRESSED = 2
@@ -198,6 +212,29 @@ class DCtx:
         if rep.code:
             raise ZLError(rep.code, self._err(rep))
         return out[: rep.value], info.type, info.fixedWidth
+
+    def decompress_multi(self, frame):
+        """ZL_DCtx_decompressMultiTBuffer: every output of the frame as
+        [(bytes as numpy uint8, ZL_Type value, element width)]."""
+        f = _as_u8(frame)
+        fi = FrameInfo(f)
+        n = fi.num_outputs()
+        bufs = [self._lib.ZL_TypedBuffer_create() for _ in range(n)]
+        try:
+            arr = (ctypes.c_void_p * max(n, 1))(*bufs)
+            rep = self._lib.ZL_DCtx_decompressMultiTBuffer(self._h, arr, n, f.ctypes.data, f.size)
+            if rep.code:
+                raise ZLError(rep.code, self._err(rep))
+            res = []
+            for b in bufs:
+                size = self._lib.ZL_TypedBuffer_byteSize(b)
+                ptr = self._lib.ZL_TypedBuffer_rPtr(b)
+                data = np.ctypeslib.as_array((ctypes.c_uint8 * max(size, 1)).from_address(ptr))[:size].copy()
+                res.append((data, self._lib.ZL_TypedBuffer_type(b), self._lib.ZL_TypedBuffer_eltWidth(b)))
+            return res
+        finally:
+            for b in bufs:
+                self._lib.ZL_TypedBuffer_free(b)
 
     def decompress_serial(self, frame, capacity):
         """ZL_DCtx_decompress (serial outputs only, as in the reference)."""

@@ -80,6 +80,8 @@ const char* ZL_ErrorCode_toString(ZL_ErrorCode code)
         case ZL_ErrorCode_node_unexpected_input_type: return "Unexpected input type for node";
         case ZL_ErrorCode_node_invalid: return "Node invalid";
         case ZL_ErrorCode_invalidRequest_singleOutputFrameOnly: return "Only single-output frames are supported";
+        case ZL_ErrorCode_userBuffers_invalidNum: return "Wrong number of output buffers";
+        case ZL_ErrorCode_outputID_invalid: return "Invalid output ID";
         case ZL_ErrorCode_invalidTransform: return "Codec not on the GPU path";
         case ZL_ErrorCode_formatVersion_unsupported: return "Format version unsupported";
         case ZL_ErrorCode_formatVersion_notSet: return "Format version not set";
@@ -139,7 +141,29 @@ ZL_Report ZL_getDecompressedSize(const void* src, size_t size)
     std::string err;
     int rc = ozl::parseFrameHeader(static_cast<const uint8_t*>(src), size, h, err);
     if (rc) return fail(rc);
+    // decode_frameheader.c:1156-1163: meaningful for single-output frames only
+    if (h.sizes.size() != 1) return fail(ZL_ErrorCode_invalidRequest_singleOutputFrameOnly);
     return ok(size_t(h.outSize));
+}
+
+ZL_Report ozl_frame_outputs(const void* frame, size_t frameSize, size_t capacity, uint64_t* offsets, uint64_t* sizes,
+                            int* types, uint32_t* widths)
+{
+    if (!frame) return fail(ZL_ErrorCode_parameter_invalid);
+    ozl::DecodePlan plan;
+    std::string err;
+    const uint8_t* f = static_cast<const uint8_t*>(frame);
+    int rc = plan.build(1, &f, &frameSize, nullptr, false, false, err);
+    if (rc) return fail(rc);
+    const ozl::FramePlan& fp = plan.frames[0];
+    size_t const n = fp.outOffs.size();
+    for (size_t o = 0; o < n && o < capacity; o++) {
+        if (offsets) offsets[o] = fp.outOffs[o];
+        if (sizes) sizes[o] = fp.outSizes[o];
+        if (types) types[o] = fp.outTypes[o];
+        if (widths) widths[o] = fp.outTypes[o] == ZL_Type_serial ? 1 : fp.outWidths[o];
+    }
+    return ok(n);
 }
 
 ZL_Report ZL_getCompressedSize(const void* src, size_t size)
@@ -496,19 +520,91 @@ ZL_Report ZL_DCtx_decompressTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* out, const vo
     return r;
 }
 
+// All outputs of a frame, decoded on the device into one destination (each
+// output at its 16-byte-aligned offset), then copied to the typed buffers
+// (decompress2.c:1580-1775).
 ZL_Report ZL_DCtx_decompressMultiTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* outputs[], size_t nbOutputs,
                                          const void* src, size_t cSize)
 {
-    if (!dctx || !outputs || nbOutputs != 1) return fail(ZL_ErrorCode_invalidRequest_singleOutputFrameOnly);
-    return ZL_DCtx_decompressTBuffer(dctx, outputs[0], src, cSize);
+    if (!dctx || !outputs || !src) return fail(ZL_ErrorCode_parameter_invalid);
+    for (size_t o = 0; o < nbOutputs; o++)
+        if (!outputs[o]) return fail(ZL_ErrorCode_parameter_invalid);
+    dctx->err.clear();
+    ozl::FrameHeader h;
+    int rc = ozl::parseFrameHeader(static_cast<const uint8_t*>(src), cSize, h, dctx->err);
+    if (rc) { resetParams(dctx); return fail(rc); }
+    if (h.sizes.size() != nbOutputs) { // decompress2.c:845
+        dctx->err = "the frame holds " + std::to_string(h.sizes.size()) + " outputs";
+        resetParams(dctx);
+        return fail(ZL_ErrorCode_userBuffers_invalidNum);
+    }
+    std::vector<uint64_t> offs;
+    uint64_t const extent = ozl::frameOutputLayout(h, offs);
+    auto done = [&](ZL_Report r) {
+        resetParams(dctx);
+        return r;
+    };
+    if (!dctx->stream && cudaStreamCreateWithFlags(&dctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        dctx->err = "no CUDA device";
+        return done(fail(ZL_ErrorCode_GENERIC));
+    }
+    if (!dctx->frame.reserve(cSize + 64) || !dctx->out.reserve(extent + 64)) {
+        dctx->err = "device allocation failed";
+        return done(fail(ZL_ErrorCode_allocation));
+    }
+    cudaStream_t s = dctx->stream;
+    if (cudaMemcpyAsync(dctx->frame.data(), src, cSize, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+        dctx->err = "copy to device failed";
+        return done(fail(ZL_ErrorCode_GENERIC));
+    }
+    const void* dF = dctx->frame.data();
+    void* dO = dctx->out.data();
+    size_t cap = size_t(extent);
+    ZL_Report r = dctx->batch.makePlan(1, &src, &cSize, &dF, &dO, &cap);
+    if (!ZL_isError(r)) r = dctx->batch.run(s, false);
+    if (!ZL_isError(r)) r = dctx->batch.check(s);
+    if (ZL_isError(r)) {
+        dctx->err = dctx->batch.err;
+        return done(r);
+    }
+    const ozl::FramePlan& fp = dctx->batch.plan.frames[0];
+    for (size_t o = 0; o < nbOutputs; o++) {
+        ZL_TypedBuffer_s* out = outputs[o];
+        size_t const bytes = size_t(fp.outSizes[o]);
+        ZL_Type const type = ZL_Type(fp.outTypes[o]);
+        size_t const w = type == ZL_Type_serial ? 1 : fp.outWidths[o];
+        void* dst;
+        if (out->wrap) {
+            if (bytes > out->capacity) { dctx->err = "output buffer too small"; return done(fail(ZL_ErrorCode_dstCapacity_tooSmall)); }
+            if (type != out->type || (type != ZL_Type_serial && w != out->width)) {
+                dctx->err = "a wrapped buffer's type or width differs from the frame's output";
+                return done(fail(ZL_ErrorCode_GENERIC));
+            }
+            dst = out->wrapped;
+        } else {
+            try {
+                out->own.resize(bytes + 1);
+            } catch (...) {
+                return done(fail(ZL_ErrorCode_allocation));
+            }
+            dst = out->own.data();
+        }
+        if (bytes && cudaMemcpyAsync(dst, static_cast<uint8_t*>(dO) + offs[o], bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return done(fail(ZL_ErrorCode_GENERIC));
+        out->type = type;
+        out->width = w;
+        out->bytes = bytes;
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess) return done(fail(ZL_ErrorCode_GENERIC));
+    return done(ok(nbOutputs));
 }
 
 // ---------------------------------------------------------------------------
 // Frame information from the frame header (decode_frameheader.c:290-470).
 struct ZL_FrameInfo_s {
     unsigned version;
-    ZL_Type type;
-    uint64_t size;
+    std::vector<int> types;
+    std::vector<uint64_t> sizes;
 };
 
 ZL_FrameInfo* ZL_FrameInfo_create(const void* src, size_t cSize)
@@ -520,8 +616,8 @@ ZL_FrameInfo* ZL_FrameInfo_create(const void* src, size_t cSize)
     ZL_FrameInfo_s* fi = new (std::nothrow) ZL_FrameInfo_s();
     if (!fi) return nullptr;
     fi->version = h.version;
-    fi->type = ZL_Type(h.outType); // the planner's type codes are ZL_Type's values
-    fi->size = h.outSize;
+    fi->types = h.types; // the planner's type codes are ZL_Type's values
+    fi->sizes = h.sizes;
     return fi;
 }
 void ZL_FrameInfo_free(ZL_FrameInfo* fi) { delete fi; }
@@ -529,25 +625,34 @@ ZL_Report ZL_FrameInfo_getFormatVersion(const ZL_FrameInfo* fi)
 {
     return fi ? ok(fi->version) : fail(ZL_ErrorCode_parameter_invalid);
 }
-ZL_Report ZL_FrameInfo_getNumOutputs(const ZL_FrameInfo* fi) { return fi ? ok(1) : fail(ZL_ErrorCode_parameter_invalid); }
+ZL_Report ZL_FrameInfo_getNumOutputs(const ZL_FrameInfo* fi)
+{
+    return fi ? ok(fi->sizes.size()) : fail(ZL_ErrorCode_parameter_invalid);
+}
+// decode_frameheader.c:421-437: an ID past the outputs is outputID_invalid
+static bool badOutput(const ZL_FrameInfo* fi, int id) { return id < 0 || size_t(id) >= fi->sizes.size(); }
 ZL_Report ZL_FrameInfo_getOutputType(const ZL_FrameInfo* fi, int id)
 {
-    if (!fi || id != 0) return fail(ZL_ErrorCode_parameter_invalid);
-    return ok(size_t(fi->type));
+    if (!fi) return fail(ZL_ErrorCode_parameter_invalid);
+    if (badOutput(fi, id)) return fail(ZL_ErrorCode_outputID_invalid);
+    return ok(size_t(fi->types[size_t(id)]));
 }
 ZL_Report ZL_FrameInfo_getDecompressedSize(const ZL_FrameInfo* fi, int id)
 {
-    if (!fi || id != 0) return fail(ZL_ErrorCode_parameter_invalid);
-    return ok(size_t(fi->size));
+    if (!fi) return fail(ZL_ErrorCode_parameter_invalid);
+    if (badOutput(fi, id)) return fail(ZL_ErrorCode_outputID_invalid);
+    return ok(size_t(fi->sizes[size_t(id)]));
 }
 ZL_Report ZL_FrameInfo_getNumElts(const ZL_FrameInfo* fi, int id)
 {
-    if (!fi || id != 0) return fail(ZL_ErrorCode_parameter_invalid);
+    if (!fi) return fail(ZL_ErrorCode_parameter_invalid);
+    if (badOutput(fi, id)) return fail(ZL_ErrorCode_outputID_invalid);
     // decode_frameheader.c:448-453: frames before v21 carry no element counts
     if (fi->version < 21) return fail(ZL_ErrorCode_GENERIC);
     // decode_frameheader.c:455-467: counts known for serial outputs only
-    if (fi->type == ZL_Type_struct || fi->type == ZL_Type_numeric) return fail(ZL_ErrorCode_temporaryLibraryLimitation);
-    return ok(size_t(fi->size));
+    int const t = fi->types[size_t(id)];
+    if (t == ZL_Type_struct || t == ZL_Type_numeric) return fail(ZL_ErrorCode_temporaryLibraryLimitation);
+    return ok(size_t(fi->sizes[size_t(id)]));
 }
 
 } // extern "C"

@@ -108,7 +108,6 @@ enum : int {
     E_HEADER = 10,
     E_CORRUPT = 12,
     E_CK_COMPRESSED = 13,
-    E_SINGLE_OUTPUT = 23,
     E_VERSION = 60,
     E_LIMIT = 81,
     E_TRANSFORM = 32,
@@ -236,6 +235,7 @@ int DecodePlan::build(size_t nbFrames, const uint8_t* const* hFrames, const size
     nodes.clear();
     hashes.clear();
     directCopies.clear();
+    gathers.clear();
     params.clear();
     arenaBytes = 0;
     totalOut = 0;
@@ -269,16 +269,52 @@ int parseFrameHeader(const uint8_t* src, size_t size, FrameHeader& h, std::strin
     unsigned const version = magic - 0xD7B1A5C0u;
     h.version = version;
     static const int typeMap[4] = { TY_SERIAL, TY_STRUCT, TY_NUMERIC, TY_STRING };
+    size_t nbOut = 1, pos = 4;
+    auto byteAt = [&](size_t i, uint8_t& v) -> bool {
+        if (i >= size) return false;
+        v = src[i];
+        return true;
+    };
     if (version < 21) {
-        size_t pos = 4 + (version >= 14);
-        if (version >= 15 && (src[4] >> 6) != 0) {
-            err = "only single-output frames are supported";
-            return E_SINGLE_OUTPUT;
+        if (version >= 15) {
+            uint8_t t;
+            if (size < pos + 1 + 4 || !byteAt(pos++, t)) { err = "truncated frame header"; return E_SRC_SMALL; }
+            nbOut = size_t(t >> 6) + 1;
+            if (nbOut == 4) {
+                if (!byteAt(pos++, t)) { err = "truncated frame header"; return E_SRC_SMALL; }
+                nbOut = size_t(t >> 4) + 4;
+            }
+            if (nbOut == 19) {
+                if (!byteAt(pos++, t)) { err = "truncated frame header"; return E_SRC_SMALL; }
+                nbOut = size_t(t) + 19;
+            }
+            if (nbOut == 274) {
+                if (pos + 2 > size) { err = "truncated frame header"; return E_SRC_SMALL; }
+                nbOut = size_t(src[pos] | (src[pos + 1] << 8)) + 274;
+                pos += 2;
+            }
+        } else if (version == 14) {
+            pos++; // the type byte
         }
-        h.outType = version >= 14 ? typeMap[src[4] & 3] : TY_SERIAL;
-        if (pos + 4 > size) { err = "truncated frame header"; return E_SRC_SMALL; }
-        h.outSize = readLE32(src + pos);
-        h.end = pos + 4;
+        if (nbOut > 2048) { err = "too many outputs"; return E_LIMIT; }
+        h.types.assign(nbOut, TY_SERIAL);
+        if (version >= 14) {
+            for (size_t n = 0; n < nbOut && n < 3; n++) h.types[n] = typeMap[(src[4] >> (2 * n)) & 3];
+            if (nbOut > 3) {
+                if (size < 6) { err = "truncated frame header"; return E_SRC_SMALL; }
+                for (size_t n = 3; n < nbOut && n < 5; n++) h.types[n] = typeMap[(src[5] >> (2 * (n - 3))) & 3];
+            }
+            uint8_t tok = 0;
+            for (size_t n = 5; n < nbOut; n++) {
+                size_t const sh = ((n - 5) % 4) * 2;
+                if (sh == 0 && !byteAt(pos++, tok)) { err = "truncated frame header"; return E_SRC_SMALL; }
+                h.types[n] = typeMap[(tok >> sh) & 3];
+            }
+        }
+        if (pos + 4 * nbOut > size) { err = "truncated frame header"; return E_SRC_SMALL; }
+        h.sizes.resize(nbOut);
+        for (size_t n = 0; n < nbOut; n++) h.sizes[n] = readLE32(src + pos + 4 * n);
+        h.end = pos + 4 * nbOut;
     } else {
         if (size < 9) { err = "frame too small"; return E_SRC_SMALL; }
         uint8_t const flags = src[4];
@@ -286,13 +322,37 @@ int parseFrameHeader(const uint8_t* src, size_t size, FrameHeader& h, std::strin
         h.hasCompressedCk = (flags >> 1) & 1;
         bool const hasComment = (flags >> 2) & 1;
         uint8_t const t1 = src[5];
-        if ((t1 & 15) != 1) { err = "only single-output frames are supported"; return E_SINGLE_OUTPUT; }
-        h.outType = typeMap[(t1 >> 4) & 3];
-        Reader rd{ src + 6, src + size };
-        uint64_t sz1;
-        if (!rd.varint(sz1)) { err = "truncated frame header"; return E_SRC_SMALL; }
-        if (sz1 == 0) { err = "unknown decompressed size"; return E_LIMIT; }
-        h.outSize = sz1 - 1;
+        pos = 6;
+        nbOut = t1 & 15;
+        size_t done = 0;
+        if (nbOut == 15) {
+            uint8_t t2;
+            if (!byteAt(pos++, t2)) { err = "truncated frame header"; return E_SRC_SMALL; }
+            nbOut = (size_t(t2) << 4) + (t1 >> 4) + 15;
+        }
+        if (nbOut == 0) { err = "frame without outputs"; return E_CORRUPT; }
+        if (nbOut > 2048) { err = "too many outputs"; return E_LIMIT; }
+        h.types.assign(nbOut, TY_SERIAL);
+        if ((t1 & 15) != 15) {
+            for (size_t n = 0; n < nbOut && n < 2; n++) h.types[n] = typeMap[(t1 >> (4 + 2 * n)) & 3];
+            done = 2;
+        }
+        uint8_t tok = 0;
+        for (size_t n = done; n < nbOut; n++) {
+            size_t const sh = ((n - done) % 4) * 2;
+            if (sh == 0 && !byteAt(pos++, tok)) { err = "truncated frame header"; return E_SRC_SMALL; }
+            h.types[n] = typeMap[(tok >> sh) & 3];
+        }
+        Reader rd{ src + pos, src + size };
+        h.sizes.resize(nbOut);
+        for (size_t n = 0; n < nbOut; n++) {
+            uint64_t sz1;
+            if (!rd.varint(sz1)) { err = "truncated frame header"; return E_SRC_SMALL; }
+            if (sz1 == 0) { err = "unknown decompressed size"; return E_LIMIT; }
+            h.sizes[n] = sz1 - 1;
+        }
+        for (size_t n = 0; n < nbOut; n++)
+            if (h.types[n] == TY_STRING) { err = "string outputs are not supported"; return E_LIMIT; }
         if (version >= 22 && hasComment) {
             uint64_t c;
             if (!rd.varint(c) || c == 0 || c > size_t(rd.end - rd.p)) { err = "bad comment"; return E_CORRUPT; }
@@ -305,8 +365,22 @@ int parseFrameHeader(const uint8_t* src, size_t size, FrameHeader& h, std::strin
             h.end++;
         }
     }
-    if (h.outType == TY_STRING) { err = "string outputs are not supported"; return E_LIMIT; }
+    for (int t : h.types)
+        if (t == TY_STRING) { err = "string outputs are not supported"; return E_LIMIT; }
+    h.outType = h.types[0];
+    h.outSize = h.sizes[0];
     return 0;
+}
+
+uint64_t frameOutputLayout(const FrameHeader& h, std::vector<uint64_t>& offsets)
+{
+    offsets.resize(h.sizes.size());
+    uint64_t extent = 0;
+    for (size_t o = 0; o < h.sizes.size(); o++) {
+        offsets[o] = (extent + 15) & ~uint64_t(15);
+        extent = offsets[o] + h.sizes[o];
+    }
+    return extent;
 }
 
 int DecodePlan::planFrame(int f, const uint8_t* src, size_t size, size_t dstCap, bool ckContent,
@@ -315,14 +389,20 @@ int DecodePlan::planFrame(int f, const uint8_t* src, size_t size, size_t dstCap,
     FrameHeader h;
     int rc = parseFrameHeader(src, size, h, err);
     if (rc) return rc;
-    if (h.outSize > dstCap) { err = "destination too small"; return E_DST_SMALL; }
+    FramePlan& fp = frames[f];
+    size_t const nbOut = h.sizes.size();
+    uint64_t const extent = frameOutputLayout(h, fp.outOffs);
+    fp.outSizes = h.sizes;
+    fp.outTypes = h.types;
+    fp.outWidths.assign(nbOut, 0);
+    if (extent > dstCap) { err = "destination too small"; return E_DST_SMALL; }
     size_t pos = h.end;
     // header checksum byte: low 8 bits of XXH3 over the header; verified on
     // the device together with the block checksums.
     if (h.hdrCk && ckCompressed)
-        hashes.push_back(PlanHash{ f, false, 0, pos - 1, src[pos - 1], E_CK_COMPRESSED, true });
-    frames[f].outType = h.outType;
-    uint64_t produced = 0;
+        hashes.push_back(PlanHash{ f, HW_FRAME, 0, pos - 1, src[pos - 1], E_CK_COMPRESSED, true });
+    fp.outType = h.outType;
+    std::vector<uint64_t> produced(nbOut, 0);
     for (;;) {
         // versions before 21 hold one block and no end-of-frame marker
         // (decompress2.c:1689-1714)
@@ -331,17 +411,16 @@ int DecodePlan::planFrame(int f, const uint8_t* src, size_t size, size_t dstCap,
             if (src[pos] == 0) { pos++; break; }
         }
         size_t consumed = 0;
-        uint64_t blockBytes = 0;
         rc = planBlock(f, h.version, src, size, pos, &consumed, h.hasContentCk, h.hasCompressedCk, ckContent,
-                       ckCompressed, 1, produced, &blockBytes, err);
+                       ckCompressed, produced, err);
         if (rc) return rc;
         pos += consumed;
-        produced += blockBytes;
         if (h.version < 21) break;
     }
-    if (produced != h.outSize) { err = "decoded size does not match the frame header"; return E_CORRUPT; }
-    frames[f].decodedSize = h.outSize;
-    frames[f].frameBytes = pos;
+    for (size_t o = 0; o < nbOut; o++)
+        if (produced[o] != h.sizes[o]) { err = "decoded size does not match the frame header"; return E_CORRUPT; }
+    fp.decodedSize = extent;
+    fp.frameBytes = pos;
     return 0;
 }
 
@@ -350,9 +429,10 @@ int DecodePlan::planFrame(int f, const uint8_t* src, size_t size, size_t dstCap,
 // (decompress2.c:1478-1570).
 int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t size, size_t start,
                           size_t* consumed, bool hasContentCk, bool hasCompressedCk, bool ckContent,
-                          bool ckCompressed, size_t nbOutputs, uint64_t outOffset, uint64_t* outBytes,
-                          std::string& err)
+                          bool ckCompressed, std::vector<uint64_t>& produced, std::string& err)
 {
+    FramePlan& fp = frames[f];
+    size_t const nbOutputs = fp.outOffs.size();
     Reader rd{ src + start, src + size };
     uint64_t nd, ns;
     // counts: single bytes before v9, varints after; the decoder count is
@@ -374,6 +454,7 @@ int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t si
     uint64_t const nodeLimit = version < 9 ? 256 : version < 20 ? 10000 : 20000;
     uint64_t const streamLimit = version < 9 ? 256 : version < 16 ? 10000 : 110000;
     if (nd >= nodeLimit || ns >= streamLimit) { err = "graph too large"; return E_LIMIT; }
+    if (nd + ns < nbOutputs) { err = "fewer streams than outputs"; return E_CORRUPT; }
     // before v21 the checksum flags open the block header (decode_frameheader.c:1002-1011)
     if (version < 21) {
         if (rd.p >= rd.end) { err = "truncated block header"; return E_SRC_SMALL; }
@@ -489,7 +570,7 @@ int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t si
             // versions before 21 hash the frame from its first byte, later
             // ones the block only (decompress2.c:1494-1500)
             size_t const hs = version < 21 ? 0 : start;
-            hashes.push_back(PlanHash{ f, false, hs, pos - hs, readLE32(src + pos), E_CK_COMPRESSED, false });
+            hashes.push_back(PlanHash{ f, HW_FRAME, hs, pos - hs, readLE32(src + pos), E_CK_COMPRESSED, false });
         }
         pos += 4;
     }
@@ -761,16 +842,27 @@ int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t si
         }
     }
 
-    // ---- outputs --------------------------------------------------------
-    PlanStream& OUT = S(total - 1);
-    if (OUT.type == 0) { err = "output not regenerated"; return E_CORRUPT; }
-    frames[f].outWidth = OUT.w;
-    frames[f].outType = OUT.type;
-    *outBytes = OUT.bytes();
-    if (OUT.producer < 0 && OUT.bytes()) {
-        // the frame stores its output verbatim: copy it into place
-        directCopies.push_back(PlanCopy{ f, OUT.off, outOffset, OUT.bytes() });
+    // ---- outputs: the last stream slots, output o in slot total - 1 - o --
+    std::vector<uint64_t> const before = produced;
+    for (size_t o = 0; o < nbOutputs; o++) {
+        PlanStream& OUT = S(total - 1 - o);
+        if (OUT.type == 0) { err = "output not regenerated"; return E_CORRUPT; }
+        if (fp.outWidths[o] == 0) {
+            fp.outWidths[o] = OUT.w;
+            fp.outTypes[o] = OUT.type;
+        } else if (fp.outWidths[o] != OUT.w || fp.outTypes[o] != OUT.type) {
+            err = "output type changes between blocks";
+            return E_CORRUPT;
+        }
+        if (produced[o] + OUT.bytes() > fp.outSizes[o]) { err = "output larger than the frame header says"; return E_CORRUPT; }
+        if (OUT.producer < 0 && OUT.bytes()) {
+            // the frame stores the output verbatim: copy it into place
+            directCopies.push_back(PlanCopy{ f, OUT.off, fp.outOffs[o] + produced[o], OUT.bytes() });
+        }
+        produced[o] += OUT.bytes();
     }
+    fp.outWidth = fp.outWidths[0];
+    fp.outType = fp.outTypes[0];
 
     // ---- fusion of numeric chains (delta <- zigzag <- view <- tsplit|bitpack)
     auto isNumView = [&](const PlanNode& nd_) {
@@ -834,9 +926,12 @@ int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t si
     }
 
     // ---- placement (reverse decoder order) ------------------------------
-    OUT.loc = L_OUT;
-    OUT.frame = f;
-    OUT.off = outOffset;
+    for (size_t o = 0; o < nbOutputs; o++) {
+        PlanStream& OUT = S(total - 1 - o);
+        OUT.loc = L_OUT;
+        OUT.frame = f;
+        OUT.off = fp.outOffs[o] + before[o];
+    }
     auto alloc = [&](PlanStream& s) {
         s.loc = L_ARENA;
         s.off = arenaBytes;
@@ -875,8 +970,27 @@ int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t si
         }
     }
     *consumed = pos - start;
-    if (hasContentCk && ckContent)
-        hashes.push_back(PlanHash{ f, true, outOffset, *outBytes, contentCk, 14, false });
+    // content checksum: XXH3 of the block's outputs one after another
+    // (STREAM_hashLastCommit_xxh3low32, src/openzl/common/stream.c:727-773)
+    if (hasContentCk && ckContent) {
+        if (nbOutputs == 1) {
+            hashes.push_back(PlanHash{ f, HW_OUTPUT, before[0], produced[0] - before[0], contentCk, 14, false });
+        } else {
+            uint64_t const base = arenaBytes, total = [&] {
+                uint64_t t = 0;
+                for (size_t o = 0; o < nbOutputs; o++) t += produced[o] - before[o];
+                return t;
+            }();
+            arenaBytes += (total + 63) & ~uint64_t(63);
+            uint64_t at = base;
+            for (size_t o = 0; o < nbOutputs; o++) {
+                uint64_t const b = produced[o] - before[o];
+                if (b) gathers.push_back(PlanGather{ f, fp.outOffs[o] + before[o], at, b });
+                at += b;
+            }
+            hashes.push_back(PlanHash{ f, HW_ARENA, base, total, contentCk, 14, false });
+        }
+    }
     return 0;
 }
 
@@ -1026,6 +1140,12 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         maxLevel = std::max(maxLevel, lv);
     }
     if (!plan.directCopies.empty()) maxLevel = std::max(maxLevel, 1);
+    // multi-output blocks gather their outputs for the content checksum after
+    // everything that writes them
+    bool anyGather = false;
+    for (const PlanGather& g : plan.gathers) anyGather |= inPart(g.frame);
+    int const gatherLevel = maxLevel + 1;
+    if (anyGather) maxLevel = gatherLevel;
     int const hashLevel = maxLevel + 1;
 
     // ---- tasks per level ---------------------------------------------------
@@ -1041,6 +1161,11 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         if (!inPart(c.frame)) continue;
         CopyTask t{ dOuts[c.frame] + c.outOff, dFrames[c.frame] + c.frameOff, c.bytes, 0 };
         B[1].copy.push_back(t);
+    }
+    for (const PlanGather& g : plan.gathers) {
+        if (!inPart(g.frame)) continue;
+        CopyTask t{ dArena + g.arenaOff, dOuts[g.frame] + g.outOff, g.bytes, 0 };
+        B[gatherLevel].copy.push_back(t);
     }
     // pointer arrays (planes) live in the pool; collect them first
     std::vector<const uint8_t*> ptrs;
@@ -1256,7 +1381,9 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         for (const PlanHash& h : plan.hashes) {
             if (!inPart(h.frame)) continue;
             HashTask t{};
-            t.data = h.inOutput ? dOuts[h.frame] + h.off : dFrames[h.frame] + h.off;
+            t.data = h.where == HW_OUTPUT ? dOuts[h.frame] + h.off
+                   : h.where == HW_ARENA  ? dArena + h.off
+                                          : dFrames[h.frame] + h.off;
             t.len = h.len;
             t.expected = h.expected;
             t.errCode = h.err;

@@ -70,9 +70,11 @@ struct PlanNode {
     uint64_t paramOff = 0;    // FSE: normalized counts in the parameter block
 };
 
+enum HashWhere : uint8_t { HW_FRAME = 0, HW_OUTPUT = 1, HW_ARENA = 2 };
+
 struct PlanHash {
     int frame;
-    bool inOutput;      // content checksum (output region) vs compressed (frame region)
+    uint8_t where;      // HW_*: the frame (compressed), its output (content), the arena (gathered outputs)
     uint64_t off, len;
     uint32_t expected;
     uint32_t err;
@@ -85,30 +87,46 @@ struct PlanCopy {
     uint64_t frameOff, outOff, bytes;
 };
 
+// One output's block gathered into the arena, so that the content checksum
+// of a multi-output block hashes contiguous bytes.
+struct PlanGather {
+    int frame;
+    uint64_t outOff, arenaOff, bytes;
+};
+
 struct FramePlan {
-    uint64_t decodedSize = 0;
-    uint64_t frameBytes = 0;  // compressed size, with the end-of-frame byte (v21+)
-    int outType = 0;
+    uint64_t decodedSize = 0;  // destination bytes: every output, each at a 16-byte-aligned offset
+    uint64_t frameBytes = 0;   // compressed size, with the end-of-frame byte (v21+)
+    int outType = 0;           // output 0
     uint32_t outWidth = 1;
+    std::vector<uint64_t> outOffs, outSizes; // per output: offset in the destination, bytes
+    std::vector<int> outTypes;
+    std::vector<uint32_t> outWidths;
 };
 
 // Frame-header fields shared by the planner and the frame-information calls.
-// Format versions 8..23; single-output frames only.
 struct FrameHeader {
     unsigned version = 0;
     bool hasContentCk = false;    // v21+; older frames carry the flags per block
     bool hasCompressedCk = false;
-    int outType = 0;              // TY_* of the one output
-    uint64_t outSize = 0;         // its decompressed size in bytes
+    std::vector<int> types;       // TY_* per output
+    std::vector<uint64_t> sizes;  // decompressed bytes per output
+    int outType = 0;              // output 0
+    uint64_t outSize = 0;
     size_t end = 0;               // first byte after the header
     bool hdrCk = false;           // v21+: header checksum byte at end - 1
 };
 
 // Parses the frame header (src/openzl/decompress/decode_frameheader.c:58-190,
-// 270-370). Returns 0 or a ZL error code: formatVersion_unsupported (60),
-// srcSize_tooSmall (3), invalidRequest_singleOutputFrameOnly (23),
-// temporaryLibraryLimitation (81) for unknown sizes, corruption (12).
+// 270-370). Format versions 8..23, up to 2048 outputs, no string outputs.
+// Returns 0 or a ZL error code: formatVersion_unsupported (60),
+// srcSize_tooSmall (3), temporaryLibraryLimitation (81) for unknown sizes or
+// string outputs, corruption (12).
 int parseFrameHeader(const uint8_t* src, size_t size, FrameHeader& h, std::string& err);
+
+// Where the batch API writes a frame's outputs in its destination: one after
+// another, each at a 16-byte-aligned offset. Returns the bytes needed.
+uint64_t frameOutputLayout(const FrameHeader& h, std::vector<uint64_t>& offsets);
 
 class DecodePlan {
   public:
@@ -122,6 +140,7 @@ class DecodePlan {
     std::vector<PlanNode> nodes;
     std::vector<PlanHash> hashes;
     std::vector<PlanCopy> directCopies;
+    std::vector<PlanGather> gathers;
     std::vector<uint8_t> params;  // host-decoded small streams (FSE normalized counts)
     uint64_t arenaBytes = 0;
     uint64_t totalOut = 0;
@@ -129,9 +148,10 @@ class DecodePlan {
   private:
     int planFrame(int f, const uint8_t* src, size_t size, size_t dstCap, bool ckContent,
                   bool ckCompressed, std::string& err);
+    // `produced` holds each output's bytes so far; the block adds its own
     int planBlock(int f, unsigned version, const uint8_t* src, size_t size, size_t start, size_t* consumed,
                   bool hasContentCk, bool hasCompressedCk, bool ckContent, bool ckCompressed,
-                  size_t nbOutputs, uint64_t outOffset, uint64_t* outBytes, std::string& err);
+                  std::vector<uint64_t>& produced, std::string& err);
 };
 
 // Resolved, device-ready plan: task pools and launch list.

@@ -44,6 +44,11 @@ def lib():
         l.ozo_tokenize.restype = ctypes.c_int64
         l.ozo_tokenize.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        l.ozo_decompress_multi.restype = ctypes.c_int64
+        l.ozo_decompress_multi.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        l.ozo_free.restype = None
+        l.ozo_free.argtypes = [ctypes.c_void_p]
         l.ozo_xxh3_64.restype = ctypes.c_uint64
         l.ozo_xxh3_64.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
         _lib = l
@@ -62,6 +67,24 @@ def decompress(frame):
     if r < 0:
         raise ValueError("oracle: decode failed (%d)" % r)
     return out[:r], t.value, w.value
+
+
+def decompress_multi(frame, max_outputs=64):
+    """Returns [(bytes as uint8 array, type, elt_width)] per output; raises on error."""
+    f = np.frombuffer(bytes(frame), np.uint8) if not isinstance(frame, np.ndarray) else frame.view(np.uint8)
+    outs = (ctypes.c_void_p * max_outputs)()
+    lens = (ctypes.c_size_t * max_outputs)()
+    types = (ctypes.c_int * max_outputs)()
+    widths = (ctypes.c_int * max_outputs)()
+    n = lib().ozo_decompress_multi(f.ctypes.data, f.size, max_outputs, outs, lens, types, widths)
+    if n < 0:
+        raise ValueError("oracle: decode failed (%d)" % n)
+    res = []
+    for o in range(n):
+        buf = (ctypes.c_uint8 * max(lens[o], 1)).from_address(outs[o])
+        res.append((np.frombuffer(buf, np.uint8)[:lens[o]].copy(), types[o], widths[o]))
+        lib().ozo_free(outs[o])
+    return res
 
 
 def compress(recipe, arr, elt_width, checksums=True):

@@ -816,12 +816,14 @@ static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, s
  * (src/openzl/decompress/decode_frameheader.c:237-340, 938-1171;
  * src/openzl/decompress/decompress2.c:632-834, 1046-1290, 1442-1570).
  * ------------------------------------------------------------------- */
+#define OZO_MAX_OUTPUTS 64
+
 typedef struct {
     unsigned version;
     int hasContentCk, hasCompressedCk;
     size_t nbOutputs;
-    int types[16];
-    uint64_t sizes[16];
+    int types[OZO_MAX_OUTPUTS];
+    uint64_t sizes[OZO_MAX_OUTPUTS];
     size_t headerSize;
 } FrameHdr;
 
@@ -858,7 +860,7 @@ static int64_t parse_frame_header_v20(FrameHdr* fh, const uint8_t* src, size_t s
     } else if (v == 14) {
         pos++; /* the type byte */
     }
-    if (nbOut > 14) return -OZO_ERR_UNSUPPORTED;
+    if (nbOut > OZO_MAX_OUTPUTS) return -OZO_ERR_UNSUPPORTED;
     fh->nbOutputs = nbOut;
     if (v < 14) {
         fh->types[0] = OZO_TYPE_SERIAL;
@@ -902,16 +904,26 @@ static int64_t parse_frame_header(FrameHdr* fh, const uint8_t* src, size_t size)
     fh->hasContentCk = flags & 1;
     fh->hasCompressedCk = (flags >> 1) & 1;
     int const hasComment = (flags >> 2) & 1;
+    /* output count and types (decode_frameheader.c:94-107, 148-173): up to
+     * 14 outputs in the low nibble with the first two types above it, else
+     * an extension byte and all types in the following bytes */
     uint8_t const t1 = src[pos++];
     size_t nbOut = t1 & 15;
-    if (nbOut == 15) return -OZO_ERR_UNSUPPORTED;
-    if (nbOut == 0 || nbOut > 14) return -OZO_ERR_UNSUPPORTED;
+    size_t done = 0;
+    if (nbOut == 15) {
+        if (pos >= size) return -OZO_ERR_SRC_SIZE;
+        nbOut = ((size_t)src[pos++] << 4) + (t1 >> 4) + 15;
+    } else {
+        for (size_t n = 0; n < nbOut && n < 2; n++) fh->types[n] = decode_type(t1 >> (4 + 2 * n));
+        done = 2;
+    }
+    if (nbOut == 0) return -OZO_ERR_UNSUPPORTED;
+    if (nbOut > OZO_MAX_OUTPUTS) return -OZO_ERR_UNSUPPORTED;
     fh->nbOutputs = nbOut;
-    for (size_t n = 0; n < nbOut && n < 2; n++) fh->types[n] = decode_type(t1 >> (4 + 2 * n));
-    if (nbOut > 2) {
+    if (nbOut > done) {
         uint8_t tok = 0;
-        for (size_t n = 2; n < nbOut; n++) {
-            size_t const sh = ((n - 2) % 4) * 2;
+        for (size_t n = done; n < nbOut; n++) {
+            size_t const sh = ((n - done) % 4) * 2;
             if (sh == 0) {
                 if (pos >= size) return -OZO_ERR_SRC_SIZE;
                 tok = src[pos++];
@@ -1242,6 +1254,51 @@ int64_t ozo_decompress(const void* srcv, size_t size, void* dst, size_t dstCap, 
     if (outEltWidth) *outEltWidth = (int)(ws[0] ? ws[0] : 1);
     return (int64_t)lens[0];
 }
+
+/* Decodes a frame of any number of outputs (ZL_DCtx_decompressMultiTBuffer,
+ * decompress2.c:1590-1760). outs[o] receives a malloc'ed buffer (release it
+ * with ozo_free), lens/types/widths its size, type and element width.
+ * Returns the number of outputs, or a negative error. */
+int64_t ozo_decompress_multi(const void* srcv, size_t size, size_t maxOut, void** outs, size_t* lens, int* types,
+                             int* widths)
+{
+    const uint8_t* src = (const uint8_t*)srcv;
+    FrameHdr fh;
+    int64_t r = parse_frame_header(&fh, src, size);
+    if (r < 0) return r;
+    if (fh.nbOutputs > maxOut) return -OZO_ERR_DST_SIZE;
+    size_t const no = fh.nbOutputs;
+    uint8_t* bufs[OZO_MAX_OUTPUTS] = { NULL };
+    size_t ln[OZO_MAX_OUTPUTS] = { 0 }, ws[OZO_MAX_OUTPUTS] = { 0 };
+    int ts[OZO_MAX_OUTPUTS] = { 0 };
+    size_t pos = (size_t)r;
+    int64_t ret = (int64_t)no;
+    for (;;) {
+        if (fh.version >= 21) {
+            if (pos >= size) { ret = -OZO_ERR_SRC_SIZE; break; }
+            if (src[pos] == 0) { pos++; break; }
+        }
+        int64_t b = decode_block(&fh, src, size, pos, bufs, ln, ts, ws);
+        if (b < 0) { ret = b; break; }
+        pos += (size_t)b;
+        if (fh.version < 21) break;
+    }
+    for (size_t o = 0; o < no && ret >= 0; o++)
+        if (ln[o] != fh.sizes[o]) ret = -OZO_ERR_CORRUPTION;
+    for (size_t o = 0; o < no; o++) {
+        if (ret < 0) {
+            free(bufs[o]);
+            continue;
+        }
+        outs[o] = bufs[o] ? bufs[o] : malloc(1);
+        lens[o] = ln[o];
+        types[o] = ts[o] ? ts[o] : fh.types[o];
+        widths[o] = (int)(ws[o] ? ws[o] : 1);
+    }
+    return ret;
+}
+
+void ozo_free(void* p) { free(p); }
 
 /* Test entry point: runs one decoder on caller streams (codec-level known
  * answers). Inputs are given in the decoder's own order. */

@@ -144,6 +144,66 @@ int64_t ref_compress(int recipe, const void* src, size_t nbElts, int eltWidth,
     return ret;
 }
 
+/* Multi-input frames: a function graph sends input i to the graph of
+ * recipe i, each registered as one of its custom graphs. */
+static ZL_Report multi_graph(ZL_Graph* g, ZL_Edge* inputs[], size_t nbInputs)
+{
+    ZL_GraphIDList const cg = ZL_Graph_getCustomGraphs(g);
+    if (cg.nbGraphIDs < nbInputs) return ZL_returnError(ZL_ErrorCode_graph_invalid);
+    for (size_t i = 0; i < nbInputs; i++) {
+        ZL_Report const r = ZL_Edge_setDestination(inputs[i], cg.graphids[i]);
+        if (ZL_isError(r)) return r;
+    }
+    return ZL_returnSuccess();
+}
+
+/* nb inputs (eltWidths[i] 0 => serial), compressed together into one frame
+ * whose outputs come back in input order. Returns the frame size or
+ * -(error code). */
+int64_t ref_compress_multi(int nb, const int* recipes, const void* const* srcs, const size_t* nbElts,
+                           const int* eltWidths, void* dst, size_t dstCap, int checksums, int formatVersion)
+{
+    if (nb <= 0 || nb > 64) return -1;
+    ZL_Compressor* c = ZL_Compressor_create();
+    if (!c) return -1;
+    if (formatVersion <= 0) formatVersion = ZL_MAX_FORMAT_VERSION;
+    ZL_Compressor_setParameter(c, ZL_CParam_formatVersion, formatVersion);
+    if (!checksums) {
+        ZL_Compressor_setParameter(c, ZL_CParam_contentChecksum, ZL_TernaryParam_disable);
+        ZL_Compressor_setParameter(c, ZL_CParam_compressedChecksum, ZL_TernaryParam_disable);
+    }
+    ZL_GraphID gids[64];
+    ZL_Type masks[64];
+    for (int i = 0; i < nb; i++) {
+        gids[i] = build(c, recipes[i], eltWidths[i]);
+        if (!ZL_GraphID_isValid(gids[i])) { ZL_Compressor_free(c); return -2; }
+        masks[i] = ZL_Type_serial | ZL_Type_numeric | ZL_Type_struct;
+    }
+    ZL_FunctionGraphDesc const d = {
+        .name = "per_input",
+        .graph_f = multi_graph,
+        .inputTypeMasks = masks,
+        .nbInputs = (size_t)nb,
+        .customGraphs = gids,
+        .nbCustomGraphs = (size_t)nb,
+    };
+    ZL_GraphID const g = ZL_Compressor_registerFunctionGraph(c, &d);
+    ZL_Report r = ZL_Compressor_selectStartingGraphID(c, g);
+    if (ZL_isError(r)) { ZL_Compressor_free(c); return -3; }
+    ZL_CCtx* cc = ZL_CCtx_create();
+    ZL_CCtx_refCompressor(cc, c);
+    ZL_TypedRef* trs[64];
+    for (int i = 0; i < nb; i++)
+        trs[i] = eltWidths[i] == 0 ? ZL_TypedRef_createSerial(srcs[i], nbElts[i])
+                                   : ZL_TypedRef_createNumeric(srcs[i], (size_t)eltWidths[i], nbElts[i]);
+    r = ZL_CCtx_compressMultiTypedRef(cc, dst, dstCap, (const ZL_TypedRef**)trs, (size_t)nb);
+    int64_t ret = ZL_isError(r) ? -(int64_t)ZL_errorCode(r) - 1000 : (int64_t)ZL_validResult(r);
+    for (int i = 0; i < nb; i++) ZL_TypedRef_free(trs[i]);
+    ZL_CCtx_free(cc);
+    ZL_Compressor_free(c);
+    return ret;
+}
+
 /* Decodes one single-output frame into dst. Writes the output's element
  * width (1 for serial) and type. Returns the decoded byte count or -(code). */
 int64_t ref_decompress(const void* src, size_t srcSize, void* dst, size_t dstCap,

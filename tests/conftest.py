@@ -20,6 +20,13 @@ def manifest():
         return json.load(f)
 
 
+@pytest.fixture(scope="session")
+def manifest_multi():
+    """Frames of several outputs, one input hash per output."""
+    with open(os.path.join(GOLDEN, "manifest_multi.json")) as f:
+        return json.load(f)
+
+
 def read_frame(case):
     with open(os.path.join(GOLDEN, case + ".zl"), "rb") as f:
         return f.read()

@@ -111,6 +111,67 @@ def build_cases():
     return c
 
 
+def build_multi_cases():
+    """Frames of several inputs (ZL_CCtx_compressMultiTypedRef), each input
+    through its own recipe graph; decode-only. (name, [(recipe, array,
+    elt_width)], format version)."""
+    rng = np.random.default_rng(20261204)
+    c = []
+    c.append(("multi2_fse_num_huf_serial", [(1, walk(rng, 20000, np.uint32, 100), 4),
+                                            (8, (rng.zipf(1.3, 15000) % 256).astype(np.uint8), 0)], 0))
+    c.append(("multi3_ts_delta_flatpack", [(2, timestamps(rng, 5000), 8), (9, walk(rng, 3000, np.uint16, 50), 2),
+                                           (14, rng.integers(0, 37, 4000).astype(np.uint8), 0)], 0))
+    c.append(("multi5_small_inputs", [(0, rng.integers(0, 256, 3).astype(np.uint8), 0),
+                                      (10, walk(rng, 2, np.uint32, 9), 4),
+                                      (7, (rng.zipf(1.3, 2000) % 40).astype(np.uint8), 0),
+                                      (12, walk(rng, 700, np.uint64, 30), 8),
+                                      (13, np.full(900, 5, np.uint8), 0)], 0))
+    c.append(("multi16_extended_count", [(9 if k % 2 else 4, walk(rng, 500 + 37 * k, np.uint32, 60), 4)
+                                         for k in range(16)], 0))
+    c.append(("multi3_v20", [(1, walk(rng, 9000, np.uint16, 300), 2), (8, (rng.zipf(1.2, 6000) % 200).astype(np.uint8), 0),
+                             (11, walk(rng, 1000, np.uint32, 40, start=900), 4)], 20))
+    c.append(("multi4_huf16_entropy", [(8, (rng.zipf(1.3, 30000) % 3000).astype(np.uint16), 2),
+                                       (17, np.minimum(rng.geometric(0.2, 20000), 255).astype(np.uint8), 0),
+                                       (3, walk(rng, 40000, np.uint8, 3), 1),
+                                       (5, rng.integers(0, 2**31, 500).astype(np.int32)[(rng.zipf(1.1, 9000) - 1) % 500], 4)],
+                0))
+    return c
+
+
+def make_multi(lib):
+    f = lib.ref_compress_multi
+    f.restype = ctypes.c_int64
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    manifest = []
+    for name, inputs, version in build_multi_cases():
+        arrs = [np.ascontiguousarray(a) for _, a, _ in inputs]
+        nb = len(inputs)
+        for cs in (1, 0):
+            rec = (ctypes.c_int * nb)(*[r for r, _, _ in inputs])
+            srcs = (ctypes.c_void_p * nb)(*[a.ctypes.data for a in arrs])
+            ns = (ctypes.c_size_t * nb)(*[a.size if w else a.nbytes for (_, _, w), a in zip(inputs, arrs)])
+            ws = (ctypes.c_int * nb)(*[w for _, _, w in inputs])
+            cap = sum(a.nbytes for a in arrs) * 2 + 8192 * nb
+            dst = np.zeros(cap, np.uint8)
+            r = f(nb, rec, srcs, ns, ws, dst.ctypes.data, cap, cs, version)
+            if r <= 0:
+                print("skip", name, cs, r)
+                continue
+            case = name + ("" if cs else "_nock")
+            with open(os.path.join(HERE, case + ".zl"), "wb") as fh:
+                fh.write(dst[:r].tobytes())
+            manifest.append({"case": case, "checksums": cs, "frame_bytes": int(r),
+                             "sha256_frame": hashlib.sha256(dst[:r].tobytes()).hexdigest(),
+                             **({"format_version": version} if version else {}),
+                             "outputs": [{"recipe": rr, "elt_width": w, "n": int(a.size),
+                                          "sha256": hashlib.sha256(a.tobytes()).hexdigest()}
+                                         for (rr, _, w), a in zip(inputs, arrs)]})
+    with open(os.path.join(HERE, "manifest_multi.json"), "w") as fh:
+        json.dump(manifest, fh, indent=1)
+    return manifest
+
+
 def main():
     subprocess.check_call(["make", "-s", "-f", "oracle/ref.mk", "-j8"], cwd=ROOT)
     lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "ref_driver.so"))
@@ -145,6 +206,8 @@ def main():
                              **({"format_version": version} if version else {})})
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
+    multi = make_multi(lib)
+    print(len(multi), "multi-output cases")
     tot = sum(os.path.getsize(os.path.join(HERE, m["case"] + ".zl")) for m in manifest)
     print(len(manifest), "cases,", tot, "bytes")
 

@@ -142,3 +142,36 @@ def test_compress_api_errors_before_any_device_work(lib):
     # unknown successor graphs are rejected at registration
     assert comp.node(api.NODE_DELTA_INT, 12345) == api.GRAPH_ILLEGAL
     assert lib.ZL_compressBound(1000) == 2 * 1000 + 520
+
+
+def test_frame_info_and_layout_of_multi_output_frames(lib, manifest_multi):
+    """ZL_FrameInfo over frames of several outputs (count, types, sizes; an
+    output ID past the last is outputID_invalid), ZL_getDecompressedSize
+    refusing them like the reference, and ozl_frame_outputs' layout: outputs
+    one after another at 16-byte-aligned offsets, with their element widths."""
+    import openzl_gb300 as oz
+
+    for m in manifest_multi:
+        fr = read_frame(m["case"])
+        fi = oz.FrameInfo(fr)
+        outs = m["outputs"]
+        assert fi.num_outputs() == len(outs)
+        assert fi.format_version() == m.get("format_version", 23)
+        for i, o in enumerate(outs):
+            w = o["elt_width"] or 1
+            assert fi.decompressed_size(i) == o["n"] * w, (m["case"], i)
+            assert fi.output_type(i) == (1 if o["elt_width"] == 0 else 4), (m["case"], i)
+        with pytest.raises(oz.ZLError) as e:
+            fi.output_type(len(outs))
+        assert e.value.code == 22
+        with pytest.raises(oz.ZLError) as e:
+            oz.get_decompressed_size(fr)
+        assert e.value.code == 23
+        assert oz.get_compressed_size(fr) == len(fr)
+        lay = oz.frame_outputs(fr)
+        end = 0
+        for o, l in zip(outs, lay):
+            assert l["offset"] % 16 == 0 and l["offset"] >= end
+            assert l["size"] == o["n"] * (o["elt_width"] or 1)
+            assert l["width"] == (o["elt_width"] or 1)
+            end = l["offset"] + l["size"]

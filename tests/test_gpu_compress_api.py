@@ -205,9 +205,11 @@ def test_typed_buffers(gpu_lib):
     r = lib.ZL_DCtx_decompressTBuffer(d._h, tb, f.ctypes.data, f.size)
     assert r.code != 0
     lib.ZL_TypedBuffer_free(tb)
-    # multi-output entry point with one output
+    # multi-output entry point with one output: returns the number of
+    # buffers filled (zl_decompress.h:511-526)
     tb = lib.ZL_TypedBuffer_create()
     arrp = (ctypes.c_void_p * 1)(tb)
     r = lib.ZL_DCtx_decompressMultiTBuffer(d._h, arrp, 1, f.ctypes.data, f.size)
-    assert r.code == 0 and r.value == arr.nbytes
+    assert r.code == 0 and r.value == 1
+    assert lib.ZL_TypedBuffer_byteSize(tb) == arr.nbytes and lib.ZL_TypedBuffer_eltWidth(tb) == 2
     lib.ZL_TypedBuffer_free(tb)

@@ -257,3 +257,71 @@ def test_older_format_versions_on_the_gpu(gpu_lib, manifest):
     with pytest.raises(oz.ZLError) as e:
         oz.DCtx().decompress(bytes(fr))
     assert e.value.code in (12, 13, 14)
+
+
+def test_multi_output_frames(gpu_lib, manifest, manifest_multi):
+    """Frames of several outputs: ZL_DCtx_decompressMultiTBuffer returns each
+    output with its type and width; the batch API, mixed with single-output
+    frames, writes each output at the offset ozl_frame_outputs gives (content
+    checksums over the gathered outputs verified on the device); a corrupted
+    frame and a wrong output count are reported."""
+    import torch
+    import openzl_gb300 as oz
+
+    d = oz.DCtx()
+    for m in manifest_multi:
+        outs = d.decompress_multi(read_frame(m["case"]))
+        assert len(outs) == len(m["outputs"]), m["case"]
+        for (data, t, w), o in zip(outs, m["outputs"]):
+            assert hashlib.sha256(data.tobytes()).hexdigest() == o["sha256"], m["case"]
+            assert w == (o["elt_width"] or 1) and t == (1 if o["elt_width"] == 0 else 4), m["case"]
+    singles = manifest[:8]
+    frames = [read_frame(m["case"]) for m in manifest_multi] + [read_frame(m["case"]) for m in singles]
+    layouts = [oz.frame_outputs(f) for f in frames]
+    extents = [l[-1]["offset"] + l[-1]["size"] for l in layouts]
+    dfr = [_dev(torch, f) for f in frames]
+    outs = [torch.full((max(e, 1) + 64,), 0xAB, dtype=torch.uint8, device="cuda") for e in extents]
+    s = torch.cuda.Stream()
+    b = oz.GpuBatch()
+    total = b.plan(frames, [x.data_ptr() for x in dfr], [o.data_ptr() for o in outs], extents)
+    assert total == sum(extents)
+    torch.cuda.synchronize()
+    for graph in (False, True):
+        b.run(s.cuda_stream, graph=graph)
+        b.check(s.cuda_stream)
+        for k, (lay, o) in enumerate(zip(layouts, outs)):
+            host = o.cpu().numpy()
+            want = manifest_multi[k]["outputs"] if k < len(manifest_multi) else [
+                {"sha256": singles[k - len(manifest_multi)]["sha256_in"]}]
+            for l, w in zip(lay, want):
+                got = host[l["offset"]:l["offset"] + l["size"]].tobytes()
+                assert hashlib.sha256(got).hexdigest() == w["sha256"], (k, graph)
+    m = next(m for m in manifest_multi if m["case"] == "multi3_ts_delta_flatpack")
+    bad = bytearray(read_frame(m["case"]))
+    bad[len(bad) // 2] ^= 0x01
+    with pytest.raises(oz.ZLError):
+        d.decompress_multi(bytes(bad))
+    # the content checksum of a multi-output block covers its gathered
+    # outputs: flip a byte of it and decode without the compressed checksum
+    # (which covers the content checksum too)
+    fr = read_frame("multi3_ts_delta_flatpack")
+    bad = bytes(fr[:-6]) + bytes([fr[-6] ^ 0x10]) + bytes(fr[-5:])  # content, compressed checksums, end marker
+    lay = oz.frame_outputs(fr)
+    ext = lay[-1]["offset"] + lay[-1]["size"]
+    dbad = _dev(torch, bad)
+    o = torch.zeros(ext + 64, dtype=torch.uint8, device="cuda")
+    bb = oz.GpuBatch(check_compressed=False)
+    bb.plan([bad], [dbad.data_ptr()], [o.data_ptr()], [ext])
+    torch.cuda.synchronize()
+    bb.run(s.cuda_stream, graph=False)
+    with pytest.raises(oz.ZLError) as e:
+        bb.check(s.cuda_stream)
+    assert e.value.code == 14
+    fr = read_frame("multi5_small_inputs")
+    import ctypes
+    lib = oz.library()
+    arr = (ctypes.c_void_p * 1)(lib.ZL_TypedBuffer_create())
+    f = np.frombuffer(fr, np.uint8)
+    rep = lib.ZL_DCtx_decompressMultiTBuffer(d._h, arr, 1, f.ctypes.data, f.size)
+    lib.ZL_TypedBuffer_free(arr[0])
+    assert rep.code == 8

@@ -44,6 +44,60 @@ def test_oracle_older_format_versions(manifest):
         oracle.decompress(bytes(fr))
 
 
+def test_oracle_decodes_multi_output_frames(manifest_multi):
+    """Frames of several outputs (output o in stream slot total-1-o of each
+    block, the content checksum over the block's outputs one after another)."""
+    assert any(len(m["outputs"]) > 14 for m in manifest_multi)  # extended output count
+    for m in manifest_multi:
+        outs = oracle.decompress_multi(read_frame(m["case"]))
+        assert len(outs) == len(m["outputs"]), m["case"]
+        for (data, t, w), o in zip(outs, m["outputs"]):
+            assert hashlib.sha256(data.tobytes()).hexdigest() == o["sha256"], m["case"]
+            assert w == (o["elt_width"] or 1) and t == (1 if o["elt_width"] == 0 else 4), m["case"]
+    m = next(m for m in manifest_multi if m["case"] == "multi3_ts_delta_flatpack")
+    fr = bytearray(read_frame(m["case"]))
+    fr[len(fr) // 2] ^= 0x40
+    with pytest.raises(ValueError):
+        oracle.decompress_multi(bytes(fr))
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
+def test_oracle_matches_reference_on_multi_input_frames():
+    """Seeded multi-input frames (1 to 40 inputs, mixed recipes, format
+    versions 15 to 23, with and without checksums) decode in the oracle."""
+    import ctypes
+
+    ref = ctypes.CDLL(REF_DRIVER)
+    f = ref.ref_compress_multi
+    f.restype = ctypes.c_int64
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(9)
+
+    def spec():
+        k = int(rng.integers(0, 6))
+        n = int(rng.choice([1, 5, 300, 5000, 40000]))
+        walk = (1000 + np.cumsum(rng.integers(-50, 51, n)))
+        return [(1, walk.astype(np.uint32), 4), (2, (1000 + np.cumsum(rng.integers(0, 900, n))).astype(np.uint64), 8),
+                (8, (rng.zipf(1.3, n) % 256).astype(np.uint8), 0), (7, (rng.zipf(1.3, n) % 40).astype(np.uint8), 0),
+                (9, walk.astype(np.uint16), 2), (0, rng.integers(0, 256, n).astype(np.uint8), 0)][k]
+
+    for trial in range(30):
+        nb = int(rng.choice([1, 2, 3, 5, 14, 15, 16, 20, 40]))
+        specs = [spec() for _ in range(nb)]
+        v = int(rng.choice([15, 16, 20, 21, 22, 23]))
+        cs = int(rng.integers(0, 2))
+        arrs = [np.ascontiguousarray(a) for _, a, _ in specs]
+        cap = sum(a.nbytes for a in arrs) * 2 + 8192 * nb
+        dst = np.zeros(cap, np.uint8)
+        r = f(nb, (ctypes.c_int * nb)(*[s[0] for s in specs]), (ctypes.c_void_p * nb)(*[a.ctypes.data for a in arrs]),
+              (ctypes.c_size_t * nb)(*[a.size if w else a.nbytes for (_, _, w), a in zip(specs, arrs)]),
+              (ctypes.c_int * nb)(*[s[2] for s in specs]), dst.ctypes.data, cap, cs, v)
+        assert r > 0, (trial, r)
+        outs = oracle.decompress_multi(dst[:r].tobytes())
+        assert [o.tobytes() for o, _, _ in outs] == [a.tobytes() for a in arrs], (trial, nb, v, cs)
+
+
 @pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
 def test_oracle_matches_reference_at_older_format_versions():
     """Seeded inputs compressed by the reference at every format version from

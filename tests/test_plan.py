@@ -33,3 +33,11 @@ def test_fused_pipeline_shape(checker):
     assert "np n=262144 w=4 mode=1 zz=1 delta=1" in out
     kinds = [l.split()[1] for l in out.splitlines() if l.strip().startswith("launch")]
     assert kinds == ["kind=1", "kind=2", "kind=8", "kind=9"], kinds
+
+
+def test_multi_output_layouts_in_bounds(checker, manifest_multi):
+    """Frames of several outputs: each output and, for the content checksum,
+    each gathered block lie inside their allocations."""
+    for m in manifest_multi:
+        r = subprocess.run([checker, os.path.join(GOLDEN, m["case"] + ".zl")], capture_output=True, text=True)
+        assert r.returncode == 0 and "bad=0" in r.stdout, (m["case"], r.stdout[-2000:], r.stderr[-2000:])
