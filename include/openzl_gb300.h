@@ -138,6 +138,8 @@ size_t ZL_TypedBuffer_byteSize(const ZL_TypedBuffer* tbuffer);
 const void* ZL_TypedBuffer_rPtr(const ZL_TypedBuffer* tbuffer);
 size_t ZL_TypedBuffer_numElts(const ZL_TypedBuffer* tbuffer);
 size_t ZL_TypedBuffer_eltWidth(const ZL_TypedBuffer* tbuffer);
+/* zl_decompress.h:590-599: a string output's lengths, numElts of them */
+const uint32_t* ZL_TypedBuffer_rStringLens(const ZL_TypedBuffer* tbuffer);
 /* zl_decompress.h:505 */
 ZL_Report ZL_DCtx_decompressTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* output, const void* compressed, size_t cSize);
 /* zl_decompress.h:527: nbOutputs must equal the frame's output count
@@ -277,10 +279,14 @@ void ozl_gpu_batch_free(OZL_GpuBatch* b);
  * reference; its ZL_FrameInfo gives counts, types and sizes but not element
  * widths, which sit in the block headers). Plans the frame on the host and
  * writes, for the first `capacity` outputs, the offset in the destination,
- * the size in bytes, the type and the element width. Returns the number of
- * outputs; the destination needs offsets[n-1] + sizes[n-1] bytes. */
+ * the size in bytes (a string output: its content), the type, the element
+ * width (1 for serial and string outputs), the number of elements (strings
+ * for a string output) and, for a string output, the offset of its 4-byte
+ * lengths (0 otherwise); any array may be NULL. Returns the number of
+ * outputs and writes the destination bytes needed to *extent. */
 ZL_Report ozl_frame_outputs(const void* frame, size_t frameSize, size_t capacity, uint64_t* offsets,
-                            uint64_t* sizes, int* types, uint32_t* widths);
+                            uint64_t* sizes, int* types, uint32_t* widths, uint64_t* counts,
+                            uint64_t* lensOffsets, uint64_t* extent);
 /* Sets a DParam for subsequent plans (same meaning as ZL_DCtx_setParameter). */
 ZL_Report ozl_gpu_batch_setParameter(OZL_GpuBatch* b, ZL_DParam param, int value);
 /* Plans the decode of nbFrames frames. h_frames[i]: host copy (planning);

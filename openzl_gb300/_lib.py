@@ -48,7 +48,8 @@ def library():
     sig = {
         "ZL_getDecompressedSize": ([vp, sz], ZLReport),
         "ZL_getCompressedSize": ([vp, sz], ZLReport),
-        "ozl_frame_outputs": ([vp, sz, sz, vp, vp, vp, vp], ZLReport),
+        "ozl_frame_outputs": ([vp, sz, sz, vp, vp, vp, vp, vp, vp, vp], ZLReport),
+        "ZL_TypedBuffer_rStringLens": ([vp], vp),
         "ZL_DCtx_create": ([], vp),
         "ZL_DCtx_free": ([vp], None),
         "ZL_DCtx_setParameter": ([vp, ctypes.c_int, ctypes.c_int], ZLReport),
@@ -157,15 +158,22 @@ def get_compressed_size(frame):
 
 def frame_outputs(frame):
     """ozl_frame_outputs: per output its offset in a batch destination, size
-    in bytes, ZL_Type value and element width, as a list of dicts."""
+    in bytes (strings: content), ZL_Type value, element width, element count
+    and (strings) the offset of the 4-byte lengths, as a list of dicts, and
+    the destination bytes needed."""
     f = _as_u8(frame)
-    n = _check(library().ozl_frame_outputs(f.ctypes.data, f.size, 0, None, None, None, None))
+    n = _check(library().ozl_frame_outputs(f.ctypes.data, f.size, 0, None, None, None, None, None, None, None))
     offs = (ctypes.c_uint64 * max(n, 1))()
     sizes = (ctypes.c_uint64 * max(n, 1))()
     types = (ctypes.c_int * max(n, 1))()
     widths = (ctypes.c_uint32 * max(n, 1))()
-    _check(library().ozl_frame_outputs(f.ctypes.data, f.size, n, offs, sizes, types, widths))
-    return [{"offset": offs[o], "size": sizes[o], "type": types[o], "width": widths[o]} for o in range(n)]
+    counts = (ctypes.c_uint64 * max(n, 1))()
+    lens = (ctypes.c_uint64 * max(n, 1))()
+    extent = ctypes.c_uint64()
+    _check(library().ozl_frame_outputs(f.ctypes.data, f.size, n, offs, sizes, types, widths, counts, lens,
+                                       ctypes.byref(extent)))
+    return [{"offset": offs[o], "size": sizes[o], "type": types[o], "width": widths[o], "count": counts[o],
+             "lens_offset": lens[o]} for o in range(n)], extent.value
 
 
 # DParam values (include/openzl_gb300.h)
@@ -213,9 +221,11 @@ class DCtx:
             raise ZLError(rep.code, self._err(rep))
         return out[: rep.value], info.type, info.fixedWidth
 
-    def decompress_multi(self, frame):
+    def decompress_multi(self, frame, with_lengths=False):
         """ZL_DCtx_decompressMultiTBuffer: every output of the frame as
-        [(bytes as numpy uint8, ZL_Type value, element width)]."""
+        [(bytes as numpy uint8, ZL_Type value, element width)], plus the
+        string lengths (numpy uint32, None for other types) with
+        `with_lengths`."""
         f = _as_u8(frame)
         fi = FrameInfo(f)
         n = fi.num_outputs()
@@ -230,7 +240,16 @@ class DCtx:
                 size = self._lib.ZL_TypedBuffer_byteSize(b)
                 ptr = self._lib.ZL_TypedBuffer_rPtr(b)
                 data = np.ctypeslib.as_array((ctypes.c_uint8 * max(size, 1)).from_address(ptr))[:size].copy()
-                res.append((data, self._lib.ZL_TypedBuffer_type(b), self._lib.ZL_TypedBuffer_eltWidth(b)))
+                t = self._lib.ZL_TypedBuffer_type(b)
+                item = (data, t, self._lib.ZL_TypedBuffer_eltWidth(b))
+                if with_lengths:
+                    lens = None
+                    if t == TYPE_STRING:
+                        k = self._lib.ZL_TypedBuffer_numElts(b)
+                        lp = self._lib.ZL_TypedBuffer_rStringLens(b)
+                        lens = np.ctypeslib.as_array((ctypes.c_uint32 * max(k, 1)).from_address(lp))[:k].copy() if k else np.zeros(0, np.uint32)
+                    item = item + (lens,)
+                res.append(item)
             return res
         finally:
             for b in bufs:
@@ -410,7 +429,7 @@ CPARAM_STICKY = 1
 CPARAM_FORMAT_VERSION = 4
 CPARAM_COMPRESSED_CHECKSUM = 6
 CPARAM_CONTENT_CHECKSUM = 7
-TYPE_SERIAL, TYPE_STRUCT, TYPE_NUMERIC = 1, 2, 4
+TYPE_SERIAL, TYPE_STRUCT, TYPE_NUMERIC, TYPE_STRING = 1, 2, 4, 8
 
 
 class Compressor:

@@ -147,7 +147,7 @@ ZL_Report ZL_getDecompressedSize(const void* src, size_t size)
 }
 
 ZL_Report ozl_frame_outputs(const void* frame, size_t frameSize, size_t capacity, uint64_t* offsets, uint64_t* sizes,
-                            int* types, uint32_t* widths)
+                            int* types, uint32_t* widths, uint64_t* counts, uint64_t* lensOffsets, uint64_t* extent)
 {
     if (!frame) return fail(ZL_ErrorCode_parameter_invalid);
     ozl::DecodePlan plan;
@@ -158,11 +158,16 @@ ZL_Report ozl_frame_outputs(const void* frame, size_t frameSize, size_t capacity
     const ozl::FramePlan& fp = plan.frames[0];
     size_t const n = fp.outOffs.size();
     for (size_t o = 0; o < n && o < capacity; o++) {
+        bool const str = fp.outTypes[o] == ZL_Type_string;
+        uint32_t const w = fp.outTypes[o] == ZL_Type_serial || str ? 1 : fp.outWidths[o];
         if (offsets) offsets[o] = fp.outOffs[o];
         if (sizes) sizes[o] = fp.outSizes[o];
         if (types) types[o] = fp.outTypes[o];
-        if (widths) widths[o] = fp.outTypes[o] == ZL_Type_serial ? 1 : fp.outWidths[o];
+        if (widths) widths[o] = w;
+        if (counts) counts[o] = str ? fp.nbStrings[o] : fp.outSizes[o] / w;
+        if (lensOffsets) lensOffsets[o] = str ? fp.lensOffs[o] : 0;
     }
+    if (extent) *extent = fp.decodedSize;
     return ok(n);
 }
 
@@ -351,7 +356,8 @@ size_t ozl_gpu_batch_launches(const OZL_GpuBatch* b) { return b ? size_t(b->laun
 const char* ozl_gpu_kind_name(int kind)
 {
     static const char* names[] = { "copy", "constant", "fse", "huffman", "flatpack", "tokenize",
-                                   "float_deconstruct", "transpose", "numeric_pipeline", "xxh3", "huffman16" };
+                                   "float_deconstruct", "transpose", "numeric_pipeline", "xxh3", "huffman16",
+                                   "widen" };
     return (kind >= 0 && kind < ozl::KIND_COUNT) ? names[kind] : "?";
 }
 
@@ -442,6 +448,7 @@ struct ZL_TypedBuffer_s {
     void* wrapped = nullptr;
     std::vector<uint8_t> own;
     size_t bytes = 0;
+    std::vector<uint32_t> lens; // string outputs
 };
 
 ZL_TypedBuffer* ZL_TypedBuffer_create(void) { return new (std::nothrow) ZL_TypedBuffer_s(); }
@@ -478,12 +485,34 @@ const void* ZL_TypedBuffer_rPtr(const ZL_TypedBuffer* t)
     if (!t) return nullptr;
     return t->wrap ? t->wrapped : static_cast<const void*>(t->own.data());
 }
-size_t ZL_TypedBuffer_numElts(const ZL_TypedBuffer* t) { return t && t->width ? t->bytes / t->width : 0; }
+size_t ZL_TypedBuffer_numElts(const ZL_TypedBuffer* t)
+{
+    if (t && t->type == ZL_Type_string) return t->lens.size();
+    return t && t->width ? t->bytes / t->width : 0;
+}
+const uint32_t* ZL_TypedBuffer_rStringLens(const ZL_TypedBuffer* t)
+{
+    return t && t->type == ZL_Type_string ? t->lens.data() : nullptr;
+}
 size_t ZL_TypedBuffer_eltWidth(const ZL_TypedBuffer* t) { return t ? t->width : 0; }
+
+ZL_Report ZL_DCtx_decompressMultiTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* outputs[], size_t nbOutputs,
+                                         const void* src, size_t cSize);
 
 ZL_Report ZL_DCtx_decompressTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* out, const void* src, size_t cSize)
 {
     if (!dctx || !out || !src) return fail(ZL_ErrorCode_parameter_invalid);
+    {
+        // a string output carries its lengths: the multi-output path fills both
+        ozl::FrameHeader h;
+        std::string e;
+        if (!ozl::parseFrameHeader(static_cast<const uint8_t*>(src), cSize, h, e) && h.types.size() == 1
+            && h.types[0] == ZL_Type_string) {
+            ZL_TypedBuffer* one[1] = { out };
+            ZL_Report r = ZL_DCtx_decompressMultiTBuffer(dctx, one, 1, src, cSize);
+            return ZL_isError(r) ? r : ok(out->bytes);
+        }
+    }
     ZL_Report ds = ZL_getDecompressedSize(src, cSize);
     if (ZL_isError(ds)) { resetParams(dctx); return ds; }
     size_t const outSize = ZL_validResult(ds);
@@ -538,8 +567,8 @@ ZL_Report ZL_DCtx_decompressMultiTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* outputs[
         resetParams(dctx);
         return fail(ZL_ErrorCode_userBuffers_invalidNum);
     }
-    std::vector<uint64_t> offs;
-    uint64_t const extent = ozl::frameOutputLayout(h, offs);
+    std::vector<uint64_t> offs, lensOffs;
+    uint64_t const extent = ozl::frameOutputLayout(h, offs, &lensOffs);
     auto done = [&](ZL_Report r) {
         resetParams(dctx);
         return r;
@@ -572,8 +601,20 @@ ZL_Report ZL_DCtx_decompressMultiTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* outputs[
         ZL_TypedBuffer_s* out = outputs[o];
         size_t const bytes = size_t(fp.outSizes[o]);
         ZL_Type const type = ZL_Type(fp.outTypes[o]);
-        size_t const w = type == ZL_Type_serial ? 1 : fp.outWidths[o];
+        size_t const w = type == ZL_Type_serial || type == ZL_Type_string ? 1 : fp.outWidths[o];
         void* dst;
+        if (type == ZL_Type_string) {
+            if (out->wrap) { dctx->err = "string outputs need a DCtx-allocated buffer"; return done(fail(ZL_ErrorCode_GENERIC)); }
+            try {
+                out->lens.resize(size_t(fp.nbStrings[o]));
+            } catch (...) {
+                return done(fail(ZL_ErrorCode_allocation));
+            }
+            if (!out->lens.empty()
+                && cudaMemcpyAsync(out->lens.data(), static_cast<uint8_t*>(dO) + lensOffs[o], 4 * out->lens.size(),
+                                   cudaMemcpyDeviceToHost, s) != cudaSuccess)
+                return done(fail(ZL_ErrorCode_GENERIC));
+        }
         if (out->wrap) {
             if (bytes > out->capacity) { dctx->err = "output buffer too small"; return done(fail(ZL_ErrorCode_dstCapacity_tooSmall)); }
             if (type != out->type || (type != ZL_Type_serial && w != out->width)) {
@@ -604,7 +645,7 @@ ZL_Report ZL_DCtx_decompressMultiTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* outputs[
 struct ZL_FrameInfo_s {
     unsigned version;
     std::vector<int> types;
-    std::vector<uint64_t> sizes;
+    std::vector<uint64_t> sizes, nbStrings;
 };
 
 ZL_FrameInfo* ZL_FrameInfo_create(const void* src, size_t cSize)
@@ -618,6 +659,7 @@ ZL_FrameInfo* ZL_FrameInfo_create(const void* src, size_t cSize)
     fi->version = h.version;
     fi->types = h.types; // the planner's type codes are ZL_Type's values
     fi->sizes = h.sizes;
+    fi->nbStrings = h.nbStrings;
     return fi;
 }
 void ZL_FrameInfo_free(ZL_FrameInfo* fi) { delete fi; }
@@ -652,6 +694,7 @@ ZL_Report ZL_FrameInfo_getNumElts(const ZL_FrameInfo* fi, int id)
     // decode_frameheader.c:455-467: counts known for serial outputs only
     int const t = fi->types[size_t(id)];
     if (t == ZL_Type_struct || t == ZL_Type_numeric) return fail(ZL_ErrorCode_temporaryLibraryLimitation);
+    if (t == ZL_Type_string) return ok(size_t(fi->nbStrings[size_t(id)]));
     return ok(size_t(fi->sizes[size_t(id)]));
 }
 

@@ -36,6 +36,7 @@ enum : uint32_t {
     T_CONV_NUM_TO_STRUCT = 8,
     T_CONV_SERIAL_TO_NUM = 9,
     T_CONV_NUM_TO_SERIAL = 10,
+    T_SEP_STRING = 12,
     T_BITPACK_SERIAL = 27,
     T_BITPACK_INT = 28,
     T_FLATPACK = 29,
@@ -76,6 +77,8 @@ Sig signature(uint32_t id)
         case T_ZIGZAG: return { true, 1, { TY_NUMERIC, 0 }, 0, TY_NUMERIC, false, false };
         case T_TSPLIT: return { true, 0, { 0, 0 }, TY_SERIAL, TY_STRUCT, false, false };
         case T_CONV_SERIAL_TO_STRUCT: return { true, 1, { TY_STRUCT, 0 }, 0, TY_SERIAL, true, false };
+        // separate_string_components (graph_conversion.h:61-66): content, lengths -> string
+        case T_SEP_STRING: return { true, 2, { TY_SERIAL, TY_NUMERIC }, 0, TY_STRING, false, false };
         case T_CONV_STRUCT_TO_SERIAL: return { true, 1, { TY_SERIAL, 0 }, 0, TY_STRUCT, true, false };
         case T_CONV_STRUCT_TO_NUM: return { true, 1, { TY_NUMERIC, 0 }, 0, TY_STRUCT, true, false };
         case T_CONV_NUM_TO_STRUCT: return { true, 1, { TY_STRUCT, 0 }, 0, TY_NUMERIC, true, false };
@@ -236,6 +239,7 @@ int DecodePlan::build(size_t nbFrames, const uint8_t* const* hFrames, const size
     hashes.clear();
     directCopies.clear();
     gathers.clear();
+    widens.clear();
     params.clear();
     arenaBytes = 0;
     totalOut = 0;
@@ -315,6 +319,9 @@ int parseFrameHeader(const uint8_t* src, size_t size, FrameHeader& h, std::strin
         h.sizes.resize(nbOut);
         for (size_t n = 0; n < nbOut; n++) h.sizes[n] = readLE32(src + pos + 4 * n);
         h.end = pos + 4 * nbOut;
+        h.nbStrings.assign(nbOut, 0);
+        for (int t : h.types)
+            if (t == TY_STRING) { err = "string outputs before format version 21"; return E_LIMIT; }
     } else {
         if (size < 9) { err = "frame too small"; return E_SRC_SMALL; }
         uint8_t const flags = src[4];
@@ -351,8 +358,10 @@ int parseFrameHeader(const uint8_t* src, size_t size, FrameHeader& h, std::strin
             if (sz1 == 0) { err = "unknown decompressed size"; return E_LIMIT; }
             h.sizes[n] = sz1 - 1;
         }
+        // string outputs: their string counts follow (decode_frameheader.c:217-236)
+        h.nbStrings.assign(nbOut, 0);
         for (size_t n = 0; n < nbOut; n++)
-            if (h.types[n] == TY_STRING) { err = "string outputs are not supported"; return E_LIMIT; }
+            if (h.types[n] == TY_STRING && !rd.varint(h.nbStrings[n])) { err = "truncated frame header"; return E_SRC_SMALL; }
         if (version >= 22 && hasComment) {
             uint64_t c;
             if (!rd.varint(c) || c == 0 || c > size_t(rd.end - rd.p)) { err = "bad comment"; return E_CORRUPT; }
@@ -365,20 +374,24 @@ int parseFrameHeader(const uint8_t* src, size_t size, FrameHeader& h, std::strin
             h.end++;
         }
     }
-    for (int t : h.types)
-        if (t == TY_STRING) { err = "string outputs are not supported"; return E_LIMIT; }
     h.outType = h.types[0];
     h.outSize = h.sizes[0];
     return 0;
 }
 
-uint64_t frameOutputLayout(const FrameHeader& h, std::vector<uint64_t>& offsets)
+uint64_t frameOutputLayout(const FrameHeader& h, std::vector<uint64_t>& offsets, std::vector<uint64_t>* lensOffsets)
 {
     offsets.resize(h.sizes.size());
+    if (lensOffsets) lensOffsets->assign(h.sizes.size(), 0);
     uint64_t extent = 0;
     for (size_t o = 0; o < h.sizes.size(); o++) {
         offsets[o] = (extent + 15) & ~uint64_t(15);
         extent = offsets[o] + h.sizes[o];
+        if (h.types[o] == TY_STRING) {
+            uint64_t const lo = (extent + 15) & ~uint64_t(15);
+            if (lensOffsets) (*lensOffsets)[o] = lo;
+            extent = lo + 4 * h.nbStrings[o];
+        }
     }
     return extent;
 }
@@ -391,7 +404,9 @@ int DecodePlan::planFrame(int f, const uint8_t* src, size_t size, size_t dstCap,
     if (rc) return rc;
     FramePlan& fp = frames[f];
     size_t const nbOut = h.sizes.size();
-    uint64_t const extent = frameOutputLayout(h, fp.outOffs);
+    uint64_t const extent = frameOutputLayout(h, fp.outOffs, &fp.lensOffs);
+    fp.nbStrings = h.nbStrings;
+    fp.stringsDone.assign(nbOut, 0);
     fp.outSizes = h.sizes;
     fp.outTypes = h.types;
     fp.outWidths.assign(nbOut, 0);
@@ -417,8 +432,13 @@ int DecodePlan::planFrame(int f, const uint8_t* src, size_t size, size_t dstCap,
         pos += consumed;
         if (h.version < 21) break;
     }
-    for (size_t o = 0; o < nbOut; o++)
+    for (size_t o = 0; o < nbOut; o++) {
         if (produced[o] != h.sizes[o]) { err = "decoded size does not match the frame header"; return E_CORRUPT; }
+        if (h.types[o] == TY_STRING && fp.stringsDone[o] != h.nbStrings[o]) {
+            err = "string count does not match the frame header";
+            return E_CORRUPT;
+        }
+    }
     fp.decodedSize = extent;
     fp.frameBytes = pos;
     return 0;
@@ -697,6 +717,24 @@ int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t si
                     O.n = in(1).n;
                     break;
                 }
+                case T_SEP_STRING: { // DI_revert_VSF_separation (decode_conversion_binding.c:230-275)
+                    PlanStream& L = in(1);
+                    if (!(L.w == 1 || L.w == 2 || L.w == 4 || L.w == 8)) { err = "string lengths width"; return E_CORRUPT; }
+                    O.w = 1;
+                    O.n = in(0).bytes();
+                    O.lens = nodeU.ins[1];
+                    if (L.host) { // lengths known here: their sum must be the content size
+                        uint64_t sum = 0;
+                        for (uint64_t i = 0; i < L.n; i++) {
+                            uint64_t v = 0;
+                            for (uint32_t b = 0; b < L.w; b++) v |= uint64_t(L.host[i * L.w + b]) << (8 * b);
+                            if (v > 0xffffffffull) { err = "string length above 32 bits"; return E_CORRUPT; }
+                            sum += v;
+                        }
+                        if (sum != O.n) { err = "string lengths do not add up to the content"; return E_CORRUPT; }
+                    }
+                    break;
+                }
                 case T_TOKENIZE_FIXED:
                 case T_TOKENIZE_NUMERIC: {
                     uint32_t iw = in(1).w;
@@ -844,9 +882,23 @@ int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t si
 
     // ---- outputs: the last stream slots, output o in slot total - 1 - o --
     std::vector<uint64_t> const before = produced;
+    std::vector<uint64_t> const stringsBefore = fp.stringsDone;
     for (size_t o = 0; o < nbOutputs; o++) {
         PlanStream& OUT = S(total - 1 - o);
         if (OUT.type == 0) { err = "output not regenerated"; return E_CORRUPT; }
+        if (OUT.type == TY_STRING) {
+            // the string node's inputs are written straight into the output
+            // (content) and after it (lengths); the node itself runs no kernel
+            if (OUT.producer < 0 || nodes[OUT.producer].id != T_SEP_STRING) {
+                err = "string outputs come from separate_string_components only";
+                return E_TRANSFORM;
+            }
+            PlanNode& sn = nodes[OUT.producer];
+            sn.dead = true;
+            PlanStream& L = streams[sn.ins[1]];
+            if (fp.stringsDone[o] + L.n > fp.nbStrings[o]) { err = "more strings than the frame header says"; return E_CORRUPT; }
+            fp.stringsDone[o] += L.n;
+        }
         if (fp.outWidths[o] == 0) {
             fp.outWidths[o] = OUT.w;
             fp.outTypes[o] = OUT.type;
@@ -931,6 +983,23 @@ int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t si
         OUT.loc = L_OUT;
         OUT.frame = f;
         OUT.off = fp.outOffs[o] + before[o];
+        if (OUT.type != TY_STRING) continue;
+        const PlanNode& sn = nodes[OUT.producer];
+        uint64_t const at[2] = { OUT.off, fp.lensOffs[o] + 4 * stringsBefore[o] };
+        for (int k = 0; k < 2; k++) {
+            PlanStream& I = streams[sn.ins[k]];
+            if (k == 1 && I.w != 4) { // narrower lengths: widened into place
+                widens.push_back(PlanWiden{ sn.ins[1], f, at[1] });
+                continue;
+            }
+            if (I.producer < 0) { // stored: copied into place
+                if (I.bytes()) directCopies.push_back(PlanCopy{ f, I.off, at[k], I.bytes() });
+            } else {
+                I.loc = L_OUT;
+                I.frame = f;
+                I.off = at[k];
+            }
+        }
     }
     auto alloc = [&](PlanStream& s) {
         s.loc = L_ARENA;
@@ -972,23 +1041,32 @@ int DecodePlan::planBlock(int f, unsigned version, const uint8_t* src, size_t si
     *consumed = pos - start;
     // content checksum: XXH3 of the block's outputs one after another
     // (STREAM_hashLastCommit_xxh3low32, src/openzl/common/stream.c:727-773)
+    // (a string output contributes its content, then from v15 its 4-byte
+    // lengths, stream.c:757-766)
     if (hasContentCk && ckContent) {
-        if (nbOutputs == 1) {
-            hashes.push_back(PlanHash{ f, HW_OUTPUT, before[0], produced[0] - before[0], contentCk, 14, false });
+        bool const strings = [&] {
+            for (int t : fp.outTypes) if (t == TY_STRING) return true;
+            return false;
+        }();
+        if (nbOutputs == 1 && !strings) {
+            hashes.push_back(PlanHash{ f, HW_OUTPUT, fp.outOffs[0] + before[0], produced[0] - before[0], contentCk, 14, false });
         } else {
-            uint64_t const base = arenaBytes, total = [&] {
-                uint64_t t = 0;
-                for (size_t o = 0; o < nbOutputs; o++) t += produced[o] - before[o];
-                return t;
-            }();
-            arenaBytes += (total + 63) & ~uint64_t(63);
+            std::vector<PlanGather> segs;
+            uint64_t const base = arenaBytes;
             uint64_t at = base;
             for (size_t o = 0; o < nbOutputs; o++) {
                 uint64_t const b = produced[o] - before[o];
-                if (b) gathers.push_back(PlanGather{ f, fp.outOffs[o] + before[o], at, b });
+                if (b) segs.push_back(PlanGather{ f, fp.outOffs[o] + before[o], at, b });
                 at += b;
+                if (fp.outTypes[o] == TY_STRING && version >= 15) {
+                    uint64_t const lb = 4 * (fp.stringsDone[o] - stringsBefore[o]);
+                    if (lb) segs.push_back(PlanGather{ f, fp.lensOffs[o] + 4 * stringsBefore[o], at, lb });
+                    at += lb;
+                }
             }
-            hashes.push_back(PlanHash{ f, HW_ARENA, base, total, contentCk, 14, false });
+            arenaBytes += (at - base + 63) & ~uint64_t(63);
+            gathers.insert(gathers.end(), segs.begin(), segs.end());
+            hashes.push_back(PlanHash{ f, HW_ARENA, base, at - base, contentCk, 14, false });
         }
     }
     return 0;
@@ -1025,6 +1103,7 @@ struct Buckets {
     std::vector<HufTask> huf;
     std::vector<Huf16Task> huf16;
     std::vector<TokenizeTask> tok;
+    std::vector<WidenTask> widen;
     std::vector<FloatDecTask> flt;
     std::vector<FlatpackTask> flat;
 };
@@ -1044,6 +1123,7 @@ uint64_t taskBytes(const Huf16Task& t)
 }
 uint64_t taskBytes(const FlatpackTask& t) { return t.n + (t.n * t.nbBits + 7) / 8 + t.alphabetSize; }
 uint64_t taskBytes(const TokenizeTask& t) { return t.n * (t.w + t.iw) + uint64_t(t.alphabetSize) * t.w; }
+uint64_t taskBytes(const WidenTask& t) { return t.n * (t.w + 4); }
 uint64_t taskBytes(const FloatDecTask& t) { return t.n * (t.eltType == 0 ? 8 : 4); }
 uint64_t taskBytes(const TransposeTask& t) { return 2 * t.n * t.W; }
 uint64_t taskBytes(const NumPipeTask& t)
@@ -1140,6 +1220,11 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         maxLevel = std::max(maxLevel, lv);
     }
     if (!plan.directCopies.empty()) maxLevel = std::max(maxLevel, 1);
+    std::vector<int> widenLevel;
+    for (const PlanWiden& wd : plan.widens) {
+        widenLevel.push_back(streamLevel(wd.stream) + 1);
+        if (inPart(wd.frame)) maxLevel = std::max(maxLevel, widenLevel.back());
+    }
     // multi-output blocks gather their outputs for the content checksum after
     // everything that writes them
     bool anyGather = false;
@@ -1161,6 +1246,12 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         if (!inPart(c.frame)) continue;
         CopyTask t{ dOuts[c.frame] + c.outOff, dFrames[c.frame] + c.frameOff, c.bytes, 0 };
         B[1].copy.push_back(t);
+    }
+    for (size_t k = 0; k < plan.widens.size(); k++) {
+        const PlanWiden& wd = plan.widens[k];
+        if (!inPart(wd.frame) || !streams[wd.stream].n) continue;
+        B[widenLevel[k]].widen.push_back(WidenTask{ addr(wd.stream), reinterpret_cast<uint32_t*>(dOuts[wd.frame] + wd.outOff),
+                                                    streams[wd.stream].n, streams[wd.stream].w, 0 });
     }
     for (const PlanGather& g : plan.gathers) {
         if (!inPart(g.frame)) continue;
@@ -1368,6 +1459,7 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         addPlain(KIND_HUF16, lv, b.huf16);
         addTiled(KIND_FLATPACK, lv, b.flat, [](const FlatpackTask& t) { return ceilDiv(t.n, kTileBytes); });
         addTiled(KIND_TOKENIZE, lv, b.tok, [](const TokenizeTask& t) { return ceilDiv(t.n, kTileElems); });
+        addTiled(KIND_WIDEN, lv, b.widen, [](const WidenTask& t) { return ceilDiv(t.n, kTileElems); });
         addTiled(KIND_FLOATDEC, lv, b.flt, [](const FloatDecTask& t) { return ceilDiv(t.n, kTileElems); });
         addTiled(KIND_TRANSPOSE, lv, b.tr, [](const TransposeTask& t) { return ceilDiv(t.n, kTileElems); });
         addTiled(KIND_NUMPIPE, lv, b.num, [](const NumPipeTask& t) { return ceilDiv(t.n, kNumTileBytes / t.w); });

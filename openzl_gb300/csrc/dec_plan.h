@@ -22,6 +22,7 @@ enum Kind : int {
     KIND_NUMPIPE,
     KIND_HASH,
     KIND_HUF16, // launched after KIND_HUF within a level
+    KIND_WIDEN, // string lengths to 4 bytes
     KIND_COUNT
 };
 
@@ -53,6 +54,7 @@ struct PlanStream {
     int parent = -1;   // for L_SUB / L_ALIAS
     uint64_t off = 0;  // offset within the location
     const uint8_t* host = nullptr; // host copy of the content, when known at plan time
+    int lens = -1;     // string streams: the stream of 4-byte string lengths
     uint64_t bytes() const { return n * w; }
 };
 
@@ -87,6 +89,13 @@ struct PlanCopy {
     uint64_t frameOff, outOff, bytes;
 };
 
+// String lengths narrower than 4 bytes, widened into an output's lengths.
+struct PlanWiden {
+    int stream;
+    int frame;
+    uint64_t outOff;
+};
+
 // One output's block gathered into the arena, so that the content checksum
 // of a multi-output block hashes contiguous bytes.
 struct PlanGather {
@@ -102,6 +111,9 @@ struct FramePlan {
     std::vector<uint64_t> outOffs, outSizes; // per output: offset in the destination, bytes
     std::vector<int> outTypes;
     std::vector<uint32_t> outWidths;
+    std::vector<uint64_t> lensOffs;          // string outputs: offset of their 4-byte lengths
+    std::vector<uint64_t> nbStrings;         // string outputs: strings in the frame header
+    std::vector<uint64_t> stringsDone;       // string outputs: strings placed so far
 };
 
 // Frame-header fields shared by the planner and the frame-information calls.
@@ -110,7 +122,8 @@ struct FrameHeader {
     bool hasContentCk = false;    // v21+; older frames carry the flags per block
     bool hasCompressedCk = false;
     std::vector<int> types;       // TY_* per output
-    std::vector<uint64_t> sizes;  // decompressed bytes per output
+    std::vector<uint64_t> sizes;  // decompressed bytes per output (strings: content bytes)
+    std::vector<uint64_t> nbStrings; // string outputs: number of strings (0 for other types)
     int outType = 0;              // output 0
     uint64_t outSize = 0;
     size_t end = 0;               // first byte after the header
@@ -118,15 +131,18 @@ struct FrameHeader {
 };
 
 // Parses the frame header (src/openzl/decompress/decode_frameheader.c:58-190,
-// 270-370). Format versions 8..23, up to 2048 outputs, no string outputs.
-// Returns 0 or a ZL error code: formatVersion_unsupported (60),
-// srcSize_tooSmall (3), temporaryLibraryLimitation (81) for unknown sizes or
-// string outputs, corruption (12).
+// 270-370). Format versions 8..23, up to 2048 outputs; string outputs from
+// format version 21 (older headers carry no string counts). Returns 0 or a
+// ZL error code: formatVersion_unsupported (60), srcSize_tooSmall (3),
+// temporaryLibraryLimitation (81) for unknown sizes or string outputs before
+// v21, corruption (12).
 int parseFrameHeader(const uint8_t* src, size_t size, FrameHeader& h, std::string& err);
 
 // Where the batch API writes a frame's outputs in its destination: one after
-// another, each at a 16-byte-aligned offset. Returns the bytes needed.
-uint64_t frameOutputLayout(const FrameHeader& h, std::vector<uint64_t>& offsets);
+// another, each at a 16-byte-aligned offset; a string output's 4-byte lengths
+// follow its content at the next 16-byte-aligned offset (`lensOffsets`, 0 for
+// other types). Returns the bytes needed.
+uint64_t frameOutputLayout(const FrameHeader& h, std::vector<uint64_t>& offsets, std::vector<uint64_t>* lensOffsets = nullptr);
 
 class DecodePlan {
   public:
@@ -141,6 +157,7 @@ class DecodePlan {
     std::vector<PlanHash> hashes;
     std::vector<PlanCopy> directCopies;
     std::vector<PlanGather> gathers;
+    std::vector<PlanWiden> widens;
     std::vector<uint8_t> params;  // host-decoded small streams (FSE normalized counts)
     uint64_t arenaBytes = 0;
     uint64_t totalOut = 0;

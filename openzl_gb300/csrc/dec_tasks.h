@@ -100,6 +100,16 @@ struct HufTask {
     uint8_t x4;
 };
 
+// String lengths of width w (1, 2 or 8 bytes) to 4-byte lengths; a value
+// above 2^32 - 1 is corruption.
+struct WidenTask {
+    const uint8_t* src;
+    uint32_t* dst;
+    uint64_t n;
+    uint32_t w;
+    uint32_t tileBase;
+};
+
 struct TokenizeTask {
     uint8_t* out;
     const uint8_t* alphabet;

@@ -660,6 +660,25 @@ __global__ void kTokenize(const TokenizeTask* __restrict__ tasks, const TileRef*
 }
 
 // ---------------------------------------------------------------------------
+// string lengths to 4 bytes (NUMOP_write32_fromNumerics in
+// DI_revert_VSF_separation, decode_conversion_binding.c:245-250)
+__global__ void kWiden(const WidenTask* __restrict__ tasks, const TileRef* __restrict__ tiles,
+                       uint32_t* __restrict__ status)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    WidenTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kTileElems;
+    uint64_t const e1 = umin64(t.n, e0 + kTileElems);
+    bool bad = false;
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+        uint64_t const v = ldElem(t.src + i * t.w, t.w);
+        bad |= v > 0xffffffffull;
+        t.dst[i] = uint32_t(v);
+    }
+    if (bad) reportError(status, DERR_CORRUPTION);
+}
+
+// ---------------------------------------------------------------------------
 // float deconstruct (decode_float_deconstruct_kernel.c semantics)
 __global__ void kFloatDec(const FloatDecTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
 {
@@ -1866,6 +1885,9 @@ long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dSc
                 break;
             case KIND_HUF16:
                 if (l.nbTasks) kHuf16<<<l.nbTasks, 128, 0, s>>>(static_cast<const Huf16Task*>(tasks), dStatus);
+                break;
+            case KIND_WIDEN:
+                kWiden<<<l.nbTiles, 256, 0, s>>>(static_cast<const WidenTask*>(tasks), tiles, dStatus);
                 break;
             case KIND_TOKENIZE:
                 kTokenize<<<l.nbTiles, 256, 0, s>>>(static_cast<const TokenizeTask*>(tasks), tiles, dStatus);

@@ -46,7 +46,8 @@ def lib():
                                    ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         l.ozo_decompress_multi.restype = ctypes.c_int64
         l.ozo_decompress_multi.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p,
-                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]
         l.ozo_free.restype = None
         l.ozo_free.argtypes = [ctypes.c_void_p]
         l.ozo_xxh3_64.restype = ctypes.c_uint64
@@ -69,21 +70,31 @@ def decompress(frame):
     return out[:r], t.value, w.value
 
 
-def decompress_multi(frame, max_outputs=64):
-    """Returns [(bytes as uint8 array, type, elt_width)] per output; raises on error."""
+def decompress_multi(frame, max_outputs=64, with_lengths=False):
+    """Returns [(bytes as uint8 array, type, elt_width)] per output, plus the
+    string lengths (uint32 array, None for other types) with `with_lengths`;
+    raises on error."""
     f = np.frombuffer(bytes(frame), np.uint8) if not isinstance(frame, np.ndarray) else frame.view(np.uint8)
     outs = (ctypes.c_void_p * max_outputs)()
     lens = (ctypes.c_size_t * max_outputs)()
     types = (ctypes.c_int * max_outputs)()
     widths = (ctypes.c_int * max_outputs)()
-    n = lib().ozo_decompress_multi(f.ctypes.data, f.size, max_outputs, outs, lens, types, widths)
+    slens = (ctypes.c_void_p * max_outputs)()
+    nbs = (ctypes.c_size_t * max_outputs)()
+    n = lib().ozo_decompress_multi(f.ctypes.data, f.size, max_outputs, outs, lens, types, widths, slens, nbs)
     if n < 0:
         raise ValueError("oracle: decode failed (%d)" % n)
     res = []
     for o in range(n):
         buf = (ctypes.c_uint8 * max(lens[o], 1)).from_address(outs[o])
-        res.append((np.frombuffer(buf, np.uint8)[:lens[o]].copy(), types[o], widths[o]))
+        data = np.frombuffer(buf, np.uint8)[:lens[o]].copy()
+        sl = None
+        if types[o] == 8:
+            sbuf = (ctypes.c_uint32 * max(nbs[o], 1)).from_address(slens[o])
+            sl = np.frombuffer(sbuf, np.uint32)[:nbs[o]].copy()
         lib().ozo_free(outs[o])
+        lib().ozo_free(slens[o])
+        res.append((data, types[o], widths[o], sl) if with_lengths else (data, types[o], widths[o]))
     return res
 
 

@@ -38,10 +38,12 @@ uint64_t ozo_xxh3_64(const void* src, size_t len);
 int64_t ozo_decompress(const void* src, size_t srcSize, void* dst, size_t dstCap,
                        int* outType, int* outEltWidth);
 
-/* Decodes a frame of any number of outputs; outs[o] is malloc'ed (free it
- * with ozo_free). Returns the number of outputs or a negative error. */
+/* Decodes a frame of any number of outputs; outs[o] and strLens[o] (the
+ * 4-byte string lengths of a string output, nbStrings[o] of them) are
+ * malloc'ed (free them with ozo_free). Returns the number of outputs or a
+ * negative error. */
 int64_t ozo_decompress_multi(const void* src, size_t srcSize, size_t maxOut, void** outs, size_t* lens, int* types,
-                             int* widths);
+                             int* widths, void** strLens, size_t* nbStrings);
 void ozo_free(void* p);
 
 /* Decompressed size recorded in a single-output frame header, or < 0. */

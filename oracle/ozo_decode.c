@@ -10,15 +10,18 @@
 typedef struct {
     int type;          /* OZO_TYPE_* */
     size_t w;          /* element width in bytes */
-    size_t n;          /* number of elements */
+    size_t n;          /* number of elements (string streams: content bytes) */
     const uint8_t* p;  /* content */
     uint8_t* own;      /* owned allocation, if any */
     int filled;
+    uint32_t* lens;    /* string streams: the length of each string (owned) */
+    size_t nbStrings;
 } OStream;
 
 static void ost_free(OStream* s)
 {
     free(s->own);
+    free(s->lens);
     memset(s, 0, sizeof(*s));
 }
 static uint8_t* ost_alloc(OStream* s, int type, size_t w, size_t n)
@@ -472,6 +475,9 @@ static DecSig sig_of(unsigned id)
             d.nbSO = 0; d.voType = OZO_TYPE_NUMERIC; d.outType = OZO_TYPE_NUMERIC; break;
         case TR_CONSTANT_SERIAL:
             d.nbSO = 1; d.soTypes[0] = OZO_TYPE_SERIAL; d.outType = OZO_TYPE_SERIAL; break;
+        case TR_SEPARATE_STRING: /* graph_conversion.h:61-66, decoder inputs: content, lengths */
+            d.nbSO = 2; d.soTypes[0] = OZO_TYPE_SERIAL; d.soTypes[1] = OZO_TYPE_NUMERIC;
+            d.outType = OZO_TYPE_STRING; break;
         case TR_CONSTANT_FIXED:
             d.nbSO = 1; d.soTypes[0] = OZO_TYPE_STRUCT; d.outType = OZO_TYPE_STRUCT; break;
         case TR_FSE_V2:
@@ -498,6 +504,24 @@ static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, s
 {
     DecSig const sg = sig_of(id);
     switch (id) {
+        case TR_SEPARATE_STRING: { /* DI_revert_VSF_separation, decode_conversion_binding.c:230-275 */
+            const OStream* c = in[0];
+            const OStream* l = in[1];
+            size_t const nb = l->n;
+            uint32_t* lens = (uint32_t*)malloc(nb * 4 + 4);
+            uint64_t sum = 0;
+            for (size_t i = 0; i < nb; i++) {
+                uint64_t const v = ozo_rdN(l->p + i * l->w, l->w);
+                if (v > 0xFFFFFFFFu) { free(lens); return -OZO_ERR_CORRUPTION; }
+                lens[i] = (uint32_t)v;
+                sum += v;
+            }
+            if (sum != (uint64_t)c->n * c->w) { free(lens); return -OZO_ERR_CORRUPTION; }
+            ost_ref(out, OZO_TYPE_STRING, 1, c->n * c->w, c->p);
+            out->lens = lens;
+            out->nbStrings = nb;
+            return 0;
+        }
         case TR_DELTA_INT: { /* decode_delta_binding.c:11-58 */
             size_t const w = in[0]->w, nd = in[0]->n;
             size_t n = 0;
@@ -824,6 +848,7 @@ typedef struct {
     size_t nbOutputs;
     int types[OZO_MAX_OUTPUTS];
     uint64_t sizes[OZO_MAX_OUTPUTS];
+    uint64_t nbStrings[OZO_MAX_OUTPUTS]; /* string outputs, v21+ */
     size_t headerSize;
 } FrameHdr;
 
@@ -884,8 +909,6 @@ static int64_t parse_frame_header_v20(FrameHdr* fh, const uint8_t* src, size_t s
     if (pos + 4 * nbOut > size) return -OZO_ERR_SRC_SIZE;
     for (size_t n = 0; n < nbOut; n++) fh->sizes[n] = ozo_rd32(src + pos + 4 * n);
     pos += 4 * nbOut;
-    for (size_t n = 0; n < nbOut; n++)
-        if (fh->types[n] == OZO_TYPE_STRING) return -OZO_ERR_UNSUPPORTED;
     fh->headerSize = pos;
     return (int64_t)pos;
 }
@@ -938,8 +961,9 @@ static int64_t parse_frame_header(FrameHdr* fh, const uint8_t* src, size_t size)
         if (ozo_varint_dec(&p, src + size, &v) || v == 0) return -OZO_ERR_CORRUPTION;
         fh->sizes[n] = v - 1;
     }
+    /* string outputs: their string counts follow (decode_frameheader.c:217-236) */
     for (size_t n = 0; n < nbOut; n++)
-        if (fh->types[n] == OZO_TYPE_STRING) return -OZO_ERR_UNSUPPORTED;
+        if (fh->types[n] == OZO_TYPE_STRING && ozo_varint_dec(&p, src + size, &fh->nbStrings[n])) return -OZO_ERR_CORRUPTION;
     pos = (size_t)(p - src);
     if (fh->version >= 22 && hasComment) {
         uint64_t csz;
@@ -965,7 +989,8 @@ typedef struct {
 
 /* Decodes one block; appends each output to outs[]. Returns block size. */
 static int64_t decode_block(const FrameHdr* fh, const uint8_t* src, size_t size, size_t start,
-                            uint8_t** outBuf, size_t* outLen, int* outType, size_t* outW)
+                            uint8_t** outBuf, size_t* outLen, int* outType, size_t* outW, uint32_t** outLens,
+                            size_t* outNbStrings)
 {
     const uint8_t* p = src + start;
     const uint8_t* const end = src + size;
@@ -1169,11 +1194,13 @@ static int64_t decode_block(const FrameHdr* fh, const uint8_t* src, size_t size,
         }
         /* outputs: last nbOutputs slots, in reverse order */
         {
+            /* content checksum: each output's bytes, and from v15 a string
+             * output's lengths after its content (stream.c:727-773) */
             size_t catLen = 0;
             for (size_t o = 0; o < fh->nbOutputs; o++) {
                 OStream* s = &streams[total - 1 - o];
                 if (!s->filled) FAIL(OZO_ERR_CORRUPTION);
-                catLen += s->n * s->w;
+                catLen += s->n * s->w + (s->type == OZO_TYPE_STRING && ver >= 15 ? 4 * s->nbStrings : 0);
             }
             uint8_t* cat = (uint8_t*)malloc(catLen + 1);
             size_t cp = 0;
@@ -1182,6 +1209,15 @@ static int64_t decode_block(const FrameHdr* fh, const uint8_t* src, size_t size,
                 size_t const b = s->n * s->w;
                 memcpy(cat + cp, s->p, b);
                 cp += b;
+                if (s->type == OZO_TYPE_STRING) {
+                    if (ver >= 15) {
+                        for (size_t i = 0; i < s->nbStrings; i++) ozo_wr32(cat + cp + 4 * i, s->lens[i]);
+                        cp += 4 * s->nbStrings;
+                    }
+                    outLens[o] = (uint32_t*)realloc(outLens[o], 4 * (outNbStrings[o] + s->nbStrings) + 4);
+                    memcpy(outLens[o] + outNbStrings[o], s->lens, 4 * s->nbStrings);
+                    outNbStrings[o] += s->nbStrings;
+                }
                 outBuf[o] = (uint8_t*)realloc(outBuf[o], outLen[o] + b + 1);
                 memcpy(outBuf[o] + outLen[o], s->p, b);
                 outLen[o] += b;
@@ -1234,6 +1270,8 @@ int64_t ozo_decompress(const void* srcv, size_t size, void* dst, size_t dstCap, 
     size_t lens[1] = { 0 };
     int types[1] = { 0 };
     size_t ws[1] = { 0 };
+    uint32_t* slens[1] = { NULL };
+    size_t nbs[1] = { 0 };
     for (;;) {
         /* versions before 21 hold exactly one block and no end marker
          * (decompress2.c:1689-1714) */
@@ -1241,11 +1279,12 @@ int64_t ozo_decompress(const void* srcv, size_t size, void* dst, size_t dstCap, 
             if (pos >= size) { free(bufs[0]); return -OZO_ERR_SRC_SIZE; }
             if (src[pos] == 0) { pos++; break; }
         }
-        int64_t b = decode_block(&fh, src, size, pos, bufs, lens, types, ws);
-        if (b < 0) { free(bufs[0]); return b; }
+        int64_t b = decode_block(&fh, src, size, pos, bufs, lens, types, ws, slens, nbs);
+        if (b < 0) { free(bufs[0]); free(slens[0]); return b; }
         pos += (size_t)b;
         if (fh.version < 21) break;
     }
+    free(slens[0]);
     if (lens[0] != fh.sizes[0]) { free(bufs[0]); return -OZO_ERR_CORRUPTION; }
     if (lens[0] > dstCap) { free(bufs[0]); return -OZO_ERR_DST_SIZE; }
     if (lens[0]) memcpy(dst, bufs[0], lens[0]);
@@ -1260,7 +1299,7 @@ int64_t ozo_decompress(const void* srcv, size_t size, void* dst, size_t dstCap, 
  * with ozo_free), lens/types/widths its size, type and element width.
  * Returns the number of outputs, or a negative error. */
 int64_t ozo_decompress_multi(const void* srcv, size_t size, size_t maxOut, void** outs, size_t* lens, int* types,
-                             int* widths)
+                             int* widths, void** strLens, size_t* nbStrings)
 {
     const uint8_t* src = (const uint8_t*)srcv;
     FrameHdr fh;
@@ -1269,8 +1308,9 @@ int64_t ozo_decompress_multi(const void* srcv, size_t size, size_t maxOut, void*
     if (fh.nbOutputs > maxOut) return -OZO_ERR_DST_SIZE;
     size_t const no = fh.nbOutputs;
     uint8_t* bufs[OZO_MAX_OUTPUTS] = { NULL };
-    size_t ln[OZO_MAX_OUTPUTS] = { 0 }, ws[OZO_MAX_OUTPUTS] = { 0 };
+    size_t ln[OZO_MAX_OUTPUTS] = { 0 }, ws[OZO_MAX_OUTPUTS] = { 0 }, nbs[OZO_MAX_OUTPUTS] = { 0 };
     int ts[OZO_MAX_OUTPUTS] = { 0 };
+    uint32_t* sl[OZO_MAX_OUTPUTS] = { NULL };
     size_t pos = (size_t)r;
     int64_t ret = (int64_t)no;
     for (;;) {
@@ -1278,22 +1318,27 @@ int64_t ozo_decompress_multi(const void* srcv, size_t size, size_t maxOut, void*
             if (pos >= size) { ret = -OZO_ERR_SRC_SIZE; break; }
             if (src[pos] == 0) { pos++; break; }
         }
-        int64_t b = decode_block(&fh, src, size, pos, bufs, ln, ts, ws);
+        int64_t b = decode_block(&fh, src, size, pos, bufs, ln, ts, ws, sl, nbs);
         if (b < 0) { ret = b; break; }
         pos += (size_t)b;
         if (fh.version < 21) break;
     }
-    for (size_t o = 0; o < no && ret >= 0; o++)
+    for (size_t o = 0; o < no && ret >= 0; o++) {
         if (ln[o] != fh.sizes[o]) ret = -OZO_ERR_CORRUPTION;
+        if (fh.version >= 21 && fh.types[o] == OZO_TYPE_STRING && nbs[o] != fh.nbStrings[o]) ret = -OZO_ERR_CORRUPTION;
+    }
     for (size_t o = 0; o < no; o++) {
         if (ret < 0) {
             free(bufs[o]);
+            free(sl[o]);
             continue;
         }
         outs[o] = bufs[o] ? bufs[o] : malloc(1);
         lens[o] = ln[o];
         types[o] = ts[o] ? ts[o] : fh.types[o];
         widths[o] = (int)(ws[o] ? ws[o] : 1);
+        strLens[o] = sl[o] ? (void*)sl[o] : malloc(4);
+        nbStrings[o] = nbs[o];
     }
     return ret;
 }

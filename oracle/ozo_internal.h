@@ -24,6 +24,7 @@ enum {
     TR_CONV_NUM_TO_STRUCT_LE = 8,
     TR_CONV_SERIAL_TO_NUM_LE = 9,
     TR_CONV_NUM_TO_SERIAL_LE = 10,
+    TR_SEPARATE_STRING = 12, /* content + lengths -> string */
     TR_BITPACK_SERIAL = 27,
     TR_BITPACK_INT = 28,
     TR_FLATPACK = 29,

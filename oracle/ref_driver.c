@@ -204,6 +204,43 @@ int64_t ref_compress_multi(int nb, const int* recipes, const void* const* srcs, 
     return ret;
 }
 
+/* One string input (nbStrings lengths over `content`) through recipe
+ * 100 + k: 100 store, 101 separate_string_components -> (content: FSE,
+ * lengths: store), 102 separate components -> (content: Huffman, lengths:
+ * delta -> bitpack -> Huffman). Returns the frame size or -(error code). */
+int64_t ref_compress_string(int recipe, const void* content, size_t contentSize, const uint32_t* lens,
+                            size_t nbStrings, void* dst, size_t dstCap, int checksums, int formatVersion)
+{
+    ZL_Compressor* c = ZL_Compressor_create();
+    if (!c) return -1;
+    if (formatVersion <= 0) formatVersion = ZL_MAX_FORMAT_VERSION;
+    ZL_Compressor_setParameter(c, ZL_CParam_formatVersion, formatVersion);
+    if (!checksums) {
+        ZL_Compressor_setParameter(c, ZL_CParam_contentChecksum, ZL_TernaryParam_disable);
+        ZL_Compressor_setParameter(c, ZL_CParam_compressedChecksum, ZL_TernaryParam_disable);
+    }
+    ZL_GraphID g = ZL_GRAPH_STORE;
+    if (recipe == 101 || recipe == 102) {
+        ZL_GraphID const lensGraph = recipe == 101 ? ZL_GRAPH_STORE : build(c, R_D_BITPACK_HUF, 4);
+        ZL_GraphID const succ[2] = { recipe == 101 ? ZL_GRAPH_FSE : ZL_GRAPH_HUFFMAN, lensGraph };
+        g = ZL_Compressor_registerStaticGraph_fromNode(c, ZL_NODE_SEPARATE_STRING_COMPONENTS, succ, 2);
+    } else if (recipe != 100) {
+        ZL_Compressor_free(c);
+        return -2;
+    }
+    ZL_Report r = ZL_Compressor_selectStartingGraphID(c, g);
+    if (ZL_isError(r)) { ZL_Compressor_free(c); return -3; }
+    ZL_CCtx* cc = ZL_CCtx_create();
+    ZL_CCtx_refCompressor(cc, c);
+    ZL_TypedRef* tr = ZL_TypedRef_createString(content, contentSize, lens, nbStrings);
+    r = ZL_CCtx_compressTypedRef(cc, dst, dstCap, tr);
+    int64_t ret = ZL_isError(r) ? -(int64_t)ZL_errorCode(r) - 1000 : (int64_t)ZL_validResult(r);
+    ZL_TypedRef_free(tr);
+    ZL_CCtx_free(cc);
+    ZL_Compressor_free(c);
+    return ret;
+}
+
 /* Decodes one single-output frame into dst. Writes the output's element
  * width (1 for serial) and type. Returns the decoded byte count or -(code). */
 int64_t ref_decompress(const void* src, size_t srcSize, void* dst, size_t dstCap,

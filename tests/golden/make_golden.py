@@ -164,12 +164,50 @@ def make_multi(lib):
             manifest.append({"case": case, "checksums": cs, "frame_bytes": int(r),
                              "sha256_frame": hashlib.sha256(dst[:r].tobytes()).hexdigest(),
                              **({"format_version": version} if version else {}),
-                             "outputs": [{"recipe": rr, "elt_width": w, "n": int(a.size),
-                                          "sha256": hashlib.sha256(a.tobytes()).hexdigest()}
+                             "outputs": [{"recipe": rr, "elt_width": w, "n": int(a.size), "type": 1 if w == 0 else 4,
+                                          "bytes": int(a.nbytes), "sha256": hashlib.sha256(a.tobytes()).hexdigest()}
                                          for (rr, _, w), a in zip(inputs, arrs)]})
+    manifest += make_strings(lib)
     with open(os.path.join(HERE, "manifest_multi.json"), "w") as fh:
         json.dump(manifest, fh, indent=1)
     return manifest
+
+
+def make_strings(lib):
+    """String inputs (one string output per frame): stored, FSE content with
+    stored lengths, Huffman content with delta/bitpack/Huffman lengths."""
+    f = lib.ref_compress_string
+    f.restype = ctypes.c_int64
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                  ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(20261205)
+    words = [bytes(rng.integers(97, 123, int(rng.integers(0, 14))).astype(np.uint8)) for _ in range(400)]
+    out = []
+    for name, recipe, nstr, version in (("str_store", 100, 3000, 0), ("str_fse_content", 101, 8000, 0),
+                                        ("str_huf_content_coded_lens", 102, 20000, 0),
+                                        ("str_huf_content_v21", 102, 5000, 21), ("str_empty_strings", 100, 50, 0)):
+        pick = (rng.zipf(1.2, nstr) - 1) % len(words)
+        strs = [words[i] if name != "str_empty_strings" else b"" for i in pick]
+        content = np.frombuffer(b"".join(strs) + b"", np.uint8).copy()
+        lens = np.array([len(x) for x in strs], np.uint32)
+        for cs in (1, 0):
+            cap = content.size * 2 + lens.nbytes * 2 + 65536
+            dst = np.zeros(cap, np.uint8)
+            r = f(recipe, content.ctypes.data if content.size else None, content.size, lens.ctypes.data, lens.size,
+                  dst.ctypes.data, cap, cs, version)
+            if r <= 0:
+                print("skip", name, cs, r)
+                continue
+            case = name + ("" if cs else "_nock")
+            with open(os.path.join(HERE, case + ".zl"), "wb") as fh:
+                fh.write(dst[:r].tobytes())
+            out.append({"case": case, "checksums": cs, "frame_bytes": int(r),
+                        "sha256_frame": hashlib.sha256(dst[:r].tobytes()).hexdigest(),
+                        **({"format_version": version} if version else {}),
+                        "outputs": [{"recipe": recipe, "elt_width": 0, "n": int(lens.size), "type": 8,
+                                     "bytes": int(content.size), "sha256": hashlib.sha256(content.tobytes()).hexdigest(),
+                                     "sha256_lens": hashlib.sha256(lens.astype("<u4").tobytes()).hexdigest()}]})
+    return out
 
 
 def main():

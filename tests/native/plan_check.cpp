@@ -66,6 +66,8 @@ int main(int argc, char** argv) {
           bad += !inR(t.data, t.len, "hash.data"); if (t.nbBlocks) bad += !inR(t.blockSums, t.nbBlocks*64, "hash.sums"); break; }
         case KIND_TOKENIZE: { auto t = ((TokenizeTask*)P(l.taskOff))[i];
           bad += !inR(t.out, t.n*t.w, "tok.out"); bad += !inR(t.idx, t.n*t.iw, "tok.idx"); bad += !inR(t.alphabet, (uint64_t)t.alphabetSize*t.w, "tok.alpha"); break; }
+        case KIND_WIDEN: { auto t = ((WidenTask*)P(l.taskOff))[i];
+          bad += !inR(t.src, t.n*t.w, "widen.src"); bad += !inR(t.dst, t.n*4, "widen.dst"); break; }
         case KIND_FLOATDEC: { auto t = ((FloatDecTask*)P(l.taskOff))[i];
           bad += !inR(t.out, t.n*(t.eltType?2:4), "flt.out"); bad += !inR(t.exponent, t.n, "flt.ex"); break; }
         case KIND_FLATPACK: { auto t = ((FlatpackTask*)P(l.taskOff))[i];

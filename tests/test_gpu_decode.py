@@ -270,15 +270,16 @@ def test_multi_output_frames(gpu_lib, manifest, manifest_multi):
 
     d = oz.DCtx()
     for m in manifest_multi:
-        outs = d.decompress_multi(read_frame(m["case"]))
+        outs = d.decompress_multi(read_frame(m["case"]), with_lengths=True)
         assert len(outs) == len(m["outputs"]), m["case"]
-        for (data, t, w), o in zip(outs, m["outputs"]):
+        for (data, t, w, lens), o in zip(outs, m["outputs"]):
             assert hashlib.sha256(data.tobytes()).hexdigest() == o["sha256"], m["case"]
-            assert w == (o["elt_width"] or 1) and t == (1 if o["elt_width"] == 0 else 4), m["case"]
+            assert t == o["type"] and w == (o["elt_width"] or 1), m["case"]
+            if t == 8:
+                assert hashlib.sha256(lens.astype("<u4").tobytes()).hexdigest() == o["sha256_lens"], m["case"]
     singles = manifest[:8]
     frames = [read_frame(m["case"]) for m in manifest_multi] + [read_frame(m["case"]) for m in singles]
-    layouts = [oz.frame_outputs(f) for f in frames]
-    extents = [l[-1]["offset"] + l[-1]["size"] for l in layouts]
+    layouts, extents = zip(*[oz.frame_outputs(f) for f in frames])
     dfr = [_dev(torch, f) for f in frames]
     outs = [torch.full((max(e, 1) + 64,), 0xAB, dtype=torch.uint8, device="cuda") for e in extents]
     s = torch.cuda.Stream()
@@ -296,6 +297,9 @@ def test_multi_output_frames(gpu_lib, manifest, manifest_multi):
             for l, w in zip(lay, want):
                 got = host[l["offset"]:l["offset"] + l["size"]].tobytes()
                 assert hashlib.sha256(got).hexdigest() == w["sha256"], (k, graph)
+                if l["type"] == 8:
+                    lens = host[l["lens_offset"]:l["lens_offset"] + 4 * l["count"]].tobytes()
+                    assert hashlib.sha256(lens).hexdigest() == w["sha256_lens"], (k, graph)
     m = next(m for m in manifest_multi if m["case"] == "multi3_ts_delta_flatpack")
     bad = bytearray(read_frame(m["case"]))
     bad[len(bad) // 2] ^= 0x01
@@ -306,8 +310,7 @@ def test_multi_output_frames(gpu_lib, manifest, manifest_multi):
     # (which covers the content checksum too)
     fr = read_frame("multi3_ts_delta_flatpack")
     bad = bytes(fr[:-6]) + bytes([fr[-6] ^ 0x10]) + bytes(fr[-5:])  # content, compressed checksums, end marker
-    lay = oz.frame_outputs(fr)
-    ext = lay[-1]["offset"] + lay[-1]["size"]
+    lay, ext = oz.frame_outputs(fr)
     dbad = _dev(torch, bad)
     o = torch.zeros(ext + 64, dtype=torch.uint8, device="cuda")
     bb = oz.GpuBatch(check_compressed=False)

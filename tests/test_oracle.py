@@ -48,17 +48,50 @@ def test_oracle_decodes_multi_output_frames(manifest_multi):
     """Frames of several outputs (output o in stream slot total-1-o of each
     block, the content checksum over the block's outputs one after another)."""
     assert any(len(m["outputs"]) > 14 for m in manifest_multi)  # extended output count
+    assert any(o["type"] == 8 for m in manifest_multi for o in m["outputs"])  # string outputs
     for m in manifest_multi:
-        outs = oracle.decompress_multi(read_frame(m["case"]))
+        outs = oracle.decompress_multi(read_frame(m["case"]), with_lengths=True)
         assert len(outs) == len(m["outputs"]), m["case"]
-        for (data, t, w), o in zip(outs, m["outputs"]):
+        for (data, t, w, lens), o in zip(outs, m["outputs"]):
             assert hashlib.sha256(data.tobytes()).hexdigest() == o["sha256"], m["case"]
-            assert w == (o["elt_width"] or 1) and t == (1 if o["elt_width"] == 0 else 4), m["case"]
+            assert t == o["type"] and w == (o["elt_width"] or 1), m["case"]
+            if t == 8:
+                assert hashlib.sha256(lens.astype("<u4").tobytes()).hexdigest() == o["sha256_lens"], m["case"]
     m = next(m for m in manifest_multi if m["case"] == "multi3_ts_delta_flatpack")
     fr = bytearray(read_frame(m["case"]))
     fr[len(fr) // 2] ^= 0x40
     with pytest.raises(ValueError):
         oracle.decompress_multi(bytes(fr))
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
+def test_oracle_matches_reference_on_string_frames():
+    """String inputs (separate_string_components, then content and lengths
+    through store, FSE or Huffman graphs) at format versions 15 to 23: the
+    oracle gives back the content and the lengths; wrong lengths are
+    corruption."""
+    import ctypes
+
+    ref = ctypes.CDLL(REF_DRIVER)
+    f = ref.ref_compress_string
+    f.restype = ctypes.c_int64
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                  ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(17)
+    words = [bytes(rng.integers(97, 123, int(rng.integers(0, 9))).astype(np.uint8)) for _ in range(100)]
+    for nstr in (1, 7, 3000):
+        strs = [words[i] for i in (rng.zipf(1.2, nstr) - 1) % len(words)]
+        content = np.frombuffer(b"".join(strs), np.uint8).copy()
+        lens = np.array([len(x) for x in strs], np.uint32)
+        for recipe in (100, 101, 102):
+            for v in (15, 20, 21, 23):
+                for cs in (0, 1):
+                    dst = np.zeros(content.size * 2 + lens.nbytes * 2 + 65536, np.uint8)
+                    r = f(recipe, content.ctypes.data if content.size else None, content.size, lens.ctypes.data,
+                          lens.size, dst.ctypes.data, dst.size, cs, v)
+                    assert r > 0, (recipe, v, nstr)
+                    (data, t, w, got), = oracle.decompress_multi(dst[:r].tobytes(), with_lengths=True)
+                    assert t == 8 and data.tobytes() == content.tobytes() and np.array_equal(got, lens), (recipe, v)
 
 
 @pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference library not built here")
