@@ -91,6 +91,10 @@ typedef enum {
     ZL_DParam_stickyParameters = 1,
     ZL_DParam_checkCompressedChecksum = 2,
     ZL_DParam_checkContentChecksum = 3,
+    /* batch API only (no counterpart in the reference): the frames decoded
+     * through Huffman and the others each split into this many runs of
+     * contiguous frames, decoded as parallel branches (1..8) */
+    OZL_DParam_partsPerKind = 1000,
 } ZL_DParam;
 
 typedef enum {

@@ -180,6 +180,7 @@ def frame_outputs(frame):
 DPARAM_STICKY = 1
 DPARAM_CHECK_COMPRESSED = 2
 DPARAM_CHECK_CONTENT = 3
+DPARAM_PARTS_PER_KIND = 1000  # OZL_DParam_partsPerKind
 
 
 class DCtx:
@@ -297,9 +298,11 @@ def decompress(frame):
 class GpuBatch:
     """Batched decode of many frames: one plan, one CUDA graph per run."""
 
-    def __init__(self, check_content=True, check_compressed=True):
+    def __init__(self, check_content=True, check_compressed=True, parts_per_kind=None):
         self._lib = library()
         self._h = self._lib.ozl_gpu_batch_create()
+        if parts_per_kind is not None:
+            _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_PARTS_PER_KIND, int(parts_per_kind)))
         if not check_content:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_CHECK_CONTENT, 2))
         if not check_compressed:

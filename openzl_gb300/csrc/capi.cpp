@@ -327,6 +327,10 @@ ZL_Report ozl_gpu_batch_setParameter(OZL_GpuBatch* b, ZL_DParam param, int value
         case ZL_DParam_checkCompressedChecksum: b->checkCompressed = value != ZL_TernaryParam_disable; break;
         case ZL_DParam_checkContentChecksum: b->checkContent = value != ZL_TernaryParam_disable; break;
         case ZL_DParam_stickyParameters: break;
+        case OZL_DParam_partsPerKind:
+            if (value < 1 || value > 8) return fail(ZL_ErrorCode_parameter_invalid);
+            b->partsPerKind = value;
+            break;
         default: return fail(ZL_ErrorCode_parameter_invalid);
     }
     return ok(0);

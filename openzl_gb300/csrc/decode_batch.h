@@ -53,11 +53,13 @@ cudaError_t prepareOnce();
 // decoded through Huffman and the others. Part 0 runs on the caller's
 // stream, the other parts on side streams forked from it and joined back by
 // events, so that a CUDA graph captured from the caller's stream holds the
-// parts as parallel branches (an FSE-heavy chain overlaps a Huffman-heavy
-// one). All parts share the plan's arena and parameter block; each has its
-// own descriptor pool and scratch.
+// parts as parallel branches: an FSE-heavy chain overlaps a Huffman-heavy
+// one, and each kind splits into runs of contiguous frames so that one run's
+// bandwidth-bound levels (numeric pipeline, checksums) overlap another run's
+// latency-bound entropy decoding. All parts share the plan's arena and
+// parameter block; each has its own descriptor pool and scratch.
 struct DecodeBatch {
-    static constexpr int kMaxParts = 2;
+    static constexpr int kMaxParts = 16;
     struct Part {
         DeviceLayout layout;
         DevBuf pool, scratch;
@@ -66,6 +68,7 @@ struct DecodeBatch {
     bool checkContent = true;
     bool checkCompressed = true;
     bool splitParts = true;
+    int partsPerKind = 1;     // runs per kind (OZL_DParam_partsPerKind)
     DecodePlan plan;
     std::vector<Part> parts;
     DevBuf arena, params, status;
@@ -171,23 +174,40 @@ struct DecodeBatch {
         dOuts.assign(reinterpret_cast<uint8_t* const*>(dO), reinterpret_cast<uint8_t* const*>(dO) + n);
         sizes.resize(n);
         for (size_t i = 0; i < n; i++) sizes[i] = size_t(plan.frames[i].decodedSize);
-        // parts: frames decoded through Huffman, then the others
+        // parts: the frames decoded through Huffman and the others, each kind
+        // in runs of contiguous frames of about equal decoded bytes
         std::vector<char> huf(n, 0);
         for (const PlanNode& nd : plan.nodes)
             if (!nd.dead && nd.id == 50 && nd.frame >= 0) huf[size_t(nd.frame)] = 1;
-        size_t nbHuf = 0;
-        for (char h : huf) nbHuf += h;
         parts.clear();
-        if (!splitParts || nbHuf == 0 || nbHuf == n) {
+        if (!splitParts) {
             parts.resize(1);
             parts[0].mask.assign(n, 1);
         } else {
-            parts.resize(2);
-            parts[0].mask.resize(n);
-            parts[1].mask.resize(n);
-            for (size_t i = 0; i < n; i++) {
-                parts[0].mask[i] = char(!huf[i]);
-                parts[1].mask[i] = huf[i];
+            for (char kind = 0; kind < 2; kind++) {
+                std::vector<size_t> fr;
+                uint64_t total = 0;
+                for (size_t i = 0; i < n; i++)
+                    if (huf[i] == kind) {
+                        fr.push_back(i);
+                        total += sizes[i];
+                    }
+                if (fr.empty()) continue;
+                size_t const g = std::min<size_t>(size_t(partsPerKind), fr.size());
+                size_t const first = parts.size();
+                parts.resize(first + g);
+                for (size_t k = 0; k < g; k++) parts[first + k].mask.assign(n, 0);
+                uint64_t acc = 0;
+                size_t k = 0;
+                for (size_t i : fr) {
+                    while (k + 1 < g && acc >= total * (k + 1) / g) k++;
+                    parts[first + k].mask[i] = 1;
+                    acc += sizes[i];
+                }
+            }
+            if (parts.empty()) {
+                parts.resize(1);
+                parts[0].mask.assign(n, 1);
             }
         }
         if (!arena.reserve(plan.arenaBytes) || !params.reserve(plan.params.size()) || !status.reserve(64)) {

@@ -328,3 +328,27 @@ def test_multi_output_frames(gpu_lib, manifest, manifest_multi):
     rep = lib.ZL_DCtx_decompressMultiTBuffer(d._h, arr, 1, f.ctypes.data, f.size)
     lib.ZL_TypedBuffer_free(arr[0])
     assert rep.code == 8
+
+
+@pytest.mark.parametrize("parts_per_kind", [1, 2, 4])
+def test_batch_parts_per_kind_keep_results(gpu_lib, manifest, parts_per_kind):
+    """Runs of frames decoded as parallel graph branches (each kind split into
+    1, 2 or 4 runs) give the same bytes, with and without the graph."""
+    import torch
+    import openzl_gb300 as oz
+
+    frames = [read_frame(m["case"]) for m in manifest]
+    dfr = [_dev(torch, f) for f in frames]
+    sizes = [oz.get_decompressed_size(f) for f in frames]
+    outs = [torch.zeros(max(n, 1) + 64, dtype=torch.uint8, device="cuda") for n in sizes]
+    s = torch.cuda.Stream()
+    b = oz.GpuBatch(parts_per_kind=parts_per_kind)
+    b.plan(frames, [d.data_ptr() for d in dfr], [o.data_ptr() for o in outs], sizes)
+    torch.cuda.synchronize()
+    for graph in (False, True):
+        for o in outs:
+            o.zero_()
+        b.run(s.cuda_stream, graph=graph)
+        b.check(s.cuda_stream)
+        for m, n, o in zip(manifest, sizes, outs):
+            assert hashlib.sha256(o[:n].cpu().numpy().tobytes()).hexdigest() == m["sha256_in"], (m["case"], graph)
