@@ -18,9 +18,12 @@
 #include "enc_engine.h"
 
 #include <algorithm>
+#include <atomic>
+#include <cstddef>
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <thread>
 
 #include "dec_exec.h"
 #include "enc_exec.h"
@@ -182,8 +185,51 @@ struct Front {
 
 } // namespace
 
+// Pinned host staging of the blobs the host computes for the device (coding
+// tables, Huffman weights, tokenize keys), uploaded in one copy.
+struct PinnedBuf {
+    uint8_t* p = nullptr;
+    size_t cap = 0;
+    ~PinnedBuf()
+    {
+        if (p) cudaFreeHost(p);
+    }
+    bool reserve(size_t bytes)
+    {
+        if (bytes <= cap) return true;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaHostAlloc(reinterpret_cast<void**>(&p), bytes, cudaHostAllocDefault) != cudaSuccess) return false;
+        cap = bytes;
+        return true;
+    }
+};
+
+// fn(i) for i < n on up to 16 host threads (chunks of 64 indices)
+template <class F>
+void parallelFor(size_t n, F fn)
+{
+    unsigned const hw = std::thread::hardware_concurrency();
+    unsigned const nt = std::min(16u, hw ? hw : 1u);
+    if (n < 256 || nt < 2) {
+        for (size_t i = 0; i < n; i++) fn(i);
+        return;
+    }
+    std::atomic<size_t> next{ 0 };
+    auto work = [&] {
+        for (size_t i; (i = next.fetch_add(64)) < n;)
+            for (size_t k = i; k < std::min(n, i + 64); k++) fn(k);
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt; t++) th.emplace_back(work);
+    work();
+    for (auto& x : th) x.join();
+}
+
 struct EncodeBatch::Impl {
     DevBuf bufA, bufE, bufF, bufSmall, bufT, bufW;
+    PinnedBuf stage;
     std::vector<Job> jobs;           // data chunks (discovery order), then nested weights jobs
     size_t nbDataJobs = 0;
     bool checksums = true;
@@ -1257,14 +1303,15 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             default: return true;
         }
     };
-    for (size_t j = 0; j < nj; j++) {
-        if (I.jobs[j].wide) {
-            if (!decide16(j)) { err = "16-bit Huffman table construction failed"; return 1; }
-            continue;
-        }
+    // 16-bit chunks first (they append nested jobs), then the others on
+    // host threads
+    for (size_t j = 0; j < nj; j++)
+        if (I.jobs[j].wide && !decide16(j)) { err = "16-bit Huffman table construction failed"; return 1; }
+    parallelFor(nj, [&](size_t j) {
+        if (I.jobs[j].wide) return;
         std::memcpy(I.jobs[j].hist.count, &hists[j * 256], 1024);
         decide(I.jobs[j]);
-    }
+    });
     // nested weights jobs (FSE graph of Huffman weights): decided on the host
     // histogram of the weights, encoded on the device with the data jobs
     for (size_t j = 0; j < I.jobs.size(); j++) {
@@ -1281,7 +1328,19 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         for (uint8_t x : W.hsrc) W.hist.count[x]++;
         J.weightsJob = int(I.jobs.size());
         I.jobs.push_back(std::move(W));
-        decide(I.jobs.back());
+    }
+    {
+        // the weights jobs created above, decided on host threads
+        size_t first = I.jobs.size();
+        for (size_t j = 0; j < I.jobs.size(); j++)
+            if (!I.jobs[j].hsrc.empty()) {
+                first = j;
+                break;
+            }
+        parallelFor(I.jobs.size() - first, [&](size_t k) {
+            Job& W = I.jobs[first + k];
+            if (!W.hsrc.empty()) decide(W);
+        });
     }
 
     // ---- phase E: entropy bitstreams -----------------------------------------------
@@ -1307,8 +1366,20 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             for (uint32_t k = 0; k < (n + kEncTile - 1) / kEncTile; k++) wideNumTiles.push_back(TileRef{ uint32_t(wideNumT.size()), k });
             wideNumT.push_back(t);
         };
-        auto layoutE = [&](Bump& b, bool real) {
+        // blobs computed on the host: device room from `stg`, uploaded in one copy
+        struct Up {
+            uint8_t* dev;
+            const void* host;
+            size_t bytes;
+        };
+        std::vector<Up> ups;
+        auto layoutE = [&](Bump& b, Bump& stg, bool real) {
             nbSizes = 0;
+            auto staged = [&](const void* host, size_t bytes, size_t room) -> uint8_t* {
+                uint8_t* d = stg.take(room, 16);
+                if (real && bytes) ups.push_back(Up{ d, host, bytes });
+                return d;
+            };
             for (size_t j = 0; j < I.jobs.size(); j++) {
                 Job& J = I.jobs[j];
                 if (J.wide) {
@@ -1320,8 +1391,8 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                         case ent::CC_TOK16: {
                             size_t const na = J.tokKeys.size();
                             J.idxOut = b.take(J.n + 64, 16);
-                            J.dKeys = b.take(2 * 256, 16);
-                            J.dIds = b.take(256, 16);
+                            J.dKeys = staged(J.tokKeys.data(), 2 * J.tokKeys.size(), 2 * 256);
+                            J.dIds = staged(J.tokIds.data(), J.tokIds.size(), 256);
                             I.jobs[size_t(J.idxJob)].dsrc = J.idxOut;
                             if (real) {
                                 Tok16Task t{ J.dsrc, J.idxOut, reinterpret_cast<const uint16_t*>(J.dKeys), J.dIds, uint32_t(J.n),
@@ -1331,7 +1402,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                                 tok16T.push_back(t);
                             }
                             if (ent::nextPow2Bits(uint64_t(J.maxSym16) + 1) < 16) {
-                                J.alphaStaged = b.take(2 * na + 16, 16);
+                                J.alphaStaged = staged(J.alphabet16.data(), J.alphabet16.size(), 2 * na + 16);
                                 J.alphaOut = b.take(J.alphaBytes + 64, 16);
                                 if (real) addWideNum(J.alphaStaged, J.alphaOut, na, J.alphaBits);
                             }
@@ -1339,8 +1410,8 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                         }
                         case ent::CC_HUF16: {
                             J.out = b.take(uint64_t(J.x4 ? 4 : 1) * J.streamCap, 16);
-                            J.dTable = b.take(2 * J.code16.size() + 16, 16);
-                            J.dNbBits = b.take(J.nbBits16.size() + 16, 16);
+                            J.dTable = staged(J.code16.data(), 2 * J.code16.size(), 2 * J.code16.size() + 16);
+                            J.dNbBits = staged(J.nbBits16.data(), J.nbBits16.size(), J.nbBits16.size() + 16);
                             J.sizeSlot = nbSizes;
                             nbSizes += 8;
                             if (real)
@@ -1352,15 +1423,14 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                     }
                     continue;
                 }
-                if (!J.hsrc.empty()) {
-                    uint8_t* p = b.take(J.hsrc.size() + 16, 16);
-                    J.dstaged = p;
-                }
+                if (!J.hsrc.empty()) J.dstaged = staged(J.hsrc.data(), J.hsrc.size(), J.hsrc.size() + 16);
                 const uint8_t* src = J.hsrc.empty() ? J.dsrc : J.dstaged;
                 switch (J.codec) {
                     case ent::CC_FSE: {
                         J.out = b.take(J.n + J.n / 128 + 512, 16);
-                        J.dTable = b.take(sizeof(ent::FseCTable), 16);
+                        // the kernel reads the state table up to 2^tableLog entries
+                        J.dTable = staged(J.fct.get(), offsetof(ent::FseCTable, state) + (2u << J.tl),
+                                          sizeof(ent::FseCTable));
                         J.sizeSlot = nbSizes++;
                         if (real) fseT.push_back(FseEncTask{ src, J.out, J.dTable, uint32_t(J.n), J.sizeSlot, J.nbStates, J.tl });
                         break;
@@ -1368,7 +1438,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                     case ent::CC_HUF: {
                         uint32_t const seg = uint32_t((J.n + 3) / 4);
                         J.out = b.take(J.x4 ? 16 + 4ull * hufEncStreamCap(seg) : J.n + J.n / 8 + 64, 16);
-                        J.dTable = b.take(sizeof(ent::HufCTable), 16);
+                        J.dTable = staged(J.hct.get(), sizeof(ent::HufCTable), sizeof(ent::HufCTable));
                         J.sizeSlot = nbSizes;
                         nbSizes += 4;
                         if (real) hufT.push_back(HufEncTask{ src, J.out, J.dTable, uint32_t(J.n), J.sizeSlot, J.x4 ? 1u : 0u });
@@ -1377,7 +1447,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                     case ent::CC_BITPACK:
                     case ent::CC_FLATPACK: {
                         J.out = b.take(J.packBytes + 64, 16);
-                        uint8_t* map = J.codec == ent::CC_FLATPACK ? b.take(256, 16) : nullptr;
+                        uint8_t* map = J.codec == ent::CC_FLATPACK ? staged(J.map, 256, 256) : nullptr;
                         J.dTable = map;
                         if (real && J.n) {
                             PackTask t{ src, J.out, map, J.n, J.packBits, 0 };
@@ -1391,8 +1461,8 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                 }
             }
         };
-        Bump sz;
-        layoutE(sz, false);
+        Bump sz, szStage;
+        layoutE(sz, szStage, false);
         size_t const taskBytes = 4096 + I.jobs.size() * (sizeof(FseEncTask) + sizeof(HufEncTask) + sizeof(PackTask)
                                                          + sizeof(Tok16Task) + 2 * sizeof(EncNumTask) + sizeof(Huf16EncTask));
         size_t tilesGuess = 0;
@@ -1400,10 +1470,19 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             if (J.codec == ent::CC_BITPACK || J.codec == ent::CC_FLATPACK) tilesGuess += (J.n + kEncTile - 1) / kEncTile;
             if (J.codec == ent::CC_TOK16) tilesGuess += 2 * ((J.n + kEncTile - 1) / kEncTile) + 1;
         }
-        size_t const total = sz.used + taskBytes + tilesGuess * sizeof(TileRef) + (nbSizes + 16) * 4 + 1024;
-        if (!I.bufE.reserve(total)) { err = "device allocation failed"; return 70; }
+        size_t const stageOff = (sz.used + taskBytes + tilesGuess * sizeof(TileRef) + (nbSizes + 16) * 4 + 1024 + 255)
+                & ~size_t(255);
+        size_t const total = stageOff + szStage.used + 256;
+        if (!I.bufE.reserve(total) || !I.stage.reserve(szStage.used + 256)) { err = "allocation failed"; return 70; }
         Bump b{ I.bufE.data(), 0 };
-        layoutE(b, true);
+        Bump stg{ I.bufE.data() + stageOff, 0 };
+        layoutE(b, stg, true);
+        if (b.used > stageOff) { err = "encode layout overflow"; return 1; }
+        parallelFor(ups.size(), [&](size_t k) {
+            std::memcpy(I.stage.p + (ups[k].dev - stg.base), ups[k].host, ups[k].bytes);
+        });
+        if (stg.used)
+            cudaMemcpyAsync(stg.base, I.stage.p, stg.used, cudaMemcpyHostToDevice, st);
         auto* dFse = reinterpret_cast<FseEncTask*>(b.take(fseT.size() * sizeof(FseEncTask) + 1));
         auto* dHuf = reinterpret_cast<HufEncTask*>(b.take(hufT.size() * sizeof(HufEncTask) + 1));
         auto* dPack = reinterpret_cast<PackTask*>(b.take(packT.size() * sizeof(PackTask) + 1));
@@ -1414,26 +1493,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         auto* dWideNum = reinterpret_cast<EncNumTask*>(b.take(wideNumT.size() * sizeof(EncNumTask) + 1));
         auto* dWideNumTiles = reinterpret_cast<TileRef*>(b.take(wideNumTiles.size() * sizeof(TileRef) + 1));
         auto* dHuf16 = reinterpret_cast<Huf16EncTask*>(b.take(huf16T.size() * sizeof(Huf16EncTask) + 1));
-        // uploads: staged weights, tables, maps, tasks
-        for (Job& J : I.jobs) {
-            if (J.wide) {
-                if (J.codec == ent::CC_TOK16) {
-                    cudaMemcpyAsync(const_cast<uint8_t*>(J.dKeys), J.tokKeys.data(), 2 * J.tokKeys.size(), cudaMemcpyHostToDevice, st);
-                    cudaMemcpyAsync(const_cast<uint8_t*>(J.dIds), J.tokIds.data(), J.tokIds.size(), cudaMemcpyHostToDevice, st);
-                    if (J.alphaStaged)
-                        cudaMemcpyAsync(const_cast<uint8_t*>(J.alphaStaged), J.alphabet16.data(), J.alphabet16.size(), cudaMemcpyHostToDevice, st);
-                }
-                if (J.codec == ent::CC_HUF16) {
-                    cudaMemcpyAsync(const_cast<uint8_t*>(J.dTable), J.code16.data(), 2 * J.code16.size(), cudaMemcpyHostToDevice, st);
-                    cudaMemcpyAsync(const_cast<uint8_t*>(J.dNbBits), J.nbBits16.data(), J.nbBits16.size(), cudaMemcpyHostToDevice, st);
-                }
-                continue;
-            }
-            if (!J.hsrc.empty()) cudaMemcpyAsync(const_cast<uint8_t*>(J.dstaged), J.hsrc.data(), J.hsrc.size(), cudaMemcpyHostToDevice, st);
-            if (J.codec == ent::CC_FSE) cudaMemcpyAsync(const_cast<uint8_t*>(J.dTable), J.fct.get(), sizeof(ent::FseCTable), cudaMemcpyHostToDevice, st);
-            if (J.codec == ent::CC_HUF) cudaMemcpyAsync(const_cast<uint8_t*>(J.dTable), J.hct.get(), sizeof(ent::HufCTable), cudaMemcpyHostToDevice, st);
-            if (J.codec == ent::CC_FLATPACK) cudaMemcpyAsync(const_cast<uint8_t*>(J.dTable), J.map, 256, cudaMemcpyHostToDevice, st);
-        }
+        // uploads: the tasks (the staged blobs went up above)
         if (!fseT.empty()) cudaMemcpyAsync(dFse, fseT.data(), fseT.size() * sizeof(FseEncTask), cudaMemcpyHostToDevice, st);
         if (!hufT.empty()) cudaMemcpyAsync(dHuf, hufT.data(), hufT.size() * sizeof(HufEncTask), cudaMemcpyHostToDevice, st);
         if (!packT.empty()) {
