@@ -88,7 +88,20 @@ struct Piece {
 
 enum : int { M_FSE = 0, M_HUF, M_CONSTANT, M_FLATPACK, M_BITPACK, M_ANY };
 
+// Discovery's record of one entropy job.
+struct JobSeed {
+    const uint8_t* dsrc;
+    uint64_t n;
+    int mode;
+    bool wide;
+};
+
 struct Job {
+    // arrays without initializers are written before they are read, so
+    // sizing the job list does not zero them
+    Job() {}
+    Job(Job&&) = default;
+    Job& operator=(Job&&) = default;
     const uint8_t* dsrc = nullptr;    // device content
     std::vector<uint8_t> hsrc;        // host content (Huffman weights)
     const uint8_t* dstaged = nullptr; // device copy of hsrc
@@ -248,6 +261,7 @@ namespace {
 struct Engine {
     bool discover;
     std::vector<Job>* jobs;
+    std::vector<JobSeed>* seeds; // discovery: the frame's jobs in order
     size_t* jobCursor;          // next data-job index (same order in both modes)
     std::vector<RStream> s;
     std::vector<RNode> nd;
@@ -370,12 +384,8 @@ struct Engine {
         if (explicitJob >= 0) return &(*jobs)[size_t(explicitJob)];
         size_t const j = (*jobCursor)++;
         if (discover) {
-            Job job;
-            job.n = s[sid].n;
-            job.mode = mode;
-            job.dsrc = s[sid].pieces.empty() ? nullptr : s[sid].pieces[0].dev;
-            job.wide = s[sid].w == 2;
-            jobs->push_back(std::move(job));
+            seeds->push_back(JobSeed{ s[sid].pieces.empty() ? nullptr : s[sid].pieces[0].dev, s[sid].n, mode,
+                                      s[sid].w == 2 });
             return nullptr;
         }
         return &(*jobs)[j];
@@ -1114,13 +1124,33 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             default: E.pipeline(r, in);
         }
     };
+    // frames in parallel, each recording its jobs; then one job list in
+    // frame order
+    std::vector<size_t> frameJobStart(nf + 1, 0);
     {
-        size_t cursor = 0;
-        for (size_t f = 0; f < nf; f++) {
+        std::vector<std::vector<JobSeed>> seeds(nf);
+        std::vector<int> errs(nf, 0);
+        parallelFor(nf, [&](size_t f) {
+            size_t cursor = 0;
             Engine E;
+            E.seeds = &seeds[f];
             runFrame(f, true, &cursor, E);
-            if (E.err) { err = "graph not supported on the GPU path"; return E.err; }
-        }
+            errs[f] = E.err;
+        });
+        for (size_t f = 0; f < nf; f++)
+            if (errs[f]) { err = "graph not supported on the GPU path"; return errs[f]; }
+        for (size_t f = 0; f < nf; f++) frameJobStart[f + 1] = frameJobStart[f] + seeds[f].size();
+        I.jobs.clear();
+        I.jobs.resize(frameJobStart[nf]);
+        parallelFor(nf, [&](size_t f) {
+            for (size_t k = 0; k < seeds[f].size(); k++) {
+                Job& J = I.jobs[frameJobStart[f] + k];
+                J.dsrc = seeds[f][k].dsrc;
+                J.n = seeds[f][k].n;
+                J.mode = seeds[f][k].mode;
+                J.wide = seeds[f][k].wide;
+            }
+        });
         I.nbDataJobs = I.jobs.size();
     }
 
@@ -1576,11 +1606,15 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
     };
     std::vector<FrameOut> outs(nf);
     {
-        size_t cursor = 0;
-        for (size_t f = 0; f < nf; f++) {
+        // frames in parallel, each from its first job; the first failing
+        // frame's error is reported
+        std::vector<int> rcs(nf, 0);
+        std::vector<const char*> msgs(nf, nullptr);
+        parallelFor(nf, [&](size_t f) {
+            size_t cursor = frameJobStart[f];
             Engine E;
             runFrame(f, false, &cursor, E);
-            if (E.err) { err = "graph replay failed"; return E.err; }
+            if (E.err) { rcs[f] = E.err; msgs[f] = "graph replay failed"; return; }
             FrameOut& O = outs[f];
             std::vector<uint8_t>& h = O.head;
             const RStream& in0 = E.s[0];
@@ -1627,16 +1661,18 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                         O.stored.push_back(p);
                         have += p.bytes;
                     }
-                    if (have != E.s[i].bytes()) { err = "internal: stored stream without content"; return 80; }
+                    if (have != E.s[i].bytes()) { rcs[f] = 80; msgs[f] = "internal: stored stream without content"; return; }
                 }
             uint64_t tot = h.size();
             for (const Piece& p : O.stored) tot += p.bytes;
             tot += checksums ? 8 : 0;
             tot += 1;
             O.total = tot;
-            if (tot > caps[f]) { err = "destination too small"; return 5; }
+            if (tot > caps[f]) { rcs[f] = 5; msgs[f] = "destination too small"; return; }
             sizes[f] = tot;
-        }
+        });
+        for (size_t f = 0; f < nf; f++)
+            if (rcs[f]) { err = msgs[f]; return rcs[f]; }
     }
 
     // ---- phase G: assembly and checksums -----------------------------------------
