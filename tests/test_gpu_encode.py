@@ -103,3 +103,34 @@ def test_gpu_encode_then_gpu_decode(gpu_lib):
     for (_, a, _), dst, sz in zip(arrs, dsts, sizes):
         frame = dst[:sz].cpu().numpy()
         assert d.decompress(frame).tobytes() == a.tobytes()
+
+
+def test_gpu_frames_equal_oracle_frames_many_frames(gpu_lib):
+    """600 frames in one call: graph discovery, decisions and replay run on
+    host threads (from 256 frames or jobs) and the frames stay identical to
+    the oracle's."""
+    import torch
+    import openzl_gb300 as oz
+
+    rng = np.random.default_rng(77)
+    cases = []
+    for k in range(600):
+        recipe = (1, 2, 3, 4, 7, 8, 17, 9)[k % 8]
+        n = int(rng.integers(2, 40000))
+        if recipe in (7, 8, 17):
+            cases.append((recipe, (rng.zipf(1.25, n) % int(rng.integers(2, 256))).astype(np.uint8), 0))
+        else:
+            dt, w = [(np.uint8, 1), (np.uint16, 2), (np.uint32, 4), (np.uint64, 8)][k % 4]
+            cases.append((recipe, _walk(rng, n, dt, int(rng.integers(1, 3000))), w))
+    enc = oz.GpuEncoder()
+    srcs = [torch.from_numpy(a.view(np.uint8).copy()).cuda() for _, a, _ in cases]
+    caps = [enc.bound(a.nbytes) for _, a, _ in cases]
+    dsts = [torch.zeros(c, dtype=torch.uint8, device="cuda") for c in caps]
+    sizes = enc.compress_batch([s.data_ptr() for s in srcs], [a.size if w else a.nbytes for _, a, w in cases],
+                               [w for _, _, w in cases], [r for r, _, _ in cases], [d.data_ptr() for d in dsts],
+                               caps, checksums=True)
+    bad = []
+    for k, ((recipe, arr, w), d, sz) in enumerate(zip(cases, dsts, sizes)):
+        if d[:sz].cpu().numpy().tobytes() != oracle.compress(recipe, arr, w).tobytes():
+            bad.append((k, recipe, w, arr.size))
+    assert not bad, bad[:10]
