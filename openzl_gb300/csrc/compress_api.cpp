@@ -117,8 +117,8 @@ struct ZL_Compressor_s {
                 out += ")";
                 return true;
             case TOKENIZE: {
-                if (g.type != ZL_Type_numeric || g.sort) return false; // numeric, first-occurrence order
-                out += "tokenize(";
+                if (g.type != ZL_Type_numeric) return false; // numeric tokenize
+                out += g.sort ? "tokenize_sorted(" : "tokenize(";
                 if (!flatten(g.succ[0], out, depth + 1)) return false;
                 out += ",";
                 if (!flatten(g.succ[1], out, depth + 1)) return false;
@@ -190,6 +190,7 @@ int recipeOf(const std::string& chain)
         { "FLATPACK", ozl::RC_FLATPACK },
         { "BITPACK", ozl::RC_BITPACK },
         { "tokenize(STORE,bitpack>HUFFMAN)", ozl::RC_TOKENIZE },
+        { "tokenize_sorted(STORE,bitpack>HUFFMAN)", ozl::RC_TOKENIZE_SORTED },
         { "bf16(STORE,FSE)", ozl::RC_BF16 },
     };
     auto it = table.find(chain);
@@ -200,7 +201,8 @@ bool numericRecipe(int r)
 {
     return r == ozl::RC_DZ_TSPLIT_FSE || r == ozl::RC_DZ_BITPACK_HUF || r == ozl::RC_D_TSPLIT_FSE
             || r == ozl::RC_D_BITPACK_HUF || r == ozl::RC_DELTA_STORE || r == ozl::RC_ZIGZAG_STORE
-            || r == ozl::RC_BITPACK_STORE || r == ozl::RC_TSPLIT_STORE || r == ozl::RC_TOKENIZE || r == ozl::RC_BF16;
+            || r == ozl::RC_BITPACK_STORE || r == ozl::RC_TSPLIT_STORE || r == ozl::RC_TOKENIZE || r == ozl::RC_TOKENIZE_SORTED
+            || r == ozl::RC_BF16;
 }
 
 ZL_Report compressOne(ZL_CCtx* c, void* dst, size_t cap, const ZL_TypedRef& in)

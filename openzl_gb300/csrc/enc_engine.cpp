@@ -241,7 +241,7 @@ void parallelFor(size_t n, F fn)
 }
 
 struct EncodeBatch::Impl {
-    DevBuf bufA, bufE, bufF, bufSmall, bufT, bufW;
+    DevBuf bufA, bufE, bufF, bufSmall, bufT, bufW, bufR;
     PinnedBuf stage;
     std::vector<Job> jobs;           // data chunks (discovery order), then nested weights jobs
     size_t nbDataJobs = 0;
@@ -804,7 +804,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             fr.n = F.n;
             continue;
         }
-        if (r == RC_TOKENIZE) {
+        if (r == RC_TOKENIZE || r == RC_TOKENIZE_SORTED) {
             if (F.n >= (1ull << 32)) { err = "tokenize input too large"; return 4; }
             fr.special = 2;
             fr.n = F.n;
@@ -1006,6 +1006,67 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             launchTokEmit(reinterpret_cast<const TokTask*>(dTasks), reinterpret_cast<const TileRef*>(dTiles),
                           uint32_t(tiles.size()), st);
             launches_++;
+            // sorted alphabets (encode_tokenize_binding.c:185-193): the
+            // first-occurrence alphabet comes back, is sorted here by increasing
+            // unsigned value, goes back, and the indices are renumbered on the
+            // device through each first-occurrence rank's sorted position
+            std::vector<size_t> sk;
+            for (size_t k = 0; k < tt.size(); k++)
+                if (frames[tokFrames[k]].recipe == RC_TOKENIZE_SORTED && fronts[tokFrames[k]].na) sk.push_back(k);
+            if (!sk.empty()) {
+                std::vector<std::vector<uint8_t>> alpha(sk.size());
+                for (size_t i = 0; i < sk.size(); i++) {
+                    const TokTask& t = tt[sk[i]];
+                    alpha[i].resize(fronts[tokFrames[sk[i]]].na * t.w);
+                    cudaMemcpyAsync(alpha[i].data(), t.alphabet, alpha[i].size(), cudaMemcpyDeviceToHost, st);
+                }
+                if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in tokenize"; return 1; }
+                std::vector<std::vector<uint32_t>> rankOf(sk.size());
+                uint64_t rankBytes = 0;
+                std::vector<TileRef> rtiles;
+                for (size_t i = 0; i < sk.size(); i++) {
+                    const TokTask& t = tt[sk[i]];
+                    size_t const na = fronts[tokFrames[sk[i]]].na;
+                    std::vector<uint64_t> val(na);
+                    for (size_t j = 0; j < na; j++) {
+                        uint64_t v = 0;
+                        for (uint32_t b = 0; b < t.w; b++) v |= uint64_t(alpha[i][j * t.w + b]) << (8 * b);
+                        val[j] = v;
+                    }
+                    std::vector<uint32_t> order(na);
+                    for (size_t j = 0; j < na; j++) order[j] = uint32_t(j);
+                    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return val[a] < val[b]; });
+                    rankOf[i].resize(na);
+                    std::vector<uint8_t> sorted(na * t.w);
+                    for (size_t j = 0; j < na; j++) {
+                        rankOf[i][order[j]] = uint32_t(j);
+                        std::memcpy(&sorted[j * t.w], &alpha[i][size_t(order[j]) * t.w], t.w);
+                    }
+                    alpha[i].swap(sorted);
+                    rankBytes += (4 * na + 255) & ~uint64_t(255);
+                    for (uint32_t k = 0; k < (t.n + kEncTile - 1) / kEncTile; k++) rtiles.push_back(TileRef{ uint32_t(i), k });
+                }
+                size_t const need = rankBytes + sk.size() * sizeof(RemapTask) + rtiles.size() * sizeof(TileRef) + 1024;
+                if (!I.bufR.reserve(need)) { err = "device allocation failed"; return 70; }
+                Bump rb{ I.bufR.data(), 0 };
+                std::vector<RemapTask> rt(sk.size());
+                for (size_t i = 0; i < sk.size(); i++) {
+                    const TokTask& t = tt[sk[i]];
+                    auto* dRank = reinterpret_cast<uint32_t*>(rb.take(4 * rankOf[i].size(), 256));
+                    cudaMemcpyAsync(dRank, rankOf[i].data(), 4 * rankOf[i].size(), cudaMemcpyHostToDevice, st);
+                    cudaMemcpyAsync(t.alphabet, alpha[i].data(), alpha[i].size(), cudaMemcpyHostToDevice, st);
+                    rt[i] = RemapTask{ t.idx, dRank, t.n, t.iw };
+                }
+                auto* dRt = reinterpret_cast<RemapTask*>(rb.take(rt.size() * sizeof(RemapTask)));
+                auto* dRtiles = reinterpret_cast<TileRef*>(rb.take(rtiles.size() * sizeof(TileRef)));
+                cudaMemcpyAsync(dRt, rt.data(), rt.size() * sizeof(RemapTask), cudaMemcpyHostToDevice, st);
+                cudaMemcpyAsync(dRtiles, rtiles.data(), rtiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
+                launchRemap(dRt, dRtiles, uint32_t(rtiles.size()), st);
+                launches_++;
+                // the host copies above are pageable: they complete before the
+                // calls return, so the vectors may go out of scope
+                if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in tokenize"; return 1; }
+            }
         }
     }
 
@@ -1106,7 +1167,8 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         if (E.s[in].bytes() < kMinStream || r == RC_STORE) { E.runSuccessor(Engine::G_STORE, in); return; }
         switch (r) {
             case RC_FSE: E.runSuccessor(Engine::G_FSE, in); break;
-            case RC_TOKENIZE: E.runSuccessor(Engine::G_TOKENIZE, in); break;
+            case RC_TOKENIZE:
+            case RC_TOKENIZE_SORTED: E.runSuccessor(Engine::G_TOKENIZE, in); break;
             case RC_BF16: E.runSuccessor(Engine::G_BF16, in); break;
             case RC_HUFFMAN: E.runSuccessor(Engine::G_HUF, in); break;
             case RC_ENTROPY: E.runSuccessor(Engine::G_ENTROPY, in); break;

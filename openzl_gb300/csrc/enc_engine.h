@@ -28,6 +28,7 @@ enum Recipe : int {
     RC_CONSTANT = 13,
     RC_FLATPACK = 14,
     RC_BITPACK = 15,
+    RC_TOKENIZE_SORTED = 16, // tokenize with the alphabet in increasing order
     RC_ENTROPY = 17,        // ZL_GRAPH_ENTROPY: FSE or Huffman per chunk (EBM_any)
 };
 

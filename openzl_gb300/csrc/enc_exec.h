@@ -26,6 +26,8 @@ void launchHist16(const Hist16Task* t, const TileRef* tiles, uint32_t nbTiles, c
 void launchTok16(const Tok16Task* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
 // 16-bit-symbol Huffman streams, one thread per stream.
 void launchHuf16Enc(const Huf16EncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);
+// Sorted tokenize: indices renumbered to the sorted alphabet.
+void launchRemap(const RemapTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
 // Tokenize, the alphabet and the indices (iw set in the tasks).
 void launchTokEmit(const TokTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
 

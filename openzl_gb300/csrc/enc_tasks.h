@@ -132,6 +132,15 @@ struct Huf16EncTask {
     uint32_t n, streamCap, sizeSlot, x4;
 };
 
+// Sorted tokenize: indices in first-occurrence order renumbered to the
+// sorted alphabet's order, idx[i] = rankOf[idx[i]].
+struct RemapTask {
+    uint8_t* idx;
+    const uint32_t* rankOf;
+    uint64_t n;
+    uint32_t iw;
+};
+
 constexpr uint32_t kEncTile = 4096; // elements per numeric/pack tile (32 per thread)
 
 } // namespace ozl

@@ -425,6 +425,16 @@ __global__ void __launch_bounds__(128) kHuf16Enc(const Huf16EncTask* __restrict_
     sizes[t.sizeSlot + 4 + k] = uint32_t(bits / 8);
 }
 
+__global__ void __launch_bounds__(256) kRemap(const RemapTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
+{
+    TileRef const tr = tiles[blockIdx.x];
+    RemapTask const t = tasks[tr.task];
+    uint64_t const e0 = uint64_t(tr.tile) * kEncTile;
+    uint64_t const e1 = min(t.n, e0 + kEncTile);
+    for (uint64_t i = e0 + threadIdx.x; i < e1; i += blockDim.x)
+        stW(t.idx + i * t.iw, t.rankOf[ldW(t.idx + i * t.iw, t.iw)], t.iw);
+}
+
 __global__ void kPut(const PutTask* __restrict__ tasks, uint32_t n)
 {
     uint32_t const i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -684,6 +694,11 @@ void launchTok16(const Tok16Task* t, const TileRef* tiles, uint32_t nbTiles, cud
 void launchHuf16Enc(const Huf16EncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s)
 {
     if (n) kHuf16Enc<<<(4 * n + 127) / 128, 128, 0, s>>>(t, n, sizes);
+}
+
+void launchRemap(const RemapTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s)
+{
+    if (nbTiles) kRemap<<<nbTiles, 256, 0, s>>>(t, tiles);
 }
 
 void launchTokEmit(const TokTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s)

@@ -45,8 +45,8 @@ def _graph(oz, comp, recipe):
         return a.GRAPH_BITPACK
     if recipe == 17:
         return a.GRAPH_ENTROPY
-    if recipe == 5:
-        return comp.tokenize(a.TYPE_NUMERIC, False, a.GRAPH_STORE, comp.node(a.NODE_BITPACK_INT, a.GRAPH_HUFFMAN))
+    if recipe in (5, 16):
+        return comp.tokenize(a.TYPE_NUMERIC, recipe == 16, a.GRAPH_STORE, comp.node(a.NODE_BITPACK_INT, a.GRAPH_HUFFMAN))
     if recipe == 6:
         return comp.node_multi(a.NODE_BFLOAT16_DECONSTRUCT, [a.GRAPH_STORE, a.GRAPH_FSE])
     raise ValueError(recipe)
@@ -63,6 +63,7 @@ def _cases():
     keys = rng.integers(0, 2**31, 10000).astype(np.uint32)
     for n in (50, 40000):
         c.append((5, keys[(rng.zipf(1.1, n) - 1) % keys.size]))
+        c.append((16, keys[(rng.zipf(1.1, n) - 1) % keys.size]))
     c.append((6, (rng.normal(0, 0.02, 30000).astype(np.float32).view(np.uint32) >> 16).astype(np.uint16)))
     for recipe in (0, 7, 8, 13, 14, 15):
         for n in (3, 5000, 120000):

@@ -36,6 +36,12 @@ def _cases(seed):
         idx = (rng.zipf(1.1, n) - 1) % keys.size
         c.append((5, keys[idx].astype(np.uint32), 4))
     c.append((5, (rng.integers(0, 200, 50000)).astype(np.uint16), 2))
+    # sorted alphabet (recipe 16): indices renumbered after a host sort
+    for n in (3, 700, 20000, 300000):
+        idx = (rng.zipf(1.1, n) - 1) % keys.size
+        c.append((16, keys[idx].astype(np.uint32), 4))
+    c.append((16, (rng.integers(0, 300, 50000)).astype(np.uint16), 2))
+    c.append((16, (rng.integers(0, 2**40, 3000)).astype(np.uint64), 8))
     c.append((5, (rng.integers(0, 2**40, 3000)).astype(np.uint64), 8))
     for n in (4, 900, 70000):
         bf = (rng.normal(0, 0.02, n).astype(np.float32).view(np.uint32) >> 16).astype(np.uint16)
