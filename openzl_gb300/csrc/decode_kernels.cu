@@ -1058,14 +1058,14 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
     auto sym = [&](uint32_t st) -> uint32_t { return symOf[st]; };
     auto nbOf = [](uint32_t e) -> uint32_t { return e & 15u; };
     auto nextOf = [](uint32_t e, uint32_t f) -> uint32_t { return (e >> 4) + f; };
-    // two transitions whose fields (at most 24 bits) start o bits below the
-    // top of the window; returns the bits they read
-    auto pair = [&](int32_t o, uint32_t ea, uint32_t eb, uint32_t& sa, uint32_t& sb) -> uint32_t {
-        uint32_t const w = br.window(o);
-        uint32_t const na = nbOf(ea), nb = nbOf(eb);
-        sa = nextOf(ea, __funnelshift_l(w, 0u, na));
-        sb = nextOf(eb, __funnelshift_l(w << na, 0u, nb));
-        return na + nb;
+    // one transition: its field is the top bits of the 64-bit register window
+    // (hi, lo), which then shifts them out; four fields take at most 48 bits
+    auto take = [](uint32_t e, uint32_t& hi, uint32_t& lo) -> uint32_t {
+        uint32_t const nb = e & 15u;
+        uint32_t const f = __funnelshift_l(hi, 0u, nb);
+        hi = __funnelshift_l(lo, hi, nb);
+        lo <<= nb;
+        return (e >> 4) + f;
     };
     // one symbol from st0, then the states rotate
     auto single = [&](uint32_t i) {
@@ -1085,24 +1085,33 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
     if (nst == 4) {
         for (; i + 4 <= lastTr; i += 4) {
             br.prepare();
+            // the 64 bits below pos, left-aligned (g is in [0, 32])
+            uint32_t hi = __funnelshift_lc(br.b, br.a, uint32_t(br.g));
+            uint32_t lo = __funnelshift_lc(br.c, br.b, uint32_t(br.g));
             uint32_t const ea = ent(st0), eb = ent(st1), ec = ent(st2), ed = ent(st3);
             uint32_t const ya = sym(st0), yb = sym(st1), yc = sym(st2), yd = sym(st3);
-            uint32_t const n1 = pair(br.g, ea, eb, st0, st1);
-            uint32_t const n2 = pair(br.g + int32_t(n1), ec, ed, st2, st3);
-            br.advance(int32_t(n1 + n2));
+            st0 = take(ea, hi, lo);
+            st1 = take(eb, hi, lo);
+            st2 = take(ec, hi, lo);
+            st3 = take(ed, hi, lo);
+            br.advance(int32_t(nbOf(ea) + nbOf(eb) + nbOf(ec) + nbOf(ed)));
             *reinterpret_cast<uint32_t*>(out + i) =
                 __byte_perm(__byte_perm(ya, yb, 0x0040), __byte_perm(yc, yd, 0x0040), 0x5410);
         }
     } else {
         for (; i + 4 <= lastTr; i += 4) {
             br.prepare();
+            uint32_t hi = __funnelshift_lc(br.b, br.a, uint32_t(br.g));
+            uint32_t lo = __funnelshift_lc(br.c, br.b, uint32_t(br.g));
             uint32_t const ea = ent(st0), eb = ent(st1);
             uint32_t const ya = sym(st0), yb = sym(st1);
-            uint32_t const n1 = pair(br.g, ea, eb, st0, st1);
+            st0 = take(ea, hi, lo);
+            st1 = take(eb, hi, lo);
             uint32_t const ec = ent(st0), ed = ent(st1);
             uint32_t const yc = sym(st0), yd = sym(st1);
-            uint32_t const n2 = pair(br.g + int32_t(n1), ec, ed, st0, st1);
-            br.advance(int32_t(n1 + n2));
+            st0 = take(ec, hi, lo);
+            st1 = take(ed, hi, lo);
+            br.advance(int32_t(nbOf(ea) + nbOf(eb) + nbOf(ec) + nbOf(ed)));
             *reinterpret_cast<uint32_t*>(out + i) =
                 __byte_perm(__byte_perm(ya, yb, 0x0040), __byte_perm(yc, yd, 0x0040), 0x5410);
         }
