@@ -8,9 +8,10 @@
  * the GPU path unchanged. The ozl_gpu_* functions are additions for callers
  * that hold their data on the device (batched and serving paths).
  *
- * Frames are OpenZL wire format 21-23 (chunked block format). Older frames
- * and codecs outside the numeric path are rejected with an error; there is
- * no CPU fallback.
+ * Frames of OpenZL wire format versions 8-23 decode; the encoder writes
+ * version 23. Codecs outside the numeric path (and the deprecated entropy
+ * codecs of versions 8-14) are rejected with an error; there is no CPU
+ * fallback.
  */
 #ifndef OPENZL_GB300_H
 #define OPENZL_GB300_H
@@ -109,6 +110,10 @@ ZL_DCtx* ZL_DCtx_create(void);
 void ZL_DCtx_free(ZL_DCtx* dctx);
 /* zl_decompress.h:140 */
 ZL_Report ZL_DCtx_setParameter(ZL_DCtx* dctx, ZL_DParam param, int value);
+/* zl_decompress.h:149: the value set, 0 when unset */
+int ZL_DCtx_getParameter(const ZL_DCtx* dctx, ZL_DParam param);
+/* zl_decompress.h:159: every parameter back to its default */
+ZL_Report ZL_DCtx_resetParameters(ZL_DCtx* dctx);
 /* zl_decompress.h:188 */
 const char* ZL_DCtx_getErrorContextString(const ZL_DCtx* dctx, ZL_Report report);
 /* zl_decompress.h:230: host buffers in and out; decoding runs on cuda:0. */
@@ -234,6 +239,36 @@ ZL_GraphID ZL_Compressor_registerTokenizeGraph(ZL_Compressor* compressor, ZL_Typ
                                                ZL_GraphID alphabetGraph, ZL_GraphID indicesGraph);
 /* zl_compressor.h:555 */
 ZL_Report ZL_Compressor_selectStartingGraphID(ZL_Compressor* compressor, ZL_GraphID graph);
+/* zl_graph_api.h:125: nonzero unless ZL_GRAPH_ILLEGAL */
+int ZL_GraphID_isValid(ZL_GraphID graphid);
+/* zl_compressor.h:105 */
+const char* ZL_Compressor_getErrorContextString(const ZL_Compressor* compressor, ZL_Report report);
+
+/* Custom codecs (zl_ctransform.h:134-359, zl_dtransform.h:79-217). A custom
+ * codec runs the caller's host functions and writes a custom transform ID,
+ * so it has no GPU form and cannot give the standard codecs' frames. These
+ * entry points exist so that callers built against the reference's headers
+ * link. Each refuses the registration: the encoders return ZL_NODE_ILLEGAL
+ * (reason in ZL_Compressor_getErrorContextString), the decoders
+ * ZL_ErrorCode_temporaryLibraryLimitation. As in the reference, the
+ * descriptor's opaque pointer is owned by the library even when registration
+ * fails, so its free function is called once. The descriptors have the
+ * reference's layout; they are opaque here because nothing else reads them. */
+#define ZL_NODE_ILLEGAL ZL_MAKE_NODE_ID(0)
+typedef struct ZL_TypedEncoderDesc_s ZL_TypedEncoderDesc;
+typedef struct ZL_VOEncoderDesc_s ZL_VOEncoderDesc;
+typedef struct ZL_MIEncoderDesc_s ZL_MIEncoderDesc;
+typedef struct ZL_TypedDecoderDesc_s ZL_TypedDecoderDesc;
+typedef struct ZL_VODecoderDesc_s ZL_VODecoderDesc;
+typedef struct ZL_MIDecoderDesc_s ZL_MIDecoderDesc;
+/* zl_ctransform.h:170, :287, :359 */
+ZL_NodeID ZL_Compressor_registerTypedEncoder(ZL_Compressor* cgraph, const ZL_TypedEncoderDesc* ctd);
+ZL_NodeID ZL_Compressor_registerVOEncoder(ZL_Compressor* cgraph, const ZL_VOEncoderDesc* ctd);
+ZL_NodeID ZL_Compressor_registerMIEncoder(ZL_Compressor* cgraph, const ZL_MIEncoderDesc* ctd);
+/* zl_dtransform.h:97, :177, :217 */
+ZL_Report ZL_DCtx_registerTypedDecoder(ZL_DCtx* dctx, const ZL_TypedDecoderDesc* dtd);
+ZL_Report ZL_DCtx_registerVODecoder(ZL_DCtx* dctx, const ZL_VODecoderDesc* dtd);
+ZL_Report ZL_DCtx_registerMIDecoder(ZL_DCtx* dctx, const ZL_MIDecoderDesc* dtd);
 
 /* zl_compress.h:39-53 */
 #define ZL_COMPRESSBOUND(s) (((s) * 2) + 512 + 8)
@@ -253,7 +288,11 @@ ZL_Report ZL_CCtx_compress(ZL_CCtx* cctx, void* dst, size_t dstCapacity, const v
 const char* ZL_CCtx_getErrorContextString(const ZL_CCtx* cctx, ZL_Report report);
 /* zl_compress.h:274 */
 ZL_Report ZL_CCtx_compressTypedRef(ZL_CCtx* cctx, void* dst, size_t dstCapacity, const ZL_TypedRef* input);
-/* zl_compress.h:295: one input per frame here (nbInputs must be 1) */
+/* zl_compress.h:295: one input per frame here. Several inputs need a
+ * function graph (ZL_Compressor_registerFunctionGraph, a host callback that
+ * routes each input), which the GPU encoder has no form of; nbInputs > 1
+ * returns ZL_ErrorCode_temporaryLibraryLimitation. Frames of several
+ * outputs decode (ZL_DCtx_decompressMultiTBuffer). */
 ZL_Report ZL_CCtx_compressMultiTypedRef(ZL_CCtx* cctx, void* dst, size_t dstCapacity, const ZL_TypedRef* inputs[],
                                         size_t nbInputs);
 /* zl_compress.h:313-394 */
@@ -383,16 +422,25 @@ const char* ozl_gpu_encoder_error(const OZL_GpuEncoder* e);
 ZL_Report ozl_gpu_xxh3_64(const void* d_data, size_t len, void* stream);
 
 /* Allocation-free variant of ozl_gpu_xxh3_64 (no counterpart in the
- * reference), for callers that cannot call cudaMalloc: the same hash and
- * kernels, with their scratch (task, block list, per-1 KiB block sums and the
- * result) in one fixed file-scope device array of OZL_XXH3_STATIC_SCRATCH
- * bytes per device instead of a per-call allocation. Accepts at most
- * OZL_XXH3_STATIC_MAX_LEN bytes; longer inputs return
+ * reference), for callers that cannot call cudaMalloc: code whose device
+ * memory is owned by another allocator (a framework's caching pool with a
+ * fixed budget), or that runs where cudaMalloc's implicit synchronization and
+ * possible failure are not allowed (a latency-bound request path). The same
+ * hash and kernels, with their scratch (task, block list, per-1 KiB block
+ * sums and the result) in one fixed file-scope device array of
+ * OZL_XXH3_STATIC_SCRATCH bytes per device instead of a per-call allocation;
+ * every GPU that loads the library holds that array until the process exits.
+ * Accepts at most OZL_XXH3_STATIC_MAX_LEN bytes; longer inputs return
  * ZL_ErrorCode_srcSize_tooLarge without touching the device. Calls no
- * allocating routine. Every call on a device shares that array: calls whose
- * work overlaps on the GPU (other streams, other host threads) race and must
- * be serialized by the caller. Synchronizes `stream`; returns the hash in the
- * report value. */
+ * allocating routine. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress, with that device current) and keeps it, so
+ * make that first call before any stream capture; the address belongs to the
+ * device's primary context, so after a cudaDeviceReset this entry point must
+ * not be called again in the same process. Every call on a device shares the
+ * array and the array keeps the last call's contents (what must start at
+ * zero is cleared by each call): calls whose work overlaps on the GPU (other
+ * streams, other host threads) race and must be serialized by the caller.
+ * Synchronizes `stream`; returns the hash in the report value. */
 #define OZL_XXH3_STATIC_MAX_LEN ((size_t)32 << 20)
 #define OZL_XXH3_STATIC_SCRATCH ((size_t)256 + ((size_t)32 << 10) * 72)
 ZL_Report ozl_gpu_xxh3_64_static(const void* d_data, size_t len, void* stream);

@@ -41,6 +41,7 @@ struct OZL_GpuBatch_s : ozl::DecodeBatch {};
 struct ZL_DCtx_s {
     ozl::DecodeBatch batch;
     bool sticky = false;
+    int raw[4] = {}; // parameter values as set, for ZL_DCtx_getParameter
     ozl::DevBuf frame, out;
     cudaStream_t stream = nullptr;
     std::string err;
@@ -201,6 +202,25 @@ ZL_Report ZL_DCtx_setParameter(ZL_DCtx* dctx, ZL_DParam param, int value)
         case ZL_DParam_checkContentChecksum: dctx->batch.checkContent = value != ZL_TernaryParam_disable; break;
         default: return fail(ZL_ErrorCode_parameter_invalid);
     }
+    dctx->raw[param] = value;
+    return ok(0);
+}
+
+/* zl_decompress.h:149: the value set, 0 when unset or unknown */
+int ZL_DCtx_getParameter(const ZL_DCtx* dctx, ZL_DParam param)
+{
+    if (!dctx || int(param) < 1 || int(param) > 3) return 0;
+    return dctx->raw[param];
+}
+
+/* zl_decompress.h:159: every parameter back to its default, sticky included */
+ZL_Report ZL_DCtx_resetParameters(ZL_DCtx* dctx)
+{
+    if (!dctx) return fail(ZL_ErrorCode_parameter_invalid);
+    dctx->sticky = false;
+    dctx->batch.checkCompressed = true;
+    dctx->batch.checkContent = true;
+    for (int& v : dctx->raw) v = 0;
     return ok(0);
 }
 
@@ -215,6 +235,8 @@ static void resetParams(ZL_DCtx* d)
     if (!d->sticky) {
         d->batch.checkCompressed = true;
         d->batch.checkContent = true;
+        d->raw[ZL_DParam_checkCompressedChecksum] = 0;
+        d->raw[ZL_DParam_checkContentChecksum] = 0;
     }
 }
 

@@ -68,6 +68,7 @@ struct ZL_Compressor_s {
     ZL_IDType next = kFirstCustomGraph;
     ZL_IDType start = G_ILLEGAL;
     int params[kNbParams] = {};
+    std::string err; // reason of the last failed call on this compressor
 
     ZL_GraphID add(Graph g)
     {
@@ -348,9 +349,21 @@ ZL_GraphID ZL_Compressor_registerTokenizeGraph(ZL_Compressor* c, ZL_Type inputTy
 ZL_Report ZL_Compressor_selectStartingGraphID(ZL_Compressor* c, ZL_GraphID graph)
 {
     if (!c) return fail(ZL_ErrorCode_parameter_invalid);
-    if (!c->known(graph.gid)) return fail(ZL_ErrorCode_graph_invalid);
+    if (!c->known(graph.gid)) {
+        c->err = "unknown graph ID";
+        return fail(ZL_ErrorCode_graph_invalid);
+    }
     c->start = graph.gid;
     return ok(0);
+}
+
+int ZL_GraphID_isValid(ZL_GraphID g) { return g.gid != G_ILLEGAL; }
+
+/* zl_compressor.h:105 */
+const char* ZL_Compressor_getErrorContextString(const ZL_Compressor* c, ZL_Report r)
+{
+    if (!c || c->err.empty()) return ZL_ErrorCode_toString(r._code);
+    return c->err.c_str();
 }
 
 size_t ZL_compressBound(size_t totalSrcSize) { return ZL_COMPRESSBOUND(totalSrcSize); }
@@ -448,3 +461,8 @@ ZL_TypedRef* ZL_TypedRef_createNumeric(const void* start, size_t numWidth, size_
 void ZL_TypedRef_free(ZL_TypedRef* t) { delete t; }
 
 } // extern "C"
+
+void ozl_compressor_set_error(ZL_Compressor* c, const char* msg)
+{
+    if (c) c->err = msg;
+}

@@ -827,15 +827,20 @@ __device__ __forceinline__ bool streamStart(const uint8_t* p, uint32_t size, con
 
 // Backward bit reader (FSE and Huffman decoders): three stream words in
 // registers, a (bits [cb + 64, cb + 96)) above b and c (bits [cb, cb + 32)),
-// cb = 32 * kb, and g = cb + 96 - pos. At the start of a step g <= 32, so the
-// 32 bits that start o <= 56 bits below the top of the window
-// (pos - o - 32 .. pos - o) are one funnel shift of (a, b) or (b, c): a step
-// reads two windows, one per pair of fields (at most 24 bits each), without
-// waiting for a refill, and refills once at its end by one or two words,
-// without a branch. prepare(), once per step, makes the next two words of
-// the ring readable. Words below the stream are never consumed by a valid
-// stream (finished() checks that the stream ends exactly at its first bit),
-// so the ring's stale contents may stand in for them.
+// cb = 32 * kb, and g = cb + 96 - pos, the bits of the window already read.
+// Invariant: g <= 32 at the start of every step. The four-symbol loops take
+// the 64 bits just below pos as one left-aligned register pair (hi, lo) =
+// two funnel shifts of (a, b, c), peel each field off the top of the pair,
+// and then call advance() once with the step's total. A step reads at most
+// four fields of at most 12 bits (FSE tableLog <= 12, Huffman codes <= 12
+// bits), i.e. n <= 48, so g + n <= 80 < 96 stays inside the three words, and
+// advance() drops one or two words without a branch, leaving g <= 32 again.
+// read(nb) is the one-field path (stream heads, tails and initial states):
+// it takes window(g), the 32 bits starting g bits below the top of the
+// window. prepare(), once per step, makes the next two words of the ring
+// readable. Words below the stream are never consumed by a valid stream
+// (finished() checks that the stream ends exactly at its first bit), so the
+// ring's stale contents may stand in for them.
 template <int RING, int AHEAD>
 struct BitWin3 {
     StreamRing<RING, AHEAD> r;
@@ -2026,8 +2031,11 @@ constexpr int kMaxDevices = 64;
 std::mutex gStaticMu;
 uint8_t* gStaticPtr[kMaxDevices] = {};
 
-// Device address of the array on the current device, looked up once per
-// device with that device current.
+// Device address of the array on the current device, looked up by the first
+// call on that device (with that device current) and kept. The address
+// belongs to the device's primary context: a cudaDeviceReset by the host
+// application unloads the module, and the entry point is not to be called
+// after one (the header says so).
 cudaError_t staticScratch(uint8_t** out)
 {
     int dev = 0;

@@ -4,13 +4,13 @@
 # oracle/ozl_oracle.c and to produce reference frames. It is never linked
 # into the product.
 #
-#   make -f oracle/ref.mk -j8            (REF defaults to /root/reference)
+#   make -f oracle/ref.mk -j8   (REF: $OZL_REFERENCE, else /root/reference)
 #
 # Recipe: every src/openzl/**/*.c except the zstd/lz4 bindings (their
 # third-party libraries are not vendored), replaced by oracle/ref_stubs.c,
 # compiled with the reference's default release flags (-O3 -DNDEBUG, no
 # -march). The x86-64 Huffman assembly loop is added on x86-64 hosts only.
-REF     ?= /root/reference
+REF     ?= $(or $(OZL_REFERENCE),/root/reference)
 OUT     := oracle/_ref
 CC      ?= gcc
 CFLAGS  := -std=gnu11 -O3 -DNDEBUG -fPIC -fvisibility=default \
