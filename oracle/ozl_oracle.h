@@ -64,6 +64,9 @@ int64_t ozo_decode_transform(unsigned id, const uint8_t* hdr, size_t hsz, size_t
                              const size_t* widths, const size_t* counts, const uint8_t* const* data, void* out,
                              size_t outCap, int* outType, size_t* outW, size_t* outN);
 int64_t ozo_tokenize(const void* src, size_t n, int w, int sorted, void* alphaOut, void* idxOut, int* iwOut);
+/* Test entry point: the largest FSE table log the encoder may pick, 11 (the
+ * reference encoder's) or 12 (the decoders' limit). Not thread-safe. */
+void ozo_test_set_fse_max_tablelog(unsigned tl);
 
 #ifdef __cplusplus
 }

@@ -1089,6 +1089,15 @@ static int node_flatpack(ECtx* c, int in)
     return a;
 }
 
+/* Largest FSE table log the encoder may pick: the reference's
+ * FSE_DEFAULT_TABLELOG (11, encode_entropy_binding.c:92-93). Tests raise it to
+ * 12, the decoder's limit (FSE_MAX_TABLELOG, fse.h:732), to make frames that
+ * exercise the widest fields; such frames are valid for the reference's
+ * decoder but its encoder never writes them. */
+static unsigned g_fseMaxTableLog = 11;
+
+void ozo_test_set_fse_max_tablelog(unsigned tl) { g_fseMaxTableLog = tl == 12 ? 12u : 11u; }
+
 /* EI_fse_v2 (encode_entropy_binding.c:51-139): outputs normalized counts
  * (numeric i16) and the bitstream. */
 static int node_fse(ECtx* c, int in, const Stats* st)
@@ -1101,7 +1110,7 @@ static int node_fse(ECtx* c, int in, const Stats* st)
     for (size_t b = 0; b < nbBytes; b++) nd->hdr[1 + b] = (uint8_t)(n >> (8 * b));
     nd->hsz = nbBytes + 1;
     unsigned const maxSV = st->maxSym;
-    unsigned const tl = fse_optimal_tablelog(11, n, maxSV, 2);
+    unsigned const tl = fse_optimal_tablelog(g_fseMaxTableLog, n, maxSV, 2);
     int16_t norm[256];
     if (fse_normalize(norm, tl, st->count, n, maxSV, 1)) c->err = OZO_ERR_GENERIC;
     int ns = new_stream(c, OZO_TYPE_NUMERIC, 2, maxSV + 1, NULL);

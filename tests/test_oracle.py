@@ -263,3 +263,36 @@ def test_oracle_encoder_matches_reference_on_seeded_inputs():
             assert r > 0
             got = oracle.compress(recipe, arr, w, checksums=bool(cs))
             assert got.tobytes() == dst[:r].tobytes(), (recipe, w, arr.size, cs)
+
+
+def tablelog12_cases():
+    """Frames whose FSE chunks use table log 12, the decoders' limit (the
+    reference's encoder stops at 11): 99,999-symbol unchunked streams, a
+    chunked stream and transpose-split planes."""
+    rng = np.random.default_rng(1212)
+    cases = [(7, (rng.zipf(1.1, 99999) % 256).astype(np.uint8), 0),
+             (7, (rng.zipf(1.05, 99999) % 256).astype(np.uint8), 0),
+             (7, (rng.zipf(1.1, 250000) % 256).astype(np.uint8), 0),
+             (3, (1000 + np.cumsum(rng.integers(-40000, 40001, 99999))).astype(np.uint16), 2)]
+    return [(r, a, w, oracle.compress_tablelog12(r, a, w)) for r, a, w in cases]
+
+
+def test_tablelog12_frames_decode_in_oracle_and_reference():
+    import ctypes
+
+    cases = tablelog12_cases()
+    ref = None
+    if os.path.exists(REF_DRIVER):
+        ref = ctypes.CDLL(REF_DRIVER)
+        ref.ref_decompress_into.restype = ctypes.c_int64
+        ref.ref_decompress_into.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                                            ctypes.c_int]
+    for recipe, arr, w, fr in cases:
+        # the frame differs from the table-log-11 frame the reference would write
+        assert fr.tobytes() != oracle.compress(recipe, arr, w).tobytes()
+        data, _, _ = oracle.decompress(fr)
+        assert data.tobytes() == arr.tobytes()
+        if ref is not None:
+            out = np.zeros(arr.nbytes + 64, np.uint8)
+            n = ref.ref_decompress_into(fr.ctypes.data, fr.size, out.ctypes.data, out.size, 1)
+            assert n == arr.nbytes and out[:n].tobytes() == arr.tobytes()
