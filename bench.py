@@ -46,6 +46,10 @@ RECIPE_BITPACK_HUF = 4  # delta -> bitpack_int -> Huffman
 RECIPE_DZ_BITPACK_HUF = 2  # delta -> zigzag -> bitpack_int -> Huffman
 OUT_ALIGN = 256
 FRAME_ALIGN = 16
+# where the CPU baseline is the C restatement (a host that cannot build the
+# reference), what it stands for
+PORT_NOTE = ("C restatement of the reference's decoder/encoder (oracle/); the reference's own library is "
+             "not buildable on this host")
 
 
 def parse_args():
@@ -64,8 +68,12 @@ def parse_args():
     p.add_argument("--no-serve", action="store_true", help="skip the serving-loop run")
     p.add_argument("--no-single", action="store_true", help="skip the single 256 MiB array run")
     p.add_argument("--no-columnar", action="store_true", help="skip the columnar/bf16 round trip")
-    p.add_argument("--serve-rates", default="1000,5000,20000,50000", help="request rates (req/s) for the serving run")
+    p.add_argument("--serve-rates", default="1000,2000,5000,10000,20000,50000",
+                   help="request rates (req/s) for the serving run")
     p.add_argument("--serve-seconds", type=float, default=1.0, help="seconds of arrivals per rate")
+    p.add_argument("--serve-requests", type=int, default=0,
+                   help="requests per rate (0: --serve-seconds of arrivals per rate)")
+    p.add_argument("--no-parity", action="store_true", help="skip the encode-parity check against the oracle")
     return p.parse_args()
 
 
@@ -100,6 +108,14 @@ def make_frame_input(f, out=None):
         out[:a.size] = a
         return out[:a.size]
     return a
+
+
+def workload_config(n_frames, decoded, compressed, parts_per_kind):
+    """The `config` object of both arms' lines (same workload, same frames)."""
+    return {"workload": WORKLOAD, "frames": n_frames, "decoded_bytes": decoded, "compressed_bytes": compressed,
+            "ratio": round(decoded / compressed, 3), "graphs": "delta->tsplit->FSE | delta->bitpack->Huffman",
+            "format_version": 23, "checksums": "content+compressed, verified on decode",
+            "l2": "inputs larger than L2 (no flush)", "parts_per_kind": parts_per_kind or "library default"}
 
 
 def layout(sizes, align):
@@ -148,6 +164,66 @@ class CpuDecoder:
             return self._ref.ref_decompress_into(src_ptr, src_size, dst_ptr, dst_cap, 1)
         t, w = ctypes.c_int(), ctypes.c_int()
         return self._port.ozo_decompress(src_ptr, src_size, dst_ptr, dst_cap, ctypes.byref(t), ctypes.byref(w))
+
+
+class CpuEncoder:
+    """The CPU compressor of the same graphs: the reference library where it
+    loads on this host, else the C restatement in oracle/."""
+
+    def __init__(self):
+        self.kind = "port"
+        self._ref = None
+        ref = os.path.join(ROOT, "oracle", "_ref", "ref_driver.so")
+        if os.path.exists(ref):
+            try:
+                l = ctypes.CDLL(ref)
+                l.ref_compress.restype = ctypes.c_int64
+                l.ref_compress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+                self._ref = l
+                self.kind = "reference"
+            except OSError:
+                self._ref = None
+        if self._ref is None:
+            from oracle import oracle
+
+            self._port = oracle.lib()
+
+    def encode(self, recipe, src_ptr, nb_elts, width, dst_ptr, dst_cap):
+        if self._ref is not None:
+            return self._ref.ref_compress(recipe, src_ptr, nb_elts, width, dst_ptr, dst_cap, 1, 0)
+        return self._port.ozo_compress(recipe, src_ptr, nb_elts, width, dst_ptr, dst_cap, 1)
+
+
+def cpu_encode_rate(spec, host_in, ooffs, osizes, idx, threads, min_seconds=2.0):
+    """CPU compression of frames `idx` on `threads` host threads, repeated
+    for at least min_seconds. Returns (GB/s of input bytes, passes)."""
+    enc = CpuEncoder()
+    caps = [2 * osizes[i] + 4096 for i in idx]
+    bufs = [np.empty(c, np.uint8) for c in caps]
+    base = host_in.ctypes.data
+
+    def one(k):
+        i = idx[k]
+        f = spec[i]
+        r = enc.encode(f["recipe"], base + ooffs[i], f["n"], f["w"], bufs[k].ctypes.data, caps[k])
+        if r <= 0:
+            raise RuntimeError("CPU encode of frame %d failed (%d)" % (i, r))
+        return osizes[i]
+
+    secs, nb, reps = 0.0, 0, 0
+    while reps < 2 or secs < min_seconds:
+        t0 = time.perf_counter()
+        if threads == 1:
+            nb += sum(one(k) for k in range(len(idx)))
+        else:
+            with ThreadPoolExecutor(threads) as ex:
+                nb += sum(ex.map(one, range(len(idx)), chunksize=2))
+        secs += time.perf_counter() - t0
+        reps += 1
+        if reps >= 10:
+            break
+    return nb / secs / 1e9, reps, enc.kind
 
 
 def cpu_decode_pass(dec, frames_h, foffs, fsizes, out_h, ooffs, osizes, idx, threads):
@@ -248,10 +324,11 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
-def ncu_traffic_per_algo_byte():
-    """DRAM bytes per algorithmic byte of the dominant decode kernel, from the
-    committed ncu summary (line 'dram_bytes_per_algorithmic_byte: X'), or None."""
-    p = os.path.join(ROOT, "profiles", "fse_decode_mixed_frames.md")
+def ncu_traffic_per_algo_byte(name="fse_decode_mixed_frames.md"):
+    """DRAM bytes per algorithmic byte of a kernel, from its committed ncu
+    summary under profiles/ (line 'dram_bytes_per_algorithmic_byte: X'), or
+    None."""
+    p = os.path.join(ROOT, "profiles", name)
     try:
         with open(p) as f:
             for line in f:
@@ -260,6 +337,80 @@ def ncu_traffic_per_algo_byte():
     except (OSError, ValueError):
         pass
     return None
+
+
+# committed ncu summaries that state a DRAM-bytes-per-algorithmic-byte ratio,
+# by (workload, kernel kind)
+TRAFFIC_PROFILES = {
+    ("mixed_frames_4096", "fse"): "fse_decode_mixed_frames.md",
+    ("timestamps_int64_256mib", "huffman"): "huf_decode_timestamps.md",
+    ("mixed_frames_4096", "huffman"): "huf_decode_mixed_frames.md",
+}
+
+
+def roofline_from_profile(prof, step_ms, algo_bytes, peak, peak_src, workload):
+    """Roofline of the dominant launch kind of one planned run, from its
+    per-launch profile [(kind, ms, algorithmic bytes)], with the whole-step
+    figures beside it."""
+    by_kind = {}
+    for kind, ms, nb in prof:
+        e = by_kind.setdefault(kind, [0.0, 0, 0])
+        e[0] += ms
+        e[1] += nb
+        e[2] += 1
+    prof_ms = sum(v[0] for v in by_kind.values())
+    top = max(by_kind, key=lambda k: by_kind[k][0])
+    top_ms, top_bytes, top_n = by_kind[top]
+    achieved = top_bytes / top_n / (top_ms / top_n / 1e3) / 1e9
+    prof_name = TRAFFIC_PROFILES.get((workload, top))
+    tpa = ncu_traffic_per_algo_byte(prof_name) if prof_name else None
+    return {
+        "bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+        "frac": round(achieved / peak, 4), "peak_source": peak_src,
+        "traffic": round(tpa * top_bytes / top_n) if tpa else None,
+        "algorithmic_bytes_per_launch": int(top_bytes / top_n), "launches": top_n,
+        "share_of_step": round(top_ms / prof_ms, 4),
+        "step": {"achieved": round(algo_bytes / (step_ms / 1e3) / 1e9, 1),
+                 "frac": round(algo_bytes / (step_ms / 1e3) / 1e9 / peak, 4),
+                 "algorithmic_bytes": int(algo_bytes)},
+        "kinds": {k: {"ms": round(v[0], 4), "launches": v[2], "gbs": round(v[1] / (v[0] / 1e3) / 1e9, 1)}
+                  for k, v in sorted(by_kind.items(), key=lambda kv: -kv[1][0])},
+    }
+
+
+def timed_batch_runs(torch, batch, stream, sptr, reps):
+    """Milliseconds per graph launch of a planned batch, CUDA events on the
+    launching stream over `reps` launches."""
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(reps):
+        batch.run(sptr, graph=True)
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def encode_parity(pairs, threads):
+    """GPU frames against the CPU restatement's frames for the same inputs
+    and graphs (the restatement is pinned byte for byte to the reference's
+    frames by the test suite). pairs: [(label, recipe, host array, elt width,
+    GPU frame as uint8)]. Returns {label: [checked, equal]}."""
+    from oracle import oracle
+
+    def one(p):
+        label, r, a, w, fr = p
+        want = oracle.compress(r, a, w, checksums=True)
+        return label, bool(want.size == fr.size and np.array_equal(want, fr))
+
+    out = {}
+    with ThreadPoolExecutor(threads) as ex:
+        for label, eq in ex.map(one, pairs):
+            e = out.setdefault(label, [0, 0])
+            e[0] += 1
+            e[1] += int(eq)
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -300,7 +451,11 @@ def timestamps(seed, n):
     return (1700000000000000000 + np.cumsum(inc)).astype(np.int64)
 
 
-def run_single_array(oz, torch, dev, sptr, seed):
+def run_single_array(oz, torch, dev, stream, sptr, seed, peak, peak_src, parity):
+    """The 256 MiB timestamp array: GPU encode, the plain per-frame decode
+    (host plan plus stage-by-stage launches per call), the same frame as a
+    one-frame captured graph (CUDA events, per-launch roofline), and the CPU
+    decoder on the same frame on one core."""
     n = 256 << 17  # 33,554,432 int64 values = 256 MiB
     a = timestamps(seed + 2, n)
     d_in = torch.from_numpy(a.view(np.uint8)).to(dev)
@@ -310,7 +465,13 @@ def run_single_array(oz, torch, dev, sptr, seed):
     fs = enc.compress_batch([d_in.data_ptr()], [n], [8], [RECIPE_DZ_BITPACK_HUF], [d_fr.data_ptr()], [cap],
                             checksums=True, stream=sptr)[0]
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    enc.compress_batch([d_in.data_ptr()], [n], [8], [RECIPE_DZ_BITPACK_HUF], [d_fr.data_ptr()], [cap],
+                       checksums=True, stream=sptr)
+    torch.cuda.synchronize()
+    enc_s = time.perf_counter() - t0
     frame_h = d_fr[:fs].cpu().numpy()
+    parity.append(("timestamps_int64_256mib", RECIPE_DZ_BITPACK_HUF, a, 8, frame_h))
     d_out = torch.empty(a.nbytes, dtype=torch.uint8, device=dev)
     dctx = oz.DCtx()
     for _ in range(2):
@@ -324,9 +485,39 @@ def run_single_array(oz, torch, dev, sptr, seed):
     dt = (time.perf_counter() - t0) / reps
     if not torch.equal(d_out, d_in):
         raise RuntimeError("single-array decode differs from the input")
+    # the same frame as a captured one-frame graph
+    batch = oz.GpuBatch()
+    batch.plan([frame_h], [d_fr.data_ptr()], [d_out.data_ptr()], [a.nbytes])
+    d_out.zero_()
+    for _ in range(3):
+        batch.run(sptr, graph=True)
+    batch.check(sptr)
+    graph_ms = timed_batch_runs(torch, batch, stream, sptr, 10)
+    batch.check(sptr)
+    if not torch.equal(d_out, d_in):
+        raise RuntimeError("single-array graph decode differs from the input")
+    roof = roofline_from_profile(batch.profile(sptr, capacity=64), graph_ms, a.nbytes + fs, peak, peak_src,
+                                 "timestamps_int64_256mib")
+    # CPU decoder on the same frame (one frame: one core, as in the reference)
+    dec = CpuDecoder()
+    out_c = np.empty(a.nbytes, np.uint8)
+    fr_c = np.ascontiguousarray(frame_h)
+    times = []
+    for _ in range(2):
+        t1 = time.perf_counter()
+        r = dec.decode(fr_c.ctypes.data, fs, out_c.ctypes.data, a.nbytes)
+        times.append(time.perf_counter() - t1)
+        if r != a.nbytes:
+            raise RuntimeError("CPU decode of the single array failed (%d)" % r)
+    if not np.array_equal(out_c, a.view(np.uint8)):
+        raise RuntimeError("CPU decode of the single array differs")
+    cpu = {"value": round(a.nbytes / min(times) / 1e9, 4), "unit": "GB/s", "cores": 1, "kind": dec.kind,
+           "sample": "the whole 256 MiB frame, 1 thread, best of 2"}
     return {"workload": "timestamps_int64_256mib", "graph": "delta->zigzag->bitpack->Huffman",
             "decoded_bytes": int(a.nbytes), "compressed_bytes": int(fs), "ratio": round(a.nbytes / fs, 3),
-            "plain_gbs": round(a.nbytes / dt / 1e9, 2), "ms": round(dt * 1e3, 3)}
+            "plain_gbs": round(a.nbytes / dt / 1e9, 2), "ms": round(dt * 1e3, 3),
+            "graph_gbs": round(a.nbytes / (graph_ms / 1e3) / 1e9, 2), "graph_ms": round(graph_ms, 3),
+            "encode_gbs": round(a.nbytes / enc_s / 1e9, 2), "roofline": roof, "cpu_baseline": cpu}
 
 
 # ---------------------------------------------------------------------------
@@ -342,7 +533,7 @@ RECIPE_TOKENIZE = 5
 RECIPE_BF16 = 6
 
 
-def run_columnar(oz, torch, dev, sptr, seed):
+def run_columnar(oz, torch, dev, stream, sptr, seed, peak, peak_src, threads, parity):
     g = torch.Generator(device=dev)
     g.manual_seed(seed + 41)
     rows = 64 << 20
@@ -371,6 +562,13 @@ def run_columnar(oz, torch, dev, sptr, seed):
     torch.cuda.synchronize()
     enc_s = time.perf_counter() - t0
     frames_h = [d_fr[o:o + f].cpu().numpy() for o, f in zip(offs, fs)]
+    # encode parity: the column and one matrix of each shape
+    host_src = {}
+    for k in (0, 1, 2, 3):
+        h = srcs[k].view(torch.uint8).reshape(-1).cpu().numpy()
+        host_src[k] = h
+        arr = h.view(np.uint32) if k == 0 else h.view(np.uint16)
+        parity.append(("columnar_zipf_int32" if k == 0 else "bf16_weights", recipes[k], arr, widths[k], frames_h[k]))
     ooffs, obytes = layout(nbytes, OUT_ALIGN)
     d_out = torch.zeros(obytes, dtype=torch.uint8, device=dev)
     batch = oz.GpuBatch()
@@ -378,21 +576,43 @@ def run_columnar(oz, torch, dev, sptr, seed):
     for _ in range(3):
         batch.run(sptr, graph=True)
     batch.check(sptr)
-    reps = 10
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        batch.run(sptr, graph=True)
+    dec_ms = timed_batch_runs(torch, batch, stream, sptr, 10)
     batch.check(sptr)
-    dec_s = (time.perf_counter() - t0) / reps
     ok = all(torch.equal(d_out[o:o + n], t.view(torch.uint8).reshape(-1)) for o, n, t in zip(ooffs, nbytes, srcs))
     if not ok:
         raise RuntimeError("columnar round trip differs")
     total = sum(nbytes)
+    roof = roofline_from_profile(batch.profile(sptr, capacity=256), dec_ms, total + sum(fs), peak, peak_src,
+                                 "columnar_bf16")
+    # CPU decoder: the column and the first six matrices, all host threads
+    dec = CpuDecoder()
+    sel = list(range(7))
+    fr_c = [np.ascontiguousarray(frames_h[k]) for k in sel]
+    out_c = [np.empty(nbytes[k], np.uint8) for k in sel]
+
+    def one(j):
+        k = sel[j]
+        r = dec.decode(fr_c[j].ctypes.data, fs[k], out_c[j].ctypes.data, nbytes[k])
+        if r != nbytes[k]:
+            raise RuntimeError("CPU decode of columnar frame %d failed (%d)" % (k, r))
+        return r
+
+    cpu_times = []
+    for _ in range(2):
+        t1 = time.perf_counter()
+        with ThreadPoolExecutor(min(threads, len(sel))) as ex:
+            cpu_bytes = sum(ex.map(one, range(len(sel))))
+        cpu_times.append(time.perf_counter() - t1)
+    for j, k in enumerate(sel[:4]):
+        if k in host_src and not np.array_equal(out_c[j], host_src[k]):
+            raise RuntimeError("CPU decode of columnar frame %d differs" % k)
+    cpu = {"value": round(cpu_bytes / min(cpu_times) / 1e9, 4), "unit": "GB/s", "cores": min(threads, len(sel)),
+           "kind": dec.kind, "sample": "the column and 6 of the 30 matrices (%.0f MiB), one frame per thread, best of 2"
+           % (cpu_bytes / 2**20)}
     return {"column_rows": rows, "column_ratio": round(nbytes[0] / fs[0], 3), "bf16_bytes": sum(nbytes[1:]),
             "bf16_ratio": round(sum(nbytes[1:]) / sum(fs[1:]), 3), "frames": len(srcs),
-            "encode_gbs": round(total / enc_s / 1e9, 2), "decode_gbs": round(total / dec_s / 1e9, 2),
-            "bit_exact": True}
+            "encode_gbs": round(total / enc_s / 1e9, 2), "decode_gbs": round(total / (dec_ms / 1e3) / 1e9, 2),
+            "decode_ms": round(dec_ms, 3), "bit_exact": True, "roofline": roof, "cpu_baseline": cpu}
 
 
 # ---------------------------------------------------------------------------
@@ -450,7 +670,7 @@ def run_serving(oz, torch, dev, sptr, args):
     results = []
     rates = [int(r) for r in args.serve_rates.split(",") if r]
     for rate in rates:
-        nreq = max(50, int(rate * args.serve_seconds))
+        nreq = args.serve_requests if args.serve_requests > 0 else max(50, int(rate * args.serve_seconds))
         gaps = rng.exponential(1.0 / rate, nreq)
         kinds = rng.random(nreq) < 0.8
         which = rng.integers(0, len(pool), nreq)
@@ -558,8 +778,8 @@ def run_reference_arm(args):
         frames_h[foffs[i]:foffs[i] + fsizes[i]] = fr
     out_h = np.zeros(obytes, np.uint8)
     dec = CpuDecoder()
-    # each step: a bounded sample (1/4 of the workload's bytes)
-    idx = cpu_sample(spec, osizes, sum(osizes) // 4, args.seed)
+    # each step decodes the whole workload (every frame), as our arm does
+    idx = list(range(len(spec)))
     for _ in range(args.warmup):
         cpu_decode_pass(dec, frames_h, foffs, fsizes, out_h, ooffs, osizes, idx, threads)
     times, nbytes = [], 0
@@ -579,10 +799,9 @@ def run_reference_arm(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot / len(times) * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic (seeded random walks)",
-        "config": {"workload": WORKLOAD, "frames": len(spec), "decoded_bytes": int(sum(osizes)),
-                   "compressed_bytes": int(sum(fsizes)), "l2": "inputs larger than L2"},
+        "config": workload_config(len(spec), int(sum(osizes)), int(sum(fsizes)), args.parts_per_kind),
         "cpu_baseline": {"value": round(gbs, 4), "unit": "GB/s", "cores": threads, "kind": dec.kind,
-                         "sample": sample},
+                         "sample": sample, **({"note": PORT_NOTE} if dec.kind == "port" else {})},
         "e2e": {"value": round(gbs, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -719,29 +938,7 @@ def main():
     # ---- roofline: per-launch profile of one run (CUDA events per launch)
     peak, peak_src = measured_hbm_peak()
     prof = batch.profile(sptr, capacity=max(64, launches + 8))
-    by_kind = {}
-    for kind, ms, nb in prof:
-        e = by_kind.setdefault(kind, [0.0, 0, 0])
-        e[0] += ms
-        e[1] += nb
-        e[2] += 1
-    prof_ms = sum(v[0] for v in by_kind.values())
-    top = max(by_kind, key=lambda k: by_kind[k][0])
-    top_ms, top_bytes, top_n = by_kind[top]
-    achieved = top_bytes / top_n / (top_ms / top_n / 1e3) / 1e9
-    tpa = ncu_traffic_per_algo_byte()
-    roofline = {
-        "bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-        "frac": round(achieved / peak, 4), "peak_source": peak_src,
-        "traffic": round(tpa * top_bytes / top_n) if tpa else None,
-        "algorithmic_bytes_per_launch": int(top_bytes / top_n), "launches": top_n,
-        "share_of_step": round(top_ms / prof_ms, 4),
-        "step": {"achieved": round((total_out + total_comp) / (ms_per_step / 1e3) / 1e9, 1),
-                 "frac": round((total_out + total_comp) / (ms_per_step / 1e3) / 1e9 / peak, 4),
-                 "algorithmic_bytes": total_out + total_comp},
-        "kinds": {k: {"ms": round(v[0], 4), "launches": v[2], "gbs": round(v[1] / (v[0] / 1e3) / 1e9, 1)}
-                  for k, v in sorted(by_kind.items(), key=lambda kv: -kv[1][0])},
-    }
+    roofline = roofline_from_profile(prof, ms_per_step, total_out + total_comp, peak, peak_src, WORKLOAD)
 
     # ---- e2e: host buffers through the C ABI, copies inside the timed region
     out_h = torch.empty(obytes, dtype=torch.uint8, pin_memory=True)
@@ -781,49 +978,86 @@ def main():
         plain = {"value": round(total_out / plain_s / 1e9, 3), "unit": "GB/s", "ms": round(plain_s * 1e3, 2),
                  "batched_over_plain": round(value / ws / (total_out / plain_s / 1e9), 2)}
 
+    # ---- encode parity: a seeded sample of the mixed frames (GPU frames
+    # against the restatement's frames), then the other workloads add theirs
+    parity = []
+    if rank == 0 and ws == 1 and not args.no_parity:
+        for i in cpu_sample(spec, osizes, 1 << 62, args.seed + 3)[:256]:
+            f = spec[i]
+            a = host_in[ooffs[i]:ooffs[i] + osizes[i]].view(_UDT[f["w"]])
+            parity.append((WORKLOAD, f["recipe"], a, f["w"], frames_np[foffs[i]:foffs[i] + fsizes[i]]))
+
     # ---- the single large array and the serving loop (rank 0, N=1 only)
     single = None
     serving = None
     if rank == 0 and ws == 1 and not args.no_single:
-        single = run_single_array(oz, torch, dev, sptr, args.seed)
+        single = run_single_array(oz, torch, dev, stream, sptr, args.seed, peak, peak_src, parity)
     if rank == 0 and ws == 1 and not args.no_serve:
         serving = run_serving(oz, torch, dev, sptr, args)
     columnar = None
     if rank == 0 and ws == 1 and not args.no_columnar:
-        columnar = run_columnar(oz, torch, dev, sptr, args.seed)
+        columnar = run_columnar(oz, torch, dev, stream, sptr, args.seed, peak, peak_src, threads, parity)
+    enc_parity = None
+    if parity:
+        t0 = time.perf_counter()
+        res = encode_parity(parity, threads)
+        enc_parity = {"frames_checked": sum(v[0] for v in res.values()), "equal": sum(v[1] for v in res.values()),
+                      "by_workload": {k: {"checked": v[0], "equal": v[1]} for k, v in res.items()},
+                      "against": "frames of the CPU restatement, which the test suite pins byte for byte to the "
+                                 "reference's frames", "seconds": round(time.perf_counter() - t0, 1)}
+        if enc_parity["equal"] != enc_parity["frames_checked"]:
+            print("encode parity: %d of %d GPU frames differ from the oracle's" % (
+                enc_parity["frames_checked"] - enc_parity["equal"], enc_parity["frames_checked"]), file=sys.stderr)
 
-    # ---- CPU baseline (rank 0, N=1 only): the same frames on the host cores
+    # ---- CPU baseline (rank 0, N=1 only): the same frames on the host
+    # cores, all threads and one thread; the CPU compressor beside it
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         dec = CpuDecoder()
         idx = cpu_sample(spec, osizes, total_out // 4, args.seed)
         out_c = np.zeros(obytes, np.uint8)
-        cpu_decode_pass(dec, frames_np, foffs, fsizes, out_c, ooffs, osizes, idx[:16], threads)
-        reps, secs, nb = 0, 0.0, 0
-        while reps < 3 or secs < 3.0:
-            t, b = cpu_decode_pass(dec, frames_np, foffs, fsizes, out_c, ooffs, osizes, idx, threads)
-            secs += t
-            nb += b
-            reps += 1
-            if reps >= 20:
-                break
+
+        def decode_rate(sel, nthreads, min_seconds):
+            cpu_decode_pass(dec, frames_np, foffs, fsizes, out_c, ooffs, osizes, sel[:16], nthreads)
+            reps, secs, nb = 0, 0.0, 0
+            while reps < 2 or secs < min_seconds:
+                t, b = cpu_decode_pass(dec, frames_np, foffs, fsizes, out_c, ooffs, osizes, sel, nthreads)
+                secs += t
+                nb += b
+                reps += 1
+                if reps >= 20:
+                    break
+            return nb / secs / 1e9, reps
+
+        all_gbs, reps = decode_rate(idx, threads, 3.0)
         for i in idx:
             if not np.array_equal(out_c[ooffs[i]:ooffs[i] + osizes[i]], host_in[ooffs[i]:ooffs[i] + osizes[i]]):
                 raise RuntimeError("CPU decode mismatch on frame %d" % i)
-        cpu = {"value": round(nb / secs / 1e9, 4), "unit": "GB/s", "cores": threads, "kind": dec.kind,
+        idx1 = cpu_sample(spec, osizes, total_out // 64, args.seed + 1)
+        one_gbs, reps1 = decode_rate(idx1, 1, 2.0)
+        eidx = cpu_sample(spec, osizes, total_out // 16, args.seed + 2)
+        enc_all, _, enc_kind = cpu_encode_rate(spec, host_in, ooffs, osizes, eidx, threads)
+        eidx1 = cpu_sample(spec, osizes, total_out // 128, args.seed + 4)
+        enc_one, _, _ = cpu_encode_rate(spec, host_in, ooffs, osizes, eidx1, 1)
+        cpu = {"value": round(all_gbs, 4), "unit": "GB/s", "cores": threads, "kind": dec.kind,
                "sample": "%d of %d frames (%.1f MiB decoded), %d passes, %d threads" % (
-                   len(idx), n_frames, sum(osizes[i] for i in idx) / 2**20, reps, threads)}
+                   len(idx), n_frames, sum(osizes[i] for i in idx) / 2**20, reps, threads),
+               "one_core": {"value": round(one_gbs, 4), "unit": "GB/s", "cores": 1,
+                            "sample": "%d frames (%.1f MiB), %d passes" % (
+                                len(idx1), sum(osizes[i] for i in idx1) / 2**20, reps1)},
+               "encode": {"value": round(enc_all, 4), "unit": "GB/s", "cores": threads, "kind": enc_kind,
+                          "one_core": round(enc_one, 4),
+                          "sample": "%d frames (%.1f MiB) on %d threads; %d frames on 1 thread" % (
+                              len(eidx), sum(osizes[i] for i in eidx) / 2**20, threads, len(eidx1))}}
+        if dec.kind == "port":
+            cpu["note"] = PORT_NOTE
 
     srt = sorted(step_ms)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded random walks)",
-        "config": {"workload": WORKLOAD, "frames": n_frames, "decoded_bytes": total_out,
-                   "compressed_bytes": total_comp, "ratio": round(total_out / total_comp, 3),
-                   "graphs": "delta->tsplit->FSE | delta->bitpack->Huffman", "format_version": 23,
-                   "checksums": "content+compressed, verified on device", "l2": "inputs larger than L2 (no flush)",
-                   "parts_per_kind": args.parts_per_kind or "library default"},
+        "config": workload_config(n_frames, total_out, total_comp, args.parts_per_kind),
         "frac_hbm": round(value / ws / peak, 4),
         "p50_ms": round(statistics.median(step_ms), 4),
         "p99_ms": round(srt[min(len(srt) - 1, int(round(0.99 * (len(srt) - 1))))], 4),
@@ -831,10 +1065,12 @@ def main():
         "single_array": single,
         "serving": serving,
         "columnar": columnar,
-        "encode": {"value": round(enc_gbs, 3), "unit": "GB/s", "note": "batched compress, host decisions included"},
+        "encode": {"value": round(enc_gbs, 3), "unit": "GB/s", "note": "batched compress, host decisions included",
+                   "parity": enc_parity},
         "autotune": tuned,
         "roofline": roofline,
         "cpu_baseline": cpu,
+        "encode_parity": enc_parity,
         "e2e": e2e,
         "gpu_launches": launches * args.steps,
         "clocks": clk,

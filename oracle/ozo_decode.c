@@ -132,6 +132,51 @@ static inline void bc_skip(BCont* r, int nb)
     if (r->pos - r->base < 32 && r->base > 0) bc_fill(r);
 }
 
+/* Fast reader for the bulk of a stream (the same bits as BCont): `c` holds
+ * the 8 stream bytes at `p`, of which the top `used` bits have been read. A
+ * refill moves p down by the whole bytes read. The fast loops run only while
+ * p is at least 8 bytes above the stream's first byte, so a group of up to
+ * 56 bits and its refill never reach position 0; the rest of the stream
+ * continues on BCont (bc_at). */
+typedef struct {
+    const uint8_t* p;
+    uint64_t c;
+    unsigned used;
+} BFast;
+
+static inline void bf_from(BFast* f, const uint8_t* src, int64_t pos) /* pos >= 64 */
+{
+    int64_t const top = (pos + 7) >> 3; /* bytes [0, top) hold the unread bits */
+    f->p = src + top - 8;
+    f->c = le64_at(f->p);
+    f->used = (unsigned)(top * 8 - pos);
+}
+static inline int64_t bf_pos(const BFast* f, const uint8_t* src)
+{
+    return (int64_t)(f->p - src) * 8 + 64 - (int64_t)f->used;
+}
+/* nb in [0, 32]: the next nb bits (0 for nb = 0) */
+static inline uint32_t bf_read(BFast* f, unsigned nb)
+{
+    uint32_t const v = (uint32_t)(((f->c << f->used) >> 1) >> (63 - nb));
+    f->used += nb;
+    return v;
+}
+static inline uint32_t bf_peek(const BFast* f, unsigned nb) { return (uint32_t)((f->c << f->used) >> (64 - nb)); }
+static inline void bf_refill(BFast* f)
+{
+    f->p -= f->used >> 3;
+    f->used &= 7;
+    f->c = le64_at(f->p);
+}
+static inline void bc_at(BCont* r, const uint8_t* src, size_t size, int64_t pos)
+{
+    r->src = src;
+    r->size = size;
+    r->pos = pos;
+    bc_fill(r);
+}
+
 /* ---------------------------------------------------------------------
  * FSE normalized-count header (src/openzl/fse/common/entropy_common.c:42-185,
  * FSE_readNCount): 4 bits tableLog-5, then per symbol a variable-width count
@@ -249,14 +294,56 @@ static int fse_decode(uint8_t* dst, size_t dstSize, const uint8_t* src, size_t s
     }
     if (dstSize < nbStates) return -OZO_ERR_CORRUPTION;
     size_t const lastTransition = dstSize - nbStates;
-    for (size_t i = 0; i < dstSize; i++) {
-        unsigned const k = (unsigned)(i % nbStates);
+    size_t i = 0;
+    /* bulk: four symbols (at most 48 bits, tableLog <= 12) per refill */
+    if (r.pos >= 64 && tableLog <= 12) {
+        BFast f;
+        bf_from(&f, src, r.pos);
+        if (nbStates == 4) {
+            uint32_t s0 = st[0], s1 = st[1], s2 = st[2], s3 = st[3];
+            while (i + 4 <= lastTransition && f.p - src >= 8) {
+                FseD const e0 = dt[s0], e1 = dt[s1], e2 = dt[s2], e3 = dt[s3];
+                dst[i] = e0.symbol;
+                dst[i + 1] = e1.symbol;
+                dst[i + 2] = e2.symbol;
+                dst[i + 3] = e3.symbol;
+                s0 = e0.newState + bf_read(&f, e0.nbBits);
+                s1 = e1.newState + bf_read(&f, e1.nbBits);
+                s2 = e2.newState + bf_read(&f, e2.nbBits);
+                s3 = e3.newState + bf_read(&f, e3.nbBits);
+                bf_refill(&f);
+                i += 4;
+            }
+            st[0] = s0, st[1] = s1, st[2] = s2, st[3] = s3;
+        } else {
+            uint32_t s0 = st[0], s1 = st[1];
+            while (i + 4 <= lastTransition && f.p - src >= 8) {
+                FseD e0 = dt[s0], e1 = dt[s1];
+                dst[i] = e0.symbol;
+                dst[i + 1] = e1.symbol;
+                s0 = e0.newState + bf_read(&f, e0.nbBits);
+                s1 = e1.newState + bf_read(&f, e1.nbBits);
+                e0 = dt[s0], e1 = dt[s1];
+                dst[i + 2] = e0.symbol;
+                dst[i + 3] = e1.symbol;
+                s0 = e0.newState + bf_read(&f, e0.nbBits);
+                s1 = e1.newState + bf_read(&f, e1.nbBits);
+                bf_refill(&f);
+                i += 4;
+            }
+            st[0] = s0, st[1] = s1;
+        }
+        bc_at(&r, src, srcSize, bf_pos(&f, src));
+    }
+    /* i is a multiple of nbStates here: state k produces symbols i = k mod nbStates */
+    for (unsigned k = 0; i < dstSize; i++) {
         FseD const e = dt[st[k]];
         dst[i] = e.symbol;
         if (i < lastTransition) {
             st[k] = e.newState + bc_peek(&r, e.nbBits);
             bc_skip(&r, e.nbBits);
         }
+        if (++k == nbStates) k = 0;
     }
     if (r.pos != 0) return -OZO_ERR_CORRUPTION;
     return 0;
@@ -304,18 +391,40 @@ static int huf_build_dtable(HufD* dt, unsigned* tableLogOut, const uint8_t* weig
     return 0;
 }
 
-static int huf_decode_stream(uint8_t* dst, size_t n, const uint8_t* src, size_t size,
-                             const HufD* dt, unsigned tableLog)
+/* The tail of one stream from symbol i on (the careful reader). */
+static int huf_finish(uint8_t* dst, size_t i, size_t n, BCont* rp, const HufD* dt, unsigned tableLog)
 {
-    BCont r;
-    if (bc_init(&r, src, size)) return -OZO_ERR_CORRUPTION;
-    for (size_t i = 0; i < n; i++) {
+    BCont r = *rp;
+    for (; i < n; i++) {
         HufD const e = dt[bc_peek(&r, (int)tableLog)];
         dst[i] = e.symbol;
         bc_skip(&r, e.nbBits);
     }
     if (r.pos != 0) return -OZO_ERR_CORRUPTION;
     return 0;
+}
+
+static int huf_decode_stream(uint8_t* dst, size_t n, const uint8_t* src, size_t size,
+                             const HufD* dt, unsigned tableLog)
+{
+    BCont r;
+    if (bc_init(&r, src, size)) return -OZO_ERR_CORRUPTION;
+    size_t i = 0;
+    if (r.pos >= 64 && tableLog <= 12) { /* four codes (<= 48 bits) per refill */
+        BFast f;
+        bf_from(&f, src, r.pos);
+        while (i + 4 <= n && f.p - src >= 8) {
+            for (int k = 0; k < 4; k++) {
+                HufD const e = dt[bf_peek(&f, tableLog)];
+                dst[i + k] = e.symbol;
+                f.used += e.nbBits;
+            }
+            bf_refill(&f);
+            i += 4;
+        }
+        bc_at(&r, src, size, bf_pos(&f, src));
+    }
+    return huf_finish(dst, i, n, &r, dt, tableLog);
 }
 
 /* 4-stream layout: 6-byte jump table of three LE16 stream sizes, output split
@@ -331,11 +440,59 @@ static int huf_decode_4x(uint8_t* dst, size_t n, const uint8_t* src, size_t size
     size_t const seg = (n + 3) / 4;
     if (3 * seg > n) return -OZO_ERR_CORRUPTION;
     const uint8_t* s = src + 6;
-    int rc;
-    if ((rc = huf_decode_stream(dst, seg, s, l1, dt, tableLog))) return rc;
-    if ((rc = huf_decode_stream(dst + seg, seg, s + l1, l2, dt, tableLog))) return rc;
-    if ((rc = huf_decode_stream(dst + 2 * seg, seg, s + l1 + l2, l3, dt, tableLog))) return rc;
-    return huf_decode_stream(dst + 3 * seg, n - 3 * seg, s + l1 + l2 + l3, l4, dt, tableLog);
+    const uint8_t* const ss[4] = { s, s + l1, s + l1 + l2, s + l1 + l2 + l3 };
+    size_t const sz[4] = { l1, l2, l3, l4 };
+    size_t const cnt[4] = { seg, seg, seg, n - 3 * seg };
+    BCont r[4];
+    for (int k = 0; k < 4; k++)
+        if (bc_init(&r[k], ss[k], sz[k])) return -OZO_ERR_CORRUPTION;
+    size_t i = 0;
+    /* the four streams interleaved, four codes each per refill, while every
+     * stream has room */
+    if (tableLog <= 12 && r[0].pos >= 64 && r[1].pos >= 64 && r[2].pos >= 64 && r[3].pos >= 64) {
+        BFast f[4];
+        for (int k = 0; k < 4; k++) bf_from(&f[k], ss[k], r[k].pos);
+        /* the four readers in locals: container, bits read, byte position */
+        uint64_t c0 = f[0].c, c1 = f[1].c, c2 = f[2].c, c3 = f[3].c;
+        unsigned u0 = f[0].used, u1 = f[1].used, u2 = f[2].used, u3 = f[3].used;
+        const uint8_t *p0 = f[0].p, *p1 = f[1].p, *p2 = f[2].p, *p3 = f[3].p;
+        const uint8_t *lo0 = ss[0] + 8, *lo1 = ss[1] + 8, *lo2 = ss[2] + 8, *lo3 = ss[3] + 8;
+        unsigned const sh = 64 - tableLog;
+        uint8_t* const o1 = dst + seg;
+        uint8_t* const o2 = dst + 2 * seg;
+        uint8_t* const o3 = dst + 3 * seg;
+        while (i + 4 <= seg && p0 >= lo0 && p1 >= lo1 && p2 >= lo2 && p3 >= lo3) {
+            for (int k = 0; k < 4; k++) {
+                HufD const e0 = dt[(c0 << u0) >> sh];
+                HufD const e1 = dt[(c1 << u1) >> sh];
+                HufD const e2 = dt[(c2 << u2) >> sh];
+                HufD const e3 = dt[(c3 << u3) >> sh];
+                dst[i + k] = e0.symbol;
+                o1[i + k] = e1.symbol;
+                o2[i + k] = e2.symbol;
+                o3[i + k] = e3.symbol;
+                u0 += e0.nbBits;
+                u1 += e1.nbBits;
+                u2 += e2.nbBits;
+                u3 += e3.nbBits;
+            }
+            p0 -= u0 >> 3, u0 &= 7, c0 = le64_at(p0);
+            p1 -= u1 >> 3, u1 &= 7, c1 = le64_at(p1);
+            p2 -= u2 >> 3, u2 &= 7, c2 = le64_at(p2);
+            p3 -= u3 >> 3, u3 &= 7, c3 = le64_at(p3);
+            i += 4;
+        }
+        f[0].c = c0, f[1].c = c1, f[2].c = c2, f[3].c = c3;
+        f[0].used = u0, f[1].used = u1, f[2].used = u2, f[3].used = u3;
+        f[0].p = p0, f[1].p = p1, f[2].p = p2, f[3].p = p3;
+        for (int k = 0; k < 4; k++) bc_at(&r[k], ss[k], sz[k], bf_pos(&f[k], ss[k]));
+    }
+    for (int k = 0; k < 4; k++) {
+        size_t const from = i < cnt[k] ? i : cnt[k];
+        int const rc = huf_finish(dst + k * seg, from, cnt[k], &r[k], dt, tableLog);
+        if (rc) return rc;
+    }
+    return 0;
 }
 
 /* ---------------------------------------------------------------------
@@ -579,6 +736,18 @@ static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, s
             for (size_t i = 0; i < nbIn; i++)
                 if (in[i]->type != OZO_TYPE_SERIAL || in[i]->n != n) return -OZO_ERR_CORRUPTION;
             uint8_t* o = ost_alloc(out, OZO_TYPE_STRUCT, W, n);
+            if (W == 2 || W == 4 || W == 8) { /* element-major: one pass over the output */
+                const uint8_t* pl[8];
+                for (size_t b = 0; b < W; b++) pl[b] = in[b]->p;
+                for (size_t e = 0; e < n; e++) {
+                    uint64_t v = 0;
+                    for (size_t b = 0; b < W; b++) v |= (uint64_t)pl[b][e] << (8 * b);
+                    if (W == 2) ozo_wr16(o + 2 * e, (uint16_t)v);
+                    else if (W == 4) ozo_wr32(o + 4 * e, (uint32_t)v);
+                    else ozo_wr64(o + 8 * e, v);
+                }
+                return 0;
+            }
             for (size_t b = 0; b < W; b++) {
                 const uint8_t* const pl = in[b]->p;
                 uint8_t* const ob = o + b;
@@ -636,15 +805,55 @@ static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, s
             }
             if ((n * (size_t)nbBits + 7) / 8 != srcSize) return -OZO_ERR_CORRUPTION;
             uint8_t* o = ost_alloc(out, sg.outType, w, n);
-            uint64_t* tmp = (uint64_t*)malloc((n + 1) * 8);
-            bitunpack(tmp, n, in[0]->p, srcSize, nbBits);
-            switch (w) {
-                case 1: for (size_t i = 0; i < n; i++) o[i] = (uint8_t)tmp[i]; break;
-                case 2: for (size_t i = 0; i < n; i++) { uint16_t x = (uint16_t)tmp[i]; ozo_wr16(o + 2 * i, x); } break;
-                case 4: for (size_t i = 0; i < n; i++) ozo_wr32(o + 4 * i, (uint32_t)tmp[i]); break;
-                default: for (size_t i = 0; i < n; i++) ozo_wr64(o + 8 * i, tmp[i]); break;
+            const uint8_t* const src = in[0]->p;
+            uint64_t const mask = nbBits >= 64 ? ~0ull : ((1ull << nbBits) - 1);
+            /* bulk: fields whose 8-byte load stays inside the source and
+             * holds the whole field; the rest through bitunpack */
+            size_t i = 0;
+            if ((size_t)nbBits == 8 * w) { /* whole elements: the packing is the identity */
+                memcpy(o, src, n * w);
+                i = n;
+            } else if (nbBits > 56) { /* 57..63 bits: the field spans up to 9 bytes */
+                size_t const fast = srcSize >= 9 ? ((srcSize - 9) * 8) / (size_t)nbBits : 0;
+                size_t const m = fast < n ? fast : n;
+                for (; i < m; i++) {
+                    size_t const bit = i * (size_t)nbBits;
+                    unsigned const sh = (unsigned)(bit & 7);
+                    uint64_t v = le64_at(src + (bit >> 3)) >> sh;
+                    if (sh) v |= (uint64_t)src[(bit >> 3) + 8] << (64 - sh);
+                    ozo_wr64(o + 8 * i, v & mask);
+                }
+            } else {
+                size_t const fast = srcSize >= 8 ? ((srcSize - 8) * 8) / (size_t)nbBits : 0;
+                size_t const m = fast < n ? fast : n;
+#define OZO_UNPACK_W(T, WR)                                                  \
+    for (; i < m; i++) {                                                     \
+        size_t const bit = i * (size_t)nbBits;                               \
+        uint64_t const v = (le64_at(src + (bit >> 3)) >> (bit & 7)) & mask;  \
+        WR;                                                                  \
+    }
+                switch (w) {
+                    case 1: OZO_UNPACK_W(uint8_t, o[i] = (uint8_t)v) break;
+                    case 2: OZO_UNPACK_W(uint16_t, ozo_wr16(o + 2 * i, (uint16_t)v)) break;
+                    case 4: OZO_UNPACK_W(uint32_t, ozo_wr32(o + 4 * i, (uint32_t)v)) break;
+                    default: OZO_UNPACK_W(uint64_t, ozo_wr64(o + 8 * i, v)) break;
+                }
+#undef OZO_UNPACK_W
             }
-            free(tmp);
+            for (; i < n; i++) { /* the last fields, bit by bit */
+                size_t const bit = i * (size_t)nbBits;
+                uint64_t v = 0;
+                for (int q = 0; q < nbBits; q++) {
+                    size_t const bq = bit + (size_t)q;
+                    v |= (uint64_t)((src[bq >> 3] >> (bq & 7)) & 1) << q;
+                }
+                switch (w) {
+                    case 1: o[i] = (uint8_t)v; break;
+                    case 2: ozo_wr16(o + 2 * i, (uint16_t)v); break;
+                    case 4: ozo_wr32(o + 4 * i, (uint32_t)v); break;
+                    default: ozo_wr64(o + 8 * i, v); break;
+                }
+            }
             return 0;
         }
         case TR_FLATPACK: { /* decode_flatpack_binding.c, decode_flatpack_kernel.c:19-60 */

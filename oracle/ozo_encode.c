@@ -145,7 +145,19 @@ static void stats_init(Stats* st, const uint8_t* src, size_t n)
 {
     memset(st, 0, sizeof(*st));
     st->n = n;
-    for (size_t i = 0; i < n; i++) st->count[src[i]]++;
+    /* four partial tables, so that runs of one symbol do not serialize on
+     * one counter */
+    uint32_t part[4][256];
+    memset(part, 0, sizeof(part));
+    size_t i = 0;
+    for (; i + 4 <= n; i += 4) {
+        part[0][src[i]]++;
+        part[1][src[i + 1]]++;
+        part[2][src[i + 2]]++;
+        part[3][src[i + 3]]++;
+    }
+    for (; i < n; i++) part[0][src[i]]++;
+    for (int s = 0; s < 256; s++) st->count[s] = part[0][s] + part[1][s] + part[2][s] + part[3][s];
     for (int s = 0; s < 256; s++)
         if (st->count[s]) { st->card++; st->maxSym = (unsigned)s; }
 }
@@ -184,12 +196,18 @@ typedef struct {
     unsigned nb;
 } BW;
 
-static void bw_add(BW* b, uint64_t v, unsigned nb)
+/* moves the whole bytes of the accumulator to the buffer: one 8-byte store
+ * where it fits, else byte by byte up to the capacity */
+static inline void bw_flush(BW* b)
 {
-    if (!nb) return;
-    v &= nb == 64 ? ~0ull : ((1ull << nb) - 1);
-    b->acc |= v << b->nb;
-    b->nb += nb;
+    if (b->pos + 8 <= b->cap) {
+        ozo_wr64(b->buf + b->pos, b->acc);
+        unsigned const k = b->nb >> 3;
+        b->pos += k;
+        b->acc = k == 8 ? 0 : b->acc >> (8 * k);
+        b->nb &= 7;
+        return;
+    }
     while (b->nb >= 8) {
         if (b->pos < b->cap) b->buf[b->pos] = (uint8_t)b->acc;
         b->pos++;
@@ -197,10 +215,23 @@ static void bw_add(BW* b, uint64_t v, unsigned nb)
         b->nb -= 8;
     }
 }
-
+static inline void bw_add(BW* b, uint64_t v, unsigned nb)
+{
+    if (!nb) return;
+    if (nb > 32) { /* two halves, low first */
+        bw_add(b, v & 0xFFFFFFFFu, 32);
+        bw_add(b, v >> 32, nb - 32);
+        return;
+    }
+    v &= (1ull << nb) - 1;
+    if (b->nb + nb > 64) bw_flush(b);
+    b->acc |= v << b->nb;
+    b->nb += nb;
+}
 static size_t bw_close(BW* b)
 {
     bw_add(b, 1, 1);
+    bw_flush(b);
     if (b->nb) {
         if (b->pos < b->cap) b->buf[b->pos] = (uint8_t)b->acc;
         b->pos++;
@@ -850,6 +881,7 @@ static size_t lhuf_stream(uint8_t* dst, size_t cap, const uint8_t* src, size_t n
         bw_add(&b, code[s], nbBits[s]);
     }
     bw_add(&b, 1, 1);
+    bw_flush(&b);
     size_t const full = b.pos;
     if (full >= bcap - 8) return 0;
     size_t const sz = full + (b.nb > 0);
@@ -961,9 +993,28 @@ static int node_delta(ECtx* c, int in)
     if (n) {
         memcpy(nd->hdr, I->data, w);
         nd->hsz = w;
-        uint64_t const m = w == 8 ? ~0ull : ((1ull << (8 * w)) - 1);
-        for (size_t i = 1; i < n; i++)
-            wr(S(o)->data + (i - 1) * w, (rd(I->data + i * w, w) - rd(I->data + (i - 1) * w, w)) & m, w);
+        const uint8_t* const x = I->data;
+        uint8_t* const d = S(o)->data;
+#define OZO_DELTA_ENC(T)                                  \
+    for (size_t i = 1; i < n; i++) {                      \
+        T a, b;                                           \
+        memcpy(&a, x + (i - 1) * sizeof(T), sizeof(T));   \
+        memcpy(&b, x + i * sizeof(T), sizeof(T));         \
+        b = (T)(b - a);                                   \
+        memcpy(d + (i - 1) * sizeof(T), &b, sizeof(T));   \
+    }
+        switch (w) {
+            case 1: OZO_DELTA_ENC(uint8_t) break;
+            case 2: OZO_DELTA_ENC(uint16_t) break;
+            case 4: OZO_DELTA_ENC(uint32_t) break;
+            case 8: OZO_DELTA_ENC(uint64_t) break;
+            default: {
+                uint64_t const m = (1ull << (8 * w)) - 1;
+                for (size_t i = 1; i < n; i++)
+                    wr(d + (i - 1) * w, (rd(x + i * w, w) - rd(x + (i - 1) * w, w)) & m, w);
+            }
+        }
+#undef OZO_DELTA_ENC
     }
     return o;
 }
@@ -989,10 +1040,25 @@ static int node_bitpack(ECtx* c, int in, unsigned trid)
 {
     size_t const w = S(in)->w, n = S(in)->n;
     uint64_t mx = 0;
-    for (size_t i = 0; i < n; i++) {
-        uint64_t v = rd(S(in)->data + i * w, w);
-        if (v > mx) mx = v;
+    const uint8_t* const x = S(in)->data;
+#define OZO_MAX_W(T)                                  \
+    for (size_t i = 0; i < n; i++) {                  \
+        T v;                                          \
+        memcpy(&v, x + i * sizeof(T), sizeof(T));     \
+        if (v > mx) mx = v;                           \
     }
+    switch (w) {
+        case 1: OZO_MAX_W(uint8_t) break;
+        case 2: OZO_MAX_W(uint16_t) break;
+        case 4: OZO_MAX_W(uint32_t) break;
+        case 8: OZO_MAX_W(uint64_t) break;
+        default:
+            for (size_t i = 0; i < n; i++) {
+                uint64_t v = rd(x + i * w, w);
+                if (v > mx) mx = v;
+            }
+    }
+#undef OZO_MAX_W
     int const nbBits = 1 + (mx ? ozo_highbit64(mx) : 0);
     size_t const dstSize = (n * (size_t)nbBits + 7) / 8;
     ENode* nd = new_node(c, trid, in, 1);
@@ -1000,11 +1066,25 @@ static int node_bitpack(ECtx* c, int in, unsigned trid)
     nd->nbOut = 1;
     uint8_t* d = S(o)->data;
     memset(d, 0, dstSize + 8);
+    /* LSB-first: fields go into a 128-bit accumulator above the bits not yet
+     * written; whole 64-bit words are flushed */
+    unsigned __int128 acc = 0;
+    unsigned nacc = 0;
+    uint8_t* q = d;
     for (size_t i = 0; i < n; i++) {
-        uint64_t v = rd(S(in)->data + i * w, w);
-        size_t bit = i * (size_t)nbBits;
-        for (int b = 0; b < nbBits; b++, bit++)
-            if ((v >> b) & 1) d[bit >> 3] |= (uint8_t)(1u << (bit & 7));
+        uint64_t const v = rd(S(in)->data + i * w, w);
+        acc |= (unsigned __int128)v << nacc;
+        nacc += (unsigned)nbBits;
+        if (nacc >= 64) {
+            ozo_wr64(q, (uint64_t)acc);
+            q += 8;
+            acc >>= 64;
+            nacc -= 64;
+        }
+    }
+    for (; nacc > 0; nacc = nacc > 8 ? nacc - 8 : 0) {
+        *q++ = (uint8_t)acc;
+        acc >>= 8;
     }
     size_t const maxN = dstSize * 8 / (size_t)nbBits;
     static const uint8_t lg[9] = { 0, 0, 1, 0, 2, 0, 0, 0, 3 };
@@ -1023,10 +1103,23 @@ static int node_tsplit(ECtx* c, int in)
     size_t const W = S(in)->w, n = S(in)->n;
     ENode* nd = new_node(c, TR_TRANSPOSE_SPLIT, in, 0);
     int first = -1;
+    uint8_t* planes[8];
     for (size_t b = 0; b < W; b++) {
         int o = new_stream(c, OZO_TYPE_SERIAL, 1, n, NULL);
         if (first < 0) first = o;
-        for (size_t e = 0; e < n; e++) S(o)->data[e] = S(in)->data[e * W + b];
+        if (b < 8) planes[b] = S(o)->data;
+    }
+    const uint8_t* const x = S(in)->data;
+    if (W == 2 || W == 4 || W == 8) { /* element-major: one pass over the input */
+        for (size_t e = 0; e < n; e++) {
+            uint64_t const v = rd(x + e * W, W);
+            for (size_t b = 0; b < W; b++) planes[b][e] = (uint8_t)(v >> (8 * b));
+        }
+    } else {
+        for (size_t b = 0; b < W; b++) {
+            uint8_t* const pl = S(first + (int)b)->data;
+            for (size_t e = 0; e < n; e++) pl[e] = x[e * W + b];
+        }
     }
     nd->nbOut = (int)W;
     return first;
@@ -1531,6 +1624,12 @@ static void out_push(Out* o, uint8_t b)
     else o->overflow = 1;
     o->pos++;
 }
+static void out_bytes(Out* o, const uint8_t* src, size_t n)
+{
+    if (n && o->pos + n <= o->cap) memcpy(o->p + o->pos, src, n);
+    else if (n) o->overflow = 1;
+    o->pos += n;
+}
 static void out_varint(Out* o, uint64_t v)
 {
     uint8_t t[10];
@@ -1607,7 +1706,7 @@ static int64_t write_frame(ECtx* c, uint8_t* dst, size_t cap, int checksums)
     }
     for (size_t i = c->ns; i-- > 0;)
         if (c->s[i].store)
-            for (size_t b = 0; b < c->s[i].n * c->s[i].w; b++) out_push(&o, c->s[i].data[b]);
+            out_bytes(&o, c->s[i].data, c->s[i].n * c->s[i].w);
     if (checksums) {
         uint32_t const h = (uint32_t)ozo_xxh3_64(in0->data, in0->n * in0->w);
         for (int b = 0; b < 4; b++) out_push(&o, (uint8_t)(h >> (8 * b)));

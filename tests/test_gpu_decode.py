@@ -372,7 +372,9 @@ def test_fse_tablelog12_streams(gpu_lib):
     outs = [torch.zeros(a.nbytes + 64, dtype=torch.uint8, device="cuda") for _, a, _, _ in cases]
     b = oz.GpuBatch()
     b.plan(frames, [t.data_ptr() for t in dfr], [o.data_ptr() for o in outs], [a.nbytes for _, a, _, _ in cases])
-    b.run(torch.cuda.current_stream().cuda_stream, graph=True)
-    b.check(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()  # graph capture needs a non-default stream
+    b.run(side.cuda_stream, graph=True)
+    b.check(side.cuda_stream)
     for (_, a, _, _), o in zip(cases, outs):
         assert o[:a.nbytes].cpu().numpy().tobytes() == a.tobytes()
