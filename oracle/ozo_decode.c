@@ -1241,6 +1241,8 @@ static int64_t decode_block(const FrameHdr* fh, const uint8_t* src, size_t size,
     uint32_t* dists = NULL;
     OStream* streams = NULL;
     int64_t ret = 0;
+    OStream** insHeap = NULL; /* decoder input lists longer than 300 */
+    size_t insHeapCap = 0;
 #define FAIL(code) do { ret = -(code); goto done; } while (0)
     size_t r;
     /* codec types: 1 bit each */
@@ -1374,8 +1376,17 @@ static int64_t decode_block(const FrameHdr* fh, const uint8_t* src, size_t size,
         for (size_t u = 0; u < nd; u++) {
             DecSig const sg = sig_of(nodes[u].id);
             size_t const nbIn = (size_t)sg.nbSO + nodes[u].nbVOs;
-            OStream* ins[300];
-            if (nbIn > 300) FAIL(OZO_ERR_UNSUPPORTED);
+            OStream* insFixed[300];
+            OStream** ins = insFixed;
+            if (nbIn > 300) { /* concatenations of many chunks */
+                if (nbIn > insHeapCap) {
+                    OStream** g = (OStream**)realloc(insHeap, nbIn * sizeof(OStream*));
+                    if (!g) FAIL(OZO_ERR_ALLOC);
+                    insHeap = g;
+                    insHeapCap = nbIn;
+                }
+                ins = insHeap;
+            }
             for (size_t k = 0; k < nbIn; k++) {
                 OStream* s = &streams[sidx + k];
                 size_t const inb = nbIn - 1 - k;
@@ -1454,6 +1465,7 @@ done:
     free(trt);
     free(storedSizes);
     free(dists);
+    free(insHeap);
     return ret;
 }
 

@@ -296,3 +296,24 @@ def test_tablelog12_frames_decode_in_oracle_and_reference():
             out = np.zeros(arr.nbytes + 64, np.uint8)
             n = ref.ref_decompress_into(fr.ctypes.data, fr.size, out.ctypes.data, out.size, 1)
             assert n == arr.nbytes and out[:n].tobytes() == arr.tobytes()
+
+
+def test_oracle_frames_of_many_chunks():
+    """A concatenation of more than 300 entropy chunks (a 12 MB serial input
+    cut into 32 KiB chunks) decodes, and the encoder's frame equals the
+    reference's."""
+    import ctypes
+
+    rng = np.random.default_rng(300)
+    a = (rng.zipf(1.3, 12 << 20) % 256).astype(np.uint8)
+    fr = oracle.compress(8, a, 0)
+    data, _, _ = oracle.decompress(fr)
+    assert data.tobytes() == a.tobytes()
+    if os.path.exists(REF_DRIVER):
+        ref = ctypes.CDLL(REF_DRIVER)
+        ref.ref_compress.restype = ctypes.c_int64
+        ref.ref_compress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                                     ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+        dst = np.zeros(a.size * 2 + 65536, np.uint8)
+        n = ref.ref_compress(8, a.ctypes.data, a.size, 0, dst.ctypes.data, dst.size, 1, 0)
+        assert n == fr.size and dst[:n].tobytes() == fr.tobytes()
