@@ -20,6 +20,7 @@
 #include <cstring>
 #include <functional>
 #include <type_traits>
+#include <unordered_map>
 
 namespace ozl {
 
@@ -1382,6 +1383,35 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
     }
     out.launches.clear();
     uint64_t scratch = 0;
+    // ---- checksums: block sums first in the scratch. A content checksum of
+    // an output that one numeric-pipeline task writes whole, from its first
+    // byte, gets its block sums from that task's output pass; the hash
+    // launch's phase 1 covers the other checksums' blocks only.
+    struct HashPlace { size_t hash; uint64_t sumsOff; uint32_t nbBlocks; bool fused; };
+    std::vector<HashPlace> hp;
+    for (size_t k = 0; k < plan.hashes.size(); k++) {
+        const PlanHash& h = plan.hashes[k];
+        if (!inPart(h.frame)) continue;
+        uint32_t const nb = h.len > 240 ? uint32_t((h.len - 1) / kHashBlock) : 0;
+        hp.push_back(HashPlace{ k, scratch, nb, false });
+        scratch += (uint64_t(nb) * 64 + 255) & ~uint64_t(255);
+    }
+    {
+        std::unordered_map<const uint8_t*, NumPipeTask*> numByOut;
+        for (Buckets& b : B)
+            for (NumPipeTask& t : b.num) numByOut.emplace(t.out, &t);
+        for (HashPlace& p : hp) {
+            const PlanHash& h = plan.hashes[p.hash];
+            if (h.where != HW_OUTPUT || !p.nbBlocks) continue;
+            auto it = numByOut.find(dOuts[h.frame] + h.off);
+            if (it == numByOut.end()) continue;
+            NumPipeTask& t = *it->second;
+            if (t.blockSums || t.n * t.w < uint64_t(p.nbBlocks) * kHashBlock) continue;
+            t.blockSums = reinterpret_cast<uint64_t*>(dScratch + p.sumsOff);
+            t.hashBlocks = p.nbBlocks;
+            p.fused = true;
+        }
+    }
     auto addTiled = [&](int kind, int lv, auto& tasks, auto tilesOf) {
         if (tasks.empty()) return;
         std::vector<TileRef> tiles;
@@ -1465,13 +1495,11 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
         addTiled(KIND_NUMPIPE, lv, b.num, [](const NumPipeTask& t) { return ceilDiv(t.n, kNumTileBytes / t.w); });
     }
     // checksums: one launch after everything else
-    bool anyHash = false;
-    for (const PlanHash& h : plan.hashes) anyHash |= inPart(h.frame);
-    if (anyHash) {
+    if (!hp.empty()) {
         std::vector<HashTask> ht;
         std::vector<TileRef> blocks;
-        for (const PlanHash& h : plan.hashes) {
-            if (!inPart(h.frame)) continue;
+        for (const HashPlace& p : hp) {
+            const PlanHash& h = plan.hashes[p.hash];
             HashTask t{};
             t.data = h.where == HW_OUTPUT ? dOuts[h.frame] + h.off
                    : h.where == HW_ARENA  ? dArena + h.off
@@ -1481,14 +1509,13 @@ int layoutPlan(const DecodePlan& plan, const uint8_t* const* dFrames, uint8_t* c
             t.errCode = h.err;
             t.low8 = h.low8 ? 1 : 0;
             t.aligned8 = (reinterpret_cast<uintptr_t>(t.data) & 7) == 0;
-            t.nbBlocks = h.len > 240 ? uint32_t((h.len - 1) / kHashBlock) : 0;
+            t.nbBlocks = p.nbBlocks;
+            t.blockSums = reinterpret_cast<uint64_t*>(dScratch + p.sumsOff);
             t.blockBase = uint32_t(blocks.size());
-            for (uint32_t k = 0; k < t.nbBlocks; k++) blocks.push_back(TileRef{ uint32_t(ht.size()), k });
+            if (!p.fused)
+                for (uint32_t k = 0; k < t.nbBlocks; k++) blocks.push_back(TileRef{ uint32_t(ht.size()), k });
             ht.push_back(t);
         }
-        uint64_t const sumsOff = scratch;
-        scratch += ((uint64_t)blocks.size() * 64 + 255) & ~uint64_t(255);
-        for (HashTask& t : ht) t.blockSums = reinterpret_cast<uint64_t*>(dScratch + sumsOff) + 8ull * t.blockBase;
         Launch L{};
         for (const HashTask& t : ht) L.algoBytes += t.len;
         L.kind = KIND_HASH;

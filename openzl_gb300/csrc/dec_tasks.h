@@ -38,6 +38,11 @@ struct NumPipeTask {
     uint8_t delta;                // source holds n-1 elements when set
     uint32_t tileBase;            // first tile index of this task in its launch
     uint32_t nbTiles;
+    // Content checksum fused into the output pass: when set, the XXH3 block
+    // sums (8 lanes per 1 KiB block, as kHashBlocks writes them) of the first
+    // hashBlocks blocks of `out` are written here.
+    uint64_t* blockSums;
+    uint32_t hashBlocks;
 };
 
 // Generic transpose-split for arbitrary widths: out[i*W + b] = planes[b][i].

@@ -152,6 +152,45 @@ __global__ void kConst(const ConstTask* __restrict__ tasks, const TileRef* __res
     }
 }
 
+// XXH3's published secret and primes (the checksum kernels below and the
+// content-checksum block sums fused into the numeric pipeline).
+__constant__ uint8_t kXxhSecret[192] = {
+    0xb8, 0xfe, 0x6c, 0x39, 0x23, 0xa4, 0x4b, 0xbe, 0x7c, 0x01, 0x81, 0x2c, 0xf7, 0x21, 0xad, 0x1c,
+    0xde, 0xd4, 0x6d, 0xe9, 0x83, 0x90, 0x97, 0xdb, 0x72, 0x40, 0xa4, 0xa4, 0xb7, 0xb3, 0x67, 0x1f,
+    0xcb, 0x79, 0xe6, 0x4e, 0xcc, 0xc0, 0xe5, 0x78, 0x82, 0x5a, 0xd0, 0x7d, 0xcc, 0xff, 0x72, 0x21,
+    0xb8, 0x08, 0x46, 0x74, 0xf7, 0x43, 0x24, 0x8e, 0xe0, 0x35, 0x90, 0xe6, 0x81, 0x3a, 0x26, 0x4c,
+    0x3c, 0x28, 0x52, 0xbb, 0x91, 0xc3, 0x00, 0xcb, 0x88, 0xd0, 0x65, 0x8b, 0x1b, 0x53, 0x2e, 0xa3,
+    0x71, 0x64, 0x48, 0x97, 0xa2, 0x0d, 0xf9, 0x4e, 0x38, 0x19, 0xef, 0x46, 0xa9, 0xde, 0xac, 0xd8,
+    0xa8, 0xfa, 0x76, 0x3f, 0xe3, 0x9c, 0x34, 0x3f, 0xf9, 0xdc, 0xbb, 0xc7, 0xc7, 0x0b, 0x4f, 0x1d,
+    0x8a, 0x51, 0xe0, 0x4b, 0xcd, 0xb4, 0x59, 0x31, 0xc8, 0x9f, 0x7e, 0xc9, 0xd9, 0x78, 0x73, 0x64,
+    0xea, 0xc5, 0xac, 0x83, 0x34, 0xd3, 0xeb, 0xc3, 0xc5, 0x81, 0xa0, 0xff, 0xfa, 0x13, 0x63, 0xeb,
+    0x17, 0x0d, 0xdd, 0x51, 0xb7, 0xf0, 0xda, 0x49, 0xd3, 0x16, 0x55, 0x26, 0x29, 0xd4, 0x68, 0x9e,
+    0x2b, 0x16, 0xbe, 0x58, 0x7d, 0x47, 0xa1, 0xfc, 0x8f, 0xf8, 0xb8, 0xd1, 0x7a, 0xd0, 0x31, 0xce,
+    0x45, 0xcb, 0x3a, 0x8f, 0x95, 0x16, 0x04, 0x28, 0xaf, 0xd7, 0xfb, 0xca, 0xbb, 0x4b, 0x40, 0x7e,
+};
+
+#define XP32_1 0x9E3779B1u
+#define XP32_2 0x85EBCA77u
+#define XP32_3 0xC2B2AE3Du
+#define XP64_1 0x9E3779B185EBCA87ull
+#define XP64_2 0xC2B2AE3D27D4EB4Full
+#define XP64_3 0x165667B19E3779F9ull
+#define XP64_4 0x85EBCA77C2B2AE63ull
+#define XP64_5 0x27D4EB2F165667C5ull
+#define XPMX1 0x165667919E3779F9ull
+#define XPMX2 0x9FB21C651E98DF25ull
+
+__device__ __forceinline__ uint64_t secret64(int off)
+{
+    uint64_t v = 0;
+    for (int b = 0; b < 8; b++) v |= uint64_t(kXxhSecret[off + b]) << (8 * b);
+    return v;
+}
+__device__ __forceinline__ uint32_t secret32(int off)
+{
+    return uint32_t(kXxhSecret[off]) | (uint32_t(kXxhSecret[off + 1]) << 8) | (uint32_t(kXxhSecret[off + 2]) << 16)
+            | (uint32_t(kXxhSecret[off + 3]) << 24);
+}
 // ---------------------------------------------------------------------------
 // Fused numeric pipeline: source (plain elements, byte planes or LSB-first
 // bit-packed fields) -> optional zigzag -> optional delta -> output elements.
@@ -482,7 +521,52 @@ __device__ __forceinline__ void npStore(uint8_t* out, uint32_t cnt, const uint32
 struct NPShared {
     uint32_t stage[kNPStagePadded];
     uint64_t warpVal[kNPThreads / 32];
+    uint64_t key[24]; // XXH3 secret words at byte offsets 0, 8, ..., 184 (fused block sums)
 };
+
+// XXH3 block sums of the output, fused into the output pass. The thread's 64
+// bytes (w, little-endian) are stripe tid % 16 of 1 KiB block `blk` of the
+// checksummed output; the 16 threads of a block are one half-warp. Each
+// thread adds its stripe's increments to 8 accumulators (acc[i ^ 1] +=
+// d[i]; acc[i] += lo32(d[i] ^ k[i]) * hi32(d[i] ^ k[i]), k[i] the secret word
+// at byte 8 (stripe + i)), then the half-warp reduce-scatters them: after
+// four exchanges (4 + 2 + 1 + 1 shuffles) every lane holds the block total of
+// accumulator 4 bit3 + 2 bit2 + bit1 of its lane index, and the even lane
+// writes it where phase 1 would have. Every lane of the warp takes part; only
+// blocks below hashBlocks are written.
+__device__ __forceinline__ void npHashStripe(const NumPipeTask& t, const uint32_t* w, uint64_t blk,
+                                             const uint64_t* key)
+{
+    uint32_t const lane = threadIdx.x & 31, s = lane & 15;
+    uint64_t acc[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) acc[i] = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        uint64_t const d = uint64_t(w[2 * i]) | (uint64_t(w[2 * i + 1]) << 32);
+        uint64_t const x = d ^ key[s + i];
+        acc[i ^ 1] += d;
+        acc[i] += uint64_t(uint32_t(x)) * (x >> 32);
+    }
+    bool const b3 = s & 8, b2 = s & 4, b1 = s & 2;
+    uint64_t v4[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        uint64_t const send = b3 ? acc[k] : acc[k + 4];
+        uint64_t const keep = b3 ? acc[k + 4] : acc[k];
+        v4[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    uint64_t v2[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        uint64_t const send = b2 ? v4[k] : v4[k + 2];
+        uint64_t const keep = b2 ? v4[k + 2] : v4[k];
+        v2[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    uint64_t v = (b1 ? v2[1] : v2[0]) + __shfl_xor_sync(0xffffffffu, b1 ? v2[0] : v2[1], 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    if (!(s & 1) && blk < t.hashBlocks) t.blockSums[8 * blk + 4 * b3 + 2 * b2 + b1] = v;
+}
 
 template <int W, int MODE>
 __device__ __forceinline__ void npReduceTile(const NumPipeTask& t, const TileRef& tr, uint64_t* sums, uint32_t g,
@@ -543,6 +627,7 @@ __device__ __forceinline__ void npTile(const NumPipeTask& t, const TileRef& tr, 
         npAdd<W>(w, t.first + prefix[g] + warpPre + (incl - tot));
     }
     if (cnt) npStore<W>(t.out + j0 * W, cnt, w);
+    if (t.blockSums) npHashStripe(t, w, (uint64_t(tr.tile) * kNumTileBytes + uint64_t(tid) * kNPBytes) >> 10, sh.key);
 }
 
 template <int W>
@@ -596,17 +681,32 @@ __global__ void __launch_bounds__(256) kNumPrefix(const NumPipeTask* __restrict_
     if (!t.delta) return;
     uint32_t const te = kNumTileBytes / t.w;
     uint32_t const nT = uint32_t((t.n + te - 1) / te);
+    // 256 tiles per round: lane L scans tiles 8L .. 8L + 7 of the round in
+    // registers, the warp scans the lanes' totals
+    const uint64_t* const in = sums + t.tileBase;
+    uint64_t* const out = prefix + t.tileBase;
     uint64_t running = 0;
-    for (uint32_t k0 = 0; k0 < nT; k0 += 32) {
-        uint32_t const k = k0 + lane;
-        uint64_t const x = k < nT ? sums[t.tileBase + k] : 0;
-        uint64_t incl = x;
+    for (uint32_t k0 = 0; k0 < nT; k0 += 256) {
+        uint32_t const k = k0 + 8 * lane;
+        uint64_t x[8];
+        uint64_t tot = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            x[j] = k + j < nT ? in[k + j] : 0;
+            tot += x[j];
+        }
+        uint64_t incl = tot;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             uint64_t const y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= uint32_t(o)) incl += y;
         }
-        if (k < nT) prefix[t.tileBase + k] = running + incl - x;
+        uint64_t run = running + incl - tot;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            if (k + j < nT) out[k + j] = run;
+            run += x[j];
+        }
         running += __shfl_sync(0xffffffffu, incl, 31);
     }
 }
@@ -620,6 +720,10 @@ __global__ void __launch_bounds__(kNPThreads) kNumPipe(const NumPipeTask* __rest
     uint32_t const g = blockIdx.x;
     TileRef const tr = tiles[g];
     NumPipeTask const t = tasks[tr.task];
+    if (t.blockSums) { // the same task for the whole CTA
+        if (threadIdx.x < 24) sh.key[threadIdx.x] = secret64(int(8 * threadIdx.x));
+        __syncthreads();
+    }
     switch (t.w) {
         case 1: npTileW<1>(t, tr, g, prefix, sh); break;
         case 2: npTileW<2>(t, tr, g, prefix, sh); break;
@@ -1492,45 +1596,10 @@ __global__ void __launch_bounds__(128) kHuf16(const Huf16Task* __restrict__ task
 // XXH3-64 checksums. Phase 1: per 1 KiB block, the 16-stripe sum of every
 // accumulator lane's increments (they commute within a block). Phase 2: per
 // task, the block chain acc = scramble(acc + blockSum) on 8 lanes, then the
-// tail stripes and the final merge on one lane. Constants are XXH3's
-// published secret and primes.
-__constant__ uint8_t kXxhSecret[192] = {
-    0xb8, 0xfe, 0x6c, 0x39, 0x23, 0xa4, 0x4b, 0xbe, 0x7c, 0x01, 0x81, 0x2c, 0xf7, 0x21, 0xad, 0x1c,
-    0xde, 0xd4, 0x6d, 0xe9, 0x83, 0x90, 0x97, 0xdb, 0x72, 0x40, 0xa4, 0xa4, 0xb7, 0xb3, 0x67, 0x1f,
-    0xcb, 0x79, 0xe6, 0x4e, 0xcc, 0xc0, 0xe5, 0x78, 0x82, 0x5a, 0xd0, 0x7d, 0xcc, 0xff, 0x72, 0x21,
-    0xb8, 0x08, 0x46, 0x74, 0xf7, 0x43, 0x24, 0x8e, 0xe0, 0x35, 0x90, 0xe6, 0x81, 0x3a, 0x26, 0x4c,
-    0x3c, 0x28, 0x52, 0xbb, 0x91, 0xc3, 0x00, 0xcb, 0x88, 0xd0, 0x65, 0x8b, 0x1b, 0x53, 0x2e, 0xa3,
-    0x71, 0x64, 0x48, 0x97, 0xa2, 0x0d, 0xf9, 0x4e, 0x38, 0x19, 0xef, 0x46, 0xa9, 0xde, 0xac, 0xd8,
-    0xa8, 0xfa, 0x76, 0x3f, 0xe3, 0x9c, 0x34, 0x3f, 0xf9, 0xdc, 0xbb, 0xc7, 0xc7, 0x0b, 0x4f, 0x1d,
-    0x8a, 0x51, 0xe0, 0x4b, 0xcd, 0xb4, 0x59, 0x31, 0xc8, 0x9f, 0x7e, 0xc9, 0xd9, 0x78, 0x73, 0x64,
-    0xea, 0xc5, 0xac, 0x83, 0x34, 0xd3, 0xeb, 0xc3, 0xc5, 0x81, 0xa0, 0xff, 0xfa, 0x13, 0x63, 0xeb,
-    0x17, 0x0d, 0xdd, 0x51, 0xb7, 0xf0, 0xda, 0x49, 0xd3, 0x16, 0x55, 0x26, 0x29, 0xd4, 0x68, 0x9e,
-    0x2b, 0x16, 0xbe, 0x58, 0x7d, 0x47, 0xa1, 0xfc, 0x8f, 0xf8, 0xb8, 0xd1, 0x7a, 0xd0, 0x31, 0xce,
-    0x45, 0xcb, 0x3a, 0x8f, 0x95, 0x16, 0x04, 0x28, 0xaf, 0xd7, 0xfb, 0xca, 0xbb, 0x4b, 0x40, 0x7e,
-};
-
-#define XP32_1 0x9E3779B1u
-#define XP32_2 0x85EBCA77u
-#define XP32_3 0xC2B2AE3Du
-#define XP64_1 0x9E3779B185EBCA87ull
-#define XP64_2 0xC2B2AE3D27D4EB4Full
-#define XP64_3 0x165667B19E3779F9ull
-#define XP64_4 0x85EBCA77C2B2AE63ull
-#define XP64_5 0x27D4EB2F165667C5ull
-#define XPMX1 0x165667919E3779F9ull
-#define XPMX2 0x9FB21C651E98DF25ull
-
-__device__ __forceinline__ uint64_t secret64(int off)
-{
-    uint64_t v = 0;
-    for (int b = 0; b < 8; b++) v |= uint64_t(kXxhSecret[off + b]) << (8 * b);
-    return v;
-}
-__device__ __forceinline__ uint32_t secret32(int off)
-{
-    return uint32_t(kXxhSecret[off]) | (uint32_t(kXxhSecret[off + 1]) << 8) | (uint32_t(kXxhSecret[off + 2]) << 16)
-            | (uint32_t(kXxhSecret[off + 3]) << 24);
-}
+// tail stripes and the final merge on one lane (the secret and primes are
+// defined above the numeric pipeline). Where the numeric pipeline writes a
+// content-checksummed output, it computes that output's block sums itself
+// and phase 1 skips those blocks.
 __device__ __forceinline__ uint64_t fold128(uint64_t a, uint64_t b)
 {
     return (a * b) ^ __umul64hi(a, b);
@@ -1732,12 +1801,20 @@ __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks
         uint32_t const i = lane & 7;
         uint64_t const init = i == 0 ? XP32_3 : i == 1 ? XP64_1 : i == 2 ? XP64_2 : i == 3 ? XP64_3
                             : i == 4 ? XP64_4 : i == 5 ? XP32_2 : i == 6 ? XP64_5 : XP32_1;
-        uint64_t acc = init;
         uint64_t const key = secret64(int(192 - 64 + 8 * i));
-        // The block chain acc = scramble(acc + sum) is serial; its inputs are
-        // not. The warp loads the sums of 32 blocks at a time (coalesced, the
-        // next batch while the current one runs), and lane i takes the value
-        // of block k for accumulator i from lane 8 * (k % 4) + i.
+        uint32_t const klo = uint32_t(key), khi = uint32_t(key >> 32);
+        // The block chain acc = scramble(acc + sum), scramble(x) = ((x ^
+        // (x >> 47)) ^ key) * PRIME32_1, is serial; its inputs are not. The
+        // warp loads the sums of 32 blocks at a time (coalesced, the next
+        // batch while the current one runs), and lane i takes the value of
+        // block k for accumulator i from lane 8 * (k % 4) + i.
+        //
+        // The chain runs on y = acc + sum of the block about to be scrambled,
+        // in 32-bit halves: x >> 47 only reaches the low half (y.hi >> 15), so
+        // with t = y.lo ^ (y.hi >> 15) ^ key.lo and u = y.hi ^ key.hi the next
+        // y is t * P + next sum (one 32x32+64-bit multiply-add) with u * P
+        // added to its high half. Per block the dependent path is a shift, a
+        // xor and two multiply-adds; the sums' additions leave it.
         const uint64_t* const bs = t.blockSums;
         uint32_t const nb = t.nbBlocks;
         uint64_t const total = 8ull * nb;
@@ -1747,6 +1824,8 @@ __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks
             uint64_t const idx = uint64_t(lane) + 32u * m;
             cur[m] = idx < total ? __ldg(bs + idx) : 0;
         }
+        uint64_t const y0 = init + __shfl_sync(0xffffffffu, cur[0], int(i)); // init + sum of block 0
+        uint32_t ylo = uint32_t(y0), yhi = uint32_t(y0 >> 32);
         for (uint32_t b0 = 0; b0 < nb; b0 += 32) {
             uint64_t nxt[8];
 #pragma unroll
@@ -1757,17 +1836,23 @@ __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks
             uint32_t const cnt = min(32u, nb - b0);
 #pragma unroll
             for (int k = 0; k < 32; k++) {
-                uint64_t const v = __shfl_sync(0xffffffffu, cur[k >> 2], int(8 * (k & 3) + i));
+                // sum of block b0 + k + 1 (0 past the last block)
+                uint64_t const nv = k < 31 ? __shfl_sync(0xffffffffu, cur[(k + 1) >> 2], int(8 * ((k + 1) & 3) + i))
+                                           : __shfl_sync(0xffffffffu, nxt[0], int(i));
                 if (uint32_t(k) < cnt) {
-                    acc += v;
-                    acc ^= acc >> 47;
-                    acc ^= key;
-                    acc *= XP32_1;
+                    uint32_t const tt = ylo ^ (yhi >> 15) ^ klo;
+                    uint32_t const u = yhi ^ khi;
+                    uint64_t const r = uint64_t(tt) * XP32_1 + nv;
+                    ylo = uint32_t(r);
+                    yhi = uint32_t(r >> 32) + u * XP32_1;
                 }
             }
 #pragma unroll
             for (int m = 0; m < 8; m++) cur[m] = nxt[m];
         }
+        // after the last block y = acc (its next sum is 0); with no block,
+        // y = init + 0
+        uint64_t acc = (uint64_t(yhi) << 32) | ylo;
         uint64_t const len = t.len;
         uint64_t const nbStripes = ((len - 1) - uint64_t(kHashBlock) * nb) / 64;
         const uint8_t* const last = t.data + uint64_t(kHashBlock) * nb;

@@ -1,3 +1,4 @@
+#include <map>
 // Host-logic check of the decode planner (test infrastructure): builds the
 // plan and layout of a frame with fake, widely separated base addresses and
 // verifies that every pointer and length a task uses lies inside an allocation.
@@ -39,6 +40,7 @@ int main(int argc, char** argv) {
   auto P = [&](size_t off) { return L.pool.data() + off; };
   auto hostPtrs = [&](const uint8_t* const* dp, int n, std::vector<const uint8_t*>& v) {
     size_t off = (const uint8_t*)dp - dPool; memcpy(v.data(), L.pool.data() + off, n * sizeof(void*)); };
+  std::map<const uint64_t*, std::pair<const uint8_t*, uint32_t>> fusedSums;
   for (auto& l : L.launches) {
     printf(" launch kind=%d level=%d tasks=%u tiles=%u\n", l.kind, l.level, l.nbTasks, l.nbTiles);
     for (uint32_t i = 0; i < l.nbTasks; i++) {
@@ -60,10 +62,26 @@ int main(int argc, char** argv) {
           else if (t.srcMode == SRC_BITPACK) bad += !inR(t.src, (ns*t.nbBits+7)/8, "np.bits");
           else { bad += !inR(t.planes, t.w*8, "np.planes"); std::vector<const uint8_t*> v(t.w); hostPtrs(t.planes, t.w, v);
                  for (auto p : v) bad += !inR(p, ns, "np.plane"); }
-          printf("   np n=%lu w=%u mode=%u zz=%u delta=%u nbBits=%u tileBase=%u\n",(unsigned long)t.n,t.w,t.srcMode,t.zigzag,t.delta,t.nbBits,t.tileBase);
+          if (t.blockSums) {  // fused content-checksum block sums: whole blocks of this output
+            bad += !inR(t.blockSums, (uint64_t)t.hashBlocks*64, "np.sums");
+            if ((uint64_t)t.hashBlocks * 1024 > t.n * t.w) { printf("BAD np.hashBlocks beyond the output\n"); bad++; }
+            fusedSums[t.blockSums] = std::make_pair(t.out, t.hashBlocks);
+          }
+          printf("   np n=%lu w=%u mode=%u zz=%u delta=%u nbBits=%u tileBase=%u fused=%u\n",(unsigned long)t.n,t.w,t.srcMode,t.zigzag,t.delta,t.nbBits,t.tileBase,t.hashBlocks);
           break; }
         case KIND_HASH: { auto t = ((HashTask*)P(l.taskOff))[i];
-          bad += !inR(t.data, t.len, "hash.data"); if (t.nbBlocks) bad += !inR(t.blockSums, t.nbBlocks*64, "hash.sums"); break; }
+          bad += !inR(t.data, t.len, "hash.data"); if (t.nbBlocks) bad += !inR(t.blockSums, t.nbBlocks*64, "hash.sums");
+          // every full block's sums come from exactly one producer: the hash
+          // launch's own block list, or the numeric task writing this output
+          uint32_t listed = 0;
+          const TileRef* tl = (const TileRef*)P(l.tileOff);
+          for (uint32_t k = 0; k < l.nbTiles; k++) listed += tl[k].task == i;
+          auto f = fusedSums.find(t.blockSums);
+          bool const fused = t.nbBlocks && f != fusedSums.end();
+          if (fused && (listed || f->second.first != t.data || f->second.second != t.nbBlocks)) {
+            printf("BAD hash %u: fused sums do not match the task\n", i); bad++; }
+          if (!fused && listed != t.nbBlocks) { printf("BAD hash %u: %u of %u blocks listed\n", i, listed, t.nbBlocks); bad++; }
+          break; }
         case KIND_TOKENIZE: { auto t = ((TokenizeTask*)P(l.taskOff))[i];
           bad += !inR(t.out, t.n*t.w, "tok.out"); bad += !inR(t.idx, t.n*t.iw, "tok.idx"); bad += !inR(t.alphabet, (uint64_t)t.alphabetSize*t.w, "tok.alpha"); break; }
         case KIND_WIDEN: { auto t = ((WidenTask*)P(l.taskOff))[i];
