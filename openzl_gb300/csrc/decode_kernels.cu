@@ -1021,7 +1021,8 @@ struct BitWin3 {
 // Table construction restates src/openzl/fse/decompress/fse_decompress.c:
 // 73-171; decode order restates fse_decompress.c:255-337 (state i % nbStates
 // emits symbol i; the last symbol of each state has no transition).
-constexpr uint32_t kFseCtaSmem = 56 * 1024; // at most eight tableLog-11 lanes per CTA
+constexpr uint32_t kFseCtaSmem = 224 * 1024; // up to 32 tableLog-11 lanes per CTA (one warp)
+constexpr uint32_t kFseDefaultLanes = 6;       // streams per CTA when the autotuner has not run
 
 constexpr int kFseRing = 16, kFseAhead = 12; // stream ring: 256 bytes per lane, 192 bytes ahead
 
@@ -1818,20 +1819,23 @@ __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks
         const uint64_t* const bs = t.blockSums;
         uint32_t const nb = t.nbBlocks;
         uint64_t const total = 8ull * nb;
-        uint64_t cur[8];
+        // batches of 32 blocks: the current one, the next, and the one after
+        // it in flight (two batches of chain steps cover an L2 round trip)
+        uint64_t cur[8], nxt[8];
 #pragma unroll
         for (int m = 0; m < 8; m++) {
             uint64_t const idx = uint64_t(lane) + 32u * m;
             cur[m] = idx < total ? __ldg(bs + idx) : 0;
+            nxt[m] = idx + 256 < total ? __ldg(bs + idx + 256) : 0;
         }
         uint64_t const y0 = init + __shfl_sync(0xffffffffu, cur[0], int(i)); // init + sum of block 0
         uint32_t ylo = uint32_t(y0), yhi = uint32_t(y0 >> 32);
         for (uint32_t b0 = 0; b0 < nb; b0 += 32) {
-            uint64_t nxt[8];
+            uint64_t nx2[8];
 #pragma unroll
             for (int m = 0; m < 8; m++) {
-                uint64_t const idx = 8ull * (b0 + 32) + lane + 32u * m;
-                nxt[m] = idx < total ? __ldg(bs + idx) : 0;
+                uint64_t const idx = 8ull * (b0 + 64) + lane + 32u * m;
+                nx2[m] = idx < total ? __ldg(bs + idx) : 0;
             }
             uint32_t const cnt = min(32u, nb - b0);
 #pragma unroll
@@ -1848,7 +1852,10 @@ __global__ void kHashFinish(const HashTask* __restrict__ tasks, uint32_t nbTasks
                 }
             }
 #pragma unroll
-            for (int m = 0; m < 8; m++) cur[m] = nxt[m];
+            for (int m = 0; m < 8; m++) {
+                cur[m] = nxt[m];
+                nxt[m] = nx2[m];
+            }
         }
         // after the last block y = acc (its next sum is 0); with no block,
         // y = init + 0
@@ -1966,7 +1973,12 @@ long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dSc
                 break;
             case KIND_FSE: {
                 uint32_t const maxLanes = fseLanes(l.param0);
-                uint32_t const lanes = l.tune && l.tune < maxLanes ? l.tune : maxLanes;
+                // untuned: large tables six streams per warp, the autotuner's
+                // choice on the mixed-frame workload (wider CTAs wait on their
+                // serial table builds and leave too few warps per SM to hide
+                // latency); small tables as many as fit
+                uint32_t const dflt = l.param0 <= 8 || maxLanes < kFseDefaultLanes ? maxLanes : kFseDefaultLanes;
+                uint32_t const lanes = l.tune && l.tune <= maxLanes ? l.tune : dflt;
                 uint32_t const grid = (l.nbTasks + lanes - 1) / lanes;
                 kFse<<<grid, 32, fseSmemBytes(lanes, l.param0), s>>>(static_cast<const FseTask*>(tasks), l.nbTasks,
                                                                      lanes, l.param0, dStatus);
