@@ -5,15 +5,18 @@
 # into the product.
 #
 #   make -f oracle/ref.mk -j8   (REF: $OZL_REFERENCE, else /root/reference)
+#   make -f oracle/ref.mk -j8 OUT=oracle/_ref/native EXTRA=-march=native
+#       (the same sources with the host's vector extensions, for the CPU
+#       baseline's second variant)
 #
 # Recipe: every src/openzl/**/*.c except the zstd/lz4 bindings (their
 # third-party libraries are not vendored), replaced by oracle/ref_stubs.c,
 # compiled with the reference's default release flags (-O3 -DNDEBUG, no
 # -march). The x86-64 Huffman assembly loop is added on x86-64 hosts only.
 REF     ?= $(or $(OZL_REFERENCE),/root/reference)
-OUT     := oracle/_ref
+OUT     ?= oracle/_ref
 CC      ?= gcc
-CFLAGS  := -std=gnu11 -O3 -DNDEBUG -fPIC -fvisibility=default \
+CFLAGS  := -std=gnu11 -O3 -DNDEBUG -fPIC -fvisibility=default $(EXTRA) \
            -I$(REF)/src -I$(REF)/include -I$(REF) -w
 SRCS    := $(shell find $(REF)/src/openzl -name '*.c' \
              -not -path '*/codecs/zstd/*' -not -path '*/codecs/lz4/*' | sort)
