@@ -447,13 +447,19 @@ ZL_Report ozl_gpu_xxh3_64_static(const void* d_data, size_t len, void* stream);
 
 /* Serving loop (no counterpart in the reference): continuous batching of
  * decompress and compress requests with host buffers on the current device.
- * `hbmBudget` bytes of device memory are split into one resident arena per
- * worker; each worker (its own CUDA stream) takes the oldest queued requests
- * of one kind that fit its arena together and runs them as one batch, so
- * batches of different workers overlap on the GPU. `checksums` selects
- * whether frames carry (compress) and have verified (decompress) both
- * checksums. Host buffers must stay valid until the request completes; a
- * request larger than one arena completes with ZL_ErrorCode_srcSize_tooLarge. */
+ * `hbmBudget` bytes of device memory are allocated once as a pool shared by
+ * the workers, and hold each batch's inputs and outputs. A free worker (its
+ * own CUDA stream) admits the oldest queued request as soon as a block of its
+ * size is free in the pool, with the next queued requests of the same kind
+ * that fit the same block (a batch is at most hbmBudget / nbWorkers unless
+ * its first request alone is larger), and runs them as one batch, so batches
+ * of different workers overlap on the GPU. `checksums` selects whether frames
+ * carry (compress) and have verified (decompress) both checksums. Host
+ * buffers must stay valid until the request completes. A request needs its
+ * input plus its output (decoded size, or ZL_compressBound of the input) in
+ * the pool; one larger than hbmBudget completes with
+ * ZL_ErrorCode_srcSize_tooLarge. Returns NULL if the pool cannot be
+ * allocated. */
 typedef struct OZL_Server_s OZL_Server;
 OZL_Server* ozl_server_create(size_t hbmBudget, int nbWorkers, int checksums);
 /* Drains the queue, then stops the workers. */

@@ -2,13 +2,18 @@
 // one GPU (ozl_server_* in include/openzl_gb300.h; no counterpart in the
 // reference, which compresses one frame per call on the CPU).
 //
-// Requests queue on the host. Each worker thread owns a CUDA stream, a
-// resident device arena (its share of the HBM budget) and its own decode and
-// encode engines. A free worker takes the oldest queued requests of one kind
-// that fit its arena together, copies them in, runs them as one batch, copies
-// the results out and reports each request's latency. Workers run their
-// batches concurrently, so requests that arrive while others are on the GPU
-// are admitted as soon as a worker and its memory free up, and their work
+// Requests queue on the host. The server holds one resident device pool of
+// the HBM budget, shared by its workers; each worker thread owns a CUDA
+// stream and its own decode and encode engines. A free worker admits the
+// oldest queued request and the next ones of the same kind, as many as fit
+// one contiguous block of the pool (at most the budget's per-worker share,
+// unless the oldest request alone is larger), copies them in, runs them as
+// one batch, copies the results out, returns the block and reports each
+// request's latency. Admission waits for free HBM, not for a free worker's
+// fixed arena: a request up to the whole budget runs as soon as enough of the
+// pool is free, and only a request larger than the budget is refused. Workers
+// run their batches concurrently, so requests that arrive while others are on
+// the GPU are admitted as soon as a worker and memory free up, and their work
 // overlaps on the device. Codec work is bit-exact and per frame, so a result
 // does not depend on the batch it ran in.
 #include <cuda_runtime.h>
@@ -16,6 +21,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
@@ -49,11 +55,60 @@ struct Request {
     double latencyUs;
 };
 
+// First-fit allocator of the shared pool's byte range (host bookkeeping;
+// the caller holds the server lock). Free blocks by offset, merged with their
+// neighbours when returned.
+struct PoolBlocks {
+    std::map<size_t, size_t> free; // offset -> bytes
+    void reset(size_t bytes)
+    {
+        free.clear();
+        if (bytes) free.emplace(0, bytes);
+    }
+    size_t largest() const
+    {
+        size_t m = 0;
+        for (auto& f : free) m = f.second > m ? f.second : m;
+        return m;
+    }
+    bool take(size_t bytes, size_t& off)
+    {
+        for (auto it = free.begin(); it != free.end(); ++it) {
+            if (it->second < bytes) continue;
+            off = it->first;
+            size_t const rest = it->second - bytes;
+            free.erase(it);
+            if (rest) free.emplace(off + bytes, rest);
+            return true;
+        }
+        return false;
+    }
+    void give(size_t off, size_t bytes)
+    {
+        auto it = free.emplace(off, bytes).first;
+        auto nx = std::next(it);
+        if (nx != free.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free.erase(nx);
+        }
+        if (it != free.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free.erase(it);
+            }
+        }
+    }
+};
+
 } // namespace
 
 struct OZL_Server_s {
     int device = 0;
-    size_t arenaBytes = 0;
+    size_t budget = 0;     // bytes of the shared pool
+    size_t share = 0;      // batch size cap: the budget's per-worker share
+    ozl::DevBuf pool;
+    PoolBlocks blocks;
     int nbWorkers = 0;
     int checksums = 1;
     std::mutex mu;
@@ -91,49 +146,61 @@ void OZL_Server_s::worker()
     cudaSetDevice(device);
     cudaStream_t s = nullptr;
     cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-    ozl::DevBuf arena;
     ozl::DecodeBatch dec;
     ozl::EncodeBatch enc;
     dec.checkContent = dec.checkCompressed = checksums != 0;
-    bool const haveArena = arena.reserve(arenaBytes);
+    auto need = [](const Request* r) { return alignUp(r->inBytes) + alignUp(r->outBytes); };
     for (;;) {
         std::vector<Request*> batch;
+        size_t off = 0, bytes = 0;
         {
             std::unique_lock<std::mutex> lk(mu);
-            cvWork.wait(lk, [&] { return stop || !pending.empty(); });
+            // the oldest request is admitted when a block of its size is free
+            // (or refused at once when it exceeds the whole budget)
+            cvWork.wait(lk, [&] {
+                if (stop && pending.empty()) return true;
+                if (pending.empty()) return false;
+                size_t const n = need(pending.front());
+                return n > budget || blocks.largest() >= n;
+            });
             if (pending.empty() && stop) break;
-            // admission: oldest requests of the head's kind that fit the arena together
-            int const kind = pending.front()->kind;
-            size_t used = 0;
+            Request* head = pending.front();
+            size_t const headNeed = need(head);
+            if (headNeed > budget) {
+                pending.pop_front();
+                head->result = ozl::reportFail(ZL_ErrorCode_srcSize_tooLarge);
+                lk.unlock();
+                finishOne(head);
+                continue;
+            }
+            // then the next requests of the same kind, oldest first, while the
+            // batch fits the largest free block and the per-worker share
+            size_t const cap = std::min(blocks.largest(), std::max(share, headNeed));
+            int const kind = head->kind;
             for (auto it = pending.begin(); it != pending.end();) {
                 Request* r = *it;
                 if (r->kind != kind) { ++it; continue; }
-                size_t const need = alignUp(r->inBytes) + alignUp(r->outBytes);
-                if (used + need > arenaBytes) {
-                    if (batch.empty()) { // larger than a whole arena: cannot run here
-                        it = pending.erase(it);
-                        r->result = ozl::reportFail(ZL_ErrorCode_srcSize_tooLarge);
-                        lk.unlock();
-                        finishOne(r);
-                        lk.lock();
-                        it = pending.begin();
-                        continue;
-                    }
-                    break;
-                }
-                used += need;
+                size_t const n = need(r);
+                if (bytes + n > cap) break;
+                bytes += n;
                 batch.push_back(r);
                 it = pending.erase(it);
             }
+            blocks.take(bytes, off); // fits: bytes <= the largest free block
+            if (!pending.empty()) cvWork.notify_one(); // another worker may admit the rest
         }
-        if (batch.empty()) continue;
-        if (!haveArena || !s) {
+        if (!pool.data() || !s) {
             for (Request* r : batch) r->result = ozl::reportFail(ZL_ErrorCode_allocation);
-            finish(batch);
-            continue;
+        } else if (batch.front()->kind == 0) {
+            runDecode(batch, dec, pool.data() + off, s);
+        } else {
+            runEncode(batch, enc, pool.data() + off, s);
         }
-        if (batch.front()->kind == 0) runDecode(batch, dec, arena.data(), s);
-        else runEncode(batch, enc, arena.data(), s);
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            blocks.give(off, bytes);
+        }
+        cvWork.notify_all(); // freed memory may admit waiting requests
         finish(batch);
     }
     if (s) cudaStreamDestroy(s);
@@ -229,8 +296,14 @@ OZL_Server* ozl_server_create(size_t hbmBudget, int nbWorkers, int checksums)
         return nullptr;
     }
     srv->nbWorkers = nbWorkers;
-    srv->arenaBytes = hbmBudget / size_t(nbWorkers) / kAlign * kAlign;
+    srv->budget = hbmBudget / kAlign * kAlign;
+    srv->share = hbmBudget / size_t(nbWorkers) / kAlign * kAlign;
     srv->checksums = checksums;
+    if (!srv->pool.reserve(srv->budget)) {
+        delete srv;
+        return nullptr;
+    }
+    srv->blocks.reset(srv->budget);
     try {
         for (int i = 0; i < nbWorkers; i++) srv->workers.emplace_back([srv] { srv->worker(); });
     } catch (...) {

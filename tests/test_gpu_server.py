@@ -108,3 +108,34 @@ def test_errors_stay_with_their_request(gpu_lib):
         else:
             assert code == 0
             assert out[:val].tobytes() == r[4].tobytes()
+
+
+def test_one_request_may_use_the_whole_budget(gpu_lib):
+    """Admission draws on one shared budget: a request larger than the
+    budget's per-worker share but within the budget runs (after the smaller
+    requests ahead of it free their memory), and the requests around it
+    still run and stay correct."""
+    import openzl_gb300 as oz
+
+    rng = np.random.default_rng(3)
+    budget = 96 << 20
+    srv = oz.Server(hbm_budget=budget, workers=4)  # per-worker share 24 MiB
+    big = (1000 + np.cumsum(rng.integers(-900, 901, 5 << 20))).astype(np.uint32)  # 20 MiB in, 20 MiB out
+    big_frame = oracle.compress(3, big, 4)
+    small = [_requests(21)[k] for k in range(10)]
+    ids, outs, wants = [], [], []
+    for r in small[:5]:
+        i, out = _submit(srv, r)
+        ids.append(i), outs.append(out), wants.append(r[4])
+    big_out = np.zeros(big.nbytes, np.uint8)
+    big_id = srv.submit_decompress(big_frame, big_out)
+    for r in small[5:]:
+        i, out = _submit(srv, r)
+        ids.append(i), outs.append(out), wants.append(r[4])
+    res = _collect(srv, len(ids) + 1)
+    srv.close()
+    assert res[big_id][0] == 0 and res[big_id][1] == big.nbytes
+    assert big_out.tobytes() == big.tobytes()
+    for i, out, want in zip(ids, outs, wants):
+        code, val, _ = res[i]
+        assert code == 0 and out[:val].tobytes() == want.tobytes()
