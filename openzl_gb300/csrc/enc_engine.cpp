@@ -109,14 +109,14 @@ struct Job {
     int mode = M_FSE;
     ent::Histo hist{};
     int codec = ent::CC_STORE;
-    // FSE
-    int16_t norm[256];
+    // FSE: tables built on the device (kFseTables) from the histogram
     unsigned tl = 0, nbStates = 2;
-    std::unique_ptr<ent::FseCTable> fct;
-    uint8_t ncount[600];
+    uint8_t* dNorm = nullptr;   // normalized counts (numeric i16)
+    uint8_t* dNcount = nullptr; // their header
+    uint32_t ncountSlot = 0;
     size_t ncountSize = 0;
-    // Huffman
-    std::unique_ptr<ent::HufCTable> hct;
+    // Huffman: code lengths and codes built on the device (kHufTables), the
+    // weights brought back for the nested FSE graph and the frame
     std::vector<uint8_t> weights;
     int weightsJob = -1;
     bool x4 = false;
@@ -241,8 +241,8 @@ void parallelFor(size_t n, F fn)
 }
 
 struct EncodeBatch::Impl {
-    DevBuf bufA, bufE, bufF, bufSmall, bufT, bufW, bufR;
-    PinnedBuf stage;
+    DevBuf bufA, bufE, bufF, bufSmall, bufT, bufW, bufR, bufH;
+    PinnedBuf stage, stageH;
     std::vector<Job> jobs;           // data chunks (discovery order), then nested weights jobs
     size_t nbDataJobs = 0;
     bool checksums = true;
@@ -416,7 +416,7 @@ struct Engine {
                 for (size_t b = 0; b < nbBytes; b++) x.hdr[1 + b] = uint8_t(j->n >> (8 * b));
                 x.hsz = nbBytes + 1;
                 int ns = newStream(T_NUMERIC, 2, j->hist.maxSym + 1);
-                s[ns].pieces.push_back(Piece{ nullptr, reinterpret_cast<const uint8_t*>(j->norm), 2ull * (j->hist.maxSym + 1) });
+                s[ns].pieces.push_back(Piece{ j->dNorm, nullptr, 2ull * (j->hist.maxSym + 1) });
                 int bs = newStream(T_SERIAL, 1, j->sizes[0]);
                 s[bs].pieces.push_back(Piece{ j->out, nullptr, j->sizes[0] });
                 nd.back().nbOut = 2;
@@ -616,7 +616,7 @@ struct Engine {
                 Job& j = (*jobs)[size_t(job)];
                 newNode(TR_NCOUNT, sid, 1);
                 int o = newStream(T_SERIAL, 1, j.ncountSize);
-                s[o].pieces.push_back(Piece{ nullptr, j.ncount, j.ncountSize });
+                s[o].pieces.push_back(Piece{ j.dNcount, nullptr, j.ncountSize });
                 nd.back().nbOut = 1;
                 runSuccessor(G_SERIAL_STORE, o);
                 return;
@@ -1308,25 +1308,14 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                 j.packBytes = j.n ? 1 + (j.packBits * j.n) / 8 : 0;
                 break;
             }
-            case ent::CC_FSE: {
+            case ent::CC_FSE: // normalization, header and table follow on the device
                 j.nbStates = j.n < 1000 ? 2 : 4;
                 j.tl = ent::fseTableLog(11, j.n, j.hist.maxSym, 2);
-                ent::fseNormalize(j.norm, j.tl, j.hist.count, j.n, j.hist.maxSym);
-                j.fct.reset(new ent::FseCTable());
-                ent::fseBuildCTable(*j.fct, j.norm, j.hist.maxSym, j.tl);
-                j.ncountSize = ent::fseWriteNCount(j.ncount, j.norm, j.hist.maxSym, j.tl);
                 break;
-            }
-            case ent::CC_HUF: {
-                unsigned const tl0 = ent::fseTableLog(11, j.n, j.hist.maxSym, 1);
-                j.hct.reset(new ent::HufCTable());
-                unsigned const tl = ent::hufBuild(*j.hct, j.hist.count, j.hist.maxSym, tl0);
-                j.weights.resize(j.hist.maxSym + 1);
-                for (unsigned s = 0; s <= j.hist.maxSym; s++)
-                    j.weights[s] = uint8_t(j.hct->nbBits[s] ? tl + 1 - j.hct->nbBits[s] : 0);
+            case ent::CC_HUF: // code lengths, codes and weights follow on the device
+                j.tl = ent::fseTableLog(11, j.n, j.hist.maxSym, 1);
                 j.x4 = j.n > 1000;
                 break;
-            }
             default: break;
         }
     };
@@ -1404,6 +1393,48 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         std::memcpy(I.jobs[j].hist.count, &hists[j * 256], 1024);
         decide(I.jobs[j]);
     });
+    // Huffman tables on the device: every 8-bit Huffman chunk's code lengths
+    // and codes (left on the device for the bitstream pass) and its weights
+    // (brought back: the nested FSE graph of the weights is decided on them,
+    // and the frame stores them or their FSE coding)
+    {
+        std::vector<size_t> hj;
+        for (size_t j = 0; j < I.jobs.size(); j++)
+            if (I.jobs[j].codec == ent::CC_HUF && !I.jobs[j].wide) hj.push_back(j);
+        if (!hj.empty()) {
+            size_t const nh = hj.size();
+            size_t const tabBytes = (sizeof(ent::HufCTable) + 15) & ~size_t(15);
+            size_t const upBytes = nh * sizeof(HufTableTask) + nh * 1024;
+            if (!I.bufH.reserve(upBytes + nh * (tabBytes + 256) + 256) || !I.stageH.reserve(upBytes + nh * 256)) {
+                err = "allocation failed";
+                return 70;
+            }
+            uint8_t* const dBase = I.bufH.data();
+            auto* dTasks = reinterpret_cast<HufTableTask*>(dBase);
+            uint8_t* const dHist = dBase + nh * sizeof(HufTableTask);
+            uint8_t* const dTabs = dHist + nh * 1024;
+            uint8_t* const dW = dTabs + nh * tabBytes;
+            auto* hTasks = reinterpret_cast<HufTableTask*>(I.stageH.p);
+            uint8_t* const hHist = I.stageH.p + nh * sizeof(HufTableTask);
+            uint8_t* const hW = I.stageH.p + upBytes;
+            parallelFor(nh, [&](size_t k) {
+                Job& J = I.jobs[hj[k]];
+                std::memcpy(hHist + k * 1024, J.hist.count, 1024);
+                J.dTable = dTabs + k * tabBytes;
+                hTasks[k] = HufTableTask{ reinterpret_cast<const uint32_t*>(dHist + k * 1024), dTabs + k * tabBytes,
+                                          dW + k * 256, J.hist.maxSym, J.tl };
+            });
+            cudaMemcpyAsync(dBase, I.stageH.p, upBytes, cudaMemcpyHostToDevice, st);
+            launchHufTables(dTasks, uint32_t(nh), st);
+            launches_++;
+            cudaMemcpyAsync(hW, dW, nh * 256, cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in Huffman tables"; return 1; }
+            parallelFor(nh, [&](size_t k) {
+                Job& J = I.jobs[hj[k]];
+                J.weights.assign(hW + k * 256, hW + k * 256 + J.hist.maxSym + 1);
+            });
+        }
+    }
     // nested weights jobs (FSE graph of Huffman weights): decided on the host
     // histogram of the weights, encoded on the device with the data jobs
     for (size_t j = 0; j < I.jobs.size(); j++) {
@@ -1437,6 +1468,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
 
     // ---- phase E: entropy bitstreams -----------------------------------------------
     {
+        std::vector<FseTableTask> fseTabT;
         std::vector<FseEncTask> fseT;
         std::vector<HufEncTask> hufT;
         std::vector<PackTask> packT;
@@ -1520,17 +1552,26 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                 switch (J.codec) {
                     case ent::CC_FSE: {
                         J.out = b.take(J.n + J.n / 128 + 512, 16);
-                        // the kernel reads the state table up to 2^tableLog entries
-                        J.dTable = staged(J.fct.get(), offsetof(ent::FseCTable, state) + (2u << J.tl),
-                                          sizeof(ent::FseCTable));
+                        // tables built on the device from the uploaded histogram
+                        uint8_t* const table = b.take(sizeof(ent::FseCTable), 16);
+                        J.dTable = table;
+                        J.dNorm = b.take(2 * 256, 16);
+                        J.dNcount = b.take(600, 16);
+                        const uint8_t* const hist = staged(J.hist.count, 1024, 1024);
                         J.sizeSlot = nbSizes++;
-                        if (real) fseT.push_back(FseEncTask{ src, J.out, J.dTable, uint32_t(J.n), J.sizeSlot, J.nbStates, J.tl });
+                        J.ncountSlot = nbSizes++;
+                        if (real) {
+                            fseTabT.push_back(FseTableTask{ reinterpret_cast<const uint32_t*>(hist), J.n, table,
+                                                            reinterpret_cast<int16_t*>(J.dNorm), J.dNcount,
+                                                            J.hist.maxSym, J.tl, J.ncountSlot, 0 });
+                            fseT.push_back(FseEncTask{ src, J.out, J.dTable, uint32_t(J.n), J.sizeSlot, J.nbStates, J.tl });
+                        }
                         break;
                     }
                     case ent::CC_HUF: {
                         uint32_t const seg = uint32_t((J.n + 3) / 4);
                         J.out = b.take(J.x4 ? 16 + 4ull * hufEncStreamCap(seg) : J.n + J.n / 8 + 64, 16);
-                        J.dTable = staged(J.hct.get(), sizeof(ent::HufCTable), sizeof(ent::HufCTable));
+                        // J.dTable: built on the device before this phase
                         J.sizeSlot = nbSizes;
                         nbSizes += 4;
                         if (real) hufT.push_back(HufEncTask{ src, J.out, J.dTable, uint32_t(J.n), J.sizeSlot, J.x4 ? 1u : 0u });
@@ -1555,7 +1596,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         };
         Bump sz, szStage;
         layoutE(sz, szStage, false);
-        size_t const taskBytes = 4096 + I.jobs.size() * (sizeof(FseEncTask) + sizeof(HufEncTask) + sizeof(PackTask)
+        size_t const taskBytes = 4096 + I.jobs.size() * (sizeof(FseTableTask) + sizeof(FseEncTask) + sizeof(HufEncTask) + sizeof(PackTask)
                                                          + sizeof(Tok16Task) + 2 * sizeof(EncNumTask) + sizeof(Huf16EncTask));
         size_t tilesGuess = 0;
         for (auto& J : I.jobs) {
@@ -1575,6 +1616,8 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         });
         if (stg.used)
             cudaMemcpyAsync(stg.base, I.stage.p, stg.used, cudaMemcpyHostToDevice, st);
+        auto* dFseTab = reinterpret_cast<FseTableTask*>(b.take(fseTabT.size() * sizeof(FseTableTask) + 1));
+        auto* dTabErr = reinterpret_cast<uint32_t*>(b.take(16));
         auto* dFse = reinterpret_cast<FseEncTask*>(b.take(fseT.size() * sizeof(FseEncTask) + 1));
         auto* dHuf = reinterpret_cast<HufEncTask*>(b.take(hufT.size() * sizeof(HufEncTask) + 1));
         auto* dPack = reinterpret_cast<PackTask*>(b.take(packT.size() * sizeof(PackTask) + 1));
@@ -1586,6 +1629,9 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         auto* dWideNumTiles = reinterpret_cast<TileRef*>(b.take(wideNumTiles.size() * sizeof(TileRef) + 1));
         auto* dHuf16 = reinterpret_cast<Huf16EncTask*>(b.take(huf16T.size() * sizeof(Huf16EncTask) + 1));
         // uploads: the tasks (the staged blobs went up above)
+        if (!fseTabT.empty())
+            cudaMemcpyAsync(dFseTab, fseTabT.data(), fseTabT.size() * sizeof(FseTableTask), cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(dTabErr, 0, 4, st);
         if (!fseT.empty()) cudaMemcpyAsync(dFse, fseT.data(), fseT.size() * sizeof(FseEncTask), cudaMemcpyHostToDevice, st);
         if (!hufT.empty()) cudaMemcpyAsync(dHuf, hufT.data(), hufT.size() * sizeof(HufEncTask), cudaMemcpyHostToDevice, st);
         if (!packT.empty()) {
@@ -1612,13 +1658,17 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             launchHuf16Enc(dHuf16, uint32_t(huf16T.size()), dSizes, st);
             launches_++;
         }
+        launchFseTables(dFseTab, uint32_t(fseTabT.size()), dSizes, dTabErr, st);
         launchFseEnc(dFse, uint32_t(fseT.size()), dSizes, st);
         launchHufEnc(dHuf, uint32_t(hufT.size()), dSizes, st);
         launchPack(dPack, dPackTiles, uint32_t(packTiles.size()), st);
-        launches_ += (fseT.empty() ? 0 : 1) + (hufT.empty() ? 0 : 1) + (packTiles.empty() ? 0 : 1);
+        launches_ += (fseT.empty() ? 0 : 2) + (hufT.empty() ? 0 : 1) + (packTiles.empty() ? 0 : 1);
         std::vector<uint32_t> hs(nbSizes + 1);
+        uint32_t tabErr = 0;
         if (nbSizes) cudaMemcpyAsync(hs.data(), dSizes, nbSizes * 4, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(&tabErr, dTabErr, 4, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in entropy encoding"; return 1; }
+        if (tabErr) { err = "FSE normalization failed"; return 1; }
         for (Job& J : I.jobs) {
             if (J.wide && J.codec == ent::CC_HUF16) {
                 // the reference writes the streams into 2n + 32 bytes; each
@@ -1638,6 +1688,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                 continue;
             }
             if (J.codec == ent::CC_FSE) {
+                J.ncountSize = hs[J.ncountSlot];
                 J.sizes[0] = hs[J.sizeSlot];
                 if (J.sizes[0] > J.n + J.n / 128 + 512) { err = "FSE bitstream over capacity"; return 1; }
             }

@@ -13,7 +13,12 @@ void launchEncMax(const EncNumTask* t, const TileRef* tiles, uint32_t nbTiles, u
 void launchEncNum(const EncNumTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
 void launchPack(const PackTask* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);
 void launchHist(const HistTask* t, uint32_t n, uint32_t* hists, cudaStream_t s);
+// FSE normalization, header and encoding table of each chunk; a failed
+// normalization sets errors[0].
+void launchFseTables(const FseTableTask* t, uint32_t n, uint32_t* sizes, uint32_t* errors, cudaStream_t s);
 void launchFseEnc(const FseEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);
+// Huffman code lengths, codes and weights of each chunk.
+void launchHufTables(const HufTableTask* t, uint32_t n, cudaStream_t s);
 void launchHufEnc(const HufEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);
 void launchPut(const PutTask* t, uint32_t n, cudaStream_t s);
 void launchBf16(const Bf16Task* t, const TileRef* tiles, uint32_t nbTiles, cudaStream_t s);

@@ -34,6 +34,32 @@ struct HistTask {
     uint32_t outIndex;   // histogram slot
 };
 
+// FSE coding tables of one chunk built on the device from its histogram:
+// normalized counts (the chunk's numeric stream), their header (fse_ncount)
+// and the encoding table that kFseEnc reads.
+struct FseTableTask {
+    const uint32_t* hist;    // 256 counts
+    uint64_t n;              // symbols in the chunk
+    uint8_t* ctable;         // ent::FseCTable
+    int16_t* norm;           // maxSym + 1 normalized counts
+    uint8_t* ncount;         // header, at most 520 bytes
+    uint32_t maxSym;
+    uint32_t tableLog;
+    uint32_t sizeSlot;       // where the header's size is written
+    uint32_t pad;
+};
+
+// Huffman code lengths and codes of one chunk built on the device from its
+// histogram, and the chunk's weights stream (tableLog + 1 - length, 0 for
+// absent symbols).
+struct HufTableTask {
+    const uint32_t* hist;    // 256 counts
+    uint8_t* ctable;         // ent::HufCTable
+    uint8_t* weights;        // maxSym + 1 weights
+    uint32_t maxSym;
+    uint32_t maxNbBits;      // the chunk's table log bound
+};
+
 struct FseEncTask {
     const uint8_t* src;
     uint8_t* out;            // capacity: n + n/128 + 512 bytes

@@ -12,6 +12,8 @@
 
 #include "enc_exec.h"
 #include "enc_tables.h"
+#include "fse_norm.h"
+#include "huf_tree.h"
 #include "enc_tasks.h"
 
 namespace ozl {
@@ -229,6 +231,168 @@ struct BitOut {
         return pos;
     }
 };
+
+// FSE coding tables on the device, one warp per chunk: lane 0 normalizes the
+// histogram and writes the normalized-count header (fse_norm.h, serial as in
+// the reference); the warp builds the encoding table (FSE_buildCTable_wksp,
+// fse_compress.c:69-207). Cells: the count -1 symbols take the top cells in
+// symbol order; occurrence k of the other symbols (in symbol order, each
+// repeated count times) goes to the k-th cell of the sequence 0, step,
+// 2 step, ... (mod size) below the top cells, 32 positions per round ranked
+// by a ballot. States: a symbol's state slots, from its cumulative count,
+// take its cells in increasing order, ranked within the round by
+// __match_any_sync. The result equals the serial construction.
+constexpr int kFseTabWarps = 4;
+struct FseBuildSmem {
+    uint32_t count[256];
+    int16_t norm[256];
+    uint16_t posCum[260];  // occurrences before each symbol (positive counts)
+    uint16_t cumul[260];   // state slots before each symbol (count -1 takes one)
+    uint16_t next[256];
+    uint8_t symbolAt[2048];
+};
+
+__global__ void __launch_bounds__(32 * kFseTabWarps) kFseTables(const FseTableTask* __restrict__ tasks, uint32_t nbTasks,
+                                                                uint32_t* __restrict__ sizes,
+                                                                uint32_t* __restrict__ errors)
+{
+    __shared__ FseBuildSmem sm[kFseTabWarps];
+    uint32_t const wid = threadIdx.x >> 5, lane = threadIdx.x & 31, lt = (1u << lane) - 1;
+    uint32_t const ti = blockIdx.x * kFseTabWarps + wid;
+    if (ti >= nbTasks) return; // the whole warp
+    FseTableTask const t = tasks[ti];
+    FseBuildSmem& S = sm[wid];
+    uint32_t const tl = t.tableLog, maxSym = t.maxSym;
+    uint32_t const size = 1u << tl, mask = size - 1, step = (size >> 1) + (size >> 3) + 3;
+    if (tl < 5 || tl > 11 || maxSym > 255) { // outside what the encoder emits
+        if (lane == 0) atomicOr(errors, 1u);
+        return;
+    }
+    for (uint32_t k = lane; k < 256; k += 32) {
+        S.count[k] = t.hist[k];
+        S.norm[k] = 0;
+    }
+    __syncwarp();
+    if (lane == 0 && !ent::fseNormalizeCounts(S.norm, tl, S.count, t.n, maxSym)) atomicOr(errors, 1u);
+    __syncwarp();
+    // lane j: symbols 8j .. 8j + 7; scans of occurrences, state slots and
+    // top cells
+    int v[8];
+    uint32_t sp = 0, sc = 0, sn = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t const sy = 8 * lane + k;
+        v[k] = sy <= maxSym ? int(S.norm[sy]) : 0;
+        sp += v[k] > 0 ? uint32_t(v[k]) : 0u;
+        sc += v[k] == -1 ? 1u : (v[k] > 0 ? uint32_t(v[k]) : 0u);
+        sn += v[k] == -1 ? 1u : 0u;
+    }
+    uint32_t ip = sp, ic = sc, in = sn;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t const yp = __shfl_up_sync(0xffffffffu, ip, o), yc = __shfl_up_sync(0xffffffffu, ic, o),
+                       yn = __shfl_up_sync(0xffffffffu, in, o);
+        if (lane >= uint32_t(o)) {
+            ip += yp;
+            ic += yc;
+            in += yn;
+        }
+    }
+    uint32_t const totalNeg = __shfl_sync(0xffffffffu, in, 31);
+    uint32_t const high = size - 1 - totalNeg;
+    uint32_t p0 = ip - sp, c0 = ic - sc, n0 = in - sn;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t const sy = 8 * lane + k;
+        S.posCum[sy] = uint16_t(p0);
+        S.cumul[sy] = uint16_t(c0);
+        S.next[sy] = uint16_t(c0);
+        p0 += v[k] > 0 ? uint32_t(v[k]) : 0u;
+        c0 += v[k] == -1 ? 1u : (v[k] > 0 ? uint32_t(v[k]) : 0u);
+        if (v[k] == -1) {
+            S.symbolAt[size - 1 - n0] = uint8_t(sy);
+            n0++;
+        }
+    }
+    if (lane == 31) {
+        S.posCum[256] = uint16_t(p0);
+        S.cumul[256] = uint16_t(c0);
+    }
+    __syncwarp();
+    // spread
+    uint32_t sCur = 0, cumNext = S.posCum[1], occBase = 0;
+    for (uint32_t b0 = 0; b0 < size; b0 += 32) {
+        uint32_t const pos = ((b0 + lane) * step) & mask;
+        bool const valid = totalNeg < size && pos <= high;
+        uint32_t const bal = __ballot_sync(0xffffffffu, valid);
+        if (valid) {
+            uint32_t const occ = occBase + __popc(bal & lt);
+            while (occ >= cumNext && sCur < 255) cumNext = S.posCum[++sCur + 1];
+            S.symbolAt[pos] = uint8_t(sCur);
+        }
+        occBase += __popc(bal);
+    }
+    __syncwarp();
+    // state table
+    ent::FseCTable* const ct = reinterpret_cast<ent::FseCTable*>(t.ctable);
+    for (uint32_t b0 = 0; b0 < size; b0 += 32) {
+        uint32_t const u = b0 + lane;
+        uint32_t const sy = S.symbolAt[u];
+        uint32_t const m = __match_any_sync(0xffffffffu, sy);
+        uint32_t const base = S.next[sy];
+        __syncwarp();
+        if (lane == 31u - __clz(m)) S.next[sy] = uint16_t(base + __popc(m));
+        ct->state[base + __popc(m & lt)] = uint16_t(size + u);
+        __syncwarp();
+    }
+    for (uint32_t sy = lane; sy < 256; sy += 32) {
+        int const c = sy <= maxSym ? int(S.norm[sy]) : 0;
+        ent::fseSymbolDeltas(c, tl, S.cumul[sy], ct->deltaNbBits[sy], ct->deltaFindState[sy]);
+    }
+    for (uint32_t sy = lane; sy <= maxSym; sy += 32) t.norm[sy] = S.norm[sy];
+    if (lane == 0) {
+        ct->tableLog = uint16_t(tl);
+        ct->maxSym = uint16_t(maxSym);
+        sizes[t.sizeSlot] = uint32_t(ent::fseWriteNCountTo(t.ncount, S.norm, maxSym, tl));
+    }
+}
+
+// Huffman code lengths and codes on the device, one warp per chunk: the
+// build (huf_tree.h, as the reference's HUF_buildCTable) is serial, so lane 0
+// runs it on the warp's shared nodes; the warp loads the histogram and writes
+// the weights.
+constexpr int kHufTabWarps = 4;
+struct HufBuildSmem {
+    ent::HufNode nodes[ent::kHufNodes];
+    uint32_t count[256];
+    uint8_t nbBits[256];
+};
+
+__global__ void __launch_bounds__(32 * kHufTabWarps) kHufTables(const HufTableTask* __restrict__ tasks, uint32_t nbTasks)
+{
+    __shared__ HufBuildSmem sm[kHufTabWarps];
+    __shared__ uint32_t sTl[kHufTabWarps];
+    uint32_t const wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t const ti = blockIdx.x * kHufTabWarps + wid;
+    if (ti >= nbTasks) return; // the whole warp
+    HufTableTask const t = tasks[ti];
+    HufBuildSmem& S = sm[wid];
+    for (uint32_t k = lane; k < 256; k += 32) S.count[k] = t.hist[k];
+    __syncwarp();
+    ent::HufCTable* const ct = reinterpret_cast<ent::HufCTable*>(t.ctable);
+    if (lane == 0) {
+        unsigned const tl = ent::hufBuildCodes(S.nodes, ct->value, S.nbBits, S.count, t.maxSym, t.maxNbBits);
+        ct->tableLog = tl;
+        sTl[wid] = tl;
+    }
+    __syncwarp();
+    uint32_t const tl = sTl[wid];
+    for (uint32_t k = lane; k < 256; k += 32) {
+        uint32_t const nb = S.nbBits[k];
+        ct->nbBits[k] = uint8_t(nb);
+        if (k <= t.maxSym) t.weights[k] = uint8_t(nb ? tl + 1 - nb : 0);
+    }
+}
 
 // FSE: one lane per chunk; the lane's table (2^tableLog next states and the
 // per-symbol transform) lives in shared memory.
@@ -654,6 +818,16 @@ void launchHist(const HistTask* t, uint32_t n, uint32_t* hists, cudaStream_t s)
 {
     if (n) kHist<<<n, 256, 0, s>>>(t, hists);
 }
+void launchFseTables(const FseTableTask* t, uint32_t n, uint32_t* sizes, uint32_t* errors, cudaStream_t s)
+{
+    if (n) kFseTables<<<(n + kFseTabWarps - 1) / kFseTabWarps, 32 * kFseTabWarps, 0, s>>>(t, n, sizes, errors);
+}
+
+void launchHufTables(const HufTableTask* t, uint32_t n, cudaStream_t s)
+{
+    if (n) kHufTables<<<(n + kHufTabWarps - 1) / kHufTabWarps, 32 * kHufTabWarps, 0, s>>>(t, n);
+}
+
 void launchFseEnc(const FseEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s)
 {
     if (n) kFseEnc<<<(n + kFseEncLanes - 1) / kFseEncLanes, 32, kFseEncLanes * kFseLaneBytes, s>>>(t, n, sizes);
