@@ -96,6 +96,11 @@ typedef enum {
      * through Huffman and the others each split into this many runs of
      * contiguous frames, decoded as parallel branches (1..8) */
     OZL_DParam_partsPerKind = 1000,
+    /* batch API only: the FSE decoder of the plan's launches until the
+     * autotuner chooses: 0 the library's default shapes, 1 one lane per
+     * stream, 2 one lane per decoder state (four lanes per stream). The
+     * bytes decoded are the same. */
+    OZL_DParam_fseKernel = 1001,
 } ZL_DParam;
 
 typedef enum {

@@ -181,6 +181,7 @@ DPARAM_STICKY = 1
 DPARAM_CHECK_COMPRESSED = 2
 DPARAM_CHECK_CONTENT = 3
 DPARAM_PARTS_PER_KIND = 1000  # OZL_DParam_partsPerKind
+DPARAM_FSE_KERNEL = 1001  # OZL_DParam_fseKernel
 
 
 class DCtx:
@@ -298,11 +299,13 @@ def decompress(frame):
 class GpuBatch:
     """Batched decode of many frames: one plan, one CUDA graph per run."""
 
-    def __init__(self, check_content=True, check_compressed=True, parts_per_kind=None):
+    def __init__(self, check_content=True, check_compressed=True, parts_per_kind=None, fse_kernel=None):
         self._lib = library()
         self._h = self._lib.ozl_gpu_batch_create()
         if parts_per_kind is not None:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_PARTS_PER_KIND, int(parts_per_kind)))
+        if fse_kernel is not None:
+            _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_FSE_KERNEL, int(fse_kernel)))
         if not check_content:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_CHECK_CONTENT, 2))
         if not check_compressed:

@@ -353,6 +353,10 @@ ZL_Report ozl_gpu_batch_setParameter(OZL_GpuBatch* b, ZL_DParam param, int value
             if (value < 1 || value > 8) return fail(ZL_ErrorCode_parameter_invalid);
             b->partsPerKind = value;
             break;
+        case OZL_DParam_fseKernel:
+            if (value < 0 || value > 2) return fail(ZL_ErrorCode_parameter_invalid);
+            b->fseKernel = value;
+            break;
         default: return fail(ZL_ErrorCode_parameter_invalid);
     }
     return ok(0);

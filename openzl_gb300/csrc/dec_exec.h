@@ -16,6 +16,11 @@ long runLaunches(const DeviceLayout& layout, uint8_t* dPool, uint8_t* dScratch, 
 // Applies the shared-memory carve-out attributes the entropy kernels need.
 // Call once per device before the first launch (and before graph capture).
 cudaError_t prepareKernels();
+// Launch::tune of an FSE launch: streams per CTA in the low byte; this flag
+// selects the kernel with one lane per decoder state (kFse4) instead of one
+// lane per stream (kFse).
+constexpr uint32_t kTuneFseLanePerState = 0x100;
+
 // Launch shapes the autotuner may try for a launch (chunks per CTA); 0 if none.
 uint32_t tuneCandidates(const Launch& l, uint32_t* out, uint32_t cap);
 

@@ -69,6 +69,7 @@ struct DecodeBatch {
     bool checkCompressed = true;
     bool splitParts = true;
     int partsPerKind = 1;     // runs per kind (OZL_DParam_partsPerKind)
+    int fseKernel = 0;        // OZL_DParam_fseKernel: 0 default shapes, 1 a lane per stream, 2 a lane per state
     DecodePlan plan;
     std::vector<Part> parts;
     DevBuf arena, params, status;
@@ -226,6 +227,7 @@ struct DecodeBatch {
             rc = layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), p.scratch.data(),
                             p.pool.data(), p.layout, err, mask);
             if (rc) return reportFail(rc);
+            applyFseKernel(p.layout);
         }
         uploaded = false;
         launches = 0;
@@ -320,6 +322,14 @@ struct DecodeBatch {
         return reportOk(0);
     }
 
+    // OZL_DParam_fseKernel: the FSE launches' kernel until the autotuner runs
+    void applyFseKernel(DeviceLayout& layout) const
+    {
+        if (!fseKernel) return;
+        for (Launch& l : layout.launches)
+            if (l.kind == KIND_FSE) l.tune = fseKernel == 2 ? (kTuneFseLanePerState | 8u) : (l.param0 <= 8 ? 32u : 6u);
+    }
+
     // Times every candidate launch shape of the tunable launches (one launch
     // at a time, CUDA events on `s`, best of `reps`) after one full run that
     // produces every launch's inputs, keeps the fastest per launch and drops
@@ -336,8 +346,8 @@ struct DecodeBatch {
         size_t tuned = 0;
         for (Part& part : parts) {
             for (size_t li = 0; li < part.layout.launches.size(); li++) {
-                uint32_t cand[8];
-                uint32_t const nc = tuneCandidates(part.layout.launches[li], cand, 8);
+                uint32_t cand[16];
+                uint32_t const nc = tuneCandidates(part.layout.launches[li], cand, 16);
                 if (nc < 2) continue;
                 float best = 1e30f;
                 uint32_t bestC = 0;
@@ -406,6 +416,7 @@ struct DecodeBatch {
             rc = layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), p.scratch.data(),
                             p.pool.data(), p.layout, err, &p.mask);
             if (rc) return false;
+            applyFseKernel(p.layout);
             host.inOff[r] = size_t(dFrames[first[r]] - dFrames[0]);
             host.outOff[r] = size_t(dOuts[first[r]] - dOuts[0]);
         }

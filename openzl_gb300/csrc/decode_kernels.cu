@@ -1231,6 +1231,145 @@ __global__ void __launch_bounds__(32) kFse(const FseTask* __restrict__ tasks, ui
     if (!br.finished()) reportError(status, DERR_CORRUPTION);
 }
 
+// FSE with one lane per state: a warp decodes up to eight streams, four lanes
+// each (lane k of a group runs state k of its stream, k < nbStates). Symbol
+// i uses state i % nbStates, so one step decodes nbStates consecutive
+// symbols, one per lane. The lanes of a group keep identical copies of the
+// stream's bit window (the same arithmetic on the same words); each looks up
+// its own state's cell, a scan over the group's field widths (two shuffles)
+// gives its field's offset below the top of the window, and the group's
+// total (a third shuffle) advances every copy. The stream's ring is filled by
+// the group's first lane; a full-warp __syncwarp() per step makes its
+// completed copies visible to the other lanes, so the step loop is
+// warp-uniform (streams of a CTA are of similar length: tasks are sorted
+// longest first) and ends when no lane of the warp has a symbol left. Tables
+// as kFse (one per stream, built by the whole warp).
+constexpr uint32_t kFse4Variant = kTuneFseLanePerState; // Launch::tune flag (dec_exec.h)
+
+__global__ void __launch_bounds__(32) kFse4(const FseTask* __restrict__ tasks, uint32_t nbTasks, uint32_t streams,
+                                            uint32_t tableLogMax, uint32_t* __restrict__ status)
+{
+    extern __shared__ __align__(16) uint8_t smemFse[];
+    __shared__ uint16_t sCum[260];
+    __shared__ __align__(16) uint16_t sNext[256];
+    uint32_t const lane = threadIdx.x;
+    for (uint32_t q = 0; q < streams; q++) {
+        uint32_t const tk = blockIdx.x * streams + q;
+        if (tk >= nbTasks) break;
+        FseTask const tt = tasks[tk];
+        fseBuildWarp(tt, smemFse, q * fseSlotBytes(tableLogMax), tableLogMax, sCum, sNext);
+    }
+    uint32_t const grp = lane >> 2, k = lane & 3;
+    uint32_t const ti = blockIdx.x * streams + grp;
+    FseTask t{};
+    bool ok = grp < streams && ti < nbTasks;
+    if (ok) t = tasks[ti];
+    uint32_t const slot = grp * fseSlotBytes(tableLogMax);
+    uint32_t* const ring = reinterpret_cast<uint32_t*>(smemFse + slot + (3u << tableLogMax));
+    const uint16_t* const tab = reinterpret_cast<const uint16_t*>(smemFse + slot);
+    const uint8_t* const symOf = smemFse + slot + (2u << tableLogMax);
+    uint32_t const tl = t.tableLog, ns = t.nbStates;
+    if (ok && ((ns != 2 && ns != 4) || tl > tableLogMax)) { // the planner admits neither
+        if (k == 0) reportError(status, DERR_CORRUPTION);
+        ok = false;
+    }
+    // stream start and ring fill (first lane of the group issues the copies)
+    StreamRing<kFseRing, kFseAhead> r;
+    int32_t pos = 0, end = 0;
+    if (ok && !streamStart(t.bits, t.bitsSize, r.g16, pos, end)) {
+        if (k == 0) reportError(status, DERR_CORRUPTION);
+        ok = false;
+    }
+    r.ring = ring;
+    r.low = 0;
+    if (ok) {
+        int32_t const mt = (pos - 1) >> 7;
+        if (k == 0) {
+            for (int32_t m = mt; m >= mt - kFseAhead; m--) r.issue(m);
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        r.low = mt;
+    }
+    __syncwarp();
+    // window: a (bits [cb + 64, cb + 96)), b, c; g = bits of the window read
+    uint32_t a = 0, b = 0, c = 0;
+    int32_t kb = 0, g = 0;
+    if (ok) {
+        int32_t const jt = (pos - 1) >> 5;
+        a = jt >= 0 ? ring[jt & (4 * kFseRing - 1)] : 0u;
+        b = jt - 1 >= 0 ? ring[(jt - 1) & (4 * kFseRing - 1)] : 0u;
+        c = jt - 2 >= 0 ? ring[(jt - 2) & (4 * kFseRing - 1)] : 0u;
+        kb = jt - 2;
+        g = (kb + 3) * 32 - pos;
+    }
+    // the group's fields of one step: lane k reads nb bits below the k-th
+    // lower lanes' fields; returns the field, sets the group's total
+    auto fields = [&](uint32_t nb, uint32_t& total) -> uint32_t {
+        uint32_t x = nb;
+        uint32_t const y1 = __shfl_up_sync(0xffffffffu, x, 1, 4);
+        if (k >= 1) x += y1;
+        uint32_t const y2 = __shfl_up_sync(0xffffffffu, x, 2, 4);
+        if (k >= 2) x += y2;
+        total = __shfl_sync(0xffffffffu, x, 3, 4);
+        uint32_t const off = x - nb; // <= 36
+        uint32_t const hi = __funnelshift_lc(b, a, uint32_t(g));
+        uint32_t const lo = __funnelshift_lc(c, b, uint32_t(g));
+        uint32_t const w = off < 32 ? __funnelshift_l(lo, hi, off) : (lo << (off - 32));
+        return __funnelshift_rc(w, 0u, 32u - nb);
+    };
+    // drop n bits (n <= 48, g <= 32): one or two words from the ring
+    auto advance = [&](uint32_t n) {
+        // the next two words below the window must be in the ring
+        int32_t const m = (kb - 2) >> 2;
+        if (ok && m < r.low) {
+            r.low = m;
+            if (k == 0) {
+                r.issue(m - kFseAhead);
+                asm volatile("cp.async.wait_group %0;" ::"n"(kFseAhead) : "memory");
+            }
+        }
+        __syncwarp();
+        // a lane without a stream has no ring (its slot may lie past the CTA's memory)
+        uint32_t const w1 = ok ? ring[(kb - 1) & (4 * kFseRing - 1)] : 0u;
+        uint32_t const w2 = ok ? ring[(kb - 2) & (4 * kFseRing - 1)] : 0u;
+        g += int32_t(n);
+        bool const one = g > 32, two = g > 64;
+        uint32_t const na = two ? c : (one ? b : a);
+        uint32_t const nb2 = two ? w1 : (one ? c : b);
+        uint32_t const nc = two ? w2 : (one ? w1 : c);
+        a = na;
+        b = nb2;
+        c = nc;
+        int32_t const kk = int32_t(one) + int32_t(two);
+        kb -= kk;
+        g -= 32 * kk;
+    };
+    // initial states: state k is the k-th field of tableLog bits from the top
+    uint32_t st = 0, total = 0;
+    {
+        bool const mine = ok && k < ns;
+        uint32_t const f = fields(mine ? tl : 0u, total);
+        st = f;
+        advance(total);
+    }
+    uint32_t const n = ok ? t.dstSize : 0;
+    uint32_t const lastTr = n > ns ? n - ns : 0; // symbols [0, lastTr) have a transition
+    uint8_t* const out = t.out;
+    for (uint32_t i = 0;; i += ns) {
+        bool const act = ok && k < ns && i + k < n;
+        if (!__any_sync(0xffffffffu, act)) break;
+        bool const tr = act && i + k < lastTr;
+        uint32_t const e = act ? uint32_t(tab[st]) : 0u;
+        uint32_t const y = act ? uint32_t(symOf[st]) : 0u;
+        uint32_t const f = fields(tr ? (e & 15u) : 0u, total);
+        if (tr) st = (e >> 4) + f;
+        if (act) out[i + k] = uint8_t(y);
+        advance(total);
+    }
+    if (k == 0) asm volatile("cp.async.wait_all;" ::: "memory"); // no copy outlives the lane
+    if (ok && k == 0 && (kb + 3) * 32 - g != end) reportError(status, DERR_CORRUPTION);
+}
+
 // ---------------------------------------------------------------------------
 // Huffman: weights -> canonical table (symbols ranked by weight then value;
 // weight w spans 2^(w-1) cells, nbBits = tableLog + 1 - w), after
@@ -1928,6 +2067,8 @@ cudaError_t prepareKernels()
 {
     cudaError_t e = cudaFuncSetAttribute(kFse, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFseCtaSmem));
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kFse4, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFseCtaSmem));
+    if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(kHuf, cudaFuncAttributeMaxDynamicSharedMemorySize, int(hufSmem(kHufChunks)));
 }
 
@@ -1938,6 +2079,8 @@ uint32_t tuneCandidates(const Launch& l, uint32_t* out, uint32_t cap)
         uint32_t const mx = fseLanes(l.param0);
         for (uint32_t c : { 32u, 16u, 8u, 6u, 5u, 4u, 3u, 2u })
             if (c <= mx && n < cap) out[n++] = c;
+        for (uint32_t c : { 8u, 6u, 4u }) // kFse4: streams per warp
+            if (c <= mx && n < cap) out[n++] = kFse4Variant | c;
     } else if (l.kind == KIND_HUF) {
         for (uint32_t c : { 8u, 6u, 4u, 2u })
             if (n < cap) out[n++] = c;
@@ -1977,6 +2120,16 @@ long runOneLaunch(const DeviceLayout& L, size_t li, uint8_t* dPool, uint8_t* dSc
                 // choice on the mixed-frame workload (wider CTAs wait on their
                 // serial table builds and leave too few warps per SM to hide
                 // latency); small tables as many as fit
+                if (l.tune & kFse4Variant) { // one lane per state, up to eight streams per warp
+                    uint32_t streams = l.tune & 0xFFu;
+                    if (streams > 8) streams = 8;
+                    if (streams > maxLanes) streams = maxLanes;
+                    if (streams == 0) streams = 1;
+                    uint32_t const grid = (l.nbTasks + streams - 1) / streams;
+                    kFse4<<<grid, 32, fseSmemBytes(streams, l.param0), s>>>(static_cast<const FseTask*>(tasks), l.nbTasks,
+                                                                            streams, l.param0, dStatus);
+                    break;
+                }
                 uint32_t const dflt = l.param0 <= 8 || maxLanes < kFseDefaultLanes ? maxLanes : kFseDefaultLanes;
                 uint32_t const lanes = l.tune && l.tune <= maxLanes ? l.tune : dflt;
                 uint32_t const grid = (l.nbTasks + lanes - 1) / lanes;
