@@ -76,6 +76,11 @@ def parse_args():
     p.add_argument("--no-parity", action="store_true", help="skip the encode-parity check against the oracle")
     p.add_argument("--fse-kernel", type=int, default=None,
                    help="batch decode: FSE kernel (1 a lane per stream, 2 a lane per state); skips the autotuner")
+    p.add_argument("--critical-symbols", type=int, default=None,
+                   help="batch decode: frames with an FSE stream of at least this many symbols as their own "
+                        "branch (0 off; default: the library's, by batch size)")
+    p.add_argument("--schedule", type=int, default=None,
+                   help="batch decode: branch priorities (0 by branch rank, 1 element-wise launches first)")
     return p.parse_args()
 
 
@@ -117,7 +122,10 @@ def workload_config(n_frames, decoded, compressed, parts_per_kind):
     return {"workload": WORKLOAD, "frames": n_frames, "decoded_bytes": decoded, "compressed_bytes": compressed,
             "ratio": round(decoded / compressed, 3), "graphs": "delta->tsplit->FSE | delta->bitpack->Huffman",
             "format_version": 23, "checksums": "content+compressed, verified on decode",
-            "l2": "inputs larger than L2 (no flush)", "parts_per_kind": parts_per_kind or "library default"}
+            "l2": "inputs larger than L2 (no flush)", "parts_per_kind": parts_per_kind or "library default",
+            "branches": "parallel branches at falling stream priorities: frames with an FSE stream of 16,000+ "
+                        "symbols, then runs of the Huffman frames and of the others (library default for batches "
+                        "of 512 MiB or more)"}
 
 
 def layout(sizes, align):
@@ -884,7 +892,8 @@ def main():
 
     # ---- plan the batched decode
     d_out = torch.zeros(obytes, dtype=torch.uint8, device=dev)
-    batch = oz.GpuBatch(parts_per_kind=args.parts_per_kind, fse_kernel=args.fse_kernel)
+    batch = oz.GpuBatch(parts_per_kind=args.parts_per_kind, fse_kernel=args.fse_kernel,
+                        critical_symbols=args.critical_symbols, schedule=args.schedule)
     host_views = [frames_np[foffs[i]:foffs[i] + fsizes[i]] for i in range(n_frames)]
     planned = batch.plan(host_views, [d_frames.data_ptr() + o for o in foffs],
                          [d_out.data_ptr() + o for o in ooffs], osizes)
@@ -946,6 +955,9 @@ def main():
     # ---- roofline: per-launch profile of one run (CUDA events per launch)
     peak, peak_src = measured_hbm_peak()
     prof = batch.profile(sptr, capacity=max(64, launches + 8))
+    # concurrency: one run without the graph, an event around every launch on
+    # its branch's stream: [branch, kind, level, ms reached, ms ended]
+    timeline = [[b_, k_, l_, round(a_, 3), round(e_, 3)] for b_, k_, l_, a_, e_ in batch.timeline(sptr, capacity=256)]
     roofline = roofline_from_profile(prof, ms_per_step, total_out + total_comp, peak, peak_src, WORKLOAD)
 
     # ---- e2e: host buffers through the C ABI, copies inside the timed region
@@ -1076,6 +1088,7 @@ def main():
         "encode": {"value": round(enc_gbs, 3), "unit": "GB/s", "note": "batched compress, host decisions included",
                    "parity": enc_parity},
         "autotune": tuned,
+        "timeline": timeline,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "encode_parity": enc_parity,

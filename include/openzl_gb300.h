@@ -94,13 +94,25 @@ typedef enum {
     ZL_DParam_checkContentChecksum = 3,
     /* batch API only (no counterpart in the reference): the frames decoded
      * through Huffman and the others each split into this many runs of
-     * contiguous frames, decoded as parallel branches (1..8) */
+     * contiguous frames, decoded as parallel branches at stream priorities
+     * that fall with the run (1..8). Default: 2 for batches that decode at
+     * least 512 MiB, else 1. */
     OZL_DParam_partsPerKind = 1000,
     /* batch API only: the FSE decoder of the plan's launches until the
      * autotuner chooses: 0 the library's default shapes, 1 one lane per
      * stream, 2 one lane per decoder state (four lanes per stream). The
      * bytes decoded are the same. */
     OZL_DParam_fseKernel = 1001,
+    /* batch API only: frames holding an FSE stream of at least this many
+     * symbols (one lane decodes such a stream serially: the batch's longest
+     * chains) decode as their own branch, ahead of the runs in stream
+     * priority; 0 turns it off. Default: 16000 for batches that decode at
+     * least 512 MiB, else off. */
+    OZL_DParam_criticalSymbols = 1002,
+    /* batch API only: stream priorities of the branches. 0: a branch's
+     * launches share its rank (critical part first, then each kind's runs in
+     * order); 1: every element-wise launch ahead of all entropy decoding. */
+    OZL_DParam_schedule = 1003,
 } ZL_DParam;
 
 typedef enum {
@@ -359,6 +371,14 @@ ZL_Report ozl_gpu_batch_check(OZL_GpuBatch* b, void* stream);
  * of launches. Synchronizes `stream`. */
 ZL_Report ozl_gpu_batch_profile(OZL_GpuBatch* b, void* stream, float* ms, int* kinds,
                                 uint64_t* bytes, size_t capacity);
+/* Concurrency timeline: runs the planned batch once without a graph, its
+ * parallel branches as ozl_gpu_batch_run does, with a timing event before
+ * and after every launch on its branch's stream. Writes 5 floats per launch
+ * (part order) to rows[5 i ..]: branch, codec family, dependency level, the
+ * ms from the run's start at which its stream reached the launch, and the ms
+ * at which the launch ended; for i < capacity. Returns the number of
+ * launches. Synchronizes `stream`. */
+ZL_Report ozl_gpu_batch_timeline(OZL_GpuBatch* b, void* stream, float* rows, size_t capacity);
 /* Name of a codec family reported by ozl_gpu_batch_profile. */
 const char* ozl_gpu_kind_name(int kind);
 /* Autotuner: times the candidate launch shapes (chunks per CTA of the FSE

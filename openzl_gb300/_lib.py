@@ -71,6 +71,7 @@ def library():
         "ozl_gpu_xxh3_64": ([vp, sz, vp], ZLReport),
         "ozl_gpu_xxh3_64_static": ([vp, sz, vp], ZLReport),
         "ozl_gpu_batch_profile": ([vp, vp, vp, vp, vp, sz], ZLReport),
+        "ozl_gpu_batch_timeline": ([vp, vp, vp, sz], ZLReport),
         "ozl_gpu_kind_name": ([ctypes.c_int], ctypes.c_char_p),
         "ozl_gpu_batch_run_host": ([vp, vp, sz, vp, sz, vp, ctypes.c_int], ZLReport),
         "ozl_gpu_batch_autotune": ([vp, vp, ctypes.c_int, vp, sz], ZLReport),
@@ -182,6 +183,8 @@ DPARAM_CHECK_COMPRESSED = 2
 DPARAM_CHECK_CONTENT = 3
 DPARAM_PARTS_PER_KIND = 1000  # OZL_DParam_partsPerKind
 DPARAM_FSE_KERNEL = 1001  # OZL_DParam_fseKernel
+DPARAM_CRITICAL_SYMBOLS = 1002  # OZL_DParam_criticalSymbols
+DPARAM_SCHEDULE = 1003  # OZL_DParam_schedule
 
 
 class DCtx:
@@ -299,13 +302,18 @@ def decompress(frame):
 class GpuBatch:
     """Batched decode of many frames: one plan, one CUDA graph per run."""
 
-    def __init__(self, check_content=True, check_compressed=True, parts_per_kind=None, fse_kernel=None):
+    def __init__(self, check_content=True, check_compressed=True, parts_per_kind=None, fse_kernel=None,
+                 critical_symbols=None, schedule=None):
         self._lib = library()
         self._h = self._lib.ozl_gpu_batch_create()
         if parts_per_kind is not None:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_PARTS_PER_KIND, int(parts_per_kind)))
         if fse_kernel is not None:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_FSE_KERNEL, int(fse_kernel)))
+        if critical_symbols is not None:
+            _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_CRITICAL_SYMBOLS, int(critical_symbols)))
+        if schedule is not None:
+            _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_SCHEDULE, int(schedule)))
         if not check_content:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_CHECK_CONTENT, 2))
         if not check_compressed:
@@ -356,6 +364,18 @@ class GpuBatch:
             self._raise(rep)
         n = min(rep.value, capacity)
         return [(self._lib.ozl_gpu_kind_name(kinds[i]).decode(), ms[i], nb[i]) for i in range(n)]
+
+    def timeline(self, stream=0, capacity=4096):
+        """One run with the branches in parallel and an event around every
+        launch: (branch, kind name, level, ms its stream reached it, ms it
+        ended), from the run's start."""
+        rows = (ctypes.c_float * (5 * capacity))()
+        rep = self._lib.ozl_gpu_batch_timeline(self._h, stream, rows, capacity)
+        if rep.code:
+            self._raise(rep)
+        n = min(rep.value, capacity)
+        return [(int(rows[5 * i]), self._lib.ozl_gpu_kind_name(int(rows[5 * i + 1])).decode(), int(rows[5 * i + 2]),
+                 rows[5 * i + 3], rows[5 * i + 4]) for i in range(n)]
 
     def run_host(self, h_in_ptr, in_bytes, h_out_ptr, out_bytes, stream=0, graph=True):
         """Host buffers in and out around one planned run (copies included)."""

@@ -357,6 +357,14 @@ ZL_Report ozl_gpu_batch_setParameter(OZL_GpuBatch* b, ZL_DParam param, int value
             if (value < 0 || value > 2) return fail(ZL_ErrorCode_parameter_invalid);
             b->fseKernel = value;
             break;
+        case OZL_DParam_criticalSymbols:
+            if (value < 0) return fail(ZL_ErrorCode_parameter_invalid);
+            b->criticalSymbols = value;
+            break;
+        case OZL_DParam_schedule:
+            if (value < 0 || value > 1) return fail(ZL_ErrorCode_parameter_invalid);
+            b->schedule = value;
+            break;
         default: return fail(ZL_ErrorCode_parameter_invalid);
     }
     return ok(0);
@@ -389,6 +397,12 @@ const char* ozl_gpu_kind_name(int kind)
                                    "float_deconstruct", "transpose", "numeric_pipeline", "xxh3", "huffman16",
                                    "widen" };
     return (kind >= 0 && kind < ozl::KIND_COUNT) ? names[kind] : "?";
+}
+
+ZL_Report ozl_gpu_batch_timeline(OZL_GpuBatch* b, void* stream, float* rows, size_t capacity)
+{
+    if (!b || (capacity && !rows)) return fail(ZL_ErrorCode_parameter_invalid);
+    return b->timeline(static_cast<cudaStream_t>(stream), rows, capacity);
 }
 
 ZL_Report ozl_gpu_batch_profile(OZL_GpuBatch* b, void* stream, float* ms, int* kinds, uint64_t* bytes,

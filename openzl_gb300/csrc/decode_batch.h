@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
 #include <mutex>
 #include <algorithm>
 #include <string>
@@ -59,17 +60,26 @@ cudaError_t prepareOnce();
 // latency-bound entropy decoding. All parts share the plan's arena and
 // parameter block; each has its own descriptor pool and scratch.
 struct DecodeBatch {
-    static constexpr int kMaxParts = 16;
+    static constexpr int kMaxParts = 17; // the critical part plus 8 runs of each of two kinds
     struct Part {
         DeviceLayout layout;
         DevBuf pool, scratch;
         std::vector<char> mask;   // frames of this part
+        bool critical = false;    // frames with a long FSE stream: highest stream priority
+        int run = 0;              // index of this run within its kind
     };
     bool checkContent = true;
     bool checkCompressed = true;
     bool splitParts = true;
-    int partsPerKind = 1;     // runs per kind (OZL_DParam_partsPerKind)
+    int partsPerKind = 0;     // runs per kind (OZL_DParam_partsPerKind); 0 = by batch size
     int fseKernel = 0;        // OZL_DParam_fseKernel: 0 default shapes, 1 a lane per stream, 2 a lane per state
+    int64_t criticalSymbols = -1; // OZL_DParam_criticalSymbols: 0 = no critical part, -1 = by batch size
+    // Batches decoding at least this many bytes split by default into a
+    // critical part (FSE streams of 16,000 symbols or more) and two runs per
+    // kind; smaller ones into the Huffman frames and the others.
+    static constexpr uint64_t kSplitBytes = 512ull << 20;
+    static constexpr uint32_t kCriticalDefault = 16000;
+    int schedule = 0;             // OZL_DParam_schedule: priority policy of the branches
     DecodePlan plan;
     std::vector<Part> parts;
     DevBuf arena, params, status;
@@ -80,8 +90,8 @@ struct DecodeBatch {
     bool uploaded = false;   // descriptors and parameters of the plan are on the device
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graphStream = nullptr;
-    cudaStream_t side[kMaxParts] = {};
-    cudaEvent_t fork = nullptr, join[kMaxParts] = {};
+    std::map<uint64_t, std::pair<cudaStream_t, int>> slots; // launch-slot streams and their priorities
+    std::vector<cudaEvent_t> events;                         // dependency events of a run
     std::string err;
 
     // Host-buffer runs (ozl_gpu_batch_run_host): the frames split into
@@ -130,11 +140,8 @@ struct DecodeBatch {
     ~DecodeBatch()
     {
         dropGraph();
-        for (int p = 0; p < kMaxParts; p++) {
-            if (side[p]) cudaStreamDestroy(side[p]);
-            if (join[p]) cudaEventDestroy(join[p]);
-        }
-        if (fork) cudaEventDestroy(fork);
+        for (auto& kv : slots) cudaStreamDestroy(kv.second.first);
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
     }
     void dropGraph()
     {
@@ -175,29 +182,44 @@ struct DecodeBatch {
         dOuts.assign(reinterpret_cast<uint8_t* const*>(dO), reinterpret_cast<uint8_t* const*>(dO) + n);
         sizes.resize(n);
         for (size_t i = 0; i < n; i++) sizes[i] = size_t(plan.frames[i].decodedSize);
-        // parts: the frames decoded through Huffman and the others, each kind
-        // in runs of contiguous frames of about equal decoded bytes
-        std::vector<char> huf(n, 0);
+        // parts: frames holding an FSE stream of at least criticalSymbols
+        // symbols (decoded serially by one lane each, so they are the batch's
+        // longest chains), the frames decoded through Huffman (transform 50),
+        // and the others. Each kind splits into runs of contiguous frames of
+        // about equal decoded bytes.
+        bool const big = plan.totalOut >= kSplitBytes;
+        int const runs = partsPerKind ? partsPerKind : big ? 2 : 1;
+        uint64_t const critical = criticalSymbols >= 0 ? uint64_t(criticalSymbols) : big ? kCriticalDefault : 0;
+        std::vector<char> kindOf(n, 0);
         for (const PlanNode& nd : plan.nodes)
-            if (!nd.dead && nd.id == 50 && nd.frame >= 0) huf[size_t(nd.frame)] = 1;
+            if (!nd.dead && nd.id == 50 && nd.frame >= 0) kindOf[size_t(nd.frame)] = 1;
+        if (critical)
+            for (const PlanNode& nd : plan.nodes)
+                if (!nd.dead && nd.id == 49 && nd.frame >= 0 && nd.out >= 0
+                    && plan.streams[size_t(nd.out)].n >= critical)
+                    kindOf[size_t(nd.frame)] = 2;
         parts.clear();
         if (!splitParts) {
             parts.resize(1);
             parts[0].mask.assign(n, 1);
         } else {
-            for (char kind = 0; kind < 2; kind++) {
+            for (char kind : { char(2), char(1), char(0) }) {
                 std::vector<size_t> fr;
                 uint64_t total = 0;
                 for (size_t i = 0; i < n; i++)
-                    if (huf[i] == kind) {
+                    if (kindOf[i] == kind) {
                         fr.push_back(i);
                         total += sizes[i];
                     }
                 if (fr.empty()) continue;
-                size_t const g = std::min<size_t>(size_t(partsPerKind), fr.size());
+                size_t const g = kind == 2 ? 1 : std::min<size_t>(size_t(runs), fr.size());
                 size_t const first = parts.size();
                 parts.resize(first + g);
-                for (size_t k = 0; k < g; k++) parts[first + k].mask.assign(n, 0);
+                for (size_t k = 0; k < g; k++) {
+                    parts[first + k].mask.assign(n, 0);
+                    parts[first + k].critical = kind == 2;
+                    parts[first + k].run = int(k);
+                }
                 uint64_t acc = 0;
                 size_t k = 0;
                 for (size_t i : fr) {
@@ -210,6 +232,10 @@ struct DecodeBatch {
                 parts.resize(1);
                 parts[0].mask.assign(n, 1);
             }
+        }
+        if (parts.size() > size_t(kMaxParts)) {
+            err = "too many parts";
+            return reportFail(ZL_ErrorCode_parameter_invalid);
         }
         if (!arena.reserve(plan.arenaBytes) || !params.reserve(plan.params.size()) || !status.reserve(64)) {
             err = "device allocation failed";
@@ -256,41 +282,165 @@ struct DecodeBatch {
         return reportOk(0);
     }
 
-    ZL_Report enqueue(cudaStream_t s)
+    // Stream of one launch slot: (part, position within its level, priority
+    // class). Kept across runs; recreated when its priority changes.
+    cudaStream_t slotStream(size_t part, size_t slot, int cls, int prio)
+    {
+        uint64_t const key = (uint64_t(part) << 24) | (uint64_t(slot) << 4) | uint64_t(cls);
+        auto it = slots.find(key);
+        if (it != slots.end() && it->second.second == prio) return it->second.first;
+        if (it != slots.end()) {
+            cudaStreamDestroy(it->second.first);
+            slots.erase(it);
+        }
+        cudaStream_t x = nullptr;
+        if (cudaStreamCreateWithPriority(&x, cudaStreamNonBlocking, prio) != cudaSuccess) return nullptr;
+        slots.emplace(key, std::make_pair(x, prio));
+        return x;
+    }
+    // the k-th event of this run (created once, reused by later runs)
+    cudaEvent_t nextEvent(size_t& k)
+    {
+        if (k == events.size()) {
+            cudaEvent_t e = nullptr;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+            events.push_back(e);
+        }
+        return events[k++];
+    }
+
+    // Enqueues the plan on `s` as a DAG: each part (branch) runs its
+    // dependency levels in order, and the launches of one level, which do not
+    // depend on one another, on streams of their own. Stream priorities
+    // order the block scheduler's work. Schedule 0: a branch's launches share
+    // its rank: the critical part (the longest chains) first, then each
+    // kind's runs in order, so that a run's element-wise work shares the SMs
+    // with the next run's entropy decoding. Schedule 1: every element-wise
+    // launch (short, memory-bound) ahead of all entropy decoding, which keeps
+    // the branch ranks. `marks` (timeline runs): a timing event before and
+    // after every launch, in part order, on its stream.
+    ZL_Report enqueue(cudaStream_t s, const std::vector<cudaEvent_t>* marks = nullptr)
     {
         if (cudaMemsetAsync(status.data(), 0, 4, s) != cudaSuccess) {
             err = "status reset failed";
             return reportFail(ZL_ErrorCode_GENERIC);
         }
         uint32_t* const st = reinterpret_cast<uint32_t*>(status.data());
-        size_t const np = parts.size();
-        if (np > 1) {
-            if (!fork && cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
-            for (size_t p = 1; p < np; p++) {
-                if (!side[p] && cudaStreamCreateWithFlags(&side[p], cudaStreamNonBlocking) != cudaSuccess)
-                    return reportFail(ZL_ErrorCode_GENERIC);
-                if (!join[p] && cudaEventCreateWithFlags(&join[p], cudaEventDisableTiming) != cudaSuccess)
-                    return reportFail(ZL_ErrorCode_GENERIC);
-            }
-            cudaEventRecord(fork, s);
-            for (size_t p = 1; p < np; p++) cudaStreamWaitEvent(side[p], fork, 0);
-        }
-        long total = 0;
-        for (size_t p = 0; p < np; p++) {
-            cudaStream_t const ps = p == 0 ? s : side[p];
-            long n = runLaunches(parts[p].layout, parts[p].pool.data(), parts[p].scratch.data(), st, ps);
+        if (parts.size() == 1 && !marks) { // one branch: its launches in order on `s`
+            long const n = runLaunches(parts[0].layout, parts[0].pool.data(), parts[0].scratch.data(), st, s);
             if (n < 0) {
                 err = std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError());
                 return reportFail(ZL_ErrorCode_GENERIC);
             }
-            total += n;
+            launches = n;
+            return reportOk(0);
         }
-        for (size_t p = 1; p < np; p++) {
-            cudaEventRecord(join[p], side[p]);
-            cudaStreamWaitEvent(s, join[p], 0);
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) least = greatest = 0;
+        bool anyCritical = false;
+        for (const Part& p : parts) anyCritical = anyCritical || p.critical;
+        auto prioOf = [&](const Part& p, int kind) {
+            int const branch = p.critical ? 0 : p.run + (anyCritical ? 1 : 0);
+            bool const entropy = kind == KIND_FSE || kind == KIND_HUF || kind == KIND_HUF16;
+            int const rank = schedule == 1 ? (entropy ? 1 + branch : 0) : branch;
+            return std::min(least, greatest + rank); // greatest is the numerically smallest
+        };
+        size_t ev = 0;
+        cudaEvent_t const start = nextEvent(ev);
+        if (!start || cudaEventRecord(start, s) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
+        long total = 0;
+        size_t mark = 0;
+        std::vector<cudaEvent_t> ends;
+        for (size_t p = 0; p < parts.size(); p++) {
+            const DeviceLayout& L = parts[p].layout;
+            cudaEvent_t ready = start; // everything the next level waits for
+            for (size_t a = 0; a < L.launches.size();) {
+                size_t b = a;
+                while (b < L.launches.size() && L.launches[b].level == L.launches[a].level) b++;
+                std::vector<cudaStream_t> used;
+                std::vector<cudaEvent_t> done;
+                for (size_t li = a; li < b; li++, mark += 2) {
+                    int const cls = (L.launches[li].kind == KIND_FSE || L.launches[li].kind == KIND_HUF
+                                     || L.launches[li].kind == KIND_HUF16) ? 1 : 0;
+                    cudaStream_t const x = slotStream(p, li - a, cls, prioOf(parts[p], L.launches[li].kind));
+                    cudaEvent_t const e = nextEvent(ev);
+                    if (!x || !e || cudaStreamWaitEvent(x, ready, 0) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
+                    if (marks) cudaEventRecord((*marks)[mark], x);
+                    long const k = runOneLaunch(L, li, parts[p].pool.data(), parts[p].scratch.data(), st, x);
+                    if (marks) cudaEventRecord((*marks)[mark + 1], x);
+                    if (k < 0) {
+                        err = std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError());
+                        return reportFail(ZL_ErrorCode_GENERIC);
+                    }
+                    total += k;
+                    if (cudaEventRecord(e, x) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
+                    used.push_back(x);
+                    done.push_back(e);
+                }
+                if (done.size() == 1) {
+                    ready = done[0];
+                } else {
+                    // join the level on its first stream
+                    for (size_t k = 1; k < done.size(); k++) cudaStreamWaitEvent(used[0], done[k], 0);
+                    cudaEvent_t const j = nextEvent(ev);
+                    if (!j || cudaEventRecord(j, used[0]) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
+                    ready = j;
+                }
+                a = b;
+            }
+            ends.push_back(ready);
         }
+        for (cudaEvent_t e : ends)
+            if (cudaStreamWaitEvent(s, e, 0) != cudaSuccess) return reportFail(ZL_ErrorCode_GENERIC);
         launches = total;
         return reportOk(0);
+    }
+
+    // One run without a graph, branches as in run(), with a timing event
+    // around every launch. Row i of `rows` (5 floats, launches in part
+    // order): part, kind, level, the ms from the run's start at which the
+    // launch's stream reached it, and the ms at which it ended. A launch may
+    // wait for SMs after its stream reaches it, so the gap between the two
+    // bounds its time from above. Synchronizes `s`.
+    ZL_Report timeline(cudaStream_t s, float* rows, size_t capacity)
+    {
+        ZL_Report const u = upload(s);
+        if (ZL_isError(u)) return u;
+        size_t const n = nbLaunches();
+        std::vector<cudaEvent_t> marks(2 * n, nullptr);
+        cudaEvent_t start = nullptr;
+        bool ok = cudaEventCreate(&start) == cudaSuccess;
+        for (auto& e : marks) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+        ZL_Report r = reportOk(0);
+        if (ok) {
+            cudaEventRecord(start, s);
+            r = enqueue(s, &marks);
+            ok = !ZL_isError(r) && cudaStreamSynchronize(s) == cudaSuccess;
+        }
+        size_t i = 0;
+        for (size_t p = 0; ok && p < parts.size(); p++)
+            for (size_t li = 0; li < parts[p].layout.launches.size(); li++, i++) {
+                if (i >= capacity) continue;
+                float a = 0, b = 0;
+                cudaEventElapsedTime(&a, start, marks[2 * i]);
+                cudaEventElapsedTime(&b, start, marks[2 * i + 1]);
+                const Launch& l = parts[p].layout.launches[li];
+                float* row = rows + 5 * i;
+                row[0] = float(p);
+                row[1] = float(l.kind);
+                row[2] = float(l.level);
+                row[3] = a;
+                row[4] = b;
+            }
+        for (auto& e : marks)
+            if (e) cudaEventDestroy(e);
+        if (start) cudaEventDestroy(start);
+        if (ZL_isError(r)) return r;
+        if (!ok) {
+            err = "timeline run failed";
+            return reportFail(ZL_ErrorCode_GENERIC);
+        }
+        return reportOk(n);
     }
 
     ZL_Report run(cudaStream_t s, bool useGraph)
@@ -313,7 +463,8 @@ struct DecodeBatch {
             cudaError_t e = cudaStreamEndCapture(s, &g);
             if (ZL_isError(r)) { if (g) cudaGraphDestroy(g); return r; }
             if (e != cudaSuccess) { err = "stream capture failed"; return reportFail(ZL_ErrorCode_GENERIC); }
-            e = cudaGraphInstantiate(&graph, g, 0);
+            // per-node priorities: the captured branches keep their streams' priorities
+            e = cudaGraphInstantiateWithFlags(&graph, g, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) { graph = nullptr; err = "graph instantiation failed"; return reportFail(ZL_ErrorCode_GENERIC); }
             graphStream = s;
@@ -537,7 +688,7 @@ struct DecodeBatch {
             cudaError_t e = cudaStreamEndCapture(s, &g);
             if (ZL_isError(r)) { if (g) cudaGraphDestroy(g); return r; }
             if (e != cudaSuccess) { err = "stream capture failed"; return reportFail(ZL_ErrorCode_GENERIC); }
-            e = cudaGraphInstantiate(&host.graph, g, 0);
+            e = cudaGraphInstantiateWithFlags(&host.graph, g, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) { host.graph = nullptr; err = "graph instantiation failed"; return reportFail(ZL_ErrorCode_GENERIC); }
             host.gIn = hIn;

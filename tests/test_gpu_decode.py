@@ -330,10 +330,12 @@ def test_multi_output_frames(gpu_lib, manifest, manifest_multi):
     assert rep.code == 8
 
 
-@pytest.mark.parametrize("parts_per_kind", [1, 2, 4])
-def test_batch_parts_per_kind_keep_results(gpu_lib, manifest, parts_per_kind):
-    """Runs of frames decoded as parallel graph branches (each kind split into
-    1, 2 or 4 runs) give the same bytes, with and without the graph."""
+@pytest.mark.parametrize("parts_per_kind,critical", [(1, 0), (2, 0), (4, 0), (1, 1000), (2, 16000), (8, 100)])
+def test_batch_parts_per_kind_keep_results(gpu_lib, manifest, parts_per_kind, critical):
+    """Runs of frames decoded as parallel graph branches at falling stream
+    priorities (each kind split into 1 to 8 runs; frames with an FSE stream of
+    at least `critical` symbols as one more branch, 17 branches at most) give
+    the same bytes, with and without the graph."""
     import torch
     import openzl_gb300 as oz
 
@@ -342,7 +344,7 @@ def test_batch_parts_per_kind_keep_results(gpu_lib, manifest, parts_per_kind):
     sizes = [oz.get_decompressed_size(f) for f in frames]
     outs = [torch.zeros(max(n, 1) + 64, dtype=torch.uint8, device="cuda") for n in sizes]
     s = torch.cuda.Stream()
-    b = oz.GpuBatch(parts_per_kind=parts_per_kind)
+    b = oz.GpuBatch(parts_per_kind=parts_per_kind, critical_symbols=critical)
     b.plan(frames, [d.data_ptr() for d in dfr], [o.data_ptr() for o in outs], sizes)
     torch.cuda.synchronize()
     for graph in (False, True):
