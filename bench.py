@@ -877,6 +877,7 @@ def main():
             torch.cuda.synchronize()
             enc_times.append(time.perf_counter() - t0)
     enc_gbs = total_out / min(enc_times) / 1e9
+    enc_phases = enc.phases()  # of the last timed call
     enc_launches = enc.launches() if hasattr(enc, "launches") else None
 
     # compact the frames back to back (FRAME_ALIGN) for the host-buffer path
@@ -1086,7 +1087,7 @@ def main():
         "serving": serving,
         "columnar": columnar,
         "encode": {"value": round(enc_gbs, 3), "unit": "GB/s", "note": "batched compress, host decisions included",
-                   "parity": enc_parity},
+                   "phases_ms": enc_phases, "parity": enc_parity},
         "autotune": tuned,
         "timeline": timeline,
         "roofline": roofline,

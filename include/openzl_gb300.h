@@ -441,6 +441,13 @@ ZL_Report ozl_gpu_compress_batch(OZL_GpuEncoder* e, size_t nbFrames, const void*
                                  int checksums, void* stream);
 /* Message describing the encoder's last error ("" when none). */
 const char* ozl_gpu_encoder_error(const OZL_GpuEncoder* e);
+/* Wall-clock milliseconds of the last ozl_gpu_compress_batch's phases, in
+ * order: front end (GPU), graph discovery (host), histograms (GPU), codec
+ * decisions and coding tables, entropy bitstreams (GPU), graph replay
+ * (host), frame assembly and checksums (GPU); a phase that ends in a stream
+ * synchronize includes its device work. Writes ms[i] for i < capacity and
+ * returns the number of phases (7). */
+ZL_Report ozl_gpu_encoder_phases(const OZL_GpuEncoder* e, float* ms, size_t capacity);
 
 /* XXH3-64 (seed 0), the hash behind OpenZL's checksums, of `len` bytes of
  * device memory; computed on the GPU. Returns the hash in the report value. */

@@ -80,6 +80,7 @@ def library():
         "ozl_gpu_compress_bound": ([sz], sz),
         "ozl_gpu_compress_batch": ([vp, sz, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, vp], ZLReport),
         "ozl_gpu_encoder_error": ([vp], ctypes.c_char_p),
+        "ozl_gpu_encoder_phases": ([vp, vp, sz], ZLReport),
         "ZL_DCtx_decompressTyped": ([vp, ctypes.POINTER(OutputInfo), vp, sz, vp, sz], ZLReport),
         "ZL_TypedBuffer_create": ([], vp),
         "ZL_TypedBuffer_free": ([vp], None),
@@ -432,6 +433,16 @@ class GpuEncoder:
         if rep.code:
             raise ZLError(rep.code, self._lib.ozl_gpu_encoder_error(self._h).decode())
         return [fs[i] for i in range(n)]
+
+    PHASES = ("front_end", "discovery", "histograms", "decisions", "bitstreams", "replay", "assembly")
+
+    def phases(self):
+        """Milliseconds of the last compress_batch's phases, by name."""
+        ms = (ctypes.c_float * len(self.PHASES))()
+        rep = self._lib.ozl_gpu_encoder_phases(self._h, ms, len(self.PHASES))
+        if rep.code:
+            raise ZLError(rep.code, "ozl_gpu_encoder_phases failed")
+        return {k: round(ms[i], 3) for i, k in enumerate(self.PHASES)}
 
 
 # ---------------------------------------------------------------------------

@@ -107,6 +107,13 @@ size_t ozl_gpu_compress_bound(size_t srcBytes) { return ozl::encodeBound(srcByte
 
 const char* ozl_gpu_encoder_error(const OZL_GpuEncoder* e) { return e ? e->err.c_str() : ""; }
 
+ZL_Report ozl_gpu_encoder_phases(const OZL_GpuEncoder* e, float* ms, size_t capacity)
+{
+    if (!e || (capacity && !ms)) return fail(ZL_ErrorCode_parameter_invalid);
+    for (size_t i = 0; i < capacity && i < size_t(ozl::EncodeBatch::kPhases); i++) ms[i] = float(e->batch.lastPhaseMs()[i]);
+    return ok(size_t(ozl::EncodeBatch::kPhases));
+}
+
 ZL_Report ozl_gpu_compress_batch(OZL_GpuEncoder* e, size_t n, const void* const* d_srcs, const size_t* nbElts,
                                  const int* eltWidths, const int* recipes, void* const* d_dsts, const size_t* caps,
                                  size_t* frameSizes, int checksums, void* stream)

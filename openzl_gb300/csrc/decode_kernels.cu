@@ -1552,7 +1552,7 @@ __global__ void __launch_bounds__(32) kHuf(const HufTask* __restrict__ tasks, ui
         }
         __syncwarp();
         uint32_t const tlk = sTl[k];
-        for (uint32_t s = threadIdx.x; s < tk.nbWeights; s += 32) {
+        for (uint32_t s = threadIdx.x; s < tk.nbWeights; s += blockDim.x) { // 4 x chunks threads
             uint32_t const w = tk.weights[s];
             if (!w) continue;
             uint32_t const len = 1u << (w - 1);

@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstddef>
 #include <cstring>
 #include <memory>
@@ -786,6 +787,15 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
     size_t const nf = frames.size();
     sizes.assign(nf, 0);
     std::vector<Front> fronts(nf);
+    for (double& m : phaseMs_) m = 0;
+    auto clock0 = std::chrono::steady_clock::now();
+    int phase = 0;
+    auto endPhase = [&]() { // closes phase `phase` and opens the next
+        auto const now = std::chrono::steady_clock::now();
+        if (phase < kPhases) phaseMs_[phase] = std::chrono::duration<double, std::milli>(now - clock0).count();
+        clock0 = now;
+        phase++;
+    };
 
     // ---- phase A: front-end plan -------------------------------------------------
     for (size_t f = 0; f < nf; f++) {
@@ -1153,6 +1163,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         }
     }
 
+    endPhase();
     // ---- phase B: discovery ------------------------------------------------------
     I.jobs.clear();
     auto runFrame = [&](size_t f, bool discover, size_t* cursor, Engine& E) {
@@ -1216,6 +1227,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         I.nbDataJobs = I.jobs.size();
     }
 
+    endPhase();
     // ---- phase C: histograms ------------------------------------------------------
     size_t const nj = I.nbDataJobs;
     std::vector<uint32_t> hists(nj * 256);
@@ -1280,6 +1292,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         }
     }
 
+    endPhase();
     // ---- phase D: decisions and tables ------------------------------------------
     auto decide = [&](Job& j) {
         j.hist.n = j.n;
@@ -1466,6 +1479,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         });
     }
 
+    endPhase();
     // ---- phase E: entropy bitstreams -----------------------------------------------
     {
         std::vector<FseTableTask> fseTabT;
@@ -1710,6 +1724,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         }
     }
 
+    endPhase();
     // ---- phase F: replay and frame layout --------------------------------------
     struct FrameOut {
         std::vector<uint8_t> head;     // frame header + chunk header + codec headers
@@ -1788,6 +1803,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             if (rcs[f]) { err = msgs[f]; return rcs[f]; }
     }
 
+    endPhase();
     // ---- phase G: assembly and checksums -----------------------------------------
     {
         // host bytes go through one staging upload
@@ -1905,6 +1921,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         }
         if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in frame assembly"; return 1; }
     }
+    endPhase();
     return 0;
 }
 

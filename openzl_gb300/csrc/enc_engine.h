@@ -49,12 +49,17 @@ class EncodeBatch {
     int compress(const std::vector<EncFrameSpec>& frames, uint8_t* const* dOut, const size_t* caps,
                  bool checksums, cudaStream_t stream, std::vector<size_t>& sizes, std::string& err);
     size_t lastLaunches() const { return launches_; }
+    // Wall-clock milliseconds of the last compress() call's phases A-G (a
+    // phase that ends in a stream synchronize includes its device work).
+    static constexpr int kPhases = 7;
+    const double* lastPhaseMs() const { return phaseMs_; }
 
     struct Impl;
 
   private:
     Impl* impl_;
     size_t launches_ = 0;
+    double phaseMs_[kPhases] = {};
 };
 
 // Worst-case frame size for `srcBytes` of input (ZL_compressBound-style).

@@ -52,6 +52,8 @@ def lib():
         l.ozo_free.argtypes = [ctypes.c_void_p]
         l.ozo_test_set_fse_max_tablelog.restype = None
         l.ozo_test_set_fse_max_tablelog.argtypes = [ctypes.c_uint]
+        l.ozo_test_set_huf_max_tablelog.restype = None
+        l.ozo_test_set_huf_max_tablelog.argtypes = [ctypes.c_uint]
         l.ozo_xxh3_64.restype = ctypes.c_uint64
         l.ozo_xxh3_64.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
         _lib = l
@@ -121,6 +123,17 @@ def compress_tablelog12(recipe, arr, elt_width, checksums=True):
         return compress(recipe, arr, elt_width, checksums)
     finally:
         lib().ozo_test_set_fse_max_tablelog(11)
+
+
+def compress_huf_tablelog12(recipe, arr, elt_width, checksums=True):
+    """Like compress(), but the Huffman encoder may pick table log 12 (the
+    decoders' limit) where the reference's encoder stops at 11. Test frames
+    for the widest Huffman tables; valid for the reference's decoder."""
+    lib().ozo_test_set_huf_max_tablelog(12)
+    try:
+        return compress(recipe, arr, elt_width, checksums)
+    finally:
+        lib().ozo_test_set_huf_max_tablelog(11)
 
 
 def xxh3_64(buf):

@@ -67,6 +67,7 @@ int64_t ozo_tokenize(const void* src, size_t n, int w, int sorted, void* alphaOu
 /* Test entry point: the largest FSE table log the encoder may pick, 11 (the
  * reference encoder's) or 12 (the decoders' limit). Not thread-safe. */
 void ozo_test_set_fse_max_tablelog(unsigned tl);
+void ozo_test_set_huf_max_tablelog(unsigned tl);
 
 #ifdef __cplusplus
 }

@@ -1191,6 +1191,12 @@ static unsigned g_fseMaxTableLog = 11;
 
 void ozo_test_set_fse_max_tablelog(unsigned tl) { g_fseMaxTableLog = tl == 12 ? 12u : 11u; }
 
+/* Test hook, like the FSE one: Huffman tables may reach table log 12 (the
+ * decoders' limit, HUF_TABLELOG_MAX) where the reference's encoder uses 11
+ * (HUF_TABLELOG_DEFAULT). */
+static unsigned g_hufMaxTableLog = 11;
+void ozo_test_set_huf_max_tablelog(unsigned tl) { g_hufMaxTableLog = tl == 12 ? 12u : 11u; }
+
 /* EI_fse_v2 (encode_entropy_binding.c:51-139): outputs normalized counts
  * (numeric i16) and the bitstream. */
 static int node_fse(ECtx* c, int in, const Stats* st)
@@ -1247,7 +1253,7 @@ static int node_huf(ECtx* c, int in, const Stats* st)
     unsigned const maxSV = st->maxSym;
     ENode* nd = new_node(c, TR_HUFFMAN_V2, in, 2);
     int ws = new_stream(c, OZO_TYPE_NUMERIC, 1, maxSV + 1, NULL);
-    unsigned tl = fse_optimal_tablelog(11, n, maxSV, 1);
+    unsigned tl = fse_optimal_tablelog(g_hufMaxTableLog, n, maxSV, 1);
     HufC ct;
     tl = huf_build_ctable(&ct, st->count, maxSV, tl);
     for (unsigned s = 0; s <= maxSV; s++)

@@ -356,6 +356,37 @@ def test_batch_parts_per_kind_keep_results(gpu_lib, manifest, parts_per_kind, cr
             assert hashlib.sha256(o[:n].cpu().numpy().tobytes()).hexdigest() == m["sha256_in"], (m["case"], graph)
 
 
+def test_huffman_tablelog12_chunks(gpu_lib):
+    """Huffman chunks at table log 12 (a table across two slots, decoded in a
+    second round of the CTA) through the host API and the batch API, before
+    and after the autotuner (CTAs of 2 to 8 chunks), against the input."""
+    import torch
+    import openzl_gb300 as oz
+    from test_oracle import huf_tablelog12_cases
+
+    cases = huf_tablelog12_cases()
+    d = oz.DCtx()
+    for recipe, arr, w, fr in cases:
+        out = d.decompress_typed(fr.tobytes())[0] if w else d.decompress(fr.tobytes())
+        assert out.tobytes() == arr.tobytes(), (recipe, arr.size)
+    frames = [fr.tobytes() for _, _, _, fr in cases]
+    dfr = [_dev(torch, f) for f in frames]
+    outs = [torch.zeros(a.nbytes + 64, dtype=torch.uint8, device="cuda") for _, a, _, _ in cases]
+    b = oz.GpuBatch()
+    b.plan(frames, [t.data_ptr() for t in dfr], [o.data_ptr() for o in outs], [a.nbytes for _, a, _, _ in cases])
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    for tune in (False, True):
+        if tune:
+            b.autotune(side.cuda_stream, reps=1)
+        for o in outs:
+            o.zero_()
+        b.run(side.cuda_stream, graph=True)
+        b.check(side.cuda_stream)
+        for (_, a, _, _), o in zip(cases, outs):
+            assert o[:a.nbytes].cpu().numpy().tobytes() == a.tobytes(), tune
+
+
 def test_fse_tablelog12_streams(gpu_lib):
     """FSE chunks at table log 12 (the widest fields and largest state bases
     of the four-state register-window loop), unchunked streams of 99,999

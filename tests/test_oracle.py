@@ -298,6 +298,39 @@ def test_tablelog12_frames_decode_in_oracle_and_reference():
             assert n == arr.nbytes and out[:n].tobytes() == arr.tobytes()
 
 
+def huf_tablelog12_cases():
+    """Frames whose Huffman chunks use table log 12, the decoders' limit (the
+    reference's encoder stops at 11): skewed bytes whose rarest codes reach
+    12 bits, unchunked and in 32 KiB chunks, and a bit-packed numeric graph."""
+    rng = np.random.default_rng(1213)
+    geo = lambda p, n: np.minimum(rng.geometric(p, n) - 1, 255)  # noqa: E731
+    cases = [(8, geo(0.2, 90000).astype(np.uint8), 0),
+             (8, geo(0.15, 400000).astype(np.uint8), 0),
+             (4, np.cumsum(geo(0.3, 60000)).astype(np.uint32), 4),
+             (4, np.cumsum(geo(0.25, 60000) + 1).astype(np.uint16), 2)]
+    return [(r, a, w, oracle.compress_huf_tablelog12(r, a, w)) for r, a, w in cases]
+
+
+def test_huf_tablelog12_frames_decode_in_oracle_and_reference():
+    import ctypes
+
+    cases = huf_tablelog12_cases()
+    ref = None
+    if os.path.exists(REF_DRIVER):
+        ref = ctypes.CDLL(REF_DRIVER)
+        ref.ref_decompress_into.restype = ctypes.c_int64
+        ref.ref_decompress_into.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                                            ctypes.c_int]
+    for recipe, arr, w, fr in cases:
+        assert fr.tobytes() != oracle.compress(recipe, arr, w).tobytes()
+        data, _, _ = oracle.decompress(fr)
+        assert data.tobytes() == arr.tobytes()
+        if ref is not None:
+            out = np.zeros(arr.nbytes + 64, np.uint8)
+            n = ref.ref_decompress_into(fr.ctypes.data, fr.size, out.ctypes.data, out.size, 1)
+            assert n == arr.nbytes and out[:n].tobytes() == arr.tobytes()
+
+
 def test_oracle_frames_of_many_chunks():
     """A concatenation of more than 300 entropy chunks (a 12 MB serial input
     cut into 32 KiB chunks) decodes, and the encoder's frame equals the
