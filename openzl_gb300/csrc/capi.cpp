@@ -10,6 +10,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/openzl_gb300.h"
@@ -51,9 +52,25 @@ struct ZL_DCtx_s {
     }
 };
 
+// A large batch is encoded as two halves of about equal bytes, each by its
+// own engine on its own host thread and stream, so that one half's host
+// phases (graph discovery, codec decisions, replay) run while the other
+// half's kernels do. Frames are independent; each half's frames are the
+// bytes a whole-batch call would write.
 struct OZL_GpuEncoder_s {
-    ozl::EncodeBatch batch;
+    static constexpr int kHalves = 2;
+    static constexpr uint64_t kSplitBytes = 64ull << 20; // smaller batches: one engine, the caller's stream
+    ozl::EncodeBatch batch[kHalves];
+    cudaStream_t streams[kHalves] = {};
+    cudaEvent_t ready = nullptr;
+    double phaseMs[ozl::EncodeBatch::kPhases] = {};
     std::string err;
+    ~OZL_GpuEncoder_s()
+    {
+        for (cudaStream_t x : streams)
+            if (x) cudaStreamDestroy(x);
+        if (ready) cudaEventDestroy(ready);
+    }
 };
 
 extern "C" {
@@ -110,7 +127,7 @@ const char* ozl_gpu_encoder_error(const OZL_GpuEncoder* e) { return e ? e->err.c
 ZL_Report ozl_gpu_encoder_phases(const OZL_GpuEncoder* e, float* ms, size_t capacity)
 {
     if (!e || (capacity && !ms)) return fail(ZL_ErrorCode_parameter_invalid);
-    for (size_t i = 0; i < capacity && i < size_t(ozl::EncodeBatch::kPhases); i++) ms[i] = float(e->batch.lastPhaseMs()[i]);
+    for (size_t i = 0; i < capacity && i < size_t(ozl::EncodeBatch::kPhases); i++) ms[i] = float(e->phaseMs[i]);
     return ok(size_t(ozl::EncodeBatch::kPhases));
 }
 
@@ -129,9 +146,51 @@ ZL_Report ozl_gpu_compress_batch(OZL_GpuEncoder* e, size_t n, const void* const*
     }
     std::vector<size_t> sizes;
     e->err.clear();
-    int rc = e->batch.compress(specs, reinterpret_cast<uint8_t* const*>(d_dsts), caps, checksums != 0,
-                               static_cast<cudaStream_t>(stream), sizes, e->err);
-    if (rc) return fail(rc);
+    uint8_t* const* const outs = reinterpret_cast<uint8_t* const*>(d_dsts);
+    cudaStream_t const us = static_cast<cudaStream_t>(stream);
+    uint64_t bytes = 0;
+    for (const ozl::EncFrameSpec& f : specs) bytes += f.n * f.w;
+    int rc = 0;
+    if (n < 2 || bytes < OZL_GpuEncoder_s::kSplitBytes) {
+        rc = e->batch[0].compress(specs, outs, caps, checksums != 0, us, sizes, e->err);
+        if (rc) return fail(rc);
+        for (int i = 0; i < ozl::EncodeBatch::kPhases; i++) e->phaseMs[i] = e->batch[0].lastPhaseMs()[i];
+    } else {
+        // halves of about equal bytes; both streams wait for the caller's
+        // work on `stream` (the inputs), and both halves synchronize theirs
+        size_t cut = 1;
+        uint64_t acc = specs[0].n * specs[0].w;
+        while (cut + 1 < n && 2 * acc < bytes) {
+            acc += specs[cut].n * specs[cut].w;
+            cut++;
+        }
+        bool okSetup = (e->ready || cudaEventCreateWithFlags(&e->ready, cudaEventDisableTiming) == cudaSuccess);
+        for (cudaStream_t& x : e->streams)
+            okSetup = okSetup && (x || cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) == cudaSuccess);
+        okSetup = okSetup && cudaEventRecord(e->ready, us) == cudaSuccess;
+        for (cudaStream_t x : e->streams) okSetup = okSetup && cudaStreamWaitEvent(x, e->ready, 0) == cudaSuccess;
+        if (!okSetup) {
+            e->err = "encoder streams could not be set up";
+            return fail(ZL_ErrorCode_GENERIC);
+        }
+        std::vector<ozl::EncFrameSpec> const lo(specs.begin(), specs.begin() + cut), hi(specs.begin() + cut, specs.end());
+        std::vector<size_t> sizesHi;
+        std::string errHi;
+        int rcHi = 0;
+        std::thread other([&] {
+            rcHi = e->batch[1].compress(hi, outs + cut, caps + cut, checksums != 0, e->streams[1], sizesHi, errHi);
+        });
+        rc = e->batch[0].compress(lo, outs, caps, checksums != 0, e->streams[0], sizes, e->err);
+        other.join();
+        if (!rc && rcHi) {
+            rc = rcHi;
+            e->err = errHi;
+        }
+        if (rc) return fail(rc);
+        sizes.insert(sizes.end(), sizesHi.begin(), sizesHi.end());
+        for (int i = 0; i < ozl::EncodeBatch::kPhases; i++)
+            e->phaseMs[i] = std::max(e->batch[0].lastPhaseMs()[i], e->batch[1].lastPhaseMs()[i]);
+    }
     size_t total = 0;
     for (size_t i = 0; i < n; i++) {
         frameSizes[i] = sizes[i];

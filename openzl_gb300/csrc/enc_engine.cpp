@@ -1625,6 +1625,11 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         Bump stg{ I.bufE.data() + stageOff, 0 };
         layoutE(b, stg, true);
         if (b.used > stageOff) { err = "encode layout overflow"; return 1; }
+        // longest chunks first: one lane encodes a chunk serially, so the
+        // longest chains start at once and the short ones fill around them
+        // (each task writes its own output and size slot)
+        std::stable_sort(fseT.begin(), fseT.end(), [](const FseEncTask& a, const FseEncTask& c) { return a.n > c.n; });
+        std::stable_sort(hufT.begin(), hufT.end(), [](const HufEncTask& a, const HufEncTask& c) { return a.n > c.n; });
         parallelFor(ups.size(), [&](size_t k) {
             std::memcpy(I.stage.p + (ups[k].dev - stg.base), ups[k].host, ups[k].bytes);
         });

@@ -7,6 +7,7 @@
 // bit order restates src/openzl/fse/bitstream.h (fields appended LSB-first,
 // a final 1 marker bit).
 #include <cstdint>
+#include <type_traits>
 
 #include <cuda_runtime.h>
 
@@ -15,6 +16,7 @@
 #include "fse_norm.h"
 #include "huf_tree.h"
 #include "enc_tasks.h"
+#include "stream_ring.cuh"
 
 namespace ozl {
 
@@ -111,6 +113,99 @@ __global__ void kEncMax(const EncNumTask* __restrict__ tasks, const TileRef* __r
     if ((threadIdx.x & 31) == 0) atomicMax(&maxima[t.maxSlot], (unsigned long long)mx);
 }
 
+// Element e of consecutive W-byte elements held as little-endian words.
+template <int W>
+__device__ __forceinline__ uint64_t elemOf(const uint32_t* u, int e)
+{
+    if constexpr (W == 8) return uint64_t(u[2 * e]) | (uint64_t(u[2 * e + 1]) << 32);
+    else if constexpr (W == 4) return u[e];
+    else if constexpr (W == 2) return (u[e >> 1] >> (16 * (e & 1))) & 0xffffu;
+    else return (u[e >> 2] >> (8 * (e & 3))) & 0xffu;
+}
+
+// The thread's 32 elements [i0, i0 + 32) of a full tile when the source is
+// 16-byte aligned, in rounds of R elements (64 bytes for 8-byte elements,
+// else 16 elements) loaded as 16-byte vectors; the element after a round,
+// which delta needs, is the next round's first (loaded one round ahead) or
+// one more load after the last. Values are transformed in registers and
+// written as vectors (plain, byte planes) or packed fields. Returns false
+// (the caller takes the element loop) when an output is not 16-byte aligned.
+template <int W>
+__device__ __forceinline__ bool encNumVec(const EncNumTask& t, uint64_t i0)
+{
+    constexpr int R = W == 8 ? 8 : 16, NV = R * W / 16, ROUNDS = 32 / R;
+    if (t.mode == EOUT_PLAIN && (reinterpret_cast<uintptr_t>(t.out) & 15)) return false;
+    if (t.mode == EOUT_PLANES && ((reinterpret_cast<uintptr_t>(t.out) | t.planeStride) & 15)) return false;
+    using V = typename std::conditional<W == 8, uint64_t, uint32_t>::type;
+    uint64_t const m = W >= 8 ? ~0ull : ((1ull << (8 * W)) - 1);
+    const uint4* const src = reinterpret_cast<const uint4*>(t.src + i0 * W);
+    WordPacker wp(t.out + (i0 / 32) * 4 * t.nbBits);
+    uint32_t u[4 * NV], nx[4 * NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) reinterpret_cast<uint4*>(u)[q] = __ldg(src + q);
+#pragma unroll
+    for (int h = 0; h < ROUNDS; h++) {
+        uint64_t after = 0; // the first element after this round
+        if (h + 1 < ROUNDS) {
+#pragma unroll
+            for (int q = 0; q < NV; q++) reinterpret_cast<uint4*>(nx)[q] = __ldg(src + NV * (h + 1) + q);
+            after = elemOf<W>(nx, 0);
+        } else if (t.delta) {
+            after = ldW(t.src + (i0 + 32) * W, W);
+        }
+        V v[R];
+#pragma unroll
+        for (int e = 0; e < R; e++) {
+            uint64_t x = elemOf<W>(u, e);
+            if (t.delta) x = ((e + 1 < R ? elemOf<W>(u, e + 1) : after) - x) & m;
+            if (t.zigzag) x = ((x << 1) ^ (0 - ((x >> (8 * W - 1)) & 1))) & m;
+            v[e] = V(x);
+        }
+        uint64_t const j = i0 + uint64_t(R) * h;
+        if (t.mode == EOUT_PLAIN) {
+            uint32_t o[4 * NV];
+#pragma unroll
+            for (int q = 0; q < 4 * NV; q++) o[q] = 0;
+#pragma unroll
+            for (int e = 0; e < R; e++) {
+                if constexpr (W == 8) {
+                    o[2 * e] = uint32_t(v[e]);
+                    o[2 * e + 1] = uint32_t(uint64_t(v[e]) >> 32);
+                } else {
+                    o[(e * W) >> 2] |= uint32_t(v[e]) << (8 * ((e * W) & 3));
+                }
+            }
+            uint4* const dst = reinterpret_cast<uint4*>(t.out + j * W);
+#pragma unroll
+            for (int q = 0; q < NV; q++) dst[q] = reinterpret_cast<const uint4*>(o)[q];
+        } else if (t.mode == EOUT_PLANES) {
+#pragma unroll
+            for (int b = 0; b < W; b++) {
+                uint32_t wd[R / 4];
+#pragma unroll
+                for (int q = 0; q < R / 4; q++) {
+                    uint32_t x = 0;
+#pragma unroll
+                    for (int c = 0; c < 4; c++) x |= uint32_t((uint64_t(v[4 * q + c]) >> (8 * b)) & 0xffu) << (8 * c);
+                    wd[q] = x;
+                }
+                uint8_t* const p = t.out + b * t.planeStride + j;
+                if constexpr (R == 16) *reinterpret_cast<uint4*>(p) = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+                else *reinterpret_cast<uint2*>(p) = make_uint2(wd[0], wd[1]);
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < R; e++) wp.put(uint64_t(v[e]), t.nbBits);
+        }
+        if (h + 1 < ROUNDS) {
+#pragma unroll
+            for (int q = 0; q < 4 * NV; q++) u[q] = nx[q];
+        }
+    }
+    if (t.mode == EOUT_BITPACK) wp.finish(4 * t.nbBits);
+    return true;
+}
+
 // front end: delta/zigzag then plain, byte planes or bit packing.
 // 128 threads x 32 consecutive elements per tile.
 __global__ void __launch_bounds__(128) kEncNum(const EncNumTask* __restrict__ tasks, const TileRef* __restrict__ tiles)
@@ -120,6 +215,19 @@ __global__ void __launch_bounds__(128) kEncNum(const EncNumTask* __restrict__ ta
     uint64_t const i0 = uint64_t(tr.tile) * kEncTile + uint64_t(threadIdx.x) * 32;
     if (i0 >= t.n) return;
     uint32_t const cnt = uint32_t(min(uint64_t(32), t.n - i0));
+    // full rounds from a 16-byte aligned source (the source holds element
+    // i0 + 32 when delta reads it: n output elements come from n + 1)
+    if (cnt == 32 && !(reinterpret_cast<uintptr_t>(t.src) & 15) && (!t.delta || i0 + 32 <= t.n)) {
+        bool done = false;
+        switch (t.w) {
+            case 1: done = encNumVec<1>(t, i0); break;
+            case 2: done = encNumVec<2>(t, i0); break;
+            case 4: done = encNumVec<4>(t, i0); break;
+            case 8: done = encNumVec<8>(t, i0); break;
+            default: break;
+        }
+        if (done) return;
+    }
     if (t.mode == EOUT_PLAIN) {
         for (uint32_t k = 0; k < cnt; k++) stW(t.out + (i0 + k) * t.w, transformed(t, i0 + k), t.w);
     } else if (t.mode == EOUT_PLANES) {
@@ -211,6 +319,20 @@ struct BitOut {
     __device__ __forceinline__ void add(uint32_t v, uint32_t bits)
     {
         acc |= uint64_t(v & ((1u << bits) - 1u)) << nb;
+        nb += bits;
+        if (nb >= 32) {
+            if (pos + 4 <= cap) *reinterpret_cast<uint32_t*>(out + pos) = uint32_t(acc);
+            pos += 4;
+            acc >>= 32;
+            nb -= 32;
+        }
+    }
+    // appends `bits` <= 32 bits of v (bits above them zero) with one flush
+    // check: used for two fields combined, so that the fields of a step are
+    // computed before any branch
+    __device__ __forceinline__ void add2(uint32_t v, uint32_t bits)
+    {
+        acc |= uint64_t(v) << nb;
         nb += bits;
         if (nb >= 32) {
             if (pos + 4 <= cap) *reinterpret_cast<uint32_t*>(out + pos) = uint32_t(acc);
@@ -394,10 +516,51 @@ __global__ void __launch_bounds__(32 * kHufTabWarps) kHufTables(const HufTableTa
     }
 }
 
+// Sources are read from their end, four symbols per 32-bit word, through a
+// per-lane ring of 16-byte blocks in shared memory filled by cp.async ahead
+// of use (the lanes of a warp read unrelated chunks, so direct byte loads
+// stall the warp on every lane's cache misses).
+constexpr int kEncRing = 8, kEncAhead = 5; // 128 bytes per lane, 80 bytes ahead
+using EncRing = StreamRing<kEncRing, kEncAhead>;
+
+// Reader of the words that hold a source's bytes [q - 4, q), q falling by 4
+// per call; q is a byte position above the 16-byte block of the source's
+// first byte.
+struct BackWords {
+    EncRing r;
+    int32_t k;   // word holding byte q - 4
+    uint32_t sh; // (q - 4) % 4, in bits
+    uint32_t hi; // word k + 1
+    // `src`, `n` > 0 bytes; `ip` the count of bytes not yet read from the top
+    __device__ __forceinline__ void start(const uint8_t* src, uint32_t n, uint32_t ip, uint32_t* ring)
+    {
+        uintptr_t const a = reinterpret_cast<uintptr_t>(src) & ~uintptr_t(15);
+        uint32_t const off = uint32_t(reinterpret_cast<uintptr_t>(src) - a);
+        r.g16 = reinterpret_cast<const uint8_t*>(a);
+        r.ring = ring;
+        r.start(int32_t(off + n) * 8);
+        int32_t const q = int32_t(off + ip);
+        k = (q - 4) >> 2;
+        sh = uint32_t((q - 4) & 3) * 8;
+        hi = sh ? r.word(k + 1) : 0u;
+    }
+    // bytes [q - 4, q) of the source, the lowest in bits 0-7
+    __device__ __forceinline__ uint32_t next()
+    {
+        uint32_t const lo = r.word(k);
+        uint32_t const w = sh ? __funnelshift_r(lo, hi, sh) : lo;
+        hi = lo;
+        k--;
+        return w;
+    }
+};
+
 // FSE: one lane per chunk; the lane's table (2^tableLog next states and the
-// per-symbol transform) lives in shared memory.
+// per-symbol transform) lives in shared memory, then its source ring.
 constexpr uint32_t kFseEncLanes = 16;
-constexpr uint32_t kFseLaneBytes = 2048 * 2 + 256 * 8;
+constexpr uint32_t kFseLaneTables = 2048 * 2 + 256 * 8;
+constexpr uint32_t kFseLaneBytes = kFseLaneTables + 16 * kEncRing;
+static_assert(kFseLaneTables % 16 == 0 && kFseLaneBytes % 16 == 0, "16-byte aligned rings");
 
 __global__ void __launch_bounds__(32) kFseEnc(const FseEncTask* __restrict__ tasks, uint32_t nbTasks,
                                               uint32_t* __restrict__ sizes)
@@ -436,20 +599,49 @@ __global__ void __launch_bounds__(32) kFseEnc(const FseEncTask* __restrict__ tas
     uint32_t s = ns - (n % ns);
     for (uint32_t k = 0; k < ns; k++) v[(s++) % ns] = initState(t.src[--ip]);
     for (uint32_t k = 0; k < n % ns; k++) encode(v[(s++) % ns], t.src[--ip]);
-    if (ns == 4) {
-        while (ip > 0) {
-            encode(v[0], t.src[ip - 1]);
-            encode(v[1], t.src[ip - 2]);
-            encode(v[2], t.src[ip - 3]);
-            encode(v[3], t.src[ip - 4]);
-            ip -= 4;
+    // ip is a multiple of nbStates now: four symbols per word, states in
+    // turn. One transition of state x for symbol y: nbOut = (x + dnb[y]) >>
+    // 16, its field is the low nbOut bits of x, its next state st[(x >>
+    // nbOut) + dfs[y]]. The fields of two transitions are joined (at most
+    // 2 x 12 bits) and appended with one flush check, after the states of
+    // the step have been computed, so the states' chains overlap.
+    auto step = [&](uint32_t& xa, uint32_t ya, uint32_t& xb, uint32_t yb) {
+        uint32_t const na = (xa + dnb[ya]) >> 16, nb = (xb + dnb[yb]) >> 16;
+        uint32_t const fa = xa & ((1u << na) - 1u), fb = xb & ((1u << nb) - 1u);
+        xa = st[(xa >> na) + dfs[ya]];
+        xb = st[(xb >> nb) + dfs[yb]];
+        bo.add2(fa | (fb << na), na + nb);
+    };
+    if (ip >= 4) {
+        BackWords bw;
+        bw.start(t.src, n, uint32_t(ip), reinterpret_cast<uint32_t*>(base + kFseLaneTables));
+        if (ns == 4) {
+            for (; ip >= 4; ip -= 4) {
+                uint32_t const w = bw.next();
+                uint32_t const y0 = w >> 24, y1 = (w >> 16) & 0xffu, y2 = (w >> 8) & 0xffu, y3 = w & 0xffu;
+                uint32_t const n0 = (v[0] + dnb[y0]) >> 16, n1 = (v[1] + dnb[y1]) >> 16;
+                uint32_t const n2 = (v[2] + dnb[y2]) >> 16, n3 = (v[3] + dnb[y3]) >> 16;
+                uint32_t const f01 = (v[0] & ((1u << n0) - 1u)) | ((v[1] & ((1u << n1) - 1u)) << n0);
+                uint32_t const f23 = (v[2] & ((1u << n2) - 1u)) | ((v[3] & ((1u << n3) - 1u)) << n2);
+                v[0] = st[(v[0] >> n0) + dfs[y0]];
+                v[1] = st[(v[1] >> n1) + dfs[y1]];
+                v[2] = st[(v[2] >> n2) + dfs[y2]];
+                v[3] = st[(v[3] >> n3) + dfs[y3]];
+                bo.add2(f01, n0 + n1);
+                bo.add2(f23, n2 + n3);
+            }
+        } else {
+            for (; ip >= 4; ip -= 4) {
+                uint32_t const w = bw.next();
+                step(v[0], w >> 24, v[1], (w >> 16) & 0xffu);
+                step(v[0], (w >> 8) & 0xffu, v[1], w & 0xffu);
+            }
         }
-    } else {
-        while (ip > 0) {
-            encode(v[0], t.src[ip - 1]);
-            encode(v[1], t.src[ip - 2]);
-            ip -= 2;
-        }
+        asm volatile("cp.async.wait_all;" ::: "memory"); // no copy outlives the lane
+    }
+    for (; ip > 0; ip -= 2) { // two states: the last pair
+        encode(v[0], t.src[ip - 1]);
+        encode(v[1], t.src[ip - 2]);
     }
     for (uint32_t k = 0; k < ns; k++) bo.add(v[k], t.tableLog);
     sizes[t.sizeSlot] = bo.close();
@@ -467,6 +659,7 @@ __global__ void __launch_bounds__(32) kHufEnc(const HufEncTask* __restrict__ tas
 {
     __shared__ uint16_t val[kHufEncChunks][256];
     __shared__ uint8_t nbb[kHufEncChunks][256];
+    __shared__ __align__(16) uint32_t rings[4 * kHufEncChunks][4 * kEncRing];
     uint32_t const c = threadIdx.x >> 2, k = threadIdx.x & 3;
     uint32_t const ti = blockIdx.x * kHufEncChunks + c;
     bool const active = ti < nbTasks;
@@ -496,7 +689,23 @@ __global__ void __launch_bounds__(32) kHufEnc(const HufEncTask* __restrict__ tas
     }
     BitOut bo(out, t.x4 ? hufStreamCap((t.n + 3) / 4) : t.n + t.n / 8 + 64);
     const uint8_t* const src = t.src + start;
-    for (uint32_t i = len; i > 0; i--) {
+    uint32_t i = len;
+    if (i >= 4) {
+        BackWords bw;
+        bw.start(src, len, len, rings[threadIdx.x]);
+        for (; i >= 4; i -= 4) {
+            // codes of at most 11 bits (the table's values hold no bits above
+            // their length): two joined per append
+            uint32_t const w = bw.next();
+            uint32_t const s3 = w >> 24, s2 = (w >> 16) & 0xffu, s1 = (w >> 8) & 0xffu, s0 = w & 0xffu;
+            uint32_t const b3 = nbb[c][s3], b2 = nbb[c][s2], b1 = nbb[c][s1], b0 = nbb[c][s0];
+            uint32_t const c3 = val[c][s3], c2 = val[c][s2], c1 = val[c][s1], c0 = val[c][s0];
+            bo.add2(c3 | (c2 << b3), b3 + b2);
+            bo.add2(c1 | (c0 << b1), b1 + b0);
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory"); // no copy outlives the lane
+    }
+    for (; i > 0; i--) {
         uint32_t const s = src[i - 1];
         bo.add(val[c][s], nbb[c][s]);
     }
