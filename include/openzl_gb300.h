@@ -441,6 +441,12 @@ ZL_Report ozl_gpu_compress_batch(OZL_GpuEncoder* e, size_t nbFrames, const void*
                                  int checksums, void* stream);
 /* Message describing the encoder's last error ("" when none). */
 const char* ozl_gpu_encoder_error(const OZL_GpuEncoder* e);
+/* Batches of 64 MiB or more are encoded in `parts` (1..16, default 8) runs of
+ * contiguous frames of about equal bytes, each on its own host thread and
+ * CUDA stream, so that one part's host work overlaps another's kernels; each
+ * part's parallel host phases use its share of the cores (-parts: all of
+ * them). The frames do not depend on it. */
+ZL_Report ozl_gpu_encoder_setParts(OZL_GpuEncoder* e, int parts);
 /* Wall-clock milliseconds of the last ozl_gpu_compress_batch's phases, in
  * order: front end (GPU), graph discovery (host), histograms (GPU), codec
  * decisions and coding tables, entropy bitstreams (GPU), graph replay

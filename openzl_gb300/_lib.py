@@ -81,6 +81,7 @@ def library():
         "ozl_gpu_compress_batch": ([vp, sz, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, vp], ZLReport),
         "ozl_gpu_encoder_error": ([vp], ctypes.c_char_p),
         "ozl_gpu_encoder_phases": ([vp, vp, sz], ZLReport),
+        "ozl_gpu_encoder_setParts": ([vp, ctypes.c_int], ZLReport),
         "ZL_DCtx_decompressTyped": ([vp, ctypes.POINTER(OutputInfo), vp, sz, vp, sz], ZLReport),
         "ZL_TypedBuffer_create": ([], vp),
         "ZL_TypedBuffer_free": ([vp], None),
@@ -433,6 +434,12 @@ class GpuEncoder:
         if rep.code:
             raise ZLError(rep.code, self._lib.ozl_gpu_encoder_error(self._h).decode())
         return [fs[i] for i in range(n)]
+
+    def set_parts(self, parts):
+        """Batches of 64 MiB or more run as `parts` (1..16) concurrent runs."""
+        rep = self._lib.ozl_gpu_encoder_setParts(self._h, int(parts))
+        if rep.code:
+            raise ZLError(rep.code, "ozl_gpu_encoder_setParts failed")
 
     PHASES = ("front_end", "discovery", "histograms", "decisions", "bitstreams", "replay", "assembly")
 

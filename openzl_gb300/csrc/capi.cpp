@@ -5,6 +5,7 @@
 // the device-resident additions. No exception crosses this boundary.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -52,16 +53,18 @@ struct ZL_DCtx_s {
     }
 };
 
-// A large batch is encoded as two halves of about equal bytes, each by its
-// own engine on its own host thread and stream, so that one half's host
-// phases (graph discovery, codec decisions, replay) run while the other
-// half's kernels do. Frames are independent; each half's frames are the
-// bytes a whole-batch call would write.
+// A large batch is encoded in parts of about equal bytes, each by its own
+// engine on its own host thread and stream, so that one part's host phases
+// (graph discovery, codec decisions, replay) run while another part's
+// kernels do. Frames are independent; each part's frames are the bytes a
+// whole-batch call would write.
 struct OZL_GpuEncoder_s {
-    static constexpr int kHalves = 2;
+    static constexpr int kMaxParts = 16;
     static constexpr uint64_t kSplitBytes = 64ull << 20; // smaller batches: one engine, the caller's stream
-    ozl::EncodeBatch batch[kHalves];
-    cudaStream_t streams[kHalves] = {};
+    int parts = 8;
+    bool shareCores = true; // each part's host phases on its share of the cores
+    ozl::EncodeBatch batch[kMaxParts];
+    cudaStream_t streams[kMaxParts] = {};
     cudaEvent_t ready = nullptr;
     double phaseMs[ozl::EncodeBatch::kPhases] = {};
     std::string err;
@@ -124,6 +127,15 @@ size_t ozl_gpu_compress_bound(size_t srcBytes) { return ozl::encodeBound(srcByte
 
 const char* ozl_gpu_encoder_error(const OZL_GpuEncoder* e) { return e ? e->err.c_str() : ""; }
 
+ZL_Report ozl_gpu_encoder_setParts(OZL_GpuEncoder* e, int parts)
+{
+    int const k = parts < 0 ? -parts : parts;
+    if (!e || k < 1 || k > OZL_GpuEncoder_s::kMaxParts) return fail(ZL_ErrorCode_parameter_invalid);
+    e->parts = k;
+    e->shareCores = parts > 0;
+    return ok(0);
+}
+
 ZL_Report ozl_gpu_encoder_phases(const OZL_GpuEncoder* e, float* ms, size_t capacity)
 {
     if (!e || (capacity && !ms)) return fail(ZL_ErrorCode_parameter_invalid);
@@ -156,40 +168,54 @@ ZL_Report ozl_gpu_compress_batch(OZL_GpuEncoder* e, size_t n, const void* const*
         if (rc) return fail(rc);
         for (int i = 0; i < ozl::EncodeBatch::kPhases; i++) e->phaseMs[i] = e->batch[0].lastPhaseMs()[i];
     } else {
-        // halves of about equal bytes; both streams wait for the caller's
-        // work on `stream` (the inputs), and both halves synchronize theirs
-        size_t cut = 1;
-        uint64_t acc = specs[0].n * specs[0].w;
-        while (cut + 1 < n && 2 * acc < bytes) {
-            acc += specs[cut].n * specs[cut].w;
-            cut++;
+        // parts of about equal bytes; every part's stream waits for the
+        // caller's work on `stream` (the inputs), and every part synchronizes
+        // its own
+        int const np = int(std::min<size_t>(size_t(e->parts), n));
+        std::vector<size_t> cut{ 0 };
+        uint64_t acc = 0;
+        for (size_t i = 0; i < n && int(cut.size()) < np; i++) {
+            acc += specs[i].n * specs[i].w;
+            if (acc * uint64_t(np) >= bytes * uint64_t(cut.size()) && i + 1 < n) cut.push_back(i + 1);
         }
+        cut.push_back(n);
+        int const parts = int(cut.size()) - 1;
         bool okSetup = (e->ready || cudaEventCreateWithFlags(&e->ready, cudaEventDisableTiming) == cudaSuccess);
-        for (cudaStream_t& x : e->streams)
-            okSetup = okSetup && (x || cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) == cudaSuccess);
+        for (int p = 0; p < parts; p++)
+            okSetup = okSetup && (e->streams[p] || cudaStreamCreateWithFlags(&e->streams[p], cudaStreamNonBlocking) == cudaSuccess);
         okSetup = okSetup && cudaEventRecord(e->ready, us) == cudaSuccess;
-        for (cudaStream_t x : e->streams) okSetup = okSetup && cudaStreamWaitEvent(x, e->ready, 0) == cudaSuccess;
+        for (int p = 0; p < parts; p++) okSetup = okSetup && cudaStreamWaitEvent(e->streams[p], e->ready, 0) == cudaSuccess;
         if (!okSetup) {
             e->err = "encoder streams could not be set up";
             return fail(ZL_ErrorCode_GENERIC);
         }
-        std::vector<ozl::EncFrameSpec> const lo(specs.begin(), specs.begin() + cut), hi(specs.begin() + cut, specs.end());
-        std::vector<size_t> sizesHi;
-        std::string errHi;
-        int rcHi = 0;
-        std::thread other([&] {
-            rcHi = e->batch[1].compress(hi, outs + cut, caps + cut, checksums != 0, e->streams[1], sizesHi, errHi);
-        });
-        rc = e->batch[0].compress(lo, outs, caps, checksums != 0, e->streams[0], sizes, e->err);
-        other.join();
-        if (!rc && rcHi) {
-            rc = rcHi;
-            e->err = errHi;
-        }
+        std::vector<std::vector<size_t>> partSizes(parts);
+        std::vector<std::string> partErr(parts);
+        std::vector<int> partRc(parts, 0);
+        unsigned const hw = std::thread::hardware_concurrency();
+        unsigned const share = std::max(2u, (hw ? hw : 16u) / unsigned(parts)); // host threads per part
+        auto runPart = [&](int p) {
+            std::vector<ozl::EncFrameSpec> const sub(specs.begin() + cut[p], specs.begin() + cut[p + 1]);
+            e->batch[p].setHostThreads(e->shareCores ? share : 0);
+            partRc[p] = e->batch[p].compress(sub, outs + cut[p], caps + cut[p], checksums != 0, e->streams[p],
+                                             partSizes[p], partErr[p]);
+        };
+        std::vector<std::thread> others;
+        for (int p = 1; p < parts; p++) others.emplace_back(runPart, p);
+        runPart(0);
+        for (std::thread& th : others) th.join();
+        for (int p = 0; p < parts && !rc; p++)
+            if (partRc[p]) {
+                rc = partRc[p];
+                e->err = partErr[p];
+            }
         if (rc) return fail(rc);
-        sizes.insert(sizes.end(), sizesHi.begin(), sizesHi.end());
-        for (int i = 0; i < ozl::EncodeBatch::kPhases; i++)
-            e->phaseMs[i] = std::max(e->batch[0].lastPhaseMs()[i], e->batch[1].lastPhaseMs()[i]);
+        for (int i = 0; i < ozl::EncodeBatch::kPhases; i++) e->phaseMs[i] = 0;
+        for (int p = 0; p < parts; p++) {
+            sizes.insert(sizes.end(), partSizes[p].begin(), partSizes[p].end());
+            for (int i = 0; i < ozl::EncodeBatch::kPhases; i++)
+                e->phaseMs[i] = std::max(e->phaseMs[i], e->batch[p].lastPhaseMs()[i]);
+        }
     }
     size_t total = 0;
     for (size_t i = 0; i < n; i++) {

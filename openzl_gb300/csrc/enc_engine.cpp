@@ -220,12 +220,15 @@ struct PinnedBuf {
     }
 };
 
+// host threads of the calling compress() (0: the machine's, at most 16)
+thread_local unsigned tlHostThreads = 0;
+
 // fn(i) for i < n on up to 16 host threads (chunks of 64 indices)
 template <class F>
 void parallelFor(size_t n, F fn)
 {
     unsigned const hw = std::thread::hardware_concurrency();
-    unsigned const nt = std::min(16u, hw ? hw : 1u);
+    unsigned const nt = std::min(tlHostThreads ? tlHostThreads : 16u, hw ? hw : 1u);
     if (n < 256 || nt < 2) {
         for (size_t i = 0; i < n; i++) fn(i);
         return;
@@ -787,6 +790,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
     size_t const nf = frames.size();
     sizes.assign(nf, 0);
     std::vector<Front> fronts(nf);
+    tlHostThreads = hostThreads_;
     for (double& m : phaseMs_) m = 0;
     auto clock0 = std::chrono::steady_clock::now();
     int phase = 0;

@@ -53,6 +53,8 @@ class EncodeBatch {
     // phase that ends in a stream synchronize includes its device work).
     static constexpr int kPhases = 7;
     const double* lastPhaseMs() const { return phaseMs_; }
+    // host threads of the parallel host phases (0: the machine's, at most 16)
+    void setHostThreads(unsigned n) { hostThreads_ = n; }
 
     struct Impl;
 
@@ -60,6 +62,7 @@ class EncodeBatch {
     Impl* impl_;
     size_t launches_ = 0;
     double phaseMs_[kPhases] = {};
+    unsigned hostThreads_ = 0;
 };
 
 // Worst-case frame size for `srcBytes` of input (ZL_compressBound-style).
