@@ -113,6 +113,10 @@ typedef enum {
      * launches share its rank (critical part first, then each kind's runs in
      * order); 1: every element-wise launch ahead of all entropy decoding. */
     OZL_DParam_schedule = 1003,
+    /* batch API only: rounds of contiguous frames of about equal decoded
+     * bytes in ozl_gpu_batch_run_host (1..16, default 12); each round's
+     * outputs go down as soon as it is decoded. */
+    OZL_DParam_hostRounds = 1004,
 } ZL_DParam;
 
 typedef enum {

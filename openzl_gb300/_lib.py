@@ -187,6 +187,7 @@ DPARAM_PARTS_PER_KIND = 1000  # OZL_DParam_partsPerKind
 DPARAM_FSE_KERNEL = 1001  # OZL_DParam_fseKernel
 DPARAM_CRITICAL_SYMBOLS = 1002  # OZL_DParam_criticalSymbols
 DPARAM_SCHEDULE = 1003  # OZL_DParam_schedule
+DPARAM_HOST_ROUNDS = 1004  # OZL_DParam_hostRounds
 
 
 class DCtx:
@@ -305,7 +306,7 @@ class GpuBatch:
     """Batched decode of many frames: one plan, one CUDA graph per run."""
 
     def __init__(self, check_content=True, check_compressed=True, parts_per_kind=None, fse_kernel=None,
-                 critical_symbols=None, schedule=None):
+                 critical_symbols=None, schedule=None, host_rounds=None):
         self._lib = library()
         self._h = self._lib.ozl_gpu_batch_create()
         if parts_per_kind is not None:
@@ -316,6 +317,8 @@ class GpuBatch:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_CRITICAL_SYMBOLS, int(critical_symbols)))
         if schedule is not None:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_SCHEDULE, int(schedule)))
+        if host_rounds is not None:
+            _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_HOST_ROUNDS, int(host_rounds)))
         if not check_content:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_CHECK_CONTENT, 2))
         if not check_compressed:

@@ -457,6 +457,11 @@ ZL_Report ozl_gpu_batch_setParameter(OZL_GpuBatch* b, ZL_DParam param, int value
             if (value < 0 || value > 1) return fail(ZL_ErrorCode_parameter_invalid);
             b->schedule = value;
             break;
+        case OZL_DParam_hostRounds:
+            if (value < 1 || value > ozl::DecodeBatch::HostPipe::kRounds) return fail(ZL_ErrorCode_parameter_invalid);
+            b->hostRounds = value;
+            b->host.reset();
+            break;
         default: return fail(ZL_ErrorCode_parameter_invalid);
     }
     return ok(0);

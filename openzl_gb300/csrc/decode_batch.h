@@ -99,8 +99,9 @@ struct DecodeBatch {
     // stream, the round decodes on its own stream as soon as they are in
     // (rounds share the SMs), and its outputs go down on a second copy stream
     // as soon as it is done, so both copy directions overlap the decode.
+    int hostRounds = 12;     // OZL_DParam_hostRounds
     struct HostPipe {
-        static constexpr int kRounds = 8;
+        static constexpr int kRounds = 16;
         std::vector<Part> rounds;
         std::vector<size_t> inOff, outOff; // round boundaries in the input / output images
         bool ready = false, uploaded = false;
@@ -543,7 +544,7 @@ struct DecodeBatch {
             if (i && (dFrames[i] < dFrames[i - 1] || dOuts[i] < dOuts[i - 1] + sizes[i - 1])) return false;
         }
         if (host.ready) return true;
-        int const K = int(std::min<size_t>(HostPipe::kRounds, n));
+        int const K = int(std::min<size_t>(size_t(hostRounds), n));
         uint64_t const target = (plan.totalOut + K - 1) / K;
         std::vector<size_t> first{ 0 };
         uint64_t acc = 0;
