@@ -71,6 +71,7 @@ def parse_args():
     p.add_argument("--serve-rates", default="1000,2000,5000,10000,20000,50000",
                    help="request rates (req/s) for the serving run")
     p.add_argument("--serve-seconds", type=float, default=1.0, help="seconds of arrivals per rate")
+    p.add_argument("--serve-workers", type=int, default=4, help="serving loop worker threads (one stream each)")
     p.add_argument("--serve-requests", type=int, default=0,
                    help="requests per rate (0: --serve-seconds of arrivals per rate)")
     p.add_argument("--no-parity", action="store_true", help="skip the encode-parity check against the oracle")
@@ -679,7 +680,7 @@ def run_serving(oz, torch, dev, sptr, args):
     outs_d = [[pinned(p[0].nbytes) for _ in range(slots)] for p in pool]
     outs_c = [[pinned(caps[i]) for _ in range(slots)] for i in range(len(pool))]
     rng = np.random.default_rng(args.seed + 5)
-    srv = oz.Server(hbm_budget=40 << 30, workers=4, checksums=True)
+    srv = oz.Server(hbm_budget=40 << 30, workers=args.serve_workers, checksums=True)
     results = []
     rates = [int(r) for r in args.serve_rates.split(",") if r]
     for rate in rates:
@@ -688,6 +689,7 @@ def run_serving(oz, torch, dev, sptr, args):
         kinds = rng.random(nreq) < 0.8
         which = rng.integers(0, len(pool), nreq)
         lat, nbytes, done = [], 0, 0
+        st0 = srv.stats()
         t0 = time.perf_counter()
         due = t0
         last_poll = t0
@@ -718,9 +720,11 @@ def run_serving(oz, torch, dev, sptr, args):
                 done += 1
         wall = time.perf_counter() - t0
         lat = np.sort(np.array(lat)) / 1e3
+        st1 = srv.stats()
         results.append({"rate": rate, "requests": nreq, "p50_ms": round(float(np.percentile(lat, 50)), 3),
                         "p99_ms": round(float(np.percentile(lat, 99)), 3), "gbs": round(nbytes / wall / 1e9, 2),
-                        "offered_gbs": round(nbytes / (gaps.sum()) / 1e9, 2)})
+                        "offered_gbs": round(nbytes / (gaps.sum()) / 1e9, 2),
+                        "workers_s": {k: round(st1[k] - st0[k], 4) for k in st1}, "wall_s": round(wall, 4)})
     srv.close()
     # plain per-request path: the same kind of requests one call at a time
     # through the reference-style API (ZL_DCtx_decompressTyped /
@@ -756,7 +760,7 @@ def run_serving(oz, torch, dev, sptr, args):
             comps[r][1].compress_numeric(src_p[i].view({1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[w]))
         nbytes += pool[i][0].nbytes
     plain_gbs = nbytes / (time.perf_counter() - t0) / 1e9
-    return {"workers": 4, "hbm_budget_gb": 40, "mix": "80% decompress / 20% compress",
+    return {"workers": args.serve_workers, "hbm_budget_gb": 40, "mix": "80% decompress / 20% compress",
             "payload": "log-normal, median 256 KiB, sigma 1.5, clipped 1 KiB..64 MiB", "pool": len(pool),
             "host_buffers": "pinned", "rates": results, "plain_per_request_gbs": round(plain_gbs, 3)}
 

@@ -517,6 +517,13 @@ uint64_t ozl_server_submit_compress(OZL_Server* server, const void* src, size_t 
  * Waits up to waitMs for a first completion. Returns the count. */
 size_t ozl_server_poll(OZL_Server* server, uint64_t* ids, ZL_Report* results, double* latencyUs, size_t max,
                        int waitMs);
+/* Cumulative worker statistics since the server was created, summed over
+ * its workers: decode batches, decode requests, seconds planning decode
+ * batches on the host, seconds running them (launch to completion, copies
+ * out included), encode batches, encode requests, seconds encoding, and
+ * seconds workers waited for a request or for free memory. Writes
+ * out[i] for i < capacity; returns the number of values (8). */
+size_t ozl_server_stats(OZL_Server* server, double* out, size_t capacity);
 /* Requests submitted and not yet returned by ozl_server_poll. */
 size_t ozl_server_in_flight(OZL_Server* server);
 

@@ -619,6 +619,7 @@ class Server:
                 ("ozl_server_poll", [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ZLReport),
                                      ctypes.POINTER(ctypes.c_double), sz, ctypes.c_int], sz),
                 ("ozl_server_in_flight", [vp], sz),
+                ("ozl_server_stats", [vp, ctypes.POINTER(ctypes.c_double), sz], sz),
             ]:
                 f = getattr(L, name)
                 f.argtypes = args
@@ -667,6 +668,15 @@ class Server:
 
     def in_flight(self):
         return self._lib.ozl_server_in_flight(self._h)
+
+    STATS = ("decode_batches", "decode_requests", "decode_plan_s", "decode_run_s", "encode_batches",
+             "encode_requests", "encode_s", "wait_s")
+
+    def stats(self):
+        """Cumulative worker statistics (ozl_server_stats), by name."""
+        v = (ctypes.c_double * len(self.STATS))()
+        k = self._lib.ozl_server_stats(self._h, v, len(self.STATS))
+        return {name: round(v[i], 4) for i, name in enumerate(self.STATS[:k])}
 
     def close(self):
         if self._h:

@@ -23,6 +23,25 @@ inline ZL_Report reportFail(int code) { return ZL_Report{ ZL_ErrorCode(code), 0 
 struct DevBuf {
     uint8_t* p = nullptr;
     size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), cap(o.cap)
+    {
+        o.p = nullptr;
+        o.cap = 0;
+    }
+    DevBuf& operator=(DevBuf&& o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p;
+            cap = o.cap;
+            o.p = nullptr;
+            o.cap = 0;
+        }
+        return *this;
+    }
     ~DevBuf() { release(); }
     void release()
     {
@@ -117,10 +136,9 @@ struct DecodeBatch {
             if (graph) cudaGraphExecDestroy(graph);
             graph = nullptr;
         }
-        void reset()
+        void reset() // keeps the rounds' device buffers for the next plan
         {
             dropGraph();
-            rounds.clear();
             ready = uploaded = false;
         }
         ~HostPipe()
@@ -140,6 +158,7 @@ struct DecodeBatch {
 
     ~DecodeBatch()
     {
+        if (lastRun) cudaEventDestroy(lastRun);
         dropGraph();
         for (auto& kv : slots) cudaStreamDestroy(kv.second.first);
         for (cudaEvent_t e : events) cudaEventDestroy(e);
@@ -199,11 +218,15 @@ struct DecodeBatch {
                 if (!nd.dead && nd.id == 49 && nd.frame >= 0 && nd.out >= 0
                     && plan.streams[size_t(nd.out)].n >= critical)
                     kindOf[size_t(nd.frame)] = 2;
-        parts.clear();
-        if (!splitParts) {
-            parts.resize(1);
-            parts[0].mask.assign(n, 1);
-        } else {
+        // the parts' device buffers outlive the plan: a new plan reuses them
+        // (no allocation, and so no device-wide synchronization, per batch)
+        struct Spec {
+            std::vector<char> mask;
+            bool critical;
+            int run;
+        };
+        std::vector<Spec> specs;
+        if (splitParts) {
             for (char kind : { char(2), char(1), char(0) }) {
                 std::vector<size_t> fr;
                 uint64_t total = 0;
@@ -214,29 +237,28 @@ struct DecodeBatch {
                     }
                 if (fr.empty()) continue;
                 size_t const g = kind == 2 ? 1 : std::min<size_t>(size_t(runs), fr.size());
-                size_t const first = parts.size();
-                parts.resize(first + g);
-                for (size_t k = 0; k < g; k++) {
-                    parts[first + k].mask.assign(n, 0);
-                    parts[first + k].critical = kind == 2;
-                    parts[first + k].run = int(k);
-                }
+                size_t const first = specs.size();
+                for (size_t k = 0; k < g; k++) specs.push_back(Spec{ std::vector<char>(n, 0), kind == 2, int(k) });
                 uint64_t acc = 0;
                 size_t k = 0;
                 for (size_t i : fr) {
                     while (k + 1 < g && acc >= total * (k + 1) / g) k++;
-                    parts[first + k].mask[i] = 1;
+                    specs[first + k].mask[i] = 1;
                     acc += sizes[i];
                 }
             }
-            if (parts.empty()) {
-                parts.resize(1);
-                parts[0].mask.assign(n, 1);
-            }
         }
-        if (parts.size() > size_t(kMaxParts)) {
+        if (specs.empty()) specs.push_back(Spec{ std::vector<char>(n, 1), false, 0 });
+        if (specs.size() > size_t(kMaxParts)) {
             err = "too many parts";
             return reportFail(ZL_ErrorCode_parameter_invalid);
+        }
+        parts.resize(specs.size());
+        for (size_t p = 0; p < specs.size(); p++) {
+            parts[p].mask = std::move(specs[p].mask);
+            parts[p].critical = specs[p].critical;
+            parts[p].run = specs[p].run;
+            parts[p].layout = DeviceLayout();
         }
         if (!arena.reserve(plan.arenaBytes) || !params.reserve(plan.params.size()) || !status.reserve(64)) {
             err = "device allocation failed";
@@ -263,9 +285,23 @@ struct DecodeBatch {
 
     // Copies the plan's descriptors and parameters to the device, ordered on
     // the stream that runs the plan (the kernels read them).
+    // The last run's end on its stream: a new plan's uploads (descriptors,
+    // parameters) wait for it, since the buffers are reused across plans and
+    // that run may be on another stream.
+    cudaEvent_t lastRun = nullptr;
+    void markRun(cudaStream_t s)
+    {
+        if (lastRun || cudaEventCreateWithFlags(&lastRun, cudaEventDisableTiming) == cudaSuccess) cudaEventRecord(lastRun, s);
+    }
+    void afterLastRun(cudaStream_t s)
+    {
+        if (lastRun) cudaStreamWaitEvent(s, lastRun, 0);
+    }
+
     ZL_Report upload(cudaStream_t s)
     {
         if (uploaded) return reportOk(0);
+        afterLastRun(s);
         for (Part& p : parts)
             if (!p.layout.pool.empty()
                 && cudaMemcpyAsync(p.pool.data(), p.layout.pool.data(), p.layout.pool.size(), cudaMemcpyHostToDevice, s)
@@ -448,7 +484,11 @@ struct DecodeBatch {
     {
         ZL_Report const u = upload(s);
         if (ZL_isError(u)) return u;
-        if (!useGraph) return enqueue(s);
+        if (!useGraph) {
+            ZL_Report const r = enqueue(s);
+            if (!ZL_isError(r)) markRun(s);
+            return r;
+        }
         if (s == nullptr) {
             err = "CUDA graph capture needs a non-default stream";
             return reportFail(ZL_ErrorCode_parameter_invalid);
@@ -471,6 +511,7 @@ struct DecodeBatch {
             graphStream = s;
         }
         if (cudaGraphLaunch(graph, s) != cudaSuccess) { err = "graph launch failed"; return reportFail(ZL_ErrorCode_GENERIC); }
+        markRun(s);
         return reportOk(0);
     }
 
@@ -554,7 +595,7 @@ struct DecodeBatch {
         }
         first.push_back(n);
         size_t const nr = first.size() - 1;
-        host.rounds.assign(nr, Part{});
+        host.rounds.resize(nr);
         host.inOff.assign(nr + 1, 0);
         host.outOff.assign(nr + 1, 0);
         for (size_t r = 0; r < nr; r++) {
@@ -657,6 +698,7 @@ struct DecodeBatch {
         ZL_Report u = upload(s);
         if (ZL_isError(u)) return u;
         if (!host.uploaded) {
+            afterLastRun(s);
             for (Part& p : host.rounds) {
                 if (p.layout.pool.empty()) continue;
                 cudaError_t const e = cudaMemcpyAsync(p.pool.data(), p.layout.pool.data(), p.layout.pool.size(),
@@ -671,6 +713,7 @@ struct DecodeBatch {
         if (!useGraph) {
             ZL_Report r = enqueueHost(hIn, hOut, s);
             if (ZL_isError(r)) return r;
+            markRun(s);
             return check(s);
         }
         if (s == nullptr) {
@@ -699,6 +742,7 @@ struct DecodeBatch {
             host.gStream = s;
         }
         if (cudaGraphLaunch(host.graph, s) != cudaSuccess) { err = "graph launch failed"; return reportFail(ZL_ErrorCode_GENERIC); }
+        markRun(s);
         return check(s);
     }
 

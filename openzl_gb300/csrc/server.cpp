@@ -18,6 +18,7 @@
 // does not depend on the batch it ran in.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -119,6 +120,15 @@ struct OZL_Server_s {
     uint64_t nextId = 1;
     bool stop = false;
     size_t inFlight = 0;
+    // cumulative per-stage times of the workers (ozl_server_stats), under mu
+    enum { ST_DEC_BATCHES, ST_DEC_REQS, ST_DEC_PLAN, ST_DEC_RUN, ST_ENC_BATCHES, ST_ENC_REQS, ST_ENC_RUN, ST_WAIT,
+           ST_COUNT };
+    double stats[ST_COUNT] = {};
+    void addStat(int k, double v)
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        stats[k] += v;
+    }
 
     void worker();
     void runDecode(std::vector<Request*>& batch, ozl::DecodeBatch& dec, uint8_t* arena, cudaStream_t s);
@@ -149,10 +159,14 @@ void OZL_Server_s::worker()
     ozl::DecodeBatch dec;
     ozl::EncodeBatch enc;
     dec.checkContent = dec.checkCompressed = checksums != 0;
+    // the encoder's parallel host phases on this worker's share of the cores
+    unsigned const hw = std::thread::hardware_concurrency();
+    enc.setHostThreads(std::max(2u, (hw ? hw : 16u) / unsigned(nbWorkers)));
     auto need = [](const Request* r) { return alignUp(r->inBytes) + alignUp(r->outBytes); };
     for (;;) {
         std::vector<Request*> batch;
         size_t off = 0, bytes = 0;
+        Clock::time_point const tIdle = Clock::now();
         {
             std::unique_lock<std::mutex> lk(mu);
             // the oldest request is admitted when a block of its size is free
@@ -188,6 +202,7 @@ void OZL_Server_s::worker()
             }
             blocks.take(bytes, off); // fits: bytes <= the largest free block
             if (!pending.empty()) cvWork.notify_one(); // another worker may admit the rest
+            stats[ST_WAIT] += std::chrono::duration<double>(Clock::now() - tIdle).count();
         }
         if (!pool.data() || !s) {
             for (Request* r : batch) r->result = ozl::reportFail(ZL_ErrorCode_allocation);
@@ -224,9 +239,18 @@ void OZL_Server_s::runDecode(std::vector<Request*>& batch, ozl::DecodeBatch& dec
         pos += alignUp(r->outBytes);
         cudaMemcpyAsync(const_cast<void*>(dF[i]), r->in, r->inBytes, cudaMemcpyHostToDevice, s);
     }
+    Clock::time_point const t0 = Clock::now();
     ZL_Report rep = dec.makePlan(n, hF.data(), fs.data(), dF.data(), dO.data(), caps.data());
+    Clock::time_point const t1 = Clock::now();
     if (!ZL_isError(rep)) rep = dec.run(s, false);
     if (!ZL_isError(rep)) rep = dec.check(s);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        stats[ST_DEC_BATCHES] += 1;
+        stats[ST_DEC_REQS] += double(n);
+        stats[ST_DEC_PLAN] += std::chrono::duration<double>(t1 - t0).count();
+        stats[ST_DEC_RUN] += std::chrono::duration<double>(Clock::now() - t1).count();
+    }
     if (ZL_isError(rep) && n > 1) {
         // attribute the error: each frame alone
         for (size_t i = 0; i < n; i++) {
@@ -265,7 +289,14 @@ void OZL_Server_s::runEncode(std::vector<Request*>& batch, ozl::EncodeBatch& enc
     }
     std::vector<size_t> sizes;
     std::string err;
+    Clock::time_point const t0 = Clock::now();
     int rc = enc.compress(specs, dOut.data(), caps.data(), checksums != 0, s, sizes, err);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        stats[ST_ENC_BATCHES] += 1;
+        stats[ST_ENC_REQS] += double(n);
+        stats[ST_ENC_RUN] += std::chrono::duration<double>(Clock::now() - t0).count();
+    }
     if (rc && n > 1) {
         for (size_t i = 0; i < n; i++) {
             std::vector<Request*> one{ batch[i] };
@@ -285,6 +316,14 @@ void OZL_Server_s::runEncode(std::vector<Request*>& batch, ozl::EncodeBatch& enc
 }
 
 extern "C" {
+
+size_t ozl_server_stats(OZL_Server* srv, double* out, size_t capacity)
+{
+    if (!srv) return 0;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    for (size_t i = 0; i < capacity && i < size_t(OZL_Server_s::ST_COUNT); i++) out[i] = srv->stats[i];
+    return size_t(OZL_Server_s::ST_COUNT);
+}
 
 OZL_Server* ozl_server_create(size_t hbmBudget, int nbWorkers, int checksums)
 {
