@@ -7,6 +7,7 @@
 #include <mutex>
 #include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/openzl_gb300.h"
@@ -264,20 +265,46 @@ struct DecodeBatch {
             err = "device allocation failed";
             return reportFail(ZL_ErrorCode_allocation);
         }
-        for (Part& p : parts) {
-            // size pass, allocate, then the real layout
+        // Each part's layout: one pass into the part's buffers when they are
+        // large enough (they outlive plans), else a size pass, a larger
+        // allocation and the real pass. Parts only read the plan, so large
+        // batches lay them out on parallel host threads.
+        std::vector<int> prc(parts.size(), 0);
+        std::vector<std::string> perr(parts.size());
+        auto layoutPart = [&](size_t k) {
+            Part& p = parts[k];
             const std::vector<char>* mask = parts.size() > 1 ? &p.mask : nullptr;
-            rc = layoutPlan(plan, dFrames.data(), dOuts.data(), nullptr, nullptr, nullptr, nullptr, p.layout, err, mask);
-            if (rc) return reportFail(rc);
-            if (!p.pool.reserve(p.layout.pool.size()) || !p.scratch.reserve(p.layout.scratchBytes)) {
-                err = "device allocation failed";
-                return reportFail(ZL_ErrorCode_allocation);
+            if (p.pool.data() && p.scratch.data()) {
+                prc[k] = layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), p.scratch.data(),
+                                    p.pool.data(), p.layout, perr[k], mask);
+                if (prc[k] || (p.layout.pool.size() + 256 <= p.pool.cap && p.layout.scratchBytes + 256 <= p.scratch.cap))
+                    return;
             }
-            rc = layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), p.scratch.data(),
-                            p.pool.data(), p.layout, err, mask);
-            if (rc) return reportFail(rc);
-            applyFseKernel(p.layout);
+            prc[k] = layoutPlan(plan, dFrames.data(), dOuts.data(), nullptr, nullptr, nullptr, nullptr, p.layout,
+                                perr[k], mask);
+            if (prc[k]) return;
+            if (!p.pool.reserve(p.layout.pool.size()) || !p.scratch.reserve(p.layout.scratchBytes)) {
+                prc[k] = ZL_ErrorCode_allocation;
+                perr[k] = "device allocation failed";
+                return;
+            }
+            prc[k] = layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), p.scratch.data(),
+                                p.pool.data(), p.layout, perr[k], mask);
+        };
+        if (parts.size() > 1 && n >= 64) {
+            std::vector<std::thread> th;
+            for (size_t k = 1; k < parts.size(); k++) th.emplace_back(layoutPart, k);
+            layoutPart(0);
+            for (std::thread& t : th) t.join();
+        } else {
+            for (size_t k = 0; k < parts.size(); k++) layoutPart(k);
         }
+        for (size_t k = 0; k < parts.size(); k++)
+            if (prc[k]) {
+                err = perr[k];
+                return reportFail(prc[k]);
+            }
+        for (Part& p : parts) applyFseKernel(p.layout);
         uploaded = false;
         launches = 0;
         return reportOk(size_t(plan.totalOut));
@@ -602,13 +629,22 @@ struct DecodeBatch {
             Part& p = host.rounds[r];
             p.mask.assign(n, 0);
             for (size_t i = first[r]; i < first[r + 1]; i++) p.mask[i] = 1;
-            int rc = layoutPlan(plan, dFrames.data(), dOuts.data(), nullptr, nullptr, nullptr, nullptr, p.layout, err,
-                                &p.mask);
-            if (rc) return false;
-            if (!p.pool.reserve(p.layout.pool.size()) || !p.scratch.reserve(p.layout.scratchBytes)) return false;
-            rc = layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), p.scratch.data(),
-                            p.pool.data(), p.layout, err, &p.mask);
-            if (rc) return false;
+            bool fits = false;
+            if (p.pool.data() && p.scratch.data()) { // one pass into buffers kept from an earlier plan
+                if (layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), p.scratch.data(),
+                               p.pool.data(), p.layout, err, &p.mask))
+                    return false;
+                fits = p.layout.pool.size() + 256 <= p.pool.cap && p.layout.scratchBytes + 256 <= p.scratch.cap;
+            }
+            if (!fits) {
+                int rc = layoutPlan(plan, dFrames.data(), dOuts.data(), nullptr, nullptr, nullptr, nullptr, p.layout,
+                                    err, &p.mask);
+                if (rc) return false;
+                if (!p.pool.reserve(p.layout.pool.size()) || !p.scratch.reserve(p.layout.scratchBytes)) return false;
+                rc = layoutPlan(plan, dFrames.data(), dOuts.data(), arena.data(), params.data(), p.scratch.data(),
+                                p.pool.data(), p.layout, err, &p.mask);
+                if (rc) return false;
+            }
             applyFseKernel(p.layout);
             host.inOff[r] = size_t(dFrames[first[r]] - dFrames[0]);
             host.outOff[r] = size_t(dOuts[first[r]] - dOuts[0]);
