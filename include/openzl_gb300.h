@@ -336,6 +336,32 @@ ZL_Report ozl_gpu_decompress(ZL_DCtx* dctx, void* d_dst, size_t dstCapacity,
                              void* stream);
 
 /* Batched decode: many frames, one plan, one CUDA graph launch per run. */
+/* Frame header summary (no counterpart in the reference; the fields its
+ * ZL_FrameInfo and ZL_getDecompressedSize give, src/openzl/decompress/
+ * decode_frameheader.c:58-370, plus what the batch API needs to place the
+ * outputs). status is 0 or the ZL error code of the header parse. */
+typedef struct {
+    int32_t status;
+    uint32_t formatVersion;
+    uint32_t nbOutputs;
+    uint32_t flags;          /* bit 0 content checksum, bit 1 compressed checksum, bit 2 header checksum byte */
+    uint64_t headerBytes;    /* offset of the first block */
+    uint64_t output0Bytes;   /* decompressed bytes of output 0 (a string output: its content) */
+    uint64_t extent;         /* destination bytes of the batch API: every output at a 16-byte-aligned
+                                offset, a string output's 4-byte lengths after its content */
+    int32_t output0Type;     /* ZL_Type of output 0 */
+    uint32_t reserved;
+} OZL_FrameInfo;
+/* The summary of one frame in host memory, parsed on the host. */
+ZL_Report ozl_frame_info(const void* frame, size_t frameSize, OZL_FrameInfo* info);
+/* The summaries of n frames in device memory, parsed on the device (one
+ * thread per frame): d_frames[i] (a device array of device pointers) holds
+ * d_frameSizes[i] bytes (a device array); the records go to d_info[i]
+ * (device memory). Enqueued on `stream`; nothing is read back. Equal to
+ * ozl_frame_info on the same bytes. Returns n. */
+ZL_Report ozl_gpu_frame_info(const void* const* d_frames, const uint64_t* d_frameSizes, size_t n,
+                             OZL_FrameInfo* d_info, void* stream);
+
 typedef struct OZL_GpuBatch_s OZL_GpuBatch;
 OZL_GpuBatch* ozl_gpu_batch_create(void);
 void ozl_gpu_batch_free(OZL_GpuBatch* b);

@@ -21,6 +21,9 @@ from ._lib import (  # noqa: F401
     get_decompressed_size,
     get_compressed_size,
     frame_outputs,
+    FrameHeaderInfo,
+    frame_header_info,
+    frame_header_info_device,
     library,
     library_path,
 )

@@ -49,6 +49,8 @@ def library():
         "ZL_getDecompressedSize": ([vp, sz], ZLReport),
         "ZL_getCompressedSize": ([vp, sz], ZLReport),
         "ozl_frame_outputs": ([vp, sz, sz, vp, vp, vp, vp, vp, vp, vp], ZLReport),
+        "ozl_frame_info": ([vp, sz, vp], ZLReport),
+        "ozl_gpu_frame_info": ([vp, vp, sz, vp, vp], ZLReport),
         "ZL_TypedBuffer_rStringLens": ([vp], vp),
         "ZL_DCtx_create": ([], vp),
         "ZL_DCtx_free": ([vp], None),
@@ -157,6 +159,30 @@ def get_decompressed_size(frame):
 def get_compressed_size(frame):
     f = _as_u8(frame)
     return _check(library().ZL_getCompressedSize(f.ctypes.data, f.size))
+
+
+class FrameHeaderInfo(ctypes.Structure):
+    """OZL_FrameInfo (include/openzl_gb300.h): a frame header's summary."""
+    _fields_ = [("status", ctypes.c_int32), ("formatVersion", ctypes.c_uint32), ("nbOutputs", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32), ("headerBytes", ctypes.c_uint64), ("output0Bytes", ctypes.c_uint64),
+                ("extent", ctypes.c_uint64), ("output0Type", ctypes.c_int32), ("reserved", ctypes.c_uint32)]
+
+
+def frame_header_info(frame):
+    """ozl_frame_info: the header summary of a frame in host memory, parsed on
+    the host (status 0 or the parse's ZL error code)."""
+    f = _as_u8(frame)
+    info = FrameHeaderInfo()
+    _check(library().ozl_frame_info(f.ctypes.data if f.size else None, f.size, ctypes.byref(info)))
+    return info
+
+
+def frame_header_info_device(d_frame_ptrs, d_frame_sizes, n, d_info, stream=0):
+    """ozl_gpu_frame_info: header summaries of n frames in device memory,
+    parsed on the device. d_frame_ptrs / d_frame_sizes: device addresses of
+    n 64-bit frame addresses / sizes; d_info: device address of n 48-byte
+    records. Enqueued on `stream`."""
+    return _check(library().ozl_gpu_frame_info(d_frame_ptrs, d_frame_sizes, n, d_info, stream))
 
 
 def frame_outputs(frame):

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libopenzl_gb300.so")
-SOURCES = ["decode_kernels.cu", "encode_kernels.cu", "dec_plan.cpp", "enc_tables.cpp", "enc_engine.cpp", "capi.cpp",
+SOURCES = ["decode_kernels.cu", "encode_kernels.cu", "frame_info.cu", "dec_plan.cpp", "enc_tables.cpp", "enc_engine.cpp", "capi.cpp",
            "compress_api.cpp", "server.cpp", "custom_codecs.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -239,6 +239,26 @@ ZL_Report ZL_getDecompressedSize(const void* src, size_t size)
     return ok(size_t(h.outSize));
 }
 
+ZL_Report ozl_frame_info(const void* frame, size_t frameSize, OZL_FrameInfo* info)
+{
+    if (!info || (!frame && frameSize)) return fail(ZL_ErrorCode_parameter_invalid);
+    *info = OZL_FrameInfo{};
+    ozl::FrameHeader h;
+    std::string err;
+    int const rc = ozl::parseFrameHeader(static_cast<const uint8_t*>(frame), frameSize, h, err);
+    info->status = rc;
+    if (rc) return ok(0);
+    std::vector<uint64_t> offs;
+    info->formatVersion = h.version;
+    info->nbOutputs = uint32_t(h.sizes.size());
+    info->flags = (h.hasContentCk ? 1u : 0u) | (h.hasCompressedCk ? 2u : 0u) | (h.hdrCk ? 4u : 0u);
+    info->headerBytes = h.end;
+    info->output0Bytes = h.outSize;
+    info->output0Type = h.outType;
+    info->extent = ozl::frameOutputLayout(h, offs);
+    return ok(0);
+}
+
 ZL_Report ozl_frame_outputs(const void* frame, size_t frameSize, size_t capacity, uint64_t* offsets, uint64_t* sizes,
                             int* types, uint32_t* widths, uint64_t* counts, uint64_t* lensOffsets, uint64_t* extent)
 {
