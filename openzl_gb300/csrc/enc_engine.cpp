@@ -246,6 +246,18 @@ void parallelFor(size_t n, F fn)
 
 struct EncodeBatch::Impl {
     DevBuf bufA, bufE, bufF, bufSmall, bufT, bufW, bufR, bufH;
+    // the inputs' content checksums run on their own stream (a long input's
+    // block chain is serial), from the front end until the assembly writes
+    // them into the frames
+    cudaStream_t hashStream = nullptr;
+    cudaEvent_t hashStart = nullptr, hashDone = nullptr;
+    bool hashPending = false;
+    ~Impl()
+    {
+        if (hashStream) cudaStreamDestroy(hashStream);
+        if (hashStart) cudaEventDestroy(hashStart);
+        if (hashDone) cudaEventDestroy(hashDone);
+    }
     PinnedBuf stage, stageH;
     std::vector<Job> jobs;           // data chunks (discovery order), then nested weights jobs
     size_t nbDataJobs = 0;
@@ -871,6 +883,12 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             if (len > 240) blocks += (len - 1) / kHashBlock;
         }
         smallBytes += blocks * (64 + sizeof(TileRef)) + 1024;
+        // a previous call that failed may have left its checksums running on
+        // the side stream, which reads this buffer
+        if (I.hashPending) {
+            cudaEventSynchronize(I.hashDone);
+            I.hashPending = false;
+        }
         if (!I.bufSmall.reserve(smallBytes)) { err = "device allocation failed"; return 70; }
         Bump b{ I.bufSmall.data(), 0 };
         auto* dMaxTasks = reinterpret_cast<EncNumTask*>(b.take(maxTasks.size() * sizeof(EncNumTask) + 1));
@@ -921,10 +939,19 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             launches_++;
         }
         if (!contentHash.empty()) {
-            cudaMemcpyAsync(dHashTasks, contentHash.data(), contentHash.size() * sizeof(HashTask), cudaMemcpyHostToDevice, st);
+            bool const ok = (I.hashStream || cudaStreamCreateWithFlags(&I.hashStream, cudaStreamNonBlocking) == cudaSuccess)
+                            && (I.hashStart || cudaEventCreateWithFlags(&I.hashStart, cudaEventDisableTiming) == cudaSuccess)
+                            && (I.hashDone || cudaEventCreateWithFlags(&I.hashDone, cudaEventDisableTiming) == cudaSuccess);
+            if (!ok) { err = "checksum stream could not be set up"; return 1; }
+            cudaStream_t const hs = I.hashStream;
+            cudaEventRecord(I.hashStart, st); // the inputs are ready on `st`
+            cudaStreamWaitEvent(hs, I.hashStart, 0);
+            cudaMemcpyAsync(dHashTasks, contentHash.data(), contentHash.size() * sizeof(HashTask), cudaMemcpyHostToDevice, hs);
             if (!contentBlocks.empty())
-                cudaMemcpyAsync(dBlocks, contentBlocks.data(), contentBlocks.size() * sizeof(TileRef), cudaMemcpyHostToDevice, st);
-            launchHash(dHashTasks, uint32_t(contentHash.size()), dBlocks, uint32_t(contentBlocks.size()), nullptr, st);
+                cudaMemcpyAsync(dBlocks, contentBlocks.data(), contentBlocks.size() * sizeof(TileRef), cudaMemcpyHostToDevice, hs);
+            launchHash(dHashTasks, uint32_t(contentHash.size()), dBlocks, uint32_t(contentBlocks.size()), nullptr, hs);
+            cudaEventRecord(I.hashDone, hs);
+            I.hashPending = true;
             launches_ += contentBlocks.empty() ? 1 : 2;
         }
         std::vector<unsigned long long> maxima(nbMax);
@@ -1923,12 +1950,14 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         launchCopy(dCopies, dTiles, uint32_t(tiles.size()), st);
         launches_++;
         if (checksums) {
+            if (I.hashPending) cudaStreamWaitEvent(st, I.hashDone, 0); // the content checksums go in now
             launchPut(dPut1, uint32_t(put1.size()), st);
             launchHash(dHT, uint32_t(blockHash.size()), dBB, uint32_t(blockBlocks.size()), nullptr, st);
             launchPut(dPut2, uint32_t(put2.size()), st);
             launches_ += 3 + (blockBlocks.empty() ? 0 : 1);
         }
         if (cudaStreamSynchronize(st) != cudaSuccess) { err = "device error in frame assembly"; return 1; }
+        I.hashPending = false;
     }
     endPhase();
     return 0;
