@@ -986,6 +986,9 @@ def main():
         raise RuntimeError("host-buffer decode differs from the input")
     e2e = {"value": round(total_out * ws / e2e_s / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": fbytes,
            "d2h_bytes_per_step": obytes, "ms_per_step": round(e2e_s * 1e3, 3)}
+    # per round of the host-buffer run: ms its frames were in, decoded, out
+    e2e["rounds"] = [[round(a, 3), round(b, 3), round(c, 3)]
+                     for a, b, c in batch.host_timeline(frames_h.data_ptr(), fbytes, out_h.data_ptr(), obytes, sptr)]
 
     # ---- plain path: one frame per call, stage-by-stage launches
     plain = None

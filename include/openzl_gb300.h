@@ -114,9 +114,13 @@ typedef enum {
      * order); 1: every element-wise launch ahead of all entropy decoding. */
     OZL_DParam_schedule = 1003,
     /* batch API only: rounds of contiguous frames of about equal decoded
-     * bytes in ozl_gpu_batch_run_host (1..16, default 12); each round's
+     * bytes in ozl_gpu_batch_run_host (1..16, default 16); each round's
      * outputs go down as soon as it is decoded. */
     OZL_DParam_hostRounds = 1004,
+    /* batch API only: rounds of ozl_gpu_batch_run_host that decode at once
+     * (round r starts after round r - depth has decoded; 0 = all at once;
+     * default 6) */
+    OZL_DParam_hostDepth = 1005,
 } ZL_DParam;
 
 typedef enum {
@@ -409,6 +413,14 @@ ZL_Report ozl_gpu_batch_profile(OZL_GpuBatch* b, void* stream, float* ms, int* k
  * at which the launch ended; for i < capacity. Returns the number of
  * launches. Synchronizes `stream`. */
 ZL_Report ozl_gpu_batch_timeline(OZL_GpuBatch* b, void* stream, float* rows, size_t capacity);
+/* Host-buffer timeline: one ozl_gpu_batch_run_host run without a graph, with
+ * timing events. Writes 3 floats per round to rows[3 r ..] (r < capacity):
+ * the ms from the run's start at which round r's frames were in, its decode
+ * ended and its outputs were out. Returns the number of rounds (0 when the
+ * frames are not laid out in order and the run is not split into rounds).
+ * Synchronizes `stream`. */
+ZL_Report ozl_gpu_batch_host_timeline(OZL_GpuBatch* b, const void* h_in, size_t inBytes, void* h_out,
+                                      size_t outBytes, void* stream, float* rows, size_t capacity);
 /* Name of a codec family reported by ozl_gpu_batch_profile. */
 const char* ozl_gpu_kind_name(int kind);
 /* Autotuner: times the candidate launch shapes (chunks per CTA of the FSE

@@ -74,6 +74,7 @@ def library():
         "ozl_gpu_xxh3_64_static": ([vp, sz, vp], ZLReport),
         "ozl_gpu_batch_profile": ([vp, vp, vp, vp, vp, sz], ZLReport),
         "ozl_gpu_batch_timeline": ([vp, vp, vp, sz], ZLReport),
+        "ozl_gpu_batch_host_timeline": ([vp, vp, sz, vp, sz, vp, vp, sz], ZLReport),
         "ozl_gpu_kind_name": ([ctypes.c_int], ctypes.c_char_p),
         "ozl_gpu_batch_run_host": ([vp, vp, sz, vp, sz, vp, ctypes.c_int], ZLReport),
         "ozl_gpu_batch_autotune": ([vp, vp, ctypes.c_int, vp, sz], ZLReport),
@@ -214,6 +215,7 @@ DPARAM_FSE_KERNEL = 1001  # OZL_DParam_fseKernel
 DPARAM_CRITICAL_SYMBOLS = 1002  # OZL_DParam_criticalSymbols
 DPARAM_SCHEDULE = 1003  # OZL_DParam_schedule
 DPARAM_HOST_ROUNDS = 1004  # OZL_DParam_hostRounds
+DPARAM_HOST_DEPTH = 1005  # OZL_DParam_hostDepth
 
 
 class DCtx:
@@ -332,7 +334,7 @@ class GpuBatch:
     """Batched decode of many frames: one plan, one CUDA graph per run."""
 
     def __init__(self, check_content=True, check_compressed=True, parts_per_kind=None, fse_kernel=None,
-                 critical_symbols=None, schedule=None, host_rounds=None):
+                 critical_symbols=None, schedule=None, host_rounds=None, host_depth=None):
         self._lib = library()
         self._h = self._lib.ozl_gpu_batch_create()
         if parts_per_kind is not None:
@@ -345,6 +347,8 @@ class GpuBatch:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_SCHEDULE, int(schedule)))
         if host_rounds is not None:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_HOST_ROUNDS, int(host_rounds)))
+        if host_depth is not None:
+            _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_HOST_DEPTH, int(host_depth)))
         if not check_content:
             _check(self._lib.ozl_gpu_batch_setParameter(self._h, DPARAM_CHECK_CONTENT, 2))
         if not check_compressed:
@@ -407,6 +411,17 @@ class GpuBatch:
         n = min(rep.value, capacity)
         return [(int(rows[5 * i]), self._lib.ozl_gpu_kind_name(int(rows[5 * i + 1])).decode(), int(rows[5 * i + 2]),
                  rows[5 * i + 3], rows[5 * i + 4]) for i in range(n)]
+
+    def host_timeline(self, h_in_ptr, in_bytes, h_out_ptr, out_bytes, stream=0, capacity=64):
+        """One host-buffer run with events: per round (ms in, ms decoded, ms
+        out) from the run's start."""
+        rows = (ctypes.c_float * (3 * capacity))()
+        rep = self._lib.ozl_gpu_batch_host_timeline(self._h, h_in_ptr, in_bytes, h_out_ptr, out_bytes, stream,
+                                                    rows, capacity)
+        if rep.code:
+            self._raise(rep)
+        n = min(rep.value, capacity)
+        return [(rows[3 * r], rows[3 * r + 1], rows[3 * r + 2]) for r in range(n)]
 
     def run_host(self, h_in_ptr, in_bytes, h_out_ptr, out_bytes, stream=0, graph=True):
         """Host buffers in and out around one planned run (copies included)."""

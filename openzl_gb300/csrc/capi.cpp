@@ -482,6 +482,11 @@ ZL_Report ozl_gpu_batch_setParameter(OZL_GpuBatch* b, ZL_DParam param, int value
             b->hostRounds = value;
             b->host.reset();
             break;
+        case OZL_DParam_hostDepth:
+            if (value < 0 || value > ozl::DecodeBatch::HostPipe::kRounds) return fail(ZL_ErrorCode_parameter_invalid);
+            b->hostDepth = value;
+            b->host.dropGraph();
+            break;
         default: return fail(ZL_ErrorCode_parameter_invalid);
     }
     return ok(0);
@@ -514,6 +519,13 @@ const char* ozl_gpu_kind_name(int kind)
                                    "float_deconstruct", "transpose", "numeric_pipeline", "xxh3", "huffman16",
                                    "widen" };
     return (kind >= 0 && kind < ozl::KIND_COUNT) ? names[kind] : "?";
+}
+
+ZL_Report ozl_gpu_batch_host_timeline(OZL_GpuBatch* b, const void* h_in, size_t inBytes, void* h_out,
+                                      size_t outBytes, void* stream, float* rows, size_t capacity)
+{
+    if (!b || b->dFrames.empty() || (capacity && !rows)) return fail(ZL_ErrorCode_parameter_invalid);
+    return b->hostTimeline(h_in, inBytes, h_out, outBytes, static_cast<cudaStream_t>(stream), rows, capacity);
 }
 
 ZL_Report ozl_gpu_batch_timeline(OZL_GpuBatch* b, void* stream, float* rows, size_t capacity)

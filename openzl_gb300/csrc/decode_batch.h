@@ -119,7 +119,8 @@ struct DecodeBatch {
     // stream, the round decodes on its own stream as soon as they are in
     // (rounds share the SMs), and its outputs go down on a second copy stream
     // as soon as it is done, so both copy directions overlap the decode.
-    int hostRounds = 12;     // OZL_DParam_hostRounds
+    int hostRounds = 16;     // OZL_DParam_hostRounds
+    int hostDepth = 6;       // OZL_DParam_hostDepth: rounds decoding at once (0 = all)
     struct HostPipe {
         static constexpr int kRounds = 16;
         std::vector<Part> rounds;
@@ -542,6 +543,51 @@ struct DecodeBatch {
         return reportOk(0);
     }
 
+    // One host-buffer run without a graph, with timing events: row r of
+    // `rows` (3 floats) holds the ms from the run's start at which round r's
+    // frames were in, its decode ended and its outputs were out. Returns the
+    // number of rounds (0 when the frames are not laid out in order for
+    // rounds). Synchronizes `s`.
+    ZL_Report hostTimeline(const void* hIn, size_t inBytes, void* hOut, size_t outBytes, cudaStream_t s, float* rows,
+                           size_t capacity)
+    {
+        if (!buildRounds(inBytes, outBytes)) return reportOk(0);
+        ZL_Report u = upload(s);
+        if (ZL_isError(u)) return u;
+        if (!host.uploaded) {
+            afterLastRun(s);
+            for (Part& p : host.rounds)
+                if (!p.layout.pool.empty())
+                    cudaMemcpyAsync(p.pool.data(), p.layout.pool.data(), p.layout.pool.size(), cudaMemcpyHostToDevice, s);
+            host.uploaded = true;
+        }
+        size_t const nr = host.rounds.size();
+        std::vector<cudaEvent_t> marks(1 + 3 * nr, nullptr);
+        bool ok = true;
+        for (auto& e : marks) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+        ZL_Report r = reportOk(nr);
+        if (ok) {
+            r = enqueueHost(hIn, hOut, s, &marks);
+            if (!ZL_isError(r)) markRun(s);
+            ok = !ZL_isError(r) && cudaStreamSynchronize(s) == cudaSuccess;
+        }
+        for (size_t k = 0; ok && k < 3 * nr && k < 3 * capacity; k++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, marks[0], marks[1 + k]);
+            rows[k] = ms;
+        }
+        for (auto& e : marks)
+            if (e) cudaEventDestroy(e);
+        if (ZL_isError(r)) return r;
+        if (!ok) {
+            err = "host timeline run failed";
+            return reportFail(ZL_ErrorCode_GENERIC);
+        }
+        ZL_Report const c = check(s);
+        if (ZL_isError(c)) return c;
+        return reportOk(nr);
+    }
+
     // OZL_DParam_fseKernel: the FSE launches' kernel until the autotuner runs
     void applyFseKernel(DeviceLayout& layout) const
     {
@@ -671,7 +717,9 @@ struct DecodeBatch {
         return true;
     }
 
-    ZL_Report enqueueHost(const void* hIn, void* hOut, cudaStream_t s)
+    // `marks` (host timelines): 1 + 3 * rounds timing events: the start,
+    // then per round its frames in, decoded, outputs out
+    ZL_Report enqueueHost(const void* hIn, void* hOut, cudaStream_t s, const std::vector<cudaEvent_t>* marks = nullptr)
     {
         size_t const nr = host.rounds.size();
         uint8_t* const dIn = const_cast<uint8_t*>(dFrames[0]);
@@ -685,12 +733,18 @@ struct DecodeBatch {
                 ok = cudaMemcpyAsync(dIn + a, static_cast<const uint8_t*>(hIn) + a, b - a, cudaMemcpyHostToDevice,
                                      host.sIn) == cudaSuccess;
             ok = ok && cudaEventRecord(host.inEv[r], host.sIn) == cudaSuccess;
+            if (marks) cudaEventRecord((*marks)[1 + 3 * r], host.sIn);
         }
+        if (marks) cudaEventRecord((*marks)[0], s);
         for (size_t r = 0; r < nr && ok; r++) {
             Part& p = host.rounds[r];
-            ok = cudaStreamWaitEvent(host.rs[r], host.inEv[r], 0) == cudaSuccess
+            // at most hostDepth rounds decode at once: round r waits for round r - depth
+            if (hostDepth > 0 && r >= size_t(hostDepth))
+                ok = cudaStreamWaitEvent(host.rs[r], host.decEv[r - size_t(hostDepth)], 0) == cudaSuccess;
+            ok = ok && cudaStreamWaitEvent(host.rs[r], host.inEv[r], 0) == cudaSuccess
                  && runLaunches(p.layout, p.pool.data(), p.scratch.data(), st, host.rs[r]) >= 0
                  && cudaEventRecord(host.decEv[r], host.rs[r]) == cudaSuccess;
+            if (marks) cudaEventRecord((*marks)[2 + 3 * r], host.rs[r]);
         }
         for (size_t r = 0; r < nr && ok; r++) {
             size_t const a = host.outOff[r], b = host.outOff[r + 1];
@@ -698,6 +752,7 @@ struct DecodeBatch {
             if (ok && b > a)
                 ok = cudaMemcpyAsync(static_cast<uint8_t*>(hOut) + a, dOuts[0] + a, b - a, cudaMemcpyDeviceToHost,
                                      host.sOut) == cudaSuccess;
+            if (marks) cudaEventRecord((*marks)[3 + 3 * r], host.sOut);
         }
         ok = ok && cudaEventRecord(host.outDone, host.sOut) == cudaSuccess
              && cudaStreamWaitEvent(s, host.outDone, 0) == cudaSuccess
