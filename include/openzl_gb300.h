@@ -129,7 +129,9 @@ typedef enum {
     ZL_TernaryParam_disable = 2,
 } ZL_TernaryParam;
 
-/* zl_decompress.h:80 */
+/* zl_decompress.h:80. A DCtx is bound to the CUDA device current when it is
+ * created: its calls decode there whatever device is current at the call,
+ * and give the caller's current device back. */
 ZL_DCtx* ZL_DCtx_create(void);
 /* zl_decompress.h:87 */
 void ZL_DCtx_free(ZL_DCtx* dctx);
@@ -298,7 +300,8 @@ ZL_Report ZL_DCtx_registerMIDecoder(ZL_DCtx* dctx, const ZL_MIDecoderDesc* dtd);
 /* zl_compress.h:39-53 */
 #define ZL_COMPRESSBOUND(s) (((s) * 2) + 512 + 8)
 size_t ZL_compressBound(size_t totalSrcSize);
-/* zl_compress.h:60-61 */
+/* zl_compress.h:60-61. A CCtx is bound to the CUDA device current when it is
+ * created, like a DCtx. */
 ZL_CCtx* ZL_CCtx_create(void);
 void ZL_CCtx_free(ZL_CCtx* cctx);
 /* zl_compress.h:152, :161, :168 */

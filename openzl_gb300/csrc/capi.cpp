@@ -41,6 +41,7 @@ cudaError_t prepareOnce()
 struct OZL_GpuBatch_s : ozl::DecodeBatch {};
 
 struct ZL_DCtx_s {
+    int device = ozl::currentDevice(); // the device current at creation: every call decodes there
     ozl::DecodeBatch batch;
     bool sticky = false;
     int raw[4] = {}; // parameter values as set, for ZL_DCtx_getParameter
@@ -356,6 +357,7 @@ ZL_Report ozl_gpu_decompress(ZL_DCtx* dctx, void* d_dst, size_t dstCap, const vo
                              size_t cSize, void* stream)
 {
     if (!dctx || !h_frame || !d_frame) return fail(ZL_ErrorCode_parameter_invalid);
+    ozl::DeviceScope const onDevice(dctx->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ZL_Report r = dctx->batch.makePlan(1, &h_frame, &cSize, &d_frame, &d_dst, &dstCap);
     if (!ZL_isError(r)) r = dctx->batch.run(s, false);
@@ -375,6 +377,7 @@ static ZL_Report decodeToHost(ZL_DCtx* dctx, void* dst, size_t dstCap, const voi
     if (ZL_isError(ds)) return ds;
     size_t const outSize = ZL_validResult(ds);
     if (outSize > dstCap) return fail(ZL_ErrorCode_dstCapacity_tooSmall);
+    ozl::DeviceScope const onDevice(dctx->device);
     if (!dctx->stream && cudaStreamCreateWithFlags(&dctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
         dctx->err = "no CUDA device";
         return fail(ZL_ErrorCode_GENERIC);
@@ -746,6 +749,7 @@ ZL_Report ZL_DCtx_decompressMultiTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* outputs[
         resetParams(dctx);
         return r;
     };
+    ozl::DeviceScope const onDevice(dctx->device);
     if (!dctx->stream && cudaStreamCreateWithFlags(&dctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
         dctx->err = "no CUDA device";
         return done(fail(ZL_ErrorCode_GENERIC));

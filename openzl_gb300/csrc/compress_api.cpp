@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/openzl_gb300.h"
+#include "device_scope.h"
 #include "enc_engine.h"
 
 namespace {
@@ -148,6 +149,7 @@ struct ZL_TypedRef_s {
 };
 
 struct ZL_CCtx_s {
+    int device = ozl::currentDevice(); // the device current at creation: every call encodes there
     const ZL_Compressor_s* comp = nullptr;
     int params[kNbParams] = {};
     ozl::EncodeBatch enc;
@@ -247,6 +249,7 @@ ZL_Report compressOne(ZL_CCtx* c, void* dst, size_t cap, const ZL_TypedRef& in)
         return fail(ZL_ErrorCode_compressionParameter_invalid);
     }
     bool const checksums = ck != ZL_TernaryParam_disable;
+    ozl::DeviceScope const onDevice(c->device);
     if (!c->stream && cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         c->err = "no CUDA device";
         return fail(ZL_ErrorCode_GENERIC);

@@ -13,6 +13,7 @@
 #include "../../include/openzl_gb300.h"
 #include "dec_exec.h"
 #include "dec_plan.h"
+#include "device_scope.h"
 
 namespace ozl {
 

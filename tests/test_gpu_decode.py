@@ -188,9 +188,17 @@ def test_batch_run_host_pipelined(gpu_lib, manifest, graph):
         b = oz.GpuBatch()
         b.plan([frames[i] for i in idx], [d_in.data_ptr() + foffs[i] for i in idx],
                [d_out.data_ptr() + ooffs[i] for i in idx], [sizes[i] for i in idx])
-        for rep in range(3):
+        for rep in range(4):
             h_out.fill_(0xAB)
-            b.run_host(h_in.data_ptr(), fbytes, h_out.data_ptr(), obytes, s.cuda_stream, graph=graph)
+            if rep == 3:  # the timeline run: rounds (in order) or none (serial path)
+                rows = b.host_timeline(h_in.data_ptr(), fbytes, h_out.data_ptr(), obytes, s.cuda_stream)
+                if order == "increasing":
+                    assert len(rows) > 1 and all(a <= c and d <= c for a, d, c in rows), rows
+                else:
+                    assert rows == []
+                    b.run_host(h_in.data_ptr(), fbytes, h_out.data_ptr(), obytes, s.cuda_stream, graph=graph)
+            else:
+                b.run_host(h_in.data_ptr(), fbytes, h_out.data_ptr(), obytes, s.cuda_stream, graph=graph)
             for i in range(len(frames)):
                 got = h_out[ooffs[i]:ooffs[i] + sizes[i]].numpy().tobytes()
                 assert hashlib.sha256(got).hexdigest() == want[i], (order, rep, i)
