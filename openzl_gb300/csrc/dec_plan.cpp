@@ -19,6 +19,8 @@
 #include <algorithm>
 #include <cstring>
 #include <functional>
+#include <iterator>
+#include <thread>
 #include <type_traits>
 #include <unordered_map>
 
@@ -252,6 +254,98 @@ int DecodePlan::build(size_t nbFrames, const uint8_t* const* hFrames, const size
             return rc;
         }
         totalOut += frames[f].decodedSize;
+    }
+    return 0;
+}
+
+int DecodePlan::buildParallel(size_t nbFrames, const uint8_t* const* hFrames, const size_t* frameSizes,
+                              const size_t* dstCapacities, bool ckContent, bool ckCompressed, std::string& err,
+                              unsigned threads)
+{
+    constexpr size_t kMinFrames = 64; // frames per thread below which threads do not pay
+    size_t const T = std::min<size_t>(threads, nbFrames / kMinFrames);
+    if (T < 2) return build(nbFrames, hFrames, frameSizes, dstCapacities, ckContent, ckCompressed, err);
+    // runs of about equal compressed bytes
+    uint64_t total = 0;
+    for (size_t f = 0; f < nbFrames; f++) total += frameSizes[f];
+    std::vector<size_t> first{ 0 };
+    uint64_t acc = 0;
+    for (size_t f = 0; f + 1 < nbFrames && first.size() < T; f++) {
+        acc += frameSizes[f];
+        if (acc * T >= total * first.size()) first.push_back(f + 1);
+    }
+    first.push_back(nbFrames);
+    size_t const runs = first.size() - 1;
+    std::vector<DecodePlan> sub(runs);
+    std::vector<int> rc(runs, 0);
+    std::vector<std::string> errs(runs);
+    auto one = [&](size_t t) {
+        size_t const f0 = first[t];
+        rc[t] = sub[t].build(first[t + 1] - f0, hFrames + f0, frameSizes + f0, dstCapacities ? dstCapacities + f0 : nullptr,
+                             ckContent, ckCompressed, errs[t]);
+    };
+    std::vector<std::thread> th;
+    for (size_t t = 1; t < runs; t++) th.emplace_back(one, t);
+    one(0);
+    for (std::thread& x : th) x.join();
+    for (size_t t = 0; t < runs; t++)
+        if (rc[t]) return build(nbFrames, hFrames, frameSizes, dstCapacities, ckContent, ckCompressed, err);
+    // join
+    frames.clear();
+    streams.clear();
+    nodes.clear();
+    hashes.clear();
+    directCopies.clear();
+    gathers.clear();
+    widens.clear();
+    params.clear();
+    arenaBytes = 0;
+    totalOut = 0;
+    for (size_t t = 0; t < runs; t++) {
+        DecodePlan& P = sub[t];
+        int const fo = int(first[t]), so = int(streams.size()), no = int(nodes.size());
+        uint64_t const ao = arenaBytes;                         // 64-byte multiple
+        uint64_t const po = (params.size() + 15) & ~size_t(15); // the next 16-byte aligned block
+        for (PlanStream& x : P.streams) {
+            if (x.producer >= 0) x.producer += no;
+            if (x.parent >= 0) x.parent += so;
+            if (x.lens >= 0) x.lens += so;
+            if (x.frame >= 0) x.frame += fo;
+            if (x.loc == L_ARENA) x.off += ao;
+            else if (x.loc == L_PARAM) x.off += po;
+        }
+        for (PlanNode& x : P.nodes) {
+            for (int& i : x.ins) i += so;
+            if (x.out >= 0) x.out += so;
+            if (x.frame >= 0) x.frame += fo;
+            x.paramOff += po;
+        }
+        for (PlanHash& x : P.hashes) {
+            x.frame += fo;
+            if (x.where == HW_ARENA) x.off += ao;
+        }
+        for (PlanCopy& x : P.directCopies) x.frame += fo;
+        for (PlanGather& x : P.gathers) {
+            x.frame += fo;
+            x.arenaOff += ao;
+        }
+        for (PlanWiden& x : P.widens) {
+            x.stream += so;
+            x.frame += fo;
+        }
+        frames.insert(frames.end(), std::make_move_iterator(P.frames.begin()), std::make_move_iterator(P.frames.end()));
+        streams.insert(streams.end(), P.streams.begin(), P.streams.end());
+        nodes.insert(nodes.end(), std::make_move_iterator(P.nodes.begin()), std::make_move_iterator(P.nodes.end()));
+        hashes.insert(hashes.end(), P.hashes.begin(), P.hashes.end());
+        directCopies.insert(directCopies.end(), P.directCopies.begin(), P.directCopies.end());
+        gathers.insert(gathers.end(), P.gathers.begin(), P.gathers.end());
+        widens.insert(widens.end(), P.widens.begin(), P.widens.end());
+        if (!P.params.empty()) {
+            params.resize(po);
+            params.insert(params.end(), P.params.begin(), P.params.end());
+        }
+        arenaBytes += P.arenaBytes;
+        totalOut += P.totalOut;
     }
     return 0;
 }

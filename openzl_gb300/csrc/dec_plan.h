@@ -150,6 +150,15 @@ class DecodePlan {
     int build(size_t nbFrames, const uint8_t* const* hFrames, const size_t* frameSizes,
               const size_t* dstCapacities, bool checkContent, bool checkCompressed,
               std::string& err);
+    // The same plan built on up to `threads` host threads: runs of frames
+    // planned apart, then joined with their stream, node, frame, arena and
+    // parameter references moved to the joined positions. Arena blocks are
+    // 64-byte multiples and parameter blocks start 16-byte aligned, so the
+    // joined plan equals the serial one. Small batches, or any error (for its
+    // exact message), take the serial build.
+    int buildParallel(size_t nbFrames, const uint8_t* const* hFrames, const size_t* frameSizes,
+                      const size_t* dstCapacities, bool checkContent, bool checkCompressed, std::string& err,
+                      unsigned threads);
 
     std::vector<FramePlan> frames;
     std::vector<PlanStream> streams;

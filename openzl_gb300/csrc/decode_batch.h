@@ -120,6 +120,7 @@ struct DecodeBatch {
     // stream, the round decodes on its own stream as soon as they are in
     // (rounds share the SMs), and its outputs go down on a second copy stream
     // as soon as it is done, so both copy directions overlap the decode.
+    unsigned planThreads = 0; // host threads of the plan build (0: the machine's, at most 8)
     int hostRounds = 16;     // OZL_DParam_hostRounds
     int hostDepth = 6;       // OZL_DParam_hostDepth: rounds decoding at once (0 = all)
     struct HostPipe {
@@ -198,8 +199,10 @@ struct DecodeBatch {
         dropGraph();
         host.reset();
         if (prepareOnce() != cudaSuccess) { err = "kernel attributes could not be set"; return reportFail(ZL_ErrorCode_GENERIC); }
-        int rc = plan.build(n, reinterpret_cast<const uint8_t* const*>(hF), fs, caps, checkContent,
-                            checkCompressed, err);
+        unsigned const hw = std::thread::hardware_concurrency();
+        unsigned const threads = planThreads ? planThreads : std::min(8u, hw ? hw : 1u);
+        int rc = plan.buildParallel(n, reinterpret_cast<const uint8_t* const*>(hF), fs, caps, checkContent,
+                                    checkCompressed, err, threads);
         if (rc) return reportFail(rc);
         dFrames.assign(reinterpret_cast<const uint8_t* const*>(dF), reinterpret_cast<const uint8_t* const*>(dF) + n);
         dOuts.assign(reinterpret_cast<uint8_t* const*>(dO), reinterpret_cast<uint8_t* const*>(dO) + n);

@@ -159,9 +159,12 @@ void OZL_Server_s::worker()
     ozl::DecodeBatch dec;
     ozl::EncodeBatch enc;
     dec.checkContent = dec.checkCompressed = checksums != 0;
-    // the encoder's parallel host phases on this worker's share of the cores
+    // the encoder's parallel host phases and the decode plans on this
+    // worker's share of the cores
     unsigned const hw = std::thread::hardware_concurrency();
-    enc.setHostThreads(std::max(2u, (hw ? hw : 16u) / unsigned(nbWorkers)));
+    unsigned const cores = std::max(2u, (hw ? hw : 16u) / unsigned(nbWorkers));
+    enc.setHostThreads(cores);
+    dec.planThreads = cores;
     auto need = [](const Request* r) { return alignUp(r->inBytes) + alignUp(r->outBytes); };
     for (;;) {
         std::vector<Request*> batch;

@@ -41,3 +41,17 @@ def test_multi_output_layouts_in_bounds(checker, manifest_multi):
     for m in manifest_multi:
         r = subprocess.run([checker, os.path.join(GOLDEN, m["case"] + ".zl")], capture_output=True, text=True)
         assert r.returncode == 0 and "bad=0" in r.stdout, (m["case"], r.stdout[-2000:], r.stderr[-2000:])
+
+
+def test_parallel_build_equals_serial(tmp_path, manifest, manifest_multi):
+    """The planner's parallel build (runs of frames on 4 threads, joined)
+    gives the serial plan and the same task descriptors, byte for byte, on
+    every golden frame (single and multi-output) repeated to 600 frames."""
+    exe = str(tmp_path / "plan_parallel_check")
+    cmd = ["g++", "-std=c++17", "-O1", "-g", "-pthread", "-fsanitize=address,undefined", "-I",
+           os.path.join(ROOT, "openzl_gb300", "csrc"), os.path.join(ROOT, "tests", "native", "plan_parallel_check.cpp"),
+           os.path.join(ROOT, "openzl_gb300", "csrc", "dec_plan.cpp"), "-o", exe]
+    subprocess.check_call(cmd)
+    files = [os.path.join(GOLDEN, m["case"] + ".zl") for m in manifest + manifest_multi]
+    r = subprocess.run([exe] + files, capture_output=True, text=True)
+    assert r.returncode == 0 and "bad=0" in r.stdout, (r.stdout[-2000:], r.stderr[-2000:])
