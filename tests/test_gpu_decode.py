@@ -338,8 +338,9 @@ def test_multi_output_frames(gpu_lib, manifest, manifest_multi):
     assert rep.code == 8
 
 
-@pytest.mark.parametrize("parts_per_kind,critical", [(1, 0), (2, 0), (4, 0), (1, 1000), (2, 16000), (8, 100)])
-def test_batch_parts_per_kind_keep_results(gpu_lib, manifest, parts_per_kind, critical):
+@pytest.mark.parametrize("parts_per_kind,critical,schedule",
+                         [(1, 0, 0), (2, 0, 0), (4, 0, 0), (1, 1000, 0), (2, 16000, 0), (8, 100, 0), (2, 16000, 1)])
+def test_batch_parts_per_kind_keep_results(gpu_lib, manifest, parts_per_kind, critical, schedule):
     """Runs of frames decoded as parallel graph branches at falling stream
     priorities (each kind split into 1 to 8 runs; frames with an FSE stream of
     at least `critical` symbols as one more branch, 17 branches at most) give
@@ -352,7 +353,7 @@ def test_batch_parts_per_kind_keep_results(gpu_lib, manifest, parts_per_kind, cr
     sizes = [oz.get_decompressed_size(f) for f in frames]
     outs = [torch.zeros(max(n, 1) + 64, dtype=torch.uint8, device="cuda") for n in sizes]
     s = torch.cuda.Stream()
-    b = oz.GpuBatch(parts_per_kind=parts_per_kind, critical_symbols=critical)
+    b = oz.GpuBatch(parts_per_kind=parts_per_kind, critical_symbols=critical, schedule=schedule)
     b.plan(frames, [d.data_ptr() for d in dfr], [o.data_ptr() for o in outs], sizes)
     torch.cuda.synchronize()
     for graph in (False, True):
@@ -362,6 +363,16 @@ def test_batch_parts_per_kind_keep_results(gpu_lib, manifest, parts_per_kind, cr
         b.check(s.cuda_stream)
         for m, n, o in zip(manifest, sizes, outs):
             assert hashlib.sha256(o[:n].cpu().numpy().tobytes()).hexdigest() == m["sha256_in"], (m["case"], graph)
+    # the timeline run: one row per planned launch, each ending after its
+    # stream reached it, and the same bytes
+    for o in outs:
+        o.zero_()
+    rows = b.timeline(s.cuda_stream)
+    b.check(s.cuda_stream)
+    assert rows and all(end >= start for _, _, _, start, end in rows), rows[:4]
+    assert len({part for part, _, _, _, _ in rows}) >= 1
+    for m, n, o in zip(manifest, sizes, outs):
+        assert hashlib.sha256(o[:n].cpu().numpy().tobytes()).hexdigest() == m["sha256_in"], m["case"]
 
 
 def test_huffman_tablelog12_chunks(gpu_lib):

@@ -140,3 +140,42 @@ def test_gpu_frames_equal_oracle_frames_many_frames(gpu_lib):
         if d[:sz].cpu().numpy().tobytes() != oracle.compress(recipe, arr, w).tobytes():
             bad.append((k, recipe, w, arr.size))
     assert not bad, bad[:10]
+
+
+@pytest.mark.parametrize("parts", [1, 3, 8])
+def test_encoder_parts_keep_frames(gpu_lib, parts):
+    """A batch of 64 MiB or more runs in parts (each on its own host thread
+    and stream); the frames equal the oracle's for every part count, and the
+    phase times are reported."""
+    import torch
+    import openzl_gb300 as oz
+
+    rng = np.random.default_rng(909)
+    cases = []
+    total = 0
+    k = 0
+    while total < (80 << 20):
+        recipe = (3, 4, 1, 2, 8)[k % 5]
+        n = int(rng.integers(100000, 700000))
+        if recipe == 8:
+            a = (rng.zipf(1.3, n) % 200).astype(np.uint8)
+            cases.append((recipe, a, 0))
+        else:
+            dt, w = [(np.uint16, 2), (np.uint32, 4), (np.uint64, 8)][k % 3]
+            a = _walk(rng, n, dt, int(rng.integers(1, 5000)))
+            cases.append((recipe, a, w))
+        total += a.nbytes
+        k += 1
+    enc = oz.GpuEncoder()
+    enc.set_parts(parts)
+    srcs = [torch.from_numpy(a.view(np.uint8).copy()).cuda() for _, a, _ in cases]
+    caps = [enc.bound(a.nbytes) for _, a, _ in cases]
+    dsts = [torch.zeros(c, dtype=torch.uint8, device="cuda") for c in caps]
+    sizes = enc.compress_batch([s.data_ptr() for s in srcs], [a.size if w else a.nbytes for _, a, w in cases],
+                               [w for _, _, w in cases], [r for r, _, _ in cases], [d.data_ptr() for d in dsts],
+                               caps, checksums=True)
+    ph = enc.phases()
+    assert set(ph) == set(oz.GpuEncoder.PHASES) and all(v >= 0 for v in ph.values()) and sum(ph.values()) > 0
+    bad = [k for k, ((recipe, arr, w), d, sz) in enumerate(zip(cases, dsts, sizes))
+           if d[:sz].cpu().numpy().tobytes() != oracle.compress(recipe, arr, w).tobytes()]
+    assert not bad, bad[:10]

@@ -65,8 +65,12 @@ def test_alone_equals_mix_equals_expected(gpu_lib):
         ids.append(i)
         outs.append(out)
     res = _collect(srv, len(reqs))
+    st = srv.stats()
     srv.close()
     assert len(res) == len(reqs)
+    # the workers' statistics count every request once
+    assert st["decode_requests"] + st["encode_requests"] == 2 * len(reqs), st
+    assert st["decode_batches"] >= 1 and st["decode_plan_s"] > 0 and st["decode_run_s"] > 0, st
     for r, i, out, a in zip(reqs, ids, outs, alone):
         code, val, lat = res[i]
         assert code == 0
