@@ -595,10 +595,30 @@ __global__ void __launch_bounds__(32) kFseEnc(const FseEncTask* __restrict__ tas
         bo.add(state, nbOut);
         state = st[(state >> nbOut) + dfs[sym]];
     };
+    // The start-up loops reach the states by a run-time index. Each access
+    // is a switch over the four constant indexes: indexing the array itself
+    // would put it, and with it every state of the main loop, in local memory.
+    auto initAt = [&](uint32_t k, uint32_t sym) {
+        uint32_t const x = initState(sym);
+        switch (k) {
+            case 0: v[0] = x; break;
+            case 1: v[1] = x; break;
+            case 2: v[2] = x; break;
+            default: v[3] = x; break;
+        }
+    };
+    auto encodeAt = [&](uint32_t k, uint32_t sym) {
+        switch (k) {
+            case 0: encode(v[0], sym); break;
+            case 1: encode(v[1], sym); break;
+            case 2: encode(v[2], sym); break;
+            default: encode(v[3], sym); break;
+        }
+    };
     int64_t ip = n;
     uint32_t s = ns - (n % ns);
-    for (uint32_t k = 0; k < ns; k++) v[(s++) % ns] = initState(t.src[--ip]);
-    for (uint32_t k = 0; k < n % ns; k++) encode(v[(s++) % ns], t.src[--ip]);
+    for (uint32_t k = 0; k < ns; k++) initAt((s++) % ns, t.src[--ip]);
+    for (uint32_t k = 0; k < n % ns; k++) encodeAt((s++) % ns, t.src[--ip]);
     // ip is a multiple of nbStates now: four symbols per word, states in
     // turn. One transition of state x for symbol y: nbOut = (x + dnb[y]) >>
     // 16, its field is the low nbOut bits of x, its next state st[(x >>
@@ -643,7 +663,12 @@ __global__ void __launch_bounds__(32) kFseEnc(const FseEncTask* __restrict__ tas
         encode(v[0], t.src[ip - 1]);
         encode(v[1], t.src[ip - 2]);
     }
-    for (uint32_t k = 0; k < ns; k++) bo.add(v[k], t.tableLog);
+    bo.add(v[0], t.tableLog);
+    bo.add(v[1], t.tableLog);
+    if (ns == 4) {
+        bo.add(v[2], t.tableLog);
+        bo.add(v[3], t.tableLog);
+    }
     sizes[t.sizeSlot] = bo.close();
 }
 
