@@ -133,6 +133,7 @@ struct Job {
     uint32_t sizeSlot = 0;
     uint32_t sizes[4] = { 0, 0, 0, 0 };
     const uint8_t* dTable = nullptr;
+    uint16_t* dFields = nullptr; // long FSE chunks: the per-state encoders' fields
     // 16-bit chunks (struct of 2-byte values)
     bool wide = false;
     unsigned maxSym16 = 0, card16 = 0;
@@ -1602,6 +1603,9 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                         J.dTable = table;
                         J.dNorm = b.take(2 * 256, 16);
                         J.dNcount = b.take(600, 16);
+                        J.dFields = J.nbStates == 4 && J.n >= kFseLongMin
+                                        ? reinterpret_cast<uint16_t*>(b.take(fseFieldBytes(uint32_t(J.n)), 16))
+                                        : nullptr;
                         const uint8_t* const hist = staged(J.hist.count, 1024, 1024);
                         J.sizeSlot = nbSizes++;
                         J.ncountSlot = nbSizes++;
@@ -1609,7 +1613,8 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                             fseTabT.push_back(FseTableTask{ reinterpret_cast<const uint32_t*>(hist), J.n, table,
                                                             reinterpret_cast<int16_t*>(J.dNorm), J.dNcount,
                                                             J.hist.maxSym, J.tl, J.ncountSlot, 0 });
-                            fseT.push_back(FseEncTask{ src, J.out, J.dTable, uint32_t(J.n), J.sizeSlot, J.nbStates, J.tl });
+                            fseT.push_back(FseEncTask{ src, J.out, J.dTable, uint32_t(J.n), J.sizeSlot, J.nbStates, J.tl,
+                                                       J.dFields });
                         }
                         break;
                     }
@@ -1660,6 +1665,9 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         // longest chains start at once and the short ones fill around them
         // (each task writes its own output and size slot)
         std::stable_sort(fseT.begin(), fseT.end(), [](const FseEncTask& a, const FseEncTask& c) { return a.n > c.n; });
+        // long chunks (one lane per state) are the first nbLong of fseT
+        size_t nbLong = 0;
+        while (nbLong < fseT.size() && fseT[nbLong].fields) nbLong++;
         std::stable_sort(hufT.begin(), hufT.end(), [](const HufEncTask& a, const HufEncTask& c) { return a.n > c.n; });
         parallelFor(ups.size(), [&](size_t k) {
             std::memcpy(I.stage.p + (ups[k].dev - stg.base), ups[k].host, ups[k].bytes);
@@ -1709,10 +1717,12 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             launches_++;
         }
         launchFseTables(dFseTab, uint32_t(fseTabT.size()), dSizes, dTabErr, st);
-        launchFseEnc(dFse, uint32_t(fseT.size()), dSizes, st);
+        launchFseEncLong(dFse, uint32_t(nbLong), dSizes, st);
+        launchFseEnc(dFse + nbLong, uint32_t(fseT.size() - nbLong), dSizes, st);
         launchHufEnc(dHuf, uint32_t(hufT.size()), dSizes, st);
         launchPack(dPack, dPackTiles, uint32_t(packTiles.size()), st);
-        launches_ += (fseT.empty() ? 0 : 2) + (hufT.empty() ? 0 : 1) + (packTiles.empty() ? 0 : 1);
+        launches_ += (fseT.empty() ? 0 : 1) + (nbLong ? 2 : 0) + (fseT.size() > nbLong ? 1 : 0)
+                     + (hufT.empty() ? 0 : 1) + (packTiles.empty() ? 0 : 1);
         std::vector<uint32_t> hs(nbSizes + 1);
         uint32_t tabErr = 0;
         if (nbSizes) cudaMemcpyAsync(hs.data(), dSizes, nbSizes * 4, cudaMemcpyDeviceToHost, st);

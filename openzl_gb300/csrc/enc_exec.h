@@ -17,6 +17,8 @@ void launchHist(const HistTask* t, uint32_t n, uint32_t* hists, cudaStream_t s);
 // normalization sets errors[0].
 void launchFseTables(const FseTableTask* t, uint32_t n, uint32_t* sizes, uint32_t* errors, cudaStream_t s);
 void launchFseEnc(const FseEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);
+// chunks with a fields scratch (four states, kFseLongMin symbols or more)
+void launchFseEncLong(const FseEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);
 // Huffman code lengths, codes and weights of each chunk.
 void launchHufTables(const HufTableTask* t, uint32_t n, cudaStream_t s);
 void launchHufEnc(const HufEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s);

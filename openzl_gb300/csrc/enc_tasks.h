@@ -68,7 +68,13 @@ struct FseEncTask {
     uint32_t sizeSlot;       // where the bitstream size is written
     uint32_t nbStates;
     uint32_t tableLog;
+    uint16_t* fields;        // chunks of kFseLongMin symbols or more: fseFieldBytes(n) of scratch
 };
+// Chunks of four states and at least this many symbols encode with one lane
+// per state (kFseEncStates, then kFseEncPack); shorter ones one lane each.
+constexpr uint32_t kFseLongMin = 4096;
+// scratch of a long chunk: one 16-bit entry per field, padded to 8 bytes
+inline size_t fseFieldBytes(uint32_t n) { return 2 * ((size_t(n) + 3) & ~size_t(3)) + 16; }
 
 struct HufEncTask {
     const uint8_t* src;

@@ -672,6 +672,158 @@ __global__ void __launch_bounds__(32) kFseEnc(const FseEncTask* __restrict__ tas
     sizes[t.sizeSlot] = bo.close();
 }
 
+// FSE, long chunks (four states, kFseLongMin symbols or more), in two
+// launches. The four states' chains are independent: only the order in which
+// their fields are appended couples them.
+//  - kFseEncStates: four lanes per chunk, lane k running state k's chain. It
+//    writes one 16-bit entry per transition (the field in bits 0-11, its
+//    width in bits 12-15) at the field's index in append order, and after its
+//    last transition its state's flush (tableLog bits) at index n - 4 + k. A
+//    chunk's n entries are then its bitstream's fields in order.
+//  - kFseEncPack: one warp per chunk appends the entries, 128 per round (four
+//    per lane): a warp scan of the lanes' widths places them, they are ORed
+//    into a window of words in shared memory, and the complete words go out
+//    (a word only when it fits the capacity, as in the one-lane encoder);
+//    then the end mark and the last bytes.
+// The bytes equal kFseEnc's for the same chunk.
+constexpr uint32_t kFseStChunks = 8; // chunks per CTA (one warp, four lanes each)
+constexpr uint32_t kFseStSlot = kFseLaneTables + 4 * 16 * kEncRing;
+static_assert(kFseStSlot % 16 == 0, "16-byte aligned rings");
+
+__global__ void __launch_bounds__(32) kFseEncStates(const FseEncTask* __restrict__ tasks, uint32_t nbTasks)
+{
+    extern __shared__ __align__(16) uint8_t smemFseSt[];
+    uint32_t const lane = threadIdx.x, g = lane >> 2, k = lane & 3u;
+    uint32_t const ti = blockIdx.x * kFseStChunks + g;
+    if (ti >= nbTasks) return; // the four lanes of a group leave together
+    unsigned const gm = 0xFu << (4 * g);
+    FseEncTask const t = tasks[ti];
+    uint8_t* const base = smemFseSt + size_t(g) * kFseStSlot;
+    uint32_t* const dnb = reinterpret_cast<uint32_t*>(base);
+    int32_t* const dfs = reinterpret_cast<int32_t*>(base + 1024);
+    uint16_t* const st = reinterpret_cast<uint16_t*>(base + 2048);
+    const ent::FseCTable* ct = reinterpret_cast<const ent::FseCTable*>(t.ctable);
+    for (uint32_t y = k; y < 256; y += 4) {
+        dnb[y] = ct->deltaNbBits[y];
+        dfs[y] = ct->deltaFindState[y];
+    }
+    uint32_t const size = 1u << t.tableLog;
+    for (uint32_t u = k; u < size; u += 4) st[u] = ct->state[u];
+    __syncwarp(gm);
+
+    uint32_t const n = t.n, r = n & 3u, s0 = 4u - r;
+    // the c-th symbol from the end belongs to state (s0 + c) % 4; the last
+    // four symbols start the states and emit nothing
+    uint32_t const cInit = (k + 4u - (s0 & 3u)) & 3u;
+    uint32_t v;
+    {
+        uint32_t const y = t.src[n - 1 - cInit];
+        uint32_t const nbOut = (dnb[y] + (1u << 15)) >> 16;
+        uint32_t const x = (nbOut << 16) - dnb[y];
+        v = st[(x >> nbOut) + dfs[y]];
+    }
+    auto trans = [&](uint32_t y) -> uint32_t {
+        uint32_t const nb = (v + dnb[y]) >> 16;
+        uint32_t const e = (v & ((1u << nb) - 1u)) | (nb << 12);
+        v = st[(v >> nb) + dfs[y]];
+        return e;
+    };
+    uint16_t* const fo = t.fields;
+    for (uint32_t c = 4; c < 4 + r; c++) // the n % 4 single symbols, fields 0 .. r - 1
+        if (((s0 + c) & 3u) == k) fo[c - 4] = uint16_t(trans(t.src[n - 1 - c]));
+    // then four symbols per word (its top byte for state 0), fields
+    // r + 4 t + k of step t
+    uint32_t ip = n - 4 - r;
+    if (ip) {
+        BackWords bw;
+        bw.start(t.src, n, ip, reinterpret_cast<uint32_t*>(base + kFseLaneTables) + k * 4 * kEncRing);
+        uint32_t const shift = 24 - 8 * k;
+        for (uint32_t f = r + k; ip; ip -= 4, f += 4) {
+            uint32_t const w = bw.next();
+            fo[f] = uint16_t(trans((w >> shift) & 0xffu));
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory"); // no copy outlives the lane
+    }
+    fo[n - 4 + k] = uint16_t((v & (size - 1u)) | (t.tableLog << 12));
+}
+
+constexpr uint32_t kFsePackWarps = 4;
+
+__global__ void __launch_bounds__(32 * kFsePackWarps) kFseEncPack(const FseEncTask* __restrict__ tasks,
+                                                                   uint32_t nbTasks, uint32_t* __restrict__ sizes)
+{
+    // 64-word windows: a round places at most 128 x 12 bits (48 words) above
+    // the partial word carried from the round before
+    __shared__ uint32_t win[kFsePackWarps][64];
+    uint32_t const lane = threadIdx.x & 31u, wi = threadIdx.x >> 5;
+    uint32_t const ti = blockIdx.x * kFsePackWarps + wi;
+    if (ti >= nbTasks) return; // the whole warp
+    FseEncTask const t = tasks[ti];
+    uint32_t* const w = win[wi];
+    w[lane] = 0;
+    w[lane + 32] = 0;
+    __syncwarp();
+    uint32_t const n = t.n, cap = t.n + t.n / 128 + 512; // the one-lane encoder's capacity
+    uint8_t* const out = t.out;
+    uint32_t B = 0, wb = 0; // bits placed; first word not written yet
+    auto flushWords = [&](uint32_t upTo) { // words [wb, upTo) are complete
+        for (uint32_t q = wb + lane; q < upTo; q += 32) {
+            uint32_t const x = w[q & 63u];
+            w[q & 63u] = 0;
+            if (4 * q + 4 <= cap) *reinterpret_cast<uint32_t*>(out + 4 * q) = x;
+        }
+        __syncwarp();
+        wb = upTo;
+    };
+    const uint2* const src = reinterpret_cast<const uint2*>(t.fields);
+    uint32_t const nw = (n + 3) >> 2; // entries in groups of four
+    uint2 d = lane < nw ? src[lane] : make_uint2(0u, 0u);
+    for (uint32_t i0 = 0; i0 < nw; i0 += 32) {
+        uint2 const cur = d;
+        uint32_t const inext = i0 + 32 + lane;
+        d = inext < nw ? src[inext] : make_uint2(0u, 0u); // the next round's entries, in flight
+        uint32_t const j = 4 * (i0 + lane);
+        uint32_t e0 = cur.x & 0xffffu, e1 = cur.x >> 16, e2 = cur.y & 0xffffu, e3 = cur.y >> 16;
+        if (j + 0 >= n) e0 = 0;
+        if (j + 1 >= n) e1 = 0;
+        if (j + 2 >= n) e2 = 0;
+        if (j + 3 >= n) e3 = 0;
+        uint32_t const sum = (e0 >> 12) + (e1 >> 12) + (e2 >> 12) + (e3 >> 12);
+        uint32_t inc = sum;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            uint32_t const y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        uint32_t p = B + inc - sum;
+        auto place = [&](uint32_t e) {
+            uint32_t const nb = e >> 12, f = e & 0xfffu;
+            if (nb) {
+                uint32_t const q = p >> 5, sh = p & 31u;
+                atomicOr(&w[q & 63u], f << sh);
+                if (sh + nb > 32) atomicOr(&w[(q + 1) & 63u], f >> (32 - sh));
+            }
+            p += nb;
+        };
+        place(e0);
+        place(e1);
+        place(e2);
+        place(e3);
+        B += __shfl_sync(0xffffffffu, inc, 31);
+        __syncwarp();
+        flushWords(B >> 5);
+    }
+    // the end mark; a word it completes goes out as a word, then the bytes
+    if (lane == 0) w[(B >> 5) & 63u] |= 1u << (B & 31u);
+    B += 1;
+    __syncwarp();
+    flushWords(B >> 5);
+    uint32_t const bytes = (B + 7) >> 3;
+    for (uint32_t b = 4 * wb + lane; b < bytes; b += 32)
+        if (b < cap) out[b] = uint8_t(w[(b >> 2) & 63u] >> (8 * (b & 3u)));
+    if (lane == 0) sizes[t.sizeSlot] = bytes;
+}
+
 // Huffman: one lane per stream (4 per chunk for 4X); symbols are appended
 // from the end of the stream to its start. Each stream writes at its own
 // offset of the chunk buffer; the frame assembly joins them.
@@ -1029,8 +1181,11 @@ __global__ void __launch_bounds__(256) kTokEmit(const TokTask* __restrict__ task
 
 cudaError_t prepareEncodeKernels()
 {
-    return cudaFuncSetAttribute(kFseEnc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(kFseEncLanes * kFseLaneBytes));
+    cudaError_t const e = cudaFuncSetAttribute(kFseEnc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               int(kFseEncLanes * kFseLaneBytes));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(kFseEncStates, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(kFseStChunks * kFseStSlot));
 }
 
 uint32_t hufEncStreamCap(uint32_t seg) { return ((seg + (seg >> 3) + 64) + 15) & ~15u; }
@@ -1065,6 +1220,12 @@ void launchHufTables(const HufTableTask* t, uint32_t n, cudaStream_t s)
 void launchFseEnc(const FseEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s)
 {
     if (n) kFseEnc<<<(n + kFseEncLanes - 1) / kFseEncLanes, 32, kFseEncLanes * kFseLaneBytes, s>>>(t, n, sizes);
+}
+void launchFseEncLong(const FseEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s)
+{
+    if (!n) return;
+    kFseEncStates<<<(n + kFseStChunks - 1) / kFseStChunks, 32, kFseStChunks * kFseStSlot, s>>>(t, n);
+    kFseEncPack<<<(n + kFsePackWarps - 1) / kFsePackWarps, 32 * kFsePackWarps, 0, s>>>(t, n, sizes);
 }
 void launchHufEnc(const HufEncTask* t, uint32_t n, uint32_t* sizes, cudaStream_t s)
 {
