@@ -939,6 +939,13 @@ def main():
     time.sleep(0.3)
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
+    # The K steps queue behind a 0.1 s device-side delay (a bounded clock
+    # spin, before the timed region), so that a pause of the host thread
+    # (driver queries of the clock sampler have stalled graph launches for
+    # milliseconds) cannot open gaps between the steps: the timed region is
+    # the device's time for exactly K steps.
+    with torch.cuda.stream(stream):
+        torch.cuda._sleep(int(0.1 * 2.07e9))
     t_start.record(stream)
     for k in range(args.steps):
         ev[k][0].record(stream)
@@ -1089,7 +1096,8 @@ def main():
         "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded random walks)",
-        "config": workload_config(n_frames, total_out, total_comp, args.parts_per_kind),
+        "config": dict(workload_config(n_frames, total_out, total_comp, args.parts_per_kind),
+                       launch="the K timed steps are queued behind a 0.1 s device-side delay before the first event"),
         "frac_hbm": round(value / ws / peak, 4),
         "p50_ms": round(statistics.median(step_ms), 4),
         "p99_ms": round(srt[min(len(srt) - 1, int(round(0.99 * (len(srt) - 1))))], 4),

@@ -732,15 +732,31 @@ __global__ void __launch_bounds__(32) kFseEncStates(const FseEncTask* __restrict
     for (uint32_t c = 4; c < 4 + r; c++) // the n % 4 single symbols, fields 0 .. r - 1
         if (((s0 + c) & 3u) == k) fo[c - 4] = uint16_t(trans(t.src[n - 1 - c]));
     // then four symbols per word (its top byte for state 0), fields
-    // r + 4 t + k of step t
+    // r + 4 t + k of step t. The next step's symbol and its two per-symbol
+    // entries do not depend on the state: they load while the state's
+    // next-state load is in flight, so a transition's chain is one shared
+    // load and a few integer operations.
     uint32_t ip = n - 4 - r;
     if (ip) {
         BackWords bw;
         bw.start(t.src, n, ip, reinterpret_cast<uint32_t*>(base + kFseLaneTables) + k * 4 * kEncRing);
         uint32_t const shift = 24 - 8 * k;
-        for (uint32_t f = r + k; ip; ip -= 4, f += 4) {
-            uint32_t const w = bw.next();
-            fo[f] = uint16_t(trans((w >> shift) & 0xffu));
+        uint32_t y = (bw.next() >> shift) & 0xffu;
+        uint32_t a = dnb[y];
+        int32_t b = dfs[y];
+        for (uint32_t f = r + k;; f += 4) {
+            uint32_t const nb = (v + a) >> 16;
+            uint32_t const e = (v & ((1u << nb) - 1u)) | (nb << 12);
+            uint32_t const next = (v >> nb) + b;
+            ip -= 4;
+            if (ip) {
+                y = (bw.next() >> shift) & 0xffu;
+                a = dnb[y];
+                b = dfs[y];
+            }
+            v = st[next];
+            fo[f] = uint16_t(e);
+            if (!ip) break;
         }
         asm volatile("cp.async.wait_all;" ::: "memory"); // no copy outlives the lane
     }
