@@ -515,11 +515,9 @@ ZL_Report ozl_gpu_xxh3_64(const void* d_data, size_t len, void* stream);
  * every GPU that loads the library holds that array until the process exits.
  * Accepts at most OZL_XXH3_STATIC_MAX_LEN bytes; longer inputs return
  * ZL_ErrorCode_srcSize_tooLarge without touching the device. Calls no
- * allocating routine. The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress, with that device current) and keeps it, so
- * make that first call before any stream capture; the address belongs to the
- * device's primary context, so after a cudaDeviceReset this entry point must
- * not be called again in the same process. Every call on a device shares the
+ * allocating routine: each call looks up the array's device address in the
+ * current device's context (cudaGetSymbolAddress), so the entry point stays
+ * valid across a cudaDeviceReset. Every call on a device shares the
  * array and the array keeps the last call's contents (what must start at
  * zero is cleared by each call): calls whose work overlaps on the GPU (other
  * streams, other host threads) race and must be serialized by the caller.

@@ -2239,8 +2239,6 @@ cudaError_t xxh3Device(const uint8_t* data, uint64_t len, uint64_t* dHashOut, ui
 // Calls that overlap on the GPU share the array and race.
 #include "../../include/openzl_gb300.h"
 
-#include <mutex>
-
 namespace {
 
 constexpr uint64_t kStaticMaxLen = OZL_XXH3_STATIC_MAX_LEN;
@@ -2263,29 +2261,15 @@ __global__ void kStageHashStatic(ozl::HashTask t, ozl::HashTask* dTask, ozl::Til
     if (i < nbBlocks) dBlocks[i] = ozl::TileRef{ 0, i };
 }
 
-constexpr int kMaxDevices = 64;
-std::mutex gStaticMu;
-uint8_t* gStaticPtr[kMaxDevices] = {};
-
-// Device address of the array on the current device, looked up by the first
-// call on that device (with that device current) and kept. The address
-// belongs to the device's primary context: a cudaDeviceReset by the host
-// application unloads the module, and the entry point is not to be called
-// after one (the header says so).
+// Device address of the array in the current device's context, looked up on
+// every call (no allocation): a cached address would go stale if the host
+// application reset the device and the module reloaded elsewhere.
 cudaError_t staticScratch(uint8_t** out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    cudaError_t const e = cudaGetSymbolAddress(&p, gXxh3Scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lk(gStaticMu);
-    if (!gStaticPtr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, gXxh3Scratch);
-        if (e != cudaSuccess) return e;
-        gStaticPtr[dev] = static_cast<uint8_t*>(p);
-    }
-    *out = gStaticPtr[dev];
+    *out = static_cast<uint8_t*>(p);
     return cudaSuccess;
 }
 
