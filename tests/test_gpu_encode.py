@@ -92,6 +92,35 @@ def test_gpu_frames_equal_oracle_frames(gpu_lib, checksums):
     assert not bad, bad[:10]
 
 
+def test_fse_chunks_around_the_per_state_threshold(gpu_lib):
+    """Serial inputs through the FSE graph: lengths around 4,096 symbols (from
+    there a chunk's four states run on four lanes and a warp packs their
+    fields), every length mod 4, around the 32 KiB chunks and the
+    100,000-symbol chunking threshold; bytes from two symbols to all 256.
+    Frames equal the oracle's byte for byte."""
+    import torch
+    import openzl_gb300 as oz
+
+    rng = np.random.default_rng(4096)
+    lengths = list(range(4092, 4101)) + [6001, 32767, 32768, 32769, 65539, 99999, 100000, 100001, 100003, 131074]
+    cases = []
+    for n in lengths:
+        cases.append((rng.random(n) < 0.02).astype(np.uint8))                       # two symbols, skewed
+        cases.append((rng.zipf(1.3, n) % 5).astype(np.uint8))
+        cases.append((rng.zipf(1.1, n) % 256).astype(np.uint8))
+        cases.append(np.minimum(rng.geometric(0.05, n), 255).astype(np.uint8))
+        cases.append(rng.integers(0, 256, n).astype(np.uint8))                      # near uniform
+    enc = oz.GpuEncoder()
+    srcs = [torch.from_numpy(a.copy()).cuda() for a in cases]
+    caps = [enc.bound(a.nbytes) for a in cases]
+    dsts = [torch.zeros(c, dtype=torch.uint8, device="cuda") for c in caps]
+    sizes = enc.compress_batch([x.data_ptr() for x in srcs], [a.nbytes for a in cases], [0] * len(cases),
+                               [7] * len(cases), [d.data_ptr() for d in dsts], caps, checksums=True)
+    bad = [(k, a.size) for k, (a, d, sz) in enumerate(zip(cases, dsts, sizes))
+           if d[:sz].cpu().numpy().tobytes() != oracle.compress(7, a, 0).tobytes()]
+    assert not bad, bad[:10]
+
+
 def test_gpu_encode_then_gpu_decode(gpu_lib):
     import torch
     import openzl_gb300 as oz
