@@ -42,8 +42,11 @@ def build(force=False, verbose=False):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     nvcc = _nvcc()
+    # host code: no fused multiply-add contraction, so that the encoder's
+    # double-precision codec decisions round as on a machine without FMA (the
+    # reference's x86-64 build) on every host, Arm included
     common = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-              "-I", os.path.join(ROOT, "include")]
+              "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(ROOT, "include")]
 
     def compile_one(src):
         obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
