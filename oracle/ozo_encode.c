@@ -440,10 +440,40 @@ static size_t fse_compress(uint8_t* dst, size_t cap, const uint8_t* src, size_t 
     size_t s = nbStates - (n % nbStates);
     for (unsigned i = 0; i < nbStates; i++) fse_init_state2(&st[(s++) % nbStates], ct, *--ip);
     for (size_t i = 0; i < n % nbStates; i++) fse_encode_symbol(&b, &st[(s++) % nbStates], ct, *--ip);
-    s = 0;
-    while (ip > src)
-        for (unsigned i = 0; i < nbStates; i++) fse_encode_symbol(&b, &st[(s++) % nbStates], ct, *--ip);
-    for (unsigned i = 0; i < nbStates; i++) bw_add(&b, st[(s++) % nbStates].value, ct->tl);
+    /* ip - src is a multiple of nbStates now: rounds of one symbol per
+     * state, state 0 first. A field has at most 12 bits, so a round appends
+     * at most 48 bits after one flush check. */
+#define OZO_FSE_ENC(v)                                                                  \
+    do {                                                                                \
+        unsigned const y_ = *--ip;                                                      \
+        uint32_t const nb_ = (uint32_t)(((v) + ct->deltaNbBits[y_]) >> 16);             \
+        b.acc |= ((v) & ((1ull << nb_) - 1)) << b.nb;                                   \
+        b.nb += nb_;                                                                    \
+        (v) = ct->state[((v) >> nb_) + ct->deltaFindState[y_]];                         \
+    } while (0)
+    uint64_t v0 = st[0].value, v1 = st[1].value;
+    if (nbStates == 4) {
+        uint64_t v2 = st[2].value, v3 = st[3].value;
+        while (ip > src) {
+            if (b.nb > 16) bw_flush(&b);
+            OZO_FSE_ENC(v0);
+            OZO_FSE_ENC(v1);
+            OZO_FSE_ENC(v2);
+            OZO_FSE_ENC(v3);
+        }
+        st[2].value = v2;
+        st[3].value = v3;
+    } else {
+        while (ip > src) {
+            if (b.nb > 40) bw_flush(&b);
+            OZO_FSE_ENC(v0);
+            OZO_FSE_ENC(v1);
+        }
+    }
+#undef OZO_FSE_ENC
+    st[0].value = v0;
+    st[1].value = v1;
+    for (unsigned i = 0; i < nbStates; i++) bw_add(&b, st[i].value, ct->tl);
     return bw_close(&b);
 }
 
@@ -703,7 +733,18 @@ static unsigned huf_build_ctable(HufC* ct, const unsigned* count, unsigned maxSV
 static size_t huf_compress1x(uint8_t* dst, size_t cap, const uint8_t* src, size_t n, const HufC* ct)
 {
     BW b = { dst, cap, 0, 0, 0 };
-    for (size_t i = n; i > 0; i--) bw_add(&b, ct->value[src[i - 1]], ct->nbBits[src[i - 1]]);
+    size_t i = n;
+    /* codes of at most 12 bits (values hold no bits above their length):
+     * four per flush check */
+    for (; i >= 4; i -= 4) {
+        if (b.nb > 16) bw_flush(&b);
+        for (int k = 1; k <= 4; k++) {
+            unsigned const y = src[i - (size_t)k];
+            b.acc |= (uint64_t)ct->value[y] << b.nb;
+            b.nb += ct->nbBits[y];
+        }
+    }
+    for (; i > 0; i--) bw_add(&b, ct->value[src[i - 1]], ct->nbBits[src[i - 1]]);
     return bw_close(&b);
 }
 
@@ -1066,25 +1107,43 @@ static int node_bitpack(ECtx* c, int in, unsigned trid)
     nd->nbOut = 1;
     uint8_t* d = S(o)->data;
     memset(d, 0, dstSize + 8);
-    /* LSB-first: fields go into a 128-bit accumulator above the bits not yet
-     * written; whole 64-bit words are flushed */
-    unsigned __int128 acc = 0;
-    unsigned nacc = 0;
+    /* LSB-first: fields go into an accumulator above the bits not yet
+     * written; whole words are flushed. Fields of at most 32 bits use a
+     * 64-bit accumulator (32-bit flushes), wider ones a 128-bit one. */
     uint8_t* q = d;
-    for (size_t i = 0; i < n; i++) {
-        uint64_t const v = rd(S(in)->data + i * w, w);
-        acc |= (unsigned __int128)v << nacc;
-        nacc += (unsigned)nbBits;
-        if (nacc >= 64) {
-            ozo_wr64(q, (uint64_t)acc);
-            q += 8;
-            acc >>= 64;
-            nacc -= 64;
+    if (nbBits <= 32) {
+        uint64_t acc = 0;
+        unsigned nacc = 0;
+#define OZO_PACK32(READ)                                      for (size_t i = 0; i < n; i++) {                              acc |= (uint64_t)(READ) << nacc;                          nacc += (unsigned)nbBits;                                 if (nacc >= 32) {                                             ozo_wr32(q, (uint32_t)acc);                               q += 4;                                                   acc >>= 32;                                               nacc -= 32;                                           }                                                     }
+        switch (w) {
+            case 1: OZO_PACK32(x[i]) break;
+            case 2: OZO_PACK32(ozo_rd16(x + 2 * i)) break;
+            case 4: OZO_PACK32(ozo_rd32(x + 4 * i)) break;
+            default: OZO_PACK32(rd(x + i * w, w)) break;
         }
-    }
-    for (; nacc > 0; nacc = nacc > 8 ? nacc - 8 : 0) {
-        *q++ = (uint8_t)acc;
-        acc >>= 8;
+#undef OZO_PACK32
+        for (; nacc > 0; nacc = nacc > 8 ? nacc - 8 : 0) {
+            *q++ = (uint8_t)acc;
+            acc >>= 8;
+        }
+    } else {
+        unsigned __int128 acc = 0;
+        unsigned nacc = 0;
+        for (size_t i = 0; i < n; i++) {
+            uint64_t const v = rd(x + i * w, w);
+            acc |= (unsigned __int128)v << nacc;
+            nacc += (unsigned)nbBits;
+            if (nacc >= 64) {
+                ozo_wr64(q, (uint64_t)acc);
+                q += 8;
+                acc >>= 64;
+                nacc -= 64;
+            }
+        }
+        for (; nacc > 0; nacc = nacc > 8 ? nacc - 8 : 0) {
+            *q++ = (uint8_t)acc;
+            acc >>= 8;
+        }
     }
     size_t const maxN = dstSize * 8 / (size_t)nbBits;
     static const uint8_t lg[9] = { 0, 0, 1, 0, 2, 0, 0, 0, 3 };
@@ -1169,15 +1228,13 @@ static int node_flatpack(ECtx* c, int in)
     int p = new_stream(c, OZO_TYPE_SERIAL, 1, packed, NULL);
     nd->nbOut = 2;
     if (n) {
+        /* LSB-first indices, then the marker bit: 1 + nbBits * n / 8 bytes */
         uint8_t* d = S(p)->data;
-        memset(d, 0, packed + 8);
-        size_t bit = 0;
-        for (size_t i = 0; i < n; i++) {
-            unsigned v = map[S(in)->data[i]];
-            for (unsigned b = 0; b < nbBits; b++, bit++)
-                if ((v >> b) & 1) d[bit >> 3] |= (uint8_t)(1u << (bit & 7));
-        }
-        d[bit >> 3] |= (uint8_t)(1u << (bit & 7));
+        memset(d + packed, 0, 8);
+        BW b = { d, packed + 8, 0, 0, 0 };
+        const uint8_t* const src = S(in)->data;
+        for (size_t i = 0; i < n; i++) bw_add(&b, map[src[i]], nbBits);
+        bw_close(&b);
     }
     return a;
 }
