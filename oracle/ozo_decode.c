@@ -739,13 +739,17 @@ static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, s
             if (W == 2 || W == 4 || W == 8) { /* element-major: one pass over the output */
                 const uint8_t* pl[8];
                 for (size_t b = 0; b < W; b++) pl[b] = in[b]->p;
-                for (size_t e = 0; e < n; e++) {
-                    uint64_t v = 0;
-                    for (size_t b = 0; b < W; b++) v |= (uint64_t)pl[b][e] << (8 * b);
-                    if (W == 2) ozo_wr16(o + 2 * e, (uint16_t)v);
-                    else if (W == 4) ozo_wr32(o + 4 * e, (uint32_t)v);
-                    else ozo_wr64(o + 8 * e, v);
-                }
+                /* the plane count as a constant, so the gather unrolls */
+#define OZO_TSPLIT_W(NW, WR)                                                   \
+    for (size_t e = 0; e < n; e++) {                                          \
+        uint64_t v = 0;                                                       \
+        for (size_t b = 0; b < (NW); b++) v |= (uint64_t)pl[b][e] << (8 * b); \
+        WR;                                                                   \
+    }
+                if (W == 2) OZO_TSPLIT_W(2, ozo_wr16(o + 2 * e, (uint16_t)v))
+                else if (W == 4) OZO_TSPLIT_W(4, ozo_wr32(o + 4 * e, (uint32_t)v))
+                else OZO_TSPLIT_W(8, ozo_wr64(o + 8 * e, v))
+#undef OZO_TSPLIT_W
                 return 0;
             }
             for (size_t b = 0; b < W; b++) {
@@ -871,10 +875,12 @@ static int dec_run(unsigned id, OStream** in, size_t nbIn, const uint8_t* hdr, s
             }
             uint8_t* o = ost_alloc(out, OZO_TYPE_SERIAL, 1, n);
             size_t bit = 0;
-            for (size_t i = 0; i < n; i++) {
-                unsigned idx = 0;
-                for (unsigned b = 0; b < nbBits; b++, bit++)
-                    idx |= (unsigned)((packed->p[bit >> 3] >> (bit & 7)) & 1) << b;
+            /* an index of at most 8 bits lies in the two bytes from bit >> 3 */
+            unsigned const mask = (1u << nbBits) - 1u;
+            for (size_t i = 0; i < n; i++, bit += nbBits) {
+                size_t const q = bit >> 3;
+                unsigned const win = packed->p[q] | (q + 1 < psz ? (unsigned)packed->p[q + 1] << 8 : 0u);
+                unsigned const idx = (win >> (bit & 7)) & mask;
                 if (idx >= asz) return -OZO_ERR_CORRUPTION;
                 o[i] = alpha->p[idx];
             }

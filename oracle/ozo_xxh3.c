@@ -56,14 +56,17 @@ static uint64_t mix16(const uint8_t* in, const uint8_t* sec)
 {
     return fold128(ozo_rd64(in) ^ ozo_rd64(sec), ozo_rd64(in + 8) ^ ozo_rd64(sec + 8));
 }
-static void accumulate512(uint64_t acc[8], const uint8_t* in, const uint8_t* sec)
+/* lane i gains the neighbouring lane's input word and the product of its
+ * own keyed word's halves; the stripe is loaded first and each lane updated
+ * once, so the compiler can vectorize the eight lanes */
+static inline void accumulate512(uint64_t acc[8], const uint8_t* in, const uint8_t* sec)
 {
+    uint64_t v[8], k[8];
     for (int i = 0; i < 8; i++) {
-        uint64_t v = ozo_rd64(in + 8 * i);
-        uint64_t k = v ^ ozo_rd64(sec + 8 * i);
-        acc[i ^ 1] += v;
-        acc[i] += (uint64_t)(uint32_t)k * (k >> 32);
+        v[i] = ozo_rd64(in + 8 * i);
+        k[i] = v[i] ^ ozo_rd64(sec + 8 * i);
     }
+    for (int i = 0; i < 8; i++) acc[i] += v[i ^ 1] + (uint64_t)(uint32_t)k[i] * (k[i] >> 32);
 }
 static void scramble(uint64_t acc[8], const uint8_t* sec)
 {
