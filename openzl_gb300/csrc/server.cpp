@@ -32,6 +32,7 @@
 #include "../../include/openzl_gb300.h"
 #include "decode_batch.h"
 #include "enc_engine.h"
+#include "pool_blocks.h"
 
 namespace {
 
@@ -56,52 +57,6 @@ struct Request {
     double latencyUs;
 };
 
-// First-fit allocator of the shared pool's byte range (host bookkeeping;
-// the caller holds the server lock). Free blocks by offset, merged with their
-// neighbours when returned.
-struct PoolBlocks {
-    std::map<size_t, size_t> free; // offset -> bytes
-    void reset(size_t bytes)
-    {
-        free.clear();
-        if (bytes) free.emplace(0, bytes);
-    }
-    size_t largest() const
-    {
-        size_t m = 0;
-        for (auto& f : free) m = f.second > m ? f.second : m;
-        return m;
-    }
-    bool take(size_t bytes, size_t& off)
-    {
-        for (auto it = free.begin(); it != free.end(); ++it) {
-            if (it->second < bytes) continue;
-            off = it->first;
-            size_t const rest = it->second - bytes;
-            free.erase(it);
-            if (rest) free.emplace(off + bytes, rest);
-            return true;
-        }
-        return false;
-    }
-    void give(size_t off, size_t bytes)
-    {
-        auto it = free.emplace(off, bytes).first;
-        auto nx = std::next(it);
-        if (nx != free.end() && it->first + it->second == nx->first) {
-            it->second += nx->second;
-            free.erase(nx);
-        }
-        if (it != free.begin()) {
-            auto pv = std::prev(it);
-            if (pv->first + pv->second == it->first) {
-                pv->second += it->second;
-                free.erase(it);
-            }
-        }
-    }
-};
-
 } // namespace
 
 struct OZL_Server_s {
@@ -109,7 +64,7 @@ struct OZL_Server_s {
     size_t budget = 0;     // bytes of the shared pool
     size_t share = 0;      // batch size cap: the budget's per-worker share
     ozl::DevBuf pool;
-    PoolBlocks blocks;
+    ozl::PoolBlocks blocks;
     int nbWorkers = 0;
     int checksums = 1;
     std::mutex mu;
