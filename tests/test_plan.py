@@ -35,6 +35,21 @@ def test_fused_pipeline_shape(checker):
     assert kinds == ["kind=1", "kind=2", "kind=8", "kind=9"], kinds
 
 
+def test_mutated_frames_are_refused_or_in_bounds(checker, manifest, manifest_multi):
+    """Malformed input: 300 mutated copies of every golden frame (bytes
+    flipped, set to 0x00 or 0xFF, truncated; half the mutations in the
+    headers) are each refused by the planner or planned with every task's
+    pointers and lengths inside their allocations, under ASan/UBSan."""
+    planned = refused = 0
+    for k, m in enumerate(list(manifest) + list(manifest_multi)):
+        r = subprocess.run([checker, os.path.join(GOLDEN, m["case"] + ".zl"), "--fuzz", "300", str(k + 1)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0 and "bad=0" in r.stdout, (m["case"], r.stdout[-2000:], r.stderr[-2000:])
+        planned += int(r.stdout.split("planned=")[1].split()[0])
+        refused += int(r.stdout.split("refused=")[1].split()[0])
+    assert planned > 1000 and refused > 1000, (planned, refused)  # both outcomes exercised
+
+
 def test_multi_output_layouts_in_bounds(checker, manifest_multi):
     """Frames of several outputs: each output and, for the content checksum,
     each gathered block lie inside their allocations."""
