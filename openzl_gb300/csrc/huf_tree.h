@@ -24,7 +24,18 @@ struct HufNode {
 // 514 nodes: a sentinel, 256 leaves sorted by decreasing count, the inner nodes
 constexpr int kHufNodes = 2 * 256 + 2;
 
-OZL_HD inline uint32_t hufBucketOf(uint32_t c) { return c < 166 ? c : uint32_t(highbit32v(c)) + 158; }
+// Rank buckets of HUF_sort (huf_compress.c:484-509): counts below the
+// distinct-count cutoff have a bucket each, larger counts one per power of
+// two from bucket 158 + highbit. The cutoff is 158 + highbit32(158) = 165
+// (the reference's comment says 166; its macro arithmetic gives 165), and
+// HUF_sort quicksorts the rank buckets from 165 on: rank r holds index
+// r - 1, so the bucket of count 164 is quicksorted too, which reorders
+// equal counts.
+constexpr uint32_t kHufDistinctCutoff = 165;
+OZL_HD inline uint32_t hufBucketOf(uint32_t c)
+{
+    return c < kHufDistinctCutoff ? c : uint32_t(highbit32v(c)) + 158;
+}
 
 OZL_HD inline void hufInsertionSort(HufNode* a, int low, int high)
 {
@@ -109,7 +120,7 @@ OZL_HD inline void hufSortByCount(HufNode* node, const uint32_t* count, unsigned
         node[pos].count = count[n];
         node[pos].byte = uint8_t(n);
     }
-    for (int n = 166; n < 191; n++) {
+    for (int n = int(kHufDistinctCutoff); n < 191; n++) {
         int const size = curr[n] - base[n];
         if (size > 1) hufQuickSortDesc(node + base[n], 0, size - 1);
     }

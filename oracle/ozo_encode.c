@@ -553,7 +553,11 @@ typedef struct {
     uint8_t nbBits;
 } HNode;
 
-static uint32_t huf_index(uint32_t c) { return c < 166 ? c : (uint32_t)ozo_highbit32(c) + 158; }
+/* HUF_getIndex (huf_compress.c:484-509): the distinct-count cutoff is
+ * 158 + highbit32(158) = 165 by the reference's macro arithmetic (its
+ * comment says 166), and HUF_sort quicksorts rank buckets from 165 on, rank
+ * r holding index r - 1: the bucket of count 164 is sorted too. */
+static uint32_t huf_index(uint32_t c) { return c < 165 ? c : (uint32_t)ozo_highbit32(c) + 158; }
 
 static void huf_insertion(HNode* a, int low, int high)
 {
@@ -607,7 +611,7 @@ static void huf_sort(HNode* node, const unsigned* count, unsigned maxSV)
         node[pos].count = count[n];
         node[pos].byte = (uint8_t)n;
     }
-    for (int n = 166; n < 191; n++) {
+    for (int n = 165; n < 191; n++) {
         int const bs = rank[n].curr - rank[n].base;
         if (bs > 1) huf_quicksort(node + rank[n].base, 0, bs - 1);
     }

@@ -1,0 +1,129 @@
+// The encoder's table builders shared by host and device (fse_norm.h,
+// huf_tree.h) against the reference's own functions, compiled from its
+// sources into oracle/_ref/libozl_ref.so: on random histograms of many
+// shapes, the FSE table log (FSE_optimalTableLog_internal), normalized counts
+// (FSE_normalizeCount with low-probability counts, as
+// encode_entropy_binding.c:100-106 calls it), the normalized-count header
+// (FSE_writeNCount), and the Huffman table log, code lengths and codes
+// (HUF_buildCTable) are equal, including histograms with groups of equal
+// counts around the sort's bucket cutoff. Prints "bad=0" when every case
+// agreed.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "fse_norm.h"
+#include "huf_tree.h"
+
+extern "C" {
+unsigned ZS_FSE_optimalTableLog_internal(unsigned maxTableLog, size_t srcSize, unsigned maxSymbolValue, unsigned minus);
+size_t ZS_FSE_normalizeCount(short* norm, unsigned tableLog, const unsigned* count, size_t srcSize,
+                             unsigned maxSymbolValue, unsigned useLowProbCount);
+size_t ZS_FSE_writeNCount(void* buffer, size_t bufferSize, const short* norm, unsigned maxSymbolValue,
+                          unsigned tableLog);
+unsigned ZS_FSE_isError(size_t code);
+size_t ZS_HUF_buildCTable(size_t* CTable, const unsigned* count, unsigned maxSymbolValue, unsigned maxNbBits);
+unsigned ZS_HUF_isError(size_t code);
+}
+
+using namespace ozl::ent;
+
+int main(int argc, char** argv)
+{
+    unsigned const seed = argc > 1 ? unsigned(std::atoi(argv[1])) : 1u;
+    long const cases = argc > 2 ? std::atol(argv[2]) : 20000;
+    std::mt19937_64 rng(seed);
+    long bad = 0, fseCases = 0, hufCases = 0;
+    for (long c = 0; c < cases; c++) {
+        unsigned count[256] = {};
+        unsigned const maxSym = 1 + unsigned(rng() % 255);
+        uint64_t const total = 2 + rng() % (rng() % 4 == 0 ? 200 : 100000);
+        int const shape = int(rng() % 6);
+        double const zs = 1.0 + double(rng() % 1000) / 500.0;
+        for (uint64_t i = 0; i < total; i++) {
+            unsigned s = 0;
+            switch (shape) {
+                case 0: s = unsigned(rng() % (maxSym + 1)); break;                      // uniform
+                case 1: {                                                                // Zipf-like
+                    double const u = double(rng() % 1000000 + 1) / 1000001.0;
+                    s = unsigned(double(maxSym + 1) * std::pow(u, zs * 2.0));
+                    break;
+                }
+                case 2: { unsigned g = 0; while (g < maxSym && rng() % 3 != 0) g++; s = g; break; } // geometric
+                case 3: s = rng() % 20 ? 0u : unsigned(rng() % (maxSym + 1)); break;   // one dominant symbol
+                case 4: s = unsigned((rng() % 8) * (maxSym / 7 + 1)) % (maxSym + 1); break; // sparse
+                default: s = rng() % 2 ? unsigned(rng() % 4) : unsigned(rng() % (maxSym + 1)); break; // many rare
+            }
+            if (s > maxSym) s = maxSym;
+            count[s]++;
+        }
+        if (rng() % 4 == 0) {
+            // groups of equal counts around the bucket cutoff (9 to 40 symbols
+            // of one count in 160..170, or of a random count): the order the
+            // reference's sort leaves equal counts in decides the codes
+            uint32_t const v = rng() % 2 ? 160 + uint32_t(rng() % 11) : 1 + uint32_t(rng() % 5000);
+            unsigned const k = 9 + unsigned(rng() % 32);
+            for (unsigned q = 0; q < k; q++) count[rng() % (maxSym + 1)] = v;
+        }
+        count[maxSym] += 1; // the largest symbol is present
+        uint64_t tot = 0;
+        unsigned distinct = 0;
+        for (unsigned s = 0; s <= maxSym; s++) {
+            tot += count[s];
+            distinct += count[s] != 0;
+        }
+        if (distinct < 2) continue; // a single symbol is not entropy-coded
+        // FSE: table log (the encoder's maximum 11, and 12), counts, header
+        for (unsigned maxTL : { 11u, 12u }) {
+            unsigned const tlRef = ZS_FSE_optimalTableLog_internal(maxTL, size_t(tot), maxSym, 2);
+            unsigned const tl = fseTableLogOf(maxTL, tot, maxSym, 2);
+            if (tl != tlRef) { bad++; std::printf("BAD fse tl %u ref %u (n=%llu max=%u)\n", tl, tlRef, (unsigned long long)tot, maxSym); continue; }
+            short normRef[256] = {};
+            size_t const r = ZS_FSE_normalizeCount(normRef, tl, count, size_t(tot), maxSym, 1);
+            int16_t norm[256] = {};
+            bool const ok = fseNormalizeCounts(norm, tl, count, tot, maxSym);
+            if (ZS_FSE_isError(r) || !ok) {
+                if (ZS_FSE_isError(r) != !ok) { bad++; std::printf("BAD fse normalize outcome\n"); }
+                continue;
+            }
+            fseCases++;
+            for (unsigned s = 0; s <= maxSym; s++)
+                if (norm[s] != normRef[s]) { bad++; std::printf("BAD fse norm[%u] %d ref %d\n", s, norm[s], normRef[s]); break; }
+            uint8_t hdr[600] = {}, hdrRef[600] = {};
+            size_t const hs = fseWriteNCountTo(hdr, norm, maxSym, tl);
+            size_t const hr = ZS_FSE_writeNCount(hdrRef, sizeof hdrRef, normRef, maxSym, tl);
+            if (ZS_FSE_isError(hr) || hs != hr || std::memcmp(hdr, hdrRef, hs) != 0) { bad++; std::printf("BAD fse header %zu ref %zu\n", hs, hr); }
+        }
+        // Huffman: table log, code lengths and codes
+        {
+            unsigned const tlRef = ZS_FSE_optimalTableLog_internal(11, size_t(tot), maxSym, 1);
+            unsigned const tl = fseTableLogOf(11, tot, maxSym, 1);
+            if (tl != tlRef) { bad++; std::printf("BAD huf tl %u ref %u\n", tl, tlRef); continue; }
+            std::vector<size_t> ct(maxSym + 2, 0);
+            size_t const mr = ZS_HUF_buildCTable(ct.data(), count, maxSym, tl);
+            static HufNode nodes[kHufNodes];
+            uint16_t value[256];
+            uint8_t nbBits[256];
+            unsigned const mb = hufBuildCodes(nodes, value, nbBits, count, maxSym, tl);
+            if (ZS_HUF_isError(mr)) { bad++; std::printf("BAD huf reference error\n"); continue; }
+            hufCases++;
+            if (mb != unsigned(mr)) { bad++; std::printf("BAD huf maxNbBits %u ref %zu\n", mb, mr); }
+            for (unsigned s = 0; s <= maxSym; s++) {
+                size_t const e = ct[1 + s];
+                unsigned const nb = unsigned(e & 0xFF);
+                unsigned const v = nb ? unsigned(e >> (8 * sizeof(size_t) - nb)) : 0u;
+                if (nb != nbBits[s] || (nb && v != value[s])) {
+                    bad++;
+                    std::printf("BAD huf sym %u: %u/%u ref %u/%u\n", s, nbBits[s], value[s], nb, v);
+                    break;
+                }
+            }
+        }
+    }
+    std::printf("fse=%ld huf=%ld bad=%ld\n", fseCases, hufCases, bad);
+    return bad ? 1 : 0;
+}

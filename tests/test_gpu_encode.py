@@ -121,6 +121,26 @@ def test_fse_chunks_around_the_per_state_threshold(gpu_lib):
     assert not bad, bad[:10]
 
 
+def test_huffman_equal_count_groups(gpu_lib):
+    """Histograms with a group of symbols of count 164 (the reference's
+    Huffman sort reorders them): GPU frames through the Huffman and entropy
+    graphs equal the oracle's, which the CPU tests pin to the reference's."""
+    import torch
+    import openzl_gb300 as oz
+    from test_oracle import equal_count_cases
+
+    cases = [(r, a) for a in equal_count_cases() for r in (8, 17)]
+    enc = oz.GpuEncoder()
+    srcs = [torch.from_numpy(a.copy()).cuda() for _, a in cases]
+    caps = [enc.bound(a.nbytes) for _, a in cases]
+    dsts = [torch.zeros(c, dtype=torch.uint8, device="cuda") for c in caps]
+    sizes = enc.compress_batch([x.data_ptr() for x in srcs], [a.nbytes for _, a in cases], [0] * len(cases),
+                               [r for r, _ in cases], [d.data_ptr() for d in dsts], caps, checksums=True)
+    bad = [(k, r) for k, ((r, a), d, sz) in enumerate(zip(cases, dsts, sizes))
+           if d[:sz].cpu().numpy().tobytes() != oracle.compress(r, a, 0).tobytes()]
+    assert not bad, bad[:10]
+
+
 def test_gpu_encode_then_gpu_decode(gpu_lib):
     import torch
     import openzl_gb300 as oz

@@ -265,6 +265,50 @@ def test_oracle_encoder_matches_reference_on_seeded_inputs():
             assert got.tobytes() == dst[:r].tobytes(), (recipe, w, arr.size, cs)
 
 
+def equal_count_cases(n=80):
+    """Serial inputs whose byte histograms (one chunk) hold 9 to 29 symbols
+    of count 164, beside up to five large counts and 20 to 150 counts of 60
+    to 239. The reference's Huffman sort quicksorts its rank buckets from the
+    count-164 bucket on (its distinct-count cutoff is 165): that reorders
+    these equal counts and decides which of them get the longer codes. Frames
+    of about one case in six differ when the bucket is left in symbol order."""
+    rng = np.random.default_rng(1640)
+    out = []
+    for _ in range(n):
+        counts = {s: int(rng.integers(2000, 9000)) for s in range(int(rng.integers(1, 6)))}
+        syms = rng.permutation(np.arange(len(counts), 256))
+        k = int(rng.integers(9, 30))
+        for s in syms[:k]:
+            counts[int(s)] = 164
+        for s in syms[k:k + int(rng.integers(20, 150))]:
+            counts[int(s)] = int(rng.integers(60, 240))
+        arr = np.concatenate([np.full(c, s, np.uint8) for s, c in counts.items()])
+        rng.shuffle(arr)
+        out.append(arr)
+    return out
+
+
+def test_oracle_matches_reference_on_equal_count_histograms():
+    """Frames through the Huffman and entropy graphs equal the reference's
+    when a group of equal counts sits in the Huffman sort's count-164 bucket."""
+    import ctypes
+
+    ref = ctypes.CDLL(REF_DRIVER)
+    ref.ref_compress.restype = ctypes.c_int64
+    ref.ref_compress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    bad = []
+    for k, arr in enumerate(equal_count_cases()):
+        for recipe in (8, 17):
+            cap = arr.nbytes * 2 + 65536
+            dst = np.zeros(cap, np.uint8)
+            r = ref.ref_compress(recipe, arr.ctypes.data, arr.nbytes, 0, dst.ctypes.data, cap, 1, 0)
+            assert r > 0
+            if oracle.compress(recipe, arr, 0).tobytes() != dst[:r].tobytes():
+                bad.append((k, recipe))
+    assert not bad, bad
+
+
 def tablelog12_cases():
     """Frames whose FSE chunks use table log 12, the decoders' limit (the
     reference's encoder stops at 11): 99,999-symbol unchunked streams, a
