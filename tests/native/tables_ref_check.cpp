@@ -4,10 +4,11 @@
 // shapes, the FSE table log (FSE_optimalTableLog_internal), normalized counts
 // (FSE_normalizeCount with low-probability counts, as
 // encode_entropy_binding.c:100-106 calls it), the normalized-count header
-// (FSE_writeNCount), and the Huffman table log, code lengths and codes
-// (HUF_buildCTable) are equal, including histograms with groups of equal
-// counts around the sort's bucket cutoff. Prints "bad=0" when every case
-// agreed.
+// (FSE_writeNCount), the Huffman table log, code lengths and codes
+// (HUF_buildCTable), including histograms with groups of equal counts around
+// the sort's bucket cutoff, and the 16-bit-symbol Huffman table
+// (ZS_largeHuffmanBuildCTable against huf16Build) are equal. Prints "bad=0"
+// when every case agreed.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -16,6 +17,7 @@
 #include <random>
 #include <vector>
 
+#include "enc_tables.h"
 #include "fse_norm.h"
 #include "huf_tree.h"
 
@@ -28,6 +30,17 @@ size_t ZS_FSE_writeNCount(void* buffer, size_t bufferSize, const short* norm, un
 unsigned ZS_FSE_isError(size_t code);
 size_t ZS_HUF_buildCTable(size_t* CTable, const unsigned* count, unsigned maxSymbolValue, unsigned maxNbBits);
 unsigned ZS_HUF_isError(size_t code);
+// ZL_Report: an error code and a value, returned in two integer registers
+struct RefReport {
+    int code;
+    size_t value;
+};
+struct RefHuf16CElt {
+    uint16_t symbol;
+    uint16_t nbBits;
+};
+RefReport ZS_largeHuffmanBuildCTable(RefHuf16CElt* ctable, const unsigned* histogram, uint16_t maxSymbolValue,
+                                     int maxNbBits);
 }
 
 using namespace ozl::ent;
@@ -124,6 +137,58 @@ int main(int argc, char** argv)
             }
         }
     }
-    std::printf("fse=%ld huf=%ld bad=%ld\n", fseCases, hufCases, bad);
+    // 16-bit symbols (huffman_struct_v2): code lengths and codes against
+    // ZS_largeHuffmanBuildCTable with the binding's table log (0: 20), on
+    // large alphabets and groups of equal counts
+    long huf16Cases = 0;
+    for (long c = 0; c < cases / 8; c++) {
+        unsigned const maxSym = 1 + unsigned(rng() % (rng() % 4 == 0 ? 65535 : 3000));
+        std::vector<uint32_t> count(maxSym + 1, 0);
+        uint64_t const total = 2 + rng() % 200000;
+        int const shape = int(rng() % 4);
+        for (uint64_t i = 0; i < total; i++) {
+            unsigned s = 0;
+            switch (shape) {
+                case 0: s = unsigned(rng() % (maxSym + 1)); break;
+                case 1: {
+                    double const u = double(rng() % 1000000 + 1) / 1000001.0;
+                    s = unsigned(double(maxSym + 1) * u * u * u);
+                    break;
+                }
+                case 2: { unsigned g = 0; while (g < maxSym && rng() % 4 != 0) g++; s = g; break; }
+                default: s = rng() % 2 ? unsigned(rng() % 64) : unsigned(rng() % (maxSym + 1)); break;
+            }
+            count[s > maxSym ? maxSym : s]++;
+        }
+        if (rng() % 3 == 0) {
+            uint32_t const v = 1 + uint32_t(rng() % 400);
+            unsigned const k = 2 + unsigned(rng() % 60);
+            for (unsigned q = 0; q < k; q++) count[rng() % (maxSym + 1)] = v;
+        }
+        count[maxSym] += 1;
+        unsigned distinct = 0;
+        for (uint32_t x : count) distinct += x != 0;
+        if (distinct < 2) continue;
+        std::vector<RefHuf16CElt> ct(maxSym + 1, RefHuf16CElt{ 0, 0 });
+        std::vector<unsigned> cnt(count.begin(), count.end());
+        RefReport const rr = ZS_largeHuffmanBuildCTable(ct.data(), cnt.data(), uint16_t(maxSym), 0);
+        std::vector<uint16_t> code(maxSym + 1, 0);
+        std::vector<uint8_t> nbb(maxSym + 1, 0);
+        int const tl = ozl::ent::huf16Build(code.data(), nbb.data(), count.data(), maxSym);
+        if (rr.code != 0 || tl < 0) {
+            if ((rr.code != 0) != (tl < 0)) { bad++; std::printf("BAD huf16 outcome %d %d\n", rr.code, tl); }
+            continue;
+        }
+        huf16Cases++;
+        if (size_t(tl) != rr.value) { bad++; std::printf("BAD huf16 tableLog %d ref %zu\n", tl, rr.value); continue; }
+        for (unsigned s = 0; s <= maxSym; s++)
+            if (ct[s].nbBits != nbb[s] || (nbb[s] && ct[s].symbol != code[s])) {
+                bad++;
+                std::printf("BAD huf16 sym %u: %u/%u ref %u/%u (max %u)\n", s, nbb[s], code[s], ct[s].nbBits,
+                            ct[s].symbol, maxSym);
+                break;
+            }
+    }
+    std::printf("fse=%ld huf=%ld huf16=%ld bad=%ld\n", fseCases, hufCases, huf16Cases, bad);
     return bad ? 1 : 0;
 }
