@@ -69,10 +69,10 @@ void Histo::finish()
         }
 }
 
-// entropyCompressChunk's codec choice for serial chunks
-// (encode_entropy_binding.c:664-736).
+double entropyEstimate(const uint32_t* count, uint64_t total) { return entropyBits(count, total); }
+
 // DataStatsU8_estimateHuffmanSizeFast (data_stats.c:287-301)
-static uint64_t hufSizeFast(double e, uint64_t n)
+uint64_t hufSizeFast(double e, uint64_t n)
 {
     if (e > 7) return n;
     double const e1 = e < 1 ? 1 : e;
@@ -81,6 +81,13 @@ static uint64_t hufSizeFast(double e, uint64_t n)
     return uint64_t(q);
 }
 
+// DataStatsU8_getFlatpackedSize and DataStatsU8_getBitpackedSize
+// (data_stats.c:301-333)
+uint64_t flatpackedSize(const Histo& h) { return (h.n * uint64_t(nextPow2Bits(h.card)) + 7) / 8 + h.card; }
+uint64_t bitpackedSize(const Histo& h) { return (h.n * uint64_t(nextPow2Bits(h.maxSym + 1)) + 7) / 8; }
+
+// entropyCompressChunk's codec choice for serial chunks
+// (encode_entropy_binding.c:664-736).
 ChunkCodec chooseCodec(const Histo& h, int mode)
 {
     uint64_t const n = h.n;
@@ -98,8 +105,8 @@ ChunkCodec chooseCodec(const Histo& h, int mode)
     uint64_t const header = h.card / 4 > 10 ? h.card / 4 : 10;
     uint64_t baseline = entropySize + header;
     if (n < baseline) baseline = n;
-    uint64_t const flat = (n * uint64_t(nextPow2Bits(h.card)) + 7) / 8 + h.card;
-    uint64_t const bp = (n * uint64_t(nextPow2Bits(h.maxSym + 1)) + 7) / 8;
+    uint64_t const flat = flatpackedSize(h);
+    uint64_t const bp = bitpackedSize(h);
     if (flat < bp) {
         if (flat < baseline) return CC_FLATPACK;
     } else if (bp < baseline) {

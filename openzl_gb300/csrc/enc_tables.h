@@ -40,6 +40,14 @@ enum : int { EM_FSE = 0, EM_HUF = 1, EM_ANY = 2 };
 // Chunk codec choice for a serial chunk under a backend mode
 // (entropyCompressChunk, encode_entropy_binding.c:602-762).
 ChunkCodec chooseCodec(const Histo& h, int mode);
+// The estimates it compares (DataStatsU8, src/openzl/shared/data_stats.c):
+// the entropy in bits per symbol (ZL_calculateEntropyU8), the fast Huffman
+// size from it (DataStatsU8_estimateHuffmanSizeFast), and the flat-packed
+// and bit-packed sizes.
+double entropyEstimate(const uint32_t* count, uint64_t total);
+uint64_t hufSizeFast(double entropy, uint64_t n);
+uint64_t flatpackedSize(const Histo& h);
+uint64_t bitpackedSize(const Histo& h);
 
 // FSE: table log, normalized counts, encoding tables.
 unsigned fseTableLog(unsigned maxTableLog, uint64_t srcSize, unsigned maxSym, unsigned minus);

@@ -7,8 +7,9 @@
 // (FSE_writeNCount), the Huffman table log, code lengths and codes
 // (HUF_buildCTable), including histograms with groups of equal counts around
 // the sort's bucket cutoff, and the 16-bit-symbol Huffman table
-// (ZS_largeHuffmanBuildCTable against huf16Build) are equal. Prints "bad=0"
-// when every case agreed.
+// (ZS_largeHuffmanBuildCTable against huf16Build), and the codec decision's
+// DataStats estimates (entropy bit for bit, Huffman, flat-packed and
+// bit-packed sizes) are equal. Prints "bad=0" when every case agreed.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -41,6 +42,15 @@ struct RefHuf16CElt {
 };
 RefReport ZS_largeHuffmanBuildCTable(RefHuf16CElt* ctable, const unsigned* histogram, uint16_t maxSymbolValue,
                                      int maxNbBits);
+// DataStatsU8 (src/openzl/shared/data_stats.h) as an opaque block
+double ZL_calculateEntropyU8(const unsigned* count, size_t totalElements);
+void DataStatsU8_init(void* stats, const void* src, size_t srcSize);
+double DataStatsU8_getEntropy(void* stats);
+size_t DataStatsU8_estimateHuffmanSizeFast(void* stats, bool delta);
+size_t DataStatsU8_getBitpackedSize(void* stats);
+size_t DataStatsU8_getFlatpackedSize(void* stats);
+size_t DataStatsU8_getCardinality(void* stats);
+uint8_t DataStatsU8_getMaxElt(void* stats);
 }
 
 using namespace ozl::ent;
@@ -189,6 +199,52 @@ int main(int argc, char** argv)
                 break;
             }
     }
-    std::printf("fse=%ld huf=%ld huf16=%ld bad=%ld\n", fseCases, hufCases, huf16Cases, bad);
+    // the codec decision's estimates (entropyCompressChunk compares them):
+    // entropy bit for bit, fast Huffman, flat-packed and bit-packed sizes,
+    // cardinality and largest symbol, on random byte arrays
+    long statCases = 0;
+    alignas(64) static unsigned char statsBlock[16384];
+    for (long c = 0; c < cases / 8; c++) {
+        size_t const n = 1 + size_t(rng() % (rng() % 4 == 0 ? 64 : 200000));
+        std::vector<uint8_t> src(n);
+        unsigned const alpha = 1 + unsigned(rng() % 256);
+        int const shape = int(rng() % 4);
+        for (size_t i = 0; i < n; i++) {
+            unsigned v = 0;
+            switch (shape) {
+                case 0: v = unsigned(rng() % alpha); break;
+                case 1: { double const u = double(rng() % 1000000) / 1000000.0; v = unsigned(double(alpha) * u * u); break; }
+                case 2: v = rng() % 50 ? 7u : unsigned(rng() % alpha); break;
+                default: v = unsigned((i / (1 + rng() % 64)) % alpha); break;
+            }
+            src[i] = uint8_t(v);
+        }
+        ozl::ent::Histo h{};
+        for (uint8_t v : src) h.count[v]++;
+        h.n = n;
+        h.finish();
+        std::memset(statsBlock, 0, sizeof statsBlock);
+        DataStatsU8_init(statsBlock, src.data(), n);
+        double const eRef = DataStatsU8_getEntropy(statsBlock);
+        double const eRef2 = ZL_calculateEntropyU8(h.count, n);
+        double const e = ozl::ent::entropyEstimate(h.count, n);
+        statCases++;
+        if (std::memcmp(&e, &eRef, sizeof e) != 0 || std::memcmp(&e, &eRef2, sizeof e) != 0) {
+            bad++;
+            std::printf("BAD entropy %.17g ref %.17g / %.17g (n=%zu)\n", e, eRef, eRef2, n);
+            continue;
+        }
+        uint64_t const hf = ozl::ent::hufSizeFast(e, n), hfRef = DataStatsU8_estimateHuffmanSizeFast(statsBlock, false);
+        uint64_t const fp = ozl::ent::flatpackedSize(h), fpRef = DataStatsU8_getFlatpackedSize(statsBlock);
+        uint64_t const bp = ozl::ent::bitpackedSize(h), bpRef = DataStatsU8_getBitpackedSize(statsBlock);
+        if (hf != hfRef || fp != fpRef || bp != bpRef || h.card != DataStatsU8_getCardinality(statsBlock)
+            || h.maxSym != DataStatsU8_getMaxElt(statsBlock)) {
+            bad++;
+            std::printf("BAD stats n=%zu huf %llu/%llu flat %llu/%llu bit %llu/%llu\n", n, (unsigned long long)hf,
+                        (unsigned long long)hfRef, (unsigned long long)fp, (unsigned long long)fpRef,
+                        (unsigned long long)bp, (unsigned long long)bpRef);
+        }
+    }
+    std::printf("fse=%ld huf=%ld huf16=%ld stats=%ld bad=%ld\n", fseCases, hufCases, huf16Cases, statCases, bad);
     return bad ? 1 : 0;
 }
