@@ -95,6 +95,7 @@ struct JobSeed {
     uint64_t n;
     int mode;
     bool wide;
+    unsigned width; // element width in bytes
 };
 
 struct Job {
@@ -136,6 +137,7 @@ struct Job {
     uint16_t* dFields = nullptr; // long FSE chunks: the per-state encoders' fields
     // 16-bit chunks (struct of 2-byte values)
     bool wide = false;
+    unsigned width = 1; // element width in bytes
     unsigned maxSym16 = 0, card16 = 0;
     std::vector<uint32_t> count16, first16; // values 0..maxSym16
     uint8_t const16[2] = { 0, 0 };
@@ -402,7 +404,7 @@ struct Engine {
         size_t const j = (*jobCursor)++;
         if (discover) {
             seeds->push_back(JobSeed{ s[sid].pieces.empty() ? nullptr : s[sid].pieces[0].dev, s[sid].n, mode,
-                                      s[sid].w == 2 });
+                                      s[sid].w == 2, unsigned(s[sid].w) });
             return nullptr;
         }
         return &(*jobs)[j];
@@ -579,7 +581,10 @@ struct Engine {
                 x.hdr[k++] = uint8_t(v);
                 x.hsz = k;
                 int o = newStream(s[sid].type, s[sid].w, 1);
-                s[o].pieces.push_back(Piece{ nullptr, fixed ? j.const16 : &j.constVal, s[sid].w });
+                if (j.mode == M_CONSTANT && j.dsrc) // the constant graph: the input's first element
+                    s[o].pieces.push_back(Piece{ j.dsrc, nullptr, s[sid].w });
+                else
+                    s[o].pieces.push_back(Piece{ nullptr, fixed ? j.const16 : &j.constVal, s[sid].w });
                 nd.back().nbOut = 1;
                 runSuccessor(G_SERIAL_STORE, o);
                 return;
@@ -1218,11 +1223,14 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
             case RC_CONSTANT:
             case RC_FLATPACK:
             case RC_BITPACK: {
-                // the whole input is one forced-codec job
-                Job* j = E.jobFor(in, r == RC_CONSTANT ? M_CONSTANT : (r == RC_FLATPACK ? M_FLATPACK : M_BITPACK), -1);
+                // the whole input is one forced-codec job; the constant
+                // graph takes serial or struct input, so numbers become
+                // struct first (graph_registry.c:132)
+                int const src = r == RC_CONSTANT ? E.convertFor(in, T_SERIAL | T_STRUCT) : in;
+                Job* j = E.jobFor(src, r == RC_CONSTANT ? M_CONSTANT : (r == RC_FLATPACK ? M_FLATPACK : M_BITPACK), -1);
                 if (j) {
                     int const g = r == RC_CONSTANT ? Engine::G_CONSTANT : (r == RC_FLATPACK ? Engine::G_FLATPACK : Engine::G_BITPACK);
-                    E.graph(Engine::G_JOB, in, int(j - I.jobs.data()) | (g << 24));
+                    E.graph(Engine::G_JOB, src, int(j - I.jobs.data()) | (g << 24));
                 }
                 break;
             }
@@ -1254,6 +1262,7 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
                 J.n = seeds[f][k].n;
                 J.mode = seeds[f][k].mode;
                 J.wide = seeds[f][k].wide;
+                J.width = seeds[f][k].width;
             }
         });
         I.nbDataJobs = I.jobs.size();
@@ -1511,6 +1520,25 @@ int EncodeBatch::compress(const std::vector<EncFrameSpec>& frames, uint8_t* cons
         });
     }
 
+    // the constant graph (EI_constant_typed, encode_constant_binding.c:27-30)
+    // refuses input whose elements are not all equal: bytes and 2-byte
+    // values by their histograms, wider elements compared on the host
+    for (Job& J : I.jobs) {
+        if (J.mode != M_CONSTANT) continue;
+        bool constant;
+        if (J.width == 2) {
+            constant = J.card16 == 1;
+        } else if (J.width <= 1) {
+            constant = J.hist.card == 1;
+        } else {
+            std::vector<uint8_t> h(size_t(J.n) * J.width);
+            constant = J.dsrc && cudaMemcpy(h.data(), J.dsrc, h.size(), cudaMemcpyDeviceToHost) == cudaSuccess;
+            for (size_t i = 1; constant && i < J.n; i++)
+                constant = std::memcmp(h.data() + i * J.width, h.data(), J.width) == 0;
+        }
+        if (!constant) { err = "the constant graph needs input whose elements are all equal"; return 1; }
+        J.codec = ent::CC_CONSTANT;
+    }
     endPhase();
     // ---- phase E: entropy bitstreams -----------------------------------------------
     {

@@ -1207,8 +1207,17 @@ static int node_splitn(ECtx* c, int in, const size_t* sizes, size_t nb)
     return first;
 }
 
+/* EI_constant_typed (encode_constant_binding.c:13-44): a serial or struct
+ * input whose elements are all equal (else node_invalid_input); the first
+ * element is the output, the element count the codec header. */
 static int node_constant(ECtx* c, int in)
 {
+    size_t const w = S(in)->w, n = S(in)->n;
+    for (size_t i = 1; i < n; i++)
+        if (memcmp(S(in)->data + i * w, S(in)->data, w) != 0) {
+            c->err = OZO_ERR_GENERIC;
+            break;
+        }
     ENode* nd = new_node(c, S(in)->type == OZO_TYPE_SERIAL ? TR_CONSTANT_SERIAL : TR_CONSTANT_FIXED, in, 1);
     nd->hsz = ozo_varint_enc(nd->hdr, S(in)->n);
     int o = new_stream(c, S(in)->type, S(in)->w, 1, S(in)->data);
@@ -1597,6 +1606,9 @@ static int run_graph(ECtx* c, int g, int sid, const void* arg)
         case G_ENTROPY:
             return graph_entropy(c, sid, 2);
         case G_CONSTANT: {
+            /* the constant graph takes serial or struct input: numbers are
+             * converted to struct first (graph_registry.c:132) */
+            sid = convert_for(c, sid, OZO_TYPE_SERIAL | OZO_TYPE_STRUCT);
             int o = node_constant(c, sid);
             return run_successor(c, G_SERIAL_STORE, o, NULL);
         }

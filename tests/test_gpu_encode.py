@@ -141,6 +141,35 @@ def test_huffman_equal_count_groups(gpu_lib):
     assert not bad, bad[:10]
 
 
+def test_constant_graph(gpu_lib):
+    """The constant graph: numbers of 1 to 8 bytes (converted to struct) and
+    serial bytes give the oracle's frames; input that is not constant is
+    refused, as the reference refuses it."""
+    import torch
+    import openzl_gb300 as oz
+    from test_oracle import constant_graph_cases
+
+    cases = constant_graph_cases()
+    enc = oz.GpuEncoder()
+    srcs = [torch.from_numpy(a.view(np.uint8).copy()).cuda() for a, _ in cases]
+    caps = [enc.bound(a.nbytes) for a, _ in cases]
+    dsts = [torch.zeros(c, dtype=torch.uint8, device="cuda") for c in caps]
+    sizes = enc.compress_batch([x.data_ptr() for x in srcs], [a.size if w else a.nbytes for a, w in cases],
+                               [w for _, w in cases], [13] * len(cases), [d.data_ptr() for d in dsts], caps,
+                               checksums=True)
+    bad = [(k, w, a.size) for k, ((a, w), d, sz) in enumerate(zip(cases, dsts, sizes))
+           if d[:sz].cpu().numpy().tobytes() != oracle.compress(13, a, w).tobytes()]
+    assert not bad, bad
+    for w, dt in [(0, np.uint8), (1, np.uint8), (2, np.uint16), (8, np.uint64)]:
+        a = np.full(1000, 7, dt)
+        a[500] = 8
+        x = torch.from_numpy(a.view(np.uint8).copy()).cuda()
+        d = torch.zeros(enc.bound(a.nbytes), dtype=torch.uint8, device="cuda")
+        with pytest.raises(Exception):
+            enc.compress_batch([x.data_ptr()], [a.size if w else a.nbytes], [w], [13], [d.data_ptr()],
+                               [enc.bound(a.nbytes)], checksums=True)
+
+
 def test_gpu_encode_then_gpu_decode(gpu_lib):
     import torch
     import openzl_gb300 as oz

@@ -309,6 +309,95 @@ def test_oracle_matches_reference_on_equal_count_histograms():
     assert not bad, bad
 
 
+def constant_graph_cases():
+    """Constant numbers of 1, 2, 4 and 8 bytes (and serial bytes) through
+    the constant graph, from 10 to 300,000 elements."""
+    out = []
+    for w, dt in [(1, np.uint8), (2, np.uint16), (4, np.uint32), (8, np.uint64)]:
+        for n in (10, 255, 1000, 100001, 300000):
+            out.append((np.full(n, 0x0102030405060708 % (256 ** w), dt), w))
+    out.append((np.full(5000, 9, np.uint8), 0))
+    return out
+
+
+def test_oracle_constant_graph_matches_reference():
+    """Numbers reach the constant graph through a conversion to struct, as
+    in the reference (the graph takes serial or struct input); frames are
+    equal, and input that is not constant fails in both."""
+    import ctypes
+
+    ref = ctypes.CDLL(REF_DRIVER)
+    ref.ref_compress.restype = ctypes.c_int64
+    ref.ref_compress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    for arr, w in constant_graph_cases():
+        cap = arr.nbytes * 2 + 65536
+        dst = np.zeros(cap, np.uint8)
+        r = ref.ref_compress(13, arr.ctypes.data, arr.size if w else arr.nbytes, w, dst.ctypes.data, cap, 1, 0)
+        assert r > 0
+        assert oracle.compress(13, arr, w).tobytes() == dst[:r].tobytes(), (w, arr.size)
+    for w, dt in [(0, np.uint8), (1, np.uint8), (4, np.uint32)]:
+        arr = np.full(1000, 7, dt)
+        arr[500] = 8
+        dst = np.zeros(8192, np.uint8)
+        assert ref.ref_compress(13, arr.ctypes.data, arr.size if w else arr.nbytes, w, dst.ctypes.data, 8192, 1, 0) < 0
+        with pytest.raises(Exception):
+            oracle.compress(13, arr, w)
+
+
+def test_oracle_matches_reference_on_random_recipes():
+    """A seeded random sweep: every numeric recipe, widths 1-8, six data
+    shapes (uniform, random walks, Zipf, constant, geometric, runs), sizes
+    around the 32 KiB and 100,000-element chunking boundaries; where the
+    reference compresses, the frames are equal."""
+    import ctypes
+
+    ref = ctypes.CDLL(REF_DRIVER)
+    ref.ref_compress.restype = ctypes.c_int64
+    ref.ref_compress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(2809)
+    sizes = [1, 2, 3, 5, 17, 255, 999, 1000, 1001, 4096, 32767, 32768, 32769, 65536, 99999, 100000, 100001, 131072]
+    dts = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}
+
+    def data(shape, n, w):
+        dt = dts[w]
+        if shape == 0:
+            return rng.integers(0, 256 ** min(w, 4), n, dtype=np.uint64).astype(dt)
+        if shape == 1:
+            s = int(rng.integers(1, 70000))
+            return (7000 + np.cumsum(rng.integers(-s, s, n))).astype(dt)
+        if shape == 2:
+            return (rng.zipf(1.0 + rng.random() * 1.5, n) % int(rng.integers(2, 70000))).astype(dt)
+        if shape == 3:
+            return np.full(n, int(rng.integers(0, 255)), dt)
+        if shape == 4:
+            return rng.geometric(1 / float(rng.integers(2, 5000)), n).astype(dt)
+        return np.repeat(rng.integers(0, 1000, n // 7 + 1), 7)[:n].astype(dt)
+
+    checked, bad = 0, []
+    for k in range(1500):
+        recipe = int(rng.choice([1, 2, 3, 4, 9, 10, 11, 12, 13, 15, 17, 7, 8, 14, 5, 16]))
+        n = int(rng.choice(sizes))
+        shape = int(rng.integers(0, 6))
+        if recipe in (7, 8, 14):
+            w, arr = 0, data(shape, n, 1)
+        elif recipe in (5, 16):
+            w, arr = 4, (data(shape, n, 4) % int(rng.integers(2, 3000))).astype(np.uint32)
+        else:
+            w = int(rng.choice([1, 2, 4, 8]))
+            arr = data(shape, n, w)
+        cap = arr.nbytes * 2 + 65536
+        dst = np.zeros(cap, np.uint8)
+        r = ref.ref_compress(recipe, arr.ctypes.data, arr.size if w else arr.nbytes, w, dst.ctypes.data, cap, 1, 0)
+        if r <= 0:
+            continue
+        checked += 1
+        if oracle.compress(recipe, arr, w).tobytes() != dst[:r].tobytes():
+            bad.append((k, recipe, w, n, shape))
+    assert checked > 1300 and not bad, (checked, bad[:10])
+
+
 def tablelog12_cases():
     """Frames whose FSE chunks use table log 12, the decoders' limit (the
     reference's encoder stops at 11): 99,999-symbol unchunked streams, a
