@@ -349,7 +349,8 @@ def test_oracle_matches_reference_on_random_recipes():
     """A seeded random sweep: every numeric recipe, widths 1-8, six data
     shapes (uniform, random walks, Zipf, constant, geometric, runs), sizes
     around the 32 KiB and 100,000-element chunking boundaries; where the
-    reference compresses, the frames are equal."""
+    reference compresses, the frames are equal and the reference's frame
+    decodes to the input in the oracle."""
     import ctypes
 
     ref = ctypes.CDLL(REF_DRIVER)
@@ -395,6 +396,9 @@ def test_oracle_matches_reference_on_random_recipes():
         checked += 1
         if oracle.compress(recipe, arr, w).tobytes() != dst[:r].tobytes():
             bad.append((k, recipe, w, n, shape))
+        # the reference's frame decodes to the input in the oracle
+        if oracle.decompress(dst[:r].copy())[0].tobytes() != arr.tobytes():
+            bad.append((k, recipe, w, n, shape, "decode"))
     assert checked > 1300 and not bad, (checked, bad[:10])
 
 
