@@ -108,7 +108,35 @@ def build_cases():
         c.append(("v%d_flatpack_serial" % v, 14, rng.integers(0, 37, 9000).astype(np.uint8), 0, True, v))
         c.append(("v%d_bitpack_graph_serial" % v, 15, rng.integers(0, 21, 9000).astype(np.uint8), 0, True, v))
         c.append(("v%d_store_serial" % v, 0, rng.integers(0, 256, 1500).astype(np.uint8), 0, True, v))
+    # numbers through the constant graph (converted to struct first)
+    for w, dt in [(2, np.uint16), (4, np.uint32), (8, np.uint64)]:
+        c.append(("constant_u%d" % (8 * w), 13, np.full(4000 + w, 0x0102030405060708 % (256 ** w), dt), w))
+    # Huffman histograms with a group of symbols of count 164, whose order
+    # the reference's sort decides (candidates 1 and 7 of the generator; in
+    # these the group straddles a code-length boundary)
+    eq = equal_count_inputs(8)
+    c.append(("huf_equal_counts_a", 8, eq[1], 0))
+    c.append(("huf_equal_counts_b", 8, eq[7], 0))
     return c
+
+
+def equal_count_inputs(n):
+    """Serial inputs with 9 to 29 symbols of count 164 beside up to five
+    large counts and 20 to 150 counts of 60 to 239 (seeded, shuffled)."""
+    rng = np.random.default_rng(1640)
+    out = []
+    for _ in range(n):
+        counts = {s: int(rng.integers(2000, 9000)) for s in range(int(rng.integers(1, 6)))}
+        syms = rng.permutation(np.arange(len(counts), 256))
+        k = int(rng.integers(9, 30))
+        for s in syms[:k]:
+            counts[int(s)] = 164
+        for s in syms[k:k + int(rng.integers(20, 150))]:
+            counts[int(s)] = int(rng.integers(60, 240))
+        arr = np.concatenate([np.full(cnt, s, np.uint8) for s, cnt in counts.items()])
+        rng.shuffle(arr)
+        out.append(arr)
+    return out
 
 
 def build_multi_cases():

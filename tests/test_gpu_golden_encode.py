@@ -35,7 +35,7 @@ def test_generator_recreates_every_golden_input(manifest):
     """The seeded generator still yields the exact inputs the reference
     compressed (input hashes recorded in the manifest)."""
     got = _inputs(manifest)
-    assert len(got) == 61
+    assert len(got) == 66
     for m, arr in got:
         assert hashlib.sha256(arr.tobytes()).hexdigest() == m["sha256_in"], m["case"]
 
