@@ -77,6 +77,22 @@ struct OZL_GpuEncoder_s {
     }
 };
 
+namespace ozl {
+// The size of a single-output frame for the library's own decode calls: the
+// whole header parsed, frames of several outputs refused (as the
+// reference's single-output decompression refuses them).
+ZL_Report singleOutputSize(const void* src, size_t size)
+{
+    if (!src) return fail(ZL_ErrorCode_srcSize_tooSmall);
+    FrameHeader h;
+    std::string err;
+    int const rc = parseFrameHeader(static_cast<const uint8_t*>(src), size, h, err);
+    if (rc) return fail(rc);
+    if (h.sizes.size() != 1) return fail(ZL_ErrorCode_invalidRequest_singleOutputFrameOnly);
+    return ok(size_t(h.outSize));
+}
+} // namespace ozl
+
 extern "C" {
 
 int ZL_isError(ZL_Report r) { return r._code != ZL_ErrorCode_no_error; }
@@ -228,16 +244,41 @@ ZL_Report ozl_gpu_compress_batch(OZL_GpuEncoder* e, size_t n, const void* const*
 
 const char* ozl_gpu_version(void) { return "openzl_gb300 0.1 (sm_103a)"; }
 
+
 ZL_Report ZL_getDecompressedSize(const void* src, size_t size)
 {
-    if (!src) return fail(ZL_ErrorCode_srcSize_tooSmall);
-    ozl::FrameHeader h;
-    std::string err;
-    int rc = ozl::parseFrameHeader(static_cast<const uint8_t*>(src), size, h, err);
-    if (rc) return fail(rc);
-    // decode_frameheader.c:1156-1163: meaningful for single-output frames only
-    if (h.sizes.size() != 1) return fail(ZL_ErrorCode_invalidRequest_singleOutputFrameOnly);
-    return ok(size_t(h.outSize));
+    // ZL_getFormatVersionFromFrame (common/wire_format.c:10-40): magic
+    // numbers outside the known range (padded by 16 versions) are unknown
+    // headers, versions outside 8..23 unsupported
+    if (!src || size < 4) return fail(ZL_ErrorCode_srcSize_tooSmall);
+    const uint8_t* const p = static_cast<const uint8_t*>(src);
+    uint32_t const magic = uint32_t(p[0]) | uint32_t(p[1]) << 8 | uint32_t(p[2]) << 16 | uint32_t(p[3]) << 24;
+    uint32_t const base = 0xD7B1A5C0u;
+    if (magic < base || magic > base + 23 + 16) return fail(ZL_ErrorCode_header_unknown);
+    if (magic < base + 8 || magic > base + 23) return fail(ZL_ErrorCode_formatVersion_unsupported);
+    unsigned const v = magic - base;
+    // getDecompressedSizeV3orMore (decode_frameheader.c:1147-1190), read as
+    // the reference reads it: from version 15 a frame whose output token (the
+    // byte after the magic, after the flags from version 21) is 64 or more
+    // is refused as not single-output; otherwise the size field right after
+    // the token (LE32 before version 21, a varint holding size + 1 from 21;
+    // 0 means unknown). For frames of several outputs that field is not
+    // always output 0's size; the reference returns it all the same.
+    size_t const hSize = 4 + (v > 13 ? 1 : 0) + (v >= 21 ? 1 : 0);
+    if (size < hSize + 4) return fail(ZL_ErrorCode_srcSize_tooSmall);
+    if (v > 14 && p[4 + (v >= 21 ? 1 : 0)] >= 64) return fail(ZL_ErrorCode_invalidRequest_singleOutputFrameOnly);
+    if (v < 21) return ok(size_t(uint32_t(p[hSize]) | uint32_t(p[hSize + 1]) << 8 | uint32_t(p[hSize + 2]) << 16
+                                 | uint32_t(p[hSize + 3]) << 24));
+    uint64_t oSize = 0;
+    size_t i = hSize;
+    for (unsigned sh = 0;; sh += 7, i++) {
+        if (i >= size) return fail(ZL_ErrorCode_srcSize_tooSmall);
+        if (sh > 63) return fail(ZL_ErrorCode_corruption);
+        oSize |= uint64_t(p[i] & 0x7F) << sh;
+        if (!(p[i] & 0x80)) break;
+    }
+    if (oSize == 0) return fail(ZL_ErrorCode_temporaryLibraryLimitation);
+    return ok(size_t(oSize - 1));
 }
 
 ZL_Report ozl_frame_info(const void* frame, size_t frameSize, OZL_FrameInfo* info)
@@ -373,7 +414,7 @@ static ZL_Report decodeToHost(ZL_DCtx* dctx, void* dst, size_t dstCap, const voi
                               uint32_t* width)
 {
     if (!dctx || !src || (dstCap && !dst)) return fail(ZL_ErrorCode_parameter_invalid);
-    ZL_Report ds = ZL_getDecompressedSize(src, cSize);
+    ZL_Report ds = ozl::singleOutputSize(src, cSize);
     if (ZL_isError(ds)) return ds;
     size_t const outSize = ZL_validResult(ds);
     if (outSize > dstCap) return fail(ZL_ErrorCode_dstCapacity_tooSmall);
@@ -689,7 +730,7 @@ ZL_Report ZL_DCtx_decompressTBuffer(ZL_DCtx* dctx, ZL_TypedBuffer* out, const vo
             return ZL_isError(r) ? r : ok(out->bytes);
         }
     }
-    ZL_Report ds = ZL_getDecompressedSize(src, cSize);
+    ZL_Report ds = ozl::singleOutputSize(src, cSize);
     if (ZL_isError(ds)) { resetParams(dctx); return ds; }
     size_t const outSize = ZL_validResult(ds);
     void* dst;

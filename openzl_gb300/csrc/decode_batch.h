@@ -18,6 +18,9 @@
 namespace ozl {
 
 inline ZL_Report reportOk(size_t v) { return ZL_Report{ ZL_ErrorCode_no_error, v }; }
+// Decoded size of a single-output frame (whole header parsed; several
+// outputs refused), for the library's own decode calls (capi.cpp).
+ZL_Report singleOutputSize(const void* src, size_t size);
 inline ZL_Report reportFail(int code) { return ZL_Report{ ZL_ErrorCode(code), 0 }; }
 
 // Grow-only device allocation with slack so that kernels may read whole

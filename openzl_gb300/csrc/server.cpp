@@ -352,7 +352,7 @@ uint64_t ozl_server_submit_decompress(OZL_Server* srv, const void* frame, size_t
     r->inBytes = frameSize;
     r->out = static_cast<uint8_t*>(dst);
     r->outCap = dstCapacity;
-    ZL_Report ds = ZL_getDecompressedSize(frame, frameSize);
+    ZL_Report ds = ozl::singleOutputSize(frame, frameSize);
     if (ZL_isError(ds)) { // answered at once, never queued
         uint64_t id;
         {
